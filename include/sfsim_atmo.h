@@ -1,0 +1,159 @@
+/*
+ * sfsim_atmo.h -- C ABI of the GB300 atmosphere lookup-table builder.
+ *
+ * The library builds sfsim's four atmosphere lookup tables (transmittance,
+ * surface radiance, ray scatter and Mie strength) on one GPU and returns them
+ * in the exact `.scatter` file layout that sfsim's runtime loads:
+ * little-endian float32, RGB interleaved, no header.
+ *
+ *   transmittance    [height][elevation][3]
+ *   surface radiance [height][sun elevation][3]
+ *   ray scatter, mie strength: 4-D tables [height][elevation][sun elevation][sun heading]
+ *     stored as 2-D tiles, row = height*n_sun_elevation + sun_elevation,
+ *     column = elevation*n_sun_heading + sun_heading, then [3].
+ *
+ * Reference interfaces replaced (paths inside wedesoft/sfsim):
+ *   src/clj/sfsim/atmosphere_lut.clj:43-105  generate-atmosphere-luts (the whole build)
+ *   src/clj/sfsim/atmosphere.clj:114-422     the integrands and table spaces
+ *   src/clj/sfsim/interpolate.clj:54-109     make-lookup-table / interpolation-table
+ *   src/clj/sfsim/matrix.clj:130, image.clj:299, util.clj:227-240  the file layout
+ * The calling convention follows the reference's own native precedent,
+ * src/c/sfsim/jolt.hh:1-25 (flat extern "C" functions, plain structs of
+ * doubles), bound from Clojure with coffi `defcfn` as in src/clj/sfsim/jolt.clj:18-23.
+ *
+ * Errors: every entry point returns 0 on success or a negative SFSIM_ATMO_E*
+ * code; sfsim_atmo_strerror() maps a code to text.  No entry point throws or
+ * aborts.  Calls are synchronous unless stated; one host thread at a time per
+ * device.
+ */
+#ifndef SFSIM_ATMO_H
+#define SFSIM_ATMO_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Error codes. */
+#define SFSIM_ATMO_OK            0
+#define SFSIM_ATMO_EINVAL       -1  /* a configuration value is out of range */
+#define SFSIM_ATMO_ENOMEM       -2  /* device or host allocation failed */
+#define SFSIM_ATMO_ECUDA        -3  /* a CUDA runtime call failed */
+#define SFSIM_ATMO_ENODEV       -4  /* no CUDA device is visible */
+#define SFSIM_ATMO_ESHAPE       -5  /* a table shape is unsupported */
+#define SFSIM_ATMO_ENULL        -6  /* a required pointer is NULL */
+#define SFSIM_ATMO_ETOOBIG      -7  /* a size exceeds a fixed capacity */
+#define SFSIM_ATMO_ENUMERIC     -8  /* a result contains NaN or Inf */
+
+/* Arithmetic of the bulk integrands.  Ray-sphere intersections and the table
+ * parameterisations always run in FP64. */
+#define SFSIM_ATMO_FP32 0
+#define SFSIM_ATMO_FP64 1
+
+/* One scattering component; mirrors the malli schema `scatter` at
+ * src/clj/sfsim/atmosphere.clj:35-39.  A component without
+ * ::scatter-quotient uses 1.0, one without ::scatter-g uses 0.0. */
+typedef struct sfsim_atmo_component {
+  double scatter_base[3];   /* scattering coefficient at height 0, 1/m, RGB */
+  double scatter_scale;     /* scale height, m */
+  double scatter_quotient;  /* extinction = scattering / quotient */
+  double scatter_g;         /* Cornette-Shanks asymmetry */
+} sfsim_atmo_component;
+
+/* Everything that the reference hard-codes in atmosphere_lut.clj:20-63. */
+typedef struct sfsim_atmo_config {
+  double radius;            /* planet radius, m (atmosphere_lut.clj:20) */
+  double height;            /* atmosphere height, m (atmosphere_lut.clj:21) */
+  double brightness[3];     /* ground albedo (atmosphere_lut.clj:28) */
+  double intensity[3];      /* sun radiance (atmosphere_lut.clj:62) */
+  sfsim_atmo_component mie;       /* first entry of `scatter` */
+  sfsim_atmo_component rayleigh;  /* second entry of `scatter` */
+  int transmittance_shape[2];     /* [height, elevation] */
+  int surface_radiance_shape[2];  /* [height, sun elevation] */
+  int ray_scatter_shape[4];       /* [height, elevation, sun elevation, sun heading] */
+  int ray_steps;            /* midpoint samples per ray integral */
+  int sphere_steps;         /* point-scatter sphere steps (theta rings = steps/2) */
+  int iterations;           /* multiple-scattering iterations after the first order */
+  int precision;            /* SFSIM_ATMO_FP32 or SFSIM_ATMO_FP64 */
+  int flags;                /* reserved, must be 0 */
+} sfsim_atmo_config;
+
+/* Fills `cfg` with the reference's production values
+ * (atmosphere_lut.clj:20-63: R 6378 km, H 35 km, T 64x255, E 16x63,
+ * S 32x127x32x8, 100 ray steps, 15 sphere steps, 5 iterations), FP32. */
+void sfsim_atmo_default_config(sfsim_atmo_config* cfg);
+
+/* Checks a configuration; 0 when it is usable. */
+int sfsim_atmo_validate(const sfsim_atmo_config* cfg);
+
+/* Number of floats in each output table (RGB included). */
+int sfsim_atmo_table_sizes(const sfsim_atmo_config* cfg, size_t* n_transmittance,
+                           size_t* n_surface_radiance, size_t* n_ray_scatter,
+                           size_t* n_mie_strength);
+
+/* Builds all four tables; replaces generate-atmosphere-luts
+ * (atmosphere_lut.clj:43-105) up to, not including, spit-floats.
+ * Output pointers are HOST memory sized by sfsim_atmo_table_sizes. */
+int sfsim_atmo_build(const sfsim_atmo_config* cfg, float* transmittance,
+                     float* surface_radiance, float* ray_scatter, float* mie_strength);
+
+/* As sfsim_atmo_build, but the outputs are DEVICE pointers and the work is
+ * queued on `stream` (a cudaStream_t, NULL for the legacy stream).  The call
+ * returns once the work is queued.  Scratch tables stay allocated inside the
+ * library between calls, keyed by device. */
+int sfsim_atmo_build_device(const sfsim_atmo_config* cfg, float* transmittance,
+                            float* surface_radiance, float* ray_scatter,
+                            float* mie_strength, void* stream);
+
+/* Builds `n` independent atmospheres that share shapes, steps, iterations and
+ * precision (they may differ in every physical parameter) in one pass of
+ * batched kernels.  Outputs are HOST arrays of n consecutive tables each. */
+int sfsim_atmo_build_batch(const sfsim_atmo_config* cfgs, int n, float* transmittance,
+                           float* surface_radiance, float* ray_scatter,
+                           float* mie_strength);
+
+/* Intermediate tables of one build, for validation.  Every pointer may be NULL.
+ * 4-D tables use the plain [height][elevation][sun elevation][sun heading][3]
+ * order, 2-D tables [height][second][3]; per-iteration arrays hold
+ * `iterations` consecutive tables. */
+typedef struct sfsim_atmo_intermediates {
+  float* transmittance_nodes;   /* T sampled at the nodes, before re-interpolation */
+  float* surface_base;          /* E0, surface-radiance-base table */
+  float* rayleigh_first;        /* first-order Rayleigh ray scatter table */
+  float* mie_first;             /* first-order Mie strength table */
+  float* point_scatter;         /* J of each iteration */
+  float* surface_delta;         /* dE of each iteration */
+  float* ray_scatter_delta;     /* dS of each iteration */
+} sfsim_atmo_intermediates;
+
+/* As sfsim_atmo_build, and also copies intermediate tables to host memory. */
+int sfsim_atmo_build_debug(const sfsim_atmo_config* cfg, float* transmittance,
+                           float* surface_radiance, float* ray_scatter,
+                           float* mie_strength, const sfsim_atmo_intermediates* inter);
+
+/* Device time of each stage of the last build on this thread's device, in ms,
+ * measured with CUDA events on the build stream when timing is enabled.
+ * Stage order: node maps, transmittance, surface base, first order,
+ * sphere setup, point scatter, surface radiance, ray scatter, accumulate,
+ * output.  Returns the number of stages written (at most `n`). */
+int sfsim_atmo_set_timing(int enabled);
+int sfsim_atmo_last_timings(double* ms, int n);
+
+/* Number of kernel launches of the last build. */
+int sfsim_atmo_last_launch_count(void);
+
+/* Frees the cached scratch tables of the current device. */
+int sfsim_atmo_release(void);
+
+/* Text for an error code. */
+const char* sfsim_atmo_strerror(int code);
+
+/* Library version string. */
+const char* sfsim_atmo_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SFSIM_ATMO_H */
