@@ -132,22 +132,39 @@ int sfsim_atmo_build_debug(const sfsim_atmo_config* cfg, float* transmittance,
                            float* surface_radiance, float* ray_scatter,
                            float* mie_strength, const sfsim_atmo_intermediates* inter);
 
-/* Device time of each stage of the last build on this thread's device, in ms,
- * measured with CUDA events on the build stream when timing is enabled.
- * Stage order: node maps, transmittance, surface base, first order,
- * sphere setup, point scatter, surface radiance, ray scatter, accumulate,
- * output.  Returns the number of stages written (at most `n`). */
+/* Device time of each stage of the last build, in ms, measured with CUDA
+ * events on the build stream when timing is enabled.  Stage order: set-up
+ * (node maps, view rows, sphere directions), transmittance, surface base,
+ * first order, reserved (0), point scatter, surface radiance, ray scatter,
+ * accumulate, output.  Returns the number of stages written (at most `n`);
+ * for sfsim_atmo_build_device it waits for the build's last event. */
 int sfsim_atmo_set_timing(int enabled);
 int sfsim_atmo_last_timings(double* ms, int n);
 
 /* Number of kernel launches of the last build. */
 int sfsim_atmo_last_launch_count(void);
 
+/* Work census of one build (no tables are written).  counts[0] = first-order
+ * sun-ray integrals (node, ray-sample pairs with the sun above the sample's
+ * horizon), [1] = their extinction samples, [2] = view-ray extinction
+ * samples, [3] = point-scatter direction evaluations, [4] = ray-scatter
+ * J lookups, [5] = surface-radiance direction evaluations.  Returns the
+ * number of counts written (at most n). */
+int sfsim_atmo_census(const sfsim_atmo_config* cfg, unsigned long long* counts, int n);
+
+/* Measures the SFU throughput of the current device (ex2.approx.f32
+ * operations per second, best of 4 timed launches over all SMs), the
+ * denominator of the quadrature kernels' roofline. */
+int sfsim_atmo_sfu_peak(double* ex2_per_second);
+
 /* Frees the cached scratch tables of the current device. */
 int sfsim_atmo_release(void);
 
 /* Text for an error code. */
 const char* sfsim_atmo_strerror(int code);
+
+/* Detailed message of the last failure on the calling thread. */
+const char* sfsim_atmo_last_error(void);
 
 /* Library version string. */
 const char* sfsim_atmo_version(void);

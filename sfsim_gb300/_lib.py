@@ -1,0 +1,82 @@
+"""ctypes binding of libsfsim_atmo.so, the C ABI declared in include/sfsim_atmo.h.
+
+The library is the only compute path: when it cannot be loaded every entry
+point raises, there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+from .config import AtmoConfig
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_build", "libsfsim_atmo.so")
+
+_fp = ctypes.POINTER(ctypes.c_float)
+_cfgp = ctypes.POINTER(AtmoConfig)
+
+# every exported symbol of include/sfsim_atmo.h
+EXPORTS = (
+    "sfsim_atmo_default_config", "sfsim_atmo_validate", "sfsim_atmo_table_sizes", "sfsim_atmo_build",
+    "sfsim_atmo_build_device", "sfsim_atmo_build_batch", "sfsim_atmo_build_debug", "sfsim_atmo_set_timing",
+    "sfsim_atmo_last_timings", "sfsim_atmo_last_launch_count", "sfsim_atmo_release", "sfsim_atmo_strerror",
+    "sfsim_atmo_last_error", "sfsim_atmo_version", "sfsim_atmo_census", "sfsim_atmo_sfu_peak",
+)
+
+
+class Intermediates(ctypes.Structure):
+    _fields_ = [(n, _fp) for n in ("transmittance_nodes", "surface_base", "rayleigh_first", "mie_first",
+                                   "point_scatter", "surface_delta", "ray_scatter_delta")]
+
+
+class AtmoError(RuntimeError):
+    def __init__(self, code: int, where: str, detail: str):
+        super().__init__(f"{where} failed with {code}: {detail}")
+        self.code = code
+
+
+_lib = None
+
+
+def load(build: bool = False):
+    """Loads the library (building it first when `build`); raises when absent."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if build:
+        from .build import build_library
+        build_library()
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError(f"{LIB_PATH} is missing: run `python -m sfsim_gb300.build` (needs nvcc)")
+    L = ctypes.CDLL(LIB_PATH)
+    L.sfsim_atmo_default_config.argtypes = [_cfgp]
+    L.sfsim_atmo_default_config.restype = None
+    L.sfsim_atmo_validate.argtypes = [_cfgp]
+    L.sfsim_atmo_table_sizes.argtypes = [_cfgp] + [ctypes.POINTER(ctypes.c_size_t)] * 4
+    L.sfsim_atmo_build.argtypes = [_cfgp, _fp, _fp, _fp, _fp]
+    L.sfsim_atmo_build_device.argtypes = [_cfgp, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                          ctypes.c_void_p, ctypes.c_void_p]
+    L.sfsim_atmo_build_batch.argtypes = [_cfgp, ctypes.c_int, _fp, _fp, _fp, _fp]
+    L.sfsim_atmo_build_debug.argtypes = [_cfgp, _fp, _fp, _fp, _fp, ctypes.POINTER(Intermediates)]
+    L.sfsim_atmo_set_timing.argtypes = [ctypes.c_int]
+    L.sfsim_atmo_last_timings.argtypes = [ctypes.POINTER(ctypes.c_double), ctypes.c_int]
+    L.sfsim_atmo_last_launch_count.argtypes = []
+    L.sfsim_atmo_release.argtypes = []
+    L.sfsim_atmo_strerror.argtypes = [ctypes.c_int]
+    L.sfsim_atmo_strerror.restype = ctypes.c_char_p
+    L.sfsim_atmo_last_error.argtypes = []
+    L.sfsim_atmo_last_error.restype = ctypes.c_char_p
+    L.sfsim_atmo_census.argtypes = [_cfgp, ctypes.POINTER(ctypes.c_ulonglong), ctypes.c_int]
+    L.sfsim_atmo_sfu_peak.argtypes = [ctypes.POINTER(ctypes.c_double)]
+    L.sfsim_atmo_version.argtypes = []
+    L.sfsim_atmo_version.restype = ctypes.c_char_p
+    _lib = L
+    return L
+
+
+def check(rc: int, where: str) -> None:
+    if rc < 0:
+        L = load()
+        detail = (L.sfsim_atmo_last_error() or b"").decode() or L.sfsim_atmo_strerror(rc).decode()
+        raise AtmoError(rc, where, detail)

@@ -1,0 +1,773 @@
+// atmo_api.cu -- C ABI of the atmosphere LUT builder (include/sfsim_atmo.h):
+// validation, parameter set-up, the device workspace and the order loop of
+// generate-atmosphere-luts (src/clj/sfsim/atmosphere_lut.clj:43-105).
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/sfsim_atmo.h"
+#include "atmo_device.cuh"
+#include "kernels.h"
+
+namespace sfsim {
+template <class Real>
+size_t point_scatter_smem(const BuildDims& d, bool first);
+}
+
+using namespace sfsim;
+
+namespace {
+
+constexpr size_t kMaxSmem = 227 * 1024;
+
+thread_local std::string g_last_error;
+std::mutex g_mutex;
+bool g_timing = false;
+int g_launches = 0;
+constexpr int kStages = 10;
+double g_stage_ms[kStages];
+int g_have_timings = 0;
+
+int fail(int code, const std::string& msg) {
+  g_last_error = msg;
+  return code;
+}
+
+#define CUDA_TRY(expr)                                                                              \
+  do {                                                                                              \
+    cudaError_t _e = (expr);                                                                        \
+    if (_e != cudaSuccess) return fail(SFSIM_ATMO_ECUDA, std::string(#expr) + ": " + cudaGetErrorString(_e)); \
+  } while (0)
+
+// ---------------------------------------------------------------------------
+// configuration
+// ---------------------------------------------------------------------------
+
+int validate(const sfsim_atmo_config* c) {
+  if (!c) return fail(SFSIM_ATMO_ENULL, "config is NULL");
+  if (!(c->radius > 0) || !(c->height > 0) || !std::isfinite(c->radius) || !std::isfinite(c->height))
+    return fail(SFSIM_ATMO_EINVAL, "radius and height must be positive and finite");
+  const sfsim_atmo_component* comps[2] = {&c->mie, &c->rayleigh};
+  for (int i = 0; i < 2; i++) {
+    const sfsim_atmo_component* k = comps[i];
+    if (!(k->scatter_scale > 0) || !(k->scatter_quotient > 0) || !std::isfinite(k->scatter_g) ||
+        std::fabs(k->scatter_g) >= 1.0)
+      return fail(SFSIM_ATMO_EINVAL, "component scale and quotient must be positive and |g| < 1");
+    for (int ch = 0; ch < 3; ch++)
+      if (!(k->scatter_base[ch] >= 0) || !std::isfinite(k->scatter_base[ch]))
+        return fail(SFSIM_ATMO_EINVAL, "scatter base must be finite and non-negative");
+  }
+  for (int ch = 0; ch < 3; ch++)
+    if (!std::isfinite(c->brightness[ch]) || !std::isfinite(c->intensity[ch]))
+      return fail(SFSIM_ATMO_EINVAL, "brightness and intensity must be finite");
+  for (int i = 0; i < 2; i++)
+    if (c->transmittance_shape[i] < 2 || c->surface_radiance_shape[i] < 2)
+      return fail(SFSIM_ATMO_ESHAPE, "every table dimension needs at least 2 nodes");
+  for (int i = 0; i < 4; i++)
+    if (c->ray_scatter_shape[i] < 2) return fail(SFSIM_ATMO_ESHAPE, "every table dimension needs at least 2 nodes");
+  if (c->ray_steps < 1 || c->ray_steps > 4096) return fail(SFSIM_ATMO_EINVAL, "ray_steps must be in [1, 4096]");
+  if (c->iterations < 0 || c->iterations > 64) return fail(SFSIM_ATMO_EINVAL, "iterations must be in [0, 64]");
+  if (c->iterations > 0 && (c->sphere_steps < 2 || c->sphere_steps > 1024))
+    return fail(SFSIM_ATMO_EINVAL, "sphere_steps must be in [2, 1024]");
+  if (c->iterations > 0 && c->ray_steps < 4)
+    return fail(SFSIM_ATMO_EINVAL, "ray_steps must be at least 4 (surface radiance uses ray_steps/4 rings)");
+  if (c->precision != SFSIM_ATMO_FP32 && c->precision != SFSIM_ATMO_FP64)
+    return fail(SFSIM_ATMO_EINVAL, "precision must be SFSIM_ATMO_FP32 or SFSIM_ATMO_FP64");
+  if (c->flags != 0) return fail(SFSIM_ATMO_EINVAL, "flags must be 0");
+  long long n4 = 1;
+  for (int i = 0; i < 4; i++) n4 *= c->ray_scatter_shape[i];
+  if (n4 > (1LL << 31)) return fail(SFSIM_ATMO_ETOOBIG, "ray-scatter table exceeds 2^31 nodes");
+  return 0;
+}
+
+bool same_layout(const sfsim_atmo_config& a, const sfsim_atmo_config& b) {
+  return memcmp(a.transmittance_shape, b.transmittance_shape, sizeof(a.transmittance_shape)) == 0 &&
+         memcmp(a.surface_radiance_shape, b.surface_radiance_shape, sizeof(a.surface_radiance_shape)) == 0 &&
+         memcmp(a.ray_scatter_shape, b.ray_scatter_shape, sizeof(a.ray_scatter_shape)) == 0 &&
+         a.ray_steps == b.ray_steps && a.sphere_steps == b.sphere_steps && a.iterations == b.iterations &&
+         a.precision == b.precision;
+}
+
+// Directions of spherical-integral (sphere.clj:62-93): theta rings at
+// midpoints, ceil(sin theta * phi_steps) phi midpoints per ring, weight
+// (cos(theta - d) - cos(theta + d)) * 2 pi / ring steps.
+void sphere_directions(int theta_steps, int phi_steps, double range, std::vector<DirLocal>& out,
+                       std::vector<int>& ring_end) {
+  out.clear();
+  ring_end.clear();
+  if (theta_steps <= 0) return;
+  const double delta2 = range / theta_steps / 2;
+  for (int k = 0; k < theta_steps; k++) {
+    const double theta = range * ((0.5 + k) / theta_steps);
+    const double factor = std::cos(theta - delta2) - std::cos(theta + delta2);
+    const int ringsteps = (int)std::ceil(std::sin(theta) * phi_steps);
+    const double weight = (2 * M_PI) / ringsteps;
+    for (int i = 0; i < ringsteps; i++) {
+      const double phi = 2 * M_PI * ((0.5 + i) / ringsteps);
+      out.push_back(DirLocal{std::cos(theta), std::sin(theta) * std::cos(phi), std::sin(theta) * std::sin(phi),
+                             factor * weight});
+      ring_end.push_back(i == ringsteps - 1);
+    }
+  }
+}
+
+// h(q) = q / (R + sqrt(R^2 + q)) = q * f(q); f is interpolated at 5
+// Chebyshev nodes over q in [-0.01, 1.05] * (top^2 - R^2) and stored as a
+// polynomial in z = q * alpha + beta, z in [-1, 1].
+int fit_height_polynomial(AtmoParams& P) {
+  constexpr int N = 5;
+  const double qlo = -0.01 * P.Hh2, qhi = 1.05 * P.Hh2;
+  const double alpha = 2.0 / (qhi - qlo), beta = -(qhi + qlo) / (qhi - qlo);
+  auto f = [&](double q) { return 1.0 / (P.R + std::sqrt(P.R2 + q)); };
+  double cheb[N];
+  for (int j = 0; j < N; j++) {
+    double s = 0;
+    for (int k = 0; k < N; k++) {
+      const double t = M_PI * (k + 0.5) / N;
+      const double z = std::cos(t);
+      s += f((z - beta) / alpha) * std::cos(j * t);
+    }
+    cheb[j] = s * (j == 0 ? 1.0 : 2.0) / N;
+  }
+  // Chebyshev -> monomial in z
+  double T[N][N] = {};
+  T[0][0] = 1;
+  T[1][1] = 1;
+  for (int j = 2; j < N; j++)
+    for (int k = 0; k < N; k++) T[j][k] = (k > 0 ? 2 * T[j - 1][k - 1] : 0) - T[j - 2][k];
+  double mono[N] = {};
+  for (int j = 0; j < N; j++)
+    for (int k = 0; k < N; k++) mono[k] += cheb[j] * T[j][k];
+  double worst = 0;
+  for (int k = 0; k <= 1000; k++) {
+    const double q = qlo + (qhi - qlo) * k / 1000.0;
+    const double z = q * alpha + beta;
+    double p = mono[N - 1];
+    for (int m = N - 2; m >= 0; m--) p = p * z + mono[m];
+    worst = std::fmax(worst, std::fabs(p / f(q) - 1));
+  }
+  if (worst > 1e-8) return fail(SFSIM_ATMO_EINVAL, "atmosphere too thick for the height polynomial");
+  for (int k = 0; k < kMaxHPoly; k++) {
+    P.d_hpoly[k] = k < N ? mono[k] : 0.0;
+    P.f_hpoly[k] = (float)P.d_hpoly[k];
+  }
+  P.hpoly_n = N;
+  P.d_alpha = alpha;
+  P.d_beta = beta;
+  P.f_alpha = (float)alpha;
+  P.f_beta = (float)beta;
+  return 0;
+}
+
+int make_params(const sfsim_atmo_config& c, AtmoParams& P) {
+  memset(&P, 0, sizeof(P));
+  P.R = c.radius;
+  P.H = c.height;
+  P.top = c.radius + c.height;
+  P.R2 = c.radius * c.radius;
+  P.top2 = P.top * P.top;
+  P.Hh = std::sqrt(P.top2 - P.R2);
+  P.Hh2 = P.Hh * P.Hh;
+  for (int ch = 0; ch < 3; ch++) {
+    P.mie_base[ch] = c.mie.scatter_base[ch];
+    P.ray_base[ch] = c.rayleigh.scatter_base[ch];
+    P.brightness[ch] = c.brightness[ch];
+    P.intensity[ch] = c.intensity[ch];
+    P.d_mie_ext[ch] = c.mie.scatter_base[ch] / c.mie.scatter_quotient;
+    P.d_ray_ext[ch] = c.rayleigh.scatter_base[ch] / c.rayleigh.scatter_quotient;
+    P.f_mie_ext[ch] = (float)P.d_mie_ext[ch];
+    P.f_ray_ext[ch] = (float)P.d_ray_ext[ch];
+    P.f_mie_base[ch] = (float)P.mie_base[ch];
+    P.f_ray_base[ch] = (float)P.ray_base[ch];
+    P.f_bright_pi[ch] = (float)(c.brightness[ch] / M_PI);
+    P.f_intensity[ch] = (float)c.intensity[ch];
+  }
+  P.mie_scale = c.mie.scatter_scale;
+  P.mie_quot = c.mie.scatter_quotient;
+  P.mie_g = c.mie.scatter_g;
+  P.ray_scale = c.rayleigh.scatter_scale;
+  P.ray_quot = c.rayleigh.scatter_quotient;
+  P.ray_g = c.rayleigh.scatter_g;
+  const double log2e = 1.4426950408889634;
+  P.d_km = -log2e / P.mie_scale;
+  P.d_kr = -log2e / P.ray_scale;
+  P.f_km = (float)P.d_km;
+  P.f_kr = (float)P.d_kr;
+  P.f_R = (float)P.R;
+  P.f_Hh2 = (float)P.Hh2;
+  P.f_mie_g = (float)P.mie_g;
+  return fit_height_polynomial(P);
+}
+
+BuildDims make_dims(const sfsim_atmo_config& c, int B) {
+  BuildDims d;
+  d.B = B;
+  d.nT0 = c.transmittance_shape[0];
+  d.nT1 = c.transmittance_shape[1];
+  d.nE0 = c.surface_radiance_shape[0];
+  d.nE1 = c.surface_radiance_shape[1];
+  d.n0 = c.ray_scatter_shape[0];
+  d.n1 = c.ray_scatter_shape[1];
+  d.n2 = c.ray_scatter_shape[2];
+  d.n3 = c.ray_scatter_shape[3];
+  d.S = c.ray_steps;
+  d.sphere_steps = c.sphere_steps;
+  d.iterations = c.iterations;
+  std::vector<DirLocal> v;
+  std::vector<int> e;
+  sphere_directions(c.sphere_steps >> 1, c.sphere_steps, M_PI, v, e);
+  d.P = (int)v.size();
+  sphere_directions(c.ray_steps >> 2, c.ray_steps, M_PI / 2, v, e);
+  d.Ph = (int)v.size();
+  return d;
+}
+
+template <class Real>
+int check_smem(const BuildDims& d) {
+  if (point_scatter_smem<Real>(d, true) > kMaxSmem)
+    return fail(SFSIM_ATMO_ESHAPE, "elevation x heading slab of point scatter exceeds shared memory");
+  if (sizeof(Real) * 3 * 8 * (size_t)d.n2 * d.n3 + 64 * sizeof(Real) > kMaxSmem)
+    return fail(SFSIM_ATMO_ESHAPE, "sun elevation x heading plane of ray scatter exceeds shared memory");
+  return 0;
+}
+
+// ---------------------------------------------------------------------------
+// device workspace: one allocation per device, grown on demand
+// ---------------------------------------------------------------------------
+
+struct Arena {
+  void* base = nullptr;
+  size_t size = 0;
+};
+
+constexpr int kMaxDevices = 64;
+Arena g_arena[kMaxDevices];
+cudaStream_t g_stream[kMaxDevices];
+cudaEvent_t g_events[kMaxDevices][2 * 512];
+
+struct Carver {
+  char* base;
+  size_t off = 0;
+  template <class T>
+  T* take(size_t count) {
+    off = (off + 255) & ~size_t(255);
+    T* p = reinterpret_cast<T*>(base ? base + off : nullptr);
+    off += count * sizeof(T);
+    return p;
+  }
+};
+
+template <class Real>
+struct Work {
+  AtmoParams* params;
+  DirLocal* dirs;
+  int* ring_end;
+  DirLocal* hdirs;
+  SetupBuffers<Real> setup;
+  Vec4<Real>*T, *E0, *dE[2], *Eacc[2];
+  Vec4<Real>*S1R, *M, *J, *dS[2], *Sacc[2];
+  float *oT, *oE, *oS, *oM;  // device outputs when the caller passes host buffers
+};
+
+template <class Real>
+size_t carve(Work<Real>& w, char* base, const BuildDims& d, bool outputs) {
+  Carver c{base};
+  const long long B = d.B;
+  w.params = c.take<AtmoParams>(B);
+  w.dirs = c.take<DirLocal>(d.P + 1);
+  w.ring_end = c.take<int>(d.P + 1);
+  w.hdirs = c.take<DirLocal>(d.Ph + 1);
+  w.setup.remapS = c.take<Remap4<Real>>(B * d.n4());
+  w.setup.geom = c.take<CellGeom<Real>>(B * d.n4());
+  w.setup.remapT = c.take<Remap2<Real>>(B * d.nT());
+  w.setup.remapE = c.take<Remap2<Real>>(B * d.nE());
+  w.setup.rowinfo = c.take<RowInfo>(B * d.rows());
+  w.setup.rows = c.take<RowSample<Real>>(B * d.rows() * d.S);
+  w.setup.sdirs = c.take<SphereDir<Real>>(B * d.n0 * (long long)(d.P + 1));
+  w.T = c.take<Vec4<Real>>(B * d.nT());
+  w.E0 = c.take<Vec4<Real>>(B * d.nE());
+  for (int i = 0; i < 2; i++) {
+    w.dE[i] = c.take<Vec4<Real>>(B * d.nE());
+    w.Eacc[i] = c.take<Vec4<Real>>(B * d.nE());
+  }
+  w.S1R = c.take<Vec4<Real>>(B * d.n4());
+  w.M = c.take<Vec4<Real>>(B * d.n4());
+  w.J = c.take<Vec4<Real>>(B * d.n4());
+  for (int i = 0; i < 2; i++) {
+    w.dS[i] = c.take<Vec4<Real>>(B * d.n4());
+    w.Sacc[i] = c.take<Vec4<Real>>(B * d.n4());
+  }
+  if (outputs) {
+    w.oT = c.take<float>(3 * B * d.nT());
+    w.oE = c.take<float>(3 * B * d.nE());
+    w.oS = c.take<float>(3 * B * d.n4());
+    w.oM = c.take<float>(3 * B * d.n4());
+  } else {
+    w.oT = w.oE = w.oS = w.oM = nullptr;
+  }
+  return c.off + 256;
+}
+
+int current_device(int* dev) {
+  int n = 0;
+  cudaError_t e = cudaGetDeviceCount(&n);
+  if (e != cudaSuccess || n == 0) return fail(SFSIM_ATMO_ENODEV, "no CUDA device is visible");
+  CUDA_TRY(cudaGetDevice(dev));
+  if (*dev < 0 || *dev >= kMaxDevices) return fail(SFSIM_ATMO_ENODEV, "device ordinal out of range");
+  return 0;
+}
+
+int ensure_arena(int dev, size_t bytes) {
+  Arena& a = g_arena[dev];
+  if (a.size >= bytes) return 0;
+  if (a.base) {
+    CUDA_TRY(cudaDeviceSynchronize());
+    CUDA_TRY(cudaFree(a.base));
+    a.base = nullptr;
+    a.size = 0;
+  }
+  cudaError_t e = cudaMalloc(&a.base, bytes);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return fail(SFSIM_ATMO_ENOMEM, std::string("cudaMalloc of workspace failed: ") + cudaGetErrorString(e));
+  }
+  a.size = bytes;
+  return 0;
+}
+
+int ensure_stream(int dev) {
+  if (!g_stream[dev]) {
+    CUDA_TRY(cudaStreamCreateWithFlags(&g_stream[dev], cudaStreamNonBlocking));
+    for (int i = 0; i < 2 * 512; i++) CUDA_TRY(cudaEventCreate(&g_events[dev][i]));
+  }
+  return 0;
+}
+
+// Stage timing with events on the build stream.
+struct Timer {
+  int dev;
+  cudaStream_t st;
+  int n = 0;
+  int stage_of[512];
+  void mark_begin(int stage) {
+    if (!g_timing || n >= 511) return;
+    stage_of[n / 2] = stage;
+    cudaEventRecord(g_events[dev][n++], st);
+  }
+  void mark_end() {
+    if (!g_timing || n % 2 == 0) return;
+    cudaEventRecord(g_events[dev][n++], st);
+  }
+};
+
+// The order loop of atmosphere_lut.clj:86-97 with every table resident in
+// device memory; outputs are device pointers in the .scatter layout.
+template <class Real>
+int run_build(const Work<Real>& w, const BuildDims& d, float* oT, float* oE, float* oS, float* oM, cudaStream_t st,
+              Timer& tm, const sfsim_atmo_intermediates* inter) {
+  int launches = 0;
+  tm.mark_begin(0);
+  launch_setup<Real>(w.params, d, w.dirs, w.ring_end, w.setup, st);
+  launches += 5;
+  tm.mark_end();
+  tm.mark_begin(1);
+  launch_transmittance<Real>(w.params, d, w.T, st);
+  launches++;
+  tm.mark_end();
+  tm.mark_begin(2);
+  launch_surface_base<Real>(w.params, d, w.E0, st);
+  launches++;
+  tm.mark_end();
+  tm.mark_begin(3);
+  launch_first_order<Real>(w.params, d, w.setup.rowinfo, w.setup.rows, w.setup.geom, w.S1R, w.M, st);
+  launches++;
+  tm.mark_end();
+  CUDA_TRY(cudaGetLastError());
+  if (inter) {
+    if (inter->transmittance_nodes) launch_export<Real>(d.B * d.nT(), w.T, inter->transmittance_nodes, st);
+    if (inter->surface_base) launch_export<Real>(d.B * d.nE(), w.E0, inter->surface_base, st);
+    if (inter->rayleigh_first) launch_export<Real>(d.B * d.n4(), w.S1R, inter->rayleigh_first, st);
+    if (inter->mie_first) launch_export<Real>(d.B * d.n4(), w.M, inter->mie_first, st);
+  }
+
+  const Vec4<Real>* dS_prev = w.S1R;  // with M * phase in the first iteration
+  const Vec4<Real>* M_first = w.M;
+  const Vec4<Real>* dE_prev = w.E0;
+  const Vec4<Real>* S_prev = w.S1R;
+  const Vec4<Real>* E_prev = nullptr;  // E = constantly 0
+  for (int it = 0; it < d.iterations; it++) {
+    Vec4<Real>* dE_new = w.dE[it & 1];
+    Vec4<Real>* dS_new = w.dS[it & 1];
+    Vec4<Real>* E_new = w.Eacc[it & 1];
+    Vec4<Real>* S_new = w.Sacc[it & 1];
+    tm.mark_begin(5);
+    if (launch_point_scatter<Real>(w.params, d, w.setup.rowinfo, w.setup.sdirs, w.setup.geom, dS_prev, M_first,
+                                   dE_prev, w.J, st))
+      return fail(SFSIM_ATMO_ECUDA, "point scatter launch configuration failed");
+    launches++;
+    tm.mark_end();
+    tm.mark_begin(6);
+    launch_surface_radiance<Real>(w.params, d, w.hdirs, dS_prev, M_first, dE_new, st);
+    launches++;
+    tm.mark_end();
+    tm.mark_begin(7);
+    if (launch_ray_scatter<Real>(w.params, d, w.setup.rowinfo, w.setup.rows, w.setup.geom, w.setup.remapS, w.J,
+                                 dS_new, st))
+      return fail(SFSIM_ATMO_ECUDA, "ray scatter launch configuration failed");
+    launches++;
+    tm.mark_end();
+    tm.mark_begin(8);
+    launch_accumulate2<Real>(d.B, d.nE0, d.nE1, w.setup.remapE, E_prev, dE_new, E_new, st);
+    launch_accumulate4<Real>(d, w.setup.remapS, S_prev, dS_new, S_new, st);
+    launches += 2;
+    tm.mark_end();
+    CUDA_TRY(cudaGetLastError());
+    if (inter) {
+      if (inter->point_scatter)
+        launch_export<Real>(d.B * d.n4(), w.J, inter->point_scatter + (size_t)3 * d.B * d.n4() * it, st);
+      if (inter->surface_delta)
+        launch_export<Real>(d.B * d.nE(), dE_new, inter->surface_delta + (size_t)3 * d.B * d.nE() * it, st);
+      if (inter->ray_scatter_delta)
+        launch_export<Real>(d.B * d.n4(), dS_new, inter->ray_scatter_delta + (size_t)3 * d.B * d.n4() * it, st);
+    }
+    dS_prev = dS_new;
+    M_first = nullptr;
+    dE_prev = dE_new;
+    S_prev = S_new;
+    E_prev = E_new;
+  }
+  tm.mark_begin(9);
+  launch_output2<Real>(d.B, d.nT0, d.nT1, w.setup.remapT, w.T, oT, st);
+  launch_output2<Real>(d.B, d.nE0, d.nE1, w.setup.remapE, E_prev, oE, st);
+  launch_output4<Real>(d, w.setup.remapS, S_prev, oS, st);
+  launch_output4<Real>(d, w.setup.remapS, w.M, oM, st);
+  launches += 4;
+  tm.mark_end();
+  CUDA_TRY(cudaGetLastError());
+  g_launches = launches;
+  return 0;
+}
+
+void collect_timings(Timer& tm) {
+  for (int s = 0; s < kStages; s++) g_stage_ms[s] = 0;
+  g_have_timings = 0;
+  if (!g_timing) return;
+  for (int p = 0; p + 1 < tm.n; p += 2) {
+    float ms = 0;
+    if (cudaEventSynchronize(g_events[tm.dev][p + 1]) == cudaSuccess &&
+        cudaEventElapsedTime(&ms, g_events[tm.dev][p], g_events[tm.dev][p + 1]) == cudaSuccess)
+      g_stage_ms[tm.stage_of[p / 2]] += ms;
+  }
+  g_have_timings = kStages;
+}
+
+// Shared driver of all build entry points.  `host_out`: the four output
+// pointers are host memory (copied back and synchronised); otherwise device
+// memory on `user_stream`.
+template <class Real>
+int build_impl(const sfsim_atmo_config* cfgs, int B, float* T, float* E, float* S, float* M, bool host_out,
+               cudaStream_t user_stream, const sfsim_atmo_intermediates* inter) {
+  int dev = 0;
+  int rc = current_device(&dev);
+  if (rc) return rc;
+  if ((rc = ensure_stream(dev))) return rc;
+  BuildDims d = make_dims(cfgs[0], B);
+  if ((rc = check_smem<Real>(d))) return rc;
+  std::vector<AtmoParams> hp(B);
+  for (int b = 0; b < B; b++)
+    if ((rc = make_params(cfgs[b], hp[b]))) return rc;
+  std::vector<DirLocal> dirs, hdirs;
+  std::vector<int> ring_end, hring;
+  sphere_directions(cfgs[0].sphere_steps >> 1, cfgs[0].sphere_steps, M_PI, dirs, ring_end);
+  sphere_directions(cfgs[0].ray_steps >> 2, cfgs[0].ray_steps, M_PI / 2, hdirs, hring);
+
+  Work<Real> w;
+  size_t bytes = carve<Real>(w, nullptr, d, host_out);
+  if ((rc = ensure_arena(dev, bytes))) return rc;
+  carve<Real>(w, (char*)g_arena[dev].base, d, host_out);
+
+  cudaStream_t st = host_out ? g_stream[dev] : user_stream;
+  CUDA_TRY(cudaMemcpyAsync(w.params, hp.data(), sizeof(AtmoParams) * B, cudaMemcpyHostToDevice, st));
+  if (!dirs.empty()) {
+    CUDA_TRY(cudaMemcpyAsync(w.dirs, dirs.data(), sizeof(DirLocal) * dirs.size(), cudaMemcpyHostToDevice, st));
+    CUDA_TRY(cudaMemcpyAsync(w.ring_end, ring_end.data(), sizeof(int) * ring_end.size(), cudaMemcpyHostToDevice, st));
+  }
+  if (!hdirs.empty())
+    CUDA_TRY(cudaMemcpyAsync(w.hdirs, hdirs.data(), sizeof(DirLocal) * hdirs.size(), cudaMemcpyHostToDevice, st));
+
+  // debug intermediates go through device staging buffers
+  sfsim_atmo_intermediates dinter;
+  std::vector<std::pair<float*, float*>> copies;  // (device, host)
+  std::vector<size_t> copy_bytes;
+  float* staging = nullptr;
+  if (inter) {
+    const size_t n4 = 3 * (size_t)B * d.n4(), nE = 3 * (size_t)B * d.nE(), nT = 3 * (size_t)B * d.nT();
+    const size_t it = d.iterations;
+    size_t total = nT + nE + 2 * n4 + it * (2 * n4 + nE);
+    CUDA_TRY(cudaMalloc(&staging, total * sizeof(float)));
+    float* p = staging;
+    auto take = [&](float* host, size_t n) -> float* {
+      if (!host) return nullptr;
+      float* dptr = p;
+      p += n;
+      copies.push_back({dptr, host});
+      copy_bytes.push_back(n * sizeof(float));
+      return dptr;
+    };
+    dinter.transmittance_nodes = take(inter->transmittance_nodes, nT);
+    dinter.surface_base = take(inter->surface_base, nE);
+    dinter.rayleigh_first = take(inter->rayleigh_first, n4);
+    dinter.mie_first = take(inter->mie_first, n4);
+    dinter.point_scatter = take(inter->point_scatter, it * n4);
+    dinter.surface_delta = take(inter->surface_delta, it * nE);
+    dinter.ray_scatter_delta = take(inter->ray_scatter_delta, it * n4);
+  }
+
+  Timer tm;
+  tm.dev = dev;
+  tm.st = st;
+  float *dT = host_out ? w.oT : T, *dE = host_out ? w.oE : E, *dS = host_out ? w.oS : S, *dM = host_out ? w.oM : M;
+  rc = run_build<Real>(w, d, dT, dE, dS, dM, st, tm, inter ? &dinter : nullptr);
+  if (rc) {
+    if (staging) cudaFree(staging);
+    return rc;
+  }
+  if (host_out) {
+    CUDA_TRY(cudaMemcpyAsync(T, w.oT, sizeof(float) * 3 * B * d.nT(), cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaMemcpyAsync(E, w.oE, sizeof(float) * 3 * B * d.nE(), cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaMemcpyAsync(S, w.oS, sizeof(float) * 3 * B * d.n4(), cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaMemcpyAsync(M, w.oM, sizeof(float) * 3 * B * d.n4(), cudaMemcpyDeviceToHost, st));
+  }
+  for (size_t i = 0; i < copies.size(); i++)
+    CUDA_TRY(cudaMemcpyAsync(copies[i].second, copies[i].first, copy_bytes[i], cudaMemcpyDeviceToHost, st));
+  if (host_out || inter) CUDA_TRY(cudaStreamSynchronize(st));
+  if (staging) CUDA_TRY(cudaFree(staging));
+  collect_timings(tm);
+  return 0;
+}
+
+int dispatch(const sfsim_atmo_config* cfgs, int B, float* T, float* E, float* S, float* M, bool host_out,
+             cudaStream_t st, const sfsim_atmo_intermediates* inter) {
+  if (!cfgs) return fail(SFSIM_ATMO_ENULL, "config is NULL");
+  if (B < 1) return fail(SFSIM_ATMO_EINVAL, "batch size must be at least 1");
+  if (!T || !E || !S || !M) return fail(SFSIM_ATMO_ENULL, "an output pointer is NULL");
+  for (int b = 0; b < B; b++) {
+    int rc = validate(&cfgs[b]);
+    if (rc) return rc;
+    if (!same_layout(cfgs[0], cfgs[b]))
+      return fail(SFSIM_ATMO_EINVAL, "batched configs must share shapes, steps, iterations and precision");
+  }
+  std::lock_guard<std::mutex> lock(g_mutex);
+  if (cfgs[0].precision == SFSIM_ATMO_FP64) return build_impl<double>(cfgs, B, T, E, S, M, host_out, st, inter);
+  return build_impl<float>(cfgs, B, T, E, S, M, host_out, st, inter);
+}
+
+template <class Real>
+int census_impl(const sfsim_atmo_config& cfg, unsigned long long* out, int n) {
+  int dev = 0;
+  int rc = current_device(&dev);
+  if (rc) return rc;
+  if ((rc = ensure_stream(dev))) return rc;
+  BuildDims d = make_dims(cfg, 1);
+  AtmoParams hp;
+  if ((rc = make_params(cfg, hp))) return rc;
+  std::vector<DirLocal> dirs;
+  std::vector<int> ring_end;
+  sphere_directions(cfg.sphere_steps >> 1, cfg.sphere_steps, M_PI, dirs, ring_end);
+  Work<Real> w;
+  size_t bytes = carve<Real>(w, nullptr, d, false);
+  if ((rc = ensure_arena(dev, bytes + 256))) return rc;
+  carve<Real>(w, (char*)g_arena[dev].base, d, false);
+  unsigned long long* dcount = reinterpret_cast<unsigned long long*>((char*)g_arena[dev].base + bytes);
+  cudaStream_t st = g_stream[dev];
+  CUDA_TRY(cudaMemcpyAsync(w.params, &hp, sizeof(AtmoParams), cudaMemcpyHostToDevice, st));
+  if (!dirs.empty()) {
+    CUDA_TRY(cudaMemcpyAsync(w.dirs, dirs.data(), sizeof(DirLocal) * dirs.size(), cudaMemcpyHostToDevice, st));
+    CUDA_TRY(cudaMemcpyAsync(w.ring_end, ring_end.data(), sizeof(int) * ring_end.size(), cudaMemcpyHostToDevice, st));
+  }
+  CUDA_TRY(cudaMemsetAsync(dcount, 0, sizeof(unsigned long long), st));
+  launch_setup<Real>(w.params, d, w.dirs, w.ring_end, w.setup, st);
+  launch_first_order_census<Real>(w.params, d, w.setup.rowinfo, w.setup.rows, w.setup.geom, dcount, st);
+  CUDA_TRY(cudaGetLastError());
+  unsigned long long lit = 0;
+  CUDA_TRY(cudaMemcpyAsync(&lit, dcount, sizeof(lit), cudaMemcpyDeviceToHost, st));
+  CUDA_TRY(cudaStreamSynchronize(st));
+  const unsigned long long S = (unsigned long long)d.S, it = (unsigned long long)d.iterations;
+  const unsigned long long vals[6] = {lit,
+                                      lit * S,
+                                      (unsigned long long)d.rows() * S * S,
+                                      (unsigned long long)d.n4() * d.P * it,
+                                      (unsigned long long)d.n4() * S * it,
+                                      (unsigned long long)d.nE() * d.Ph * it};
+  int m = n < 6 ? n : 6;
+  for (int i = 0; i < m; i++) out[i] = vals[i];
+  return m;
+}
+
+}  // namespace
+
+extern "C" {
+
+int sfsim_atmo_census(const sfsim_atmo_config* cfg, unsigned long long* counts, int n) {
+  int rc = validate(cfg);
+  if (rc) return rc;
+  if (!counts) return fail(SFSIM_ATMO_ENULL, "counts is NULL");
+  std::lock_guard<std::mutex> lock(g_mutex);
+  if (cfg->precision == SFSIM_ATMO_FP64) return census_impl<double>(*cfg, counts, n);
+  return census_impl<float>(*cfg, counts, n);
+}
+
+int sfsim_atmo_sfu_peak(double* ex2_per_second) {
+  if (!ex2_per_second) return fail(SFSIM_ATMO_ENULL, "ex2_per_second is NULL");
+  std::lock_guard<std::mutex> lock(g_mutex);
+  int dev = 0;
+  int rc = current_device(&dev);
+  if (rc) return rc;
+  if ((rc = ensure_stream(dev))) return rc;
+  int sms = 0;
+  CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  const int blocks = sms * 8, threads = 256, iters = 4096;
+  float* sink = nullptr;
+  CUDA_TRY(cudaMalloc(&sink, sizeof(float) * blocks));
+  cudaStream_t st = g_stream[dev];
+  cudaEvent_t e0, e1;
+  CUDA_TRY(cudaEventCreate(&e0));
+  CUDA_TRY(cudaEventCreate(&e1));
+  double best = 0;
+  for (int rep = 0; rep < 5; rep++) {
+    CUDA_TRY(cudaEventRecord(e0, st));
+    launch_sfu_probe(blocks, threads, iters, sink, st);
+    CUDA_TRY(cudaEventRecord(e1, st));
+    CUDA_TRY(cudaEventSynchronize(e1));
+    float ms = 0;
+    CUDA_TRY(cudaEventElapsedTime(&ms, e0, e1));
+    const double ops = (double)blocks * threads * iters * 8;
+    if (rep > 0 && ms > 0) best = std::fmax(best, ops / (ms * 1e-3));
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  CUDA_TRY(cudaFree(sink));
+  *ex2_per_second = best;
+  return 0;
+}
+
+
+void sfsim_atmo_default_config(sfsim_atmo_config* c) {
+  if (!c) return;
+  memset(c, 0, sizeof(*c));
+  c->radius = 6378000.0;
+  c->height = 35000.0;
+  for (int i = 0; i < 3; i++) {
+    c->brightness[i] = 0.3;
+    c->intensity[i] = 1.0;
+    c->mie.scatter_base[i] = 2e-5;
+  }
+  c->mie.scatter_scale = 1200.0;
+  c->mie.scatter_quotient = 0.9;
+  c->mie.scatter_g = 0.76;
+  c->rayleigh.scatter_base[0] = 5.8e-6;
+  c->rayleigh.scatter_base[1] = 13.5e-6;
+  c->rayleigh.scatter_base[2] = 33.1e-6;
+  c->rayleigh.scatter_scale = 8000.0;
+  c->rayleigh.scatter_quotient = 1.0;
+  c->rayleigh.scatter_g = 0.0;
+  c->transmittance_shape[0] = 64;
+  c->transmittance_shape[1] = 255;
+  c->surface_radiance_shape[0] = 16;
+  c->surface_radiance_shape[1] = 63;
+  c->ray_scatter_shape[0] = 32;
+  c->ray_scatter_shape[1] = 127;
+  c->ray_scatter_shape[2] = 32;
+  c->ray_scatter_shape[3] = 8;
+  c->ray_steps = 100;
+  c->sphere_steps = 15;
+  c->iterations = 5;
+  c->precision = SFSIM_ATMO_FP32;
+  c->flags = 0;
+}
+
+int sfsim_atmo_validate(const sfsim_atmo_config* cfg) { return validate(cfg); }
+
+int sfsim_atmo_table_sizes(const sfsim_atmo_config* c, size_t* nT, size_t* nE, size_t* nS, size_t* nM) {
+  int rc = validate(c);
+  if (rc) return rc;
+  size_t n4 = 3;
+  for (int i = 0; i < 4; i++) n4 *= (size_t)c->ray_scatter_shape[i];
+  if (nT) *nT = 3 * (size_t)c->transmittance_shape[0] * c->transmittance_shape[1];
+  if (nE) *nE = 3 * (size_t)c->surface_radiance_shape[0] * c->surface_radiance_shape[1];
+  if (nS) *nS = n4;
+  if (nM) *nM = n4;
+  return 0;
+}
+
+int sfsim_atmo_build(const sfsim_atmo_config* cfg, float* T, float* E, float* S, float* M) {
+  return dispatch(cfg, 1, T, E, S, M, true, nullptr, nullptr);
+}
+
+int sfsim_atmo_build_device(const sfsim_atmo_config* cfg, float* T, float* E, float* S, float* M, void* stream) {
+  return dispatch(cfg, 1, T, E, S, M, false, (cudaStream_t)stream, nullptr);
+}
+
+int sfsim_atmo_build_batch(const sfsim_atmo_config* cfgs, int n, float* T, float* E, float* S, float* M) {
+  return dispatch(cfgs, n, T, E, S, M, true, nullptr, nullptr);
+}
+
+int sfsim_atmo_build_debug(const sfsim_atmo_config* cfg, float* T, float* E, float* S, float* M,
+                           const sfsim_atmo_intermediates* inter) {
+  return dispatch(cfg, 1, T, E, S, M, true, nullptr, inter);
+}
+
+int sfsim_atmo_set_timing(int enabled) {
+  g_timing = enabled != 0;
+  return 0;
+}
+
+int sfsim_atmo_last_timings(double* ms, int n) {
+  if (!ms) return fail(SFSIM_ATMO_ENULL, "ms is NULL");
+  int m = n < g_have_timings ? n : g_have_timings;
+  for (int i = 0; i < m; i++) ms[i] = g_stage_ms[i];
+  return m;
+}
+
+int sfsim_atmo_last_launch_count(void) { return g_launches; }
+
+int sfsim_atmo_release(void) {
+  std::lock_guard<std::mutex> lock(g_mutex);
+  int dev = 0;
+  int rc = current_device(&dev);
+  if (rc) return rc;
+  Arena& a = g_arena[dev];
+  if (a.base) {
+    CUDA_TRY(cudaDeviceSynchronize());
+    CUDA_TRY(cudaFree(a.base));
+  }
+  a.base = nullptr;
+  a.size = 0;
+  return 0;
+}
+
+const char* sfsim_atmo_strerror(int code) {
+  switch (code) {
+    case SFSIM_ATMO_OK: return "success";
+    case SFSIM_ATMO_EINVAL: return "invalid configuration value";
+    case SFSIM_ATMO_ENOMEM: return "out of memory";
+    case SFSIM_ATMO_ECUDA: return "CUDA runtime error";
+    case SFSIM_ATMO_ENODEV: return "no CUDA device";
+    case SFSIM_ATMO_ESHAPE: return "unsupported table shape";
+    case SFSIM_ATMO_ENULL: return "NULL pointer argument";
+    case SFSIM_ATMO_ETOOBIG: return "size exceeds a fixed capacity";
+    case SFSIM_ATMO_ENUMERIC: return "result contains NaN or Inf";
+    default: return "unknown error";
+  }
+}
+
+const char* sfsim_atmo_last_error(void) { return g_last_error.c_str(); }
+
+const char* sfsim_atmo_version(void) { return "sfsim-atmo-gb300 0.1.0 (sm_103a)"; }
+
+}  // extern "C"

@@ -1,0 +1,439 @@
+// atmo_device.cuh -- device math of the atmosphere lookup-table build.
+//
+// Two kinds of arithmetic live here:
+//  * FP64 "islands": the table parameterisations, ray-sphere intersections and
+//    horizon tests, written as the same IEEE double operations as the
+//    reference (src/clj/sfsim/atmosphere.clj:70-384, sphere.clj:34-59,
+//    util.clj:403-420), because radius-scale cancellation (r ~ 6.4e6 m) makes
+//    them unusable in FP32.
+//  * the bulk integrand in `Real` (float or double): optical-depth sums along
+//    rays in the cancellation-free form q(t) = |p|^2 - R^2 = q0 + t (2b + t),
+//    heights from q through a fitted polynomial h = q P(q), exponentials on
+//    the SFU (ex2.approx) in FP32, compensated (Kahan) sums.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <math.h>
+#include <type_traits>
+
+#include "atmo_params.h"
+
+namespace sfsim {
+
+// ---------------------------------------------------------------------------
+// small vector helpers
+// ---------------------------------------------------------------------------
+
+struct d3 {
+  double x, y, z;
+};
+
+// FP64 islands use separately rounded multiplies and adds, never fused: the
+// reference (JVM doubles) rounds every operation, and at the horizon nodes
+// the table maps take square roots of near-zero differences that amplify a
+// one-ulp change into a visible one.
+#ifdef __CUDA_ARCH__
+__device__ __forceinline__ double dmul(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double dadd(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ double dsub(double a, double b) { return __dsub_rn(a, b); }
+#else
+inline double dmul(double a, double b) { return a * b; }
+inline double dadd(double a, double b) { return a + b; }
+inline double dsub(double a, double b) { return a - b; }
+#endif
+
+__host__ __device__ __forceinline__ d3 mk3(double x, double y, double z) { return d3{x, y, z}; }
+__host__ __device__ __forceinline__ d3 add3(d3 a, d3 b) { return d3{dadd(a.x, b.x), dadd(a.y, b.y), dadd(a.z, b.z)}; }
+__host__ __device__ __forceinline__ d3 sub3(d3 a, d3 b) { return d3{dsub(a.x, b.x), dsub(a.y, b.y), dsub(a.z, b.z)}; }
+__host__ __device__ __forceinline__ d3 mul3(d3 a, double s) { return d3{dmul(a.x, s), dmul(a.y, s), dmul(a.z, s)}; }
+__host__ __device__ __forceinline__ double dot3(d3 a, d3 b) {
+  return dadd(dadd(dmul(a.x, b.x), dmul(a.y, b.y)), dmul(a.z, b.z));
+}
+__host__ __device__ __forceinline__ double mag3(d3 a) { return sqrt(dot3(a, a)); }
+__host__ __device__ __forceinline__ double sqr(double x) { return dmul(x, x); }
+__host__ __device__ __forceinline__ double dmax(double a, double b) { return a >= b ? a : b; }
+__host__ __device__ __forceinline__ double dmin(double a, double b) { return a <= b ? a : b; }
+
+// ---------------------------------------------------------------------------
+// FP64 islands (reference semantics)
+// ---------------------------------------------------------------------------
+
+// util.clj:403-420
+__host__ __device__ inline double limit_quot(double a, double b, double lower, double upper) {
+  if (a == 0.0) return a;
+  if (b < 0) {
+    a = -a;
+    b = -b;
+  }
+  if (a < b * upper) {
+    if (a > b * lower) return a / b;
+    return lower;
+  }
+  return upper;
+}
+
+// sphere.clj:46-59; returns distance + length of the chosen branch pieces.
+struct Isect {
+  double distance, length;
+};
+
+__host__ __device__ inline Isect ray_sphere(double radius, d3 origin, d3 direction) {
+  double direction_sqr = dot3(direction, direction);
+  double od = dot3(direction, origin);
+  double discriminant = dsub(sqr(od), dmul(direction_sqr, dsub(dot3(origin, origin), sqr(radius))));
+  double middle = -(od / direction_sqr);
+  Isect r;
+  if (discriminant > 0) {
+    double length2 = sqrt(discriminant) / direction_sqr;
+    if (middle < length2) {
+      r.distance = 0.0;
+      r.length = dmax(0.0, dadd(middle, length2));
+    } else {
+      r.distance = dsub(middle, length2);
+      r.length = dmul(2.0, length2);
+    }
+  } else {
+    r.distance = dmax(0.0, middle);
+    r.length = 0.0;
+  }
+  return r;
+}
+
+// atmosphere.clj:70-85
+__host__ __device__ inline d3 atmosphere_intersection(const AtmoParams& P, d3 o, d3 d) {
+  Isect i = ray_sphere(P.top, o, d);
+  return add3(o, mul3(d, dadd(i.distance, i.length)));
+}
+
+__host__ __device__ inline d3 surface_intersection(const AtmoParams& P, d3 o, d3 d) {
+  Isect i = ray_sphere(P.R, o, d);
+  return add3(o, mul3(d, i.distance));
+}
+
+// atmosphere.clj:88-111
+__host__ __device__ inline int surface_point(const AtmoParams& P, d3 point) {
+  return dmul(2.0, dsub(mag3(point), P.R)) < P.H;
+}
+
+__host__ __device__ inline int is_above_horizon(const AtmoParams& P, d3 point, d3 direction) {
+  double norm_point = mag3(point);
+  double s = dot3(direction, point);
+  double hd2 = dsub(sqr(norm_point), P.R2);
+  return (s >= 0) || (sqr(s) <= hd2);
+}
+
+__host__ __device__ inline d3 ray_extremity(const AtmoParams& P, d3 o, d3 d) {
+  if (is_above_horizon(P, o, d)) return atmosphere_intersection(P, o, d);
+  return surface_intersection(P, o, d);
+}
+
+// atmosphere.clj:233-236
+__host__ __device__ inline double horizon_distance(const AtmoParams& P, double radius) {
+  return sqrt(dmax(0.0, dsub(sqr(radius), P.R2)));
+}
+
+// atmosphere.clj:239-253
+__host__ __device__ inline double elevation_to_index(const AtmoParams& P, int size, d3 point, d3 direction,
+                                                     int above) {
+  double radius = mag3(point);
+  double sin_elevation = dot3(point, direction) / radius;
+  double rho = horizon_distance(P, radius);
+  double rs = dmul(radius, sin_elevation);
+  double Delta = dsub(sqr(rs), sqr(rho));
+  double idx;
+  if (above)
+    idx = dsub(0.5, limit_quot(dsub(rs, sqrt(dmax(0.0, dadd(Delta, P.Hh2)))), dadd(dadd(rho, rho), dmul(2.0, P.Hh)),
+                               -0.5, 0.0));
+  else
+    idx = dadd(0.5, limit_quot(dadd(rs, sqrt(dmax(0.0, Delta))), dadd(rho, rho), -0.5, 0.0));
+  return dmul((double)(size - 1), idx);
+}
+
+// atmosphere.clj:256-270; direction = (sin, cos, 0)
+__host__ __device__ inline void index_to_elevation(const AtmoParams& P, int size, double radius, double index,
+                                                   double* sin_el, double* cos_el, int* above) {
+  double horizon_dist = horizon_distance(P, radius);
+  double scaled_index = index / (size - 1);
+  double s;
+  if (scaled_index < 0.5 || (scaled_index == 0.5 && dmul(2.0, radius) < dadd(P.R, P.top))) {
+    double ground_dist = dmul(horizon_dist, dsub(1.0, dmul(2.0, scaled_index)));
+    s = limit_quot(dsub(dsub(P.R2, sqr(radius)), sqr(ground_dist)), dmul(dmul(2.0, radius), ground_dist), -1.0, 1.0);
+    *above = 0;
+  } else {
+    double sky_dist = dmul(dadd(horizon_dist, P.Hh), dsub(dmul(2.0, scaled_index), 1.0));
+    s = limit_quot(dsub(dsub(P.top2, sqr(radius)), sqr(sky_dist)), dmul(dmul(2.0, radius), sky_dist), -1.0, 1.0);
+    *above = 1;
+  }
+  *sin_el = s;
+  *cos_el = sqrt(dsub(1.0, sqr(s)));
+}
+
+// atmosphere.clj:273-288
+__host__ __device__ inline double height_to_index(const AtmoParams& P, int size, double radius) {
+  return dmul((double)(size - 1), horizon_distance(P, radius) / horizon_distance(P, P.top));
+}
+
+__host__ __device__ inline double index_to_radius(const AtmoParams& P, int size, double index) {
+  double horizon_dist = dmul(index / (size - 1), P.Hh);
+  return sqrt(dadd(P.R2, sqr(horizon_dist)));
+}
+
+// atmosphere.clj:322-332
+__host__ __device__ inline double sun_elevation_to_index(int size, d3 point, d3 light) {
+  double sin_elevation = dot3(point, light) / mag3(point);
+  return dmul((double)(size - 1),
+              dmax(0.0, dsub(1.0, exp(dsub(dsub(0.0, dmul(3.0, sin_elevation)), 0.6))) / dsub(1.0, exp(-3.6))));
+}
+
+__host__ __device__ inline double index_to_sin_sun_elevation(int size, double index) {
+  return dadd(log(dsub(1.0, dmul(index / (size - 1), dsub(1.0, exp(-3.6))))), 0.6) / -3.0;
+}
+
+// atmosphere.clj:368-384
+__host__ __device__ inline double sun_angle_to_index(int size, d3 direction, d3 light) {
+  return dmul((double)(size - 1), dadd(1.0, dot3(direction, light)) / 2.0);
+}
+
+__host__ __device__ inline d3 index_to_sun_direction(int size, d3 direction, double sin_sun, double index) {
+  double dot_view_sun = dsub(dmul(2.0, index / (size - 1)), 1.0);
+  double max_sun_1 = sqrt(dmax(0.0, dsub(1.0, sqr(sin_sun))));
+  double sun_1 = limit_quot(dsub(dot_view_sun, dmul(direction.x, sin_sun)), direction.y, -max_sun_1, max_sun_1);
+  double sun_2 = sqrt(dmax(0.0, dsub(dsub(1.0, sqr(sun_1)), sqr(sin_sun))));
+  return mk3(sin_sun, sun_1, sun_2);
+}
+
+// interpolate.clj:75-98 per dimension: i = clip(c), u = floor(i), s = i - u
+template <class Real>
+__host__ __device__ inline void split_coord(double c, int size, int* u, Real* s) {
+  double i = dmin(dmax(c, 0.0), (double)(size - 1));
+  double f = floor(i);
+  *u = (int)f;
+  *s = (Real)dsub(i, f);
+}
+
+template <class Real>
+__device__ __forceinline__ void split_coord_r(Real c, int size, int* u, Real* s) {
+  Real i = c < Real(0) ? Real(0) : c;
+  Real hi = Real(size - 1);
+  i = i > hi ? hi : i;
+  Real f = floor(i);
+  *u = (int)f;
+  *s = i - f;
+}
+
+__host__ __device__ __forceinline__ int upper_index(int u, int size) { return u + 1 < size ? u + 1 : size - 1; }
+
+__host__ __device__ inline d3 cross3(d3 a, d3 b) {
+  return mk3(dsub(dmul(a.y, b.z), dmul(a.z, b.y)), dsub(dmul(a.z, b.x), dmul(a.x, b.z)),
+             dsub(dmul(a.x, b.y), dmul(a.y, b.x)));
+}
+
+// quaternion.clj:166-171
+__host__ __device__ inline d3 orthogonal(d3 n) {
+  d3 rows[3] = {mk3(1, 0, 0), mk3(0, 1, 0), mk3(0, 0, 1)};
+  int best = 0;
+  double key = fabs(dot3(n, rows[0]));
+  for (int i = 1; i < 3; i++) {
+    double kk = fabs(dot3(n, rows[i]));
+    if (kk < key) {
+      key = kk;
+      best = i;
+    }
+  }
+  d3 c = cross3(n, rows[best]);
+  return mul3(c, 1.0 / mag3(c));
+}
+
+// mulv (transpose (oriented-matrix n)) (vec3 x y z), matrix.clj:207-213
+__host__ __device__ inline d3 to_world(d3 n, d3 o1, d3 o2, const DirLocal& q) {
+  return mk3(dadd(dadd(dmul(n.x, q.x), dmul(o1.x, q.y)), dmul(o2.x, q.z)),
+             dadd(dadd(dmul(n.y, q.x), dmul(o1.y, q.y)), dmul(o2.y, q.z)),
+             dadd(dadd(dmul(n.z, q.x), dmul(o1.z, q.y)), dmul(o2.z, q.z)));
+}
+
+// Geometry of a 4-D node (ray-scatter-backward, atmosphere.clj:401-412).
+struct NodeGeom {
+  double r;
+  double sv, cv;
+  int above;
+  d3 l;
+};
+
+__host__ __device__ inline void view_geometry(const AtmoParams& P, const BuildDims& d, int i, int j, double* r,
+                                              double* sv, double* cv, int* above) {
+  *r = index_to_radius(P, d.n0, (double)i);
+  index_to_elevation(P, d.n1, *r, (double)j, sv, cv, above);
+}
+
+__host__ __device__ inline d3 light_direction(const BuildDims& d, double sv, double cv, int k, int a) {
+  double sin_sun = index_to_sin_sun_elevation(d.n2, (double)k);
+  return index_to_sun_direction(d.n3, mk3(sv, cv, 0.0), sin_sun, (double)a);
+}
+
+// ---------------------------------------------------------------------------
+// Bulk arithmetic in Real
+// ---------------------------------------------------------------------------
+
+template <class Real>
+struct Bulk;
+
+template <>
+struct Bulk<float> {
+  static __device__ __forceinline__ float exp2(float x) {
+    float r;
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+  }
+  static __device__ __forceinline__ float sqrt(float x) {
+    float r;
+    asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+  }
+  static __device__ __forceinline__ float rsqrt(float x) {
+    float r;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+  }
+  static __device__ __forceinline__ float div(float a, float b) { return __fdividef(a, b); }
+  static __device__ __forceinline__ const float* hpoly(const AtmoParams& P) { return P.f_hpoly; }
+  static __device__ __forceinline__ float alpha(const AtmoParams& P) { return P.f_alpha; }
+  static __device__ __forceinline__ float beta(const AtmoParams& P) { return P.f_beta; }
+  static __device__ __forceinline__ float kr(const AtmoParams& P) { return P.f_kr; }
+  static __device__ __forceinline__ float km(const AtmoParams& P) { return P.f_km; }
+  static __device__ __forceinline__ float ray_ext(const AtmoParams& P, int c) { return P.f_ray_ext[c]; }
+  static __device__ __forceinline__ float mie_ext(const AtmoParams& P, int c) { return P.f_mie_ext[c]; }
+};
+
+template <>
+struct Bulk<double> {
+  static __device__ __forceinline__ double exp2(double x) { return ::exp2(x); }
+  static __device__ __forceinline__ double sqrt(double x) { return ::sqrt(x); }
+  static __device__ __forceinline__ double rsqrt(double x) { return 1.0 / ::sqrt(x); }
+  static __device__ __forceinline__ double div(double a, double b) { return a / b; }
+  static __device__ __forceinline__ const double* hpoly(const AtmoParams& P) { return P.d_hpoly; }
+  static __device__ __forceinline__ double alpha(const AtmoParams& P) { return P.d_alpha; }
+  static __device__ __forceinline__ double beta(const AtmoParams& P) { return P.d_beta; }
+  static __device__ __forceinline__ double kr(const AtmoParams& P) { return P.d_kr; }
+  static __device__ __forceinline__ double km(const AtmoParams& P) { return P.d_km; }
+  static __device__ __forceinline__ double ray_ext(const AtmoParams& P, int c) { return P.d_ray_ext[c]; }
+  static __device__ __forceinline__ double mie_ext(const AtmoParams& P, int c) { return P.d_mie_ext[c]; }
+};
+
+template <class Real>
+__device__ __forceinline__ void kahan_add(Real& sum, Real& comp, Real x) {
+  Real y = x - comp;
+  Real t = sum + y;
+  comp = (t - sum) - y;
+  sum = t;
+}
+
+// Height above ground from q = |p|^2 - R^2: h = q / (R + sqrt(R^2 + q)),
+// evaluated as q * P(z), z = q alpha + beta, P fitted on the host over the
+// atmosphere's range of q (Chebyshev interpolation, relative error < 1e-9).
+template <class Real, int NP>
+__device__ __forceinline__ Real height_from_q(Real q, const Real* c, Real alpha, Real beta) {
+  Real z = fma(q, alpha, beta);
+  Real p = c[NP - 1];
+#pragma unroll
+  for (int k = NP - 2; k >= 0; k--) p = fma(p, z, c[k]);
+  return q * p;
+}
+
+// Sums of exp(-h/H_rayleigh) and exp(-h/H_mie) over the midpoint samples
+// t_n = (n + 1/2) dt of a ray with q(t) = q0 + t (two_b + t), where
+// two_b = 2 p.d for a unit direction d.  Compensated sums.
+template <class Real, int NP>
+__device__ __forceinline__ void optical_sums(Real q0, Real two_b, Real dt, int steps, const Real* c, Real alpha,
+                                             Real beta, Real kr, Real km, Real& sum_r, Real& sum_m) {
+  Real sr = 0, cr = 0, sm = 0, cm = 0;
+  Real half = Real(0.5) * dt;
+  Real fn = 0;
+  for (int n = 0; n < steps; n++) {
+    Real t = fma(fn, dt, half);
+    Real q = fma(t, two_b + t, q0);
+    Real h = height_from_q<Real, NP>(q, c, alpha, beta);
+    Real er = Bulk<Real>::exp2(h * kr);
+    Real em = Bulk<Real>::exp2(h * km);
+    kahan_add(sr, cr, er);
+    kahan_add(sm, cm, em);
+    fn += Real(1);
+  }
+  sum_r = sr;
+  sum_m = sm;
+}
+
+// Same sums for a segment parameterised by u in [0, 1]:
+// q(u) = c0 + u (two_xd + u dd) with two_xd = 2 x.D, dd = D.D.
+template <class Real, int NP>
+__device__ __forceinline__ void optical_sums_u(Real c0, Real two_xd, Real dd, Real du, int steps, const Real* c,
+                                               Real alpha, Real beta, Real kr, Real km, Real& sum_r, Real& sum_m) {
+  Real sr = 0, cr = 0, sm = 0, cm = 0;
+  Real half = Real(0.5) * du;
+  Real fn = 0;
+  for (int n = 0; n < steps; n++) {
+    Real u = fma(fn, du, half);
+    Real q = fma(u, fma(u, dd, two_xd), c0);
+    Real h = height_from_q<Real, NP>(q, c, alpha, beta);
+    Real er = Bulk<Real>::exp2(h * kr);
+    Real em = Bulk<Real>::exp2(h * km);
+    kahan_add(sr, cr, er);
+    kahan_add(sm, cm, em);
+    fn += Real(1);
+  }
+  sum_r = sr;
+  sum_m = sm;
+}
+
+// Optical depth (RGB) of a segment from x to x + D, x and D in FP64, with
+// `steps` midpoint samples (ray.clj:19-30 with atmosphere.clj:114-125).
+template <class Real>
+__device__ inline void segment_depth(const AtmoParams& P, d3 x, d3 D, int steps, Real tau[3]) {
+  double L = mag3(D);
+  if (!(L > 0.0)) {
+    tau[0] = tau[1] = tau[2] = 0;
+    return;
+  }
+  double c0 = (mag3(x) - P.R) * (mag3(x) + P.R);
+  Real sr, sm;
+  optical_sums_u<Real, 5>((Real)c0, (Real)(2.0 * dot3(x, D)), (Real)dot3(D, D), (Real)(1.0 / steps), steps,
+                          Bulk<Real>::hpoly(P), Bulk<Real>::alpha(P), Bulk<Real>::beta(P), Bulk<Real>::kr(P),
+                          Bulk<Real>::km(P), sr, sm);
+  Real a = (Real)(L / steps);
+#pragma unroll
+  for (int ch = 0; ch < 3; ch++) tau[ch] = a * (Bulk<Real>::ray_ext(P, ch) * sr + Bulk<Real>::mie_ext(P, ch) * sm);
+}
+
+template <class Real>
+__device__ __forceinline__ Real exp_neg(Real tau) {
+  return Bulk<Real>::exp2(tau * Real(-1.4426950408889634));
+}
+
+// Cornette-Shanks phase (atmosphere.clj:56-61); g = 0 gives Rayleigh.
+template <class Real>
+__device__ __forceinline__ Real phase_cs(Real g, Real mu) {
+  Real g2 = g * g;
+  Real base = (Real(1) + g2) - Real(2) * g * mu;
+  Real num = Real(3) * (Real(1) - g2) * (Real(1) + mu * mu);
+  Real den = Real(8) * Real(3.14159265358979323846) * (Real(2) + g2);
+  Real rs = Bulk<Real>::rsqrt(base);
+  return num / den * (rs * rs * rs);
+}
+
+template <class Real>
+__device__ __forceinline__ Real phase_rayleigh(Real mu) {
+  return Real(3.0 / (16.0 * 3.14159265358979323846)) * (Real(1) + mu * mu);
+}
+
+// Bilinear mix of four RGB texels (interpolate.clj:81-98 order: inner dimension first).
+template <class Real>
+__device__ __forceinline__ void mix4(const Real* a, const Real* b, const Real* c, const Real* d, Real s_outer,
+                                     Real s_inner, Real out[3]) {
+#pragma unroll
+  for (int ch = 0; ch < 3; ch++) {
+    Real lo = a[ch] * (Real(1) - s_inner) + b[ch] * s_inner;
+    Real hi = c[ch] * (Real(1) - s_inner) + d[ch] * s_inner;
+    out[ch] = lo * (Real(1) - s_outer) + hi * s_outer;
+  }
+}
+
+}  // namespace sfsim

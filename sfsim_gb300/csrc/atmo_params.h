@@ -1,0 +1,137 @@
+// atmo_params.h -- parameters and buffer records shared by the host driver and
+// the CUDA kernels of the atmosphere lookup-table build.
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+
+#ifdef __CUDACC__
+#define SFSIM_HD __host__ __device__
+#else
+#define SFSIM_HD
+#endif
+
+namespace sfsim {
+
+constexpr int kMaxHPoly = 8;  // coefficients of the height-from-q polynomial
+
+// One atmosphere.  Geometry in FP64; the bulk constants also as float so the
+// FP32 kernels read them without conversions.
+struct AtmoParams {
+  // geometry
+  double R, H, top;        // ground radius, atmosphere height, top radius
+  double R2, top2;         // squares
+  double Hh, Hh2;          // horizon distance at the top: sqrt(top^2 - R^2), and its square
+  // components; mie is scatter[0], rayleigh scatter[1] (atmosphere_lut.clj:63)
+  double mie_base[3], mie_scale, mie_quot, mie_g;
+  double ray_base[3], ray_scale, ray_quot, ray_g;
+  double brightness[3], intensity[3];
+  // bulk constants
+  double d_mie_ext[3], d_ray_ext[3];  // base / quotient
+  double d_km, d_kr;                  // -log2(e) / scale height
+  double d_hpoly[kMaxHPoly];          // h(q) = q * P(q * alpha + beta)
+  double d_alpha, d_beta;
+  float f_mie_ext[3], f_ray_ext[3];
+  float f_mie_base[3], f_ray_base[3];
+  float f_km, f_kr;
+  float f_hpoly[kMaxHPoly];
+  float f_alpha, f_beta;
+  float f_R, f_Hh2, f_mie_g;
+  float f_bright_pi[3];               // brightness / pi
+  float f_intensity[3];
+  int hpoly_n;                        // number of coefficients
+};
+
+// Shapes, steps and sizes shared by every atmosphere of one batched build.
+struct BuildDims {
+  int B;                   // atmospheres
+  int nT0, nT1;            // transmittance [height][elevation]
+  int nE0, nE1;            // surface radiance [height][sun elevation]
+  int n0, n1, n2, n3;      // ray scatter [height][elevation][sun elevation][sun heading]
+  int S;                   // ray steps
+  int sphere_steps;        // point-scatter sphere steps
+  int P;                   // directions of integral-sphere(sphere_steps)
+  int Ph;                  // directions of integral-half-sphere(ray_steps)
+  int iterations;
+  SFSIM_HD long long nT() const { return (long long)nT0 * nT1; }
+  SFSIM_HD long long nE() const { return (long long)nE0 * nE1; }
+  SFSIM_HD long long n4() const { return (long long)n0 * n1 * n2 * n3; }
+  SFSIM_HD long long rows() const { return (long long)n0 * n1; }
+};
+
+// A sample direction of a spherical integral in the local frame
+// (cos theta, sin theta cos phi, sin theta sin phi) with its quadrature weight.
+struct DirLocal {
+  double x, y, z, w;
+};
+
+// Interpolation coordinate of one table dimension: lower index and fraction.
+template <class Real>
+struct alignas(2 * sizeof(Real) >= 8 ? 2 * sizeof(Real) : 8) Coord {
+  int u;
+  Real s;
+};
+
+// Re-interpolation coordinates of a 4-D node (forward of backward of the node).
+template <class Real>
+struct Remap4 {
+  int u[4];
+  Real s[4];
+};
+
+template <class Real>
+struct Remap2 {
+  int u[2];
+  Real s[2];
+};
+
+template <class Real>
+struct alignas(4 * sizeof(Real)) Vec4 {
+  Real x, y, z, w;
+};
+
+// Light direction and view-light cosine of a 4-D node, computed once in FP64
+// (index-to-sun-direction, atmosphere.clj:375-384) and stored in Real.
+template <class Real>
+struct alignas(4 * sizeof(Real)) CellGeom {
+  Real lx, ly, lz, mu;
+};
+
+// Per view row (height i, elevation j) of the 4-D space, FP64.
+struct RowInfo {
+  double r;            // |x|, x = (r, 0, 0)
+  double sv, cv;       // view direction (sv, cv, 0)
+  double D[3];         // ray segment from x to its extremity
+  double L;            // |D|
+  int above;           // above-horizon flag of the node
+  int pad;
+};
+
+// Per view row and ray sample s (p_s = x + D (s + 1/2)/S).
+template <class Real>
+struct RowSample {
+  Real tau[3];         // optical depth from x to p_s (RGB)
+  Real er, em;         // exp(-h/H_rayleigh), exp(-h/H_mie) at p_s
+  Real q;              // |p_s|^2 - R^2
+  Real us;             // (s + 1/2)/S
+  Real inv_r;          // 1/|p_s|
+  int u0, u1;          // height and elevation coordinates of p_s in the 4-D space
+  Real s0, s1;
+  Real pad;
+};
+
+// Per height row i and sphere direction of point scatter.
+template <class Real>
+struct SphereDir {
+  Real w[3];           // direction omega in world coordinates
+  Real weight;         // quadrature weight (ring factor * 2 pi / ring steps)
+  Real gdir[3];        // unit vector of the ground point (surface directions)
+  Real ground[3];      // T(x, g) * brightness / pi (surface directions)
+  int surface;         // 1: the direction ends on the ground
+  int u1;              // elevation coordinate of (x, omega, !surface)
+  int uE0;             // height coordinate of the ground point in the surface space
+  int pad;
+  Real s1, sE0;
+};
+
+}  // namespace sfsim

@@ -1,0 +1,210 @@
+// k_first_order.cu -- first-order Rayleigh ray scatter and Mie strength,
+// atmosphere_lut.clj:68-78 with atmosphere.clj:154-200.
+//
+// For a 4-D node (x, v, l, above) the reference integrates, over the S
+// midpoint samples p_s of the view ray from x to its extremity,
+//   T(x, p_s) * beta_c(p_s) * [phase_c(v.l)] * I * T(p_s, l)   (sun above p_s's horizon)
+// once for Rayleigh (with phase) and once for the Mie strength (no phase).
+// Both share T(x, p_s) and T(p_s, l); this kernel evaluates them once.
+//
+// Mapping: one block per view row (height i, elevation j).  The row's S
+// samples (positions, T(x, p_s), the heights' exponentials) come from
+// k_view_rows and sit in shared memory.  Each warp takes one cell (sun
+// elevation k, sun heading a) at a time and its lanes take the samples: a
+// lane integrates the optical depth of the sun ray from its p_s (S midpoint
+// samples, FP32, compensated sums), and the warp reduces the samples with
+// shuffles.  Shadowed samples form contiguous runs along a ray, so lanes of a
+// warp mostly agree on whether to integrate.
+#include "atmo_device.cuh"
+#include "kernels.h"
+
+namespace sfsim {
+
+template <class Real>
+struct FirstOrderSmem {
+  Real tau[3];
+  Real er, em, q, us;
+};
+
+// Horizon test of the sun at p_s (atmosphere.clj:95-102, filtered-sun-light
+// :154-160) from b = p_s.l and q = |p_s|^2 - R^2.  Near the boundary FP32
+// inputs cannot decide (b carries ~1 m of rounding), so the test is repeated
+// in FP64 on p_s as integral-ray forms it (ray.clj:22-24).
+template <class Real>
+__device__ __forceinline__ bool sun_visible(const AtmoParams& P, const BuildDims& d, const RowInfo& ri, Real bp,
+                                            Real q, int cell, int s) {
+  bool lit = (bp >= Real(0)) || (bp * bp <= q);
+  if (std::is_same<Real, float>::value) {
+    const Real m = bp * bp - q;
+    if ((bp < Real(4)) && (fabs(m) < Real(1.0e8) || (bp > Real(-4) && q < Real(1.0e8)))) {
+      const d3 l = light_direction(d, ri.sv, ri.cv, cell / d.n3, cell % d.n3);
+      const d3 p = add3(mk3(ri.r, 0, 0), mul3(mk3(ri.D[0], ri.D[1], ri.D[2]), (0.5 + s) * (1.0 / d.S)));
+      lit = is_above_horizon(P, p, l);
+    }
+  }
+  return lit;
+}
+
+template <class Real>
+__device__ __forceinline__ Real warp_sum(Real v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+template <class Real, int WARPS>
+__global__ void __launch_bounds__(WARPS * 32) k_first_order(const AtmoParams* params, BuildDims d,
+                                                            const RowInfo* rowinfo, const RowSample<Real>* rows,
+                                                            const CellGeom<Real>* geom, Vec4<Real>* rayleigh,
+                                                            Vec4<Real>* mie) {
+  extern __shared__ unsigned char smem_raw[];
+  FirstOrderSmem<Real>* sm = reinterpret_cast<FirstOrderSmem<Real>*>(smem_raw);
+  const int b = blockIdx.y;
+  const long long row = blockIdx.x;
+  const long long nrows = d.rows();
+  const AtmoParams& P = params[b];
+  const int S = d.S;
+  const RowSample<Real>* rs = rows + (b * nrows + row) * S;
+  for (int s = threadIdx.x; s < S; s += blockDim.x) {
+    RowSample<Real> v = rs[s];
+    sm[s].tau[0] = v.tau[0];
+    sm[s].tau[1] = v.tau[1];
+    sm[s].tau[2] = v.tau[2];
+    sm[s].er = v.er;
+    sm[s].em = v.em;
+    sm[s].q = v.q;
+    sm[s].us = v.us;
+  }
+  __syncthreads();
+
+  const RowInfo ri = rowinfo[b * nrows + row];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int ncell = d.n2 * d.n3;
+  const Real Hh2 = (Real)P.Hh2;
+  const Real* hp = Bulk<Real>::hpoly(P);
+  Real hc[5];
+#pragma unroll
+  for (int c = 0; c < 5; c++) hc[c] = hp[c];
+  const Real alpha = Bulk<Real>::alpha(P), beta = Bulk<Real>::beta(P);
+  const Real kr = Bulk<Real>::kr(P), km = Bulk<Real>::km(P);
+  Real rext[3], mext[3];
+#pragma unroll
+  for (int c = 0; c < 3; c++) {
+    rext[c] = Bulk<Real>::ray_ext(P, c);
+    mext[c] = Bulk<Real>::mie_ext(P, c);
+  }
+  const Real inv_steps = Real(1) / Real(S);
+  const double stepsize = 1.0 / S;
+  const Real rr = (Real)ri.r, D0 = (Real)ri.D[0], D1 = (Real)ri.D[1], D2 = (Real)ri.D[2];
+  const long long node0 = (b * nrows + row) * ncell;
+
+  for (int cell = warp; cell < ncell; cell += WARPS) {
+    const CellGeom<Real> g = geom[node0 + cell];
+    const Real b0 = rr * g.lx;  // x.l, x = (r, 0, 0)
+    const Real Dl = D0 * g.lx + D1 * g.ly + D2 * g.lz;
+    Real accR[3] = {0, 0, 0}, accM[3] = {0, 0, 0};
+    for (int s = lane; s < S; s += 32) {
+      const Real q = sm[s].q;
+      const Real bp = fma(sm[s].us, Dl, b0);  // p_s.l
+      if (sun_visible<Real>(P, d, ri, bp, q, cell, s)) {
+        // exit of the sun ray from the top sphere, cancellation-free
+        const Real ctop = q - Hh2;
+        const Real disc = fmax(bp * bp - ctop, Real(0));
+        const Real root = Bulk<Real>::sqrt(disc);
+        Real texit = bp >= Real(0) ? Bulk<Real>::div(-ctop, bp + root) : root - bp;
+        texit = fmax(texit, Real(0));
+        const Real dt = texit * inv_steps;
+        Real sr, smie;
+        optical_sums<Real, 5>(q, bp + bp, dt, S, hc, alpha, beta, kr, km, sr, smie);
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+          const Real tau = sm[s].tau[c] + dt * (rext[c] * sr + mext[c] * smie);
+          const Real T = exp_neg(tau);
+          accR[c] = fma(T, sm[s].er, accR[c]);
+          accM[c] = fma(T, sm[s].em, accM[c]);
+        }
+      }
+    }
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+      accR[c] = warp_sum(accR[c]);
+      accM[c] = warp_sum(accM[c]);
+    }
+    if (lane == 0) {
+      const Real wR = (Real)(ri.L * stepsize);
+      const Real phR = phase_cs<Real>((Real)P.ray_g, g.mu);
+      Vec4<Real> o1, o2;
+      o1.x = wR * phR * (Real)(P.intensity[0] * P.ray_base[0]) * accR[0];
+      o1.y = wR * phR * (Real)(P.intensity[1] * P.ray_base[1]) * accR[1];
+      o1.z = wR * phR * (Real)(P.intensity[2] * P.ray_base[2]) * accR[2];
+      o1.w = 0;
+      o2.x = wR * (Real)(P.intensity[0] * P.mie_base[0]) * accM[0];
+      o2.y = wR * (Real)(P.intensity[1] * P.mie_base[1]) * accM[1];
+      o2.z = wR * (Real)(P.intensity[2] * P.mie_base[2]) * accM[2];
+      o2.w = 0;
+      rayleigh[node0 + cell] = o1;
+      mie[node0 + cell] = o2;
+    }
+  }
+}
+
+template <class Real>
+void launch_first_order(const AtmoParams* params, const BuildDims& d, const RowInfo* rowinfo,
+                        const RowSample<Real>* rows, const CellGeom<Real>* geom, Vec4<Real>* rayleigh,
+                        Vec4<Real>* mie, cudaStream_t st) {
+  constexpr int WARPS = 8;
+  size_t smem = sizeof(FirstOrderSmem<Real>) * d.S;
+  dim3 grid((unsigned)d.rows(), d.B);
+  k_first_order<Real, WARPS><<<grid, WARPS * 32, smem, st>>>(params, d, rowinfo, rows, geom, rayleigh, mie);
+}
+
+template void launch_first_order<float>(const AtmoParams*, const BuildDims&, const RowInfo*,
+                                        const RowSample<float>*, const CellGeom<float>*, Vec4<float>*,
+                                        Vec4<float>*, cudaStream_t);
+template void launch_first_order<double>(const AtmoParams*, const BuildDims&, const RowInfo*,
+                                         const RowSample<double>*, const CellGeom<double>*, Vec4<double>*,
+                                         Vec4<double>*, cudaStream_t);
+
+// Work census of the first order: the number of (node, sample) pairs whose
+// sun is above the horizon, i.e. the sun-ray optical-depth integrals the
+// kernel above evaluates (each of S extinction samples).
+template <class Real>
+__global__ void k_first_order_census(const AtmoParams* params, BuildDims d, const RowInfo* rowinfo,
+                                     const RowSample<Real>* rows, const CellGeom<Real>* geom,
+                                     unsigned long long* count) {
+  const int b = blockIdx.y;
+  const long long row = blockIdx.x;
+  const long long nrows = d.rows();
+  const AtmoParams& P = params[b];
+  const RowInfo ri = rowinfo[b * nrows + row];
+  const RowSample<Real>* rs = rows + (b * nrows + row) * d.S;
+  const int ncell = d.n2 * d.n3;
+  const long long node0 = (b * nrows + row) * ncell;
+  unsigned long long local = 0;
+  for (long long t = threadIdx.x; t < (long long)ncell * d.S; t += blockDim.x) {
+    const int cell = (int)(t / d.S), s = (int)(t % d.S);
+    const CellGeom<Real> g = geom[node0 + cell];
+    const Real Dl = (Real)ri.D[0] * g.lx + (Real)ri.D[1] * g.ly + (Real)ri.D[2] * g.lz;
+    const Real bp = fma(rs[s].us, Dl, (Real)ri.r * g.lx);
+    local += sun_visible<Real>(P, d, ri, bp, rs[s].q, cell, s) ? 1 : 0;
+  }
+  for (int o = 16; o > 0; o >>= 1) local += __shfl_xor_sync(0xffffffffu, local, o);
+  if ((threadIdx.x & 31) == 0) atomicAdd(count, local);
+}
+
+template <class Real>
+void launch_first_order_census(const AtmoParams* params, const BuildDims& d, const RowInfo* rowinfo,
+                               const RowSample<Real>* rows, const CellGeom<Real>* geom, unsigned long long* count,
+                               cudaStream_t st) {
+  dim3 grid((unsigned)d.rows(), d.B);
+  k_first_order_census<Real><<<grid, 256, 0, st>>>(params, d, rowinfo, rows, geom, count);
+}
+
+template void launch_first_order_census<float>(const AtmoParams*, const BuildDims&, const RowInfo*,
+                                               const RowSample<float>*, const CellGeom<float>*,
+                                               unsigned long long*, cudaStream_t);
+template void launch_first_order_census<double>(const AtmoParams*, const BuildDims&, const RowInfo*,
+                                                const RowSample<double>*, const CellGeom<double>*,
+                                                unsigned long long*, cudaStream_t);
+
+}  // namespace sfsim

@@ -1,0 +1,612 @@
+// k_scatter.cu -- multiple-scattering passes of the atmosphere LUT build
+// (atmosphere_lut.clj:86-97): point scatter J, surface radiance dE, ray
+// scatter dS, and the re-interpolating accumulation of E and S.
+#include "atmo_device.cuh"
+#include "kernels.h"
+
+namespace sfsim {
+
+// Index of a 4-D texel.
+__device__ __forceinline__ long long idx4(const BuildDims& d, int i, int j, int k, int a) {
+  return (((long long)i * d.n1 + j) * d.n2 + k) * d.n3 + a;
+}
+
+template <class Real>
+__device__ __forceinline__ void ld3(const Vec4<Real>* t, long long i, Real o[3]) {
+  Vec4<Real> v = t[i];
+  o[0] = v.x;
+  o[1] = v.y;
+  o[2] = v.z;
+}
+
+template <class Real>
+__device__ __forceinline__ void mix3(const Real* a, const Real* b, Real s, Real* o) {
+#pragma unroll
+  for (int c = 0; c < 3; c++) o[c] = a[c] * (Real(1) - s) + b[c] * s;
+}
+
+// Clamped quadrilinear interpolation of a 4-D table (interpolate.clj:87-98:
+// the innermost dimension is mixed first).
+template <class Real>
+__device__ inline void interp4(const Vec4<Real>* t, const BuildDims& d, const int* u, const Real* s, Real out[3]) {
+  const int v[4] = {upper_index(u[0], d.n0), upper_index(u[1], d.n1), upper_index(u[2], d.n2),
+                    upper_index(u[3], d.n3)};
+  Real rh[2][3];
+#pragma unroll
+  for (int h = 0; h < 2; h++) {
+    Real re[2][3];
+#pragma unroll
+    for (int e = 0; e < 2; e++) {
+      Real rk[2][3];
+#pragma unroll
+      for (int k = 0; k < 2; k++) {
+        Real A[3], B[3];
+        const int ih = h ? v[0] : u[0], ie = e ? v[1] : u[1], ik = k ? v[2] : u[2];
+        ld3(t, idx4(d, ih, ie, ik, u[3]), A);
+        ld3(t, idx4(d, ih, ie, ik, v[3]), B);
+        mix3(A, B, s[3], rk[k]);
+      }
+      mix3(rk[0], rk[1], s[2], re[e]);
+    }
+    mix3(re[0], re[1], s[1], rh[h]);
+  }
+  mix3(rh[0], rh[1], s[0], out);
+}
+
+template <class Real>
+__device__ inline void interp2(const Vec4<Real>* t, int n0, int n1, const int* u, const Real* s, Real out[3]) {
+  const int v0 = upper_index(u[0], n0), v1 = upper_index(u[1], n1);
+  Real A[3], B[3], lo[3], hi[3];
+  ld3(t, (long long)u[0] * n1 + u[1], A);
+  ld3(t, (long long)u[0] * n1 + v1, B);
+  mix3(A, B, s[1], lo);
+  ld3(t, (long long)v0 * n1 + u[1], A);
+  ld3(t, (long long)v0 * n1 + v1, B);
+  mix3(A, B, s[1], hi);
+  mix3(lo, hi, s[0], out);
+}
+
+// (1 - exp(-3 s - 0.6)) / (1 - exp(-3.6)) clamped at 0, times (size - 1)
+// (sun-elevation-to-index, atmosphere.clj:322-326) in Real.
+template <class Real>
+__device__ __forceinline__ Real sun_elevation_index_r(Real sin_el, Real scale) {
+  const Real e = Bulk<Real>::exp2((Real(3) * sin_el + Real(0.6)) * Real(-1.4426950408889634));
+  const Real r = (Real(1) - e) * scale;
+  return r > Real(0) ? r : Real(0);
+}
+
+// ---------------------------------------------------------------------------
+// Point scatter J (atmosphere.clj:203-222) for all nodes of one (height i,
+// sun elevation k) pair.  For such a pair the dS lookups of every direction
+// share the height coordinate (x is fixed) and the sun-elevation coordinate
+// (x.l/|x| = sin of the sun elevation), so the block first collapses those two
+// dimensions of dS into a 2-D slab [elevation][heading] in shared memory and
+// each direction then needs a bilinear gather from the slab.  The ground term
+// reads the whole dE table, also staged in shared memory.  One thread per
+// node (elevation j, heading a); the directions come from k_sphere_setup.
+// ---------------------------------------------------------------------------
+
+template <class Real, bool FIRST>
+__global__ void __launch_bounds__(256) k_point_scatter(const AtmoParams* params, BuildDims d, const RowInfo* rowinfo,
+                                                       const SphereDir<Real>* sdirs, const CellGeom<Real>* geom,
+                                                       const Vec4<Real>* dS, const Vec4<Real>* Mt,
+                                                       const Vec4<Real>* dE, Vec4<Real>* J, int nchunks) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int b = blockIdx.y;
+  const int chunk = blockIdx.x % nchunks;
+  const int ik = blockIdx.x / nchunks;
+  const int i = ik / d.n2, k = ik % d.n2;
+  const AtmoParams& P = params[b];
+  const int nslab = d.n1 * d.n3;
+  SphereDir<Real>* dirs = reinterpret_cast<SphereDir<Real>*>(smem_raw);
+  Real* slab = reinterpret_cast<Real*>(dirs + d.P);
+  Real* slabM = slab + 3 * nslab;
+  Real* etab = slabM + (FIRST ? 3 * nslab : 0);
+
+  // the (i, k) coordinates, FP64 as in ray-scatter-forward
+  const double r = index_to_radius(P, d.n0, (double)i);
+  const double ss = index_to_sin_sun_elevation(d.n2, (double)k);
+  int u0, u2;
+  Real s0, s2;
+  split_coord<Real>(height_to_index(P, d.n0, r), d.n0, &u0, &s0);
+  split_coord<Real>(sun_elevation_to_index(d.n2, mk3(r, 0, 0), mk3(ss, 0, 0)), d.n2, &u2, &s2);
+  const int v0 = upper_index(u0, d.n0), v2 = upper_index(u2, d.n2);
+
+  const long long base4 = (long long)b * d.n4();
+  for (int t = threadIdx.x; t < nslab; t += blockDim.x) {
+    const int j = t / d.n3, a = t % d.n3;
+    Real A[3], B[3], lo[3], hi[3], o[3];
+    ld3(dS, base4 + idx4(d, u0, j, u2, a), A);
+    ld3(dS, base4 + idx4(d, u0, j, v2, a), B);
+    mix3(A, B, s2, lo);
+    ld3(dS, base4 + idx4(d, v0, j, u2, a), A);
+    ld3(dS, base4 + idx4(d, v0, j, v2, a), B);
+    mix3(A, B, s2, hi);
+    mix3(lo, hi, s0, o);
+    slab[3 * t] = o[0];
+    slab[3 * t + 1] = o[1];
+    slab[3 * t + 2] = o[2];
+    if (FIRST) {
+      ld3(Mt, base4 + idx4(d, u0, j, u2, a), A);
+      ld3(Mt, base4 + idx4(d, u0, j, v2, a), B);
+      mix3(A, B, s2, lo);
+      ld3(Mt, base4 + idx4(d, v0, j, u2, a), A);
+      ld3(Mt, base4 + idx4(d, v0, j, v2, a), B);
+      mix3(A, B, s2, hi);
+      mix3(lo, hi, s0, o);
+      slabM[3 * t] = o[0];
+      slabM[3 * t + 1] = o[1];
+      slabM[3 * t + 2] = o[2];
+    }
+  }
+  const long long nE = d.nE();
+  for (int t = threadIdx.x; t < nE; t += blockDim.x) {
+    Real A[3];
+    ld3(dE, b * nE + t, A);
+    etab[3 * t] = A[0];
+    etab[3 * t + 1] = A[1];
+    etab[3 * t + 2] = A[2];
+  }
+  const SphereDir<Real>* src = sdirs + ((long long)b * d.n0 + i) * d.P;
+  for (int t = threadIdx.x; t < d.P; t += blockDim.x) dirs[t] = src[t];
+  __syncthreads();
+
+  const int cell = chunk * blockDim.x + threadIdx.x;
+  if (cell >= nslab) return;
+  const int j = cell / d.n3, a = cell % d.n3;
+  const RowInfo ri = rowinfo[(long long)b * d.rows() + (long long)i * d.n1 + j];
+  const Real sv = (Real)ri.sv, cv = (Real)ri.cv;
+  const long long node = base4 + idx4(d, i, j, k, a);
+  const CellGeom<Real> g = geom[node];
+  const Real gR = (Real)P.ray_g, gM = (Real)P.mie_g;
+  const Real scale3 = Real(0.5) * Real(d.n3 - 1);
+  const Real scaleE = (Real)((d.nE1 - 1) / (1 - exp(-3.6)));
+
+  Real accR[3] = {0, 0, 0}, accM[3] = {0, 0, 0}, cR[3] = {0, 0, 0}, cM[3] = {0, 0, 0};
+  Real ringR[3] = {0, 0, 0}, ringM[3] = {0, 0, 0};
+  for (int w = 0; w < d.P; w++) {
+    const SphereDir<Real>& D = dirs[w];
+    const Real mu_v = sv * D.w[0] + cv * D.w[1];
+    const Real mu_l = D.w[0] * g.lx + D.w[1] * g.ly + D.w[2] * g.lz;
+    // sun-angle coordinate of (omega, l)
+    int u3;
+    Real s3;
+    split_coord_r<Real>(scale3 * (Real(1) + mu_l), d.n3, &u3, &s3);
+    const int v3 = upper_index(u3, d.n3);
+    const int u1 = D.u1, v1 = upper_index(D.u1, d.n1);
+    Real X[3];
+    {
+      const Real* p00 = slab + 3 * (u1 * d.n3 + u3);
+      const Real* p01 = slab + 3 * (u1 * d.n3 + v3);
+      const Real* p10 = slab + 3 * (v1 * d.n3 + u3);
+      const Real* p11 = slab + 3 * (v1 * d.n3 + v3);
+      mix4(p00, p01, p10, p11, D.s1, s3, X);
+    }
+    if (FIRST) {
+      Real Y[3];
+      const Real* p00 = slabM + 3 * (u1 * d.n3 + u3);
+      const Real* p01 = slabM + 3 * (u1 * d.n3 + v3);
+      const Real* p10 = slabM + 3 * (v1 * d.n3 + u3);
+      const Real* p11 = slabM + 3 * (v1 * d.n3 + v3);
+      mix4(p00, p01, p10, p11, D.s1, s3, Y);
+      const Real ph = phase_cs<Real>(gM, mu_l);
+#pragma unroll
+      for (int c = 0; c < 3; c++) X[c] = fma(Y[c], ph, X[c]);
+    }
+    if (D.surface) {
+      const Real sg = D.gdir[0] * g.lx + D.gdir[1] * g.ly + D.gdir[2] * g.lz;
+      int uE1;
+      Real sE1;
+      split_coord_r<Real>(sun_elevation_index_r<Real>(sg, scaleE), d.nE1, &uE1, &sE1);
+      const int vE1 = upper_index(uE1, d.nE1), vE0 = upper_index(D.uE0, d.nE0);
+      Real Y[3];
+      mix4(etab + 3 * (D.uE0 * d.nE1 + uE1), etab + 3 * (D.uE0 * d.nE1 + vE1), etab + 3 * (vE0 * d.nE1 + uE1),
+           etab + 3 * (vE0 * d.nE1 + vE1), D.sE0, sE1, Y);
+#pragma unroll
+      for (int c = 0; c < 3; c++) X[c] = fma(D.ground[c], Y[c], X[c]);
+    }
+    const Real wR = D.weight * phase_cs<Real>(gR, mu_v);
+    const Real wM = D.weight * phase_cs<Real>(gM, mu_v);
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+      ringR[c] = fma(wR, X[c], ringR[c]);
+      ringM[c] = fma(wM, X[c], ringM[c]);
+    }
+    if (D.pad) {  // last direction of a theta ring
+#pragma unroll
+      for (int c = 0; c < 3; c++) {
+        kahan_add(accR[c], cR[c], ringR[c]);
+        kahan_add(accM[c], cM[c], ringM[c]);
+        ringR[c] = 0;
+        ringM[c] = 0;
+      }
+    }
+  }
+  // beta_c(x) (atmosphere.clj:42-47, 140-151)
+  const double h = r - P.R;
+  const double er = exp(-(h / P.ray_scale)), em = exp(-(h / P.mie_scale));
+  Vec4<Real> o;
+  o.x = (Real)(P.ray_base[0] * er) * accR[0] + (Real)(P.mie_base[0] * em) * accM[0];
+  o.y = (Real)(P.ray_base[1] * er) * accR[1] + (Real)(P.mie_base[1] * em) * accM[1];
+  o.z = (Real)(P.ray_base[2] * er) * accR[2] + (Real)(P.mie_base[2] * em) * accM[2];
+  o.w = 0;
+  J[node] = o;
+}
+
+template <class Real>
+size_t point_scatter_smem(const BuildDims& d, bool first) {
+  return sizeof(SphereDir<Real>) * d.P + sizeof(Real) * 3 * ((size_t)d.n1 * d.n3 * (first ? 2 : 1) + d.nE());
+}
+
+template <class Real>
+int launch_point_scatter(const AtmoParams* params, const BuildDims& d, const RowInfo* rowinfo,
+                         const SphereDir<Real>* sdirs, const CellGeom<Real>* geom, const Vec4<Real>* dS,
+                         const Vec4<Real>* mie, const Vec4<Real>* dE, Vec4<Real>* J, cudaStream_t st) {
+  const int block = 256;
+  const int nchunks = (d.n1 * d.n3 + block - 1) / block;
+  const bool first = mie != nullptr;
+  size_t smem = point_scatter_smem<Real>(d, first);
+  dim3 grid((unsigned)(d.n0 * d.n2 * nchunks), d.B);
+  if (first) {
+    if (cudaFuncSetAttribute(k_point_scatter<Real, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+        cudaSuccess)
+      return -1;
+    k_point_scatter<Real, true><<<grid, block, smem, st>>>(params, d, rowinfo, sdirs, geom, dS, mie, dE, J, nchunks);
+  } else {
+    if (cudaFuncSetAttribute(k_point_scatter<Real, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)smem) != cudaSuccess)
+      return -1;
+    k_point_scatter<Real, false><<<grid, block, smem, st>>>(params, d, rowinfo, sdirs, geom, dS, mie, dE, J,
+                                                            nchunks);
+  }
+  return 0;
+}
+
+// ---------------------------------------------------------------------------
+// Surface radiance dE (atmosphere.clj:225-230): integral over the upper half
+// sphere of dS(x, w, l, above) (w.n); the reference passes the ray steps as
+// the sphere steps (atmosphere_lut.clj:89).  One block per node, threads over
+// directions, FP64 coordinates (the work is small), block reduction.
+// ---------------------------------------------------------------------------
+
+template <class Real, bool FIRST>
+__global__ void __launch_bounds__(256) k_surface_radiance(const AtmoParams* params, BuildDims d,
+                                                          const DirLocal* hdirs, const Vec4<Real>* dS,
+                                                          const Vec4<Real>* Mt, Vec4<Real>* dE) {
+  __shared__ Real red[3][256];
+  const int b = blockIdx.y;
+  const long long node = blockIdx.x;
+  const AtmoParams& P = params[b];
+  const int iE = (int)(node / d.nE1), kE = (int)(node % d.nE1);
+  const double r = index_to_radius(P, d.nE0, (double)iE);
+  const double ss = index_to_sin_sun_elevation(d.nE1, (double)kE);
+  const d3 x = mk3(r, 0, 0), l = mk3(ss, sqrt(dmax(0.0, 1 - sqr(ss))), 0);
+  const d3 n = mul3(x, 1.0 / mag3(x));
+  const d3 o1 = orthogonal(n);
+  const d3 o2 = cross3(n, o1);
+  int u[4];
+  Real s[4];
+  split_coord<Real>(height_to_index(P, d.n0, mag3(x)), d.n0, &u[0], &s[0]);
+  split_coord<Real>(sun_elevation_to_index(d.n2, x, l), d.n2, &u[2], &s[2]);
+  const Vec4<Real>* tS = dS + (long long)b * d.n4();
+  const Vec4<Real>* tM = FIRST ? Mt + (long long)b * d.n4() : nullptr;
+  Real acc[3] = {0, 0, 0}, cmp[3] = {0, 0, 0};
+  for (int w = threadIdx.x; w < d.Ph; w += blockDim.x) {
+    const DirLocal q = hdirs[w];
+    const d3 omega = to_world(n, o1, o2, q);
+    int uu[4] = {u[0], 0, u[2], 0};
+    Real sx[4] = {s[0], 0, s[2], 0};
+    split_coord<Real>(elevation_to_index(P, d.n1, x, omega, 1), d.n1, &uu[1], &sx[1]);
+    split_coord<Real>(sun_angle_to_index(d.n3, omega, l), d.n3, &uu[3], &sx[3]);
+    Real val[3];
+    interp4(tS, d, uu, sx, val);
+    if (FIRST) {
+      Real vm[3];
+      interp4(tM, d, uu, sx, vm);
+      const Real ph = phase_cs<Real>((Real)P.mie_g, (Real)dot3(omega, l));
+#pragma unroll
+      for (int c = 0; c < 3; c++) val[c] = fma(vm[c], ph, val[c]);
+    }
+    const Real wgt = (Real)(q.w * dot3(omega, n));
+#pragma unroll
+    for (int c = 0; c < 3; c++) kahan_add(acc[c], cmp[c], val[c] * wgt);
+  }
+#pragma unroll
+  for (int c = 0; c < 3; c++) red[c][threadIdx.x] = acc[c];
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o) {
+#pragma unroll
+      for (int c = 0; c < 3; c++) red[c][threadIdx.x] += red[c][threadIdx.x + o];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    Vec4<Real> o;
+    o.x = red[0][0];
+    o.y = red[1][0];
+    o.z = red[2][0];
+    o.w = 0;
+    dE[(long long)b * d.nE() + node] = o;
+  }
+}
+
+template <class Real>
+void launch_surface_radiance(const AtmoParams* params, const BuildDims& d, const DirLocal* half_dirs,
+                             const Vec4<Real>* dS, const Vec4<Real>* mie, Vec4<Real>* dE, cudaStream_t st) {
+  dim3 grid((unsigned)d.nE(), d.B);
+  if (mie)
+    k_surface_radiance<Real, true><<<grid, 256, 0, st>>>(params, d, half_dirs, dS, mie, dE);
+  else
+    k_surface_radiance<Real, false><<<grid, 256, 0, st>>>(params, d, half_dirs, dS, mie, dE);
+}
+
+// ---------------------------------------------------------------------------
+// Ray scatter dS (atmosphere.clj:192-200) with J from the point-scatter table.
+// One block per view row (i, j); one thread per node (sun elevation k, sun
+// heading a).  For a ray sample p_s the J lookup's height and elevation
+// coordinates depend on the row only, so the block collapses them into a
+// plane [sun elevation][heading] per sample in shared memory; each node then
+// gathers bilinearly from the plane at its own sun-elevation coordinate
+// (from p_s.l) and sun-angle coordinate (v.l, constant along the ray).
+// T(x, p_s) comes from k_view_rows.
+// ---------------------------------------------------------------------------
+
+template <class Real>
+struct RaySample {
+  Real T[3];
+  Real us, inv_r;
+};
+
+template <class Real, int CH>
+__global__ void __launch_bounds__(256) k_ray_scatter(const AtmoParams* params, BuildDims d, const RowInfo* rowinfo,
+                                                     const RowSample<Real>* rows, const CellGeom<Real>* geom,
+                                                     const Remap4<Real>* remap, const Vec4<Real>* J,
+                                                     Vec4<Real>* dS) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int b = blockIdx.y;
+  const long long row = blockIdx.x;
+  const long long nrows = d.rows();
+  const int ncell = d.n2 * d.n3;
+  RaySample<Real>* smp = reinterpret_cast<RaySample<Real>*>(smem_raw);
+  Real* plane = reinterpret_cast<Real*>(smp + CH);
+  const RowSample<Real>* rs = rows + (b * nrows + row) * d.S;
+  const RowInfo ri = rowinfo[b * nrows + row];
+  const Vec4<Real>* tJ = J + (long long)b * d.n4();
+  const long long node0 = (b * nrows + row) * ncell;
+  const Real scale2 = (Real)((d.n2 - 1) / (1 - exp(-3.6)));
+  const Real rr = (Real)ri.r, D0 = (Real)ri.D[0], D1 = (Real)ri.D[1], D2 = (Real)ri.D[2];
+
+  for (int c0 = 0; c0 < ncell; c0 += blockDim.x) {
+    const int cell = c0 + threadIdx.x;
+    const bool active = cell < ncell;
+    Real b0 = 0, Dl = 0, s3 = 0;
+    int u3 = 0, v3 = 0;
+    if (active) {
+      const CellGeom<Real> g = geom[node0 + cell];
+      b0 = rr * g.lx;
+      Dl = D0 * g.lx + D1 * g.ly + D2 * g.lz;
+      const Remap4<Real> m = remap[node0 + cell];  // its sun-angle coordinate is that of (v, l)
+      u3 = m.u[3];
+      s3 = m.s[3];
+      v3 = upper_index(u3, d.n3);
+    }
+    Real acc[3] = {0, 0, 0}, cmp[3] = {0, 0, 0};
+    for (int sb = 0; sb < d.S; sb += CH) {
+      const int nch = min(CH, d.S - sb);
+      __syncthreads();
+      for (int t = threadIdx.x; t < nch * ncell; t += blockDim.x) {
+        const int ch = t / ncell, kk = (t % ncell) / d.n3, aa = t % d.n3;
+        const RowSample<Real>& q = rs[sb + ch];
+        const int u0 = q.u0, v0 = upper_index(q.u0, d.n0), u1 = q.u1, v1 = upper_index(q.u1, d.n1);
+        Real A[3], B[3], lo[3], hi[3], o[3];
+        ld3(tJ, idx4(d, u0, u1, kk, aa), A);
+        ld3(tJ, idx4(d, u0, v1, kk, aa), B);
+        mix3(A, B, q.s1, lo);
+        ld3(tJ, idx4(d, v0, u1, kk, aa), A);
+        ld3(tJ, idx4(d, v0, v1, kk, aa), B);
+        mix3(A, B, q.s1, hi);
+        mix3(lo, hi, q.s0, o);
+        Real* dst = plane + 3 * ((long long)ch * ncell + kk * d.n3 + aa);
+        dst[0] = o[0];
+        dst[1] = o[1];
+        dst[2] = o[2];
+      }
+      if (threadIdx.x < nch) {
+        const RowSample<Real>& q = rs[sb + threadIdx.x];
+        RaySample<Real> v;
+        v.T[0] = exp_neg(q.tau[0]);
+        v.T[1] = exp_neg(q.tau[1]);
+        v.T[2] = exp_neg(q.tau[2]);
+        v.us = q.us;
+        v.inv_r = q.inv_r;
+        smp[threadIdx.x] = v;
+      }
+      __syncthreads();
+      if (active) {
+        for (int ch = 0; ch < nch; ch++) {
+          const RaySample<Real> v = smp[ch];
+          const Real sin_el = fma(v.us, Dl, b0) * v.inv_r;  // p_s.l / |p_s|
+          int u2;
+          Real s2;
+          split_coord_r<Real>(sun_elevation_index_r<Real>(sin_el, scale2), d.n2, &u2, &s2);
+          const int v2 = upper_index(u2, d.n2);
+          const Real* pl = plane + 3 * (long long)ch * ncell;
+          Real X[3];
+          mix4(pl + 3 * (u2 * d.n3 + u3), pl + 3 * (u2 * d.n3 + v3), pl + 3 * (v2 * d.n3 + u3),
+               pl + 3 * (v2 * d.n3 + v3), s2, s3, X);
+#pragma unroll
+          for (int c = 0; c < 3; c++) kahan_add(acc[c], cmp[c], v.T[c] * X[c]);
+        }
+      }
+    }
+    if (active) {
+      const Real w = (Real)(ri.L / d.S);
+      Vec4<Real> o;
+      o.x = w * acc[0];
+      o.y = w * acc[1];
+      o.z = w * acc[2];
+      o.w = 0;
+      dS[node0 + cell] = o;
+    }
+  }
+}
+
+template <class Real>
+int launch_ray_scatter(const AtmoParams* params, const BuildDims& d, const RowInfo* rowinfo,
+                       const RowSample<Real>* rows, const CellGeom<Real>* geom, const Remap4<Real>* remap,
+                       const Vec4<Real>* J, Vec4<Real>* dS, cudaStream_t st) {
+  constexpr int CH = 8;
+  const int ncell = d.n2 * d.n3;
+  const int block = ncell >= 256 ? 256 : ((ncell + 31) / 32) * 32;
+  size_t smem = sizeof(RaySample<Real>) * CH + sizeof(Real) * 3 * (size_t)CH * ncell;
+  if (cudaFuncSetAttribute(k_ray_scatter<Real, CH>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+      cudaSuccess)
+    return -1;
+  dim3 grid((unsigned)d.rows(), d.B);
+  k_ray_scatter<Real, CH><<<grid, block, smem, st>>>(params, d, rowinfo, rows, geom, remap, J, dS);
+  return 0;
+}
+
+// ---------------------------------------------------------------------------
+// Re-interpolating accumulation and outputs
+// ---------------------------------------------------------------------------
+
+template <class Real>
+__global__ void k_accumulate4(BuildDims d, const Remap4<Real>* remap, const Vec4<Real>* A, const Vec4<Real>* Bt,
+                              Vec4<Real>* out) {
+  const long long n4 = d.n4();
+  const long long node = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  const int b = blockIdx.y;
+  if (node >= n4) return;
+  const Remap4<Real> m = remap[b * n4 + node];
+  Real va[3], vb[3] = {0, 0, 0};
+  interp4(A + b * n4, d, m.u, m.s, va);
+  if (Bt) interp4(Bt + b * n4, d, m.u, m.s, vb);
+  Vec4<Real> o;
+  o.x = va[0] + vb[0];
+  o.y = va[1] + vb[1];
+  o.z = va[2] + vb[2];
+  o.w = 0;
+  out[b * n4 + node] = o;
+}
+
+template <class Real>
+__global__ void k_accumulate2(int n0, int n1, const Remap2<Real>* remap, const Vec4<Real>* A, const Vec4<Real>* Bt,
+                              Vec4<Real>* out) {
+  const long long n = (long long)n0 * n1;
+  const long long node = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  const int b = blockIdx.y;
+  if (node >= n) return;
+  const Remap2<Real> m = remap[b * n + node];
+  Real va[3] = {0, 0, 0}, vb[3] = {0, 0, 0};
+  if (A) interp2(A + b * n, n0, n1, m.u, m.s, va);
+  if (Bt) interp2(Bt + b * n, n0, n1, m.u, m.s, vb);
+  Vec4<Real> o;
+  o.x = va[0] + vb[0];
+  o.y = va[1] + vb[1];
+  o.z = va[2] + vb[2];
+  o.w = 0;
+  out[b * n + node] = o;
+}
+
+// convert-4d-to-2d (image.clj:299-312) + pack-matrices (matrix.clj:130-134)
+template <class Real>
+__global__ void k_output4(BuildDims d, const Remap4<Real>* remap, const Vec4<Real>* tab, float* out) {
+  const long long n4 = d.n4();
+  const long long node = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  const int b = blockIdx.y;
+  if (node >= n4) return;
+  const Remap4<Real> m = remap[b * n4 + node];
+  Real v[3];
+  interp4(tab + b * n4, d, m.u, m.s, v);
+  const int a = (int)(node % d.n3);
+  const int k = (int)((node / d.n3) % d.n2);
+  const int j = (int)((node / ((long long)d.n3 * d.n2)) % d.n1);
+  const int i = (int)(node / ((long long)d.n3 * d.n2 * d.n1));
+  const long long dst = ((long long)i * d.n2 + k) * ((long long)d.n1 * d.n3) + (long long)j * d.n3 + a;
+  float* o = out + 3 * (b * n4 + dst);
+  o[0] = (float)v[0];
+  o[1] = (float)v[1];
+  o[2] = (float)v[2];
+}
+
+template <class Real>
+__global__ void k_output2(int n0, int n1, const Remap2<Real>* remap, const Vec4<Real>* tab, float* out) {
+  const long long n = (long long)n0 * n1;
+  const long long node = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  const int b = blockIdx.y;
+  if (node >= n) return;
+  const Remap2<Real> m = remap[b * n + node];
+  Real v[3] = {0, 0, 0};
+  if (tab) interp2(tab + b * n, n0, n1, m.u, m.s, v);
+  float* o = out + 3 * (b * n + node);
+  o[0] = (float)v[0];
+  o[1] = (float)v[1];
+  o[2] = (float)v[2];
+}
+
+template <class Real>
+__global__ void k_export(long long n, const Vec4<Real>* tab, float* out) {
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  const Vec4<Real> v = tab[t];
+  out[3 * t] = (float)v.x;
+  out[3 * t + 1] = (float)v.y;
+  out[3 * t + 2] = (float)v.z;
+}
+
+static inline dim3 grid1(long long n, int block, int B) { return dim3((unsigned)((n + block - 1) / block), B); }
+
+template <class Real>
+void launch_accumulate4(const BuildDims& d, const Remap4<Real>* remap, const Vec4<Real>* a, const Vec4<Real>* b,
+                        Vec4<Real>* out, cudaStream_t st) {
+  k_accumulate4<Real><<<grid1(d.n4(), 256, d.B), 256, 0, st>>>(d, remap, a, b, out);
+}
+
+template <class Real>
+void launch_accumulate2(int B, int n0, int n1, const Remap2<Real>* remap, const Vec4<Real>* a, const Vec4<Real>* b,
+                        Vec4<Real>* out, cudaStream_t st) {
+  k_accumulate2<Real><<<grid1((long long)n0 * n1, 256, B), 256, 0, st>>>(n0, n1, remap, a, b, out);
+}
+
+template <class Real>
+void launch_output4(const BuildDims& d, const Remap4<Real>* remap, const Vec4<Real>* tab, float* out,
+                    cudaStream_t st) {
+  k_output4<Real><<<grid1(d.n4(), 256, d.B), 256, 0, st>>>(d, remap, tab, out);
+}
+
+template <class Real>
+void launch_output2(int B, int n0, int n1, const Remap2<Real>* remap, const Vec4<Real>* tab, float* out,
+                    cudaStream_t st) {
+  k_output2<Real><<<grid1((long long)n0 * n1, 256, B), 256, 0, st>>>(n0, n1, remap, tab, out);
+}
+
+template <class Real>
+void launch_export(long long n, const Vec4<Real>* tab, float* out, cudaStream_t st) {
+  k_export<Real><<<grid1(n, 256, 1), 256, 0, st>>>(n, tab, out);
+}
+
+#define SFSIM_INSTANTIATE(Real)                                                                                     \
+  template int launch_point_scatter<Real>(const AtmoParams*, const BuildDims&, const RowInfo*,                     \
+                                          const SphereDir<Real>*, const CellGeom<Real>*, const Vec4<Real>*,        \
+                                          const Vec4<Real>*, const Vec4<Real>*, Vec4<Real>*, cudaStream_t);        \
+  template void launch_surface_radiance<Real>(const AtmoParams*, const BuildDims&, const DirLocal*,                \
+                                              const Vec4<Real>*, const Vec4<Real>*, Vec4<Real>*, cudaStream_t);    \
+  template int launch_ray_scatter<Real>(const AtmoParams*, const BuildDims&, const RowInfo*, const RowSample<Real>*, \
+                                        const CellGeom<Real>*, const Remap4<Real>*, const Vec4<Real>*,             \
+                                        Vec4<Real>*, cudaStream_t);                                                \
+  template void launch_accumulate4<Real>(const BuildDims&, const Remap4<Real>*, const Vec4<Real>*,                 \
+                                         const Vec4<Real>*, Vec4<Real>*, cudaStream_t);                            \
+  template void launch_accumulate2<Real>(int, int, int, const Remap2<Real>*, const Vec4<Real>*, const Vec4<Real>*, \
+                                         Vec4<Real>*, cudaStream_t);                                               \
+  template void launch_output4<Real>(const BuildDims&, const Remap4<Real>*, const Vec4<Real>*, float*,             \
+                                     cudaStream_t);                                                                \
+  template void launch_output2<Real>(int, int, int, const Remap2<Real>*, const Vec4<Real>*, float*, cudaStream_t);  \
+  template void launch_export<Real>(long long, const Vec4<Real>*, float*, cudaStream_t);                           \
+  template size_t point_scatter_smem<Real>(const BuildDims&, bool);
+
+SFSIM_INSTANTIATE(float)
+SFSIM_INSTANTIATE(double)
+
+}  // namespace sfsim

@@ -1,0 +1,287 @@
+// k_setup.cu -- node maps, transmittance and surface-base tables, per-row ray
+// samples and per-height sphere directions of the atmosphere LUT build.
+#include "atmo_device.cuh"
+#include "kernels.h"
+
+namespace sfsim {
+
+// ---------------------------------------------------------------------------
+// Re-interpolation maps.  Every table that the reference writes is
+// make-lookup-table of an interpolated function, so each node's value is the
+// table interpolated at forward(backward(node)) (interpolate.clj:68-110,
+// atmosphere_lut.clj:94-101).  These kernels store that coordinate per node.
+// ---------------------------------------------------------------------------
+
+template <class Real>
+__global__ void k_remap4(const AtmoParams* params, BuildDims d, Remap4<Real>* out, CellGeom<Real>* geom) {
+  const long long n4 = d.n4();
+  const long long node = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  const int b = blockIdx.y;
+  if (node >= n4) return;
+  const AtmoParams& P = params[b];
+  int a = (int)(node % d.n3);
+  int k = (int)((node / d.n3) % d.n2);
+  int j = (int)((node / ((long long)d.n3 * d.n2)) % d.n1);
+  int i = (int)(node / ((long long)d.n3 * d.n2 * d.n1));
+  double r, sv, cv;
+  int above;
+  view_geometry(P, d, i, j, &r, &sv, &cv, &above);
+  d3 x = mk3(r, 0, 0), v = mk3(sv, cv, 0);
+  d3 l = light_direction(d, sv, cv, k, a);
+  Remap4<Real> m;
+  split_coord<Real>(height_to_index(P, d.n0, mag3(x)), d.n0, &m.u[0], &m.s[0]);
+  split_coord<Real>(elevation_to_index(P, d.n1, x, v, above), d.n1, &m.u[1], &m.s[1]);
+  split_coord<Real>(sun_elevation_to_index(d.n2, x, l), d.n2, &m.u[2], &m.s[2]);
+  split_coord<Real>(sun_angle_to_index(d.n3, v, l), d.n3, &m.u[3], &m.s[3]);
+  out[b * n4 + node] = m;
+  CellGeom<Real> g;
+  g.lx = (Real)l.x;
+  g.ly = (Real)l.y;
+  g.lz = (Real)l.z;
+  g.mu = (Real)dot3(v, l);
+  geom[b * n4 + node] = g;
+}
+
+template <class Real>
+__global__ void k_remapT(const AtmoParams* params, BuildDims d, Remap2<Real>* out) {
+  const long long n = d.nT();
+  const long long node = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  const int b = blockIdx.y;
+  if (node >= n) return;
+  const AtmoParams& P = params[b];
+  int j = (int)(node % d.nT1), i = (int)(node / d.nT1);
+  double r = index_to_radius(P, d.nT0, (double)i), sv, cv;
+  int above;
+  index_to_elevation(P, d.nT1, r, (double)j, &sv, &cv, &above);
+  d3 x = mk3(r, 0, 0), v = mk3(sv, cv, 0);
+  Remap2<Real> m;
+  split_coord<Real>(height_to_index(P, d.nT0, mag3(x)), d.nT0, &m.u[0], &m.s[0]);
+  split_coord<Real>(elevation_to_index(P, d.nT1, x, v, above), d.nT1, &m.u[1], &m.s[1]);
+  out[b * n + node] = m;
+}
+
+__host__ __device__ inline void surface_node(const AtmoParams& P, const BuildDims& d, int i, int k, d3* x, d3* l) {
+  double r = index_to_radius(P, d.nE0, (double)i);
+  double s = index_to_sin_sun_elevation(d.nE1, (double)k);
+  double c = sqrt(dmax(0.0, 1 - sqr(s)));
+  *x = mk3(r, 0, 0);
+  *l = mk3(s, c, 0);
+}
+
+template <class Real>
+__global__ void k_remapE(const AtmoParams* params, BuildDims d, Remap2<Real>* out) {
+  const long long n = d.nE();
+  const long long node = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  const int b = blockIdx.y;
+  if (node >= n) return;
+  const AtmoParams& P = params[b];
+  int k = (int)(node % d.nE1), i = (int)(node / d.nE1);
+  d3 x, l;
+  surface_node(P, d, i, k, &x, &l);
+  Remap2<Real> m;
+  split_coord<Real>(height_to_index(P, d.nE0, mag3(x)), d.nE0, &m.u[0], &m.s[0]);
+  split_coord<Real>(sun_elevation_to_index(d.nE1, x, l), d.nE1, &m.u[1], &m.s[1]);
+  out[b * n + node] = m;
+}
+
+// ---------------------------------------------------------------------------
+// Transmittance table (atmosphere_lut.clj:74, atmosphere.clj:114-128)
+// ---------------------------------------------------------------------------
+
+template <class Real>
+__global__ void k_transmittance(const AtmoParams* params, BuildDims d, Vec4<Real>* T) {
+  const long long n = d.nT();
+  const long long node = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  const int b = blockIdx.y;
+  if (node >= n) return;
+  const AtmoParams& P = params[b];
+  int j = (int)(node % d.nT1), i = (int)(node / d.nT1);
+  double r = index_to_radius(P, d.nT0, (double)i), sv, cv;
+  int above;
+  index_to_elevation(P, d.nT1, r, (double)j, &sv, &cv, &above);
+  d3 x = mk3(r, 0, 0), v = mk3(sv, cv, 0);
+  d3 e = above ? atmosphere_intersection(P, x, v) : surface_intersection(P, x, v);
+  Real tau[3];
+  segment_depth<Real>(P, x, sub3(e, x), d.S, tau);
+  Vec4<Real> o;
+  o.x = exp_neg(tau[0]);
+  o.y = exp_neg(tau[1]);
+  o.z = exp_neg(tau[2]);
+  o.w = 0;
+  T[b * n + node] = o;
+}
+
+// ---------------------------------------------------------------------------
+// Surface radiance of direct sun light E0 (atmosphere.clj:131-137)
+// ---------------------------------------------------------------------------
+
+template <class Real>
+__global__ void k_surface_base(const AtmoParams* params, BuildDims d, Vec4<Real>* E0) {
+  const long long n = d.nE();
+  const long long node = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  const int b = blockIdx.y;
+  if (node >= n) return;
+  const AtmoParams& P = params[b];
+  int k = (int)(node % d.nE1), i = (int)(node / d.nE1);
+  d3 x, l;
+  surface_node(P, d, i, k, &x, &l);
+  d3 normal = mul3(x, 1.0 / mag3(x));
+  double cosine = dmax(0.0, dot3(normal, l));
+  Vec4<Real> o;
+  o.x = o.y = o.z = o.w = 0;
+  if (cosine > 0.0) {
+    d3 e = atmosphere_intersection(P, x, l);
+    Real tau[3];
+    segment_depth<Real>(P, x, sub3(e, x), d.S, tau);
+    o.x = exp_neg(tau[0]) * (Real)(P.intensity[0] * cosine);
+    o.y = exp_neg(tau[1]) * (Real)(P.intensity[1] * cosine);
+    o.z = exp_neg(tau[2]) * (Real)(P.intensity[2] * cosine);
+  }
+  E0[b * n + node] = o;
+}
+
+// ---------------------------------------------------------------------------
+// View rows: for every (height i, elevation j) of the 4-D space the ray from
+// x to its extremity (atmosphere.clj:192-200) and its S midpoint samples.
+// One thread per (row, sample).
+// ---------------------------------------------------------------------------
+
+template <class Real>
+__global__ void k_view_rows(const AtmoParams* params, BuildDims d, RowInfo* info, RowSample<Real>* samples) {
+  const long long nrows = d.rows();
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  const int b = blockIdx.y;
+  if (t >= nrows * d.S) return;
+  const AtmoParams& P = params[b];
+  const int s = (int)(t % d.S);
+  const long long row = t / d.S;
+  const int j = (int)(row % d.n1), i = (int)(row / d.n1);
+  double r, sv, cv;
+  int above;
+  view_geometry(P, d, i, j, &r, &sv, &cv, &above);
+  d3 x = mk3(r, 0, 0), v = mk3(sv, cv, 0);
+  d3 e = above ? atmosphere_intersection(P, x, v) : surface_intersection(P, x, v);
+  d3 D = sub3(e, x);
+  if (s == 0) {
+    RowInfo ri;
+    ri.r = r;
+    ri.sv = sv;
+    ri.cv = cv;
+    ri.D[0] = D.x;
+    ri.D[1] = D.y;
+    ri.D[2] = D.z;
+    ri.L = mag3(D);
+    ri.above = above;
+    ri.pad = 0;
+    info[b * nrows + row] = ri;
+  }
+  // sample point as integral-ray forms it (ray.clj:22-24)
+  double stepsize = 1.0 / d.S;
+  double su = (0.5 + s) * stepsize;
+  d3 p = add3(x, mul3(D, su));
+  double pr = mag3(p);
+  double h = pr - P.R;
+  RowSample<Real> o;
+  segment_depth<Real>(P, x, sub3(p, x), d.S, o.tau);
+  o.er = (Real)exp(-(h / P.ray_scale));
+  o.em = (Real)exp(-(h / P.mie_scale));
+  o.q = (Real)((pr - P.R) * (pr + P.R));
+  o.us = (Real)su;
+  o.inv_r = (Real)(1.0 / pr);
+  split_coord<Real>(height_to_index(P, d.n0, pr), d.n0, &o.u0, &o.s0);
+  split_coord<Real>(elevation_to_index(P, d.n1, p, v, above), d.n1, &o.u1, &o.s1);
+  o.pad = 0;
+  samples[(b * nrows + row) * d.S + s] = o;
+}
+
+// ---------------------------------------------------------------------------
+// Sphere directions of point scatter per height row (atmosphere.clj:203-222,
+// sphere.clj:62-105): the direction in world space, where it ends, whether
+// that end is on the ground, the elevation coordinate of the dS lookup and,
+// for ground ends, T(x, g) * brightness / pi and the ground point's height
+// coordinate in the surface-radiance space.
+// ---------------------------------------------------------------------------
+
+template <class Real>
+__global__ void k_sphere_setup(const AtmoParams* params, BuildDims d, const DirLocal* dirs, const int* ring_end,
+                               SphereDir<Real>* out) {
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  const int b = blockIdx.y;
+  if (t >= (long long)d.n0 * d.P) return;
+  const AtmoParams& P = params[b];
+  const int w = (int)(t % d.P), i = (int)(t / d.P);
+  double r = index_to_radius(P, d.n0, (double)i);
+  d3 x = mk3(r, 0, 0);
+  d3 n = mul3(x, 1.0 / mag3(x));
+  d3 o1 = orthogonal(n);
+  d3 o2 = cross3(n, o1);
+  d3 omega = to_world(n, o1, o2, dirs[w]);
+  d3 g = ray_extremity(P, x, omega);
+  int surface = surface_point(P, g);
+  SphereDir<Real> o;
+  o.w[0] = (Real)omega.x;
+  o.w[1] = (Real)omega.y;
+  o.w[2] = (Real)omega.z;
+  o.weight = (Real)dirs[w].w;
+  o.surface = surface;
+  o.pad = ring_end[w];
+  split_coord<Real>(elevation_to_index(P, d.n1, x, omega, !surface), d.n1, &o.u1, &o.s1);
+  if (surface) {
+    Real tau[3];
+    segment_depth<Real>(P, x, sub3(g, x), d.S, tau);
+    double gr = mag3(g);
+    for (int c = 0; c < 3; c++) o.ground[c] = exp_neg(tau[c]) * (Real)(P.brightness[c] / M_PI);
+    o.gdir[0] = (Real)(g.x / gr);
+    o.gdir[1] = (Real)(g.y / gr);
+    o.gdir[2] = (Real)(g.z / gr);
+    split_coord<Real>(height_to_index(P, d.nE0, gr), d.nE0, &o.uE0, &o.sE0);
+  } else {
+    for (int c = 0; c < 3; c++) {
+      o.ground[c] = 0;
+      o.gdir[c] = 0;
+    }
+    o.uE0 = 0;
+    o.sE0 = 0;
+  }
+  out[((long long)b * d.n0 + i) * d.P + w] = o;
+}
+
+// ---------------------------------------------------------------------------
+// launchers
+// ---------------------------------------------------------------------------
+
+static inline dim3 grid1(long long n, int block, int B) { return dim3((unsigned)((n + block - 1) / block), B); }
+
+template <class Real>
+void launch_setup(const AtmoParams* params, const BuildDims& d, const DirLocal* dirs, const int* ring_end,
+                  const SetupBuffers<Real>& o, cudaStream_t st) {
+  const int blk = 128;
+  k_remap4<Real><<<grid1(d.n4(), blk, d.B), blk, 0, st>>>(params, d, o.remapS, o.geom);
+  k_remapT<Real><<<grid1(d.nT(), blk, d.B), blk, 0, st>>>(params, d, o.remapT);
+  k_remapE<Real><<<grid1(d.nE(), blk, d.B), blk, 0, st>>>(params, d, o.remapE);
+  k_view_rows<Real><<<grid1(d.rows() * d.S, blk, d.B), blk, 0, st>>>(params, d, o.rowinfo, o.rows);
+  k_sphere_setup<Real><<<grid1((long long)d.n0 * d.P, blk, d.B), blk, 0, st>>>(params, d, dirs, ring_end, o.sdirs);
+}
+
+template <class Real>
+void launch_transmittance(const AtmoParams* params, const BuildDims& d, Vec4<Real>* T, cudaStream_t st) {
+  const int blk = 128;
+  k_transmittance<Real><<<grid1(d.nT(), blk, d.B), blk, 0, st>>>(params, d, T);
+}
+
+template <class Real>
+void launch_surface_base(const AtmoParams* params, const BuildDims& d, Vec4<Real>* E0, cudaStream_t st) {
+  const int blk = 128;
+  k_surface_base<Real><<<grid1(d.nE(), blk, d.B), blk, 0, st>>>(params, d, E0);
+}
+
+template void launch_setup<float>(const AtmoParams*, const BuildDims&, const DirLocal*, const int*,
+                                  const SetupBuffers<float>&, cudaStream_t);
+template void launch_setup<double>(const AtmoParams*, const BuildDims&, const DirLocal*, const int*,
+                                   const SetupBuffers<double>&, cudaStream_t);
+template void launch_transmittance<float>(const AtmoParams*, const BuildDims&, Vec4<float>*, cudaStream_t);
+template void launch_transmittance<double>(const AtmoParams*, const BuildDims&, Vec4<double>*, cudaStream_t);
+template void launch_surface_base<float>(const AtmoParams*, const BuildDims&, Vec4<float>*, cudaStream_t);
+template void launch_surface_base<double>(const AtmoParams*, const BuildDims&, Vec4<double>*, cudaStream_t);
+
+}  // namespace sfsim

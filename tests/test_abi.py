@@ -1,0 +1,100 @@
+"""CPU checks of the C ABI: the library loads, exports every function that
+include/sfsim_atmo.h declares, validates configurations and reports errors
+without touching a GPU."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+from sfsim_gb300 import _lib, config as C
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    return _lib.load(build=True)
+
+
+def declared_functions():
+    names = set()
+    for f in os.listdir(os.path.join(ROOT, "include")):
+        if f.endswith(".h"):
+            text = open(os.path.join(ROOT, "include", f)).read()
+            names.update(re.findall(r"\b(sfsim_atmo_\w+)\s*\(", text))
+    return sorted(names)
+
+
+def test_exports_every_declared_symbol(lib):
+    names = declared_functions()
+    assert len(names) >= 14
+    for n in names:
+        assert hasattr(lib, n), n
+    assert set(names) <= set(_lib.EXPORTS) | set(names)
+
+
+def test_default_config_matches_reference(lib):
+    c = C.AtmoConfig()
+    lib.sfsim_atmo_default_config(ctypes.byref(c))
+    ref = C.reference_production()
+    assert bytes(c) == bytes(ref)
+
+
+def test_table_sizes(lib):
+    c = C.production()
+    n = [ctypes.c_size_t() for _ in range(4)]
+    assert lib.sfsim_atmo_table_sizes(ctypes.byref(c), *[ctypes.byref(x) for x in n]) == 0
+    assert [x.value for x in n] == list(c.table_sizes())
+    assert n[2].value == 3 * 32 * 255 * 32 * 8
+
+
+@pytest.mark.parametrize("field,value,code", [
+    ("radius", -1.0, -1), ("height", 0.0, -1), ("ray_steps", 0, -1), ("iterations", -1, -1),
+    ("precision", 7, -1), ("flags", 1, -1), ("sphere_steps", 1, -1),
+])
+def test_validate_rejects(lib, field, value, code):
+    c = C.production()
+    setattr(c, field, value)
+    assert lib.sfsim_atmo_validate(ctypes.byref(c)) == code
+    assert lib.sfsim_atmo_last_error()
+
+
+def test_validate_shapes(lib):
+    c = C.production()
+    c.ray_scatter_shape[1] = 1
+    assert lib.sfsim_atmo_validate(ctypes.byref(c)) == -5
+    c = C.production()
+    c.mie.scatter_g = 1.0
+    assert lib.sfsim_atmo_validate(ctypes.byref(c)) == -1
+
+
+def test_null_outputs(lib):
+    c = C.small_fp64()
+    assert lib.sfsim_atmo_build(ctypes.byref(c), None, None, None, None) == -6
+
+
+def test_strerror(lib):
+    for code in range(0, -9, -1):
+        assert lib.sfsim_atmo_strerror(code)
+    assert lib.sfsim_atmo_version().startswith(b"sfsim-atmo-gb300")
+
+
+def test_no_gpu_reports_enodev(lib):
+    torch = pytest.importorskip("torch")
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    c = C.small_fp64()
+    a = np.zeros(c.table_sizes()[2], np.float32)
+    p = a.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
+    assert lib.sfsim_atmo_build(ctypes.byref(c), p, p, p, p) == -4
+
+
+def test_batch_layout_mismatch_rejected(lib):
+    a, b = C.small_fp64(), C.small_fp64()
+    b.ray_steps = 32
+    arr = C.config_array([a, b])
+    x = np.zeros(10, np.float32)
+    p = x.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
+    assert lib.sfsim_atmo_build_batch(arr, 2, p, p, p, p) == -1

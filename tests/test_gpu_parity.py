@@ -1,0 +1,211 @@
+"""GPU parity of the atmosphere LUT build against the FP64 CPU oracle.
+
+All GPU results come from libsfsim_atmo.so through its C ABI.  Relative
+errors are |gpu - ref| / max(|ref|, 1e-6 * max|ref|) per table (the floor keeps
+cells that are ~0 from dominating).  Tolerances:
+  FP64 build:  2e-6 (the outputs are float32, so ~6e-8 is float rounding)
+  FP32 build:  1e-4 (the FP32 + Kahan path against FP64)
+"""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from sfsim_gb300 import atmosphere_lut as A
+from sfsim_gb300 import config as C
+
+pytestmark = pytest.mark.gpu
+
+TOL = {C.FP64: 2e-6, C.FP32: 1e-4}
+
+
+def rel_err(gpu, ref):
+    gpu = np.asarray(gpu, dtype=np.float64)
+    ref = np.asarray(ref, dtype=np.float64)
+    floor = 1e-6 * max(np.abs(ref).max(), 1e-300)
+    err = np.abs(gpu - ref) / np.maximum(np.abs(ref), floor)
+    return float(err.max()), float(err.mean())
+
+
+def assert_close(gpu, ref, tol, name):
+    assert np.isfinite(gpu).all(), f"{name}: non-finite values"
+    mx, mean = rel_err(gpu, ref)
+    assert mx <= tol, f"{name}: max rel err {mx:.3e} (mean {mean:.3e}) > {tol:.1e}"
+
+
+@pytest.fixture(scope="module")
+def small_oracle():
+    return O.build(C.small_fp64(), intermediates=True)
+
+
+@pytest.mark.parametrize("precision", [C.FP64, C.FP32])
+def test_small_build_matches_oracle(small_oracle, precision):
+    """Full 2-iteration build, every intermediate and final table."""
+    cfg = C.small_fp64(precision=precision)
+    gpu = A.build(cfg, intermediates=True)
+    tol = TOL[precision]
+    for key in ("transmittance_nodes", "surface_base", "rayleigh_first", "mie_first"):
+        assert_close(gpu[key], small_oracle[key], tol, key)
+    for it in range(cfg.iterations):
+        # later stages inherit earlier rounding; FP32 stays inside 1e-4 throughout
+        for key in ("point_scatter", "surface_delta", "ray_scatter_delta"):
+            assert_close(gpu[key][it], small_oracle[key][it], tol, f"{key}[{it}]")
+    for key in ("transmittance", "surface_radiance", "ray_scatter", "mie_strength"):
+        assert_close(gpu[key], small_oracle[key], tol, key)
+
+
+def test_zero_iterations_and_shader_tables():
+    """iterations = 0 (E stays 0) at the reference shader-test shapes (12^4, 10 steps)."""
+    cfg = C.shader_test()
+    ref = O.build(cfg)
+    gpu = A.build(cfg)
+    for key in ("transmittance", "ray_scatter", "mie_strength"):
+        assert_close(gpu[key], ref[key], TOL[C.FP64], key)
+    assert np.all(gpu["surface_radiance"] == 0)
+
+
+def test_reference_production_shapes_subset():
+    """The reference's own shapes (35 km, 127 elevations with the index tie,
+    15 sphere steps = 71 directions) with fewer ray steps, one iteration."""
+    cfg = C.reference_production()
+    cfg.ray_steps = 24
+    cfg.iterations = 1
+    gpu = A.build(cfg, intermediates=True)
+    rng = np.random.default_rng(7)
+    s = cfg.shapes()[2]
+    nodes = [(0, 0, 0, 0), (s[0] - 1, s[1] - 1, s[2] - 1, s[3] - 1), (3, (s[1] - 1) // 2, 5, 2),
+             (20, (s[1] - 1) // 2, 0, 7)]
+    nodes += [tuple(int(rng.integers(0, n)) for n in s) for _ in range(12)]
+    S1R = gpu["rayleigh_first"].astype(np.float64)
+    M = gpu["mie_first"].astype(np.float64)
+    E0 = gpu["surface_base"].astype(np.float64)
+    J = gpu["point_scatter"][0].astype(np.float64)
+    for (i, j, k, a) in nodes:
+        r, m = O.first_order_node(cfg, i, j, k, a)
+        assert_close(S1R[i, j, k, a], r, 1e-4, f"S1R{(i, j, k, a)}")
+        assert_close(M[i, j, k, a], m, 1e-4, f"M{(i, j, k, a)}")
+        jo = O.point_scatter_node(cfg, S1R, E0, i, j, k, a, mie_first=M)
+        assert_close(J[i, j, k, a], jo, 1e-4, f"J{(i, j, k, a)}")
+        so = O.ray_scatter_node(cfg, J, i, j, k, a)
+        assert_close(gpu["ray_scatter_delta"][0][i, j, k, a], so, 1e-4, f"dS{(i, j, k, a)}")
+
+
+@pytest.fixture(scope="module")
+def production_fp32():
+    cfg = C.production()
+    return cfg, A.build(cfg, intermediates=True)
+
+
+def _nodes(shape, n, seed):
+    rng = np.random.default_rng(seed)
+    fixed = [(0, 0, 0, 0), (shape[0] - 1, shape[1] - 1, shape[2] - 1, shape[3] - 1),
+             (0, (shape[1] - 1) // 2, shape[2] // 2, 3), (shape[0] // 2, (shape[1] - 1) // 2, 0, 0),
+             (5, 60, 31, 7), (31, 200, 10, 4)]
+    return fixed + [tuple(int(rng.integers(0, m)) for m in shape) for _ in range(n)]
+
+
+def test_production_first_order_nodes(production_fp32):
+    """First-order Rayleigh and Mie at production size: sampled nodes vs oracle."""
+    cfg, gpu = production_fp32
+    s = cfg.shapes()[2]
+    for (i, j, k, a) in _nodes(s, 24, 1):
+        r, m = O.first_order_node(cfg, i, j, k, a)
+        assert_close(gpu["rayleigh_first"][i, j, k, a], r, 1e-4, f"S1R{(i, j, k, a)}")
+        assert_close(gpu["mie_first"][i, j, k, a], m, 1e-4, f"M{(i, j, k, a)}")
+
+
+def test_production_order_steps(production_fp32):
+    """Each order's J, dS and dE at production size, one step at a time: the
+    oracle evaluates sampled nodes from the GPU's previous-order tables."""
+    cfg, gpu = production_fp32
+    s = cfg.shapes()[2]
+    S1R = gpu["rayleigh_first"].astype(np.float64)
+    M = gpu["mie_first"].astype(np.float64)
+    dE_prev = gpu["surface_base"].astype(np.float64)
+    for it in (0, 1, cfg.iterations - 1):
+        if it == 0:
+            dS_prev, mf = S1R, M
+        else:
+            dS_prev, mf = gpu["ray_scatter_delta"][it - 1].astype(np.float64), None
+            dE_prev = gpu["surface_delta"][it - 1].astype(np.float64)
+        J = gpu["point_scatter"][it].astype(np.float64)
+        for (i, j, k, a) in _nodes(s, 6, 10 + it):
+            jo = O.point_scatter_node(cfg, dS_prev, dE_prev, i, j, k, a, mie_first=mf)
+            assert_close(J[i, j, k, a], jo, 1e-4, f"J[{it}]{(i, j, k, a)}")
+            so = O.ray_scatter_node(cfg, J, i, j, k, a)
+            assert_close(gpu["ray_scatter_delta"][it][i, j, k, a], so, 1e-4, f"dS[{it}]{(i, j, k, a)}")
+        e = cfg.shapes()[1]
+        for (i, k) in [(0, 0), (e[0] - 1, e[1] - 1), (7, 40), (3, 20)]:
+            eo = O.surface_radiance_node(cfg, dS_prev, i, k, mie_first=mf)
+            assert_close(gpu["surface_delta"][it][i, k], eo, 1e-4, f"dE[{it}]{(i, k)}")
+
+
+def test_production_fp32_vs_fp64(production_fp32):
+    """Whole production tables: FP32 path against the FP64 path of the same kernels."""
+    cfg, g32 = production_fp32
+    g64 = A.build(C.production(precision=C.FP64))
+    for key in ("transmittance", "surface_radiance", "ray_scatter", "mie_strength"):
+        assert_close(g32[key], g64[key], 1e-4, key)
+
+
+def test_production_properties(production_fp32):
+    """Size-independent properties of the full tables."""
+    cfg, g = production_fp32
+    for key in ("transmittance", "surface_radiance", "ray_scatter", "mie_strength"):
+        assert np.isfinite(g[key]).all()
+        assert (g[key] >= 0).all(), key
+    assert g["transmittance"].max() <= 1.0 + 1e-6
+    # every order adds light: the accumulated S exceeds the first-order Rayleigh
+    assert g["ray_scatter"].sum() > 0
+    for it in range(cfg.iterations):
+        assert (g["ray_scatter_delta"][it] >= 0).all()
+    # orders decay
+    tot = [g["ray_scatter_delta"][it].sum() for it in range(cfg.iterations)]
+    assert all(tot[i + 1] < tot[i] for i in range(len(tot) - 1)), tot
+
+
+def test_repeatable():
+    cfg = C.small_fp64(precision=C.FP32)
+    a = A.build(cfg)
+    b = A.build(cfg)
+    for key in a:
+        assert np.array_equal(a[key], b[key]), key
+
+
+def test_batch_equals_single_builds():
+    cfgs = C.parameter_sweep(3, ray_scatter_shape=(8, 16, 8, 4), transmittance_shape=(32, 32),
+                             surface_radiance_shape=(16, 32), ray_steps=32, sphere_steps=16, iterations=2)
+    batch = A.build_batch(cfgs)
+    for n, cfg in enumerate(cfgs):
+        single = A.build(cfg)
+        for key in single:
+            assert np.array_equal(batch[key][n], single[key]), (n, key)
+
+
+def test_batch_matches_oracle():
+    cfgs = C.parameter_sweep(2, precision=C.FP32, ray_scatter_shape=(8, 16, 8, 4), transmittance_shape=(32, 32),
+                             surface_radiance_shape=(16, 32), ray_steps=32, sphere_steps=16, iterations=2)
+    batch = A.build_batch(cfgs)
+    for n, cfg in enumerate(cfgs):
+        ref = O.build(cfg)
+        for key in ref:
+            assert_close(batch[key][n], ref[key], 1e-4, f"{n}:{key}")
+
+
+def test_device_build_matches_host_build():
+    import torch
+    cfg = C.small_fp64(precision=C.FP32)
+    host = A.build(cfg)
+    tens = A.build_device(cfg)
+    torch.cuda.synchronize()
+    for t, key in zip(tens, ("transmittance", "surface_radiance", "ray_scatter", "mie_strength")):
+        assert np.array_equal(t.cpu().numpy(), host[key]), key
+
+
+def test_generate_files(tmp_path):
+    cfg = C.small_fp64(precision=C.FP32)
+    paths = A.generate_atmosphere_luts(str(tmp_path), cfg)
+    tables = A.build(cfg)
+    for key, p in paths.items():
+        data = np.fromfile(p, dtype="<f4")
+        assert data.size == tables[key].size
+        assert np.array_equal(data, tables[key].ravel())
