@@ -45,6 +45,10 @@ def parse():
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--cpu-sample-s", type=float, default=15.0, help="seconds of CPU baseline sampling")
+    p.add_argument("--profile", default=None,
+                   help="only run --builds builds of a named configuration (small_fp64, production, "
+                        "reference_production, shader_test), for profilers")
+    p.add_argument("--builds", type=int, default=2)
     return p.parse_args()
 
 
@@ -358,9 +362,24 @@ def run_reference(args):
     return result
 
 
+def run_profile(args):
+    """Plain builds of one configuration with nothing else on the GPU (for ncu)."""
+    import torch
+
+    from sfsim_gb300 import atmosphere_lut as A, config as C
+    cfg = getattr(C, args.profile)()
+    torch.cuda.set_device(0)
+    for _ in range(args.builds):
+        A.build_device(cfg)
+    torch.cuda.synchronize()
+    print(json.dumps({"profile": args.profile, "builds": args.builds, "config": cfg.describe()}))
+
+
 def main():
     args = parse()
-    if args.impl == "reference":
+    if args.profile:
+        run_profile(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_ours(args)
