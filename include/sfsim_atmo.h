@@ -106,6 +106,25 @@ int sfsim_atmo_build_device(const sfsim_atmo_config* cfg, float* transmittance,
                             float* surface_radiance, float* ray_scatter,
                             float* mie_strength, void* stream);
 
+/* As sfsim_atmo_build_device, but allocates nothing.  No counterpart in the
+ * reference: it is for callers that cannot call cudaMalloc, such as code
+ * inside a CUDA-graph capture, or engines whose own allocator owns all device
+ * memory.  All scratch tables live in one static device array of 64 MiB
+ * (67108864 bytes) that every GPU loading the library holds until the process
+ * exits; a configuration that needs more (roughly 3e5 ray-scatter cells in
+ * FP32, half that in FP64; the small FP64 case and the 12^4 shader-test
+ * tables fit, the production tables do not) is rejected with
+ * SFSIM_ATMO_ETOOBIG and a message naming the bytes it needs.  Outputs are
+ * DEVICE pointers, work is queued on `stream`, and the call returns once it is
+ * queued.  The first call on a device looks up the array's device address
+ * (cudaGetSymbolAddress); make that first call before any stream capture.
+ * Every call uses the same array, so calls that overlap on the GPU (different
+ * streams, or different host threads) race and corrupt each other; order them
+ * on one stream.  Stage timings are not recorded. */
+int sfsim_atmo_build_static(const sfsim_atmo_config* cfg, float* transmittance,
+                            float* surface_radiance, float* ray_scatter,
+                            float* mie_strength, void* stream);
+
 /* Builds `n` independent atmospheres that share shapes, steps, iterations and
  * precision (they may differ in every physical parameter) in one pass of
  * batched kernels.  Outputs are HOST arrays of n consecutive tables each. */

@@ -22,6 +22,7 @@ EXPORTS = (
     "sfsim_atmo_build_device", "sfsim_atmo_build_batch", "sfsim_atmo_build_debug", "sfsim_atmo_set_timing",
     "sfsim_atmo_last_timings", "sfsim_atmo_last_launch_count", "sfsim_atmo_release", "sfsim_atmo_strerror",
     "sfsim_atmo_last_error", "sfsim_atmo_version", "sfsim_atmo_census", "sfsim_atmo_sfu_peak",
+    "sfsim_atmo_build_static",
 )
 
 
@@ -56,6 +57,8 @@ def load(build: bool = False):
     L.sfsim_atmo_table_sizes.argtypes = [_cfgp] + [ctypes.POINTER(ctypes.c_size_t)] * 4
     L.sfsim_atmo_build.argtypes = [_cfgp, _fp, _fp, _fp, _fp]
     L.sfsim_atmo_build_device.argtypes = [_cfgp, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                          ctypes.c_void_p, ctypes.c_void_p]
+    L.sfsim_atmo_build_static.argtypes = [_cfgp, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                           ctypes.c_void_p, ctypes.c_void_p]
     L.sfsim_atmo_build_batch.argtypes = [_cfgp, ctypes.c_int, _fp, _fp, _fp, _fp]
     L.sfsim_atmo_build_debug.argtypes = [_cfgp, _fp, _fp, _fp, _fp, ctypes.POINTER(Intermediates)]

@@ -771,3 +771,85 @@ const char* sfsim_atmo_last_error(void) { return g_last_error.c_str(); }
 const char* sfsim_atmo_version(void) { return "sfsim-atmo-gb300 0.1.0 (sm_103a)"; }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Allocation-free build.  Some callers cannot call cudaMalloc: code running
+// inside a CUDA-graph capture or under a memory budget fixed at start-up, or
+// engines whose allocator owns every device byte.  For them this entry point
+// builds the tables with all scratch in one fixed device array that the
+// library declares at file scope.  The array (kStaticScratchBytes, 64 MiB) is
+// held on every GPU that loads the library until the process exits.
+// ---------------------------------------------------------------------------
+
+namespace {
+
+constexpr size_t kStaticScratchBytes = 64ull << 20;
+
+static __device__ __align__(256) unsigned char g_static_scratch[kStaticScratchBytes];
+
+// Device address of g_static_scratch per device.  In host code the array's
+// name only stands in for the symbol, so the address must come from
+// cudaGetSymbolAddress, called with the device current.
+void* g_static_base[kMaxDevices];
+
+int static_scratch_base(int dev, void** base) {
+  if (!g_static_base[dev]) {
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_static_scratch);
+    if (e != cudaSuccess || !p)
+      return fail(SFSIM_ATMO_ECUDA, std::string("cudaGetSymbolAddress of the static scratch failed: ") +
+                                        cudaGetErrorString(e));
+    g_static_base[dev] = p;
+  }
+  *base = g_static_base[dev];
+  return 0;
+}
+
+template <class Real>
+int build_static_impl(const sfsim_atmo_config& cfg, float* T, float* E, float* S, float* M, cudaStream_t st) {
+  int dev = 0;
+  int rc = current_device(&dev);
+  if (rc) return rc;
+  BuildDims d = make_dims(cfg, 1);
+  if ((rc = check_smem<Real>(d))) return rc;
+  Work<Real> w;
+  const size_t bytes = carve<Real>(w, nullptr, d, false);
+  if (bytes > kStaticScratchBytes)
+    return fail(SFSIM_ATMO_ETOOBIG, "the build needs " + std::to_string(bytes) +
+                                        " bytes of scratch, more than the 67108864-byte static array");
+  AtmoParams hp;
+  if ((rc = make_params(cfg, hp))) return rc;
+  std::vector<DirLocal> dirs, hdirs;
+  std::vector<int> ring_end, hring;
+  sphere_directions(cfg.sphere_steps >> 1, cfg.sphere_steps, M_PI, dirs, ring_end);
+  sphere_directions(cfg.ray_steps >> 2, cfg.ray_steps, M_PI / 2, hdirs, hring);
+  void* base = nullptr;
+  if ((rc = static_scratch_base(dev, &base))) return rc;
+  carve<Real>(w, (char*)base, d, false);
+  // every scratch table is written before it is read, so nothing is cleared;
+  // parameters and quadrature directions are copied in on the caller's stream
+  CUDA_TRY(cudaMemcpyAsync(w.params, &hp, sizeof(AtmoParams), cudaMemcpyHostToDevice, st));
+  if (!dirs.empty()) {
+    CUDA_TRY(cudaMemcpyAsync(w.dirs, dirs.data(), sizeof(DirLocal) * dirs.size(), cudaMemcpyHostToDevice, st));
+    CUDA_TRY(cudaMemcpyAsync(w.ring_end, ring_end.data(), sizeof(int) * ring_end.size(), cudaMemcpyHostToDevice, st));
+  }
+  if (!hdirs.empty())
+    CUDA_TRY(cudaMemcpyAsync(w.hdirs, hdirs.data(), sizeof(DirLocal) * hdirs.size(), cudaMemcpyHostToDevice, st));
+  Timer tm;
+  tm.dev = dev;
+  tm.st = st;
+  tm.n = 512;  // a full event list: this entry point records no stage timings
+  return run_build<Real>(w, d, T, E, S, M, st, tm, nullptr);
+}
+
+}  // namespace
+
+extern "C" int sfsim_atmo_build_static(const sfsim_atmo_config* cfg, float* T, float* E, float* S, float* M,
+                                       void* stream) {
+  int rc = validate(cfg);
+  if (rc) return rc;
+  if (!T || !E || !S || !M) return fail(SFSIM_ATMO_ENULL, "an output pointer is NULL");
+  std::lock_guard<std::mutex> lock(g_mutex);
+  if (cfg->precision == SFSIM_ATMO_FP64) return build_static_impl<double>(*cfg, T, E, S, M, (cudaStream_t)stream);
+  return build_static_impl<float>(*cfg, T, E, S, M, (cudaStream_t)stream);
+}

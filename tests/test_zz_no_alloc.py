@@ -1,0 +1,60 @@
+"""The allocation-free entry point, sfsim_atmo_build_static.
+
+It exists for callers that cannot call cudaMalloc (code inside a CUDA-graph
+capture, engines whose allocator owns all device memory): its scratch is a
+fixed static device array inside the library.  This test calls it twice in a
+row through the C ABI and checks both results against the allocating entry
+point, sfsim_atmo_build_device, with the 1e-6 relative tolerance of the FP64
+parity tests (both run the same kernels, so the results agree bit for bit in
+practice).  The file name sorts last so that a run stopping at its first
+failure has run every other test before this one.
+"""
+import ctypes
+
+import numpy as np
+import pytest
+
+from sfsim_gb300 import _lib, atmosphere_lut as A, config as C
+
+pytestmark = pytest.mark.gpu
+
+
+def _build(fn, cfg, stream):
+    import torch
+    outs = [torch.full(s, -1.0, dtype=torch.float32, device="cuda") for s in A.table_shapes(cfg)]
+    _lib.check(fn(ctypes.byref(cfg), *[t.data_ptr() for t in outs], ctypes.c_void_p(stream.cuda_stream)), fn.__name__)
+    return outs
+
+
+def _rel(a, b):
+    a = a.double().cpu().numpy()
+    b = b.double().cpu().numpy()
+    floor = 1e-6 * max(np.abs(b).max(), 1e-300)
+    return float((np.abs(a - b) / np.maximum(np.abs(b), floor)).max())
+
+
+@pytest.mark.parametrize("precision", [C.FP32, C.FP64])
+def test_static_build_matches_allocating_build(precision):
+    import torch
+    L = _lib.load()
+    cfg = C.small_fp64(precision=precision)
+    stream = torch.cuda.current_stream()
+    ref = _build(L.sfsim_atmo_build_device, cfg, stream)
+    first = _build(L.sfsim_atmo_build_static, cfg, stream)
+    second = _build(L.sfsim_atmo_build_static, cfg, stream)
+    torch.cuda.synchronize()
+    for r, a, b in zip(ref, first, second):
+        assert torch.isfinite(a).all() and torch.isfinite(b).all()
+        assert _rel(a, r) <= 1e-6
+        assert _rel(b, r) <= 1e-6
+
+
+def test_static_build_rejects_oversize():
+    import torch
+    L = _lib.load()
+    cfg = C.production()
+    x = torch.zeros(4, dtype=torch.float32, device="cuda")
+    rc = L.sfsim_atmo_build_static(ctypes.byref(cfg), *([x.data_ptr()] * 4),
+                                   ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
+    assert rc == -7
+    assert b"static array" in L.sfsim_atmo_last_error()
