@@ -157,6 +157,13 @@ int fit_height_polynomial(AtmoParams& P) {
     P.f_hpoly[k] = (float)P.d_hpoly[k];
   }
   P.hpoly_n = N;
+  const double kr = -1.4426950408889634 / P.ray_scale;
+  for (int k = 0; k < kMaxHPoly; k++) {
+    P.d_hpr[k] = P.d_hpoly[k] * kr;
+    P.f_hpr[k] = (float)P.d_hpr[k];
+  }
+  P.d_hratio = P.ray_scale / P.mie_scale;
+  P.f_hratio = (float)P.d_hratio;
   P.d_alpha = alpha;
   P.d_beta = beta;
   P.f_alpha = (float)alpha;
@@ -231,7 +238,7 @@ template <class Real>
 int check_smem(const BuildDims& d) {
   if (point_scatter_smem<Real>(d, true) > kMaxSmem)
     return fail(SFSIM_ATMO_ESHAPE, "elevation x heading slab of point scatter exceeds shared memory");
-  if (sizeof(Real) * 3 * 8 * (size_t)d.n2 * d.n3 + 64 * sizeof(Real) > kMaxSmem)
+  if (sizeof(Real) * 3 * 16 * (size_t)d.n2 * d.n3 + 16 * 64 > kMaxSmem)
     return fail(SFSIM_ATMO_ESHAPE, "sun elevation x heading plane of ray scatter exceeds shared memory");
   return 0;
 }

@@ -31,11 +31,15 @@ struct AtmoParams {
   double d_km, d_kr;                  // -log2(e) / scale height
   double d_hpoly[kMaxHPoly];          // h(q) = q * P(q * alpha + beta)
   double d_alpha, d_beta;
+  double d_hpr[kMaxHPoly];            // -log2(e)/H_rayleigh * h(q) = q * Pr(z)
+  double d_hratio;                    // H_rayleigh / H_mie
   float f_mie_ext[3], f_ray_ext[3];
   float f_mie_base[3], f_ray_base[3];
   float f_km, f_kr;
   float f_hpoly[kMaxHPoly];
   float f_alpha, f_beta;
+  float f_hpr[kMaxHPoly];
+  float f_hratio;
   float f_R, f_Hh2, f_mie_g;
   float f_bright_pi[3];               // brightness / pi
   float f_intensity[3];

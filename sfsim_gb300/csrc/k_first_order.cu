@@ -53,7 +53,7 @@ __device__ __forceinline__ Real warp_sum(Real v) {
 }
 
 template <class Real, int WARPS>
-__global__ void __launch_bounds__(WARPS * 32) k_first_order(const AtmoParams* params, BuildDims d,
+__global__ void __launch_bounds__(WARPS * 32, 4) k_first_order(const AtmoParams* params, BuildDims d,
                                                             const RowInfo* rowinfo, const RowSample<Real>* rows,
                                                             const CellGeom<Real>* geom, Vec4<Real>* rayleigh,
                                                             Vec4<Real>* mie) {
@@ -81,12 +81,12 @@ __global__ void __launch_bounds__(WARPS * 32) k_first_order(const AtmoParams* pa
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int ncell = d.n2 * d.n3;
   const Real Hh2 = (Real)P.Hh2;
-  const Real* hp = Bulk<Real>::hpoly(P);
+  const Real* hp = Bulk<Real>::hpr(P);
   Real hc[5];
 #pragma unroll
   for (int c = 0; c < 5; c++) hc[c] = hp[c];
   const Real alpha = Bulk<Real>::alpha(P), beta = Bulk<Real>::beta(P);
-  const Real kr = Bulk<Real>::kr(P), km = Bulk<Real>::km(P);
+  const Real ratio = Bulk<Real>::hratio(P);
   Real rext[3], mext[3];
 #pragma unroll
   for (int c = 0; c < 3; c++) {
@@ -115,7 +115,7 @@ __global__ void __launch_bounds__(WARPS * 32) k_first_order(const AtmoParams* pa
         texit = fmax(texit, Real(0));
         const Real dt = texit * inv_steps;
         Real sr, smie;
-        optical_sums<Real, 5>(q, bp + bp, dt, S, hc, alpha, beta, kr, km, sr, smie);
+        sun_sums<Real, 5>(q, bp, dt, S, hc, alpha, beta, ratio, sr, smie);
 #pragma unroll
         for (int c = 0; c < 3; c++) {
           const Real tau = sm[s].tau[c] + dt * (rext[c] * sr + mext[c] * smie);

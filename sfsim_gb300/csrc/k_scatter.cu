@@ -77,31 +77,73 @@ __device__ __forceinline__ Real sun_elevation_index_r(Real sin_el, Real scale) {
 
 // ---------------------------------------------------------------------------
 // Point scatter J (atmosphere.clj:203-222) for all nodes of one (height i,
-// sun elevation k) pair.  For such a pair the dS lookups of every direction
-// share the height coordinate (x is fixed) and the sun-elevation coordinate
-// (x.l/|x| = sin of the sun elevation), so the block first collapses those two
-// dimensions of dS into a 2-D slab [elevation][heading] in shared memory and
-// each direction then needs a bilinear gather from the slab.  The ground term
-// reads the whole dE table, also staged in shared memory.  One thread per
-// node (elevation j, heading a); the directions come from k_sphere_setup.
+// sun elevation k) pair.  For such a pair every dS lookup shares the height
+// coordinate (x is fixed) and the sun-elevation coordinate (x.l/|x| is the
+// sin of the sun elevation), and a direction's elevation coordinate depends
+// on the direction alone.  So the block first gathers, per direction, dS
+// along the heading axis (8 corners per heading) into a row in shared
+// memory; a node then reads two texels of its direction's row at its own
+// sun-angle coordinate (omega.l).  The ground term reads the dE table, also
+// staged in shared memory.  One thread per node (elevation j, heading a);
+// directions, ground ends and T(x, ground) come from k_sphere_setup.
 // ---------------------------------------------------------------------------
 
+// Cornette-Shanks phase with its g-only factors hoisted:
+// phase = k (1 + mu^2) (a + b mu)^-3/2, k = 3(1-g^2)/(8 pi (2+g^2)), a = 1+g^2, b = -2g.
+template <class Real>
+struct PhaseCS {
+  Real k, a, b;
+  __device__ __forceinline__ PhaseCS(double g) {
+    k = (Real)(3.0 * (1.0 - g * g) / (8.0 * 3.14159265358979323846 * (2.0 + g * g)));
+    a = (Real)(1.0 + g * g);
+    b = (Real)(-2.0 * g);
+  }
+  __device__ __forceinline__ Real operator()(Real mu) const {
+    const Real r = Bulk<Real>::rsqrt(fma(b, mu, a));
+    return k * fma(mu, mu, Real(1)) * (r * r * r);
+  }
+};
+
+template <class Real>
+__device__ __forceinline__ void gather_heading_row(const Vec4<Real>* t, const BuildDims& d, int u0, int v0, Real s0,
+                                                   int u1, int v1, Real s1, int u2, int v2, Real s2, int a,
+                                                   Real* dst) {
+  Real A[3], B[3], lo[3], hi[3], e0[3], e1[3];
+  // height and sun elevation first, then elevation
+  ld3(t, idx4(d, u0, u1, u2, a), A);
+  ld3(t, idx4(d, u0, u1, v2, a), B);
+  mix3(A, B, s2, lo);
+  ld3(t, idx4(d, v0, u1, u2, a), A);
+  ld3(t, idx4(d, v0, u1, v2, a), B);
+  mix3(A, B, s2, hi);
+  mix3(lo, hi, s0, e0);
+  ld3(t, idx4(d, u0, v1, u2, a), A);
+  ld3(t, idx4(d, u0, v1, v2, a), B);
+  mix3(A, B, s2, lo);
+  ld3(t, idx4(d, v0, v1, u2, a), A);
+  ld3(t, idx4(d, v0, v1, v2, a), B);
+  mix3(A, B, s2, hi);
+  mix3(lo, hi, s0, e1);
+  mix3(e0, e1, s1, dst);
+}
+
 template <class Real, bool FIRST>
-__global__ void __launch_bounds__(256) k_point_scatter(const AtmoParams* params, BuildDims d, const RowInfo* rowinfo,
-                                                       const SphereDir<Real>* sdirs, const CellGeom<Real>* geom,
-                                                       const Vec4<Real>* dS, const Vec4<Real>* Mt,
-                                                       const Vec4<Real>* dE, Vec4<Real>* J, int nchunks) {
+__global__ void __launch_bounds__(256, 4) k_point_scatter(const AtmoParams* params, BuildDims d,
+                                                          const RowInfo* rowinfo, const SphereDir<Real>* sdirs,
+                                                          const CellGeom<Real>* geom, const Vec4<Real>* dS,
+                                                          const Vec4<Real>* Mt, const Vec4<Real>* dE,
+                                                          Vec4<Real>* J, int nchunks) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int b = blockIdx.y;
   const int chunk = blockIdx.x % nchunks;
   const int ik = blockIdx.x / nchunks;
   const int i = ik / d.n2, k = ik % d.n2;
   const AtmoParams& P = params[b];
-  const int nslab = d.n1 * d.n3;
+  const int nrow = d.P * d.n3;
   SphereDir<Real>* dirs = reinterpret_cast<SphereDir<Real>*>(smem_raw);
-  Real* slab = reinterpret_cast<Real*>(dirs + d.P);
-  Real* slabM = slab + 3 * nslab;
-  Real* etab = slabM + (FIRST ? 3 * nslab : 0);
+  Real* rows = reinterpret_cast<Real*>(dirs + d.P);
+  Real* rowsM = rows + 3 * nrow;
+  Real* etab = rowsM + (FIRST ? 3 * nrow : 0);
 
   // the (i, k) coordinates, FP64 as in ray-scatter-forward
   const double r = index_to_radius(P, d.n0, (double)i);
@@ -113,31 +155,14 @@ __global__ void __launch_bounds__(256) k_point_scatter(const AtmoParams* params,
   const int v0 = upper_index(u0, d.n0), v2 = upper_index(u2, d.n2);
 
   const long long base4 = (long long)b * d.n4();
-  for (int t = threadIdx.x; t < nslab; t += blockDim.x) {
-    const int j = t / d.n3, a = t % d.n3;
-    Real A[3], B[3], lo[3], hi[3], o[3];
-    ld3(dS, base4 + idx4(d, u0, j, u2, a), A);
-    ld3(dS, base4 + idx4(d, u0, j, v2, a), B);
-    mix3(A, B, s2, lo);
-    ld3(dS, base4 + idx4(d, v0, j, u2, a), A);
-    ld3(dS, base4 + idx4(d, v0, j, v2, a), B);
-    mix3(A, B, s2, hi);
-    mix3(lo, hi, s0, o);
-    slab[3 * t] = o[0];
-    slab[3 * t + 1] = o[1];
-    slab[3 * t + 2] = o[2];
-    if (FIRST) {
-      ld3(Mt, base4 + idx4(d, u0, j, u2, a), A);
-      ld3(Mt, base4 + idx4(d, u0, j, v2, a), B);
-      mix3(A, B, s2, lo);
-      ld3(Mt, base4 + idx4(d, v0, j, u2, a), A);
-      ld3(Mt, base4 + idx4(d, v0, j, v2, a), B);
-      mix3(A, B, s2, hi);
-      mix3(lo, hi, s0, o);
-      slabM[3 * t] = o[0];
-      slabM[3 * t + 1] = o[1];
-      slabM[3 * t + 2] = o[2];
-    }
+  const SphereDir<Real>* src = sdirs + ((long long)b * d.n0 + i) * d.P;
+  for (int t = threadIdx.x; t < d.P; t += blockDim.x) dirs[t] = src[t];
+  for (int t = threadIdx.x; t < nrow; t += blockDim.x) {
+    const int w = t / d.n3, a = t - w * d.n3;
+    const int u1 = src[w].u1, v1 = upper_index(u1, d.n1);
+    const Real s1 = src[w].s1;
+    gather_heading_row(dS + base4, d, u0, v0, s0, u1, v1, s1, u2, v2, s2, a, rows + 3 * t);
+    if (FIRST) gather_heading_row(Mt + base4, d, u0, v0, s0, u1, v1, s1, u2, v2, s2, a, rowsM + 3 * t);
   }
   const long long nE = d.nE();
   for (int t = threadIdx.x; t < nE; t += blockDim.x) {
@@ -147,54 +172,43 @@ __global__ void __launch_bounds__(256) k_point_scatter(const AtmoParams* params,
     etab[3 * t + 1] = A[1];
     etab[3 * t + 2] = A[2];
   }
-  const SphereDir<Real>* src = sdirs + ((long long)b * d.n0 + i) * d.P;
-  for (int t = threadIdx.x; t < d.P; t += blockDim.x) dirs[t] = src[t];
   __syncthreads();
 
   const int cell = chunk * blockDim.x + threadIdx.x;
-  if (cell >= nslab) return;
+  if (cell >= d.n1 * d.n3) return;
   const int j = cell / d.n3, a = cell % d.n3;
   const RowInfo ri = rowinfo[(long long)b * d.rows() + (long long)i * d.n1 + j];
   const Real sv = (Real)ri.sv, cv = (Real)ri.cv;
   const long long node = base4 + idx4(d, i, j, k, a);
   const CellGeom<Real> g = geom[node];
-  const Real gR = (Real)P.ray_g, gM = (Real)P.mie_g;
+  const PhaseCS<Real> phR(P.ray_g), phM(P.mie_g);
   const Real scale3 = Real(0.5) * Real(d.n3 - 1);
   const Real scaleE = (Real)((d.nE1 - 1) / (1 - exp(-3.6)));
+  const int n3x3 = 3 * d.n3;
 
   Real accR[3] = {0, 0, 0}, accM[3] = {0, 0, 0}, cR[3] = {0, 0, 0}, cM[3] = {0, 0, 0};
   Real ringR[3] = {0, 0, 0}, ringM[3] = {0, 0, 0};
   for (int w = 0; w < d.P; w++) {
     const SphereDir<Real>& D = dirs[w];
-    const Real mu_v = sv * D.w[0] + cv * D.w[1];
-    const Real mu_l = D.w[0] * g.lx + D.w[1] * g.ly + D.w[2] * g.lz;
-    // sun-angle coordinate of (omega, l)
+    const Real mu_v = fma(sv, D.w[0], cv * D.w[1]);
+    const Real mu_l = fma(D.w[0], g.lx, fma(D.w[1], g.ly, D.w[2] * g.lz));
+    // sun-angle coordinate of (omega, l) along the direction's heading row
     int u3;
     Real s3;
     split_coord_r<Real>(scale3 * (Real(1) + mu_l), d.n3, &u3, &s3);
     const int v3 = upper_index(u3, d.n3);
-    const int u1 = D.u1, v1 = upper_index(D.u1, d.n1);
+    const Real* row = rows + w * n3x3;
     Real X[3];
-    {
-      const Real* p00 = slab + 3 * (u1 * d.n3 + u3);
-      const Real* p01 = slab + 3 * (u1 * d.n3 + v3);
-      const Real* p10 = slab + 3 * (v1 * d.n3 + u3);
-      const Real* p11 = slab + 3 * (v1 * d.n3 + v3);
-      mix4(p00, p01, p10, p11, D.s1, s3, X);
-    }
-    if (FIRST) {
-      Real Y[3];
-      const Real* p00 = slabM + 3 * (u1 * d.n3 + u3);
-      const Real* p01 = slabM + 3 * (u1 * d.n3 + v3);
-      const Real* p10 = slabM + 3 * (v1 * d.n3 + u3);
-      const Real* p11 = slabM + 3 * (v1 * d.n3 + v3);
-      mix4(p00, p01, p10, p11, D.s1, s3, Y);
-      const Real ph = phase_cs<Real>(gM, mu_l);
 #pragma unroll
-      for (int c = 0; c < 3; c++) X[c] = fma(Y[c], ph, X[c]);
+    for (int c = 0; c < 3; c++) X[c] = fma(row[3 * v3 + c] - row[3 * u3 + c], s3, row[3 * u3 + c]);
+    if (FIRST) {
+      const Real* rowM = rowsM + w * n3x3;
+      const Real ph = phM(mu_l);
+#pragma unroll
+      for (int c = 0; c < 3; c++) X[c] = fma(fma(rowM[3 * v3 + c] - rowM[3 * u3 + c], s3, rowM[3 * u3 + c]), ph, X[c]);
     }
     if (D.surface) {
-      const Real sg = D.gdir[0] * g.lx + D.gdir[1] * g.ly + D.gdir[2] * g.lz;
+      const Real sg = fma(D.gdir[0], g.lx, fma(D.gdir[1], g.ly, D.gdir[2] * g.lz));
       int uE1;
       Real sE1;
       split_coord_r<Real>(sun_elevation_index_r<Real>(sg, scaleE), d.nE1, &uE1, &sE1);
@@ -205,8 +219,8 @@ __global__ void __launch_bounds__(256) k_point_scatter(const AtmoParams* params,
 #pragma unroll
       for (int c = 0; c < 3; c++) X[c] = fma(D.ground[c], Y[c], X[c]);
     }
-    const Real wR = D.weight * phase_cs<Real>(gR, mu_v);
-    const Real wM = D.weight * phase_cs<Real>(gM, mu_v);
+    const Real wR = D.weight * phR(mu_v);
+    const Real wM = D.weight * phM(mu_v);
 #pragma unroll
     for (int c = 0; c < 3; c++) {
       ringR[c] = fma(wR, X[c], ringR[c]);
@@ -235,7 +249,7 @@ __global__ void __launch_bounds__(256) k_point_scatter(const AtmoParams* params,
 
 template <class Real>
 size_t point_scatter_smem(const BuildDims& d, bool first) {
-  return sizeof(SphereDir<Real>) * d.P + sizeof(Real) * 3 * ((size_t)d.n1 * d.n3 * (first ? 2 : 1) + d.nE());
+  return sizeof(SphereDir<Real>) * d.P + sizeof(Real) * 3 * ((size_t)d.P * d.n3 * (first ? 2 : 1) + d.nE());
 }
 
 template <class Real>
@@ -355,7 +369,8 @@ void launch_surface_radiance(const AtmoParams* params, const BuildDims& d, const
 template <class Real>
 struct RaySample {
   Real T[3];
-  Real us, inv_r;
+  Real us, inv_r, s0, s1;
+  int p00, p01, p10, p11;  // J offsets of the four (height, elevation) planes
 };
 
 template <class Real, int CH>
@@ -376,76 +391,87 @@ __global__ void __launch_bounds__(256) k_ray_scatter(const AtmoParams* params, B
   const long long node0 = (b * nrows + row) * ncell;
   const Real scale2 = (Real)((d.n2 - 1) / (1 - exp(-3.6)));
   const Real rr = (Real)ri.r, D0 = (Real)ri.D[0], D1 = (Real)ri.D[1], D2 = (Real)ri.D[2];
+  const int n3x3 = 3 * d.n3;
 
   for (int c0 = 0; c0 < ncell; c0 += blockDim.x) {
     const int cell = c0 + threadIdx.x;
     const bool active = cell < ncell;
     Real b0 = 0, Dl = 0, s3 = 0;
-    int u3 = 0, v3 = 0;
+    int o3u = 0, o3v = 0;
     if (active) {
       const CellGeom<Real> g = geom[node0 + cell];
       b0 = rr * g.lx;
-      Dl = D0 * g.lx + D1 * g.ly + D2 * g.lz;
+      Dl = fma(D0, g.lx, fma(D1, g.ly, D2 * g.lz));
       const Remap4<Real> m = remap[node0 + cell];  // its sun-angle coordinate is that of (v, l)
-      u3 = m.u[3];
+      o3u = 3 * m.u[3];
+      o3v = 3 * upper_index(m.u[3], d.n3);
       s3 = m.s[3];
-      v3 = upper_index(u3, d.n3);
     }
-    Real acc[3] = {0, 0, 0}, cmp[3] = {0, 0, 0};
+    Real acc[2][3] = {{0, 0, 0}, {0, 0, 0}};
     for (int sb = 0; sb < d.S; sb += CH) {
       const int nch = min(CH, d.S - sb);
       __syncthreads();
-      for (int t = threadIdx.x; t < nch * ncell; t += blockDim.x) {
-        const int ch = t / ncell, kk = (t % ncell) / d.n3, aa = t % d.n3;
-        const RowSample<Real>& q = rs[sb + ch];
-        const int u0 = q.u0, v0 = upper_index(q.u0, d.n0), u1 = q.u1, v1 = upper_index(q.u1, d.n1);
-        Real A[3], B[3], lo[3], hi[3], o[3];
-        ld3(tJ, idx4(d, u0, u1, kk, aa), A);
-        ld3(tJ, idx4(d, u0, v1, kk, aa), B);
-        mix3(A, B, q.s1, lo);
-        ld3(tJ, idx4(d, v0, u1, kk, aa), A);
-        ld3(tJ, idx4(d, v0, v1, kk, aa), B);
-        mix3(A, B, q.s1, hi);
-        mix3(lo, hi, q.s0, o);
-        Real* dst = plane + 3 * ((long long)ch * ncell + kk * d.n3 + aa);
-        dst[0] = o[0];
-        dst[1] = o[1];
-        dst[2] = o[2];
-      }
       if (threadIdx.x < nch) {
-        const RowSample<Real>& q = rs[sb + threadIdx.x];
+        const RowSample<Real> q = rs[sb + threadIdx.x];
         RaySample<Real> v;
         v.T[0] = exp_neg(q.tau[0]);
         v.T[1] = exp_neg(q.tau[1]);
         v.T[2] = exp_neg(q.tau[2]);
         v.us = q.us;
         v.inv_r = q.inv_r;
+        v.s0 = q.s0;
+        v.s1 = q.s1;
+        const int v0 = upper_index(q.u0, d.n0), v1 = upper_index(q.u1, d.n1);
+        v.p00 = (q.u0 * d.n1 + q.u1) * ncell;
+        v.p01 = (q.u0 * d.n1 + v1) * ncell;
+        v.p10 = (v0 * d.n1 + q.u1) * ncell;
+        v.p11 = (v0 * d.n1 + v1) * ncell;
         smp[threadIdx.x] = v;
       }
       __syncthreads();
+      for (int ch = 0; ch < nch; ch++) {
+        const RaySample<Real>& v = smp[ch];
+        for (int t = threadIdx.x; t < ncell; t += blockDim.x) {
+          Real A[3], B[3], lo[3], hi[3];
+          ld3(tJ, (long long)v.p00 + t, A);
+          ld3(tJ, (long long)v.p01 + t, B);
+#pragma unroll
+          for (int c = 0; c < 3; c++) lo[c] = fma(B[c] - A[c], v.s1, A[c]);
+          ld3(tJ, (long long)v.p10 + t, A);
+          ld3(tJ, (long long)v.p11 + t, B);
+#pragma unroll
+          for (int c = 0; c < 3; c++) hi[c] = fma(B[c] - A[c], v.s1, A[c]);
+          Real* dst = plane + 3 * (ch * ncell + t);
+#pragma unroll
+          for (int c = 0; c < 3; c++) dst[c] = fma(hi[c] - lo[c], v.s0, lo[c]);
+        }
+      }
+      __syncthreads();
       if (active) {
+#pragma unroll 2
         for (int ch = 0; ch < nch; ch++) {
-          const RaySample<Real> v = smp[ch];
-          const Real sin_el = fma(v.us, Dl, b0) * v.inv_r;  // p_s.l / |p_s|
+          const Real sin_el = fma(smp[ch].us, Dl, b0) * smp[ch].inv_r;  // p_s.l / |p_s|
           int u2;
           Real s2;
           split_coord_r<Real>(sun_elevation_index_r<Real>(sin_el, scale2), d.n2, &u2, &s2);
-          const int v2 = upper_index(u2, d.n2);
-          const Real* pl = plane + 3 * (long long)ch * ncell;
-          Real X[3];
-          mix4(pl + 3 * (u2 * d.n3 + u3), pl + 3 * (u2 * d.n3 + v3), pl + 3 * (v2 * d.n3 + u3),
-               pl + 3 * (v2 * d.n3 + v3), s2, s3, X);
+          const Real* lo = plane + 3 * ch * ncell + u2 * n3x3;
+          const Real* hi = u2 + 1 < d.n2 ? lo + n3x3 : lo;
+          Real* a = acc[ch & 1];
 #pragma unroll
-          for (int c = 0; c < 3; c++) kahan_add(acc[c], cmp[c], v.T[c] * X[c]);
+          for (int c = 0; c < 3; c++) {
+            const Real x0 = fma(lo[o3v + c] - lo[o3u + c], s3, lo[o3u + c]);
+            const Real x1 = fma(hi[o3v + c] - hi[o3u + c], s3, hi[o3u + c]);
+            a[c] = fma(smp[ch].T[c], fma(x1 - x0, s2, x0), a[c]);
+          }
         }
       }
     }
     if (active) {
       const Real w = (Real)(ri.L / d.S);
       Vec4<Real> o;
-      o.x = w * acc[0];
-      o.y = w * acc[1];
-      o.z = w * acc[2];
+      o.x = w * (acc[0][0] + acc[1][0]);
+      o.y = w * (acc[0][1] + acc[1][1]);
+      o.z = w * (acc[0][2] + acc[1][2]);
       o.w = 0;
       dS[node0 + cell] = o;
     }
@@ -456,7 +482,7 @@ template <class Real>
 int launch_ray_scatter(const AtmoParams* params, const BuildDims& d, const RowInfo* rowinfo,
                        const RowSample<Real>* rows, const CellGeom<Real>* geom, const Remap4<Real>* remap,
                        const Vec4<Real>* J, Vec4<Real>* dS, cudaStream_t st) {
-  constexpr int CH = 8;
+  constexpr int CH = 16;
   const int ncell = d.n2 * d.n3;
   const int block = ncell >= 256 ? 256 : ((ncell + 31) / 32) * 32;
   size_t smem = sizeof(RaySample<Real>) * CH + sizeof(Real) * 3 * (size_t)CH * ncell;
