@@ -163,6 +163,52 @@ int sfsim_atmo_last_timings(double* ms, int n);
 /* Number of kernel launches of the last build. */
 int sfsim_atmo_last_launch_count(void);
 
+/* ---- Queries of a built atmosphere ---------------------------------------
+ * A context builds the four tables of `cfg` on the current device and keeps
+ * them, with the point-scatter tables summed over the iterations, for
+ * queries.  Query inputs and outputs are DEVICE arrays of n [3] vectors; the
+ * work is queued on `stream`. */
+typedef struct sfsim_atmo_context sfsim_atmo_context;
+
+int sfsim_atmo_context_create(const sfsim_atmo_config* cfg, sfsim_atmo_context** ctx);
+int sfsim_atmo_context_destroy(sfsim_atmo_context* ctx);
+
+/* Device pointers (owned by the context) of the four tables, .scatter layout. */
+int sfsim_atmo_context_tables(const sfsim_atmo_context* ctx, float** transmittance,
+                              float** surface_radiance, float** ray_scatter, float** mie_strength);
+
+/* Device pointer of the point-scatter table summed over all iterations,
+ * [height][elevation][sun elevation][heading][4] floats (RGB + pad); NULL
+ * when the build has no iterations. */
+int sfsim_atmo_context_point_scatter_sum(const sfsim_atmo_context* ctx, float** jsum);
+
+/* Table lookups as sfsim's shaders perform them (FP32, clamped bilinear
+ * texture filtering; weight_bits 0 for exact weights or 8 for GL's 8-bit
+ * fixed-point weights), replacing resources/shaders/atmosphere/:
+ *   kind 0  transmittance-track.glsl  transmittance_track(a, b)
+ *   kind 1  transmittance-outer.glsl  transmittance_outer(a, b = direction)
+ *   kind 2  ray-scatter-track.glsl    ray_scatter_track(light, a, b)
+ *   kind 3  ray-scatter-outer.glsl    ray_scatter_outer(light, a, b = direction)
+ *   kind 4  in-scatter S + M phase(mie g, b.light) at point a, direction b,
+ *           table half chosen by is_above_horizon(a, b) */
+int sfsim_atmo_query_table(const sfsim_atmo_context* ctx, int kind, long long n, const float* a,
+                           const float* b, const float* light, float* out, int weight_bits,
+                           void* stream);
+
+/* Rendered in-scatter S + M phase(mie g, v.l) at position x, unit view v and
+ * unit sun l (FP64 inputs) by direct quadrature, without the 4-D table: the
+ * first order integrated at the point as atmosphere.clj:154-200 does, plus
+ * ray scatter of the summed point-scatter table (the higher orders). */
+int sfsim_atmo_query_direct(const sfsim_atmo_context* ctx, long long n, const double* x,
+                            const double* v, const double* l, float* out, void* stream);
+
+/* The surrogate's tensor-core GEMM, exposed for validation: C = A * B^T with
+ * A [M][K] and B [N][K] row-major bf16 DEVICE arrays and C [M][N] float,
+ * FP32 accumulation on tcgen05 tensor cores.  N <= 256; K a multiple of
+ * 64 * splits; splits > 1 divides K over CTAs and sums into C atomically. */
+int sfsim_atmo_gemm_bf16(const void* A, const void* B, float* C, int M, int N, long long K, int splits,
+                         void* stream);
+
 /* Work census of one build (no tables are written).  counts[0] = first-order
  * sun-ray integrals (node, ray-sample pairs with the sun above the sample's
  * horizon), [1] = their extinction samples, [2] = view-ray extinction

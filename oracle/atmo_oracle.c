@@ -1035,6 +1035,31 @@ void oracle_remap4_node(const sfsim_atmo_config* cfg, const double* table, int i
   node_remap4(&rc, idx, out);
 }
 
+/* Rendered in-scatter S + M phase(mie, v.l) at an arbitrary (x, v, l), the
+ * quantity the 4-D tables sample (ray-scatter-outer.glsl:18-20): the first
+ * order by ray-scatter with point-scatter-component / strength-component
+ * (atmosphere_lut.clj:68-78) and the higher orders by ray-scatter of the
+ * point-scatter table summed over the iterations (NULL: first order only).
+ * The table half is chosen by is-above-horizon?. */
+void oracle_rendered_inscatter(const sfsim_atmo_config* cfg, const double* Jsum, const double* x, const double* v,
+                               const double* l, double* out) {
+  build_t b; build_from_config(cfg, &b);
+  v3 X = vload(x), Vd = vload(v), L = vload(l);
+  int above = is_above_horizon(&b.planet, X, Vd);
+  j0_ctx jr = {&b.planet, b.comps, 2, &b.comps[1], b.ray_steps, b.intensity, 0};
+  j0_ctx jm = {&b.planet, b.comps, 2, &b.comps[0], b.ray_steps, b.intensity, 1};
+  v3 s1 = ray_scatter(&b.planet, b.comps, 2, b.ray_steps, j0_fn, &jr, X, Vd, L, above);
+  v3 m = ray_scatter(&b.planet, b.comps, 2, b.ray_steps, j0_fn, &jm, X, Vd, L, above);
+  v3 r = add(s1, mult(m, phase(b.comps[0].g, dot(Vd, L))));
+  if (Jsum) {
+    table_t t;
+    tab4(&t, &b, Jsum);
+    interp4_ctx f = {&b.planet, b.sshape, &t, NULL, 0.0, 0};
+    r = add(r, ray_scatter(&b.planet, b.comps, 2, b.ray_steps, interp4_fn, &f, X, Vd, L, above));
+  }
+  vstore(out, r);
+}
+
 /* ------------------------------------------------------------------------ */
 /* Exported unit functions for the known-answer tests                        */
 /* ------------------------------------------------------------------------ */
@@ -1502,6 +1527,13 @@ static f3 ray_scatter_outer_f(const glsl_env* e, f3 light, f3 point, f3 directio
   return in_scatter_at_f(e, idx, fdot(direction, light));
 }
 
+/* in-scatter at (point, direction) with the horizon test choosing the half */
+static f3 in_scatter_query_f(const glsl_env* e, f3 light, f3 point, f3 direction) {
+  float idx[4];
+  ray_scatter_forward_f(e, point, direction, light, is_above_horizon_f(e, point, direction), idx);
+  return in_scatter_at_f(e, idx, fdot(direction, light));
+}
+
 /* kind 0: transmittance_track(p, q); 1: transmittance_outer(p, d);
  * 2: ray_scatter_track(light, p, q); 3: ray_scatter_outer(light, p, d) */
 void oracle_glsl_query(const oracle_glsl_tables* t, int kind, const float* light, const float* p, const float* q,
@@ -1515,7 +1547,8 @@ void oracle_glsl_query(const oracle_glsl_tables* t, int kind, const float* light
     case 0: r = transmittance_track_f(&e, P, Q); break;
     case 1: r = transmittance_outer_f(&e, P, Q); break;
     case 2: r = ray_scatter_track_f(&e, L, P, Q); break;
-    default: r = ray_scatter_outer_f(&e, L, P, Q); break;
+    case 3: r = ray_scatter_outer_f(&e, L, P, Q); break;
+    default: r = in_scatter_query_f(&e, L, P, Q); break;
   }
   out[0] = r.x; out[1] = r.y; out[2] = r.z;
 }

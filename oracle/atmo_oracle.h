@@ -57,6 +57,11 @@ void oracle_surface_radiance_node(const sfsim_atmo_config* cfg, const double* dS
 void oracle_remap4_node(const sfsim_atmo_config* cfg, const double* table, int i, int j, int k, int a,
                         double* out);
 
+/* Rendered in-scatter S + M phase at an arbitrary (x, v, l); Jsum is the
+ * point-scatter table summed over the iterations or NULL. */
+void oracle_rendered_inscatter(const sfsim_atmo_config* cfg, const double* Jsum, const double* x, const double* v,
+                               const double* l, double* out);
+
 /* Tables for the GLSL restatement. */
 typedef struct {
   float radius, max_height;

@@ -397,10 +397,18 @@ def remap4_node(cfg, table, i, j, k, a):
     return np.array(o[:])
 
 
+def rendered_inscatter(cfg, x, v, l, jsum=None):
+    o = _out3()
+    js = _c64(jsum) if jsum is not None else None
+    lib().oracle_rendered_inscatter(ctypes.byref(cfg), _dptr(js), _v(x), _v(v), _v(l), o)
+    return np.array(o[:])
+
+
 # --- GLSL consumer restatement --------------------------------------------------
 
 def glsl_query(tables: dict, kind: int, light, p, q, weight_bits: int = 0):
-    """kind 0 transmittance_track, 1 transmittance_outer, 2 ray_scatter_track, 3 ray_scatter_outer."""
+    """kind 0 transmittance_track, 1 transmittance_outer, 2 ray_scatter_track, 3 ray_scatter_outer,
+    4 in-scatter at (p, direction q) with the horizon test choosing the table half."""
     T = np.ascontiguousarray(tables["transmittance"], dtype=np.float32)
     S = np.ascontiguousarray(tables["ray_scatter"], dtype=np.float32)
     M = np.ascontiguousarray(tables["mie_strength"], dtype=np.float32)

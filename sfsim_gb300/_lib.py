@@ -22,7 +22,9 @@ EXPORTS = (
     "sfsim_atmo_build_device", "sfsim_atmo_build_batch", "sfsim_atmo_build_debug", "sfsim_atmo_set_timing",
     "sfsim_atmo_last_timings", "sfsim_atmo_last_launch_count", "sfsim_atmo_release", "sfsim_atmo_strerror",
     "sfsim_atmo_last_error", "sfsim_atmo_version", "sfsim_atmo_census", "sfsim_atmo_sfu_peak",
-    "sfsim_atmo_build_static",
+    "sfsim_atmo_build_static", "sfsim_atmo_context_create", "sfsim_atmo_context_destroy",
+    "sfsim_atmo_context_tables", "sfsim_atmo_context_point_scatter_sum", "sfsim_atmo_query_table",
+    "sfsim_atmo_query_direct", "sfsim_atmo_gemm_bf16",
 )
 
 
@@ -72,6 +74,14 @@ def load(build: bool = False):
     L.sfsim_atmo_last_error.restype = ctypes.c_char_p
     L.sfsim_atmo_census.argtypes = [_cfgp, ctypes.POINTER(ctypes.c_ulonglong), ctypes.c_int]
     L.sfsim_atmo_sfu_peak.argtypes = [ctypes.POINTER(ctypes.c_double)]
+    vp = ctypes.c_void_p
+    L.sfsim_atmo_context_create.argtypes = [_cfgp, ctypes.POINTER(vp)]
+    L.sfsim_atmo_context_destroy.argtypes = [vp]
+    L.sfsim_atmo_context_tables.argtypes = [vp] + [ctypes.POINTER(vp)] * 4
+    L.sfsim_atmo_context_point_scatter_sum.argtypes = [vp, ctypes.POINTER(vp)]
+    L.sfsim_atmo_query_table.argtypes = [vp, ctypes.c_int, ctypes.c_longlong, vp, vp, vp, vp, ctypes.c_int, vp]
+    L.sfsim_atmo_query_direct.argtypes = [vp, ctypes.c_longlong, vp, vp, vp, vp, vp]
+    L.sfsim_atmo_gemm_bf16.argtypes = [vp, vp, vp, ctypes.c_int, ctypes.c_int, ctypes.c_longlong, ctypes.c_int, vp]
     L.sfsim_atmo_version.argtypes = []
     L.sfsim_atmo_version.restype = ctypes.c_char_p
     _lib = L

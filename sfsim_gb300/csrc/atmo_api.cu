@@ -119,6 +119,41 @@ void sphere_directions(int theta_steps, int phi_steps, double range, std::vector
 // h(q) = q / (R + sqrt(R^2 + q)) = q * f(q); f is interpolated at 5
 // Chebyshev nodes over q in [-0.01, 1.05] * (top^2 - R^2) and stored as a
 // polynomial in z = q * alpha + beta, z in [-1, 1].
+// Chebyshev interpolant of f(q) = 1/(R + sqrt(R^2 + q)) with N nodes on
+// [qlo, qhi], as monomial coefficients in z = q alpha + beta; returns the
+// largest relative error on a fine grid.
+double chebyshev_height_fit(const AtmoParams& P, int N, double qlo, double qhi, double* mono) {
+  const double alpha = 2.0 / (qhi - qlo), beta = -(qhi + qlo) / (qhi - qlo);
+  auto f = [&](double q) { return 1.0 / (P.R + std::sqrt(P.R2 + q)); };
+  double cheb[8] = {};
+  for (int j = 0; j < N; j++) {
+    double s = 0;
+    for (int k = 0; k < N; k++) {
+      const double t = M_PI * (k + 0.5) / N;
+      s += f((std::cos(t) - beta) / alpha) * std::cos(j * t);
+    }
+    cheb[j] = s * (j == 0 ? 1.0 : 2.0) / N;
+  }
+  double T[8][8] = {};
+  T[0][0] = 1;
+  T[1][1] = 1;
+  for (int j = 2; j < N; j++)
+    for (int k = 0; k < N; k++) T[j][k] = (k > 0 ? 2 * T[j - 1][k - 1] : 0) - T[j - 2][k];
+  for (int k = 0; k < N; k++) {
+    mono[k] = 0;
+    for (int j = 0; j < N; j++) mono[k] += cheb[j] * T[j][k];
+  }
+  double worst = 0;
+  for (int k = 0; k <= 1000; k++) {
+    const double q = qlo + (qhi - qlo) * k / 1000.0;
+    const double z = q * alpha + beta;
+    double p = mono[N - 1];
+    for (int m = N - 2; m >= 0; m--) p = p * z + mono[m];
+    worst = std::fmax(worst, std::fabs(p / f(q) - 1));
+  }
+  return worst;
+}
+
 int fit_height_polynomial(AtmoParams& P) {
   constexpr int N = 5;
   const double qlo = -0.01 * P.Hh2, qhi = 1.05 * P.Hh2;
@@ -161,6 +196,12 @@ int fit_height_polynomial(AtmoParams& P) {
   for (int k = 0; k < kMaxHPoly; k++) {
     P.d_hpr[k] = P.d_hpoly[k] * kr;
     P.f_hpr[k] = (float)P.d_hpr[k];
+  }
+  {
+    double mono4[8];
+    if (chebyshev_height_fit(P, 4, qlo, qhi, mono4) > 1e-7)
+      return fail(SFSIM_ATMO_EINVAL, "atmosphere too thick for the degree-3 height polynomial");
+    for (int k = 0; k < 4; k++) P.f_hpr4[k] = (float)(mono4[k] * kr);
   }
   P.d_hratio = P.ray_scale / P.mie_scale;
   P.f_hratio = (float)P.d_hratio;
@@ -376,7 +417,7 @@ struct Timer {
 // device memory; outputs are device pointers in the .scatter layout.
 template <class Real>
 int run_build(const Work<Real>& w, const BuildDims& d, float* oT, float* oE, float* oS, float* oM, cudaStream_t st,
-              Timer& tm, const sfsim_atmo_intermediates* inter) {
+              Timer& tm, const sfsim_atmo_intermediates* inter, Vec4<float>* jsum = nullptr) {
   int launches = 0;
   tm.mark_begin(0);
   launch_setup<Real>(w.params, d, w.dirs, w.ring_end, w.setup, st);
@@ -418,6 +459,10 @@ int run_build(const Work<Real>& w, const BuildDims& d, float* oT, float* oE, flo
       return fail(SFSIM_ATMO_ECUDA, "point scatter launch configuration failed");
     launches++;
     tm.mark_end();
+    if (jsum) {
+      launch_add_to_sum<Real>(d.B * d.n4(), w.J, jsum, it == 0, st);
+      launches++;
+    }
     tm.mark_begin(6);
     launch_surface_radiance<Real>(w.params, d, w.hdirs, dS_prev, M_first, dE_new, st);
     launches++;
@@ -780,6 +825,71 @@ const char* sfsim_atmo_version(void) { return "sfsim-atmo-gb300 0.1.0 (sm_103a)"
 }  // extern "C"
 
 // ---------------------------------------------------------------------------
+// Contexts: a built atmosphere kept on the device for queries.
+// ---------------------------------------------------------------------------
+
+struct sfsim_atmo_context {
+  int dev;
+  sfsim_atmo_config cfg;
+  BuildDims dims;
+  void* mem;
+  AtmoParams* params;
+  float *T, *E, *S, *M;
+  Vec4<float>* jsum;  // point scatter summed over the iterations, NULL without iterations
+};
+
+namespace {
+
+template <class Real>
+int context_build(sfsim_atmo_context* c) {
+  int rc = 0;
+  const sfsim_atmo_config& cfg = c->cfg;
+  BuildDims d = make_dims(cfg, 1);
+  if ((rc = check_smem<Real>(d))) return rc;
+  AtmoParams hp;
+  if ((rc = make_params(cfg, hp))) return rc;
+  std::vector<DirLocal> dirs, hdirs;
+  std::vector<int> ring_end, hring;
+  sphere_directions(cfg.sphere_steps >> 1, cfg.sphere_steps, M_PI, dirs, ring_end);
+  sphere_directions(cfg.ray_steps >> 2, cfg.ray_steps, M_PI / 2, hdirs, hring);
+  Work<Real> w;
+  const size_t wbytes = carve<Real>(w, nullptr, d, true);
+  const size_t total = wbytes + sizeof(Vec4<float>) * (size_t)d.n4() + 256;
+  cudaError_t e = cudaMalloc(&c->mem, total);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    c->mem = nullptr;
+    return fail(SFSIM_ATMO_ENOMEM, std::string("cudaMalloc of the context failed: ") + cudaGetErrorString(e));
+  }
+  carve<Real>(w, (char*)c->mem, d, true);
+  c->jsum = cfg.iterations > 0 ? reinterpret_cast<Vec4<float>*>((char*)c->mem + ((wbytes + 255) & ~size_t(255)))
+                               : nullptr;
+  cudaStream_t st = g_stream[c->dev];
+  CUDA_TRY(cudaMemcpyAsync(w.params, &hp, sizeof(AtmoParams), cudaMemcpyHostToDevice, st));
+  if (!dirs.empty()) {
+    CUDA_TRY(cudaMemcpyAsync(w.dirs, dirs.data(), sizeof(DirLocal) * dirs.size(), cudaMemcpyHostToDevice, st));
+    CUDA_TRY(cudaMemcpyAsync(w.ring_end, ring_end.data(), sizeof(int) * ring_end.size(), cudaMemcpyHostToDevice, st));
+  }
+  if (!hdirs.empty())
+    CUDA_TRY(cudaMemcpyAsync(w.hdirs, hdirs.data(), sizeof(DirLocal) * hdirs.size(), cudaMemcpyHostToDevice, st));
+  Timer tm;
+  tm.dev = c->dev;
+  tm.st = st;
+  tm.n = 512;  // no stage timings for context builds
+  if ((rc = run_build<Real>(w, d, w.oT, w.oE, w.oS, w.oM, st, tm, nullptr, c->jsum))) return rc;
+  CUDA_TRY(cudaStreamSynchronize(st));
+  c->dims = d;
+  c->params = w.params;
+  c->T = w.oT;
+  c->E = w.oE;
+  c->S = w.oS;
+  c->M = w.oM;
+  return 0;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
 // Allocation-free build.  Some callers cannot call cudaMalloc: code running
 // inside a CUDA-graph capture or under a memory budget fixed at start-up, or
 // engines whose allocator owns every device byte.  For them this entry point
@@ -859,4 +969,118 @@ extern "C" int sfsim_atmo_build_static(const sfsim_atmo_config* cfg, float* T, f
   std::lock_guard<std::mutex> lock(g_mutex);
   if (cfg->precision == SFSIM_ATMO_FP64) return build_static_impl<double>(*cfg, T, E, S, M, (cudaStream_t)stream);
   return build_static_impl<float>(*cfg, T, E, S, M, (cudaStream_t)stream);
+}
+
+extern "C" {
+
+int sfsim_atmo_context_create(const sfsim_atmo_config* cfg, sfsim_atmo_context** out) {
+  if (!out) return fail(SFSIM_ATMO_ENULL, "out is NULL");
+  *out = nullptr;
+  int rc = validate(cfg);
+  if (rc) return rc;
+  std::lock_guard<std::mutex> lock(g_mutex);
+  int dev = 0;
+  if ((rc = current_device(&dev))) return rc;
+  if ((rc = ensure_stream(dev))) return rc;
+  sfsim_atmo_context* c = new sfsim_atmo_context();
+  c->dev = dev;
+  c->cfg = *cfg;
+  c->mem = nullptr;
+  rc = cfg->precision == SFSIM_ATMO_FP64 ? context_build<double>(c) : context_build<float>(c);
+  if (rc) {
+    if (c->mem) cudaFree(c->mem);
+    delete c;
+    return rc;
+  }
+  *out = c;
+  return 0;
+}
+
+int sfsim_atmo_context_destroy(sfsim_atmo_context* ctx) {
+  if (!ctx) return 0;
+  int cur = 0;
+  cudaGetDevice(&cur);
+  cudaSetDevice(ctx->dev);
+  cudaError_t e = ctx->mem ? cudaFree(ctx->mem) : cudaSuccess;
+  cudaSetDevice(cur);
+  delete ctx;
+  if (e != cudaSuccess) return fail(SFSIM_ATMO_ECUDA, std::string("cudaFree: ") + cudaGetErrorString(e));
+  return 0;
+}
+
+int sfsim_atmo_context_tables(const sfsim_atmo_context* ctx, float** T, float** E, float** S, float** M) {
+  if (!ctx) return fail(SFSIM_ATMO_ENULL, "context is NULL");
+  if (T) *T = ctx->T;
+  if (E) *E = ctx->E;
+  if (S) *S = ctx->S;
+  if (M) *M = ctx->M;
+  return 0;
+}
+
+int sfsim_atmo_context_point_scatter_sum(const sfsim_atmo_context* ctx, float** jsum) {
+  if (!ctx || !jsum) return fail(SFSIM_ATMO_ENULL, "NULL argument");
+  *jsum = reinterpret_cast<float*>(ctx->jsum);
+  return 0;
+}
+
+int sfsim_atmo_query_table(const sfsim_atmo_context* ctx, int kind, long long n, const float* a, const float* b,
+                           const float* light, float* out, int weight_bits, void* stream) {
+  if (!ctx) return fail(SFSIM_ATMO_ENULL, "context is NULL");
+  if (kind < 0 || kind > 4) return fail(SFSIM_ATMO_EINVAL, "query kind must be in [0, 4]");
+  if (weight_bits < 0 || weight_bits > 16) return fail(SFSIM_ATMO_EINVAL, "weight_bits must be in [0, 16]");
+  if (n < 0) return fail(SFSIM_ATMO_EINVAL, "n must be non-negative");
+  if (n == 0) return 0;
+  if (!a || !b || !out || (kind >= 2 && !light)) return fail(SFSIM_ATMO_ENULL, "a point array is NULL");
+  QueryTables q;
+  q.radius = (float)ctx->cfg.radius;
+  q.max_height = (float)ctx->cfg.height;
+  q.mie_g = (float)ctx->cfg.mie.scatter_g;
+  q.t_height = ctx->dims.nT0;
+  q.t_elevation = ctx->dims.nT1;
+  q.height = ctx->dims.n0;
+  q.elevation = ctx->dims.n1;
+  q.light = ctx->dims.n2;
+  q.heading = ctx->dims.n3;
+  q.T = ctx->T;
+  q.S = ctx->S;
+  q.M = ctx->M;
+  launch_query_table(q, kind, n, a, b, light, out, weight_bits, (cudaStream_t)stream);
+  CUDA_TRY(cudaGetLastError());
+  return 0;
+}
+
+int sfsim_atmo_query_direct(const sfsim_atmo_context* ctx, long long n, const double* x, const double* v,
+                            const double* l, float* out, void* stream) {
+  if (!ctx) return fail(SFSIM_ATMO_ENULL, "context is NULL");
+  if (n < 0) return fail(SFSIM_ATMO_EINVAL, "n must be non-negative");
+  if (n == 0) return 0;
+  if (!x || !v || !l || !out) return fail(SFSIM_ATMO_ENULL, "a point array is NULL");
+  launch_query_direct(ctx->params, ctx->dims, ctx->jsum, n, x, v, l, out, (cudaStream_t)stream);
+  CUDA_TRY(cudaGetLastError());
+  return 0;
+}
+
+}  // extern "C"
+
+extern "C" int sfsim_atmo_gemm_bf16(const void* A, const void* B, float* C, int M, int N, long long K, int splits,
+                                    void* stream) {
+  if (!A || !B || !C) return fail(SFSIM_ATMO_ENULL, "a matrix pointer is NULL");
+  if (M < 1 || N < 1 || N > 256 || K < 64 || splits < 1 || K % (64LL * splits) != 0)
+    return fail(SFSIM_ATMO_EINVAL, "need M >= 1, 1 <= N <= 256, K a multiple of 64 * splits");
+  GemmArgs g = {};
+  g.A = (const __nv_bfloat16*)A;
+  g.lda = K;
+  g.B = (const __nv_bfloat16*)B;
+  g.ldb = K;
+  g.M = M;
+  g.N = N;
+  g.K = K;
+  g.alpha = 1.0f;
+  g.ldc = N;
+  if (splits > 1) g.Cacc = C;
+  else g.Cf32 = C;
+  if (splits > 1) CUDA_TRY(cudaMemsetAsync(C, 0, sizeof(float) * (size_t)M * N, (cudaStream_t)stream));
+  if (launch_gemm_tn(g, splits, (cudaStream_t)stream)) return fail(SFSIM_ATMO_ECUDA, "GEMM launch configuration failed");
+  CUDA_TRY(cudaGetLastError());
+  return 0;
 }

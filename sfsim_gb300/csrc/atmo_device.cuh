@@ -296,7 +296,8 @@ struct Bulk<float> {
   }
   static __device__ __forceinline__ float div(float a, float b) { return __fdividef(a, b); }
   static __device__ __forceinline__ const float* hpoly(const AtmoParams& P) { return P.f_hpoly; }
-  static __device__ __forceinline__ const float* hpr(const AtmoParams& P) { return P.f_hpr; }
+  static constexpr int kSunNP = 4;  // the FP32 sun-ray loop uses the degree-3 fit
+  static __device__ __forceinline__ const float* hpr(const AtmoParams& P) { return P.f_hpr4; }
   static __device__ __forceinline__ float hratio(const AtmoParams& P) { return P.f_hratio; }
   static __device__ __forceinline__ float alpha(const AtmoParams& P) { return P.f_alpha; }
   static __device__ __forceinline__ float beta(const AtmoParams& P) { return P.f_beta; }
@@ -313,6 +314,7 @@ struct Bulk<double> {
   static __device__ __forceinline__ double rsqrt(double x) { return 1.0 / ::sqrt(x); }
   static __device__ __forceinline__ double div(double a, double b) { return a / b; }
   static __device__ __forceinline__ const double* hpoly(const AtmoParams& P) { return P.d_hpoly; }
+  static constexpr int kSunNP = 5;
   static __device__ __forceinline__ const double* hpr(const AtmoParams& P) { return P.d_hpr; }
   static __device__ __forceinline__ double hratio(const AtmoParams& P) { return P.d_hratio; }
   static __device__ __forceinline__ double alpha(const AtmoParams& P) { return P.d_alpha; }
@@ -380,13 +382,21 @@ __device__ __forceinline__ void sun_sums(Real q0, Real b, Real dt, int steps, co
   const Real A = fma(dt, fma(Real(0.25), dt, b), q0);
   const Real B = dt * fma(Real(2), b, dt);
   const Real C = dt * dt;
+  // sample n = 4m + u: q = A_u + f (B_u + f C) with f = 4m, A_u = A + u (B + u C),
+  // B_u = B + 2 u C, so the counter f advances once per four samples
+  Real Au[4], Bu[4];
+#pragma unroll
+  for (int u = 0; u < 4; u++) {
+    Au[u] = fma(Real(u), fma(Real(u), C, B), A);
+    Bu[u] = fma(Real(2 * u), C, B);
+  }
   Real sr[4] = {0, 0, 0, 0}, sm[4] = {0, 0, 0, 0};
-  Real fn = 0;
+  Real f = 0;
   int n = 0;
   for (; n + 4 <= steps; n += 4) {
 #pragma unroll
     for (int u = 0; u < 4; u++) {
-      const Real q = fma(fn, fma(fn, C, B), A);
+      const Real q = fma(f, fma(f, C, Bu[u]), Au[u]);
       const Real z = fma(q, alpha, beta);
       Real p = pr[NP - 1];
 #pragma unroll
@@ -394,10 +404,11 @@ __device__ __forceinline__ void sun_sums(Real q0, Real b, Real dt, int steps, co
       const Real xr = q * p;
       sr[u] += Bulk<Real>::exp2(xr);
       sm[u] += Bulk<Real>::exp2(xr * ratio);
-      fn += Real(1);
     }
+    f += Real(4);
   }
   for (; n < steps; n++) {
+    const Real fn = Real(n);
     const Real q = fma(fn, fma(fn, C, B), A);
     const Real z = fma(q, alpha, beta);
     Real p = pr[NP - 1];
@@ -406,7 +417,6 @@ __device__ __forceinline__ void sun_sums(Real q0, Real b, Real dt, int steps, co
     const Real xr = q * p;
     sr[0] += Bulk<Real>::exp2(xr);
     sm[0] += Bulk<Real>::exp2(xr * ratio);
-    fn += Real(1);
   }
   sum_r = (sr[0] + sr[1]) + (sr[2] + sr[3]);
   sum_m = (sm[0] + sm[1]) + (sm[2] + sm[3]);
@@ -484,6 +494,79 @@ __device__ __forceinline__ void mix4(const Real* a, const Real* b, const Real* c
     Real hi = c[ch] * (Real(1) - s_inner) + d[ch] * s_inner;
     out[ch] = lo * (Real(1) - s_outer) + hi * s_outer;
   }
+}
+
+// ---------------------------------------------------------------------------
+// Table gathers
+// ---------------------------------------------------------------------------
+
+// Index of a 4-D texel.
+__device__ __forceinline__ long long idx4(const BuildDims& d, int i, int j, int k, int a) {
+  return (((long long)i * d.n1 + j) * d.n2 + k) * d.n3 + a;
+}
+
+template <class Real>
+__device__ __forceinline__ void ld3(const Vec4<Real>* t, long long i, Real o[3]) {
+  Vec4<Real> v = t[i];
+  o[0] = v.x;
+  o[1] = v.y;
+  o[2] = v.z;
+}
+
+template <class Real>
+__device__ __forceinline__ void mix3(const Real* a, const Real* b, Real s, Real* o) {
+#pragma unroll
+  for (int c = 0; c < 3; c++) o[c] = a[c] * (Real(1) - s) + b[c] * s;
+}
+
+// Clamped quadrilinear interpolation of a 4-D table (interpolate.clj:87-98:
+// the innermost dimension is mixed first).
+template <class Real>
+__device__ inline void interp4(const Vec4<Real>* t, const BuildDims& d, const int* u, const Real* s, Real out[3]) {
+  const int v[4] = {upper_index(u[0], d.n0), upper_index(u[1], d.n1), upper_index(u[2], d.n2),
+                    upper_index(u[3], d.n3)};
+  Real rh[2][3];
+#pragma unroll
+  for (int h = 0; h < 2; h++) {
+    Real re[2][3];
+#pragma unroll
+    for (int e = 0; e < 2; e++) {
+      Real rk[2][3];
+#pragma unroll
+      for (int k = 0; k < 2; k++) {
+        Real A[3], B[3];
+        const int ih = h ? v[0] : u[0], ie = e ? v[1] : u[1], ik = k ? v[2] : u[2];
+        ld3(t, idx4(d, ih, ie, ik, u[3]), A);
+        ld3(t, idx4(d, ih, ie, ik, v[3]), B);
+        mix3(A, B, s[3], rk[k]);
+      }
+      mix3(rk[0], rk[1], s[2], re[e]);
+    }
+    mix3(re[0], re[1], s[1], rh[h]);
+  }
+  mix3(rh[0], rh[1], s[0], out);
+}
+
+template <class Real>
+__device__ inline void interp2(const Vec4<Real>* t, int n0, int n1, const int* u, const Real* s, Real out[3]) {
+  const int v0 = upper_index(u[0], n0), v1 = upper_index(u[1], n1);
+  Real A[3], B[3], lo[3], hi[3];
+  ld3(t, (long long)u[0] * n1 + u[1], A);
+  ld3(t, (long long)u[0] * n1 + v1, B);
+  mix3(A, B, s[1], lo);
+  ld3(t, (long long)v0 * n1 + u[1], A);
+  ld3(t, (long long)v0 * n1 + v1, B);
+  mix3(A, B, s[1], hi);
+  mix3(lo, hi, s[0], out);
+}
+
+// (1 - exp(-3 s - 0.6)) / (1 - exp(-3.6)) clamped at 0, times (size - 1)
+// (sun-elevation-to-index, atmosphere.clj:322-326) in Real.
+template <class Real>
+__device__ __forceinline__ Real sun_elevation_index_r(Real sin_el, Real scale) {
+  const Real e = Bulk<Real>::exp2((Real(3) * sin_el + Real(0.6)) * Real(-1.4426950408889634));
+  const Real r = (Real(1) - e) * scale;
+  return r > Real(0) ? r : Real(0);
 }
 
 }  // namespace sfsim

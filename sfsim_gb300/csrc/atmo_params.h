@@ -39,6 +39,7 @@ struct AtmoParams {
   float f_hpoly[kMaxHPoly];
   float f_alpha, f_beta;
   float f_hpr[kMaxHPoly];
+  float f_hpr4[4];                    // degree-3 fit of the same, for the FP32 sun-ray loop
   float f_hratio;
   float f_R, f_Hh2, f_mie_g;
   float f_bright_pi[3];               // brightness / pi

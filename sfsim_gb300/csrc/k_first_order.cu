@@ -81,10 +81,11 @@ __global__ void __launch_bounds__(WARPS * 32, 4) k_first_order(const AtmoParams*
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int ncell = d.n2 * d.n3;
   const Real Hh2 = (Real)P.Hh2;
+  constexpr int NP = Bulk<Real>::kSunNP;
   const Real* hp = Bulk<Real>::hpr(P);
-  Real hc[5];
+  Real hc[NP];
 #pragma unroll
-  for (int c = 0; c < 5; c++) hc[c] = hp[c];
+  for (int c = 0; c < NP; c++) hc[c] = hp[c];
   const Real alpha = Bulk<Real>::alpha(P), beta = Bulk<Real>::beta(P);
   const Real ratio = Bulk<Real>::hratio(P);
   Real rext[3], mext[3];
@@ -115,7 +116,7 @@ __global__ void __launch_bounds__(WARPS * 32, 4) k_first_order(const AtmoParams*
         texit = fmax(texit, Real(0));
         const Real dt = texit * inv_steps;
         Real sr, smie;
-        sun_sums<Real, 5>(q, bp, dt, S, hc, alpha, beta, ratio, sr, smie);
+        sun_sums<Real, NP>(q, bp, dt, S, hc, alpha, beta, ratio, sr, smie);
 #pragma unroll
         for (int c = 0; c < 3; c++) {
           const Real tau = sm[s].tau[c] + dt * (rext[c] * sr + mext[c] * smie);

@@ -1,0 +1,221 @@
+// k_mlp.cu -- CUDA-core kernels of the ray-scatter surrogate: a Fourier-
+// feature MLP over the four table coordinates (height, elevation, sun
+// elevation, sun heading; each in [0, 1]) with 4 x 256 SiLU hidden layers and
+// 3 log-RGB outputs.  The hidden-layer GEMMs run on the tensor cores
+// (k_gemm.cu); these kernels do the features, the 256 -> 3 head, the loss,
+// bias gradients, Adam and the sampling of training batches.
+#include <cuda_bf16.h>
+
+#include "atmo_device.cuh"
+#include "kernels.h"
+
+namespace sfsim {
+
+// Frequencies of the features: pi * 2^(k/2), k = 0..15.
+__device__ __forceinline__ float feature_frequency(int k) { return exp2f(0.5f * (float)k); }
+
+// F[i][32 d + 2 k] = sin(pi f_k u_d), F[i][32 d + 2 k + 1] = cos(pi f_k u_d);
+// also the transpose FT[128][n] when requested.
+__global__ void k_features(long long n, const float* __restrict__ coords, __nv_bfloat16* __restrict__ F,
+                           __nv_bfloat16* __restrict__ FT) {
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t >= n * kMlpIn / 2) return;
+  const long long i = t / (kMlpIn / 2);
+  const int f = (int)(t % (kMlpIn / 2));  // 0..63 = d * 16 + k
+  const int d = f >> 4, k = f & 15;
+  float s, c;
+  sincospif(feature_frequency(k) * coords[i * 4 + d], &s, &c);
+  const __nv_bfloat16 bs = __float2bfloat16(s), bc = __float2bfloat16(c);
+  F[i * kMlpIn + 2 * f] = bs;
+  F[i * kMlpIn + 2 * f + 1] = bc;
+  if (FT) {
+    FT[(long long)(2 * f) * n + i] = bs;
+    FT[(long long)(2 * f + 1) * n + i] = bc;
+  }
+}
+
+// out[i][c] = sum_j H[i][j] W5[c][j] + b5[c]; one warp per row.
+__global__ void k_head_forward(long long n, const __nv_bfloat16* __restrict__ H, const float* __restrict__ W5,
+                               const float* __restrict__ b5, float* __restrict__ out) {
+  const long long row = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (row >= n) return;
+  float acc[3] = {0, 0, 0};
+  for (int j = lane; j < kMlpHidden; j += 32) {
+    const float h = __bfloat162float(H[row * kMlpHidden + j]);
+#pragma unroll
+    for (int c = 0; c < 3; c++) acc[c] = fmaf(h, W5[c * kMlpHidden + j], acc[c]);
+  }
+#pragma unroll
+  for (int c = 0; c < 3; c++) {
+    for (int o = 16; o > 0; o >>= 1) acc[c] += __shfl_xor_sync(0xffffffffu, acc[c], o);
+    if (lane == 0) out[row * 3 + c] = acc[c] + b5[c];
+  }
+}
+
+// Mean squared error over rows and channels: dout = 2 (out - target) / (3 n),
+// loss += sum (out - target)^2 / (3 n).
+__global__ void k_loss_grad(long long n, const float* __restrict__ out, const float* __restrict__ target,
+                            float* __restrict__ dout, float* __restrict__ loss) {
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  float e2 = 0;
+  if (t < 3 * n) {
+    const float e = out[t] - target[t];
+    dout[t] = 2.0f * e / (3.0f * (float)n);
+    e2 = e * e / (3.0f * (float)n);
+  }
+  for (int o = 16; o > 0; o >>= 1) e2 += __shfl_xor_sync(0xffffffffu, e2, o);
+  if ((threadIdx.x & 31) == 0 && e2 != 0.0f) atomicAdd(loss, e2);
+}
+
+// Backward of the head: dZ4[i][j] = (sum_c dout[i][c] W5[c][j]) * dsilu4[i][j]
+// (BF16, also transposed), and dW5 += dout^T H4, db5 += sum dout.
+__global__ void k_head_backward(long long n, const float* __restrict__ dout, const __nv_bfloat16* __restrict__ H,
+                                const float* __restrict__ W5, const float* __restrict__ dsilu,
+                                __nv_bfloat16* __restrict__ dZ, __nv_bfloat16* __restrict__ dZT,
+                                float* __restrict__ dW5, float* __restrict__ db5) {
+  __shared__ float sW[3 * kMlpHidden];
+  __shared__ float sdW[3 * kMlpHidden];
+  for (int t = threadIdx.x; t < 3 * kMlpHidden; t += blockDim.x) {
+    sW[t] = W5[t];
+    sdW[t] = 0;
+  }
+  __syncthreads();
+  // thread = hidden unit j; the block walks a range of rows
+  const int j = threadIdx.x;  // blockDim.x == kMlpHidden
+  const long long rows_per_block = (n + gridDim.x - 1) / gridDim.x;
+  const long long r0 = blockIdx.x * rows_per_block, r1 = min(n, r0 + rows_per_block);
+  float gw[3] = {0, 0, 0}, gb[3] = {0, 0, 0};
+  for (long long i = r0; i < r1; i++) {
+    const float d0 = dout[i * 3], d1 = dout[i * 3 + 1], d2 = dout[i * 3 + 2];
+    const float h = __bfloat162float(H[i * kMlpHidden + j]);
+    gw[0] = fmaf(d0, h, gw[0]);
+    gw[1] = fmaf(d1, h, gw[1]);
+    gw[2] = fmaf(d2, h, gw[2]);
+    if (j == 0) {
+      gb[0] += d0;
+      gb[1] += d1;
+      gb[2] += d2;
+    }
+    const float dh = fmaf(d0, sW[j], fmaf(d1, sW[kMlpHidden + j], d2 * sW[2 * kMlpHidden + j]));
+    const __nv_bfloat16 dz = __float2bfloat16(dh * dsilu[i * kMlpHidden + j]);
+    dZ[i * kMlpHidden + j] = dz;
+    dZT[(long long)j * n + i] = dz;
+  }
+#pragma unroll
+  for (int c = 0; c < 3; c++) atomicAdd(dW5 + c * kMlpHidden + j, gw[c]);
+  if (j == 0) {
+#pragma unroll
+    for (int c = 0; c < 3; c++) atomicAdd(db5 + c, gb[c]);
+  }
+}
+
+// db[j] += sum_i dZT[j][i] (the transposed gradients make the rows contiguous)
+__global__ void k_bias_grad(long long n, int width, const __nv_bfloat16* __restrict__ dZT, float* __restrict__ db) {
+  const int j = blockIdx.x;
+  float s = 0;
+  for (long long i = threadIdx.x; i < n; i += blockDim.x) s += __bfloat162float(dZT[(long long)j * n + i]);
+  __shared__ float red[256];
+  red[threadIdx.x] = s;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) db[j] += red[0];
+  (void)width;
+}
+
+// Adam with bias correction on FP32 master weights; refreshes the BF16
+// copy W_bf16 [rows][cols] and its transpose WT_bf16 [cols][rows] when given.
+__global__ void k_adam(long long count, float* __restrict__ w, const float* __restrict__ g, float* __restrict__ m,
+                       float* __restrict__ v, float lr, float beta1, float beta2, float eps, float c1, float c2,
+                       int rows, int cols, __nv_bfloat16* __restrict__ wb, __nv_bfloat16* __restrict__ wbt) {
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t >= count) return;
+  const float gt = g[t];
+  const float mt = beta1 * m[t] + (1 - beta1) * gt;
+  const float vt = beta2 * v[t] + (1 - beta2) * gt * gt;
+  m[t] = mt;
+  v[t] = vt;
+  const float mhat = mt / c1, vhat = vt / c2;
+  const float wt = w[t] - lr * mhat / (sqrtf(vhat) + eps);
+  w[t] = wt;
+  if (wb) {
+    const int r = (int)(t / cols), c = (int)(t % cols);
+    wb[t] = __float2bfloat16(wt);
+    if (wbt) wbt[(long long)c * rows + r] = __float2bfloat16(wt);
+  }
+}
+
+__global__ void k_to_bf16(long long count, const float* __restrict__ w, int rows, int cols,
+                          __nv_bfloat16* __restrict__ wb, __nv_bfloat16* __restrict__ wbt) {
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t >= count) return;
+  const int r = (int)(t / cols), c = (int)(t % cols);
+  wb[t] = __float2bfloat16(w[t]);
+  if (wbt) wbt[(long long)c * rows + r] = __float2bfloat16(w[t]);
+}
+
+// SplitMix64 hash for reproducible sampling.
+__device__ __forceinline__ unsigned long long mix64(unsigned long long z) {
+  z += 0x9E3779B97F4A7C15ull;
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+
+// Batch of n rows: a fraction `node_frac` drawn from pool A (na samples),
+// the rest from pool B (nb samples); each sample is 4 coords + 3 targets.
+__global__ void k_gather_batch(long long n, unsigned long long seed, float node_frac, const float* __restrict__ poolA,
+                               long long na, const float* __restrict__ poolB, long long nb, float* __restrict__ coords,
+                               float* __restrict__ target) {
+  const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const unsigned long long h = mix64(seed ^ (unsigned long long)i * 0x2545F4914F6CDD1Dull);
+  const bool fromA = nb == 0 || ((h >> 40) & 0xFFFFFF) < (unsigned long long)(node_frac * 16777216.0f);
+  const float* src = fromA ? poolA + 7 * (long long)(mix64(h) % (unsigned long long)na)
+                           : poolB + 7 * (long long)(mix64(h + 1) % (unsigned long long)nb);
+#pragma unroll
+  for (int c = 0; c < 4; c++) coords[i * 4 + c] = src[c];
+#pragma unroll
+  for (int c = 0; c < 3; c++) target[i * 3 + c] = src[4 + c];
+}
+
+static inline unsigned grid_for(long long n, int blk) { return (unsigned)((n + blk - 1) / blk); }
+
+void launch_features(long long n, const float* coords, __nv_bfloat16* F, __nv_bfloat16* FT, cudaStream_t st) {
+  k_features<<<grid_for(n * kMlpIn / 2, 256), 256, 0, st>>>(n, coords, F, FT);
+}
+void launch_head_forward(long long n, const __nv_bfloat16* H, const float* W5, const float* b5, float* out,
+                         cudaStream_t st) {
+  k_head_forward<<<grid_for(n * 32, 256), 256, 0, st>>>(n, H, W5, b5, out);
+}
+void launch_loss_grad(long long n, const float* out, const float* target, float* dout, float* loss, cudaStream_t st) {
+  k_loss_grad<<<grid_for(3 * n, 256), 256, 0, st>>>(n, out, target, dout, loss);
+}
+void launch_head_backward(long long n, const float* dout, const __nv_bfloat16* H, const float* W5,
+                          const float* dsilu, __nv_bfloat16* dZ, __nv_bfloat16* dZT, float* dW5, float* db5,
+                          cudaStream_t st) {
+  const int blocks = (int)min(1024LL, (n + 63) / 64);
+  k_head_backward<<<blocks, kMlpHidden, 0, st>>>(n, dout, H, W5, dsilu, dZ, dZT, dW5, db5);
+}
+void launch_bias_grad(long long n, int width, const __nv_bfloat16* dZT, float* db, cudaStream_t st) {
+  k_bias_grad<<<width, 256, 0, st>>>(n, width, dZT, db);
+}
+void launch_adam(long long count, float* w, const float* g, float* m, float* v, float lr, float beta1, float beta2,
+                 float eps, int step, int rows, int cols, __nv_bfloat16* wb, __nv_bfloat16* wbt, cudaStream_t st) {
+  const float c1 = 1.0f - powf(beta1, (float)step), c2 = 1.0f - powf(beta2, (float)step);
+  k_adam<<<grid_for(count, 256), 256, 0, st>>>(count, w, g, m, v, lr, beta1, beta2, eps, c1, c2, rows, cols, wb,
+                                                wbt);
+}
+void launch_to_bf16(long long count, const float* w, int rows, int cols, __nv_bfloat16* wb, __nv_bfloat16* wbt,
+                    cudaStream_t st) {
+  k_to_bf16<<<grid_for(count, 256), 256, 0, st>>>(count, w, rows, cols, wb, wbt);
+}
+void launch_gather_batch(long long n, unsigned long long seed, float node_frac, const float* poolA, long long na,
+                         const float* poolB, long long nb, float* coords, float* target, cudaStream_t st) {
+  k_gather_batch<<<grid_for(n, 256), 256, 0, st>>>(n, seed, node_frac, poolA, na, poolB, nb, coords, target);
+}
+
+}  // namespace sfsim

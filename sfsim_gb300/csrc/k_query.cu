@@ -1,0 +1,399 @@
+// k_query.cu -- queries of a built atmosphere at arbitrary points:
+//  * the table lookups sfsim's shaders perform (resources/shaders/atmosphere/
+//    transmittance-track.glsl, transmittance-outer.glsl, ray-scatter-track.glsl,
+//    ray-scatter-outer.glsl with core/interpolate-2d.glsl, interpolate-4d.glsl
+//    and the core/*-to-index.glsl maps), restated in FP32 as the GLSL computes
+//    them, on the .scatter tables;
+//  * the rendered in-scatter S + M phase(mie, v.l) at (x, v, l) by direct
+//    quadrature: the first order integrated at the point (atmosphere.clj:
+//    154-200) plus ray scatter of the summed point-scatter tables.
+#include "atmo_device.cuh"
+#include "kernels.h"
+
+namespace sfsim {
+
+// ---------------------------------------------------------------------------
+// GLSL restatement (FP32)
+// ---------------------------------------------------------------------------
+
+struct f3 {
+  float x, y, z;
+};
+__device__ __forceinline__ f3 F3(float x, float y, float z) { return f3{x, y, z}; }
+__device__ __forceinline__ float fdot(f3 a, f3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__device__ __forceinline__ f3 fsub(f3 a, f3 b) { return F3(a.x - b.x, a.y - b.y, a.z - b.z); }
+__device__ __forceinline__ f3 fadd(f3 a, f3 b) { return F3(a.x + b.x, a.y + b.y, a.z + b.z); }
+__device__ __forceinline__ f3 fmul(f3 a, float s) { return F3(a.x * s, a.y * s, a.z * s); }
+__device__ __forceinline__ f3 femul(f3 a, f3 b) { return F3(a.x * b.x, a.y * b.y, a.z * b.z); }
+
+// core/limit-quot.glsl
+__device__ __forceinline__ float limit_quot_f(float a, float b, float lower, float upper) {
+  if (a == 0.0f) return 0.0f;
+  if (b < 0) {
+    a = -a;
+    b = -b;
+  }
+  if (a < b * upper) {
+    if (a > b * lower) return a / b;
+    return lower;
+  }
+  return upper;
+}
+
+// core/horizon-distance.glsl
+__device__ __forceinline__ float horizon_distance_f(float ground_radius, float radius_sqr) {
+  return sqrtf(fmaxf(0.0f, radius_sqr - ground_radius * ground_radius));
+}
+
+struct GlslEnv {
+  float radius, max_height;
+  int t_height, t_elevation;           // transmittance table
+  int height, elevation, light, heading;  // 4-D tables
+  const float* T;                      // width t_elevation, height t_height
+  const float* S;                      // width elevation*heading, height height*light
+  const float* M;
+  int weight_bits;                     // 0: exact weights; 8: GL 8-bit fixed-point filtering
+  float mie_g;
+};
+
+// core/height-to-index.glsl (normalised)
+__device__ __forceinline__ float height_to_index_g(const GlslEnv& e, f3 p) {
+  const float top = e.radius + e.max_height;
+  return horizon_distance_f(e.radius, fdot(p, p)) / horizon_distance_f(e.radius, top * top);
+}
+
+// core/elevation-to-index.glsl
+__device__ __forceinline__ float elevation_to_index_g(const GlslEnv& e, f3 p, f3 d, bool above) {
+  const float pr = sqrtf(fdot(p, p));
+  const float sin_el = fdot(p, d) / pr;
+  const float rho = horizon_distance_f(e.radius, pr * pr);
+  const float delta = pr * pr * sin_el * sin_el - rho * rho;
+  if (above) {
+    const float top = e.radius + e.max_height;
+    const float h = sqrtf(top * top - e.radius * e.radius);
+    return 0.5f - limit_quot_f(pr * sin_el - sqrtf(fmaxf(0.0f, delta + h * h)), 2 * rho + 2 * h, -0.5f, 0.0f);
+  }
+  return 0.5f + limit_quot_f(pr * sin_el + sqrtf(fmaxf(0.0f, delta)), 2 * rho, -0.5f, 0.0f);
+}
+
+// core/sun-elevation-to-index.glsl, core/sun-angle-to-index.glsl
+__device__ __forceinline__ float sun_elevation_to_index_g(f3 p, f3 l) {
+  const float s = fdot(p, l) / sqrtf(fdot(p, p));
+  return fmaxf(0.0f, (1 - expf(-3 * s - 0.6f)) / (1 - expf(-3.6f)));
+}
+__device__ __forceinline__ float sun_angle_to_index_g(f3 d, f3 l) { return 0.5f * (1 + fdot(d, l)); }
+
+// core/is-above-horizon.glsl
+__device__ __forceinline__ bool is_above_horizon_g(const GlslEnv& e, f3 p, f3 d) {
+  const float dist = sqrtf(fdot(p, p));
+  const float s = fdot(d, p);
+  return s >= 0 || s * s <= dist * dist - e.radius * e.radius;
+}
+
+// texture() with GL_LINEAR and CLAMP_TO_EDGE on an RGB float texture at
+// texel coordinates (x, y) = uv * size - 0.5
+__device__ __forceinline__ float q_weight(float f, int bits) {
+  if (!bits) return f;
+  const float s = (float)(1 << bits);
+  return floorf(f * s + 0.5f) / s;
+}
+
+__device__ __forceinline__ f3 texel(const float* t, int w, int h, int x, int y) {
+  x = min(max(x, 0), w - 1);
+  y = min(max(y, 0), h - 1);
+  const float* p = t + 3 * ((long long)y * w + x);
+  return F3(p[0], p[1], p[2]);
+}
+
+__device__ __forceinline__ f3 texture_g(const float* t, int w, int h, float u, float v, int bits) {
+  const float x = u * w - 0.5f, y = v * h - 0.5f;
+  const float x0 = floorf(x), y0 = floorf(y);
+  const float fx = q_weight(x - x0, bits), fy = q_weight(y - y0, bits);
+  const int ix = (int)x0, iy = (int)y0;
+  const f3 a = texel(t, w, h, ix, iy), b = texel(t, w, h, ix + 1, iy);
+  const f3 c = texel(t, w, h, ix, iy + 1), d = texel(t, w, h, ix + 1, iy + 1);
+  const f3 top = fadd(fmul(a, 1 - fx), fmul(b, fx));
+  const f3 bot = fadd(fmul(c, 1 - fx), fmul(d, fx));
+  return fadd(fmul(top, 1 - fy), fmul(bot, fy));
+}
+
+// core/interpolate-2d.glsl + convert-2d-index.glsl; idx = (x, y)
+__device__ __forceinline__ f3 interpolate_2d_g(const float* t, int size_y, int size_x, float ix, float iy, int bits) {
+  const float u = (ix * (size_x - 1) + 0.5f) / size_x;
+  const float v = (iy * (size_y - 1) + 0.5f) / size_y;
+  return texture_g(t, size_x, size_y, u, v, bits);
+}
+
+// core/interpolate-4d.glsl + make-2d-index-from-4d.glsl; idx = (x, y, z, w)
+__device__ __forceinline__ f3 interpolate_4d_g(const float* t, int size_w, int size_z, int size_y, int size_x,
+                                               const float* idx, int bits) {
+  const float px = idx[0] * (size_x - 1), py = idx[1] * (size_y - 1);
+  const float pz = idx[2] * (size_z - 1), pw = idx[3] * (size_w - 1);
+  const float fz = pz - floorf(pz), fw = pw - floorf(pw);
+  const float zf = floorf(pz), wf = floorf(pw);
+  const float dx = (float)(size_x * size_z), dy = (float)(size_y * size_w);
+  const float z1 = fminf(zf + 1, (float)(size_z - 1)), w1 = fminf(wf + 1, (float)(size_w - 1));
+  const float s = (0.5f + px + zf * size_x) / dx, tt = (0.5f + px + z1 * size_x) / dx;
+  const float p = (0.5f + py + wf * size_y) / dy, q = (0.5f + py + w1 * size_y) / dy;
+  const int W = size_x * size_z, H = size_y * size_w;
+  const f3 sp = texture_g(t, W, H, s, p, bits), tp = texture_g(t, W, H, tt, p, bits);
+  const f3 sq = texture_g(t, W, H, s, q, bits), tq = texture_g(t, W, H, tt, q, bits);
+  return fadd(fadd(fmul(sp, (1 - fz) * (1 - fw)), fmul(tp, fz * (1 - fw))),
+              fadd(fmul(sq, (1 - fz) * fw), fmul(tq, fz * fw)));
+}
+
+// atmosphere/phase-function.glsl
+__device__ __forceinline__ float phase_g(float g, float mu) {
+  return 3 * (1 - g * g) * (1 + mu * mu) / (8 * 3.14159265358979323846f * (2 + g * g) * powf(1 + g * g - 2 * g * mu, 1.5f));
+}
+
+__device__ __forceinline__ void transmittance_forward_g(const GlslEnv& e, f3 p, f3 d, bool above, float* out) {
+  out[0] = elevation_to_index_g(e, p, d, above);
+  out[1] = height_to_index_g(e, p);
+}
+
+// atmosphere/transmittance-track.glsl
+__device__ f3 transmittance_track_g(const GlslEnv& e, f3 p, f3 q) {
+  const float dist = sqrtf(fdot(fsub(q, p), fsub(q, p)));
+  if (dist > 0) {
+    const f3 d = fmul(fsub(q, p), 1.0f / dist);
+    const bool above = is_above_horizon_g(e, p, d);
+    float a[2], b[2];
+    transmittance_forward_g(e, p, d, above, a);
+    transmittance_forward_g(e, q, d, above, b);
+    const f3 t1 = interpolate_2d_g(e.T, e.t_height, e.t_elevation, a[0], a[1], e.weight_bits);
+    const f3 t2 = interpolate_2d_g(e.T, e.t_height, e.t_elevation, b[0], b[1], e.weight_bits);
+    return F3(t1.x / t2.x, t1.y / t2.y, t1.z / t2.z);
+  }
+  return F3(1, 1, 1);
+}
+
+// atmosphere/transmittance-outer.glsl
+__device__ f3 transmittance_outer_g(const GlslEnv& e, f3 p, f3 d) {
+  float a[2];
+  transmittance_forward_g(e, p, d, true, a);
+  return interpolate_2d_g(e.T, e.t_height, e.t_elevation, a[0], a[1], e.weight_bits);
+}
+
+// core/ray-scatter-forward.glsl: (sun angle, sun elevation, elevation, height)
+__device__ __forceinline__ void ray_scatter_forward_g(const GlslEnv& e, f3 p, f3 d, f3 l, bool above, float* out) {
+  out[0] = sun_angle_to_index_g(d, l);
+  out[1] = sun_elevation_to_index_g(p, l);
+  out[2] = elevation_to_index_g(e, p, d, above);
+  out[3] = height_to_index_g(e, p);
+}
+
+__device__ __forceinline__ f3 in_scatter_g(const GlslEnv& e, const float* idx, float mu) {
+  const f3 s = interpolate_4d_g(e.S, e.height, e.elevation, e.light, e.heading, idx, e.weight_bits);
+  const f3 m = interpolate_4d_g(e.M, e.height, e.elevation, e.light, e.heading, idx, e.weight_bits);
+  return fadd(s, fmul(m, phase_g(e.mie_g, mu)));
+}
+
+// atmosphere/ray-scatter-track.glsl
+__device__ f3 ray_scatter_track_g(const GlslEnv& e, f3 l, f3 p, f3 q) {
+  const float dist = sqrtf(fdot(fsub(q, p), fsub(q, p)));
+  if (dist > 0) {
+    const f3 d = fmul(fsub(q, p), 1.0f / dist);
+    const bool above = is_above_horizon_g(e, p, d);
+    const float mu = fdot(d, l);
+    float ip[4], iq[4];
+    ray_scatter_forward_g(e, p, d, l, above, ip);
+    const f3 sp = in_scatter_g(e, ip, mu);
+    ray_scatter_forward_g(e, q, d, l, above, iq);
+    const f3 sq = in_scatter_g(e, iq, mu);
+    const f3 t = transmittance_track_g(e, p, q);
+    return fsub(sp, femul(t, sq));
+  }
+  return F3(0, 0, 0);
+}
+
+// atmosphere/ray-scatter-outer.glsl
+__device__ f3 ray_scatter_outer_g(const GlslEnv& e, f3 l, f3 p, f3 d) {
+  float idx[4];
+  ray_scatter_forward_g(e, p, d, l, true, idx);
+  return in_scatter_g(e, idx, fdot(d, l));
+}
+
+// In-scatter of the tables at (p, d, l) with the horizon test choosing the
+// table half, the lookup the rendered in-scatter comparison uses.
+__device__ f3 in_scatter_at_g(const GlslEnv& e, f3 l, f3 p, f3 d) {
+  float idx[4];
+  ray_scatter_forward_g(e, p, d, l, is_above_horizon_g(e, p, d), idx);
+  return in_scatter_g(e, idx, fdot(d, l));
+}
+
+__global__ void k_query_table(GlslEnv e, int kind, long long n, const float* A, const float* Bv, const float* L,
+                              float* out) {
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  const f3 a = F3(A[3 * t], A[3 * t + 1], A[3 * t + 2]);
+  const f3 b = F3(Bv[3 * t], Bv[3 * t + 1], Bv[3 * t + 2]);
+  const f3 l = L ? F3(L[3 * t], L[3 * t + 1], L[3 * t + 2]) : F3(0, 0, 1);
+  f3 r;
+  switch (kind) {
+    case 0: r = transmittance_track_g(e, a, b); break;
+    case 1: r = transmittance_outer_g(e, a, b); break;
+    case 2: r = ray_scatter_track_g(e, l, a, b); break;
+    case 3: r = ray_scatter_outer_g(e, l, a, b); break;
+    default: r = in_scatter_at_g(e, l, a, b); break;
+  }
+  out[3 * t] = r.x;
+  out[3 * t + 1] = r.y;
+  out[3 * t + 2] = r.z;
+}
+
+void launch_query_table(const QueryTables& q, int kind, long long n, const float* a, const float* b, const float* l,
+                        float* out, int weight_bits, cudaStream_t st) {
+  GlslEnv e;
+  e.radius = q.radius;
+  e.max_height = q.max_height;
+  e.t_height = q.t_height;
+  e.t_elevation = q.t_elevation;
+  e.height = q.height;
+  e.elevation = q.elevation;
+  e.light = q.light;
+  e.heading = q.heading;
+  e.T = q.T;
+  e.S = q.S;
+  e.M = q.M;
+  e.weight_bits = weight_bits;
+  e.mie_g = q.mie_g;
+  const int blk = 128;
+  k_query_table<<<(unsigned)((n + blk - 1) / blk), blk, 0, st>>>(e, kind, n, a, b, l, out);
+}
+
+// ---------------------------------------------------------------------------
+// Direct quadrature of the rendered in-scatter at (x, v, l)
+// ---------------------------------------------------------------------------
+
+// Elevation coordinate (atmosphere.clj:239-253) at a sample p of the ray
+// x + t v in FP32.  (p.v)^2 - (|p|^2 - R^2) = R^2 - d^2 and
+// (p.v)^2 - (|p|^2 - R^2) + H^2 = top^2 - d^2 with d the distance of the line
+// from the centre, so both square roots are per-ray constants taken in FP64;
+// the differences that cancel are rewritten with them.
+__device__ __forceinline__ float elevation_coordinate_f(float q, float pv, float root_top, float root_gnd, float Hh,
+                                                        bool above) {
+  const float rho = sqrtf(fmaxf(q, 0.0f));
+  if (above) {
+    const float a = (pv > 0 && root_top > 0) ? (q - Hh * Hh) / (pv + root_top) : pv - root_top;
+    return 0.5f - limit_quot_f(a, rho + rho + 2 * Hh, -0.5f, 0.0f);
+  }
+  const float a = (pv < 0 && root_gnd > 0) ? q / (pv - root_gnd) : pv + root_gnd;
+  return 0.5f + limit_quot_f(a, rho + rho, -0.5f, 0.0f);
+}
+
+template <int WARPS>
+__global__ void __launch_bounds__(WARPS * 32) k_query_direct(const AtmoParams* params, BuildDims d,
+                                                             const Vec4<float>* Jsum, long long n, const double* X,
+                                                             const double* V, const double* Lt, float* out) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const long long qi = blockIdx.x * (long long)WARPS + warp;
+  if (qi >= n) return;
+  const AtmoParams& P = params[0];
+  const d3 x = mk3(X[3 * qi], X[3 * qi + 1], X[3 * qi + 2]);
+  const d3 v = mk3(V[3 * qi], V[3 * qi + 1], V[3 * qi + 2]);
+  const d3 l = mk3(Lt[3 * qi], Lt[3 * qi + 1], Lt[3 * qi + 2]);
+  const int S = d.S;
+  // FP64 per query: the view ray (atmosphere.clj:192-198)
+  const int above = is_above_horizon(P, x, v);
+  const d3 e = above ? atmosphere_intersection(P, x, v) : surface_intersection(P, x, v);
+  const d3 D = sub3(e, x);
+  const double L = mag3(D);
+  const double xr = mag3(x);
+  const double c0 = dmul(dsub(xr, P.R), dadd(xr, P.R));
+  const double xv = dot3(x, v);
+  const double dperp2 = dsub(dot3(x, x), sqr(xv));  // squared distance of the line from the centre
+  const float root_top = (float)sqrt(dmax(0.0, dsub(P.top2, dperp2)));
+  const float root_gnd = (float)sqrt(dmax(0.0, dsub(P.R2, dperp2)));
+  const float fc0 = (float)c0, two_xD = (float)(2.0 * dot3(x, D)), DD = (float)dot3(D, D);
+  const float b0 = (float)dot3(x, l), Dl = (float)dot3(D, l), mu = (float)dot3(v, l);
+  const float fL = (float)L, fxv = (float)xv, Hh = (float)P.Hh, Hh2 = (float)P.Hh2;
+  const float* hp = P.f_hpoly;
+  const float* hr = P.f_hpr4;
+  const float scale2 = (float)((d.n2 - 1) / (1 - exp(-3.6)));
+  int u3;
+  float s3;
+  split_coord_r<float>(0.5f * (d.n3 - 1) * (1 + mu), d.n3, &u3, &s3);
+  float accR[3] = {0, 0, 0}, accM[3] = {0, 0, 0}, accJ[3] = {0, 0, 0};
+  for (int s = lane; s < S; s += 32) {
+    const float su = (s + 0.5f) / S;
+    // q and optical depth from x to p_s along the view ray
+    const float q = fmaf(su, fmaf(su, DD, two_xD), fc0);
+    float sr, sm;
+    optical_sums_u<float, 5>(fc0, two_xD * su, DD * su * su, 1.0f / S, S, hp, P.f_alpha, P.f_beta, P.f_kr, P.f_km,
+                             sr, sm);
+    const float segL = fL * su / S;
+    float taux[3];
+#pragma unroll
+    for (int c = 0; c < 3; c++) taux[c] = segL * (P.f_ray_ext[c] * sr + P.f_mie_ext[c] * sm);
+    const float h = height_from_q<float, 5>(q, hp, P.f_alpha, P.f_beta);
+    const float er = Bulk<float>::exp2(h * P.f_kr), em = Bulk<float>::exp2(h * P.f_km);
+    // first order: the sun seen from p_s (atmosphere.clj:154-160)
+    const float bp = fmaf(su, Dl, b0);
+    bool lit = (bp >= 0.0f) || (bp * bp <= q);
+    const float m = bp * bp - q;
+    if ((bp < 4.0f) && (fabsf(m) < 1.0e8f || (bp > -4.0f && q < 1.0e8f))) {
+      const d3 p = add3(x, mul3(D, (0.5 + s) * (1.0 / S)));
+      lit = is_above_horizon(P, p, l);
+    }
+    if (lit) {
+      const float ctop = q - Hh2;
+      const float root = Bulk<float>::sqrt(fmaxf(bp * bp - ctop, 0.0f));
+      float texit = bp >= 0.0f ? Bulk<float>::div(-ctop, bp + root) : root - bp;
+      texit = fmaxf(texit, 0.0f);
+      const float dt = texit / S;
+      float tr, tm;
+      sun_sums<float, 4>(q, bp, dt, S, hr, P.f_alpha, P.f_beta, P.f_hratio, tr, tm);
+#pragma unroll
+      for (int c = 0; c < 3; c++) {
+        const float T = exp_neg(taux[c] + dt * (P.f_ray_ext[c] * tr + P.f_mie_ext[c] * tm));
+        accR[c] = fmaf(T, er, accR[c]);
+        accM[c] = fmaf(T, em, accM[c]);
+      }
+    }
+    // higher orders: J summed over the orders at forward(p_s, v, l, above)
+    if (Jsum) {
+      const float pr = sqrtf(P.f_R * P.f_R + q);
+      const float pv = fxv + su * fL;
+      int u[4];
+      float w[4];
+      split_coord_r<float>((d.n0 - 1) * (sqrtf(fmaxf(q, 0.0f)) / Hh), d.n0, &u[0], &w[0]);
+      split_coord_r<float>((d.n1 - 1) * elevation_coordinate_f(q, pv, root_top, root_gnd, Hh, above), d.n1, &u[1],
+                           &w[1]);
+      split_coord_r<float>(sun_elevation_index_r<float>(bp / pr, scale2), d.n2, &u[2], &w[2]);
+      u[3] = u3;
+      w[3] = s3;
+      float jv[3];
+      interp4<float>(Jsum, d, u, w, jv);
+#pragma unroll
+      for (int c = 0; c < 3; c++) accJ[c] = fmaf(exp_neg(taux[c]), jv[c], accJ[c]);
+    }
+  }
+#pragma unroll
+  for (int c = 0; c < 3; c++) {
+    for (int o = 16; o > 0; o >>= 1) {
+      accR[c] += __shfl_xor_sync(0xffffffffu, accR[c], o);
+      accM[c] += __shfl_xor_sync(0xffffffffu, accM[c], o);
+      accJ[c] += __shfl_xor_sync(0xffffffffu, accJ[c], o);
+    }
+  }
+  if (lane == 0) {
+    const float w = fL / S;
+    const float phR = phase_cs<float>((float)P.ray_g, mu), phM = phase_cs<float>((float)P.mie_g, mu);
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+      const float s1 = w * phR * (float)(P.intensity[c] * P.ray_base[c]) * accR[c];
+      const float m1 = w * (float)(P.intensity[c] * P.mie_base[c]) * accM[c];
+      out[3 * qi + c] = s1 + m1 * phM + w * accJ[c];
+    }
+  }
+}
+
+void launch_query_direct(const AtmoParams* params, const BuildDims& d, const Vec4<float>* Jsum, long long n,
+                         const double* x, const double* v, const double* l, float* out, cudaStream_t st) {
+  constexpr int WARPS = 8;
+  const unsigned blocks = (unsigned)((n + WARPS - 1) / WARPS);
+  k_query_direct<WARPS><<<blocks, WARPS * 32, 0, st>>>(params, d, Jsum, n, x, v, l, out);
+}
+
+}  // namespace sfsim

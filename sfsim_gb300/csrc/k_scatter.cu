@@ -6,75 +6,6 @@
 
 namespace sfsim {
 
-// Index of a 4-D texel.
-__device__ __forceinline__ long long idx4(const BuildDims& d, int i, int j, int k, int a) {
-  return (((long long)i * d.n1 + j) * d.n2 + k) * d.n3 + a;
-}
-
-template <class Real>
-__device__ __forceinline__ void ld3(const Vec4<Real>* t, long long i, Real o[3]) {
-  Vec4<Real> v = t[i];
-  o[0] = v.x;
-  o[1] = v.y;
-  o[2] = v.z;
-}
-
-template <class Real>
-__device__ __forceinline__ void mix3(const Real* a, const Real* b, Real s, Real* o) {
-#pragma unroll
-  for (int c = 0; c < 3; c++) o[c] = a[c] * (Real(1) - s) + b[c] * s;
-}
-
-// Clamped quadrilinear interpolation of a 4-D table (interpolate.clj:87-98:
-// the innermost dimension is mixed first).
-template <class Real>
-__device__ inline void interp4(const Vec4<Real>* t, const BuildDims& d, const int* u, const Real* s, Real out[3]) {
-  const int v[4] = {upper_index(u[0], d.n0), upper_index(u[1], d.n1), upper_index(u[2], d.n2),
-                    upper_index(u[3], d.n3)};
-  Real rh[2][3];
-#pragma unroll
-  for (int h = 0; h < 2; h++) {
-    Real re[2][3];
-#pragma unroll
-    for (int e = 0; e < 2; e++) {
-      Real rk[2][3];
-#pragma unroll
-      for (int k = 0; k < 2; k++) {
-        Real A[3], B[3];
-        const int ih = h ? v[0] : u[0], ie = e ? v[1] : u[1], ik = k ? v[2] : u[2];
-        ld3(t, idx4(d, ih, ie, ik, u[3]), A);
-        ld3(t, idx4(d, ih, ie, ik, v[3]), B);
-        mix3(A, B, s[3], rk[k]);
-      }
-      mix3(rk[0], rk[1], s[2], re[e]);
-    }
-    mix3(re[0], re[1], s[1], rh[h]);
-  }
-  mix3(rh[0], rh[1], s[0], out);
-}
-
-template <class Real>
-__device__ inline void interp2(const Vec4<Real>* t, int n0, int n1, const int* u, const Real* s, Real out[3]) {
-  const int v0 = upper_index(u[0], n0), v1 = upper_index(u[1], n1);
-  Real A[3], B[3], lo[3], hi[3];
-  ld3(t, (long long)u[0] * n1 + u[1], A);
-  ld3(t, (long long)u[0] * n1 + v1, B);
-  mix3(A, B, s[1], lo);
-  ld3(t, (long long)v0 * n1 + u[1], A);
-  ld3(t, (long long)v0 * n1 + v1, B);
-  mix3(A, B, s[1], hi);
-  mix3(lo, hi, s[0], out);
-}
-
-// (1 - exp(-3 s - 0.6)) / (1 - exp(-3.6)) clamped at 0, times (size - 1)
-// (sun-elevation-to-index, atmosphere.clj:322-326) in Real.
-template <class Real>
-__device__ __forceinline__ Real sun_elevation_index_r(Real sin_el, Real scale) {
-  const Real e = Bulk<Real>::exp2((Real(3) * sin_el + Real(0.6)) * Real(-1.4426950408889634));
-  const Real r = (Real(1) - e) * scale;
-  return r > Real(0) ? r : Real(0);
-}
-
 // ---------------------------------------------------------------------------
 // Point scatter J (atmosphere.clj:203-222) for all nodes of one (height i,
 // sun elevation k) pair.  For such a pair every dS lookup shares the height
@@ -128,7 +59,7 @@ __device__ __forceinline__ void gather_heading_row(const Vec4<Real>* t, const Bu
 }
 
 template <class Real, bool FIRST>
-__global__ void __launch_bounds__(256, 4) k_point_scatter(const AtmoParams* params, BuildDims d,
+__global__ void __launch_bounds__(256, 3) k_point_scatter(const AtmoParams* params, BuildDims d,
                                                           const RowInfo* rowinfo, const SphereDir<Real>* sdirs,
                                                           const CellGeom<Real>* geom, const Vec4<Real>* dS,
                                                           const Vec4<Real>* Mt, const Vec4<Real>* dE,
@@ -174,8 +105,11 @@ __global__ void __launch_bounds__(256, 4) k_point_scatter(const AtmoParams* para
   }
   __syncthreads();
 
-  const int cell = chunk * blockDim.x + threadIdx.x;
-  if (cell >= d.n1 * d.n3) return;
+  // a lane past the last node keeps running (it feeds the warp's shuffles) but stores nothing
+  const int nslab = d.n1 * d.n3;
+  const int cell_raw = chunk * blockDim.x + threadIdx.x;
+  const bool valid = cell_raw < nslab;
+  const int cell = valid ? cell_raw : nslab - 1;
   const int j = cell / d.n3, a = cell % d.n3;
   const RowInfo ri = rowinfo[(long long)b * d.rows() + (long long)i * d.n1 + j];
   const Real sv = (Real)ri.sv, cv = (Real)ri.cv;
@@ -185,57 +119,88 @@ __global__ void __launch_bounds__(256, 4) k_point_scatter(const AtmoParams* para
   const Real scale3 = Real(0.5) * Real(d.n3 - 1);
   const Real scaleE = (Real)((d.nE1 - 1) / (1 - exp(-3.6)));
   const int n3x3 = 3 * d.n3;
+  // The phases depend on (j, direction) only.  When the n3 headings of one j
+  // fill aligned lane groups, each lane evaluates them for one direction of a
+  // batch of n3 and the group exchanges them by shuffles.
+  const int G = d.n3;
+  const bool share = (32 % G == 0) && (blockDim.x % G == 0);
+  const int lane = threadIdx.x & 31;
+  const int gbase = share ? (lane & ~(G - 1)) : lane;
+  const int gpos = lane - gbase;
 
   Real accR[3] = {0, 0, 0}, accM[3] = {0, 0, 0}, cR[3] = {0, 0, 0}, cM[3] = {0, 0, 0};
   Real ringR[3] = {0, 0, 0}, ringM[3] = {0, 0, 0};
-  for (int w = 0; w < d.P; w++) {
-    const SphereDir<Real>& D = dirs[w];
-    const Real mu_v = fma(sv, D.w[0], cv * D.w[1]);
-    const Real mu_l = fma(D.w[0], g.lx, fma(D.w[1], g.ly, D.w[2] * g.lz));
-    // sun-angle coordinate of (omega, l) along the direction's heading row
-    int u3;
-    Real s3;
-    split_coord_r<Real>(scale3 * (Real(1) + mu_l), d.n3, &u3, &s3);
-    const int v3 = upper_index(u3, d.n3);
-    const Real* row = rows + w * n3x3;
-    Real X[3];
-#pragma unroll
-    for (int c = 0; c < 3; c++) X[c] = fma(row[3 * v3 + c] - row[3 * u3 + c], s3, row[3 * u3 + c]);
-    if (FIRST) {
-      const Real* rowM = rowsM + w * n3x3;
-      const Real ph = phM(mu_l);
-#pragma unroll
-      for (int c = 0; c < 3; c++) X[c] = fma(fma(rowM[3 * v3 + c] - rowM[3 * u3 + c], s3, rowM[3 * u3 + c]), ph, X[c]);
+  const int step = share ? G : 1;
+  for (int w0 = 0; w0 < d.P; w0 += step) {
+    Real pRb = 0, pMb = 0;
+    if (share) {
+      const int wb = w0 + gpos;
+      if (wb < d.P) {
+        const Real mu_v = fma(sv, dirs[wb].w[0], cv * dirs[wb].w[1]);
+        pRb = phR(mu_v);
+        pMb = phM(mu_v);
+      }
     }
-    if (D.surface) {
-      const Real sg = fma(D.gdir[0], g.lx, fma(D.gdir[1], g.ly, D.gdir[2] * g.lz));
-      int uE1;
-      Real sE1;
-      split_coord_r<Real>(sun_elevation_index_r<Real>(sg, scaleE), d.nE1, &uE1, &sE1);
-      const int vE1 = upper_index(uE1, d.nE1), vE0 = upper_index(D.uE0, d.nE0);
-      Real Y[3];
-      mix4(etab + 3 * (D.uE0 * d.nE1 + uE1), etab + 3 * (D.uE0 * d.nE1 + vE1), etab + 3 * (vE0 * d.nE1 + uE1),
-           etab + 3 * (vE0 * d.nE1 + vE1), D.sE0, sE1, Y);
+    const int wend = min(w0 + step, d.P);
+    for (int w = w0; w < wend; w++) {
+      const SphereDir<Real>& D = dirs[w];
+      Real pR, pM;
+      if (share) {
+        pR = __shfl_sync(0xffffffffu, pRb, gbase + (w - w0));
+        pM = __shfl_sync(0xffffffffu, pMb, gbase + (w - w0));
+      } else {
+        const Real mu_v = fma(sv, D.w[0], cv * D.w[1]);
+        pR = phR(mu_v);
+        pM = phM(mu_v);
+      }
+      const Real mu_l = fma(D.w[0], g.lx, fma(D.w[1], g.ly, D.w[2] * g.lz));
+      // sun-angle coordinate of (omega, l) along the direction's heading row
+      int u3;
+      Real s3;
+      split_coord_r<Real>(scale3 * (Real(1) + mu_l), d.n3, &u3, &s3);
+      const int v3 = upper_index(u3, d.n3);
+      const Real* row = rows + w * n3x3;
+      Real X[3];
 #pragma unroll
-      for (int c = 0; c < 3; c++) X[c] = fma(D.ground[c], Y[c], X[c]);
-    }
-    const Real wR = D.weight * phR(mu_v);
-    const Real wM = D.weight * phM(mu_v);
+      for (int c = 0; c < 3; c++) X[c] = fma(row[3 * v3 + c] - row[3 * u3 + c], s3, row[3 * u3 + c]);
+      if (FIRST) {
+        const Real* rowM = rowsM + w * n3x3;
+        const Real ph = phM(mu_l);
 #pragma unroll
-    for (int c = 0; c < 3; c++) {
-      ringR[c] = fma(wR, X[c], ringR[c]);
-      ringM[c] = fma(wM, X[c], ringM[c]);
-    }
-    if (D.pad) {  // last direction of a theta ring
+        for (int c = 0; c < 3; c++)
+          X[c] = fma(fma(rowM[3 * v3 + c] - rowM[3 * u3 + c], s3, rowM[3 * u3 + c]), ph, X[c]);
+      }
+      if (D.surface) {
+        const Real sg = fma(D.gdir[0], g.lx, fma(D.gdir[1], g.ly, D.gdir[2] * g.lz));
+        int uE1;
+        Real sE1;
+        split_coord_r<Real>(sun_elevation_index_r<Real>(sg, scaleE), d.nE1, &uE1, &sE1);
+        const int vE1 = upper_index(uE1, d.nE1), vE0 = upper_index(D.uE0, d.nE0);
+        Real Y[3];
+        mix4(etab + 3 * (D.uE0 * d.nE1 + uE1), etab + 3 * (D.uE0 * d.nE1 + vE1), etab + 3 * (vE0 * d.nE1 + uE1),
+             etab + 3 * (vE0 * d.nE1 + vE1), D.sE0, sE1, Y);
+#pragma unroll
+        for (int c = 0; c < 3; c++) X[c] = fma(D.ground[c], Y[c], X[c]);
+      }
+      const Real wR = D.weight * pR;
+      const Real wM = D.weight * pM;
 #pragma unroll
       for (int c = 0; c < 3; c++) {
-        kahan_add(accR[c], cR[c], ringR[c]);
-        kahan_add(accM[c], cM[c], ringM[c]);
-        ringR[c] = 0;
-        ringM[c] = 0;
+        ringR[c] = fma(wR, X[c], ringR[c]);
+        ringM[c] = fma(wM, X[c], ringM[c]);
+      }
+      if (D.pad) {  // last direction of a theta ring
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+          kahan_add(accR[c], cR[c], ringR[c]);
+          kahan_add(accM[c], cM[c], ringM[c]);
+          ringR[c] = 0;
+          ringM[c] = 0;
+        }
       }
     }
   }
+  if (!valid) return;
   // beta_c(x) (atmosphere.clj:42-47, 140-151)
   const double h = r - P.R;
   const double er = exp(-(h / P.ray_scale)), em = exp(-(h / P.mie_scale));
@@ -292,6 +257,8 @@ __global__ void __launch_bounds__(256) k_surface_radiance(const AtmoParams* para
   const long long node = blockIdx.x;
   const AtmoParams& P = params[b];
   const int iE = (int)(node / d.nE1), kE = (int)(node % d.nE1);
+  // FP64 per node: x = (r, 0, 0), l = (sin, cos, 0), the frame, and the
+  // height and sun-elevation coordinates shared by every direction
   const double r = index_to_radius(P, d.nE0, (double)iE);
   const double ss = index_to_sin_sun_elevation(d.nE1, (double)kE);
   const d3 x = mk3(r, 0, 0), l = mk3(ss, sqrt(dmax(0.0, 1 - sqr(ss))), 0);
@@ -302,29 +269,54 @@ __global__ void __launch_bounds__(256) k_surface_radiance(const AtmoParams* para
   Real s[4];
   split_coord<Real>(height_to_index(P, d.n0, mag3(x)), d.n0, &u[0], &s[0]);
   split_coord<Real>(sun_elevation_to_index(d.n2, x, l), d.n2, &u[2], &s[2]);
+  const double c0 = dmul(dsub(r, P.R), dadd(r, P.R));  // |x|^2 - R^2
+  // elevation coordinate of (x, w, above) (atmosphere.clj:239-253) in Real:
+  // r sin_el = x.w, rho^2 = q, Delta + H^2 = (x.w)^2 + (H^2 - q) with both
+  // terms non-negative, and r sin_el - sqrt(Delta + H^2) rewritten without
+  // cancellation when x.w > 0
+  const Real q = (Real)c0, Hh2mq = (Real)dsub(P.Hh2, c0), rho = (Real)sqrt(dmax(0.0, c0));
+  const Real den = rho + rho + Real(2) * (Real)P.Hh, rr = (Real)r;
+  const Real lx = (Real)l.x, ly = (Real)l.y;
+  const Real scale1 = Real(d.n1 - 1), scale3 = Real(0.5) * Real(d.n3 - 1);
   const Vec4<Real>* tS = dS + (long long)b * d.n4();
   const Vec4<Real>* tM = FIRST ? Mt + (long long)b * d.n4() : nullptr;
   Real acc[3] = {0, 0, 0}, cmp[3] = {0, 0, 0};
   for (int w = threadIdx.x; w < d.Ph; w += blockDim.x) {
-    const DirLocal q = hdirs[w];
-    const d3 omega = to_world(n, o1, o2, q);
+    const DirLocal qd = hdirs[w];
+    const d3 omega = to_world(n, o1, o2, qd);
+    const Real wx = (Real)omega.x, wy = (Real)omega.y;
+    const Real pv = rr * wx;
+    const Real root = Bulk<Real>::sqrt(fma(pv, pv, Hh2mq));
+    const Real a = pv > Real(0) ? -Hh2mq / (pv + root) : pv - root;
     int uu[4] = {u[0], 0, u[2], 0};
     Real sx[4] = {s[0], 0, s[2], 0};
-    split_coord<Real>(elevation_to_index(P, d.n1, x, omega, 1), d.n1, &uu[1], &sx[1]);
-    split_coord<Real>(sun_angle_to_index(d.n3, omega, l), d.n3, &uu[3], &sx[3]);
+    Real lq;
+    {
+      // limit-quot (util.clj:403-420) with limits -0.5, 0
+      Real aa = a, bb = den;
+      if (aa == Real(0)) lq = Real(0);
+      else {
+        if (bb < Real(0)) { aa = -aa; bb = -bb; }
+        lq = aa < Real(0) ? (aa > bb * Real(-0.5) ? aa / bb : Real(-0.5)) : Real(0);
+      }
+    }
+    split_coord_r<Real>(scale1 * (Real(0.5) - lq), d.n1, &uu[1], &sx[1]);
+    const Real mu = fma(wx, lx, wy * ly);  // w.l, l.z = 0
+    split_coord_r<Real>(scale3 * (Real(1) + mu), d.n3, &uu[3], &sx[3]);
     Real val[3];
     interp4(tS, d, uu, sx, val);
     if (FIRST) {
       Real vm[3];
       interp4(tM, d, uu, sx, vm);
-      const Real ph = phase_cs<Real>((Real)P.mie_g, (Real)dot3(omega, l));
+      const Real ph = phase_cs<Real>((Real)P.mie_g, mu);
 #pragma unroll
       for (int c = 0; c < 3; c++) val[c] = fma(vm[c], ph, val[c]);
     }
-    const Real wgt = (Real)(q.w * dot3(omega, n));
+    const Real wgt = (Real)(qd.w * dot3(omega, n));
 #pragma unroll
     for (int c = 0; c < 3; c++) kahan_add(acc[c], cmp[c], val[c] * wgt);
   }
+  (void)q;
 #pragma unroll
   for (int c = 0; c < 3; c++) red[c][threadIdx.x] = acc[c];
   __syncthreads();
@@ -573,6 +565,26 @@ __global__ void k_output2(int n0, int n1, const Remap2<Real>* remap, const Vec4<
 }
 
 template <class Real>
+__global__ void k_add_to_sum(long long n, const Vec4<Real>* J, Vec4<float>* jsum, bool first) {
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  const Vec4<Real> v = J[t];
+  Vec4<float> o;
+  if (first) {
+    o.x = (float)v.x;
+    o.y = (float)v.y;
+    o.z = (float)v.z;
+  } else {
+    o = jsum[t];
+    o.x += (float)v.x;
+    o.y += (float)v.y;
+    o.z += (float)v.z;
+  }
+  o.w = 0;
+  jsum[t] = o;
+}
+
+template <class Real>
 __global__ void k_export(long long n, const Vec4<Real>* tab, float* out) {
   const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (t >= n) return;
@@ -609,6 +621,11 @@ void launch_output2(int B, int n0, int n1, const Remap2<Real>* remap, const Vec4
 }
 
 template <class Real>
+void launch_add_to_sum(long long n, const Vec4<Real>* J, Vec4<float>* jsum, bool first, cudaStream_t st) {
+  k_add_to_sum<Real><<<grid1(n, 256, 1), 256, 0, st>>>(n, J, jsum, first);
+}
+
+template <class Real>
 void launch_export(long long n, const Vec4<Real>* tab, float* out, cudaStream_t st) {
   k_export<Real><<<grid1(n, 256, 1), 256, 0, st>>>(n, tab, out);
 }
@@ -630,6 +647,7 @@ void launch_export(long long n, const Vec4<Real>* tab, float* out, cudaStream_t 
                                      cudaStream_t);                                                                \
   template void launch_output2<Real>(int, int, int, const Remap2<Real>*, const Vec4<Real>*, float*, cudaStream_t);  \
   template void launch_export<Real>(long long, const Vec4<Real>*, float*, cudaStream_t);                           \
+  template void launch_add_to_sum<Real>(long long, const Vec4<Real>*, Vec4<float>*, bool, cudaStream_t);            \
   template size_t point_scatter_smem<Real>(const BuildDims&, bool);
 
 SFSIM_INSTANTIATE(float)

@@ -1,6 +1,7 @@
 // kernels.h -- host-side launchers of the atmosphere LUT build kernels.
 #pragma once
 
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
 #include "atmo_params.h"
@@ -79,8 +80,80 @@ template <class Real>
 void launch_output2(int B, int n0, int n1, const Remap2<Real>* remap, const Vec4<Real>* tab, float* out,
                     cudaStream_t st);
 
+// Tables of a built atmosphere as sfsim's shaders read them (.scatter layout).
+struct QueryTables {
+  float radius, max_height, mie_g;
+  int t_height, t_elevation;
+  int height, elevation, light, heading;
+  const float* T;
+  const float* S;
+  const float* M;
+};
+
+// kind 0 transmittance_track(a, b), 1 transmittance_outer(a, b), 2
+// ray_scatter_track(l, a, b), 3 ray_scatter_outer(l, a, b), 4 in-scatter at
+// (a, b, l) with the horizon test choosing the table half.  Points [n][3].
+void launch_query_table(const QueryTables& q, int kind, long long n, const float* a, const float* b, const float* l,
+                        float* out, int weight_bits, cudaStream_t st);
+
+// Rendered in-scatter S + M phase(mie, v.l) at (x, v, l) by quadrature with
+// the order-summed point-scatter table Jsum (NULL: first order only).
+void launch_query_direct(const AtmoParams* params, const BuildDims& d, const Vec4<float>* Jsum, long long n,
+                         const double* x, const double* v, const double* l, float* out, cudaStream_t st);
+
+// jsum = (first ? 0 : jsum) + J, converted to float.
+template <class Real>
+void launch_add_to_sum(long long n, const Vec4<Real>* J, Vec4<float>* jsum, bool first, cudaStream_t st);
+
 // Plain-order float copy of an internal table (debug intermediates).
 template <class Real>
 void launch_export(long long n, const Vec4<Real>* tab, float* out, cudaStream_t st);
+
+// Tensor-core GEMM C[m][n] = alpha * sum_k A[m][k] B[n][k] (BF16 in, FP32
+// accumulate) with the epilogue the surrogate MLP needs.  M any, N <= 256,
+// K a multiple of 64 * splits; split > 1 only with the Cacc output.
+struct GemmArgs {
+  const __nv_bfloat16* A;
+  long long lda;
+  const __nv_bfloat16* B;
+  long long ldb;
+  int M, N;
+  long long K;
+  float alpha;
+  const float* bias;  // [N] added after alpha, or NULL
+  const float* dact;  // [M][N] multiplier applied after the bias, or NULL
+  float* Cf32;        // [M][ldc] or NULL
+  long long ldc;
+  float* Cacc;        // [M][ldc] accumulated with atomicAdd, or NULL
+  float* Dsilu;       // SiLU'(z) [M][N], or NULL
+  int silu;           // apply SiLU before the BF16 outputs
+  __nv_bfloat16* Hbf16;   // [M][ldh] or NULL
+  long long ldh;
+  __nv_bfloat16* HTbf16;  // transposed [N][ldht] or NULL
+  long long ldht;
+  int* error;         // set to 1 when a wait times out
+};
+
+int launch_gemm_tn(const GemmArgs& g, int splits, cudaStream_t st);
+
+// ---- surrogate MLP: 4 coordinates -> 128 Fourier features -> 4 x 256 SiLU -> 3 ----
+constexpr int kMlpIn = 128;
+constexpr int kMlpHidden = 256;
+constexpr int kMlpLayers = 4;
+
+void launch_features(long long n, const float* coords, __nv_bfloat16* F, __nv_bfloat16* FT, cudaStream_t st);
+void launch_head_forward(long long n, const __nv_bfloat16* H, const float* W5, const float* b5, float* out,
+                         cudaStream_t st);
+void launch_loss_grad(long long n, const float* out, const float* target, float* dout, float* loss, cudaStream_t st);
+void launch_head_backward(long long n, const float* dout, const __nv_bfloat16* H, const float* W5,
+                          const float* dsilu, __nv_bfloat16* dZ, __nv_bfloat16* dZT, float* dW5, float* db5,
+                          cudaStream_t st);
+void launch_bias_grad(long long n, int width, const __nv_bfloat16* dZT, float* db, cudaStream_t st);
+void launch_adam(long long count, float* w, const float* g, float* m, float* v, float lr, float beta1, float beta2,
+                 float eps, int step, int rows, int cols, __nv_bfloat16* wb, __nv_bfloat16* wbt, cudaStream_t st);
+void launch_to_bf16(long long count, const float* w, int rows, int cols, __nv_bfloat16* wb, __nv_bfloat16* wbt,
+                    cudaStream_t st);
+void launch_gather_batch(long long n, unsigned long long seed, float node_frac, const float* poolA, long long na,
+                         const float* poolB, long long nb, float* coords, float* target, cudaStream_t st);
 
 }  // namespace sfsim

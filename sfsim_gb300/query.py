@@ -1,0 +1,113 @@
+"""Queries of a built atmosphere on the GPU (the C ABI's context functions).
+
+`Context(cfg)` builds the four tables on the current CUDA device and keeps
+them there with the point-scatter table summed over the iterations.  Its
+methods take and return torch CUDA tensors of shape [n, 3]:
+  table(kind, a, b, light)  the lookups sfsim's shaders perform
+                            (resources/shaders/atmosphere/*.glsl)
+  direct(x, v, l)           rendered in-scatter S + M phase by direct quadrature
+"""
+from __future__ import annotations
+
+import ctypes
+
+from . import _lib
+from .config import AtmoConfig
+
+TRANSMITTANCE_TRACK = 0
+TRANSMITTANCE_OUTER = 1
+RAY_SCATTER_TRACK = 2
+RAY_SCATTER_OUTER = 3
+IN_SCATTER = 4
+
+
+class Context:
+    def __init__(self, cfg: AtmoConfig):
+        self.cfg = cfg.copy()
+        self._L = _lib.load()
+        self._ptr = ctypes.c_void_p()
+        _lib.check(self._L.sfsim_atmo_context_create(ctypes.byref(self.cfg), ctypes.byref(self._ptr)),
+                   "sfsim_atmo_context_create")
+
+    def close(self):
+        if self._ptr:
+            self._L.sfsim_atmo_context_destroy(self._ptr)
+            self._ptr = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def tables(self):
+        """Copies of the four tables (.scatter layout) as torch CUDA tensors."""
+        import torch
+        from .atmosphere_lut import table_shapes
+        ptrs = [ctypes.c_void_p() for _ in range(4)]
+        _lib.check(self._L.sfsim_atmo_context_tables(self._ptr, *[ctypes.byref(p) for p in ptrs]), "tables")
+        out = []
+        for p, shape in zip(ptrs, table_shapes(self.cfg)):
+            t = torch.empty(shape, dtype=torch.float32, device="cuda")
+            n = t.numel() * 4
+            torch.cuda.synchronize()
+            _cuda_copy(t.data_ptr(), p.value, n)
+            out.append(t)
+        return out
+
+    def point_scatter_sum(self):
+        """The point-scatter table summed over the iterations, [n0,n1,n2,n3,4] (RGB + pad), or None."""
+        import torch
+        p = ctypes.c_void_p()
+        _lib.check(self._L.sfsim_atmo_context_point_scatter_sum(self._ptr, ctypes.byref(p)), "point_scatter_sum")
+        if not p.value:
+            return None
+        s = tuple(self.cfg.ray_scatter_shape) + (4,)
+        t = torch.empty(s, dtype=torch.float32, device="cuda")
+        _cuda_copy(t.data_ptr(), p.value, t.numel() * 4)
+        return t
+
+    def table(self, kind: int, a, b, light=None, weight_bits: int = 0, out=None):
+        import torch
+        a = a.contiguous().float()
+        b = b.contiguous().float()
+        light = light.contiguous().float() if light is not None else None
+        n = a.shape[0]
+        out = out if out is not None else torch.empty((n, 3), dtype=torch.float32, device="cuda")
+        st = torch.cuda.current_stream().cuda_stream
+        _lib.check(self._L.sfsim_atmo_query_table(self._ptr, kind, n, a.data_ptr(), b.data_ptr(),
+                                                  light.data_ptr() if light is not None else None,
+                                                  out.data_ptr(), weight_bits, st), "query_table")
+        return out
+
+    def direct(self, x, v, l, out=None):
+        import torch
+        x = x.contiguous().double()
+        v = v.contiguous().double()
+        l = l.contiguous().double()
+        n = x.shape[0]
+        out = out if out is not None else torch.empty((n, 3), dtype=torch.float32, device="cuda")
+        st = torch.cuda.current_stream().cuda_stream
+        _lib.check(self._L.sfsim_atmo_query_direct(self._ptr, n, x.data_ptr(), v.data_ptr(), l.data_ptr(),
+                                                   out.data_ptr(), st), "query_direct")
+        return out
+
+
+def _cuda_copy(dst: int, src: int, nbytes: int) -> None:
+    """Device-to-device copy through torch (no extra CUDA bindings needed)."""
+    import torch
+    s = torch.cuda.current_stream()
+    # wrap the raw pointer as a tensor view through the CUDA array interface
+    class _Arr:
+        def __init__(self, ptr, n):
+            self.__cuda_array_interface__ = {"shape": (n,), "typestr": "|u1", "data": (ptr, False), "version": 3}
+    src_t = torch.as_tensor(_Arr(src, nbytes), device="cuda")
+    dst_t = torch.as_tensor(_Arr(dst, nbytes), device="cuda")
+    dst_t.copy_(src_t)
+    s.synchronize()
