@@ -202,6 +202,46 @@ int sfsim_atmo_query_table(const sfsim_atmo_context* ctx, int kind, long long n,
 int sfsim_atmo_query_direct(const sfsim_atmo_context* ctx, long long n, const double* x,
                             const double* v, const double* l, float* out, void* stream);
 
+/* ---- Surrogate of the rendered in-scatter ----------------------------------
+ * An MLP over the four table coordinates in [0, 1] (height, elevation, sun
+ * elevation, sun heading, as the in-scatter lookup forms them): 16-frequency
+ * sin/cos features per coordinate (128) -> 4 x 256 SiLU -> 3 outputs, the
+ * log of (S + M phase + 1e-8).  BF16 weights and activations, FP32
+ * accumulation and master weights; the hidden layers run on tcgen05 tensor
+ * cores in the forward and both backward GEMMs.  No counterpart in the
+ * reference. */
+typedef struct sfsim_atmo_surrogate_config {
+  int steps;                /* Adam steps */
+  int batch;                /* rows per step, a multiple of 1024 */
+  long long direct_samples; /* off-grid training points integrated by sfsim_atmo_query_direct */
+  float node_fraction;      /* share of each batch drawn from the table nodes */
+  float lr;                 /* initial learning rate, cosine decay to 0 */
+  unsigned long long seed;
+} sfsim_atmo_surrogate_config;
+
+/* Trains (or continues training) the context's surrogate on the GPU;
+ * loss_history (host, `steps` floats, may be NULL) receives each step's loss. */
+int sfsim_atmo_surrogate_train(sfsim_atmo_context* ctx, const sfsim_atmo_surrogate_config* cfg,
+                               float* loss_history);
+
+/* Parameter vector (FP32, W1 [256][128], b1, W2, b2, W3, b3, W4, b4 [256][256],
+ * W5 [3][256], b5): *count receives its length; `get` copies it out, `set`
+ * replaces it (host arrays, either may be NULL). */
+int sfsim_atmo_surrogate_parameters(sfsim_atmo_context* ctx, float* get, const float* set, long long* count);
+
+/* Loss and parameter gradients of one batch (host coords [n][4], targets
+ * [n][3]; n a multiple of 1024) without updating, for validation. */
+int sfsim_atmo_surrogate_gradients(sfsim_atmo_context* ctx, long long n, const float* coords,
+                                   const float* targets, float* loss, float* grads);
+
+/* Rendered in-scatter at (x, v, l) from the surrogate (DEVICE arrays as in
+ * sfsim_atmo_query_direct).  With threshold > 0, points where the surrogate
+ * and the table lookup differ by more than `threshold` (relative, floor 1e-7)
+ * are recomputed by direct quadrature; *n_fallback receives their number. */
+int sfsim_atmo_query_surrogate(sfsim_atmo_context* ctx, long long n, const double* x, const double* v,
+                               const double* l, float* out, float threshold, long long* n_fallback,
+                               void* stream);
+
 /* The surrogate's tensor-core GEMM, exposed for validation: C = A * B^T with
  * A [M][K] and B [N][K] row-major bf16 DEVICE arrays and C [M][N] float,
  * FP32 accumulation on tcgen05 tensor cores.  N <= 256; K a multiple of

@@ -24,8 +24,14 @@ EXPORTS = (
     "sfsim_atmo_last_error", "sfsim_atmo_version", "sfsim_atmo_census", "sfsim_atmo_sfu_peak",
     "sfsim_atmo_build_static", "sfsim_atmo_context_create", "sfsim_atmo_context_destroy",
     "sfsim_atmo_context_tables", "sfsim_atmo_context_point_scatter_sum", "sfsim_atmo_query_table",
-    "sfsim_atmo_query_direct", "sfsim_atmo_gemm_bf16",
+    "sfsim_atmo_query_direct", "sfsim_atmo_gemm_bf16", "sfsim_atmo_surrogate_train",
+    "sfsim_atmo_surrogate_parameters", "sfsim_atmo_surrogate_gradients", "sfsim_atmo_query_surrogate",
 )
+
+
+class SurrogateConfig(ctypes.Structure):
+    _fields_ = [("steps", ctypes.c_int), ("batch", ctypes.c_int), ("direct_samples", ctypes.c_longlong),
+                ("node_fraction", ctypes.c_float), ("lr", ctypes.c_float), ("seed", ctypes.c_ulonglong)]
 
 
 class Intermediates(ctypes.Structure):
@@ -82,6 +88,11 @@ def load(build: bool = False):
     L.sfsim_atmo_query_table.argtypes = [vp, ctypes.c_int, ctypes.c_longlong, vp, vp, vp, vp, ctypes.c_int, vp]
     L.sfsim_atmo_query_direct.argtypes = [vp, ctypes.c_longlong, vp, vp, vp, vp, vp]
     L.sfsim_atmo_gemm_bf16.argtypes = [vp, vp, vp, ctypes.c_int, ctypes.c_int, ctypes.c_longlong, ctypes.c_int, vp]
+    L.sfsim_atmo_surrogate_train.argtypes = [vp, ctypes.POINTER(SurrogateConfig), vp]
+    L.sfsim_atmo_surrogate_parameters.argtypes = [vp, vp, vp, ctypes.POINTER(ctypes.c_longlong)]
+    L.sfsim_atmo_surrogate_gradients.argtypes = [vp, ctypes.c_longlong, vp, vp, vp, vp]
+    L.sfsim_atmo_query_surrogate.argtypes = [vp, ctypes.c_longlong, vp, vp, vp, vp, ctypes.c_float,
+                                             ctypes.POINTER(ctypes.c_longlong), vp]
     L.sfsim_atmo_version.argtypes = []
     L.sfsim_atmo_version.restype = ctypes.c_char_p
     _lib = L

@@ -828,6 +828,8 @@ const char* sfsim_atmo_version(void) { return "sfsim-atmo-gb300 0.1.0 (sm_103a)"
 // Contexts: a built atmosphere kept on the device for queries.
 // ---------------------------------------------------------------------------
 
+struct Surrogate;
+
 struct sfsim_atmo_context {
   int dev;
   sfsim_atmo_config cfg;
@@ -836,6 +838,8 @@ struct sfsim_atmo_context {
   AtmoParams* params;
   float *T, *E, *S, *M;
   Vec4<float>* jsum;  // point scatter summed over the iterations, NULL without iterations
+  void* geom;         // per-node light directions (CellGeom<Real>)
+  Surrogate* sur;     // trained surrogate or NULL
 };
 
 namespace {
@@ -880,6 +884,7 @@ int context_build(sfsim_atmo_context* c) {
   CUDA_TRY(cudaStreamSynchronize(st));
   c->dims = d;
   c->params = w.params;
+  c->geom = w.setup.geom;
   c->T = w.oT;
   c->E = w.oE;
   c->S = w.oS;
@@ -888,6 +893,273 @@ int context_build(sfsim_atmo_context* c) {
 }
 
 }  // namespace
+
+// ---------------------------------------------------------------------------
+// Surrogate of the rendered in-scatter: Fourier features of the four table
+// coordinates -> 4 x 256 SiLU -> 3 log-RGB outputs, trained on the GPU.
+// ---------------------------------------------------------------------------
+
+constexpr float kLogEps = 1e-8f;  // outputs are log(value + kLogEps)
+
+// parameter offsets (floats) in the concatenated FP32 vector
+struct MlpLayout {
+  long long W[5], b[5], total;
+  int in[5], out[5];
+  MlpLayout() {
+    const int ins[5] = {kMlpIn, kMlpHidden, kMlpHidden, kMlpHidden, kMlpHidden};
+    const int outs[5] = {kMlpHidden, kMlpHidden, kMlpHidden, kMlpHidden, 3};
+    long long o = 0;
+    for (int l = 0; l < 5; l++) {
+      in[l] = ins[l];
+      out[l] = outs[l];
+      W[l] = o;
+      o += (long long)outs[l] * ins[l];
+      b[l] = o;
+      o += outs[l];
+    }
+    total = o;
+  }
+};
+
+struct Surrogate {
+  MlpLayout lay;
+  long long batch = 0;             // rows of the activation buffers
+  float *w = nullptr, *g = nullptr, *m = nullptr, *v = nullptr;  // master weights, grads, Adam moments
+  __nv_bfloat16 *wb[4] = {}, *wbt[4] = {};  // BF16 W_l [out][in] and W_l^T [in][out]
+  // activations of one batch
+  float *coords = nullptr, *target = nullptr, *out = nullptr, *dout = nullptr, *loss = nullptr;
+  __nv_bfloat16 *F = nullptr, *FT = nullptr, *H[4] = {}, *HT[4] = {}, *dZ[4] = {}, *dZT[4] = {};
+  float* dsilu[4] = {};
+  int* error = nullptr;
+  int trained_steps = 0;
+  std::vector<void*> allocs;
+  float* alloc_f(size_t n) {
+    void* p = nullptr;
+    if (cudaMalloc(&p, n * sizeof(float)) != cudaSuccess) return nullptr;
+    allocs.push_back(p);
+    return (float*)p;
+  }
+  __nv_bfloat16* alloc_h(size_t n) {
+    void* p = nullptr;
+    if (cudaMalloc(&p, n * sizeof(__nv_bfloat16)) != cudaSuccess) return nullptr;
+    allocs.push_back(p);
+    return (__nv_bfloat16*)p;
+  }
+  void free_all() {
+    for (void* p : allocs) cudaFree(p);
+    allocs.clear();
+  }
+};
+
+void surrogate_free(sfsim_atmo_context* c) {
+  if (c->sur) {
+    c->sur->free_all();
+    delete c->sur;
+    c->sur = nullptr;
+  }
+}
+
+// Xavier-uniform initial weights (seeded LCG on the host), zero biases.
+void init_weights(const MlpLayout& lay, unsigned long long seed, std::vector<float>& h) {
+  h.assign(lay.total, 0.0f);
+  unsigned long long s = seed * 6364136223846793005ull + 1442695040888963407ull;
+  for (int l = 0; l < 5; l++) {
+    const double a = std::sqrt(6.0 / (lay.in[l] + lay.out[l]));
+    for (long long t = 0; t < (long long)lay.in[l] * lay.out[l]; t++) {
+      s = s * 6364136223846793005ull + 1442695040888963407ull;
+      const double u = (double)(s >> 11) * (1.0 / 9007199254740992.0);
+      h[lay.W[l] + t] = (float)((2.0 * u - 1.0) * a);
+    }
+  }
+}
+
+int surrogate_alloc(sfsim_atmo_context* c, long long batch, unsigned long long seed) {
+  if (!c->sur) {
+    c->sur = new Surrogate();
+    Surrogate& S = *c->sur;
+    const long long P = S.lay.total;
+    S.w = S.alloc_f(P);
+    S.g = S.alloc_f(P);
+    S.m = S.alloc_f(P);
+    S.v = S.alloc_f(P);
+    S.loss = S.alloc_f(1);
+    void* e = nullptr;
+    if (cudaMalloc(&e, sizeof(int)) != cudaSuccess) return fail(SFSIM_ATMO_ENOMEM, "surrogate allocation failed");
+    S.allocs.push_back(e);
+    S.error = (int*)e;
+    for (int l = 0; l < 4; l++) {
+      S.wb[l] = S.alloc_h((size_t)S.lay.in[l] * S.lay.out[l]);
+      S.wbt[l] = S.alloc_h((size_t)S.lay.in[l] * S.lay.out[l]);
+    }
+    if (!S.w || !S.g || !S.m || !S.v || !S.loss || !S.wb[3] || !S.wbt[3])
+      return fail(SFSIM_ATMO_ENOMEM, "surrogate allocation failed");
+    std::vector<float> h;
+    init_weights(S.lay, seed, h);
+    CUDA_TRY(cudaMemcpy(S.w, h.data(), sizeof(float) * P, cudaMemcpyHostToDevice));
+    CUDA_TRY(cudaMemset(S.m, 0, sizeof(float) * P));
+    CUDA_TRY(cudaMemset(S.v, 0, sizeof(float) * P));
+    CUDA_TRY(cudaMemset(S.error, 0, sizeof(int)));
+    for (int l = 0; l < 4; l++)
+      launch_to_bf16((long long)S.lay.in[l] * S.lay.out[l], S.w + S.lay.W[l], S.lay.out[l], S.lay.in[l], S.wb[l],
+                     S.wbt[l], 0);
+    CUDA_TRY(cudaGetLastError());
+  }
+  Surrogate& S = *c->sur;
+  if (S.batch < batch) {
+    // activation buffers for `batch` rows
+    auto drop = [&](void* p) {
+      if (!p) return;
+      for (size_t i = 0; i < S.allocs.size(); i++)
+        if (S.allocs[i] == p) {
+          cudaFree(p);
+          S.allocs.erase(S.allocs.begin() + i);
+          return;
+        }
+    };
+    drop(S.coords); drop(S.target); drop(S.out); drop(S.dout); drop(S.F); drop(S.FT);
+    for (int l = 0; l < 4; l++) {
+      drop(S.H[l]); drop(S.HT[l]); drop(S.dZ[l]); drop(S.dZT[l]); drop(S.dsilu[l]);
+    }
+    S.coords = S.alloc_f(4 * batch);
+    S.target = S.alloc_f(3 * batch);
+    S.out = S.alloc_f(3 * batch);
+    S.dout = S.alloc_f(3 * batch);
+    S.F = S.alloc_h(kMlpIn * batch);
+    S.FT = S.alloc_h(kMlpIn * batch);
+    bool okay = S.coords && S.target && S.out && S.dout && S.F && S.FT;
+    for (int l = 0; l < 4 && okay; l++) {
+      S.H[l] = S.alloc_h(kMlpHidden * batch);
+      S.HT[l] = S.alloc_h(kMlpHidden * batch);
+      S.dZ[l] = S.alloc_h(kMlpHidden * batch);
+      S.dZT[l] = S.alloc_h(kMlpHidden * batch);
+      S.dsilu[l] = S.alloc_f(kMlpHidden * batch);
+      okay = S.H[l] && S.HT[l] && S.dZ[l] && S.dZT[l] && S.dsilu[l];
+    }
+    if (!okay) {
+      S.batch = 0;
+      return fail(SFSIM_ATMO_ENOMEM, "surrogate activation allocation failed");
+    }
+    S.batch = batch;
+  }
+  return 0;
+}
+
+// Forward pass over n rows of S.coords (n <= S.batch); `train` keeps what the
+// backward pass needs.  Leaves log-RGB predictions in S.out.
+int surrogate_forward(Surrogate& S, long long n, bool train, cudaStream_t st) {
+  launch_features(n, S.coords, S.F, train ? S.FT : nullptr, st);
+  const __nv_bfloat16* prev = S.F;
+  for (int l = 0; l < 4; l++) {
+    GemmArgs g = {};
+    g.A = prev;
+    g.lda = S.lay.in[l];
+    g.B = S.wb[l];
+    g.ldb = S.lay.in[l];
+    g.M = (int)n;
+    g.N = S.lay.out[l];
+    g.K = S.lay.in[l];
+    g.alpha = 1.0f;
+    g.bias = S.w + S.lay.b[l];
+    g.Dsilu = train ? S.dsilu[l] : nullptr;
+    g.silu = 1;
+    g.Hbf16 = S.H[l];
+    g.ldh = S.lay.out[l];
+    g.HTbf16 = train ? S.HT[l] : nullptr;
+    g.ldht = n;
+    g.error = S.error;
+    if (launch_gemm_tn(g, 1, st)) return fail(SFSIM_ATMO_ECUDA, "forward GEMM launch failed");
+    prev = S.H[l];
+  }
+  launch_head_forward(n, S.H[3], S.w + S.lay.W[4], S.w + S.lay.b[4], S.out, st);
+  CUDA_TRY(cudaGetLastError());
+  return 0;
+}
+
+// Gradients of the mean squared log-RGB error over n rows into S.g (zeroed
+// first); the loss lands in S.loss.
+int surrogate_backward(Surrogate& S, long long n, cudaStream_t st) {
+  CUDA_TRY(cudaMemsetAsync(S.g, 0, sizeof(float) * S.lay.total, st));
+  CUDA_TRY(cudaMemsetAsync(S.loss, 0, sizeof(float), st));
+  launch_loss_grad(n, S.out, S.target, S.dout, S.loss, st);
+  launch_head_backward(n, S.dout, S.H[3], S.w + S.lay.W[4], S.dsilu[3], S.dZ[3], S.dZT[3], S.g + S.lay.W[4],
+                       S.g + S.lay.b[4], st);
+  int splits = 1;
+  while (splits < 64 && n % (64LL * splits * 2) == 0) splits *= 2;
+  for (int l = 3; l >= 0; l--) {
+    // dW_l = dZ_l^T H_{l-1}: A = dZ_l^T [out][n], B = H_{l-1}^T [in][n], K = n
+    GemmArgs g = {};
+    g.A = S.dZT[l];
+    g.lda = n;
+    g.B = l > 0 ? S.HT[l - 1] : S.FT;
+    g.ldb = n;
+    g.M = S.lay.out[l];
+    g.N = S.lay.in[l];
+    g.K = n;
+    g.alpha = 1.0f;
+    g.Cacc = S.g + S.lay.W[l];
+    g.ldc = S.lay.in[l];
+    g.error = S.error;
+    if (launch_gemm_tn(g, splits, st)) return fail(SFSIM_ATMO_ECUDA, "weight-gradient GEMM launch failed");
+    launch_bias_grad(n, S.lay.out[l], S.dZT[l], S.g + S.lay.b[l], st);
+    if (l > 0) {
+      // dZ_{l-1} = (dZ_l W_l) * SiLU'(z_{l-1}): A = dZ_l [n][out], B = W_l^T [in][out]
+      GemmArgs h = {};
+      h.A = S.dZ[l];
+      h.lda = S.lay.out[l];
+      h.B = S.wbt[l];
+      h.ldb = S.lay.out[l];
+      h.M = (int)n;
+      h.N = S.lay.in[l];
+      h.K = S.lay.out[l];
+      h.alpha = 1.0f;
+      h.dact = S.dsilu[l - 1];
+      h.Hbf16 = S.dZ[l - 1];
+      h.ldh = S.lay.in[l];
+      h.HTbf16 = S.dZT[l - 1];
+      h.ldht = n;
+      h.error = S.error;
+      if (launch_gemm_tn(h, 1, st)) return fail(SFSIM_ATMO_ECUDA, "activation-gradient GEMM launch failed");
+    }
+  }
+  CUDA_TRY(cudaGetLastError());
+  return 0;
+}
+
+void surrogate_adam(Surrogate& S, float lr, int step, cudaStream_t st) {
+  const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
+  for (int l = 0; l < 5; l++) {
+    const long long nw = (long long)S.lay.in[l] * S.lay.out[l];
+    launch_adam(nw, S.w + S.lay.W[l], S.g + S.lay.W[l], S.m + S.lay.W[l], S.v + S.lay.W[l], lr, b1, b2, eps, step,
+                S.lay.out[l], S.lay.in[l], l < 4 ? S.wb[l] : nullptr, l < 4 ? S.wbt[l] : nullptr, st);
+    launch_adam(S.lay.out[l], S.w + S.lay.b[l], S.g + S.lay.b[l], S.m + S.lay.b[l], S.v + S.lay.b[l], lr, b1, b2,
+                eps, step, 1, S.lay.out[l], nullptr, nullptr, st);
+  }
+}
+
+QueryTables context_tables(const sfsim_atmo_context* ctx) {
+  QueryTables q;
+  q.radius = (float)ctx->cfg.radius;
+  q.max_height = (float)ctx->cfg.height;
+  q.mie_g = (float)ctx->cfg.mie.scatter_g;
+  q.t_height = ctx->dims.nT0;
+  q.t_elevation = ctx->dims.nT1;
+  q.height = ctx->dims.n0;
+  q.elevation = ctx->dims.n1;
+  q.light = ctx->dims.n2;
+  q.heading = ctx->dims.n3;
+  q.T = ctx->T;
+  q.S = ctx->S;
+  q.M = ctx->M;
+  return q;
+}
+
+int check_error_flag(Surrogate& S, cudaStream_t st) {
+  int h = 0;
+  CUDA_TRY(cudaMemcpyAsync(&h, S.error, sizeof(int), cudaMemcpyDeviceToHost, st));
+  CUDA_TRY(cudaStreamSynchronize(st));
+  if (h) return fail(SFSIM_ATMO_ECUDA, "a tensor-core GEMM wait timed out");
+  return 0;
+}
 
 // ---------------------------------------------------------------------------
 // Allocation-free build.  Some callers cannot call cudaMalloc: code running
@@ -986,6 +1258,7 @@ int sfsim_atmo_context_create(const sfsim_atmo_config* cfg, sfsim_atmo_context**
   c->dev = dev;
   c->cfg = *cfg;
   c->mem = nullptr;
+  c->sur = nullptr;
   rc = cfg->precision == SFSIM_ATMO_FP64 ? context_build<double>(c) : context_build<float>(c);
   if (rc) {
     if (c->mem) cudaFree(c->mem);
@@ -1001,6 +1274,7 @@ int sfsim_atmo_context_destroy(sfsim_atmo_context* ctx) {
   int cur = 0;
   cudaGetDevice(&cur);
   cudaSetDevice(ctx->dev);
+  surrogate_free(ctx);
   cudaError_t e = ctx->mem ? cudaFree(ctx->mem) : cudaSuccess;
   cudaSetDevice(cur);
   delete ctx;
@@ -1084,3 +1358,184 @@ extern "C" int sfsim_atmo_gemm_bf16(const void* A, const void* B, float* C, int 
   CUDA_TRY(cudaGetLastError());
   return 0;
 }
+
+// ---------------------------------------------------------------------------
+// Surrogate entry points
+// ---------------------------------------------------------------------------
+
+namespace {
+
+int surrogate_pools(sfsim_atmo_context* c, long long n_direct, unsigned long long seed, float** node_pool,
+                    float** direct_pool, std::vector<void*>& temps, cudaStream_t st) {
+  const BuildDims& d = c->dims;
+  void* p = nullptr;
+  if (cudaMalloc(&p, sizeof(float) * 7 * (size_t)d.n4()) != cudaSuccess)
+    return fail(SFSIM_ATMO_ENOMEM, "node pool allocation failed");
+  temps.push_back(p);
+  *node_pool = (float*)p;
+  launch_node_pool(d, c->S, c->M, (const CellGeom<float>*)c->geom, (float)c->cfg.mie.scatter_g, kLogEps, *node_pool,
+                   st);
+  *direct_pool = nullptr;
+  if (n_direct > 0) {
+    if (cudaMalloc(&p, sizeof(float) * 7 * (size_t)n_direct) != cudaSuccess)
+      return fail(SFSIM_ATMO_ENOMEM, "direct pool allocation failed");
+    temps.push_back(p);
+    *direct_pool = (float*)p;
+    const long long chunk = 1 << 20;
+    double* xvl = nullptr;
+    float *vals = nullptr, *crd = nullptr;
+    if (cudaMalloc(&xvl, sizeof(double) * 9 * chunk) != cudaSuccess ||
+        cudaMalloc(&vals, sizeof(float) * 3 * chunk) != cudaSuccess ||
+        cudaMalloc(&crd, sizeof(float) * 4 * chunk) != cudaSuccess)
+      return fail(SFSIM_ATMO_ENOMEM, "direct sample allocation failed");
+    temps.push_back(xvl);
+    temps.push_back(vals);
+    temps.push_back(crd);
+    const QueryTables q = context_tables(c);
+    for (long long o = 0; o < n_direct; o += chunk) {
+      const long long m = std::min(chunk, n_direct - o);
+      launch_random_queries(m, seed * 1000003ull + (unsigned long long)o, c->cfg.radius, c->cfg.height, xvl,
+                            xvl + 3 * chunk, xvl + 6 * chunk, st);
+      launch_query_direct(c->params, d, c->jsum, m, xvl, xvl + 3 * chunk, xvl + 6 * chunk, vals, st);
+      launch_query_coords(q, m, xvl, xvl + 3 * chunk, xvl + 6 * chunk, crd, nullptr, st);
+      launch_make_pool(m, crd, vals, kLogEps, *direct_pool + 7 * o, st);
+    }
+  }
+  CUDA_TRY(cudaGetLastError());
+  return 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+int sfsim_atmo_surrogate_train(sfsim_atmo_context* ctx, const sfsim_atmo_surrogate_config* sc, float* loss_history) {
+  if (!ctx || !sc) return fail(SFSIM_ATMO_ENULL, "NULL argument");
+  if (ctx->cfg.precision != SFSIM_ATMO_FP32) return fail(SFSIM_ATMO_EINVAL, "the surrogate needs an FP32 context");
+  if (sc->steps < 0 || sc->batch < 1024 || sc->batch % 1024 != 0 || sc->direct_samples < 0 ||
+      !(sc->node_fraction >= 0 && sc->node_fraction <= 1) || !(sc->lr > 0))
+    return fail(SFSIM_ATMO_EINVAL, "steps >= 0, batch a positive multiple of 1024, lr > 0, node_fraction in [0, 1]");
+  std::lock_guard<std::mutex> lock(g_mutex);
+  int cur = 0;
+  CUDA_TRY(cudaGetDevice(&cur));
+  if (cur != ctx->dev) return fail(SFSIM_ATMO_EINVAL, "the context belongs to another device");
+  int rc = surrogate_alloc(ctx, sc->batch, sc->seed);
+  if (rc) return rc;
+  Surrogate& S = *ctx->sur;
+  cudaStream_t st = g_stream[ctx->dev];
+  std::vector<void*> temps;
+  float *node_pool = nullptr, *direct_pool = nullptr;
+  float* hist = nullptr;
+  rc = surrogate_pools(ctx, sc->direct_samples, sc->seed, &node_pool, &direct_pool, temps, st);
+  if (!rc && cudaMalloc(&hist, sizeof(float) * std::max(1, sc->steps)) != cudaSuccess)
+    rc = fail(SFSIM_ATMO_ENOMEM, "loss history allocation failed");
+  if (hist) temps.push_back(hist);
+  const long long n = sc->batch;
+  for (int t = 0; t < sc->steps && !rc; t++) {
+    const float lr = sc->lr * 0.5f * (1.0f + std::cos(3.14159265358979f * (float)t / (float)sc->steps));
+    launch_gather_batch(n, sc->seed * 0x9E3779B97F4A7C15ull + (unsigned long long)t, sc->node_fraction, node_pool,
+                        ctx->dims.n4(), direct_pool, sc->direct_samples, S.coords, S.target, st);
+    if ((rc = surrogate_forward(S, n, true, st))) break;
+    if ((rc = surrogate_backward(S, n, st))) break;
+    surrogate_adam(S, lr, S.trained_steps + t + 1, st);
+    if (cudaMemcpyAsync(hist + t, S.loss, sizeof(float), cudaMemcpyDeviceToDevice, st) != cudaSuccess)
+      rc = fail(SFSIM_ATMO_ECUDA, "loss copy failed");
+  }
+  if (!rc && loss_history && sc->steps > 0 &&
+      cudaMemcpyAsync(loss_history, hist, sizeof(float) * sc->steps, cudaMemcpyDeviceToHost, st) != cudaSuccess)
+    rc = fail(SFSIM_ATMO_ECUDA, "loss history copy failed");
+  if (!rc) rc = check_error_flag(S, st);
+  cudaStreamSynchronize(st);
+  for (void* p : temps) cudaFree(p);
+  if (!rc) S.trained_steps += sc->steps;
+  return rc;
+}
+
+int sfsim_atmo_surrogate_parameters(sfsim_atmo_context* ctx, float* get, const float* set, long long* count) {
+  if (!ctx) return fail(SFSIM_ATMO_ENULL, "context is NULL");
+  MlpLayout lay;
+  if (count) *count = lay.total;
+  if (!get && !set) return 0;
+  std::lock_guard<std::mutex> lock(g_mutex);
+  int rc = surrogate_alloc(ctx, 1024, 1);
+  if (rc) return rc;
+  Surrogate& S = *ctx->sur;
+  if (set) {
+    CUDA_TRY(cudaMemcpy(S.w, set, sizeof(float) * lay.total, cudaMemcpyHostToDevice));
+    for (int l = 0; l < 4; l++)
+      launch_to_bf16((long long)lay.in[l] * lay.out[l], S.w + lay.W[l], lay.out[l], lay.in[l], S.wb[l], S.wbt[l], 0);
+    CUDA_TRY(cudaDeviceSynchronize());
+  }
+  if (get) CUDA_TRY(cudaMemcpy(get, S.w, sizeof(float) * lay.total, cudaMemcpyDeviceToHost));
+  return 0;
+}
+
+int sfsim_atmo_surrogate_gradients(sfsim_atmo_context* ctx, long long n, const float* coords, const float* targets,
+                                   float* loss, float* grads) {
+  if (!ctx || !coords || !targets) return fail(SFSIM_ATMO_ENULL, "NULL argument");
+  if (n < 1024 || n % 1024 != 0) return fail(SFSIM_ATMO_EINVAL, "n must be a positive multiple of 1024");
+  std::lock_guard<std::mutex> lock(g_mutex);
+  int rc = surrogate_alloc(ctx, n, 1);
+  if (rc) return rc;
+  Surrogate& S = *ctx->sur;
+  cudaStream_t st = g_stream[ctx->dev];
+  CUDA_TRY(cudaMemcpyAsync(S.coords, coords, sizeof(float) * 4 * n, cudaMemcpyHostToDevice, st));
+  CUDA_TRY(cudaMemcpyAsync(S.target, targets, sizeof(float) * 3 * n, cudaMemcpyHostToDevice, st));
+  if ((rc = surrogate_forward(S, n, true, st))) return rc;
+  if ((rc = surrogate_backward(S, n, st))) return rc;
+  if (loss) CUDA_TRY(cudaMemcpyAsync(loss, S.loss, sizeof(float), cudaMemcpyDeviceToHost, st));
+  if (grads) CUDA_TRY(cudaMemcpyAsync(grads, S.g, sizeof(float) * S.lay.total, cudaMemcpyDeviceToHost, st));
+  CUDA_TRY(cudaStreamSynchronize(st));
+  return check_error_flag(S, st);
+}
+
+int sfsim_atmo_query_surrogate(sfsim_atmo_context* ctx, long long n, const double* x, const double* v,
+                               const double* l, float* out, float threshold, long long* n_fallback, void* stream) {
+  if (!ctx || !x || !v || !l || !out) return fail(SFSIM_ATMO_ENULL, "NULL argument");
+  if (!ctx->sur) return fail(SFSIM_ATMO_EINVAL, "the context has no trained surrogate");
+  if (n < 0) return fail(SFSIM_ATMO_EINVAL, "n must be non-negative");
+  if (n_fallback) *n_fallback = 0;
+  if (n == 0) return 0;
+  std::lock_guard<std::mutex> lock(g_mutex);
+  const long long chunk = 1 << 18;
+  int rc = surrogate_alloc(ctx, chunk, 1);
+  if (rc) return rc;
+  Surrogate& S = *ctx->sur;
+  cudaStream_t st = (cudaStream_t)stream;
+  const QueryTables q = context_tables(ctx);
+  const bool fallback = threshold > 0;
+  unsigned char* mask = nullptr;
+  unsigned long long* count = nullptr;
+  if (fallback) {
+    if (cudaMalloc(&mask, n) != cudaSuccess || cudaMalloc(&count, sizeof(unsigned long long)) != cudaSuccess) {
+      if (mask) cudaFree(mask);
+      return fail(SFSIM_ATMO_ENOMEM, "fallback mask allocation failed");
+    }
+    CUDA_TRY(cudaMemsetAsync(count, 0, sizeof(unsigned long long), st));
+  }
+  // S.dout holds the table values of a chunk when falling back
+  for (long long o = 0; o < n && !rc; o += chunk) {
+    const long long m = std::min(chunk, n - o);
+    const long long mp = (m + 127) / 128 * 128;
+    launch_query_coords(q, m, x + 3 * o, v + 3 * o, l + 3 * o, S.coords, fallback ? S.dout : nullptr, st);
+    if (mp > m) CUDA_TRY(cudaMemsetAsync(S.coords + 4 * m, 0, sizeof(float) * 4 * (mp - m), st));
+    if ((rc = surrogate_forward(S, mp, false, st))) break;
+    launch_surrogate_finish(m, S.out, kLogEps, fallback ? S.dout : nullptr, threshold, 1e-7f, out + 3 * o,
+                            fallback ? mask + o : nullptr, count, st);
+  }
+  if (!rc && fallback)
+    launch_query_direct(ctx->params, ctx->dims, ctx->jsum, n, x, v, l, out, st, mask);
+  if (!rc && cudaGetLastError() != cudaSuccess) rc = fail(SFSIM_ATMO_ECUDA, "surrogate query launch failed");
+  if (fallback) {
+    unsigned long long h = 0;
+    if (!rc && cudaMemcpyAsync(&h, count, sizeof(h), cudaMemcpyDeviceToHost, st) == cudaSuccess &&
+        cudaStreamSynchronize(st) == cudaSuccess && n_fallback)
+      *n_fallback = (long long)h;
+    cudaStreamSynchronize(st);
+    cudaFree(mask);
+    cudaFree(count);
+  }
+  return rc;
+}
+
+}  // extern "C"

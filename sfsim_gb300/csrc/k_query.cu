@@ -242,8 +242,7 @@ __global__ void k_query_table(GlslEnv e, int kind, long long n, const float* A, 
   out[3 * t + 2] = r.z;
 }
 
-void launch_query_table(const QueryTables& q, int kind, long long n, const float* a, const float* b, const float* l,
-                        float* out, int weight_bits, cudaStream_t st) {
+static GlslEnv make_env(const QueryTables& q, int weight_bits) {
   GlslEnv e;
   e.radius = q.radius;
   e.max_height = q.max_height;
@@ -258,8 +257,159 @@ void launch_query_table(const QueryTables& q, int kind, long long n, const float
   e.M = q.M;
   e.weight_bits = weight_bits;
   e.mie_g = q.mie_g;
+  return e;
+}
+
+void launch_query_table(const QueryTables& q, int kind, long long n, const float* a, const float* b, const float* l,
+                        float* out, int weight_bits, cudaStream_t st) {
+  const GlslEnv e = make_env(q, weight_bits);
   const int blk = 128;
   k_query_table<<<(unsigned)((n + blk - 1) / blk), blk, 0, st>>>(e, kind, n, a, b, l, out);
+}
+
+// Table coordinates in [0, 1] of (x, v, l) as the in-scatter lookup forms them
+// (core/ray-scatter-forward.glsl order reversed to height, elevation, sun
+// elevation, sun heading), with the table half chosen by the horizon test;
+// the table value there (S + M phase) as a by-product when `table` is set.
+__global__ void k_query_coords(GlslEnv e, long long n, const double* X, const double* V, const double* L,
+                               float* coords, float* table) {
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  const f3 p = F3((float)X[3 * t], (float)X[3 * t + 1], (float)X[3 * t + 2]);
+  const f3 d = F3((float)V[3 * t], (float)V[3 * t + 1], (float)V[3 * t + 2]);
+  const f3 l = F3((float)L[3 * t], (float)L[3 * t + 1], (float)L[3 * t + 2]);
+  float idx[4];
+  ray_scatter_forward_g(e, p, d, l, is_above_horizon_g(e, p, d), idx);
+  coords[4 * t] = idx[3];
+  coords[4 * t + 1] = idx[2];
+  coords[4 * t + 2] = idx[1];
+  coords[4 * t + 3] = idx[0];
+  if (table) {
+    const f3 r = in_scatter_g(e, idx, fdot(d, l));
+    table[3 * t] = r.x;
+    table[3 * t + 1] = r.y;
+    table[3 * t + 2] = r.z;
+  }
+}
+
+void launch_query_coords(const QueryTables& q, long long n, const double* x, const double* v, const double* l,
+                         float* coords, float* table, cudaStream_t st) {
+  const GlslEnv e = make_env(q, 0);
+  const int blk = 128;
+  k_query_coords<<<(unsigned)((n + blk - 1) / blk), blk, 0, st>>>(e, n, x, v, l, coords, table);
+}
+
+__device__ __forceinline__ unsigned long long hash64(unsigned long long z) {
+  z += 0x9E3779B97F4A7C15ull;
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+
+__device__ __forceinline__ double unit_uniform(unsigned long long h) { return (double)(h >> 11) * (1.0 / 9007199254740992.0); }
+
+// Uniform direction on the sphere from two uniforms (z uniform in [-1, 1]).
+__device__ __forceinline__ d3 sphere_direction(double u1, double u2) {
+  const double z = 2.0 * u1 - 1.0, phi = 2.0 * 3.14159265358979323846 * u2;
+  const double r = sqrt(dmax(0.0, 1.0 - z * z));
+  return mk3(r * cos(phi), r * sin(phi), z);
+}
+
+// Random queries: height uniform in [0, H], position direction, view and sun
+// uniform on the sphere.
+__global__ void k_random_queries(long long n, unsigned long long seed, double R, double H, double* X, double* V,
+                                 double* L) {
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  unsigned long long h = hash64(seed * 0x632BE59BD9B4E019ull + (unsigned long long)t);
+  double u[7];
+  for (int i = 0; i < 7; i++) {
+    h = hash64(h);
+    u[i] = unit_uniform(h);
+  }
+  const double r = R + H * u[0];
+  const d3 p = sphere_direction(u[1], u[2]), v = sphere_direction(u[3], u[4]), l = sphere_direction(u[5], u[6]);
+  X[3 * t] = r * p.x;
+  X[3 * t + 1] = r * p.y;
+  X[3 * t + 2] = r * p.z;
+  V[3 * t] = v.x;
+  V[3 * t + 1] = v.y;
+  V[3 * t + 2] = v.z;
+  L[3 * t] = l.x;
+  L[3 * t + 1] = l.y;
+  L[3 * t + 2] = l.z;
+}
+
+void launch_random_queries(long long n, unsigned long long seed, double R, double H, double* x, double* v, double* l,
+                           cudaStream_t st) {
+  k_random_queries<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(n, seed, R, H, x, v, l);
+}
+
+// Training pool of the table nodes: coordinates node / (size - 1) and the
+// log of the stored in-scatter S + M phase(mie g, v.l) (.scatter layout).
+__global__ void k_node_pool(BuildDims d, const float* S, const float* M, const CellGeom<float>* geom, float mie_g,
+                            float eps, float* pool) {
+  const long long node = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (node >= d.n4()) return;
+  const int a = (int)(node % d.n3);
+  const int k = (int)((node / d.n3) % d.n2);
+  const int j = (int)((node / ((long long)d.n3 * d.n2)) % d.n1);
+  const int i = (int)(node / ((long long)d.n3 * d.n2 * d.n1));
+  const long long dst = ((long long)i * d.n2 + k) * ((long long)d.n1 * d.n3) + (long long)j * d.n3 + a;
+  const float ph = phase_cs<float>(mie_g, geom[node].mu);
+  float* o = pool + 7 * node;
+  o[0] = (float)i / (d.n0 - 1);
+  o[1] = (float)j / (d.n1 - 1);
+  o[2] = (float)k / (d.n2 - 1);
+  o[3] = (float)a / (d.n3 - 1);
+  for (int c = 0; c < 3; c++) o[4 + c] = logf(fmaxf(S[3 * dst + c] + M[3 * dst + c] * ph, 0.0f) + eps);
+}
+
+void launch_node_pool(const BuildDims& d, const float* S, const float* M, const CellGeom<float>* geom, float mie_g,
+                      float eps, float* pool, cudaStream_t st) {
+  k_node_pool<<<(unsigned)((d.n4() + 255) / 256), 256, 0, st>>>(d, S, M, geom, mie_g, eps, pool);
+}
+
+// pool rows (coords, log(value + eps)) from coordinates and values
+__global__ void k_make_pool(long long n, const float* coords, const float* values, float eps, float* pool) {
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  for (int c = 0; c < 4; c++) pool[7 * t + c] = coords[4 * t + c];
+  for (int c = 0; c < 3; c++) pool[7 * t + 4 + c] = logf(fmaxf(values[3 * t + c], 0.0f) + eps);
+}
+
+void launch_make_pool(long long n, const float* coords, const float* values, float eps, float* pool,
+                      cudaStream_t st) {
+  k_make_pool<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(n, coords, values, eps, pool);
+}
+
+// out = exp(y) - eps; mask[i] = 1 where it differs from the table value by
+// more than `thr` relative (floor `floor_abs`), when `table` is given.
+__global__ void k_surrogate_finish(long long n, const float* y, float eps, const float* table, float thr,
+                                   float floor_abs, float* out, unsigned char* mask, unsigned long long* count) {
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  bool flag = false;
+  if (t < n) {
+    for (int c = 0; c < 3; c++) {
+      const float v = fmaxf(expf(y[3 * t + c]) - eps, 0.0f);
+      out[3 * t + c] = v;
+      if (table) {
+        const float r = table[3 * t + c];
+        if (fabsf(v - r) > thr * fmaxf(fabsf(r), floor_abs)) flag = true;
+      }
+    }
+    if (mask) mask[t] = flag ? 1 : 0;
+  }
+  if (count) {
+    const unsigned b = __ballot_sync(0xffffffffu, flag);
+    if ((threadIdx.x & 31) == 0 && b) atomicAdd(count, (unsigned long long)__popc(b));
+  }
+}
+
+void launch_surrogate_finish(long long n, const float* y, float eps, const float* table, float thr, float floor_abs,
+                             float* out, unsigned char* mask, unsigned long long* count, cudaStream_t st) {
+  k_surrogate_finish<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(n, y, eps, table, thr, floor_abs, out, mask,
+                                                                   count);
 }
 
 // ---------------------------------------------------------------------------
@@ -285,10 +435,12 @@ __device__ __forceinline__ float elevation_coordinate_f(float q, float pv, float
 template <int WARPS>
 __global__ void __launch_bounds__(WARPS * 32) k_query_direct(const AtmoParams* params, BuildDims d,
                                                              const Vec4<float>* Jsum, long long n, const double* X,
-                                                             const double* V, const double* Lt, float* out) {
+                                                             const double* V, const double* Lt, float* out,
+                                                             const unsigned char* mask) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const long long qi = blockIdx.x * (long long)WARPS + warp;
   if (qi >= n) return;
+  if (mask && !mask[qi]) return;
   const AtmoParams& P = params[0];
   const d3 x = mk3(X[3 * qi], X[3 * qi + 1], X[3 * qi + 2]);
   const d3 v = mk3(V[3 * qi], V[3 * qi + 1], V[3 * qi + 2]);
@@ -390,10 +542,11 @@ __global__ void __launch_bounds__(WARPS * 32) k_query_direct(const AtmoParams* p
 }
 
 void launch_query_direct(const AtmoParams* params, const BuildDims& d, const Vec4<float>* Jsum, long long n,
-                         const double* x, const double* v, const double* l, float* out, cudaStream_t st) {
+                         const double* x, const double* v, const double* l, float* out, cudaStream_t st,
+                         const unsigned char* mask) {
   constexpr int WARPS = 8;
   const unsigned blocks = (unsigned)((n + WARPS - 1) / WARPS);
-  k_query_direct<WARPS><<<blocks, WARPS * 32, 0, st>>>(params, d, Jsum, n, x, v, l, out);
+  k_query_direct<WARPS><<<blocks, WARPS * 32, 0, st>>>(params, d, Jsum, n, x, v, l, out, mask);
 }
 
 }  // namespace sfsim

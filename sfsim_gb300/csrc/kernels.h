@@ -99,7 +99,21 @@ void launch_query_table(const QueryTables& q, int kind, long long n, const float
 // Rendered in-scatter S + M phase(mie, v.l) at (x, v, l) by quadrature with
 // the order-summed point-scatter table Jsum (NULL: first order only).
 void launch_query_direct(const AtmoParams* params, const BuildDims& d, const Vec4<float>* Jsum, long long n,
-                         const double* x, const double* v, const double* l, float* out, cudaStream_t st);
+                         const double* x, const double* v, const double* l, float* out, cudaStream_t st,
+                         const unsigned char* mask = nullptr);
+
+// Table coordinates in [0, 1] (height, elevation, sun elevation, heading) of
+// (x, v, l) as the in-scatter lookup forms them; the lookup's value too when
+// `table` is non-NULL.
+void launch_query_coords(const QueryTables& q, long long n, const double* x, const double* v, const double* l,
+                         float* coords, float* table, cudaStream_t st);
+void launch_random_queries(long long n, unsigned long long seed, double R, double H, double* x, double* v, double* l,
+                           cudaStream_t st);
+void launch_node_pool(const BuildDims& d, const float* S, const float* M, const CellGeom<float>* geom, float mie_g,
+                      float eps, float* pool, cudaStream_t st);
+void launch_make_pool(long long n, const float* coords, const float* values, float eps, float* pool, cudaStream_t st);
+void launch_surrogate_finish(long long n, const float* y, float eps, const float* table, float thr, float floor_abs,
+                             float* out, unsigned char* mask, unsigned long long* count, cudaStream_t st);
 
 // jsum = (first ? 0 : jsum) + J, converted to float.
 template <class Real>

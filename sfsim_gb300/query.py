@@ -86,6 +86,56 @@ class Context:
                                                   out.data_ptr(), weight_bits, st), "query_table")
         return out
 
+    # -- surrogate -------------------------------------------------------------
+    def train_surrogate(self, steps=2000, batch=65536, direct_samples=1 << 20, node_fraction=0.75, lr=1e-3,
+                        seed=1):
+        """Trains the surrogate MLP on the GPU; returns the per-step losses (numpy)."""
+        import numpy as np
+        c = _lib.SurrogateConfig(steps, batch, direct_samples, node_fraction, lr, seed)
+        hist = np.zeros(max(steps, 1), np.float32)
+        _lib.check(self._L.sfsim_atmo_surrogate_train(self._ptr, ctypes.byref(c), hist.ctypes.data), "train")
+        return hist[:steps]
+
+    def surrogate_parameters(self, set_to=None):
+        import numpy as np
+        n = ctypes.c_longlong()
+        _lib.check(self._L.sfsim_atmo_surrogate_parameters(self._ptr, None, None, ctypes.byref(n)), "parameters")
+        out = np.zeros(n.value, np.float32)
+        src = None
+        if set_to is not None:
+            src = np.ascontiguousarray(set_to, dtype=np.float32)
+            assert src.size == n.value
+        _lib.check(self._L.sfsim_atmo_surrogate_parameters(self._ptr, out.ctypes.data,
+                                                           src.ctypes.data if src is not None else None,
+                                                           ctypes.byref(n)), "parameters")
+        return out
+
+    def surrogate_gradients(self, coords, targets):
+        """Loss and parameter gradients of one batch (numpy in, numpy out)."""
+        import numpy as np
+        coords = np.ascontiguousarray(coords, dtype=np.float32)
+        targets = np.ascontiguousarray(targets, dtype=np.float32)
+        n = coords.shape[0]
+        grads = np.zeros(self.surrogate_parameters().size, np.float32)
+        loss = np.zeros(1, np.float32)
+        _lib.check(self._L.sfsim_atmo_surrogate_gradients(self._ptr, n, coords.ctypes.data, targets.ctypes.data,
+                                                          loss.ctypes.data, grads.ctypes.data), "gradients")
+        return float(loss[0]), grads
+
+    def surrogate(self, x, v, l, threshold=0.0, out=None):
+        """Rendered in-scatter from the surrogate; returns (out, number of points recomputed directly)."""
+        import torch
+        x = x.contiguous().double()
+        v = v.contiguous().double()
+        l = l.contiguous().double()
+        n = x.shape[0]
+        out = out if out is not None else torch.empty((n, 3), dtype=torch.float32, device="cuda")
+        nf = ctypes.c_longlong()
+        st = torch.cuda.current_stream().cuda_stream
+        _lib.check(self._L.sfsim_atmo_query_surrogate(self._ptr, n, x.data_ptr(), v.data_ptr(), l.data_ptr(),
+                                                      out.data_ptr(), threshold, ctypes.byref(nf), st), "surrogate")
+        return out, nf.value
+
     def direct(self, x, v, l, out=None):
         import torch
         x = x.contiguous().double()

@@ -1,0 +1,79 @@
+"""float64 numpy reference of the surrogate MLP (test infrastructure): the
+same network as sfsim_gb300's kernels, with BF16 rounding applied at the
+same points (features, hidden activations and their gradients, the BF16
+weight copies), so that its gradients check the GPU's forward and backward
+GEMMs."""
+import numpy as np
+
+N_IN, N_HID = 128, 256
+SHAPES = [(N_HID, N_IN), (N_HID, N_HID), (N_HID, N_HID), (N_HID, N_HID), (3, N_HID)]
+
+
+def bf16(x):
+    """Round to bfloat16 (nearest even) and return as float64."""
+    a = np.asarray(x, dtype=np.float32)
+    u = a.view(np.uint32).astype(np.uint64)
+    r = ((u + 0x7FFF + ((u >> 16) & 1)) >> 16) << 16
+    return r.astype(np.uint32).view(np.float32).astype(np.float64)
+
+
+def unpack(params):
+    out, o = [], 0
+    for (r, c) in SHAPES:
+        W = params[o:o + r * c].reshape(r, c).astype(np.float64)
+        o += r * c
+        b = params[o:o + r].astype(np.float64)
+        o += r
+        out.append((W, b))
+    return out
+
+
+def features(coords):
+    k = np.arange(16)
+    f = 2.0 ** (0.5 * k)
+    ang = np.pi * coords[:, :, None].astype(np.float64) * f[None, None, :]  # [n, 4, 16]
+    F = np.stack([np.sin(ang), np.cos(ang)], axis=-1).reshape(coords.shape[0], N_IN)
+    return F
+
+
+def silu(z):
+    return z / (1 + np.exp(-z))
+
+
+def dsilu(z):
+    s = 1 / (1 + np.exp(-z))
+    return s * (1 + z * (1 - s))
+
+
+def loss_and_grads(params, coords, targets):
+    layers = unpack(params)
+    n = coords.shape[0]
+    H = [bf16(features(coords))]
+    Z = []
+    for l in range(4):
+        W, b = layers[l]
+        z = H[-1] @ bf16(W).T + b
+        Z.append(z)
+        H.append(bf16(silu(z)))
+    W5, b5 = layers[4]
+    out = H[4] @ W5.T + b5
+    e = out - targets
+    loss = np.mean(e * e)
+    dout = 2 * e / (3 * n)
+    grads = []
+    dW5 = dout.T @ H[4]
+    db5 = dout.sum(axis=0)
+    dZ = bf16((dout @ W5) * dsilu(Z[3]))
+    g = [None] * 5
+    g[4] = (dW5, db5)
+    for l in range(3, -1, -1):
+        W, b = layers[l]
+        dW = dZ.T @ H[l]
+        db = dZ.sum(axis=0)
+        g[l] = (dW, db)
+        if l > 0:
+            dZ = bf16((dZ @ bf16(W)) * dsilu(Z[l - 1]))
+    for (dW, db) in g:
+        grads.append(dW.ravel())
+        grads.append(db.ravel())
+    return loss, np.concatenate(grads)

@@ -1,0 +1,78 @@
+"""The ray-scatter surrogate: gradients of the GPU's tensor-core forward and
+backward passes against a float64 reference, training on the GPU, and what
+the trained network gains over the lookup table and over direct quadrature."""
+import numpy as np
+import pytest
+
+from sfsim_gb300 import config as C
+from sfsim_gb300.query import Context
+from tests.mlp_reference import loss_and_grads
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    c = Context(C.small_fp64(precision=C.FP32))
+    yield c
+    c.close()
+
+
+def test_gradients_match_reference(ctx):
+    rng = np.random.default_rng(3)
+    n = 2048
+    coords = rng.uniform(0, 1, (n, 4)).astype(np.float32)
+    targets = rng.normal(-8, 2, (n, 3)).astype(np.float32)
+    params = ctx.surrogate_parameters()
+    loss, grads = ctx.surrogate_gradients(coords, targets)
+    rloss, rgrads = loss_and_grads(params, coords, targets)
+    assert abs(loss - rloss) <= 1e-3 * abs(rloss)
+    # per tensor: relative norm of the difference
+    from tests.mlp_reference import SHAPES
+    o = 0
+    for (r, c) in SHAPES:
+        for size in (r * c, r):
+            g, rg = grads[o:o + size], rgrads[o:o + size]
+            o += size
+            rel = np.linalg.norm(g - rg) / max(np.linalg.norm(rg), 1e-30)
+            assert rel < 2e-2, (r, c, size, rel)
+    assert o == grads.size
+
+
+def random_queries(cfg, n, seed):
+    rng = np.random.default_rng(seed)
+    h = rng.uniform(0.0, cfg.height, n)
+
+    def unit(k):
+        v = rng.normal(size=(k, 3))
+        return v / np.linalg.norm(v, axis=1, keepdims=True)
+    return unit(n) * (cfg.radius + h)[:, None], unit(n), unit(n)
+
+
+def test_training_reduces_loss_and_surrogate_gains(ctx):
+    import torch
+    hist = ctx.train_surrogate(steps=600, batch=16384, direct_samples=1 << 16, lr=2e-3, seed=5)
+    assert np.isfinite(hist).all()
+    assert hist[-50:].mean() < 0.05 * hist[:10].mean(), (hist[:10].mean(), hist[-50:].mean())
+    cfg = ctx.cfg
+    x, v, l = random_queries(cfg, 4096, 11)
+    xt, vt, lt = (torch.tensor(z, dtype=torch.float64, device="cuda") for z in (x, v, l))
+    direct = ctx.direct(xt, vt, lt).cpu().numpy()
+    x32, v32, l32 = (torch.tensor(z, dtype=torch.float32, device="cuda") for z in (x, v, l))
+    table = ctx.table(4, x32, v32, l32).cpu().numpy()
+    sur, nf0 = ctx.surrogate(xt, vt, lt)
+    sur = sur.cpu().numpy()
+    assert nf0 == 0
+    floor = 1e-6 * np.abs(direct).max()
+
+    def err(a):
+        return np.abs(a - direct) / np.maximum(np.abs(direct), floor)
+    e_table, e_sur = err(table), err(sur)
+    # the network reproduces the table's interpolant to within its own error
+    assert np.median(e_sur) < 0.1, np.median(e_sur)
+    # with fallback at threshold t every point is within the table's error plus t
+    t = 0.02
+    fb, nf = ctx.surrogate(xt, vt, lt, threshold=t)
+    e_fb = err(fb.cpu().numpy())
+    assert 0 <= nf < 4096
+    assert np.percentile(e_fb, 99) <= np.percentile(e_table, 99) + t + 1e-3
