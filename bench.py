@@ -49,6 +49,8 @@ def parse():
                    help="only run --builds builds of a named configuration (small_fp64, production, "
                         "reference_production, shader_test), for profilers")
     p.add_argument("--builds", type=int, default=2)
+    p.add_argument("--no-extras", dest="extras", action="store_false",
+                   help="skip the parameter-sweep and query/surrogate measurements")
     return p.parse_args()
 
 
@@ -233,6 +235,9 @@ def run_ours(args):
     achieved = 2.0 * ext_samples / (fo_ms * 1e-3) / 1e9  # two exponentials per extinction sample
     peak_g = peak.value / 1e9
 
+    sweep = run_sweep(L, A, C) if args.extras else None
+    queries = run_queries(C) if args.extras else None
+
     if world > 1:
         dist.barrier()
     result = None
@@ -258,12 +263,113 @@ def run_ours(args):
                          "ext_samples": ext_samples, "kernel_ms": fo_ms},
             "clocks": clk,
             "cpu_baseline": cpu,
+            "sweep": sweep,
+            "queries": queries,
         }
         print(json.dumps(result), flush=True)
     if world > 1:
         dist.barrier()
         dist.destroy_process_group()
     return result
+
+
+# ---------------------------------------------------------------------------
+# secondary measurements: parameter sweep, queries and the surrogate
+# ---------------------------------------------------------------------------
+
+def run_sweep(L, A, C):
+    """64 atmospheres drawn from the sweep distribution, shapes 16x128x16x8, 4
+    iterations, built in one batched pass; device time from the stage events."""
+    import time as _t
+    cfgs = C.parameter_sweep(64)
+    read = A.stage_timings(True)
+    A.build_batch(cfgs[:2])  # warm-up
+    t0 = _t.perf_counter()
+    A.build_batch(cfgs)
+    wall = _t.perf_counter() - t0
+    dev_ms = sum(read().values())
+    A.stage_timings(False)
+    n4 = 1
+    for v in cfgs[0].ray_scatter_shape:
+        n4 *= v
+    return {"atmospheres": len(cfgs), "shape": list(cfgs[0].ray_scatter_shape), "iterations": cfgs[0].iterations,
+            "device_s": dev_ms * 1e-3, "e2e_s": wall, "cells_per_s": len(cfgs) * n4 / (dev_ms * 1e-3)}
+
+
+def _random_queries(n, R, H, seed):
+    import torch
+    g = torch.Generator(device="cuda").manual_seed(seed)
+    h = torch.rand(n, device="cuda", dtype=torch.float64, generator=g) * H
+
+    def unit():
+        v = torch.randn(n, 3, device="cuda", dtype=torch.float64, generator=g)
+        return v / v.norm(dim=1, keepdim=True)
+    return unit() * (R + h)[:, None], unit(), unit()
+
+
+def _timed(fn, reps=3):
+    import torch
+    fn()
+    torch.cuda.synchronize()
+    s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    best = None
+    for _ in range(reps):
+        s.record()
+        r = fn()
+        e.record()
+        torch.cuda.synchronize()
+        ms = s.elapsed_time(e)
+        best = ms if best is None else min(best, ms)
+    return best, r
+
+
+def run_queries(C):
+    """2^24 random in-scatter queries (height uniform 0-100 km, view and sun
+    uniform on the sphere) on the production tables: table lookup, direct
+    quadrature, the trained surrogate and the surrogate with fallback; errors
+    relative to direct quadrature (floor 1e-6 of the largest value)."""
+    import time as _t
+
+    import torch
+
+    from sfsim_gb300.query import Context
+    cfg = C.production()
+    ctx = Context(cfg)
+    t0 = _t.perf_counter()
+    steps, batch = 3000, 65536
+    hist = ctx.train_surrogate(steps=steps, batch=batch, direct_samples=1 << 23, node_fraction=0.75, lr=1e-3, seed=1)
+    torch.cuda.synchronize()
+    train_s = _t.perf_counter() - t0
+    n = 1 << 24
+    x, v, l = _random_queries(n, cfg.radius, cfg.height, 2)
+    x32, v32, l32 = x.float(), v.float(), l.float()
+    out = torch.empty((n, 3), dtype=torch.float32, device="cuda")
+    t_table, table = _timed(lambda: ctx.table(4, x32, v32, l32, out=out).clone())
+    t_direct, direct = _timed(lambda: ctx.direct(x, v, l, out=out).clone(), reps=1)
+    t_sur, (sur, _) = _timed(lambda: ctx.surrogate(x, v, l, out=out))
+    sur = sur.clone()
+    res = {}
+    for thr in (1e-2, 1e-3):
+        t_fb, (fb, nf) = _timed(lambda: ctx.surrogate(x, v, l, threshold=thr, out=out), reps=1)
+        res[thr] = (t_fb, fb.clone(), nf)
+    floor = 1e-6 * direct.abs().max()
+
+    def stats(a):
+        e = ((a - direct).abs() / torch.maximum(direct.abs(), floor)).max(dim=1).values
+        q = torch.quantile(e[: 1 << 20], torch.tensor([0.5, 0.99], device="cuda", dtype=e.dtype))
+        return {"median": float(q[0]), "p99": float(q[1]), "max": float(e.max()),
+                "frac_le_1e-3": float((e <= 1e-3).double().mean())}
+    qps = lambda ms: n / (ms * 1e-3)  # noqa: E731
+    r = {"n": n, "train_steps": steps, "train_batch": batch, "train_s": train_s,
+         "train_loss_first": float(hist[:10].mean()), "train_loss_last": float(hist[-100:].mean()),
+         "table": {"qps": qps(t_table), "err": stats(table)},
+         "direct": {"qps": qps(t_direct)},
+         "surrogate": {"qps": qps(t_sur), "err": stats(sur), "vs_direct": t_direct / t_sur}}
+    for thr, (t_fb, fb, nf) in res.items():
+        r[f"surrogate_fallback_{thr:g}"] = {"qps": qps(t_fb), "fallback_fraction": nf / n, "err": stats(fb),
+                                            "vs_direct": t_direct / t_fb}
+    ctx.close()
+    return r
 
 
 # ---------------------------------------------------------------------------

@@ -202,6 +202,12 @@ int sfsim_atmo_query_table(const sfsim_atmo_context* ctx, int kind, long long n,
 int sfsim_atmo_query_direct(const sfsim_atmo_context* ctx, long long n, const double* x,
                             const double* v, const double* l, float* out, void* stream);
 
+/* Table coordinates in [0, 1] of (x, v, l): height, elevation, sun elevation
+ * and sun heading as core/ray-scatter-forward.glsl forms them (FP32), with
+ * the table half chosen by is_above_horizon; coords is a DEVICE [n][4]. */
+int sfsim_atmo_query_coords(const sfsim_atmo_context* ctx, long long n, const double* x, const double* v,
+                            const double* l, float* coords, void* stream);
+
 /* ---- Surrogate of the rendered in-scatter ----------------------------------
  * An MLP over the four table coordinates in [0, 1] (height, elevation, sun
  * elevation, sun heading, as the in-scatter lookup forms them): 16-frequency
@@ -235,7 +241,9 @@ int sfsim_atmo_surrogate_gradients(sfsim_atmo_context* ctx, long long n, const f
                                    const float* targets, float* loss, float* grads);
 
 /* Rendered in-scatter at (x, v, l) from the surrogate (DEVICE arrays as in
- * sfsim_atmo_query_direct).  With threshold > 0, points where the surrogate
+ * sfsim_atmo_query_direct), one fused tensor-core kernel: coordinates,
+ * features, the four hidden layers (tcgen05 MMA into tensor memory) and the
+ * head per 128 queries.  With threshold > 0, points where the surrogate
  * and the table lookup differ by more than `threshold` (relative, floor 1e-7)
  * are recomputed by direct quadrature; *n_fallback receives their number. */
 int sfsim_atmo_query_surrogate(sfsim_atmo_context* ctx, long long n, const double* x, const double* v,

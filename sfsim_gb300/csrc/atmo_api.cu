@@ -1489,6 +1489,16 @@ int sfsim_atmo_surrogate_gradients(sfsim_atmo_context* ctx, long long n, const f
   return check_error_flag(S, st);
 }
 
+int sfsim_atmo_query_coords(const sfsim_atmo_context* ctx, long long n, const double* x, const double* v,
+                            const double* l, float* coords, void* stream) {
+  if (!ctx || !x || !v || !l || !coords) return fail(SFSIM_ATMO_ENULL, "NULL argument");
+  if (n < 0) return fail(SFSIM_ATMO_EINVAL, "n must be non-negative");
+  if (n == 0) return 0;
+  launch_query_coords(context_tables(ctx), n, x, v, l, coords, nullptr, (cudaStream_t)stream);
+  CUDA_TRY(cudaGetLastError());
+  return 0;
+}
+
 int sfsim_atmo_query_surrogate(sfsim_atmo_context* ctx, long long n, const double* x, const double* v,
                                const double* l, float* out, float threshold, long long* n_fallback, void* stream) {
   if (!ctx || !x || !v || !l || !out) return fail(SFSIM_ATMO_ENULL, "NULL argument");
@@ -1497,9 +1507,6 @@ int sfsim_atmo_query_surrogate(sfsim_atmo_context* ctx, long long n, const doubl
   if (n_fallback) *n_fallback = 0;
   if (n == 0) return 0;
   std::lock_guard<std::mutex> lock(g_mutex);
-  const long long chunk = 1 << 18;
-  int rc = surrogate_alloc(ctx, chunk, 1);
-  if (rc) return rc;
   Surrogate& S = *ctx->sur;
   cudaStream_t st = (cudaStream_t)stream;
   const QueryTables q = context_tables(ctx);
@@ -1513,18 +1520,13 @@ int sfsim_atmo_query_surrogate(sfsim_atmo_context* ctx, long long n, const doubl
     }
     CUDA_TRY(cudaMemsetAsync(count, 0, sizeof(unsigned long long), st));
   }
-  // S.dout holds the table values of a chunk when falling back
-  for (long long o = 0; o < n && !rc; o += chunk) {
-    const long long m = std::min(chunk, n - o);
-    const long long mp = (m + 127) / 128 * 128;
-    launch_query_coords(q, m, x + 3 * o, v + 3 * o, l + 3 * o, S.coords, fallback ? S.dout : nullptr, st);
-    if (mp > m) CUDA_TRY(cudaMemsetAsync(S.coords + 4 * m, 0, sizeof(float) * 4 * (mp - m), st));
-    if ((rc = surrogate_forward(S, mp, false, st))) break;
-    launch_surrogate_finish(m, S.out, kLogEps, fallback ? S.dout : nullptr, threshold, 1e-7f, out + 3 * o,
-                            fallback ? mask + o : nullptr, count, st);
-  }
-  if (!rc && fallback)
-    launch_query_direct(ctx->params, ctx->dims, ctx->jsum, n, x, v, l, out, st, mask);
+  const float* biases[4];
+  for (int i = 0; i < 4; i++) biases[i] = S.w + S.lay.b[i];
+  int rc = 0;
+  if (launch_surrogate_infer(q, n, x, v, l, S.wb, biases, S.w + S.lay.W[4], S.w + S.lay.b[4], kLogEps,
+                             fallback ? threshold : 0.0f, 1e-7f, out, mask, count, S.error, st))
+    rc = fail(SFSIM_ATMO_ECUDA, "surrogate inference launch configuration failed");
+  if (!rc && fallback) launch_query_direct(ctx->params, ctx->dims, ctx->jsum, n, x, v, l, out, st, mask);
   if (!rc && cudaGetLastError() != cudaSuccess) rc = fail(SFSIM_ATMO_ECUDA, "surrogate query launch failed");
   if (fallback) {
     unsigned long long h = 0;

@@ -7,8 +7,11 @@
 //  * the rendered in-scatter S + M phase(mie, v.l) at (x, v, l) by direct
 //    quadrature: the first order integrated at the point (atmosphere.clj:
 //    154-200) plus ray scatter of the summed point-scatter tables.
+#include <cuda_bf16.h>
+
 #include "atmo_device.cuh"
 #include "kernels.h"
+#include "tc.cuh"
 
 namespace sfsim {
 
@@ -547,6 +550,198 @@ void launch_query_direct(const AtmoParams* params, const BuildDims& d, const Vec
   constexpr int WARPS = 8;
   const unsigned blocks = (unsigned)((n + WARPS - 1) / WARPS);
   k_query_direct<WARPS><<<blocks, WARPS * 32, 0, st>>>(params, d, Jsum, n, x, v, l, out, mask);
+}
+
+// ---------------------------------------------------------------------------
+// Fused surrogate inference on the tensor cores.  One CTA of 128 threads
+// evaluates 128 queries: coordinates and features (thread = query) into a
+// K-major BF16 tile in shared memory, then for each hidden layer the weights
+// stream through shared memory in K chunks of 64 and one thread issues the
+// tcgen05.mma that accumulate the 128 x 256 layer in tensor memory.  Each
+// layer's epilogue (bias, SiLU, BF16) writes the next layer's input back into
+// the same tile; the last one folds the 256 -> 3 head in.  Outputs are
+// exp(y) - 1e-8 and, when a threshold is given, the flag of queries whose
+// surrogate and table values disagree.  Every wait is bounded.
+// ---------------------------------------------------------------------------
+
+struct InferArgs {
+  GlslEnv env;
+  long long n;
+  const double *X, *V, *L;
+  const __nv_bfloat16* W[4];  // [out][in]
+  const float* b[4];
+  const float* W5;            // [3][256]
+  const float* b5;
+  float* out;
+  float threshold, floor_abs, eps;
+  unsigned char* mask;
+  unsigned long long* count;
+  int* error;
+};
+
+constexpr int kInferSmemA = 128 * 256 * 2;  // activations: 128 rows x 256 K, row groups 4096 B apart
+constexpr int kInferSmemW = 256 * 64 * 2;   // one K chunk of a weight matrix, row groups 1024 B apart
+
+__global__ void __launch_bounds__(128) k_surrogate_infer(InferArgs g) {
+  extern __shared__ __align__(1024) unsigned char smem[];
+  __shared__ uint64_t mbar;
+  __shared__ uint32_t tmem_slot;
+  unsigned char* A = smem;
+  unsigned char* Wt = smem + kInferSmemA;
+  const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
+  const long long q = (long long)blockIdx.x * 128 + t;
+  const bool valid = q < g.n;
+  const long long qq = valid ? q : g.n - 1;
+
+  if (warp == 0) tc::tmem_alloc(&tmem_slot, 256);
+  if (t == 0) tc::mbar_init(&mbar, 1);
+
+  // coordinates, table value and features of this thread's query
+  const f3 p = F3((float)g.X[3 * qq], (float)g.X[3 * qq + 1], (float)g.X[3 * qq + 2]);
+  const f3 d = F3((float)g.V[3 * qq], (float)g.V[3 * qq + 1], (float)g.V[3 * qq + 2]);
+  const f3 l = F3((float)g.L[3 * qq], (float)g.L[3 * qq + 1], (float)g.L[3 * qq + 2]);
+  float idx[4];
+  ray_scatter_forward_g(g.env, p, d, l, is_above_horizon_g(g.env, p, d), idx);
+  f3 table = F3(0, 0, 0);
+  if (g.threshold > 0) table = in_scatter_g(g.env, idx, fdot(d, l));
+  const float u[4] = {idx[3], idx[2], idx[1], idx[0]};
+#pragma unroll
+  for (int dd = 0; dd < 4; dd++) {
+#pragma unroll
+    for (int kc = 0; kc < 2; kc++) {  // 8 frequencies = 16 features = two 16-byte chunks
+      __nv_bfloat16 v8[8];
+#pragma unroll
+      for (int j = 0; j < 4; j++) {
+        float sn, cs;
+        sincospif(exp2f(0.5f * (float)(kc * 4 + j)) * u[dd], &sn, &cs);
+        v8[2 * j] = __float2bfloat16(sn);
+        v8[2 * j + 1] = __float2bfloat16(cs);
+      }
+      const int k = dd * 32 + kc * 8;
+      *reinterpret_cast<uint4*>(A + tc::tile_offset(t, k, 256)) = *reinterpret_cast<const uint4*>(v8);
+      // the second half of the 16 frequencies of this coordinate
+      __nv_bfloat16 w8[8];
+#pragma unroll
+      for (int j = 0; j < 4; j++) {
+        float sn, cs;
+        sincospif(exp2f(0.5f * (float)(8 + kc * 4 + j)) * u[dd], &sn, &cs);
+        w8[2 * j] = __float2bfloat16(sn);
+        w8[2 * j + 1] = __float2bfloat16(cs);
+      }
+      *reinterpret_cast<uint4*>(A + tc::tile_offset(t, k + 16, 256)) = *reinterpret_cast<const uint4*>(w8);
+    }
+  }
+  tc::fence_before();
+  __syncthreads();
+  tc::fence_after();
+  const uint32_t tmem = tmem_slot;
+  const uint32_t idesc = tc::idesc_bf16(128, 256);
+  uint32_t parity = 0;
+  bool ok = true;
+  float head[3] = {0, 0, 0};
+  for (int layer = 0; layer < 4 && ok; layer++) {
+    const int K = layer == 0 ? kMlpIn : kMlpHidden;
+    const __nv_bfloat16* W = g.W[layer];
+    for (int kc = 0; kc < K / 64 && ok; kc++) {
+      // weight chunk: 256 rows x 64 K
+      for (int c = t; c < 256 * 8; c += 128) {
+        const int row = c >> 3, ch = c & 7;
+        const uint4 v = *reinterpret_cast<const uint4*>(W + (long long)row * K + kc * 64 + ch * 8);
+        *reinterpret_cast<uint4*>(Wt + tc::tile_offset(row, ch * 8)) = v;
+      }
+      tc::fence_async_smem();
+      __syncthreads();
+      if (t == 0) {
+        tc::fence_after();
+        const uint32_t a0 = tc::smem_u32(A), w0 = tc::smem_u32(Wt);
+#pragma unroll
+        for (int ks = 0; ks < 4; ks++) {
+          const uint64_t da = tc::smem_desc(a0 + kc * 1024 + ks * 256, 128, 4096);
+          const uint64_t db = tc::smem_desc(w0 + ks * 256, 128, 1024);
+          tc::mma(tmem, da, db, idesc, (kc > 0 || ks > 0) ? 1u : 0u);
+        }
+        tc::commit(&mbar);
+      }
+      bool done = tc::mbar_wait(&mbar, parity, 1 << 22);
+      if (!done) done = tc::mbar_wait(&mbar, parity, 1 << 22);
+      parity ^= 1;
+      tc::fence_after();
+      ok = __syncthreads_and(done) != 0;
+    }
+    if (!ok) break;
+    // epilogue: row t of the accumulator (warp w owns rows 32w..32w+31)
+    const float* bias = g.b[layer];
+    for (int n0 = 0; n0 < 256; n0 += 8) {
+      float v[8];
+      tc::tmem_ld8(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)n0, v);
+      __nv_bfloat16 h8[8];
+#pragma unroll
+      for (int i = 0; i < 8; i++) {
+        const float z = v[i] + bias[n0 + i];
+        const float h = __bfloat162float(__float2bfloat16(z / (1.0f + __expf(-z))));
+        h8[i] = __float2bfloat16(h);
+        if (layer == 3) {
+#pragma unroll
+          for (int c = 0; c < 3; c++) head[c] = fmaf(h, g.W5[c * 256 + n0 + i], head[c]);
+        }
+      }
+      if (layer < 3) *reinterpret_cast<uint4*>(A + tc::tile_offset(t, n0, 256)) = *reinterpret_cast<const uint4*>(h8);
+    }
+    tc::fence_before();
+    __syncthreads();
+    tc::fence_after();
+  }
+  (void)lane;
+  bool flag = false;
+  if (ok && valid) {
+    const float tv[3] = {table.x, table.y, table.z};
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+      const float y = head[c] + g.b5[c];
+      const float val = fmaxf(expf(y) - g.eps, 0.0f);
+      g.out[3 * q + c] = val;
+      if (g.threshold > 0 && fabsf(val - tv[c]) > g.threshold * fmaxf(fabsf(tv[c]), g.floor_abs)) flag = true;
+    }
+    if (g.mask) g.mask[q] = flag ? 1 : 0;
+  }
+  if (!ok && t == 0 && g.error) atomicExch(g.error, 1);
+  if (g.count) {
+    const unsigned bal = __ballot_sync(0xffffffffu, flag);
+    if (lane == 0 && bal) atomicAdd(g.count, (unsigned long long)__popc(bal));
+  }
+  tc::fence_before();
+  __syncthreads();
+  if (warp == 0) tc::tmem_dealloc(tmem, 256);
+}
+
+int launch_surrogate_infer(const QueryTables& qt, long long n, const double* x, const double* v, const double* l,
+                           const __nv_bfloat16* const* W, const float* const* b, const float* W5, const float* b5,
+                           float eps, float threshold, float floor_abs, float* out, unsigned char* mask,
+                           unsigned long long* count, int* error, cudaStream_t st) {
+  InferArgs g;
+  g.env = make_env(qt, 0);
+  g.n = n;
+  g.X = x;
+  g.V = v;
+  g.L = l;
+  for (int i = 0; i < 4; i++) {
+    g.W[i] = W[i];
+    g.b[i] = b[i];
+  }
+  g.W5 = W5;
+  g.b5 = b5;
+  g.out = out;
+  g.threshold = threshold;
+  g.floor_abs = floor_abs;
+  g.eps = eps;
+  g.mask = mask;
+  g.count = count;
+  g.error = error;
+  const int smem = kInferSmemA + kInferSmemW;
+  if (cudaFuncSetAttribute(k_surrogate_infer, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess)
+    return -1;
+  k_surrogate_infer<<<(unsigned)((n + 127) / 128), 128, smem, st>>>(g);
+  return 0;
 }
 
 }  // namespace sfsim

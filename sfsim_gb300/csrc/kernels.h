@@ -112,6 +112,11 @@ void launch_random_queries(long long n, unsigned long long seed, double R, doubl
 void launch_node_pool(const BuildDims& d, const float* S, const float* M, const CellGeom<float>* geom, float mie_g,
                       float eps, float* pool, cudaStream_t st);
 void launch_make_pool(long long n, const float* coords, const float* values, float eps, float* pool, cudaStream_t st);
+// Fused tensor-core inference of the surrogate for n queries; see k_query.cu.
+int launch_surrogate_infer(const QueryTables& qt, long long n, const double* x, const double* v, const double* l,
+                           const __nv_bfloat16* const* W, const float* const* b, const float* W5, const float* b5,
+                           float eps, float threshold, float floor_abs, float* out, unsigned char* mask,
+                           unsigned long long* count, int* error, cudaStream_t st);
 void launch_surrogate_finish(long long n, const float* y, float eps, const float* table, float thr, float floor_abs,
                              float* out, unsigned char* mask, unsigned long long* count, cudaStream_t st);
 

@@ -136,6 +136,18 @@ class Context:
                                                       out.data_ptr(), threshold, ctypes.byref(nf), st), "surrogate")
         return out, nf.value
 
+    def coords(self, x, v, l):
+        """Table coordinates [n, 4] in [0, 1] of the queries (height, elevation, sun elevation, heading)."""
+        import torch
+        x = x.contiguous().double()
+        v = v.contiguous().double()
+        l = l.contiguous().double()
+        out = torch.empty((x.shape[0], 4), dtype=torch.float32, device="cuda")
+        _lib.check(self._L.sfsim_atmo_query_coords(self._ptr, x.shape[0], x.data_ptr(), v.data_ptr(), l.data_ptr(),
+                                                   out.data_ptr(), torch.cuda.current_stream().cuda_stream),
+                   "query_coords")
+        return out
+
     def direct(self, x, v, l, out=None):
         import torch
         x = x.contiguous().double()

@@ -77,3 +77,14 @@ def loss_and_grads(params, coords, targets):
         grads.append(dW.ravel())
         grads.append(db.ravel())
     return loss, np.concatenate(grads)
+
+
+def forward(params, coords):
+    """Network output (log-RGB) for coords [n][4], with the GPU's BF16 roundings."""
+    layers = unpack(params)
+    H = bf16(features(coords))
+    for l in range(4):
+        W, b = layers[l]
+        H = bf16(silu(H @ bf16(W).T + b))
+    W5, b5 = layers[4]
+    return H @ W5.T + b5

@@ -6,7 +6,7 @@ import pytest
 
 from sfsim_gb300 import config as C
 from sfsim_gb300.query import Context
-from tests.mlp_reference import loss_and_grads
+from tests.mlp_reference import forward, loss_and_grads
 
 pytestmark = pytest.mark.gpu
 
@@ -76,3 +76,21 @@ def test_training_reduces_loss_and_surrogate_gains(ctx):
     e_fb = err(fb.cpu().numpy())
     assert 0 <= nf < 4096
     assert np.percentile(e_fb, 99) <= np.percentile(e_table, 99) + t + 1e-3
+
+
+def test_fused_inference_matches_reference(ctx):
+    """The fused tensor-core inference kernel against the float64 forward pass
+    at the coordinates the GPU forms for the same queries."""
+    import torch
+    params = ctx.surrogate_parameters()  # also creates an untrained surrogate when run alone
+    cfg = ctx.cfg
+    x, v, l = random_queries(cfg, 1000, 21)
+    xt, vt, lt = (torch.tensor(z, dtype=torch.float64, device="cuda") for z in (x, v, l))
+    coords = ctx.coords(xt, vt, lt).cpu().numpy()
+    assert np.all((coords >= 0) & (coords <= 1))
+    out, nf = ctx.surrogate(xt, vt, lt)
+    y = np.log(out.cpu().numpy().astype(np.float64) + 1e-8)
+    ref = forward(params, coords)
+    ref_val = np.maximum(np.exp(ref) - 1e-8, 0)
+    mask = ref_val > 1e-6  # compare in log space where the value is well above the 1e-8 offset
+    assert np.abs(y - ref)[mask].max() < 2e-2, float(np.abs(y - ref)[mask].max())
