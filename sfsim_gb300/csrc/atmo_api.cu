@@ -930,6 +930,7 @@ struct Surrogate {
   float *coords = nullptr, *target = nullptr, *out = nullptr, *dout = nullptr, *loss = nullptr;
   __nv_bfloat16 *F = nullptr, *FT = nullptr, *H[4] = {}, *HT[4] = {}, *dZ[4] = {}, *dZT[4] = {};
   float* dsilu[4] = {};
+  unsigned char* packed = nullptr;  // weight chunks of the fused inference kernel
   int* error = nullptr;
   int trained_steps = 0;
   std::vector<void*> allocs;
@@ -991,7 +992,8 @@ int surrogate_alloc(sfsim_atmo_context* c, long long batch, unsigned long long s
       S.wb[l] = S.alloc_h((size_t)S.lay.in[l] * S.lay.out[l]);
       S.wbt[l] = S.alloc_h((size_t)S.lay.in[l] * S.lay.out[l]);
     }
-    if (!S.w || !S.g || !S.m || !S.v || !S.loss || !S.wb[3] || !S.wbt[3])
+    S.packed = reinterpret_cast<unsigned char*>(S.alloc_h(infer_packed_bytes() / 2));
+    if (!S.w || !S.g || !S.m || !S.v || !S.loss || !S.wb[3] || !S.wbt[3] || !S.packed)
       return fail(SFSIM_ATMO_ENOMEM, "surrogate allocation failed");
     std::vector<float> h;
     init_weights(S.lay, seed, h);
@@ -1522,9 +1524,10 @@ int sfsim_atmo_query_surrogate(sfsim_atmo_context* ctx, long long n, const doubl
   }
   const float* biases[4];
   for (int i = 0; i < 4; i++) biases[i] = S.w + S.lay.b[i];
-  int rc = 0;
+  int rc = 0, sms = 0;
+  CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->dev));
   if (launch_surrogate_infer(q, n, x, v, l, S.wb, biases, S.w + S.lay.W[4], S.w + S.lay.b[4], kLogEps,
-                             fallback ? threshold : 0.0f, 1e-7f, out, mask, count, S.error, st))
+                             fallback ? threshold : 0.0f, 1e-7f, out, mask, count, S.error, S.packed, sms, st))
     rc = fail(SFSIM_ATMO_ECUDA, "surrogate inference launch configuration failed");
   if (!rc && fallback) launch_query_direct(ctx->params, ctx->dims, ctx->jsum, n, x, v, l, out, st, mask);
   if (!rc && cudaGetLastError() != cudaSuccess) rc = fail(SFSIM_ATMO_ECUDA, "surrogate query launch failed");

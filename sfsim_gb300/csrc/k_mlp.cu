@@ -11,9 +11,6 @@
 
 namespace sfsim {
 
-// Frequencies of the features: pi * 2^(k/2), k = 0..15.
-__device__ __forceinline__ float feature_frequency(int k) { return exp2f(0.5f * (float)k); }
-
 // F[i][32 d + 2 k] = sin(pi f_k u_d), F[i][32 d + 2 k + 1] = cos(pi f_k u_d);
 // also the transpose FT[128][n] when requested.
 __global__ void k_features(long long n, const float* __restrict__ coords, __nv_bfloat16* __restrict__ F,

@@ -553,24 +553,75 @@ void launch_query_direct(const AtmoParams* params, const BuildDims& d, const Vec
 }
 
 // ---------------------------------------------------------------------------
-// Fused surrogate inference on the tensor cores.  One CTA of 128 threads
-// evaluates 128 queries: coordinates and features (thread = query) into a
-// K-major BF16 tile in shared memory, then for each hidden layer the weights
-// stream through shared memory in K chunks of 64 and one thread issues the
-// tcgen05.mma that accumulate the 128 x 256 layer in tensor memory.  Each
-// layer's epilogue (bias, SiLU, BF16) writes the next layer's input back into
-// the same tile; the last one folds the 256 -> 3 head in.  Outputs are
-// exp(y) - 1e-8 and, when a threshold is given, the flag of queries whose
-// surrogate and table values disagree.  Every wait is bounded.
+// Fused surrogate inference on the tensor cores.
+//
+// A persistent CTA per SM evaluates groups of 256 queries (two 128-row tiles
+// A0, A1 of BF16 activations, K-major core-matrix layout, 64 KB each).  Warps
+// 0-7 own one query each per thread (warps 0-3 tile 0, 4-7 tile 1): they form
+// the coordinates and Fourier features, and after every layer read their row
+// of the FP32 accumulator from tensor memory (tcgen05.ld), add the bias, apply
+// SiLU and write the BF16 result back as the next layer's input; the last
+// layer folds the 256 -> 3 head in.  Warp 8 is the producer: one thread
+// streams the 28 weight chunks of a group (256 rows x 32 K, 16 KB each,
+// pre-packed in the tensor cores' layout) through a five-stage shared-memory
+// ring with bulk TMA copies, and issues the tcgen05.mma of both tiles on each
+// chunk (one weight fetch serves 256 queries) into two 128 x 256 FP32
+// accumulators in tensor memory (all 512 columns).  Stages are released by
+// tcgen05.commit, layers handed over by two mbarriers (accumulator complete,
+// activations written).  Every wait is bounded: on timeout the CTA records an
+// error, lets its copies and MMAs drain and returns.
 // ---------------------------------------------------------------------------
+
+constexpr int kInferKC = 32;                                          // K per weight chunk
+constexpr int kInferChunkBytes = kMlpHidden * kInferKC * 2;           // 16 KB
+constexpr int kInferChunks0 = kMlpIn / kInferKC;                      // layer 0
+constexpr int kInferChunksH = kMlpHidden / kInferKC;                  // hidden layers
+constexpr int kInferChunks = kInferChunks0 + 3 * kInferChunksH;       // 28 per group
+constexpr int kInferStages = 5;
+constexpr int kInferTileBytes = 128 * kMlpHidden * 2;                 // 64 KB
+constexpr int kInferThreads = 288;
+constexpr int kInferWaitLimit = 1 << 22;
+constexpr int kInferSmemRing = 2 * kInferTileBytes;
+constexpr int kInferSmemBias = kInferSmemRing + kInferStages * kInferChunkBytes;
+constexpr int kInferSmemHead = kInferSmemBias + 4 * kMlpHidden * 4;
+constexpr int kInferSmemBar = kInferSmemHead + 4 * kMlpHidden * 4;   // W5 (3 x 256) and b5
+constexpr int kInferSmem = kInferSmemBar + (2 * kInferStages + 2) * 8 + 16;
+
+size_t infer_packed_bytes() { return (size_t)kInferChunks * kInferChunkBytes; }
+
+// Packs the BF16 hidden-layer weights W_l [256][in] into the chunk sequence
+// the inference kernel streams: chunk c = (layer, 32-wide K slice), element
+// (n, k) at byte (n / 8) * 512 + (k % 32 / 8) * 128 + (n % 8) * 16 + (k % 8) * 2.
+// One thread moves 8 consecutive K of one row.
+__global__ void k_pack_infer(const __nv_bfloat16* W0, const __nv_bfloat16* W1, const __nv_bfloat16* W2,
+                             const __nv_bfloat16* W3, unsigned char* packed) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  constexpr int n0 = kMlpHidden * (kMlpIn / 8);
+  constexpr int nh = kMlpHidden * (kMlpHidden / 8);
+  if (t >= n0 + 3 * nh) return;
+  int layer, r, K, chunk0;
+  const __nv_bfloat16* W;
+  if (t < n0) {
+    layer = 0, r = t, K = kMlpIn, chunk0 = 0, W = W0;
+  } else {
+    layer = 1 + (t - n0) / nh, r = (t - n0) % nh, K = kMlpHidden;
+    chunk0 = kInferChunks0 + (layer - 1) * kInferChunksH;
+    W = layer == 1 ? W1 : layer == 2 ? W2 : W3;
+  }
+  const int n = r / (K / 8), k = (r % (K / 8)) * 8;
+  const uint4 v = *reinterpret_cast<const uint4*>(W + (long long)n * K + k);
+  unsigned char* dst = packed + (size_t)(chunk0 + k / kInferKC) * kInferChunkBytes + (n >> 3) * (kInferKC * 16) +
+                       ((k % kInferKC) >> 3) * 128 + (n & 7) * 16;
+  *reinterpret_cast<uint4*>(dst) = v;
+}
 
 struct InferArgs {
   GlslEnv env;
   long long n;
   const double *X, *V, *L;
-  const __nv_bfloat16* W[4];  // [out][in]
+  const unsigned char* packed;  // kInferChunks weight chunks
   const float* b[4];
-  const float* W5;            // [3][256]
+  const float* W5;              // [3][256]
   const float* b5;
   float* out;
   float threshold, floor_abs, eps;
@@ -579,155 +630,249 @@ struct InferArgs {
   int* error;
 };
 
-constexpr int kInferSmemA = 128 * 256 * 2;  // activations: 128 rows x 256 K, row groups 4096 B apart
-constexpr int kInferSmemW = 256 * 64 * 2;   // one K chunk of a weight matrix, row groups 1024 B apart
+__device__ __forceinline__ float tanh_approx(float x) {
+  float y;
+  asm("tanh.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
 
-__global__ void __launch_bounds__(128) k_surrogate_infer(InferArgs g) {
-  extern __shared__ __align__(1024) unsigned char smem[];
-  __shared__ uint64_t mbar;
-  __shared__ uint32_t tmem_slot;
-  unsigned char* A = smem;
-  unsigned char* Wt = smem + kInferSmemA;
-  const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
-  const long long q = (long long)blockIdx.x * 128 + t;
-  const bool valid = q < g.n;
-  const long long qq = valid ? q : g.n - 1;
-
-  if (warp == 0) tc::tmem_alloc(&tmem_slot, 256);
-  if (t == 0) tc::mbar_init(&mbar, 1);
-
-  // coordinates, table value and features of this thread's query
-  const f3 p = F3((float)g.X[3 * qq], (float)g.X[3 * qq + 1], (float)g.X[3 * qq + 2]);
-  const f3 d = F3((float)g.V[3 * qq], (float)g.V[3 * qq + 1], (float)g.V[3 * qq + 2]);
-  const f3 l = F3((float)g.L[3 * qq], (float)g.L[3 * qq + 1], (float)g.L[3 * qq + 2]);
-  float idx[4];
-  ray_scatter_forward_g(g.env, p, d, l, is_above_horizon_g(g.env, p, d), idx);
-  f3 table = F3(0, 0, 0);
-  if (g.threshold > 0) table = in_scatter_g(g.env, idx, fdot(d, l));
-  const float u[4] = {idx[3], idx[2], idx[1], idx[0]};
+// Sines and cosines of pi f_k u for the 16 feature frequencies f_k = 2^(k/2):
+// sincospi at f_0 and f_1, the rest by exact angle doubling
+// (sin 2a = 2 sin a cos a, cos 2a = 1 - 2 sin^2 a), written as 4 x 8 BF16
+// (sin, cos pairs in k order) at K columns col0 .. col0 + 31 of row `row`.
+__device__ __forceinline__ void write_features(float u, unsigned char* A, int row, int col0) {
+  float s[16], c[16];
+  sincospif(u, &s[0], &c[0]);
+  sincospif(kFeatureSqrt2 * u, &s[1], &c[1]);
 #pragma unroll
-  for (int dd = 0; dd < 4; dd++) {
+  for (int k = 2; k < 16; k++) {
+    const float ss = s[k - 2] + s[k - 2];
+    s[k] = ss * c[k - 2];
+    c[k] = fmaf(-ss, s[k - 2], 1.0f);
+  }
 #pragma unroll
-    for (int kc = 0; kc < 2; kc++) {  // 8 frequencies = 16 features = two 16-byte chunks
-      __nv_bfloat16 v8[8];
+  for (int q = 0; q < 4; q++) {
+    uint32_t w[4];
 #pragma unroll
-      for (int j = 0; j < 4; j++) {
-        float sn, cs;
-        sincospif(exp2f(0.5f * (float)(kc * 4 + j)) * u[dd], &sn, &cs);
-        v8[2 * j] = __float2bfloat16(sn);
-        v8[2 * j + 1] = __float2bfloat16(cs);
-      }
-      const int k = dd * 32 + kc * 8;
-      *reinterpret_cast<uint4*>(A + tc::tile_offset(t, k, 256)) = *reinterpret_cast<const uint4*>(v8);
-      // the second half of the 16 frequencies of this coordinate
-      __nv_bfloat16 w8[8];
-#pragma unroll
-      for (int j = 0; j < 4; j++) {
-        float sn, cs;
-        sincospif(exp2f(0.5f * (float)(8 + kc * 4 + j)) * u[dd], &sn, &cs);
-        w8[2 * j] = __float2bfloat16(sn);
-        w8[2 * j + 1] = __float2bfloat16(cs);
-      }
-      *reinterpret_cast<uint4*>(A + tc::tile_offset(t, k + 16, 256)) = *reinterpret_cast<const uint4*>(w8);
+    for (int j = 0; j < 4; j++) {
+      const __nv_bfloat162 h = __floats2bfloat162_rn(s[4 * q + j], c[4 * q + j]);
+      w[j] = *reinterpret_cast<const uint32_t*>(&h);
     }
+    *reinterpret_cast<uint4*>(A + tc::tile_offset(row, col0 + 8 * q, kMlpHidden)) = make_uint4(w[0], w[1], w[2], w[3]);
+  }
+}
+
+// Producer thread: weight chunks through the ring, MMAs of both tiles.
+__device__ void infer_producer(const InferArgs& g, long long my_groups, unsigned char* smem, uint32_t tmem,
+                               uint64_t* full, uint64_t* empty, uint64_t* acc_bar, uint64_t* act_bar,
+                               volatile int* abort_flag) {
+  unsigned char* ring = smem + kInferSmemRing;
+  const long long total = my_groups * kInferChunks;
+  long long issued = 0, c = 0;
+  auto issue = [&](long long k) {
+    const int s = (int)(k % kInferStages);
+    tc::mbar_expect_tx(&full[s], kInferChunkBytes);
+    tc::bulk_g2s(ring + s * kInferChunkBytes, g.packed + (size_t)(k % kInferChunks) * kInferChunkBytes,
+                 kInferChunkBytes, &full[s]);
+  };
+  for (; issued < total && issued < kInferStages; issued++) issue(issued);
+  const uint32_t idesc = tc::idesc_bf16(128, kMlpHidden);
+  const uint32_t a_base = tc::smem_u32(smem), w_base = tc::smem_u32(ring);
+  uint32_t act_phase = 0;
+  bool ok = true;
+  for (long long gi = 0; gi < my_groups && ok; gi++) {
+    for (int layer = 0; layer < 4 && ok; layer++) {
+      ok = tc::mbar_wait(act_bar, act_phase & 1, kInferWaitLimit) && !*abort_flag;
+      act_phase++;
+      if (!ok) break;
+      tc::fence_after();
+      const int nk = layer == 0 ? kInferChunks0 : kInferChunksH;
+      for (int j = 0; j < nk; j++, c++) {
+        const int s = (int)(c % kInferStages);
+        if (!(ok = tc::mbar_wait(&full[s], (uint32_t)((c / kInferStages) & 1), kInferWaitLimit))) break;
+        tc::fence_after();
+        const uint32_t w0 = w_base + s * kInferChunkBytes;
+#pragma unroll
+        for (int tile = 0; tile < 2; tile++) {
+          const uint32_t a0 = a_base + tile * kInferTileBytes + j * (kInferKC / 8) * 128;
+#pragma unroll
+          for (int ks = 0; ks < kInferKC / 16; ks++)
+            tc::mma(tmem + tile * kMlpHidden, tc::smem_desc(a0 + ks * 256, 128, kMlpHidden * 16),
+                    tc::smem_desc(w0 + ks * 256, 128, kInferKC * 16), idesc, (j > 0 || ks > 0) ? 1u : 0u);
+        }
+        tc::commit(&empty[s]);
+        if (c >= 1 && issued < total) {  // refill the stage of the previous chunk
+          const long long p = c - 1;
+          if (!(ok = tc::mbar_wait(&empty[p % kInferStages], (uint32_t)((p / kInferStages) & 1), kInferWaitLimit)))
+            break;
+          issue(issued++);
+        }
+      }
+      if (ok) tc::commit(acc_bar);
+    }
+  }
+  if (!ok) {
+    *abort_flag = 1;
+    if (g.error) atomicExch(g.error, 1);
+    // let the copies in flight land and the issued MMAs finish before the CTA leaves
+    for (long long k = c; k < issued; k++)
+      tc::mbar_wait(&full[k % kInferStages], (uint32_t)((k / kInferStages) & 1), kInferWaitLimit);
+    if (c >= 1) tc::mbar_wait(&empty[(c - 1) % kInferStages], (uint32_t)(((c - 1) / kInferStages) & 1), kInferWaitLimit);
+  }
+}
+
+__global__ void __launch_bounds__(kInferThreads, 1) k_surrogate_infer(InferArgs g) {
+  extern __shared__ __align__(1024) unsigned char smem[];
+  float* s_bias = reinterpret_cast<float*>(smem + kInferSmemBias);  // 0.5 b_l, 4 x 256
+  float* s_w5 = reinterpret_cast<float*>(smem + kInferSmemHead);    // W5 [3][256], then b5
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem + kInferSmemBar);
+  uint64_t* empty = full + kInferStages;
+  uint64_t* acc_bar = empty + kInferStages;
+  uint64_t* act_bar = acc_bar + 1;
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(act_bar + 1);
+  volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
+  const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
+  const long long ngroups = (g.n + 255) / 256;
+  const long long my_groups = blockIdx.x < ngroups ? (ngroups - 1 - blockIdx.x) / gridDim.x + 1 : 0;
+
+  for (int i = t; i < 4 * kMlpHidden; i += kInferThreads) s_bias[i] = 0.5f * g.b[i / kMlpHidden][i % kMlpHidden];
+  for (int i = t; i < 3 * kMlpHidden; i += kInferThreads) s_w5[i] = g.W5[i];
+  if (t < 3) s_w5[3 * kMlpHidden + t] = g.b5[t];
+  if (warp == 0) tc::tmem_alloc(tmem_slot, 2 * kMlpHidden);
+  if (t == 0) {
+    for (int s = 0; s < kInferStages; s++) {
+      tc::mbar_init(&full[s], 1);
+      tc::mbar_init(&empty[s], 1);
+    }
+    tc::mbar_init(acc_bar, 1);
+    tc::mbar_init(act_bar, 256);
+    *abort_flag = 0;
+    tc::fence_mbar_init();
   }
   tc::fence_before();
   __syncthreads();
   tc::fence_after();
-  const uint32_t tmem = tmem_slot;
-  const uint32_t idesc = tc::idesc_bf16(128, 256);
-  uint32_t parity = 0;
-  bool ok = true;
-  float head[3] = {0, 0, 0};
-  for (int layer = 0; layer < 4 && ok; layer++) {
-    const int K = layer == 0 ? kMlpIn : kMlpHidden;
-    const __nv_bfloat16* W = g.W[layer];
-    for (int kc = 0; kc < K / 64 && ok; kc++) {
-      // weight chunk: 256 rows x 64 K
-      for (int c = t; c < 256 * 8; c += 128) {
-        const int row = c >> 3, ch = c & 7;
-        const uint4 v = *reinterpret_cast<const uint4*>(W + (long long)row * K + kc * 64 + ch * 8);
-        *reinterpret_cast<uint4*>(Wt + tc::tile_offset(row, ch * 8)) = v;
-      }
+  const uint32_t tmem = *tmem_slot;
+
+  if (warp == 8) {
+    if (lane == 0) infer_producer(g, my_groups, smem, tmem, full, empty, acc_bar, act_bar, abort_flag);
+    __syncwarp();
+  } else {
+    const int tile = warp >> 2, row = (warp & 3) * 32 + lane;
+    unsigned char* A = smem + tile * kInferTileBytes;
+    const uint32_t trow = tmem + ((uint32_t)((warp & 3) * 32) << 16) + (uint32_t)(tile * kMlpHidden);
+    uint32_t acc_phase = 0;
+    bool ok = true;
+    for (long long gi = 0; gi < my_groups && ok; gi++) {
+      const long long q = (blockIdx.x + gi * gridDim.x) * 256 + tile * 128 + row;
+      const bool valid = q < g.n;
+      const long long qq = valid ? q : g.n - 1;
+      const f3 p = F3((float)g.X[3 * qq], (float)g.X[3 * qq + 1], (float)g.X[3 * qq + 2]);
+      const f3 d = F3((float)g.V[3 * qq], (float)g.V[3 * qq + 1], (float)g.V[3 * qq + 2]);
+      const f3 l = F3((float)g.L[3 * qq], (float)g.L[3 * qq + 1], (float)g.L[3 * qq + 2]);
+      float idx[4];
+      ray_scatter_forward_g(g.env, p, d, l, is_above_horizon_g(g.env, p, d), idx);
+      f3 table = F3(0, 0, 0);
+      if (g.threshold > 0) table = in_scatter_g(g.env, idx, fdot(d, l));
+      // coordinates (height, elevation, sun elevation, heading) = idx reversed
+#pragma unroll
+      for (int dd = 0; dd < 4; dd++) write_features(idx[3 - dd], A, row, 32 * dd);
       tc::fence_async_smem();
-      __syncthreads();
-      if (t == 0) {
+      tc::fence_before();
+      tc::mbar_arrive(act_bar);
+      float head[3] = {0, 0, 0};
+      for (int layer = 0; layer < 4; layer++) {
+        bool done = tc::mbar_wait(acc_bar, acc_phase & 1, kInferWaitLimit);
+        acc_phase++;
+        if (!__all_sync(0xffffffffu, done) || *abort_flag) {
+          ok = false;
+          break;
+        }
         tc::fence_after();
-        const uint32_t a0 = tc::smem_u32(A), w0 = tc::smem_u32(Wt);
+        const float* hb = s_bias + layer * kMlpHidden;
+        for (int n0 = 0; n0 < kMlpHidden; n0 += 64) {
+          uint32_t r[64];
+          tc::tmem_ld64(trow + (uint32_t)n0, r);
 #pragma unroll
-        for (int ks = 0; ks < 4; ks++) {
-          const uint64_t da = tc::smem_desc(a0 + kc * 1024 + ks * 256, 128, 4096);
-          const uint64_t db = tc::smem_desc(w0 + ks * 256, 128, 1024);
-          tc::mma(tmem, da, db, idesc, (kc > 0 || ks > 0) ? 1u : 0u);
+          for (int i8 = 0; i8 < 8; i8++) {
+            const float4 b0 = *reinterpret_cast<const float4*>(hb + n0 + 8 * i8);
+            const float4 b1 = *reinterpret_cast<const float4*>(hb + n0 + 8 * i8 + 4);
+            const float bb[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
+            uint32_t w[4];
+            float hv[8];
+#pragma unroll
+            for (int j = 0; j < 8; j += 2) {
+              // SiLU(z) = z sigmoid(z) = hz (1 + tanh hz) with hz = z / 2
+              const float h0 = fmaf(0.5f, __uint_as_float(r[8 * i8 + j]), bb[j]);
+              const float h1 = fmaf(0.5f, __uint_as_float(r[8 * i8 + j + 1]), bb[j + 1]);
+              const __nv_bfloat162 hh = __floats2bfloat162_rn(fmaf(h0, tanh_approx(h0), h0), fmaf(h1, tanh_approx(h1), h1));
+              w[j / 2] = *reinterpret_cast<const uint32_t*>(&hh);
+              hv[j] = __low2float(hh);
+              hv[j + 1] = __high2float(hh);
+            }
+            if (layer < 3) {
+              *reinterpret_cast<uint4*>(A + tc::tile_offset(row, n0 + 8 * i8, kMlpHidden)) =
+                  make_uint4(w[0], w[1], w[2], w[3]);
+            } else {
+#pragma unroll
+              for (int cc = 0; cc < 3; cc++) {
+                const float4 w0 = *reinterpret_cast<const float4*>(s_w5 + cc * kMlpHidden + n0 + 8 * i8);
+                const float4 w1 = *reinterpret_cast<const float4*>(s_w5 + cc * kMlpHidden + n0 + 8 * i8 + 4);
+                head[cc] = fmaf(hv[0], w0.x, fmaf(hv[1], w0.y, fmaf(hv[2], w0.z, fmaf(hv[3], w0.w, head[cc]))));
+                head[cc] = fmaf(hv[4], w1.x, fmaf(hv[5], w1.y, fmaf(hv[6], w1.z, fmaf(hv[7], w1.w, head[cc]))));
+              }
+            }
+          }
         }
-        tc::commit(&mbar);
-      }
-      bool done = tc::mbar_wait(&mbar, parity, 1 << 22);
-      if (!done) done = tc::mbar_wait(&mbar, parity, 1 << 22);
-      parity ^= 1;
-      tc::fence_after();
-      ok = __syncthreads_and(done) != 0;
-    }
-    if (!ok) break;
-    // epilogue: row t of the accumulator (warp w owns rows 32w..32w+31)
-    const float* bias = g.b[layer];
-    for (int n0 = 0; n0 < 256; n0 += 8) {
-      float v[8];
-      tc::tmem_ld8(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)n0, v);
-      __nv_bfloat16 h8[8];
-#pragma unroll
-      for (int i = 0; i < 8; i++) {
-        const float z = v[i] + bias[n0 + i];
-        const float h = __bfloat162float(__float2bfloat16(z / (1.0f + __expf(-z))));
-        h8[i] = __float2bfloat16(h);
-        if (layer == 3) {
-#pragma unroll
-          for (int c = 0; c < 3; c++) head[c] = fmaf(h, g.W5[c * 256 + n0 + i], head[c]);
+        if (layer < 3) {
+          tc::fence_async_smem();
+          tc::fence_before();
+          tc::mbar_arrive(act_bar);
         }
       }
-      if (layer < 3) *reinterpret_cast<uint4*>(A + tc::tile_offset(t, n0, 256)) = *reinterpret_cast<const uint4*>(h8);
-    }
-    tc::fence_before();
-    __syncthreads();
-    tc::fence_after();
-  }
-  (void)lane;
-  bool flag = false;
-  if (ok && valid) {
-    const float tv[3] = {table.x, table.y, table.z};
+      if (!ok) break;
+      bool flag = false;
+      if (valid) {
+        const float tv[3] = {table.x, table.y, table.z};
 #pragma unroll
-    for (int c = 0; c < 3; c++) {
-      const float y = head[c] + g.b5[c];
-      const float val = fmaxf(expf(y) - g.eps, 0.0f);
-      g.out[3 * q + c] = val;
-      if (g.threshold > 0 && fabsf(val - tv[c]) > g.threshold * fmaxf(fabsf(tv[c]), g.floor_abs)) flag = true;
+        for (int cc = 0; cc < 3; cc++) {
+          const float y = head[cc] + s_w5[3 * kMlpHidden + cc];
+          const float val = fmaxf(expf(y) - g.eps, 0.0f);
+          g.out[3 * q + cc] = val;
+          if (g.threshold > 0 && fabsf(val - tv[cc]) > g.threshold * fmaxf(fabsf(tv[cc]), g.floor_abs)) flag = true;
+        }
+        if (g.mask) g.mask[q] = flag ? 1 : 0;
+      }
+      if (g.count) {
+        const unsigned bal = __ballot_sync(0xffffffffu, flag);
+        if (lane == 0 && bal) atomicAdd(g.count, (unsigned long long)__popc(bal));
+      }
     }
-    if (g.mask) g.mask[q] = flag ? 1 : 0;
-  }
-  if (!ok && t == 0 && g.error) atomicExch(g.error, 1);
-  if (g.count) {
-    const unsigned bal = __ballot_sync(0xffffffffu, flag);
-    if (lane == 0 && bal) atomicAdd(g.count, (unsigned long long)__popc(bal));
+    if (!ok) {
+      *abort_flag = 1;
+      if (lane == 0 && g.error) atomicExch(g.error, 1);
+    }
   }
   tc::fence_before();
   __syncthreads();
-  if (warp == 0) tc::tmem_dealloc(tmem, 256);
+  if (warp == 0) tc::tmem_dealloc(tmem, 2 * kMlpHidden);
 }
 
 int launch_surrogate_infer(const QueryTables& qt, long long n, const double* x, const double* v, const double* l,
                            const __nv_bfloat16* const* W, const float* const* b, const float* W5, const float* b5,
                            float eps, float threshold, float floor_abs, float* out, unsigned char* mask,
-                           unsigned long long* count, int* error, cudaStream_t st) {
+                           unsigned long long* count, int* error, unsigned char* packed, int num_sms,
+                           cudaStream_t st) {
+  constexpr int nthreads = kMlpHidden * (kMlpIn / 8) + 3 * kMlpHidden * (kMlpHidden / 8);
+  k_pack_infer<<<(nthreads + 255) / 256, 256, 0, st>>>(W[0], W[1], W[2], W[3], packed);
   InferArgs g;
   g.env = make_env(qt, 0);
   g.n = n;
   g.X = x;
   g.V = v;
   g.L = l;
-  for (int i = 0; i < 4; i++) {
-    g.W[i] = W[i];
-    g.b[i] = b[i];
-  }
+  g.packed = packed;
+  for (int i = 0; i < 4; i++) g.b[i] = b[i];
   g.W5 = W5;
   g.b5 = b5;
   g.out = out;
@@ -737,10 +882,12 @@ int launch_surrogate_infer(const QueryTables& qt, long long n, const double* x, 
   g.mask = mask;
   g.count = count;
   g.error = error;
-  const int smem = kInferSmemA + kInferSmemW;
-  if (cudaFuncSetAttribute(k_surrogate_infer, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess)
+  if (cudaFuncSetAttribute(k_surrogate_infer, cudaFuncAttributeMaxDynamicSharedMemorySize, kInferSmem) !=
+      cudaSuccess)
     return -1;
-  k_surrogate_infer<<<(unsigned)((n + 127) / 128), 128, smem, st>>>(g);
+  const long long groups = (n + 255) / 256;
+  const unsigned grid = (unsigned)(groups < num_sms ? groups : num_sms);
+  k_surrogate_infer<<<grid, kInferThreads, kInferSmem, st>>>(g);
   return 0;
 }
 

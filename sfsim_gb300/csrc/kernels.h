@@ -116,7 +116,10 @@ void launch_make_pool(long long n, const float* coords, const float* values, flo
 int launch_surrogate_infer(const QueryTables& qt, long long n, const double* x, const double* v, const double* l,
                            const __nv_bfloat16* const* W, const float* const* b, const float* W5, const float* b5,
                            float eps, float threshold, float floor_abs, float* out, unsigned char* mask,
-                           unsigned long long* count, int* error, cudaStream_t st);
+                           unsigned long long* count, int* error, unsigned char* packed, int num_sms,
+                           cudaStream_t st);
+// Bytes of the packed weight chunks the inference kernel streams.
+size_t infer_packed_bytes();
 void launch_surrogate_finish(long long n, const float* y, float eps, const float* table, float thr, float floor_abs,
                              float* out, unsigned char* mask, unsigned long long* count, cudaStream_t st);
 
@@ -159,6 +162,12 @@ int launch_gemm_tn(const GemmArgs& g, int splits, cudaStream_t st);
 constexpr int kMlpIn = 128;
 constexpr int kMlpHidden = 256;
 constexpr int kMlpLayers = 4;
+// Feature frequencies f_k = 2^(k/2), k = 0..15: powers of two times 1 or the
+// float nearest sqrt(2), so that doubling the angle steps k by two exactly.
+constexpr float kFeatureSqrt2 = 1.41421356237309505f;
+__host__ __device__ __forceinline__ float feature_frequency(int k) {
+  return (k & 1 ? kFeatureSqrt2 : 1.0f) * (float)(1 << (k >> 1));
+}
 
 void launch_features(long long n, const float* coords, __nv_bfloat16* F, __nv_bfloat16* FT, cudaStream_t st);
 void launch_head_forward(long long n, const __nv_bfloat16* H, const float* W5, const float* b5, float* out,
