@@ -323,11 +323,24 @@ def _timed(fn, reps=3):
     return best, r
 
 
-def run_queries(C):
+def query_error_stats(a, ref):
+    """Per-query relative error (max over RGB, floor 1e-6 of the largest
+    reference value) summarised."""
+    import torch
+    floor = 1e-6 * ref.abs().max()
+    e = ((a - ref).abs() / torch.maximum(ref.abs(), floor)).max(dim=1).values
+    q = torch.quantile(e[: 1 << 20].double(), torch.tensor([0.5, 0.9, 0.99], device=e.device, dtype=torch.float64))
+    return {"median": float(q[0]), "p90": float(q[1]), "p99": float(q[2]), "max": float(e.max()),
+            "frac_le_1e-3": float((e <= 1e-3).double().mean()), "frac_le_1e-2": float((e <= 1e-2).double().mean())}
+
+
+def run_queries(C, steps=3000, batch=65536, direct_samples=1 << 24, lr=3e-3, huber_delta=0.0,
+                thresholds=(3e-2, 1e-2, 3e-3, 1e-3)):
     """2^24 random in-scatter queries (height uniform 0-100 km, view and sun
     uniform on the sphere) on the production tables: table lookup, direct
-    quadrature, the trained surrogate and the surrogate with fallback; errors
-    relative to direct quadrature (floor 1e-6 of the largest value)."""
+    quadrature, the trained surrogate (the lookup with the network's
+    correction) and the surrogate with fallback to direct quadrature where its
+    predicted error exceeds a threshold; errors relative to direct quadrature."""
     import time as _t
 
     import torch
@@ -336,8 +349,8 @@ def run_queries(C):
     cfg = C.production()
     ctx = Context(cfg)
     t0 = _t.perf_counter()
-    steps, batch = 3000, 65536
-    hist = ctx.train_surrogate(steps=steps, batch=batch, direct_samples=1 << 23, node_fraction=0.75, lr=1e-3, seed=1)
+    hist = ctx.train_surrogate(steps=steps, batch=batch, direct_samples=direct_samples, node_fraction=0.0, lr=lr,
+                               seed=1, huber_delta=huber_delta)
     torch.cuda.synchronize()
     train_s = _t.perf_counter() - t0
     n = 1 << 24
@@ -348,26 +361,18 @@ def run_queries(C):
     t_direct, direct = _timed(lambda: ctx.direct(x, v, l, out=out).clone(), reps=1)
     t_sur, (sur, _) = _timed(lambda: ctx.surrogate(x, v, l, out=out))
     sur = sur.clone()
-    res = {}
-    for thr in (1e-2, 1e-3):
-        t_fb, (fb, nf) = _timed(lambda: ctx.surrogate(x, v, l, threshold=thr, out=out), reps=1)
-        res[thr] = (t_fb, fb.clone(), nf)
-    floor = 1e-6 * direct.abs().max()
-
-    def stats(a):
-        e = ((a - direct).abs() / torch.maximum(direct.abs(), floor)).max(dim=1).values
-        q = torch.quantile(e[: 1 << 20], torch.tensor([0.5, 0.99], device="cuda", dtype=e.dtype))
-        return {"median": float(q[0]), "p99": float(q[1]), "max": float(e.max()),
-                "frac_le_1e-3": float((e <= 1e-3).double().mean())}
     qps = lambda ms: n / (ms * 1e-3)  # noqa: E731
-    r = {"n": n, "train_steps": steps, "train_batch": batch, "train_s": train_s,
+    r = {"n": n, "train_steps": steps, "train_batch": batch, "direct_samples": direct_samples, "lr": lr,
+         "huber_delta": huber_delta, "train_s": train_s,
          "train_loss_first": float(hist[:10].mean()), "train_loss_last": float(hist[-100:].mean()),
-         "table": {"qps": qps(t_table), "err": stats(table)},
+         "table": {"qps": qps(t_table), "err": query_error_stats(table, direct)},
          "direct": {"qps": qps(t_direct)},
-         "surrogate": {"qps": qps(t_sur), "err": stats(sur), "vs_direct": t_direct / t_sur}}
-    for thr, (t_fb, fb, nf) in res.items():
-        r[f"surrogate_fallback_{thr:g}"] = {"qps": qps(t_fb), "fallback_fraction": nf / n, "err": stats(fb),
-                                            "vs_direct": t_direct / t_fb}
+         "surrogate": {"qps": qps(t_sur), "err": query_error_stats(sur, direct), "vs_direct": t_direct / t_sur}}
+    del table, sur
+    for thr in thresholds:
+        t_fb, (fb, nf) = _timed(lambda: ctx.surrogate(x, v, l, threshold=thr, out=out), reps=1)
+        r[f"surrogate_fallback_{thr:g}"] = {"qps": qps(t_fb), "fallback_fraction": nf / n,
+                                            "err": query_error_stats(fb, direct), "vs_direct": t_direct / t_fb}
     ctx.close()
     return r
 

@@ -202,9 +202,12 @@ int sfsim_atmo_query_table(const sfsim_atmo_context* ctx, int kind, long long n,
 int sfsim_atmo_query_direct(const sfsim_atmo_context* ctx, long long n, const double* x,
                             const double* v, const double* l, float* out, void* stream);
 
-/* Table coordinates in [0, 1] of (x, v, l): height, elevation, sun elevation
- * and sun heading as core/ray-scatter-forward.glsl forms them (FP32), with
- * the table half chosen by is_above_horizon; coords is a DEVICE [n][4]. */
+/* The surrogate's six coordinates in [0, 1] of (x, v, l): the table
+ * coordinates height, elevation, sun elevation and sun heading as
+ * core/ray-scatter-forward.glsl forms them (FP32), with the table half chosen
+ * by is_above_horizon; then (1 + sin of the sun elevation) / 2 without the
+ * lookup's clamp, and the table half (0 upper, 1 lower).  coords is a DEVICE
+ * [n][6]. */
 int sfsim_atmo_query_coords(const sfsim_atmo_context* ctx, long long n, const double* x, const double* v,
                             const double* l, float* coords, void* stream);
 
@@ -223,6 +226,7 @@ typedef struct sfsim_atmo_surrogate_config {
   float node_fraction;      /* share of each batch drawn from the table nodes */
   float lr;                 /* initial learning rate, cosine decay to 0 */
   unsigned long long seed;
+  float huber_delta;        /* > 0: Huber loss of the corrections with this threshold; 0: squared error */
 } sfsim_atmo_surrogate_config;
 
 /* Trains (or continues training) the context's surrogate on the GPU;
@@ -230,22 +234,29 @@ typedef struct sfsim_atmo_surrogate_config {
 int sfsim_atmo_surrogate_train(sfsim_atmo_context* ctx, const sfsim_atmo_surrogate_config* cfg,
                                float* loss_history);
 
-/* Parameter vector (FP32, W1 [256][128], b1, W2, b2, W3, b3, W4, b4 [256][256],
- * W5 [3][256], b5): *count receives its length; `get` copies it out, `set`
- * replaces it (host arrays, either may be NULL). */
+/* Parameter vector (FP32, W1 [256][192], b1, W2, b2, W3, b3, W4, b4 [256][256],
+ * W5 [4][256], b5 [4]): *count receives its length; `get` copies it out, `set`
+ * replaces it (host arrays, either may be NULL).  Outputs 0-2 are corrections
+ * r = log(value + 1e-7) - log(table + 1e-7) to the in-scatter lookup, output 3
+ * the log of their expected squared error. */
 int sfsim_atmo_surrogate_parameters(sfsim_atmo_context* ctx, float* get, const float* set, long long* count);
 
-/* Loss and parameter gradients of one batch (host coords [n][4], targets
- * [n][3]; n a multiple of 1024) without updating, for validation. */
+/* Loss (mean squared error of the corrections) and parameter gradients of
+ * one batch (host coords [n][6], target corrections [n][3]; n a multiple of
+ * 1024) without updating, for validation.  The gradients also carry the
+ * Gaussian negative log-likelihood of the squared error under the predicted
+ * variance, weighted 0.01. */
 int sfsim_atmo_surrogate_gradients(sfsim_atmo_context* ctx, long long n, const float* coords,
                                    const float* targets, float* loss, float* grads);
 
 /* Rendered in-scatter at (x, v, l) from the surrogate (DEVICE arrays as in
- * sfsim_atmo_query_direct), one fused tensor-core kernel: coordinates,
- * features, the four hidden layers (tcgen05 MMA into tensor memory) and the
- * head per 128 queries.  With threshold > 0, points where the surrogate
- * and the table lookup differ by more than `threshold` (relative, floor 1e-7)
- * are recomputed by direct quadrature; *n_fallback receives their number. */
+ * sfsim_atmo_query_direct), one fused tensor-core kernel: coordinates, the
+ * table lookup, features, the four hidden layers (tcgen05 MMA into tensor
+ * memory) and the head per 256 queries; the value is the lookup corrected by
+ * the network, (table + 1e-7) exp(r) - 1e-7.  With threshold > 0, points whose
+ * predicted relative error (the square root of the variance output) exceeds
+ * `threshold` are recomputed by direct quadrature; *n_fallback receives their
+ * number. */
 int sfsim_atmo_query_surrogate(sfsim_atmo_context* ctx, long long n, const double* x, const double* v,
                                const double* l, float* out, float threshold, long long* n_fallback,
                                void* stream);

@@ -32,7 +32,8 @@ EXPORTS = (
 
 class SurrogateConfig(ctypes.Structure):
     _fields_ = [("steps", ctypes.c_int), ("batch", ctypes.c_int), ("direct_samples", ctypes.c_longlong),
-                ("node_fraction", ctypes.c_float), ("lr", ctypes.c_float), ("seed", ctypes.c_ulonglong)]
+                ("node_fraction", ctypes.c_float), ("lr", ctypes.c_float), ("seed", ctypes.c_ulonglong),
+                ("huber_delta", ctypes.c_float)]
 
 
 class Intermediates(ctypes.Structure):

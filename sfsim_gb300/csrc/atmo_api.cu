@@ -896,10 +896,13 @@ int context_build(sfsim_atmo_context* c) {
 
 // ---------------------------------------------------------------------------
 // Surrogate of the rendered in-scatter: Fourier features of the four table
-// coordinates -> 4 x 256 SiLU -> 3 log-RGB outputs, trained on the GPU.
+// coordinates -> 4 x 256 SiLU -> 3 log-space corrections to the table lookup
+// and the log of their expected squared error, trained on the GPU against the
+// direct quadrature.
 // ---------------------------------------------------------------------------
 
-constexpr float kLogEps = 1e-8f;  // outputs are log(value + kLogEps)
+constexpr float kLogEps = 1e-7f;     // corrections are log(value + kLogEps) - log(table + kLogEps)
+constexpr float kVarWeight = 0.01f;  // weight of the variance output's gradient in the shared layers
 
 // parameter offsets (floats) in the concatenated FP32 vector
 struct MlpLayout {
@@ -907,7 +910,7 @@ struct MlpLayout {
   int in[5], out[5];
   MlpLayout() {
     const int ins[5] = {kMlpIn, kMlpHidden, kMlpHidden, kMlpHidden, kMlpHidden};
-    const int outs[5] = {kMlpHidden, kMlpHidden, kMlpHidden, kMlpHidden, 3};
+    const int outs[5] = {kMlpHidden, kMlpHidden, kMlpHidden, kMlpHidden, kMlpOut};
     long long o = 0;
     for (int l = 0; l < 5; l++) {
       in[l] = ins[l];
@@ -1022,10 +1025,10 @@ int surrogate_alloc(sfsim_atmo_context* c, long long batch, unsigned long long s
     for (int l = 0; l < 4; l++) {
       drop(S.H[l]); drop(S.HT[l]); drop(S.dZ[l]); drop(S.dZT[l]); drop(S.dsilu[l]);
     }
-    S.coords = S.alloc_f(4 * batch);
+    S.coords = S.alloc_f(kMlpCoords * batch);
     S.target = S.alloc_f(3 * batch);
-    S.out = S.alloc_f(3 * batch);
-    S.dout = S.alloc_f(3 * batch);
+    S.out = S.alloc_f(kMlpOut * batch);
+    S.dout = S.alloc_f(kMlpOut * batch);
     S.F = S.alloc_h(kMlpIn * batch);
     S.FT = S.alloc_h(kMlpIn * batch);
     bool okay = S.coords && S.target && S.out && S.dout && S.F && S.FT;
@@ -1047,7 +1050,7 @@ int surrogate_alloc(sfsim_atmo_context* c, long long batch, unsigned long long s
 }
 
 // Forward pass over n rows of S.coords (n <= S.batch); `train` keeps what the
-// backward pass needs.  Leaves log-RGB predictions in S.out.
+// backward pass needs.  Leaves the kMlpOut outputs per row in S.out.
 int surrogate_forward(Surrogate& S, long long n, bool train, cudaStream_t st) {
   launch_features(n, S.coords, S.F, train ? S.FT : nullptr, st);
   const __nv_bfloat16* prev = S.F;
@@ -1077,12 +1080,12 @@ int surrogate_forward(Surrogate& S, long long n, bool train, cudaStream_t st) {
   return 0;
 }
 
-// Gradients of the mean squared log-RGB error over n rows into S.g (zeroed
+// Gradients of the loss (k_mlp.cu: k_loss_grad) over n rows into S.g (zeroed
 // first); the loss lands in S.loss.
-int surrogate_backward(Surrogate& S, long long n, cudaStream_t st) {
+int surrogate_backward(Surrogate& S, long long n, float huber, cudaStream_t st) {
   CUDA_TRY(cudaMemsetAsync(S.g, 0, sizeof(float) * S.lay.total, st));
   CUDA_TRY(cudaMemsetAsync(S.loss, 0, sizeof(float), st));
-  launch_loss_grad(n, S.out, S.target, S.dout, S.loss, st);
+  launch_loss_grad(n, S.out, S.target, huber, kVarWeight, S.dout, S.loss, st);
   launch_head_backward(n, S.dout, S.H[3], S.w + S.lay.W[4], S.dsilu[3], S.dZ[3], S.dZT[3], S.g + S.lay.W[4],
                        S.g + S.lay.b[4], st);
   int splits = 1;
@@ -1371,36 +1374,36 @@ int surrogate_pools(sfsim_atmo_context* c, long long n_direct, unsigned long lon
                     float** direct_pool, std::vector<void*>& temps, cudaStream_t st) {
   const BuildDims& d = c->dims;
   void* p = nullptr;
-  if (cudaMalloc(&p, sizeof(float) * 7 * (size_t)d.n4()) != cudaSuccess)
+  if (cudaMalloc(&p, sizeof(float) * kPoolRow * (size_t)d.n4()) != cudaSuccess)
     return fail(SFSIM_ATMO_ENOMEM, "node pool allocation failed");
   temps.push_back(p);
   *node_pool = (float*)p;
-  launch_node_pool(d, c->S, c->M, (const CellGeom<float>*)c->geom, (float)c->cfg.mie.scatter_g, kLogEps, *node_pool,
-                   st);
+  launch_node_pool(d, *node_pool, st);
   *direct_pool = nullptr;
   if (n_direct > 0) {
-    if (cudaMalloc(&p, sizeof(float) * 7 * (size_t)n_direct) != cudaSuccess)
+    if (cudaMalloc(&p, sizeof(float) * kPoolRow * (size_t)n_direct) != cudaSuccess)
       return fail(SFSIM_ATMO_ENOMEM, "direct pool allocation failed");
     temps.push_back(p);
     *direct_pool = (float*)p;
     const long long chunk = 1 << 20;
     double* xvl = nullptr;
-    float *vals = nullptr, *crd = nullptr;
-    if (cudaMalloc(&xvl, sizeof(double) * 9 * chunk) != cudaSuccess ||
-        cudaMalloc(&vals, sizeof(float) * 3 * chunk) != cudaSuccess ||
-        cudaMalloc(&crd, sizeof(float) * 4 * chunk) != cudaSuccess)
+    float *vals = nullptr, *crd = nullptr, *tab = nullptr;
+    auto get = [&](void** q, size_t bytes) {
+      if (cudaMalloc(q, bytes) != cudaSuccess) return false;
+      temps.push_back(*q);
+      return true;
+    };
+    if (!get((void**)&xvl, sizeof(double) * 9 * chunk) || !get((void**)&vals, sizeof(float) * 3 * chunk) ||
+        !get((void**)&crd, sizeof(float) * kMlpCoords * chunk) || !get((void**)&tab, sizeof(float) * 3 * chunk))
       return fail(SFSIM_ATMO_ENOMEM, "direct sample allocation failed");
-    temps.push_back(xvl);
-    temps.push_back(vals);
-    temps.push_back(crd);
     const QueryTables q = context_tables(c);
     for (long long o = 0; o < n_direct; o += chunk) {
       const long long m = std::min(chunk, n_direct - o);
       launch_random_queries(m, seed * 1000003ull + (unsigned long long)o, c->cfg.radius, c->cfg.height, xvl,
                             xvl + 3 * chunk, xvl + 6 * chunk, st);
       launch_query_direct(c->params, d, c->jsum, m, xvl, xvl + 3 * chunk, xvl + 6 * chunk, vals, st);
-      launch_query_coords(q, m, xvl, xvl + 3 * chunk, xvl + 6 * chunk, crd, nullptr, st);
-      launch_make_pool(m, crd, vals, kLogEps, *direct_pool + 7 * o, st);
+      launch_query_coords(q, m, xvl, xvl + 3 * chunk, xvl + 6 * chunk, crd, tab, st);
+      launch_make_pool(m, crd, vals, tab, kLogEps, *direct_pool + kPoolRow * o, st);
     }
   }
   CUDA_TRY(cudaGetLastError());
@@ -1415,8 +1418,9 @@ int sfsim_atmo_surrogate_train(sfsim_atmo_context* ctx, const sfsim_atmo_surroga
   if (!ctx || !sc) return fail(SFSIM_ATMO_ENULL, "NULL argument");
   if (ctx->cfg.precision != SFSIM_ATMO_FP32) return fail(SFSIM_ATMO_EINVAL, "the surrogate needs an FP32 context");
   if (sc->steps < 0 || sc->batch < 1024 || sc->batch % 1024 != 0 || sc->direct_samples < 0 ||
-      !(sc->node_fraction >= 0 && sc->node_fraction <= 1) || !(sc->lr > 0))
-    return fail(SFSIM_ATMO_EINVAL, "steps >= 0, batch a positive multiple of 1024, lr > 0, node_fraction in [0, 1]");
+      !(sc->node_fraction >= 0 && sc->node_fraction <= 1) || !(sc->lr > 0) || !(sc->huber_delta >= 0))
+    return fail(SFSIM_ATMO_EINVAL,
+                "steps >= 0, batch a positive multiple of 1024, lr > 0, node_fraction in [0, 1], huber_delta >= 0");
   std::lock_guard<std::mutex> lock(g_mutex);
   int cur = 0;
   CUDA_TRY(cudaGetDevice(&cur));
@@ -1438,7 +1442,7 @@ int sfsim_atmo_surrogate_train(sfsim_atmo_context* ctx, const sfsim_atmo_surroga
     launch_gather_batch(n, sc->seed * 0x9E3779B97F4A7C15ull + (unsigned long long)t, sc->node_fraction, node_pool,
                         ctx->dims.n4(), direct_pool, sc->direct_samples, S.coords, S.target, st);
     if ((rc = surrogate_forward(S, n, true, st))) break;
-    if ((rc = surrogate_backward(S, n, st))) break;
+    if ((rc = surrogate_backward(S, n, sc->huber_delta, st))) break;
     surrogate_adam(S, lr, S.trained_steps + t + 1, st);
     if (cudaMemcpyAsync(hist + t, S.loss, sizeof(float), cudaMemcpyDeviceToDevice, st) != cudaSuccess)
       rc = fail(SFSIM_ATMO_ECUDA, "loss copy failed");
@@ -1481,10 +1485,10 @@ int sfsim_atmo_surrogate_gradients(sfsim_atmo_context* ctx, long long n, const f
   if (rc) return rc;
   Surrogate& S = *ctx->sur;
   cudaStream_t st = g_stream[ctx->dev];
-  CUDA_TRY(cudaMemcpyAsync(S.coords, coords, sizeof(float) * 4 * n, cudaMemcpyHostToDevice, st));
+  CUDA_TRY(cudaMemcpyAsync(S.coords, coords, sizeof(float) * kMlpCoords * n, cudaMemcpyHostToDevice, st));
   CUDA_TRY(cudaMemcpyAsync(S.target, targets, sizeof(float) * 3 * n, cudaMemcpyHostToDevice, st));
   if ((rc = surrogate_forward(S, n, true, st))) return rc;
-  if ((rc = surrogate_backward(S, n, st))) return rc;
+  if ((rc = surrogate_backward(S, n, 0.0f, st))) return rc;
   if (loss) CUDA_TRY(cudaMemcpyAsync(loss, S.loss, sizeof(float), cudaMemcpyDeviceToHost, st));
   if (grads) CUDA_TRY(cudaMemcpyAsync(grads, S.g, sizeof(float) * S.lay.total, cudaMemcpyDeviceToHost, st));
   CUDA_TRY(cudaStreamSynchronize(st));
@@ -1527,7 +1531,7 @@ int sfsim_atmo_query_surrogate(sfsim_atmo_context* ctx, long long n, const doubl
   int rc = 0, sms = 0;
   CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->dev));
   if (launch_surrogate_infer(q, n, x, v, l, S.wb, biases, S.w + S.lay.W[4], S.w + S.lay.b[4], kLogEps,
-                             fallback ? threshold : 0.0f, 1e-7f, out, mask, count, S.error, S.packed, sms, st))
+                             fallback ? threshold : 0.0f, out, mask, count, S.error, S.packed, sms, st))
     rc = fail(SFSIM_ATMO_ECUDA, "surrogate inference launch configuration failed");
   if (!rc && fallback) launch_query_direct(ctx->params, ctx->dims, ctx->jsum, n, x, v, l, out, st, mask);
   if (!rc && cudaGetLastError() != cudaSuccess) rc = fail(SFSIM_ATMO_ECUDA, "surrogate query launch failed");

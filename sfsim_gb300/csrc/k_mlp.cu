@@ -18,10 +18,10 @@ __global__ void k_features(long long n, const float* __restrict__ coords, __nv_b
   const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (t >= n * kMlpIn / 2) return;
   const long long i = t / (kMlpIn / 2);
-  const int f = (int)(t % (kMlpIn / 2));  // 0..63 = d * 16 + k
+  const int f = (int)(t % (kMlpIn / 2));  // d * 16 + k
   const int d = f >> 4, k = f & 15;
   float s, c;
-  sincospif(feature_frequency(k) * coords[i * 4 + d], &s, &c);
+  sincospif(feature_frequency(k) * coords[i * kMlpCoords + d], &s, &c);
   const __nv_bfloat16 bs = __float2bfloat16(s), bc = __float2bfloat16(c);
   F[i * kMlpIn + 2 * f] = bs;
   F[i * kMlpIn + 2 * f + 1] = bc;
@@ -31,39 +31,55 @@ __global__ void k_features(long long n, const float* __restrict__ coords, __nv_b
   }
 }
 
-// out[i][c] = sum_j H[i][j] W5[c][j] + b5[c]; one warp per row.
+// out[i][c] = sum_j H[i][j] W5[c][j] + b5[c], c < kMlpOut; one warp per row.
 __global__ void k_head_forward(long long n, const __nv_bfloat16* __restrict__ H, const float* __restrict__ W5,
                                const float* __restrict__ b5, float* __restrict__ out) {
   const long long row = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (row >= n) return;
-  float acc[3] = {0, 0, 0};
+  float acc[kMlpOut] = {};
   for (int j = lane; j < kMlpHidden; j += 32) {
     const float h = __bfloat162float(H[row * kMlpHidden + j]);
 #pragma unroll
-    for (int c = 0; c < 3; c++) acc[c] = fmaf(h, W5[c * kMlpHidden + j], acc[c]);
+    for (int c = 0; c < kMlpOut; c++) acc[c] = fmaf(h, W5[c * kMlpHidden + j], acc[c]);
   }
 #pragma unroll
-  for (int c = 0; c < 3; c++) {
+  for (int c = 0; c < kMlpOut; c++) {
     for (int o = 16; o > 0; o >>= 1) acc[c] += __shfl_xor_sync(0xffffffffu, acc[c], o);
-    if (lane == 0) out[row * 3 + c] = acc[c] + b5[c];
+    if (lane == 0) out[row * kMlpOut + c] = acc[c] + b5[c];
   }
 }
 
-// Mean squared error over rows and channels: dout = 2 (out - target) / (3 n),
-// loss += sum (out - target)^2 / (3 n).
+// Per row: e_c = out_c - target_c (c < 3), m = mean e_c^2, s = out_3.
+// dout_c = 2 e_c / (3 n), with e_c clamped to [-huber, huber] when huber > 0
+// (the Huber loss); dout_3 = var_weight (1 - m exp(-s)) / (2 n), the
+// gradient of the Gaussian negative log-likelihood (m exp(-s) + s) / 2 of the
+// squared error under the predicted variance exp(s), with m held fixed.
+// loss += m / n.
 __global__ void k_loss_grad(long long n, const float* __restrict__ out, const float* __restrict__ target,
-                            float* __restrict__ dout, float* __restrict__ loss) {
+                            float huber, float var_weight, float* __restrict__ dout, float* __restrict__ loss) {
   const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   float e2 = 0;
-  if (t < 3 * n) {
-    const float e = out[t] - target[t];
-    dout[t] = 2.0f * e / (3.0f * (float)n);
-    e2 = e * e / (3.0f * (float)n);
+  if (t < n) {
+    const float inv = 1.0f / (float)n;
+    float m = 0;
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+      const float e = out[t * kMlpOut + c] - target[t * 3 + c];
+      const float ge = huber > 0 ? fminf(fmaxf(e, -huber), huber) : e;
+      dout[t * kMlpOut + c] = 2.0f * ge * inv / 3.0f;
+      m += e * e;
+    }
+    m *= 1.0f / 3.0f;
+    const float s = fminf(fmaxf(out[t * kMlpOut + 3], -40.0f), 20.0f);
+    dout[t * kMlpOut + 3] = var_weight * 0.5f * (1.0f - m * __expf(-s)) * inv;
+    e2 = m * inv;
   }
   for (int o = 16; o > 0; o >>= 1) e2 += __shfl_xor_sync(0xffffffffu, e2, o);
   if ((threadIdx.x & 31) == 0 && e2 != 0.0f) atomicAdd(loss, e2);
 }
+
+static_assert(kMlpOut == 4, "the head kernels read rows of dout as float4");
 
 // Backward of the head: dZ4[i][j] = (sum_c dout[i][c] W5[c][j]) * dsilu4[i][j]
 // (BF16, also transposed), and dW5 += dout^T H4, db5 += sum dout.
@@ -71,39 +87,34 @@ __global__ void k_head_backward(long long n, const float* __restrict__ dout, con
                                 const float* __restrict__ W5, const float* __restrict__ dsilu,
                                 __nv_bfloat16* __restrict__ dZ, __nv_bfloat16* __restrict__ dZT,
                                 float* __restrict__ dW5, float* __restrict__ db5) {
-  __shared__ float sW[3 * kMlpHidden];
-  __shared__ float sdW[3 * kMlpHidden];
-  for (int t = threadIdx.x; t < 3 * kMlpHidden; t += blockDim.x) {
-    sW[t] = W5[t];
-    sdW[t] = 0;
-  }
+  __shared__ float sW[kMlpOut * kMlpHidden];
+  for (int t = threadIdx.x; t < kMlpOut * kMlpHidden; t += blockDim.x) sW[t] = W5[t];
   __syncthreads();
   // thread = hidden unit j; the block walks a range of rows
   const int j = threadIdx.x;  // blockDim.x == kMlpHidden
   const long long rows_per_block = (n + gridDim.x - 1) / gridDim.x;
   const long long r0 = blockIdx.x * rows_per_block, r1 = min(n, r0 + rows_per_block);
-  float gw[3] = {0, 0, 0}, gb[3] = {0, 0, 0};
+  float gw[kMlpOut] = {}, gb[kMlpOut] = {};
   for (long long i = r0; i < r1; i++) {
-    const float d0 = dout[i * 3], d1 = dout[i * 3 + 1], d2 = dout[i * 3 + 2];
+    const float4 d = *reinterpret_cast<const float4*>(dout + i * kMlpOut);
+    const float dd[kMlpOut] = {d.x, d.y, d.z, d.w};
     const float h = __bfloat162float(H[i * kMlpHidden + j]);
-    gw[0] = fmaf(d0, h, gw[0]);
-    gw[1] = fmaf(d1, h, gw[1]);
-    gw[2] = fmaf(d2, h, gw[2]);
-    if (j == 0) {
-      gb[0] += d0;
-      gb[1] += d1;
-      gb[2] += d2;
+    float dh = 0;
+#pragma unroll
+    for (int c = 0; c < kMlpOut; c++) {
+      gw[c] = fmaf(dd[c], h, gw[c]);
+      gb[c] += dd[c];
+      dh = fmaf(dd[c], sW[c * kMlpHidden + j], dh);
     }
-    const float dh = fmaf(d0, sW[j], fmaf(d1, sW[kMlpHidden + j], d2 * sW[2 * kMlpHidden + j]));
     const __nv_bfloat16 dz = __float2bfloat16(dh * dsilu[i * kMlpHidden + j]);
     dZ[i * kMlpHidden + j] = dz;
     dZT[(long long)j * n + i] = dz;
   }
 #pragma unroll
-  for (int c = 0; c < 3; c++) atomicAdd(dW5 + c * kMlpHidden + j, gw[c]);
+  for (int c = 0; c < kMlpOut; c++) atomicAdd(dW5 + c * kMlpHidden + j, gw[c]);
   if (j == 0) {
 #pragma unroll
-    for (int c = 0; c < 3; c++) atomicAdd(db5 + c, gb[c]);
+    for (int c = 0; c < kMlpOut; c++) atomicAdd(db5 + c, gb[c]);
   }
 }
 
@@ -163,7 +174,8 @@ __device__ __forceinline__ unsigned long long mix64(unsigned long long z) {
 }
 
 // Batch of n rows: a fraction `node_frac` drawn from pool A (na samples),
-// the rest from pool B (nb samples); each sample is 4 coords + 3 targets.
+// the rest from pool B (nb samples); each sample is kMlpCoords coordinates and
+// 3 targets.
 __global__ void k_gather_batch(long long n, unsigned long long seed, float node_frac, const float* __restrict__ poolA,
                                long long na, const float* __restrict__ poolB, long long nb, float* __restrict__ coords,
                                float* __restrict__ target) {
@@ -171,12 +183,12 @@ __global__ void k_gather_batch(long long n, unsigned long long seed, float node_
   if (i >= n) return;
   const unsigned long long h = mix64(seed ^ (unsigned long long)i * 0x2545F4914F6CDD1Dull);
   const bool fromA = nb == 0 || ((h >> 40) & 0xFFFFFF) < (unsigned long long)(node_frac * 16777216.0f);
-  const float* src = fromA ? poolA + 7 * (long long)(mix64(h) % (unsigned long long)na)
-                           : poolB + 7 * (long long)(mix64(h + 1) % (unsigned long long)nb);
+  const float* src = fromA ? poolA + kPoolRow * (long long)(mix64(h) % (unsigned long long)na)
+                           : poolB + kPoolRow * (long long)(mix64(h + 1) % (unsigned long long)nb);
 #pragma unroll
-  for (int c = 0; c < 4; c++) coords[i * 4 + c] = src[c];
+  for (int c = 0; c < kMlpCoords; c++) coords[i * kMlpCoords + c] = src[c];
 #pragma unroll
-  for (int c = 0; c < 3; c++) target[i * 3 + c] = src[4 + c];
+  for (int c = 0; c < 3; c++) target[i * 3 + c] = src[kMlpCoords + c];
 }
 
 static inline unsigned grid_for(long long n, int blk) { return (unsigned)((n + blk - 1) / blk); }
@@ -188,8 +200,9 @@ void launch_head_forward(long long n, const __nv_bfloat16* H, const float* W5, c
                          cudaStream_t st) {
   k_head_forward<<<grid_for(n * 32, 256), 256, 0, st>>>(n, H, W5, b5, out);
 }
-void launch_loss_grad(long long n, const float* out, const float* target, float* dout, float* loss, cudaStream_t st) {
-  k_loss_grad<<<grid_for(3 * n, 256), 256, 0, st>>>(n, out, target, dout, loss);
+void launch_loss_grad(long long n, const float* out, const float* target, float huber, float var_weight, float* dout,
+                      float* loss, cudaStream_t st) {
+  k_loss_grad<<<grid_for(n, 256), 256, 0, st>>>(n, out, target, huber, var_weight, dout, loss);
 }
 void launch_head_backward(long long n, const float* dout, const __nv_bfloat16* H, const float* W5,
                           const float* dsilu, __nv_bfloat16* dZ, __nv_bfloat16* dZT, float* dW5, float* db5,

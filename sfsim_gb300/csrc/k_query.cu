@@ -270,10 +270,24 @@ void launch_query_table(const QueryTables& q, int kind, long long n, const float
   k_query_table<<<(unsigned)((n + blk - 1) / blk), blk, 0, st>>>(e, kind, n, a, b, l, out);
 }
 
-// Table coordinates in [0, 1] of (x, v, l) as the in-scatter lookup forms them
-// (core/ray-scatter-forward.glsl order reversed to height, elevation, sun
-// elevation, sun heading), with the table half chosen by the horizon test;
-// the table value there (S + M phase) as a by-product when `table` is set.
+// The surrogate's coordinates of (p, d, l): the table coordinates as the
+// in-scatter lookup forms them (core/ray-scatter-forward.glsl order reversed
+// to height, elevation, sun elevation, sun heading) with the table half chosen
+// by the horizon test, then (1 + sin of the sun elevation) / 2 and the half
+// (0 upper, 1 lower).  idx receives the lookup's indices.
+__device__ __forceinline__ void network_coords(const GlslEnv& e, f3 p, f3 d, f3 l, float* u, float* idx) {
+  const bool above = is_above_horizon_g(e, p, d);
+  ray_scatter_forward_g(e, p, d, l, above, idx);
+  u[0] = idx[3];
+  u[1] = idx[2];
+  u[2] = idx[1];
+  u[3] = idx[0];
+  u[4] = fminf(fmaxf(0.5f * (1.0f + fdot(p, l) / sqrtf(fdot(p, p))), 0.0f), 1.0f);
+  u[5] = above ? 0.0f : 1.0f;
+}
+
+// The surrogate's coordinates of (x, v, l); the table value there (S + M
+// phase) as a by-product when `table` is set.
 __global__ void k_query_coords(GlslEnv e, long long n, const double* X, const double* V, const double* L,
                                float* coords, float* table) {
   const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
@@ -281,12 +295,10 @@ __global__ void k_query_coords(GlslEnv e, long long n, const double* X, const do
   const f3 p = F3((float)X[3 * t], (float)X[3 * t + 1], (float)X[3 * t + 2]);
   const f3 d = F3((float)V[3 * t], (float)V[3 * t + 1], (float)V[3 * t + 2]);
   const f3 l = F3((float)L[3 * t], (float)L[3 * t + 1], (float)L[3 * t + 2]);
-  float idx[4];
-  ray_scatter_forward_g(e, p, d, l, is_above_horizon_g(e, p, d), idx);
-  coords[4 * t] = idx[3];
-  coords[4 * t + 1] = idx[2];
-  coords[4 * t + 2] = idx[1];
-  coords[4 * t + 3] = idx[0];
+  float idx[4], u[kMlpCoords];
+  network_coords(e, p, d, l, u, idx);
+#pragma unroll
+  for (int c = 0; c < kMlpCoords; c++) coords[kMlpCoords * t + c] = u[c];
   if (table) {
     const f3 r = in_scatter_g(e, idx, fdot(d, l));
     table[3 * t] = r.x;
@@ -348,71 +360,42 @@ void launch_random_queries(long long n, unsigned long long seed, double R, doubl
   k_random_queries<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(n, seed, R, H, x, v, l);
 }
 
-// Training pool of the table nodes: coordinates node / (size - 1) and the
-// log of the stored in-scatter S + M phase(mie g, v.l) (.scatter layout).
-__global__ void k_node_pool(BuildDims d, const float* S, const float* M, const CellGeom<float>* geom, float mie_g,
-                            float eps, float* pool) {
+// Training pool of the table nodes: coordinates node / (size - 1) with a zero
+// correction, since the lookup reproduces the stored value at a node.  The
+// sun elevation inverts core/sun-elevation-to-index.glsl.
+__global__ void k_node_pool(BuildDims d, float* pool) {
   const long long node = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (node >= d.n4()) return;
-  const int a = (int)(node % d.n3);
-  const int k = (int)((node / d.n3) % d.n2);
-  const int j = (int)((node / ((long long)d.n3 * d.n2)) % d.n1);
-  const int i = (int)(node / ((long long)d.n3 * d.n2 * d.n1));
-  const long long dst = ((long long)i * d.n2 + k) * ((long long)d.n1 * d.n3) + (long long)j * d.n3 + a;
-  const float ph = phase_cs<float>(mie_g, geom[node].mu);
-  float* o = pool + 7 * node;
-  o[0] = (float)i / (d.n0 - 1);
-  o[1] = (float)j / (d.n1 - 1);
-  o[2] = (float)k / (d.n2 - 1);
-  o[3] = (float)a / (d.n3 - 1);
-  for (int c = 0; c < 3; c++) o[4 + c] = logf(fmaxf(S[3 * dst + c] + M[3 * dst + c] * ph, 0.0f) + eps);
+  float* o = pool + kPoolRow * node;
+  o[0] = (float)(node / ((long long)d.n3 * d.n2 * d.n1)) / (d.n0 - 1);
+  o[1] = (float)((node / ((long long)d.n3 * d.n2)) % d.n1) / (d.n1 - 1);
+  o[2] = (float)((node / d.n3) % d.n2) / (d.n2 - 1);
+  o[3] = (float)(node % d.n3) / (d.n3 - 1);
+  const float sin_el = -(logf(1.0f - o[2] * (1.0f - expf(-3.6f))) + 0.6f) / 3.0f;
+  o[4] = fminf(fmaxf(0.5f * (1.0f + sin_el), 0.0f), 1.0f);
+  o[5] = o[1] > 0.5f ? 1.0f : 0.0f;
+  for (int c = 0; c < 3; c++) o[kMlpCoords + c] = 0.0f;
 }
 
-void launch_node_pool(const BuildDims& d, const float* S, const float* M, const CellGeom<float>* geom, float mie_g,
-                      float eps, float* pool, cudaStream_t st) {
-  k_node_pool<<<(unsigned)((d.n4() + 255) / 256), 256, 0, st>>>(d, S, M, geom, mie_g, eps, pool);
+void launch_node_pool(const BuildDims& d, float* pool, cudaStream_t st) {
+  k_node_pool<<<(unsigned)((d.n4() + 255) / 256), 256, 0, st>>>(d, pool);
 }
 
-// pool rows (coords, log(value + eps)) from coordinates and values
-__global__ void k_make_pool(long long n, const float* coords, const float* values, float eps, float* pool) {
+// pool rows (coords, log(value + eps) - log(table + eps)) from coordinates,
+// directly integrated values and the table lookups at the same queries
+__global__ void k_make_pool(long long n, const float* coords, const float* values, const float* table, float eps,
+                            float* pool) {
   const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (t >= n) return;
-  for (int c = 0; c < 4; c++) pool[7 * t + c] = coords[4 * t + c];
-  for (int c = 0; c < 3; c++) pool[7 * t + 4 + c] = logf(fmaxf(values[3 * t + c], 0.0f) + eps);
+  for (int c = 0; c < kMlpCoords; c++) pool[kPoolRow * t + c] = coords[kMlpCoords * t + c];
+  for (int c = 0; c < 3; c++)
+    pool[kPoolRow * t + kMlpCoords + c] =
+        logf(fmaxf(values[3 * t + c], 0.0f) + eps) - logf(fmaxf(table[3 * t + c], 0.0f) + eps);
 }
 
-void launch_make_pool(long long n, const float* coords, const float* values, float eps, float* pool,
-                      cudaStream_t st) {
-  k_make_pool<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(n, coords, values, eps, pool);
-}
-
-// out = exp(y) - eps; mask[i] = 1 where it differs from the table value by
-// more than `thr` relative (floor `floor_abs`), when `table` is given.
-__global__ void k_surrogate_finish(long long n, const float* y, float eps, const float* table, float thr,
-                                   float floor_abs, float* out, unsigned char* mask, unsigned long long* count) {
-  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  bool flag = false;
-  if (t < n) {
-    for (int c = 0; c < 3; c++) {
-      const float v = fmaxf(expf(y[3 * t + c]) - eps, 0.0f);
-      out[3 * t + c] = v;
-      if (table) {
-        const float r = table[3 * t + c];
-        if (fabsf(v - r) > thr * fmaxf(fabsf(r), floor_abs)) flag = true;
-      }
-    }
-    if (mask) mask[t] = flag ? 1 : 0;
-  }
-  if (count) {
-    const unsigned b = __ballot_sync(0xffffffffu, flag);
-    if ((threadIdx.x & 31) == 0 && b) atomicAdd(count, (unsigned long long)__popc(b));
-  }
-}
-
-void launch_surrogate_finish(long long n, const float* y, float eps, const float* table, float thr, float floor_abs,
-                             float* out, unsigned char* mask, unsigned long long* count, cudaStream_t st) {
-  k_surrogate_finish<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(n, y, eps, table, thr, floor_abs, out, mask,
-                                                                   count);
+void launch_make_pool(long long n, const float* coords, const float* values, const float* table, float eps,
+                      float* pool, cudaStream_t st) {
+  k_make_pool<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(n, coords, values, table, eps, pool);
 }
 
 // ---------------------------------------------------------------------------
@@ -558,10 +541,12 @@ void launch_query_direct(const AtmoParams* params, const BuildDims& d, const Vec
 // A persistent CTA per SM evaluates groups of 256 queries (two 128-row tiles
 // A0, A1 of BF16 activations, K-major core-matrix layout, 64 KB each).  Warps
 // 0-7 own one query each per thread (warps 0-3 tile 0, 4-7 tile 1): they form
-// the coordinates and Fourier features, and after every layer read their row
-// of the FP32 accumulator from tensor memory (tcgen05.ld), add the bias, apply
-// SiLU and write the BF16 result back as the next layer's input; the last
-// layer folds the 256 -> 3 head in.  Warp 8 is the producer: one thread
+// the coordinates, the table lookup and the Fourier features, and after every
+// layer read their row of the FP32 accumulator from tensor memory
+// (tcgen05.ld), add the bias, apply SiLU and write the BF16 result back as the
+// next layer's input; the last layer folds the 256 -> 4 head in.  The value is
+// (table + eps) exp(r) - eps, and a query whose predicted squared error exp(s)
+// exceeds threshold^2 is flagged for the direct quadrature.  Warp 8 is the producer: one thread
 // streams the 28 weight chunks of a group (256 rows x 32 K, 16 KB each,
 // pre-packed in the tensor cores' layout) through a five-stage shared-memory
 // ring with bulk TMA copies, and issues the tcgen05.mma of both tiles on each
@@ -584,7 +569,7 @@ constexpr int kInferWaitLimit = 1 << 22;
 constexpr int kInferSmemRing = 2 * kInferTileBytes;
 constexpr int kInferSmemBias = kInferSmemRing + kInferStages * kInferChunkBytes;
 constexpr int kInferSmemHead = kInferSmemBias + 4 * kMlpHidden * 4;
-constexpr int kInferSmemBar = kInferSmemHead + 4 * kMlpHidden * 4;   // W5 (3 x 256) and b5
+constexpr int kInferSmemBar = kInferSmemHead + (kMlpOut * kMlpHidden + 4) * 4;  // W5 (4 x 256) and b5
 constexpr int kInferSmem = kInferSmemBar + (2 * kInferStages + 2) * 8 + 16;
 
 size_t infer_packed_bytes() { return (size_t)kInferChunks * kInferChunkBytes; }
@@ -621,10 +606,11 @@ struct InferArgs {
   const double *X, *V, *L;
   const unsigned char* packed;  // kInferChunks weight chunks
   const float* b[4];
-  const float* W5;              // [3][256]
+  const float* W5;              // [kMlpOut][256]
   const float* b5;
   float* out;
-  float threshold, floor_abs, eps;
+  float log_var_limit;          // flag queries with s above this (2 log threshold), or +inf
+  float eps;
   unsigned char* mask;
   unsigned long long* count;
   int* error;
@@ -724,7 +710,7 @@ __device__ void infer_producer(const InferArgs& g, long long my_groups, unsigned
 __global__ void __launch_bounds__(kInferThreads, 1) k_surrogate_infer(InferArgs g) {
   extern __shared__ __align__(1024) unsigned char smem[];
   float* s_bias = reinterpret_cast<float*>(smem + kInferSmemBias);  // 0.5 b_l, 4 x 256
-  float* s_w5 = reinterpret_cast<float*>(smem + kInferSmemHead);    // W5 [3][256], then b5
+  float* s_w5 = reinterpret_cast<float*>(smem + kInferSmemHead);    // W5 [4][256], then b5
   uint64_t* full = reinterpret_cast<uint64_t*>(smem + kInferSmemBar);
   uint64_t* empty = full + kInferStages;
   uint64_t* acc_bar = empty + kInferStages;
@@ -736,8 +722,8 @@ __global__ void __launch_bounds__(kInferThreads, 1) k_surrogate_infer(InferArgs 
   const long long my_groups = blockIdx.x < ngroups ? (ngroups - 1 - blockIdx.x) / gridDim.x + 1 : 0;
 
   for (int i = t; i < 4 * kMlpHidden; i += kInferThreads) s_bias[i] = 0.5f * g.b[i / kMlpHidden][i % kMlpHidden];
-  for (int i = t; i < 3 * kMlpHidden; i += kInferThreads) s_w5[i] = g.W5[i];
-  if (t < 3) s_w5[3 * kMlpHidden + t] = g.b5[t];
+  for (int i = t; i < kMlpOut * kMlpHidden; i += kInferThreads) s_w5[i] = g.W5[i];
+  if (t < kMlpOut) s_w5[kMlpOut * kMlpHidden + t] = g.b5[t];
   if (warp == 0) tc::tmem_alloc(tmem_slot, 2 * kMlpHidden);
   if (t == 0) {
     for (int s = 0; s < kInferStages; s++) {
@@ -770,17 +756,16 @@ __global__ void __launch_bounds__(kInferThreads, 1) k_surrogate_infer(InferArgs 
       const f3 p = F3((float)g.X[3 * qq], (float)g.X[3 * qq + 1], (float)g.X[3 * qq + 2]);
       const f3 d = F3((float)g.V[3 * qq], (float)g.V[3 * qq + 1], (float)g.V[3 * qq + 2]);
       const f3 l = F3((float)g.L[3 * qq], (float)g.L[3 * qq + 1], (float)g.L[3 * qq + 2]);
-      float idx[4];
-      ray_scatter_forward_g(g.env, p, d, l, is_above_horizon_g(g.env, p, d), idx);
-      f3 table = F3(0, 0, 0);
-      if (g.threshold > 0) table = in_scatter_g(g.env, idx, fdot(d, l));
-      // coordinates (height, elevation, sun elevation, heading) = idx reversed
+      float idx[4], u[kMlpCoords];
+      network_coords(g.env, p, d, l, u, idx);
 #pragma unroll
-      for (int dd = 0; dd < 4; dd++) write_features(idx[3 - dd], A, row, 32 * dd);
+      for (int dd = 0; dd < kMlpCoords; dd++) write_features(u[dd], A, row, 32 * dd);
       tc::fence_async_smem();
       tc::fence_before();
       tc::mbar_arrive(act_bar);
-      float head[3] = {0, 0, 0};
+      // the table lookup overlaps the first layer's MMAs
+      const f3 table = in_scatter_g(g.env, idx, fdot(d, l));
+      float head[kMlpOut] = {};
       for (int layer = 0; layer < 4; layer++) {
         bool done = tc::mbar_wait(acc_bar, acc_phase & 1, kInferWaitLimit);
         acc_phase++;
@@ -815,7 +800,7 @@ __global__ void __launch_bounds__(kInferThreads, 1) k_surrogate_infer(InferArgs 
                   make_uint4(w[0], w[1], w[2], w[3]);
             } else {
 #pragma unroll
-              for (int cc = 0; cc < 3; cc++) {
+              for (int cc = 0; cc < kMlpOut; cc++) {
                 const float4 w0 = *reinterpret_cast<const float4*>(s_w5 + cc * kMlpHidden + n0 + 8 * i8);
                 const float4 w1 = *reinterpret_cast<const float4*>(s_w5 + cc * kMlpHidden + n0 + 8 * i8 + 4);
                 head[cc] = fmaf(hv[0], w0.x, fmaf(hv[1], w0.y, fmaf(hv[2], w0.z, fmaf(hv[3], w0.w, head[cc]))));
@@ -836,11 +821,10 @@ __global__ void __launch_bounds__(kInferThreads, 1) k_surrogate_infer(InferArgs 
         const float tv[3] = {table.x, table.y, table.z};
 #pragma unroll
         for (int cc = 0; cc < 3; cc++) {
-          const float y = head[cc] + s_w5[3 * kMlpHidden + cc];
-          const float val = fmaxf(expf(y) - g.eps, 0.0f);
-          g.out[3 * q + cc] = val;
-          if (g.threshold > 0 && fabsf(val - tv[cc]) > g.threshold * fmaxf(fabsf(tv[cc]), g.floor_abs)) flag = true;
+          const float r = head[cc] + s_w5[kMlpOut * kMlpHidden + cc];
+          g.out[3 * q + cc] = fmaxf((fmaxf(tv[cc], 0.0f) + g.eps) * expf(r) - g.eps, 0.0f);
         }
+        flag = head[3] + s_w5[kMlpOut * kMlpHidden + 3] > g.log_var_limit;
         if (g.mask) g.mask[q] = flag ? 1 : 0;
       }
       if (g.count) {
@@ -860,7 +844,7 @@ __global__ void __launch_bounds__(kInferThreads, 1) k_surrogate_infer(InferArgs 
 
 int launch_surrogate_infer(const QueryTables& qt, long long n, const double* x, const double* v, const double* l,
                            const __nv_bfloat16* const* W, const float* const* b, const float* W5, const float* b5,
-                           float eps, float threshold, float floor_abs, float* out, unsigned char* mask,
+                           float eps, float threshold, float* out, unsigned char* mask,
                            unsigned long long* count, int* error, unsigned char* packed, int num_sms,
                            cudaStream_t st) {
   constexpr int nthreads = kMlpHidden * (kMlpIn / 8) + 3 * kMlpHidden * (kMlpHidden / 8);
@@ -876,8 +860,7 @@ int launch_surrogate_infer(const QueryTables& qt, long long n, const double* x, 
   g.W5 = W5;
   g.b5 = b5;
   g.out = out;
-  g.threshold = threshold;
-  g.floor_abs = floor_abs;
+  g.log_var_limit = threshold > 0 ? 2.0f * logf(threshold) : INFINITY;
   g.eps = eps;
   g.mask = mask;
   g.count = count;

@@ -102,26 +102,24 @@ void launch_query_direct(const AtmoParams* params, const BuildDims& d, const Vec
                          const double* x, const double* v, const double* l, float* out, cudaStream_t st,
                          const unsigned char* mask = nullptr);
 
-// Table coordinates in [0, 1] (height, elevation, sun elevation, heading) of
-// (x, v, l) as the in-scatter lookup forms them; the lookup's value too when
-// `table` is non-NULL.
+// The surrogate's kMlpCoords coordinates of (x, v, l), the first four the
+// table coordinates as the in-scatter lookup forms them; the lookup's value
+// too when `table` is non-NULL.
 void launch_query_coords(const QueryTables& q, long long n, const double* x, const double* v, const double* l,
                          float* coords, float* table, cudaStream_t st);
 void launch_random_queries(long long n, unsigned long long seed, double R, double H, double* x, double* v, double* l,
                            cudaStream_t st);
-void launch_node_pool(const BuildDims& d, const float* S, const float* M, const CellGeom<float>* geom, float mie_g,
-                      float eps, float* pool, cudaStream_t st);
-void launch_make_pool(long long n, const float* coords, const float* values, float eps, float* pool, cudaStream_t st);
+void launch_node_pool(const BuildDims& d, float* pool, cudaStream_t st);
+void launch_make_pool(long long n, const float* coords, const float* values, const float* table, float eps,
+                      float* pool, cudaStream_t st);
 // Fused tensor-core inference of the surrogate for n queries; see k_query.cu.
 int launch_surrogate_infer(const QueryTables& qt, long long n, const double* x, const double* v, const double* l,
                            const __nv_bfloat16* const* W, const float* const* b, const float* W5, const float* b5,
-                           float eps, float threshold, float floor_abs, float* out, unsigned char* mask,
+                           float eps, float threshold, float* out, unsigned char* mask,
                            unsigned long long* count, int* error, unsigned char* packed, int num_sms,
                            cudaStream_t st);
 // Bytes of the packed weight chunks the inference kernel streams.
 size_t infer_packed_bytes();
-void launch_surrogate_finish(long long n, const float* y, float eps, const float* table, float thr, float floor_abs,
-                             float* out, unsigned char* mask, unsigned long long* count, cudaStream_t st);
 
 // jsum = (first ? 0 : jsum) + J, converted to float.
 template <class Real>
@@ -158,10 +156,18 @@ struct GemmArgs {
 
 int launch_gemm_tn(const GemmArgs& g, int splits, cudaStream_t st);
 
-// ---- surrogate MLP: 4 coordinates -> 128 Fourier features -> 4 x 256 SiLU -> 3 ----
-constexpr int kMlpIn = 128;
+// ---- surrogate MLP: 6 coordinates -> 192 Fourier features -> 4 x 256 SiLU -> 4 ----
+// Coordinates in [0, 1]: the four table coordinates (height, elevation, sun
+// elevation, sun heading), the sun elevation (1 + sin) / 2 without the
+// table's clamp at sin = -0.2, and 0 / 1 for the upper / lower table half.
+// Outputs: r_c (c < 3), the correction log(value_c + eps) - log(table_c + eps)
+// to the table lookup, and s, the log of the expected squared error of r.
+constexpr int kMlpCoords = 6;
+constexpr int kMlpIn = 32 * kMlpCoords;
+constexpr int kPoolRow = kMlpCoords + 3;  // floats per training sample: coordinates, corrections
 constexpr int kMlpHidden = 256;
 constexpr int kMlpLayers = 4;
+constexpr int kMlpOut = 4;
 // Feature frequencies f_k = 2^(k/2), k = 0..15: powers of two times 1 or the
 // float nearest sqrt(2), so that doubling the angle steps k by two exactly.
 constexpr float kFeatureSqrt2 = 1.41421356237309505f;
@@ -172,7 +178,12 @@ __host__ __device__ __forceinline__ float feature_frequency(int k) {
 void launch_features(long long n, const float* coords, __nv_bfloat16* F, __nv_bfloat16* FT, cudaStream_t st);
 void launch_head_forward(long long n, const __nv_bfloat16* H, const float* W5, const float* b5, float* out,
                          cudaStream_t st);
-void launch_loss_grad(long long n, const float* out, const float* target, float* dout, float* loss, cudaStream_t st);
+// Loss: mean squared error of r (Huber with threshold `huber` when > 0) plus,
+// weighted by `var_weight` in the gradients, the Gaussian negative
+// log-likelihood of s given the squared error (which does not reach r).  The
+// loss value is the mean squared error alone.
+void launch_loss_grad(long long n, const float* out, const float* target, float huber, float var_weight, float* dout,
+                      float* loss, cudaStream_t st);
 void launch_head_backward(long long n, const float* dout, const __nv_bfloat16* H, const float* W5,
                           const float* dsilu, __nv_bfloat16* dZ, __nv_bfloat16* dZT, float* dW5, float* db5,
                           cudaStream_t st);

@@ -87,11 +87,14 @@ class Context:
         return out
 
     # -- surrogate -------------------------------------------------------------
-    def train_surrogate(self, steps=2000, batch=65536, direct_samples=1 << 20, node_fraction=0.75, lr=1e-3,
-                        seed=1):
-        """Trains the surrogate MLP on the GPU; returns the per-step losses (numpy)."""
+    def train_surrogate(self, steps=2000, batch=65536, direct_samples=1 << 20, node_fraction=0.0, lr=1e-3,
+                        seed=1, huber_delta=0.0):
+        """Trains the surrogate MLP on the GPU against `direct_samples` random
+        queries integrated by direct quadrature (node_fraction of each batch
+        drawn from the table nodes with a zero correction instead); returns
+        the per-step mean squared errors of the log-space correction (numpy)."""
         import numpy as np
-        c = _lib.SurrogateConfig(steps, batch, direct_samples, node_fraction, lr, seed)
+        c = _lib.SurrogateConfig(steps, batch, direct_samples, node_fraction, lr, seed, huber_delta)
         hist = np.zeros(max(steps, 1), np.float32)
         _lib.check(self._L.sfsim_atmo_surrogate_train(self._ptr, ctypes.byref(c), hist.ctypes.data), "train")
         return hist[:steps]
@@ -123,7 +126,9 @@ class Context:
         return float(loss[0]), grads
 
     def surrogate(self, x, v, l, threshold=0.0, out=None):
-        """Rendered in-scatter from the surrogate; returns (out, number of points recomputed directly)."""
+        """Rendered in-scatter from the surrogate-corrected table lookup; with
+        threshold > 0 the points whose predicted relative error exceeds it are
+        recomputed by direct quadrature.  Returns (out, number recomputed)."""
         import torch
         x = x.contiguous().double()
         v = v.contiguous().double()
@@ -137,12 +142,13 @@ class Context:
         return out, nf.value
 
     def coords(self, x, v, l):
-        """Table coordinates [n, 4] in [0, 1] of the queries (height, elevation, sun elevation, heading)."""
+        """The surrogate's coordinates [n, 6] in [0, 1] of the queries: the table coordinates (height,
+        elevation, sun elevation, heading), the unclamped sun elevation and the table half."""
         import torch
         x = x.contiguous().double()
         v = v.contiguous().double()
         l = l.contiguous().double()
-        out = torch.empty((x.shape[0], 4), dtype=torch.float32, device="cuda")
+        out = torch.empty((x.shape[0], 6), dtype=torch.float32, device="cuda")
         _lib.check(self._L.sfsim_atmo_query_coords(self._ptr, x.shape[0], x.data_ptr(), v.data_ptr(), l.data_ptr(),
                                                    out.data_ptr(), torch.cuda.current_stream().cuda_stream),
                    "query_coords")

@@ -5,8 +5,11 @@ weight copies), so that its gradients check the GPU's forward and backward
 GEMMs."""
 import numpy as np
 
-N_IN, N_HID = 128, 256
-SHAPES = [(N_HID, N_IN), (N_HID, N_HID), (N_HID, N_HID), (N_HID, N_HID), (3, N_HID)]
+N_COORDS = 6
+N_IN, N_HID = 32 * N_COORDS, 256
+N_OUT = 4  # three log-space corrections to the table lookup and a log variance
+SHAPES = [(N_HID, N_IN), (N_HID, N_HID), (N_HID, N_HID), (N_HID, N_HID), (N_OUT, N_HID)]
+VAR_WEIGHT = 0.01
 
 
 def bf16(x):
@@ -30,7 +33,7 @@ def unpack(params):
 
 def features(coords):
     k = np.arange(16)
-    f = 2.0 ** (0.5 * k)
+    f = np.where(k % 2 == 1, np.float32(np.sqrt(2.0)), 1.0) * 2.0 ** (k // 2)
     ang = np.pi * coords[:, :, None].astype(np.float64) * f[None, None, :]  # [n, 4, 16]
     F = np.stack([np.sin(ang), np.cos(ang)], axis=-1).reshape(coords.shape[0], N_IN)
     return F
@@ -45,7 +48,10 @@ def dsilu(z):
     return s * (1 + z * (1 - s))
 
 
-def loss_and_grads(params, coords, targets):
+def loss_and_grads(params, coords, targets, var_weight=VAR_WEIGHT):
+    """Mean squared error of the corrections (the reported loss) with the
+    Gaussian negative log-likelihood of the squared error under the predicted
+    variance exp(s) added to the gradients, weighted by var_weight."""
     layers = unpack(params)
     n = coords.shape[0]
     H = [bf16(features(coords))]
@@ -57,9 +63,11 @@ def loss_and_grads(params, coords, targets):
         H.append(bf16(silu(z)))
     W5, b5 = layers[4]
     out = H[4] @ W5.T + b5
-    e = out - targets
-    loss = np.mean(e * e)
-    dout = 2 * e / (3 * n)
+    e = out[:, :3] - targets
+    m = np.mean(e * e, axis=1)
+    loss = np.mean(m)
+    s = np.clip(out[:, 3], -40, 20)
+    dout = np.concatenate([2 * e / (3 * n), (var_weight * 0.5 * (1 - m * np.exp(-s)) / n)[:, None]], axis=1)
     grads = []
     dW5 = dout.T @ H[4]
     db5 = dout.sum(axis=0)
@@ -80,7 +88,8 @@ def loss_and_grads(params, coords, targets):
 
 
 def forward(params, coords):
-    """Network output (log-RGB) for coords [n][4], with the GPU's BF16 roundings."""
+    """Network outputs [n][4] (three corrections, log variance) for coords
+    [n][4], with the GPU's BF16 roundings."""
     layers = unpack(params)
     H = bf16(features(coords))
     for l in range(4):
