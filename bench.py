@@ -49,6 +49,9 @@ def parse():
                    help="only run --builds builds of a named configuration (small_fp64, production, "
                         "reference_production, shader_test), for profilers")
     p.add_argument("--builds", type=int, default=2)
+    p.add_argument("--profile-surrogate", type=int, default=0, metavar="N",
+                   help="only train the surrogate 4 steps on the production tables and run --builds batches of "
+                        "N surrogate queries, for profilers")
     p.add_argument("--no-extras", dest="extras", action="store_false",
                    help="skip the parameter-sweep and query/surrogate measurements")
     return p.parse_args()
@@ -334,7 +337,7 @@ def query_error_stats(a, ref):
             "frac_le_1e-3": float((e <= 1e-3).double().mean()), "frac_le_1e-2": float((e <= 1e-2).double().mean())}
 
 
-def run_queries(C, steps=3000, batch=65536, direct_samples=1 << 24, lr=3e-3, huber_delta=0.0,
+def run_queries(C, steps=3000, batch=65536, direct_samples=1 << 25, lr=3e-3, huber_delta=0.02,
                 thresholds=(3e-2, 1e-2, 3e-3, 1e-3)):
     """2^24 random in-scatter queries (height uniform 0-100 km, view and sun
     uniform on the sphere) on the production tables: table lookup, direct
@@ -486,9 +489,31 @@ def run_profile(args):
     print(json.dumps({"profile": args.profile, "builds": args.builds, "config": cfg.describe()}))
 
 
+def run_profile_surrogate(args):
+    """Four training steps (batch 65536) and --builds batches of N fused
+    surrogate queries on the production tables (for ncu)."""
+    import torch
+
+    from sfsim_gb300 import config as C
+    from sfsim_gb300.query import Context
+    torch.cuda.set_device(0)
+    cfg = C.production()
+    with Context(cfg) as ctx:
+        ctx.train_surrogate(steps=4, batch=65536, direct_samples=1 << 16, lr=1e-3, seed=1)
+        n = args.profile_surrogate
+        x, v, l = _random_queries(n, cfg.radius, cfg.height, 2)
+        out = torch.empty((n, 3), dtype=torch.float32, device="cuda")
+        for _ in range(args.builds):
+            ctx.surrogate(x, v, l, out=out)
+        torch.cuda.synchronize()
+    print(json.dumps({"profile_surrogate": n, "builds": args.builds}))
+
+
 def main():
     args = parse()
-    if args.profile:
+    if args.profile_surrogate:
+        run_profile_surrogate(args)
+    elif args.profile:
         run_profile(args)
     elif args.impl == "reference":
         run_reference(args)

@@ -903,6 +903,7 @@ int context_build(sfsim_atmo_context* c) {
 
 constexpr float kLogEps = 1e-7f;     // corrections are log(value + kLogEps) - log(table + kLogEps)
 constexpr float kVarWeight = 0.01f;  // weight of the variance output's gradient in the shared layers
+constexpr long long kQueryChunk = 1 << 22;  // surrogate queries per lookup + inference pass
 
 // parameter offsets (floats) in the concatenated FP32 vector
 struct MlpLayout {
@@ -934,6 +935,8 @@ struct Surrogate {
   __nv_bfloat16 *F = nullptr, *FT = nullptr, *H[4] = {}, *HT[4] = {}, *dZ[4] = {}, *dZT[4] = {};
   float* dsilu[4] = {};
   unsigned char* packed = nullptr;  // weight chunks of the fused inference kernel
+  float* qbuf = nullptr;            // coordinates and table values of one chunk of queries
+  long long qcap = 0;               // queries qbuf holds
   int* error = nullptr;
   int trained_steps = 0;
   std::vector<void*> allocs;
@@ -952,6 +955,9 @@ struct Surrogate {
   void free_all() {
     for (void* p : allocs) cudaFree(p);
     allocs.clear();
+    if (qbuf) cudaFree(qbuf);
+    qbuf = nullptr;
+    qcap = 0;
   }
 };
 
@@ -1530,9 +1536,31 @@ int sfsim_atmo_query_surrogate(sfsim_atmo_context* ctx, long long n, const doubl
   for (int i = 0; i < 4; i++) biases[i] = S.w + S.lay.b[i];
   int rc = 0, sms = 0;
   CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->dev));
-  if (launch_surrogate_infer(q, n, x, v, l, S.wb, biases, S.w + S.lay.W[4], S.w + S.lay.b[4], kLogEps,
-                             fallback ? threshold : 0.0f, out, mask, count, S.error, S.packed, sms, st))
-    rc = fail(SFSIM_ATMO_ECUDA, "surrogate inference launch configuration failed");
+  // queries go through in chunks: the lookup kernel forms coordinates and
+  // table values into a cached scratch buffer, the fused kernel evaluates them
+  const long long chunk = std::min(n, kQueryChunk);
+  if (S.qcap < chunk) {
+    if (S.qbuf) cudaFree(S.qbuf);
+    S.qbuf = nullptr;
+    S.qcap = 0;
+    if (cudaMalloc(&S.qbuf, sizeof(float) * (kMlpCoords + 3) * (size_t)chunk) != cudaSuccess) {
+      S.qbuf = nullptr;
+      rc = fail(SFSIM_ATMO_ENOMEM, "query scratch allocation failed");
+    } else {
+      S.qcap = chunk;
+    }
+  }
+  if (!rc) launch_pack_infer(S.wb, S.packed, st);
+  for (long long o = 0; o < n && !rc; o += chunk) {
+    const long long m = std::min(chunk, n - o);
+    float* crd = S.qbuf;
+    float* tab = S.qbuf + kMlpCoords * chunk;
+    launch_query_coords(q, m, x + 3 * o, v + 3 * o, l + 3 * o, crd, tab, st);
+    if (launch_surrogate_infer(m, crd, tab, S.packed, biases, S.w + S.lay.W[4], S.w + S.lay.b[4], kLogEps,
+                               fallback ? threshold : 0.0f, out + 3 * o, mask ? mask + o : nullptr, count, S.error,
+                               sms, st))
+      rc = fail(SFSIM_ATMO_ECUDA, "surrogate inference launch configuration failed");
+  }
   if (!rc && fallback) launch_query_direct(ctx->params, ctx->dims, ctx->jsum, n, x, v, l, out, st, mask);
   if (!rc && cudaGetLastError() != cudaSuccess) rc = fail(SFSIM_ATMO_ECUDA, "surrogate query launch failed");
   if (fallback) {

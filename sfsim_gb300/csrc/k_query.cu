@@ -538,15 +538,18 @@ void launch_query_direct(const AtmoParams* params, const BuildDims& d, const Vec
 // ---------------------------------------------------------------------------
 // Fused surrogate inference on the tensor cores.
 //
-// A persistent CTA per SM evaluates groups of 256 queries (two 128-row tiles
-// A0, A1 of BF16 activations, K-major core-matrix layout, 64 KB each).  Warps
-// 0-7 own one query each per thread (warps 0-3 tile 0, 4-7 tile 1): they form
-// the coordinates, the table lookup and the Fourier features, and after every
-// layer read their row of the FP32 accumulator from tensor memory
-// (tcgen05.ld), add the bias, apply SiLU and write the BF16 result back as the
-// next layer's input; the last layer folds the 256 -> 4 head in.  The value is
-// (table + eps) exp(r) - eps, and a query whose predicted squared error exp(s)
-// exceeds threshold^2 is flagged for the direct quadrature.  Warp 8 is the producer: one thread
+// The coordinates and the table value of each query come from the lookup
+// kernel (k_query_coords) run just before.  A persistent CTA per SM then
+// evaluates groups of 256 queries (two 128-row tiles A0, A1 of BF16
+// activations, K-major core-matrix layout, 64 KB each).  Warps 0-7 own one
+// query each per thread (warps 0-3 tile 0, 4-7 tile 1): they write the
+// Fourier features, and after every layer read their row of the FP32
+// accumulator from tensor memory (tcgen05.ld, the next 32 columns in flight
+// while the current ones are processed), add the bias, apply SiLU and write
+// the BF16 result back as the next layer's input; the last layer folds the
+// 256 -> 4 head in.  The value is (table + eps) exp(r) - eps, and a query whose
+// predicted squared error exp(s) exceeds threshold^2 is flagged for the direct
+// quadrature.  Warp 8 is the producer: one thread
 // streams the 28 weight chunks of a group (256 rows x 32 K, 16 KB each,
 // pre-packed in the tensor cores' layout) through a five-stage shared-memory
 // ring with bulk TMA copies, and issues the tcgen05.mma of both tiles on each
@@ -601,9 +604,9 @@ __global__ void k_pack_infer(const __nv_bfloat16* W0, const __nv_bfloat16* W1, c
 }
 
 struct InferArgs {
-  GlslEnv env;
   long long n;
-  const double *X, *V, *L;
+  const float* coords;          // [n][kMlpCoords]
+  const float* table;           // [n][3], the lookup's value
   const unsigned char* packed;  // kInferChunks weight chunks
   const float* b[4];
   const float* W5;              // [kMlpOut][256]
@@ -649,7 +652,7 @@ __device__ __forceinline__ void write_features(float u, unsigned char* A, int ro
 }
 
 // Producer thread: weight chunks through the ring, MMAs of both tiles.
-__device__ void infer_producer(const InferArgs& g, long long my_groups, unsigned char* smem, uint32_t tmem,
+__device__ __forceinline__ void infer_producer(const InferArgs& g, long long my_groups, unsigned char* smem, uint32_t tmem,
                                uint64_t* full, uint64_t* empty, uint64_t* acc_bar, uint64_t* act_bar,
                                volatile int* abort_flag) {
   unsigned char* ring = smem + kInferSmemRing;
@@ -721,7 +724,9 @@ __global__ void __launch_bounds__(kInferThreads, 1) k_surrogate_infer(InferArgs 
   const long long ngroups = (g.n + 255) / 256;
   const long long my_groups = blockIdx.x < ngroups ? (ngroups - 1 - blockIdx.x) / gridDim.x + 1 : 0;
 
-  for (int i = t; i < 4 * kMlpHidden; i += kInferThreads) s_bias[i] = 0.5f * g.b[i / kMlpHidden][i % kMlpHidden];
+#pragma unroll
+  for (int layer = 0; layer < 4; layer++)  // constant indices keep the kernel parameters out of local memory
+    for (int i = t; i < kMlpHidden; i += kInferThreads) s_bias[layer * kMlpHidden + i] = 0.5f * g.b[layer][i];
   for (int i = t; i < kMlpOut * kMlpHidden; i += kInferThreads) s_w5[i] = g.W5[i];
   if (t < kMlpOut) s_w5[kMlpOut * kMlpHidden + t] = g.b5[t];
   if (warp == 0) tc::tmem_alloc(tmem_slot, 2 * kMlpHidden);
@@ -753,18 +758,14 @@ __global__ void __launch_bounds__(kInferThreads, 1) k_surrogate_infer(InferArgs 
       const long long q = (blockIdx.x + gi * gridDim.x) * 256 + tile * 128 + row;
       const bool valid = q < g.n;
       const long long qq = valid ? q : g.n - 1;
-      const f3 p = F3((float)g.X[3 * qq], (float)g.X[3 * qq + 1], (float)g.X[3 * qq + 2]);
-      const f3 d = F3((float)g.V[3 * qq], (float)g.V[3 * qq + 1], (float)g.V[3 * qq + 2]);
-      const f3 l = F3((float)g.L[3 * qq], (float)g.L[3 * qq + 1], (float)g.L[3 * qq + 2]);
-      float idx[4], u[kMlpCoords];
-      network_coords(g.env, p, d, l, u, idx);
+      float u[kMlpCoords];
+#pragma unroll
+      for (int c = 0; c < kMlpCoords; c++) u[c] = g.coords[kMlpCoords * qq + c];
 #pragma unroll
       for (int dd = 0; dd < kMlpCoords; dd++) write_features(u[dd], A, row, 32 * dd);
       tc::fence_async_smem();
       tc::fence_before();
       tc::mbar_arrive(act_bar);
-      // the table lookup overlaps the first layer's MMAs
-      const f3 table = in_scatter_g(g.env, idx, fdot(d, l));
       float head[kMlpOut] = {};
       for (int layer = 0; layer < 4; layer++) {
         bool done = tc::mbar_wait(acc_bar, acc_phase & 1, kInferWaitLimit);
@@ -775,13 +776,18 @@ __global__ void __launch_bounds__(kInferThreads, 1) k_surrogate_infer(InferArgs 
         }
         tc::fence_after();
         const float* hb = s_bias + layer * kMlpHidden;
-        for (int n0 = 0; n0 < kMlpHidden; n0 += 64) {
-          uint32_t r[64];
-          tc::tmem_ld64(trow + (uint32_t)n0, r);
+        uint32_t rb[2][32];
+        tc::tmem_ld32_async(trow, rb[0]);
+        tc::tmem_wait_ld(rb[0]);
 #pragma unroll
-          for (int i8 = 0; i8 < 8; i8++) {
-            const float4 b0 = *reinterpret_cast<const float4*>(hb + n0 + 8 * i8);
-            const float4 b1 = *reinterpret_cast<const float4*>(hb + n0 + 8 * i8 + 4);
+        for (int blk = 0; blk < kMlpHidden / 32; blk++) {
+          if (blk + 1 < kMlpHidden / 32) tc::tmem_ld32_async(trow + (uint32_t)(32 * (blk + 1)), rb[(blk + 1) & 1]);
+          const uint32_t* r = rb[blk & 1];
+#pragma unroll
+          for (int i8 = 0; i8 < 4; i8++) {
+            const int n0 = 32 * blk + 8 * i8;
+            const float4 b0 = *reinterpret_cast<const float4*>(hb + n0);
+            const float4 b1 = *reinterpret_cast<const float4*>(hb + n0 + 4);
             const float bb[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
             uint32_t w[4];
             float hv[8];
@@ -790,24 +796,25 @@ __global__ void __launch_bounds__(kInferThreads, 1) k_surrogate_infer(InferArgs 
               // SiLU(z) = z sigmoid(z) = hz (1 + tanh hz) with hz = z / 2
               const float h0 = fmaf(0.5f, __uint_as_float(r[8 * i8 + j]), bb[j]);
               const float h1 = fmaf(0.5f, __uint_as_float(r[8 * i8 + j + 1]), bb[j + 1]);
-              const __nv_bfloat162 hh = __floats2bfloat162_rn(fmaf(h0, tanh_approx(h0), h0), fmaf(h1, tanh_approx(h1), h1));
+              const __nv_bfloat162 hh =
+                  __floats2bfloat162_rn(fmaf(h0, tanh_approx(h0), h0), fmaf(h1, tanh_approx(h1), h1));
               w[j / 2] = *reinterpret_cast<const uint32_t*>(&hh);
               hv[j] = __low2float(hh);
               hv[j + 1] = __high2float(hh);
             }
             if (layer < 3) {
-              *reinterpret_cast<uint4*>(A + tc::tile_offset(row, n0 + 8 * i8, kMlpHidden)) =
-                  make_uint4(w[0], w[1], w[2], w[3]);
+              *reinterpret_cast<uint4*>(A + tc::tile_offset(row, n0, kMlpHidden)) = make_uint4(w[0], w[1], w[2], w[3]);
             } else {
 #pragma unroll
               for (int cc = 0; cc < kMlpOut; cc++) {
-                const float4 w0 = *reinterpret_cast<const float4*>(s_w5 + cc * kMlpHidden + n0 + 8 * i8);
-                const float4 w1 = *reinterpret_cast<const float4*>(s_w5 + cc * kMlpHidden + n0 + 8 * i8 + 4);
+                const float4 w0 = *reinterpret_cast<const float4*>(s_w5 + cc * kMlpHidden + n0);
+                const float4 w1 = *reinterpret_cast<const float4*>(s_w5 + cc * kMlpHidden + n0 + 4);
                 head[cc] = fmaf(hv[0], w0.x, fmaf(hv[1], w0.y, fmaf(hv[2], w0.z, fmaf(hv[3], w0.w, head[cc]))));
                 head[cc] = fmaf(hv[4], w1.x, fmaf(hv[5], w1.y, fmaf(hv[6], w1.z, fmaf(hv[7], w1.w, head[cc]))));
               }
             }
           }
+          if (blk + 1 < kMlpHidden / 32) tc::tmem_wait_ld(rb[(blk + 1) & 1]);
         }
         if (layer < 3) {
           tc::fence_async_smem();
@@ -818,7 +825,7 @@ __global__ void __launch_bounds__(kInferThreads, 1) k_surrogate_infer(InferArgs 
       if (!ok) break;
       bool flag = false;
       if (valid) {
-        const float tv[3] = {table.x, table.y, table.z};
+        const float tv[3] = {g.table[3 * q], g.table[3 * q + 1], g.table[3 * q + 2]};
 #pragma unroll
         for (int cc = 0; cc < 3; cc++) {
           const float r = head[cc] + s_w5[kMlpOut * kMlpHidden + cc];
@@ -842,19 +849,19 @@ __global__ void __launch_bounds__(kInferThreads, 1) k_surrogate_infer(InferArgs 
   if (warp == 0) tc::tmem_dealloc(tmem, 2 * kMlpHidden);
 }
 
-int launch_surrogate_infer(const QueryTables& qt, long long n, const double* x, const double* v, const double* l,
-                           const __nv_bfloat16* const* W, const float* const* b, const float* W5, const float* b5,
-                           float eps, float threshold, float* out, unsigned char* mask,
-                           unsigned long long* count, int* error, unsigned char* packed, int num_sms,
-                           cudaStream_t st) {
+void launch_pack_infer(const __nv_bfloat16* const* W, unsigned char* packed, cudaStream_t st) {
   constexpr int nthreads = kMlpHidden * (kMlpIn / 8) + 3 * kMlpHidden * (kMlpHidden / 8);
   k_pack_infer<<<(nthreads + 255) / 256, 256, 0, st>>>(W[0], W[1], W[2], W[3], packed);
+}
+
+int launch_surrogate_infer(long long n, const float* coords, const float* table, const unsigned char* packed,
+                           const float* const* b, const float* W5, const float* b5, float eps, float threshold,
+                           float* out, unsigned char* mask, unsigned long long* count, int* error, int num_sms,
+                           cudaStream_t st) {
   InferArgs g;
-  g.env = make_env(qt, 0);
   g.n = n;
-  g.X = x;
-  g.V = v;
-  g.L = l;
+  g.coords = coords;
+  g.table = table;
   g.packed = packed;
   for (int i = 0; i < 4; i++) g.b[i] = b[i];
   g.W5 = W5;

@@ -112,12 +112,14 @@ void launch_random_queries(long long n, unsigned long long seed, double R, doubl
 void launch_node_pool(const BuildDims& d, float* pool, cudaStream_t st);
 void launch_make_pool(long long n, const float* coords, const float* values, const float* table, float eps,
                       float* pool, cudaStream_t st);
-// Fused tensor-core inference of the surrogate for n queries; see k_query.cu.
-int launch_surrogate_infer(const QueryTables& qt, long long n, const double* x, const double* v, const double* l,
-                           const __nv_bfloat16* const* W, const float* const* b, const float* W5, const float* b5,
-                           float eps, float threshold, float* out, unsigned char* mask,
-                           unsigned long long* count, int* error, unsigned char* packed, int num_sms,
+// Fused tensor-core inference of the surrogate for n queries from their
+// coordinates and table values (launch_query_coords); see k_query.cu.
+int launch_surrogate_infer(long long n, const float* coords, const float* table, const unsigned char* packed,
+                           const float* const* b, const float* W5, const float* b5, float eps, float threshold,
+                           float* out, unsigned char* mask, unsigned long long* count, int* error, int num_sms,
                            cudaStream_t st);
+// Packs the BF16 hidden-layer weights into the inference kernel's chunks.
+void launch_pack_infer(const __nv_bfloat16* const* W, unsigned char* packed, cudaStream_t st);
 // Bytes of the packed weight chunks the inference kernel streams.
 size_t infer_packed_bytes();
 

@@ -131,6 +131,33 @@ __device__ __forceinline__ void tmem_ld64(uint32_t taddr, uint32_t* r) {
 }
 #undef SFSIM_R8
 
+#define SFSIM_O8(i) "=r"(r[i]), "=r"(r[i + 1]), "=r"(r[i + 2]), "=r"(r[i + 3]), "=r"(r[i + 4]), "=r"(r[i + 5]), \
+                    "=r"(r[i + 6]), "=r"(r[i + 7])
+#define SFSIM_IO8(i) "+r"(r[i]), "+r"(r[i + 1]), "+r"(r[i + 2]), "+r"(r[i + 3]), "+r"(r[i + 4]), "+r"(r[i + 5]), \
+                     "+r"(r[i + 6]), "+r"(r[i + 7])
+
+// 32 lanes x 32 columns of 32 bits without waiting: r is valid only after
+// tmem_wait_ld(r).
+__device__ __forceinline__ void tmem_ld32_async(uint32_t taddr, uint32_t* r) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+      "%15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
+      : SFSIM_O8(0), SFSIM_O8(8), SFSIM_O8(16), SFSIM_O8(24)
+      : "r"(taddr)
+      : "memory");
+}
+
+// Waits for this thread's tensor-memory loads; the registers of the last one
+// pass through the wait so that no use of them is scheduled before it.
+__device__ __forceinline__ void tmem_wait_ld(uint32_t* r) {
+  asm volatile("tcgen05.wait::ld.sync.aligned;"
+               : SFSIM_IO8(0), SFSIM_IO8(8), SFSIM_IO8(16), SFSIM_IO8(24)
+               :
+               : "memory");
+}
+#undef SFSIM_O8
+#undef SFSIM_IO8
+
 // Byte offset of element (row, k) of a K-major tile of `kw` K per row
 // group (core matrices adjacent in K 128 B apart, row groups kw * 16 B apart).
 __device__ __forceinline__ uint32_t tile_offset(int row, int k, int kw = 64) {
