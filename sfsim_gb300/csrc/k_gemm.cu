@@ -3,18 +3,25 @@
 // needs.  C[m][n] = sum_k A[m][k] B[n][k] ("TN": both operands row-major with
 // K contiguous).
 //
-// One CTA of 128 threads computes a 128 x N tile (N <= 256, N % 16 == 0) over
-// a K range.  Per K chunk of 64 the threads copy A (128 x 64) and B (N x 64)
-// from global memory into shared memory in the canonical no-swizzle K-major
-// layout of the tensor cores (8-row x 16-byte core matrices; core matrices
-// adjacent in K 128 B apart, adjacent in M/N 1024 B apart), then one thread
-// issues four tcgen05.mma (K = 16 each) into the TMEM accumulator and commits
-// them to an mbarrier that every thread waits on before the buffers are
-// refilled.  The epilogue reads the accumulator with tcgen05.ld (warp w owns
-// rows 32w..32w+31).  Every wait is bounded; on timeout the CTA records an
-// error, releases its tensor memory and returns.
+// A persistent, warp-specialised kernel.  Work items are output tiles of
+// 128 x Nt (Nt = N rounded up to 16, at most 256) times split-K slices of the
+// K range, dealt round-robin to one CTA per SM.  Warp 0 is the producer: one thread loads K chunks of 64 of A
+// (128 x 64) and B (Nt x 64) with TMA tensor copies (128-byte swizzle) into a
+// ring of shared-memory stages.  Warp 1 issues the tcgen05.mma (K = 16 each,
+// 128-byte-swizzled K-major descriptors) into one of two tensor-memory
+// accumulators and releases each stage with tcgen05.commit.  Warps 2-9 are the
+// epilogue, two per group of 32 tensor-memory lanes (one per half of the
+// columns): they read the finished accumulator (tcgen05.ld, the next 32
+// columns in flight while the current ones are written) and apply the
+// epilogue while the MMAs of the next tile run into the other accumulator.
+// Every wait is bounded; on timeout the CTA records an error, drains its
+// copies and MMAs and returns.
+#include <cuda.h>
 #include <cuda_bf16.h>
 #include <stdint.h>
+
+#include <algorithm>
+#include <mutex>
 
 #include "atmo_device.cuh"
 #include "kernels.h"
@@ -22,21 +29,32 @@
 
 namespace sfsim {
 
+constexpr int kGemmBK = 64;                 // K per stage: one 128-byte swizzle atom of bf16
+constexpr int kGemmWaitLimit = 1 << 22;
+constexpr int kGemmThreads = 320;  // producer, MMA, 8 epilogue warps
+constexpr int kGemmEpilogueThreads = 256;
+constexpr int kGemmSmemBudget = 192 * 1024;  // stages
+constexpr int kGemmTileA = 128 * kGemmBK * 2;
 
+// K-major operand with 128-byte swizzle: rows of 128 B, 16-byte chunks XOR
+// (row % 8), 8-row groups 1024 B apart (SBO); the descriptor of the K = 16
+// step ks starts 32 * ks bytes into the atom.
+__device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr) {
+  uint64_t d = 0;
+  d |= (uint64_t)((saddr >> 4) & 0x3FFFu);
+  d |= (uint64_t)1 << 16;                 // leading byte offset (unused with swizzling)
+  d |= (uint64_t)(1024 >> 4) << 32;       // stride byte offset
+  d |= (uint64_t)1 << 46;                 // descriptor version
+  d |= (uint64_t)2 << 61;                 // layout: 128-byte swizzle
+  return d;
+}
 
-constexpr int kGemmBK = 64;
-constexpr int kWaitLimit = 1 << 22;
-
-// Copies rows [0, nrows) x K columns [k0, k0 + 64) of a row-major bf16 matrix
-// (leading dimension ld) into a K-major core-matrix tile; rows >= valid read 0.
-__device__ __forceinline__ void load_tile(const __nv_bfloat16* src, long long ld, int nrows, int valid, long long k0,
-                                          unsigned char* tile) {
-  for (int c = threadIdx.x; c < nrows * 8; c += blockDim.x) {
-    const int row = c >> 3, kc = c & 7;
-    uint4 v = make_uint4(0, 0, 0, 0);
-    if (row < valid) v = *reinterpret_cast<const uint4*>(src + (long long)row * ld + k0 + kc * 8);
-    *reinterpret_cast<uint4*>(tile + tc::tile_offset(row, kc * 8)) = v;
-  }
+__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, int x, int y, uint64_t* mbar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], "
+      "[%4];" ::"r"(tc::smem_u32(dst)),
+      "l"(map), "r"(x), "r"(y), "r"(tc::smem_u32(mbar))
+      : "memory");
 }
 
 __device__ __forceinline__ float silu(float z) { return z / (1.0f + __expf(-z)); }
@@ -45,103 +63,301 @@ __device__ __forceinline__ float dsilu(float z) {
   return s * (1.0f + z * (1.0f - s));
 }
 
-template <int N>
-__global__ void __launch_bounds__(128) k_gemm_tn(GemmArgs g) {
-  extern __shared__ __align__(1024) unsigned char smem[];
-  __shared__ uint64_t mbar;
-  __shared__ uint32_t tmem_slot;
-  unsigned char* tileA = smem;
-  unsigned char* tileB = smem + 128 * kGemmBK * 2;
-  const int m0 = blockIdx.x * 128;
-  const int split = blockIdx.y;
-  const long long kper = g.K / gridDim.y;
-  const long long kbeg = (long long)split * kper;
-  constexpr uint32_t ncols = N <= 32 ? 32 : N <= 64 ? 64 : N <= 128 ? 128 : 256;
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+struct GemmKernelArgs {
+  GemmArgs g;
+  int nt;          // N rounded up to 16: the MMA's N and the B box height
+  int stages;
+  int tiles_m, splits;
+  long long kper;  // K per split, a multiple of kGemmBK
+};
 
-  if (warp == 0) tc::tmem_alloc(&tmem_slot, ncols);
-  if (threadIdx.x == 0) tc::mbar_init(&mbar, 1);
+// 32 columns of the epilogue for row m, columns n0 .. n0 + 31.
+__device__ __forceinline__ void gemm_epilogue32(const GemmArgs& g, const uint32_t* r, int m, int n0) {
+  const bool row_ok = m < g.M;
+  if (!row_ok) return;
+#pragma unroll
+  for (int i8 = 0; i8 < 4; i8++) {
+    const int nb = n0 + 8 * i8;
+    if (nb >= g.N) break;
+    float z[8];
+#pragma unroll
+    for (int i = 0; i < 8; i++) z[i] = __uint_as_float(r[8 * i8 + i]) * g.alpha;
+    const bool full8 = nb + 8 <= g.N;
+    if (g.bias) {
+#pragma unroll
+      for (int i = 0; i < 8; i++)
+        if (nb + i < g.N) z[i] += g.bias[nb + i];
+    }
+    if (g.dact) {
+      const float* src = g.dact + (long long)m * g.N + nb;
+      if (full8 && (g.N % 4 == 0)) {
+        const float4 a = *reinterpret_cast<const float4*>(src), b = *reinterpret_cast<const float4*>(src + 4);
+        z[0] *= a.x, z[1] *= a.y, z[2] *= a.z, z[3] *= a.w, z[4] *= b.x, z[5] *= b.y, z[6] *= b.z, z[7] *= b.w;
+      } else {
+#pragma unroll
+        for (int i = 0; i < 8; i++)
+          if (nb + i < g.N) z[i] *= src[i];
+      }
+    }
+#pragma unroll
+    for (int i = 0; i < 8; i++) {
+      const int n = nb + i;
+      if (n >= g.N) break;
+      if (g.Cf32) g.Cf32[(long long)m * g.ldc + n] = z[i];
+      if (g.Cacc) atomicAdd(g.Cacc + (long long)m * g.ldc + n, z[i]);
+    }
+    if (g.Dsilu) {
+      float* dst = g.Dsilu + (long long)m * g.N + nb;
+      if (full8 && (g.N % 4 == 0)) {
+        float d[8];
+#pragma unroll
+        for (int i = 0; i < 8; i++) d[i] = dsilu(z[i]);
+        *reinterpret_cast<float4*>(dst) = make_float4(d[0], d[1], d[2], d[3]);
+        *reinterpret_cast<float4*>(dst + 4) = make_float4(d[4], d[5], d[6], d[7]);
+      } else {
+#pragma unroll
+        for (int i = 0; i < 8; i++)
+          if (nb + i < g.N) dst[i] = dsilu(z[i]);
+      }
+    }
+    if (g.Hbf16 || g.HTbf16) {
+      __nv_bfloat16 h[8];
+#pragma unroll
+      for (int i = 0; i < 8; i++) h[i] = __float2bfloat16(g.silu ? silu(z[i]) : z[i]);
+      if (g.Hbf16) {
+        __nv_bfloat16* dst = g.Hbf16 + (long long)m * g.ldh + nb;
+        if (full8 && (g.ldh % 8 == 0)) {
+          *reinterpret_cast<uint4*>(dst) = *reinterpret_cast<const uint4*>(h);
+        } else {
+#pragma unroll
+          for (int i = 0; i < 8; i++)
+            if (nb + i < g.N) dst[i] = h[i];
+        }
+      }
+      if (g.HTbf16) {
+#pragma unroll
+        for (int i = 0; i < 8; i++)
+          if (nb + i < g.N) g.HTbf16[(long long)(nb + i) * g.ldht + m] = h[i];
+      }
+    }
+  }
+}
+
+__global__ void __launch_bounds__(kGemmThreads, 1)
+    k_gemm_tn(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB, GemmKernelArgs a) {
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  // 1024-byte alignment for the swizzle atoms
+  unsigned char* smem = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  const int S = a.stages;
+  const int stage_bytes = kGemmTileA + a.nt * kGemmBK * 2;
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem + S * stage_bytes);
+  uint64_t* empty = full + S;
+  uint64_t* tfull = empty + S;   // [2] accumulator ready
+  uint64_t* tempty = tfull + 2;  // [2] accumulator drained by the epilogue
+  uint64_t* drain = tempty + 2;
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(drain + 1);
+  volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const uint32_t ncols = a.nt <= 32 ? 32 : a.nt <= 64 ? 64 : a.nt <= 128 ? 128 : 256;  // per accumulator
+  const long long ntiles = (long long)a.tiles_m * a.splits;
+  const long long my_tiles = blockIdx.x < ntiles ? (ntiles - 1 - blockIdx.x) / gridDim.x + 1 : 0;
+  const int kchunks = (int)(a.kper / kGemmBK);
+
+  if (warp == 0) tc::tmem_alloc(tmem_slot, 2 * ncols);
+  if (threadIdx.x == 32) {
+    for (int s = 0; s < S; s++) {
+      tc::mbar_init(&full[s], 1);
+      tc::mbar_init(&empty[s], 1);
+    }
+    for (int b = 0; b < 2; b++) {
+      tc::mbar_init(&tfull[b], 1);
+      tc::mbar_init(&tempty[b], kGemmEpilogueThreads);
+    }
+    tc::mbar_init(drain, 1);
+    *abort_flag = 0;
+    tc::fence_mbar_init();
+  }
   tc::fence_before();
   __syncthreads();
   tc::fence_after();
-  const uint32_t tmem = tmem_slot;
-  const uint32_t idesc = tc::idesc_bf16(128, N);
-  bool ok = true;
-  uint32_t parity = 0;
-  const int validA = min(128, g.M - m0);
-  for (long long k = 0; k < kper && ok; k += kGemmBK) {
-    load_tile(g.A + (long long)m0 * g.lda, g.lda, 128, validA, kbeg + k, tileA);
-    load_tile(g.B, g.ldb, N, g.N, kbeg + k, tileB);
-    tc::fence_async_smem();
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      tc::fence_after();
-      const uint32_t a0 = tc::smem_u32(tileA), b0 = tc::smem_u32(tileB);
-#pragma unroll
-      for (int ks = 0; ks < kGemmBK / 16; ks++) {
-        const uint64_t da = tc::smem_desc(a0 + ks * 256, 128, 1024);
-        const uint64_t db = tc::smem_desc(b0 + ks * 256, 128, 1024);
-        tc::mma(tmem, da, db, idesc, (k > 0 || ks > 0) ? 1u : 0u);
-      }
-      tc::commit(&mbar);
-    }
-    bool done = tc::mbar_wait(&mbar, parity, kWaitLimit);
-    if (!done) done = tc::mbar_wait(&mbar, parity, kWaitLimit);  // in-flight MMAs get a second window
-    parity ^= 1;
-    tc::fence_after();
-    ok = __syncthreads_and(done) != 0;  // one decision for the whole CTA
-  }
+  const uint32_t tmem = *tmem_slot;
 
-  if (ok) {
-    // epilogue: warp w owns accumulator rows 32w..32w+31
-    const int m = m0 + warp * 32 + lane;
-    const bool row_ok = m < g.M;
-    for (int n0 = 0; n0 < N; n0 += 8) {
-      float v[8];
-      tc::tmem_ld8(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)n0, v);
-      if (!row_ok) continue;
-#pragma unroll
-      for (int i = 0; i < 8; i++) {
-        const int n = n0 + i;
-        if (n >= g.N) continue;
-        float z = v[i] * g.alpha;
-        if (g.bias) z += g.bias[n];
-        if (g.dact) z *= g.dact[(long long)m * g.N + n];
-        if (g.Cf32) g.Cf32[(long long)m * g.ldc + n] = z;
-        if (g.Cacc) atomicAdd(g.Cacc + (long long)m * g.ldc + n, z);
-        if (g.Dsilu) g.Dsilu[(long long)m * g.N + n] = dsilu(z);
-        const float h = g.silu ? silu(z) : z;
-        if (g.Hbf16) g.Hbf16[(long long)m * g.ldh + n] = __float2bfloat16(h);
-        if (g.HTbf16) g.HTbf16[(long long)n * g.ldht + m] = __float2bfloat16(h);
+  if (warp == 0) {
+    if (lane == 0) {
+      // producer
+      long long issued = 0;
+      bool ok = true;
+      for (long long ti = 0; ti < my_tiles && ok; ti++) {
+        const long long tile = blockIdx.x + ti * gridDim.x;
+        const int tm = (int)(tile % a.tiles_m), split = (int)(tile / a.tiles_m);
+        for (int kc = 0; kc < kchunks; kc++, issued++) {
+          const int s = (int)(issued % S);
+          if (issued >= S &&
+              !(ok = tc::mbar_wait(&empty[s], (uint32_t)(((issued - S) / S) & 1), kGemmWaitLimit) && !*abort_flag))
+            break;
+          unsigned char* st = smem + s * stage_bytes;
+          tc::mbar_expect_tx(&full[s], (uint32_t)stage_bytes);
+          const int k = (int)(split * a.kper + (long long)kc * kGemmBK);
+          tma_load_2d(st, &mapA, k, tm * 128, &full[s]);
+          tma_load_2d(st + kGemmTileA, &mapB, k, 0, &full[s]);
+        }
       }
+      if (!ok) {
+        *abort_flag = 1;
+        if (a.g.error) atomicExch(a.g.error, 1);
+      }
+      // copies in flight land before the CTA leaves: wait for the last S issued
+      for (long long k = issued > S ? issued - S : 0; k < issued; k++)
+        tc::mbar_wait(&full[k % S], (uint32_t)((k / S) & 1), kGemmWaitLimit);
     }
-  } else if (threadIdx.x == 0 && g.error) {
-    atomicExch(g.error, 1);
+    __syncwarp();
+  } else if (warp == 1) {
+    if (lane == 0) {
+      // MMA issuer
+      const uint32_t idesc = tc::idesc_bf16(128, a.nt);
+      const uint32_t base = tc::smem_u32(smem);
+      long long c = 0;
+      bool ok = true;
+      for (long long ti = 0; ti < my_tiles && ok; ti++) {
+        const int b = (int)(ti & 1);
+        if (ti >= 2 &&
+            !(ok = tc::mbar_wait(&tempty[b], (uint32_t)(((ti - 2) >> 1) & 1), kGemmWaitLimit) && !*abort_flag))
+          break;
+        tc::fence_after();
+        const uint32_t d = tmem + (uint32_t)(b * ncols);
+        for (int kc = 0; kc < kchunks; kc++, c++) {
+          const int s = (int)(c % S);
+          if (!(ok = tc::mbar_wait(&full[s], (uint32_t)((c / S) & 1), kGemmWaitLimit) && !*abort_flag)) break;
+          tc::fence_after();
+          const uint32_t sa = base + s * stage_bytes, sb = sa + kGemmTileA;
+#pragma unroll
+          for (int ks = 0; ks < kGemmBK / 16; ks++)
+            tc::mma(d, sw128_desc(sa + 32 * ks), sw128_desc(sb + 32 * ks), idesc, (kc > 0 || ks > 0) ? 1u : 0u);
+          tc::commit(&empty[s]);
+        }
+        if (ok) tc::commit(&tfull[b]);
+      }
+      if (!ok) {
+        *abort_flag = 1;
+        if (a.g.error) atomicExch(a.g.error, 1);
+      }
+      // every MMA issued by this thread completes before the CTA leaves
+      tc::commit(drain);
+      tc::mbar_wait(drain, 0, kGemmWaitLimit);
+    }
+    __syncwarp();
+  } else {
+    // epilogue: warp w reads tensor-memory lanes 32 (w % 4) .. + 31, columns
+    // of its half
+    const int q = warp & 3, half = (warp - 2) >> 2;
+    bool ok = true;
+    for (long long ti = 0; ti < my_tiles && ok; ti++) {
+      const long long tile = blockIdx.x + ti * gridDim.x;
+      const int tm = (int)(tile % a.tiles_m);
+      const int b = (int)(ti & 1);
+      bool done = tc::mbar_wait(&tfull[b], (uint32_t)((ti >> 1) & 1), kGemmWaitLimit);
+      if (!__all_sync(0xffffffffu, done) || *abort_flag) {
+        ok = false;
+        break;
+      }
+      tc::fence_after();
+      const int m = tm * 128 + q * 32 + lane;
+      const uint32_t trow = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(b * ncols);
+      const int nall = (a.nt + 31) / 32, nh = (nall + 1) / 2;
+      const int b0 = half * nh, b1 = min(nall, b0 + nh);
+      if (b0 < b1) {
+        uint32_t rb[2][32];
+        tc::tmem_ld32_async(trow + (uint32_t)(32 * b0), rb[0]);
+        tc::tmem_wait_ld(rb[0]);
+        for (int blk = b0; blk < b1; blk += 2) {
+          if (blk + 1 < b1) tc::tmem_ld32_async(trow + (uint32_t)(32 * (blk + 1)), rb[1]);
+          gemm_epilogue32(a.g, rb[0], m, 32 * blk);
+          if (blk + 1 < b1) {
+            tc::tmem_wait_ld(rb[1]);
+            if (blk + 2 < b1) tc::tmem_ld32_async(trow + (uint32_t)(32 * (blk + 2)), rb[0]);
+            gemm_epilogue32(a.g, rb[1], m, 32 * (blk + 1));
+            if (blk + 2 < b1) tc::tmem_wait_ld(rb[0]);
+          }
+        }
+      }
+      tc::fence_before();
+      tc::mbar_arrive(&tempty[b]);
+    }
+    if (!ok) {
+      *abort_flag = 1;
+      if (lane == 0 && a.g.error) atomicExch(a.g.error, 1);
+    }
   }
   tc::fence_before();
   __syncthreads();
-  if (warp == 0) tc::tmem_dealloc(tmem, ncols);
+  if (warp == 0) tc::tmem_dealloc(tmem, 2 * ncols);
 }
 
-template <int N>
-static int launch_n(const GemmArgs& g, int splits, cudaStream_t st) {
-  const size_t smem = (size_t)(128 + N) * kGemmBK * 2;
-  if (cudaFuncSetAttribute(k_gemm_tn<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
-    return -1;
-  dim3 grid((unsigned)((g.M + 127) / 128), splits);
-  k_gemm_tn<N><<<grid, 128, smem, st>>>(g);
-  return 0;
+// ---------------------------------------------------------------------------
+// Host side: tensor maps through the driver entry point (no link to libcuda)
+// ---------------------------------------------------------------------------
+
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+static EncodeTiledFn encode_fn() {
+  static EncodeTiledFn fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<EncodeTiledFn>(p);
+  });
+  return fn;
+}
+
+// rows x cols bf16, row-major with leading dimension ld (elements); box
+// box_rows x 64 with 128-byte swizzle; out-of-range rows read as zero.
+static bool make_map(CUtensorMap* map, const void* base, long long rows, long long cols, long long ld, int box_rows) {
+  EncodeTiledFn fn = encode_fn();
+  if (!fn) return false;
+  const cuuint64_t dims[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
+  const cuuint64_t strides[1] = {(cuuint64_t)(ld * 2)};
+  const cuuint32_t box[2] = {(cuuint32_t)kGemmBK, (cuuint32_t)box_rows};
+  const cuuint32_t estr[2] = {1, 1};
+  return fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(base), dims, strides, box, estr,
+            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
 int launch_gemm_tn(const GemmArgs& g, int splits, cudaStream_t st) {
-  // the B tile holds N rows rounded up to a multiple of 16
-  if (g.K % (kGemmBK * splits) != 0) return -1;
-  if (g.N <= 16) return launch_n<16>(g, splits, st);
-  if (g.N <= 32) return launch_n<32>(g, splits, st);
-  if (g.N <= 64) return launch_n<64>(g, splits, st);
-  if (g.N <= 128) return launch_n<128>(g, splits, st);
-  if (g.N <= 256) return launch_n<256>(g, splits, st);
-  return -1;
+  if (g.N < 1 || g.N > 256 || g.M < 1 || splits < 1) return -1;
+  if (g.K % ((long long)kGemmBK * splits) != 0) return -1;
+  // TMA: 16-byte aligned bases and row strides
+  if ((reinterpret_cast<uintptr_t>(g.A) & 15) || (reinterpret_cast<uintptr_t>(g.B) & 15) || (g.lda % 8) ||
+      (g.ldb % 8))
+    return -1;
+  GemmKernelArgs a;
+  a.g = g;
+  a.nt = (g.N + 15) / 16 * 16;
+  a.splits = splits;
+  a.tiles_m = (g.M + 127) / 128;
+  a.kper = g.K / splits;
+  const int stage_bytes = kGemmTileA + a.nt * kGemmBK * 2;
+  const long long kchunks = a.kper / kGemmBK;
+  a.stages = (int)std::min<long long>(std::min(kGemmSmemBudget / stage_bytes, 8), std::max<long long>(kchunks, 2));
+  CUtensorMap mapA, mapB;
+  if (!make_map(&mapA, g.A, g.M, g.K, g.lda, 128) || !make_map(&mapB, g.B, g.N, g.K, g.ldb, a.nt)) return -1;
+  size_t smem = 1024 + (size_t)a.stages * stage_bytes + (2 * a.stages + 5) * 8 + 16;
+  // two 256-column accumulators take all of an SM's tensor memory: one CTA per SM
+  if (a.nt > 128) smem = std::max<size_t>(smem, 120 * 1024);
+  if (cudaFuncSetAttribute(k_gemm_tn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+    return -1;
+  int dev = 0, sms = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+    return -1;
+  const long long ntiles = (long long)a.tiles_m * splits;
+  const unsigned grid = (unsigned)std::min<long long>(ntiles, sms);
+  k_gemm_tn<<<grid, kGemmThreads, smem, st>>>(mapA, mapB, a);
+  return 0;
 }
 
 }  // namespace sfsim
