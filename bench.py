@@ -337,7 +337,29 @@ def query_error_stats(a, ref):
             "frac_le_1e-3": float((e <= 1e-3).double().mean()), "frac_le_1e-2": float((e <= 1e-2).double().mean())}
 
 
-def run_queries(C, steps=3000, batch=65536, direct_samples=1 << 25, lr=3e-3, huber_delta=0.02,
+MLP_FLOPS_PER_QUERY = 2 * (192 * 256 + 3 * 256 * 256 + 256 * 4)
+
+
+def surrogate_roofline(n, ms):
+    """Tensor roofline of a surrogate call: the network's algorithmic flops
+    over the whole call (lookup and packing included) against the measured
+    BF16 peak (burst, the call is timed alone)."""
+    peak = None
+    try:
+        with open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "MEASURED_PEAKS.json")) as f:
+            peak = json.load(f).get("bf16_tflops")
+    except (OSError, ValueError):
+        pass
+    src = "MEASURED_PEAKS.json bf16_tflops (burst)"
+    if not peak:
+        peak, src = 1900.0, "fallback 1.9 PFLOP/s"
+    achieved = n * MLP_FLOPS_PER_QUERY / (ms * 1e-3) / 1e12
+    return {"bound": "tensor", "kernel": "k_surrogate_infer", "achieved": achieved, "peak": peak,
+            "unit": "TFLOP/s", "frac": achieved / peak, "peak_source": src,
+            "flops_per_query": MLP_FLOPS_PER_QUERY}
+
+
+def run_queries(C, steps=10000, batch=65536, direct_samples=1 << 25, lr=3e-3, huber_delta=0.02,
                 thresholds=(3e-2, 1e-2, 3e-3, 1e-3)):
     """2^24 random in-scatter queries (height uniform 0-100 km, view and sun
     uniform on the sphere) on the production tables: table lookup, direct
@@ -370,7 +392,8 @@ def run_queries(C, steps=3000, batch=65536, direct_samples=1 << 25, lr=3e-3, hub
          "train_loss_first": float(hist[:10].mean()), "train_loss_last": float(hist[-100:].mean()),
          "table": {"qps": qps(t_table), "err": query_error_stats(table, direct)},
          "direct": {"qps": qps(t_direct)},
-         "surrogate": {"qps": qps(t_sur), "err": query_error_stats(sur, direct), "vs_direct": t_direct / t_sur}}
+         "surrogate": {"qps": qps(t_sur), "err": query_error_stats(sur, direct), "vs_direct": t_direct / t_sur,
+                       "roofline": surrogate_roofline(n, t_sur)}}
     del table, sur
     for thr in thresholds:
         t_fb, (fb, nf) = _timed(lambda: ctx.surrogate(x, v, l, threshold=thr, out=out), reps=1)

@@ -256,7 +256,8 @@ int sfsim_atmo_surrogate_gradients(sfsim_atmo_context* ctx, long long n, const f
  * the network, (table + 1e-7) exp(r) - 1e-7.  With threshold > 0, points whose
  * predicted relative error (the square root of the variance output) exceeds
  * `threshold` are recomputed by direct quadrature; *n_fallback receives their
- * number. */
+ * number.  Without a threshold the call is asynchronous on `stream`; with one
+ * it synchronises and also reports a tensor-core wait that timed out. */
 int sfsim_atmo_query_surrogate(sfsim_atmo_context* ctx, long long n, const double* x, const double* v,
                                const double* l, float* out, float threshold, long long* n_fallback,
                                void* stream);

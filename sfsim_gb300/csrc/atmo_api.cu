@@ -1095,7 +1095,7 @@ int surrogate_backward(Surrogate& S, long long n, float huber, cudaStream_t st) 
   launch_head_backward(n, S.dout, S.H[3], S.w + S.lay.W[4], S.dsilu[3], S.dZ[3], S.dZT[3], S.g + S.lay.W[4],
                        S.g + S.lay.b[4], st);
   int splits = 1;
-  while (splits < 128 && n % (64LL * splits * 2) == 0) splits *= 2;
+  while (splits < 64 && n % (64LL * splits * 2) == 0) splits *= 2;
   for (int l = 3; l >= 0; l--) {
     // dW_l = dZ_l^T H_{l-1}: A = dZ_l^T [out][n], B = H_{l-1}^T [in][n], K = n
     GemmArgs g = {};
@@ -1571,6 +1571,8 @@ int sfsim_atmo_query_surrogate(sfsim_atmo_context* ctx, long long n, const doubl
     cudaStreamSynchronize(st);
     cudaFree(mask);
     cudaFree(count);
+    // the call synchronised: report a wait that timed out in the inference kernel
+    if (!rc) rc = check_error_flag(S, st);
   }
   return rc;
 }

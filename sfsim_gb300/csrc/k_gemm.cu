@@ -90,7 +90,7 @@ __device__ __forceinline__ void gemm_epilogue32(const GemmArgs& g, const uint32_
     }
     if (g.dact) {
       const float* src = g.dact + (long long)m * g.N + nb;
-      if (full8 && (g.N % 4 == 0)) {
+      if (full8 && (g.N % 4 == 0) && (reinterpret_cast<uintptr_t>(g.dact) & 15) == 0) {
         const float4 a = *reinterpret_cast<const float4*>(src), b = *reinterpret_cast<const float4*>(src + 4);
         z[0] *= a.x, z[1] *= a.y, z[2] *= a.z, z[3] *= a.w, z[4] *= b.x, z[5] *= b.y, z[6] *= b.z, z[7] *= b.w;
       } else {
@@ -99,16 +99,24 @@ __device__ __forceinline__ void gemm_epilogue32(const GemmArgs& g, const uint32_
           if (nb + i < g.N) z[i] *= src[i];
       }
     }
+    if (g.Cacc && full8 && (g.ldc % 4 == 0) && (reinterpret_cast<uintptr_t>(g.Cacc) & 15) == 0) {
+      // vector reductions: a quarter of the atomic operations
+      float4* dst = reinterpret_cast<float4*>(g.Cacc + (long long)m * g.ldc + nb);
+      atomicAdd(dst, make_float4(z[0], z[1], z[2], z[3]));
+      atomicAdd(dst + 1, make_float4(z[4], z[5], z[6], z[7]));
+    } else if (g.Cacc) {
 #pragma unroll
-    for (int i = 0; i < 8; i++) {
-      const int n = nb + i;
-      if (n >= g.N) break;
-      if (g.Cf32) g.Cf32[(long long)m * g.ldc + n] = z[i];
-      if (g.Cacc) atomicAdd(g.Cacc + (long long)m * g.ldc + n, z[i]);
+      for (int i = 0; i < 8; i++)
+        if (nb + i < g.N) atomicAdd(g.Cacc + (long long)m * g.ldc + nb + i, z[i]);
+    }
+    if (g.Cf32) {
+#pragma unroll
+      for (int i = 0; i < 8; i++)
+        if (nb + i < g.N) g.Cf32[(long long)m * g.ldc + nb + i] = z[i];
     }
     if (g.Dsilu) {
       float* dst = g.Dsilu + (long long)m * g.N + nb;
-      if (full8 && (g.N % 4 == 0)) {
+      if (full8 && (g.N % 4 == 0) && (reinterpret_cast<uintptr_t>(g.Dsilu) & 15) == 0) {
         float d[8];
 #pragma unroll
         for (int i = 0; i < 8; i++) d[i] = dsilu(z[i]);
@@ -126,7 +134,7 @@ __device__ __forceinline__ void gemm_epilogue32(const GemmArgs& g, const uint32_
       for (int i = 0; i < 8; i++) h[i] = __float2bfloat16(g.silu ? silu(z[i]) : z[i]);
       if (g.Hbf16) {
         __nv_bfloat16* dst = g.Hbf16 + (long long)m * g.ldh + nb;
-        if (full8 && (g.ldh % 8 == 0)) {
+        if (full8 && (g.ldh % 8 == 0) && (reinterpret_cast<uintptr_t>(g.Hbf16) & 15) == 0) {
           *reinterpret_cast<uint4*>(dst) = *reinterpret_cast<const uint4*>(h);
         } else {
 #pragma unroll
