@@ -47,8 +47,8 @@ class GlslTables(ctypes.Structure):
 
 
 def build_library(force: bool = False) -> str:
-    if force or not os.path.exists(_LIB_PATH):
-        subprocess.run(["make", "-s", "-C", _HERE], check=True)
+    # make is incremental: it rebuilds only when a source changed
+    subprocess.run(["make", "-s", "-C", _HERE] + (["-B"] if force else []), check=True)
     return _LIB_PATH
 
 
@@ -425,3 +425,93 @@ def glsl_query(tables: dict, kind: int, light, p, q, weight_bits: int = 0):
     f3 = lambda x: (ctypes.c_float * 3)(*[float(v) for v in x])  # noqa: E731
     lib().oracle_glsl_query(ctypes.byref(t), kind, f3(light), f3(p), f3(q), o)
     return np.array(o[:], dtype=np.float64)
+
+
+# --- cloud-noise builders (noise_oracle.c) ----------------------------------------
+
+def worley(divisions: int, size: int, grid):
+    """worley-noise (worley.clj:96-109) for a given point grid [d][d][d][3]."""
+    g = np.ascontiguousarray(grid, dtype=np.float64)
+    assert g.shape == (divisions, divisions, divisions, 3)
+    out = np.zeros(size ** 3, np.float64)
+    lib().noise_worley(divisions, size, g.ctypes.data_as(_dp), out.ctypes.data_as(_dp))
+    return out
+
+
+def worley_closest(grid, divisions: int, size: int, point):
+    """closest-distance-to-point-in-grid on a grid [nk][nj][ni][3]."""
+    g = np.ascontiguousarray(grid, dtype=np.float64)
+    f = lib().noise_worley_closest_grid
+    f.restype = ctypes.c_double
+    return f(g.ctypes.data_as(_dp), g.shape[0], g.shape[1], g.shape[2], divisions, size, _v(point))
+
+
+def perlin(divisions: int, size: int, gradients):
+    """perlin-noise (perlin.clj:122-133) for gradient indices [d][d][d] into the twelve vectors."""
+    g = np.ascontiguousarray(gradients, dtype=np.int32)
+    assert g.shape == (divisions, divisions, divisions)
+    out = np.zeros(size ** 3, np.float64)
+    lib().noise_perlin(divisions, size, g.ctypes.data_as(_ip), out.ctypes.data_as(_dp))
+    return out
+
+
+def perlin_sample(gradients, divisions: int, size: int, cell):
+    g = np.ascontiguousarray(gradients, dtype=np.int32)
+    f = lib().noise_perlin_sample
+    f.restype = ctypes.c_double
+    return f(g.ctypes.data_as(_ip), divisions, size, _v(cell))
+
+
+def perlin_ease(t: float) -> float:
+    f = lib().noise_perlin_ease
+    f.restype = ctypes.c_double
+    f.argtypes = [ctypes.c_double]
+    return f(t)
+
+
+def blue(m: int, seed_indices, sigma: float):
+    """blue-noise (bluenoise.clj:162-172) from the given seed pixels; returns m*m ranks."""
+    seed = np.ascontiguousarray(seed_indices, dtype=np.int32)
+    out = np.zeros(m * m, np.int32)
+    f = lib().noise_blue
+    f.argtypes = [ctypes.c_int, ctypes.c_int, _ip, ctypes.c_double, _ip]
+    assert f(m, len(seed), seed.ctypes.data_as(_ip), sigma, out.ctypes.data_as(_ip)) == 0
+    return out
+
+
+def blue_table(m: int, sigma: float):
+    t = np.zeros((m // 2 + 1) ** 2, np.float64)
+    f = lib().noise_blue_table
+    f.argtypes = [ctypes.c_int, ctypes.c_double, _dp]
+    f(m, sigma, t.ctypes.data_as(_dp))
+    return t
+
+
+def blue_density_array(mask, m: int, sigma: float):
+    msk = np.ascontiguousarray(mask, dtype=np.uint8)
+    t = blue_table(m, sigma)
+    out = np.zeros(m * m, np.float64)
+    lib().noise_blue_density_array(msk.ctypes.data_as(ctypes.POINTER(ctypes.c_ubyte)), m, t.ctypes.data_as(_dp),
+                                   out.ctypes.data_as(_dp))
+    return out
+
+
+def blue_seed_pattern(mask, m: int, sigma: float):
+    msk = np.array(mask, dtype=np.uint8)
+    t = blue_table(m, sigma)
+    lib().noise_blue_seed_pattern(msk.ctypes.data_as(ctypes.POINTER(ctypes.c_ubyte)), m, t.ctypes.data_as(_dp))
+    return msk.astype(bool)
+
+
+def blue_wrap(x: int, m: int) -> int:
+    return lib().noise_blue_wrap(x, m)
+
+
+def blue_phase(phase: int, mask, m: int, n: int, sigma: float, dither):
+    """dither-phase1/2/3 (bluenoise.clj:127-169) from a mask; returns (dither, mask after the phase)."""
+    msk = np.array(mask, dtype=np.uint8)
+    d = np.array(dither, dtype=np.int32)
+    f = lib().noise_blue_phase
+    f.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_ubyte), ctypes.c_int, ctypes.c_int, ctypes.c_double, _ip]
+    f(phase, msk.ctypes.data_as(ctypes.POINTER(ctypes.c_ubyte)), m, n, sigma, d.ctypes.data_as(_ip))
+    return d, msk.astype(bool)

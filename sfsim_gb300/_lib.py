@@ -26,7 +26,7 @@ EXPORTS = (
     "sfsim_atmo_context_tables", "sfsim_atmo_context_point_scatter_sum", "sfsim_atmo_query_table",
     "sfsim_atmo_query_direct", "sfsim_atmo_gemm_bf16", "sfsim_atmo_surrogate_train",
     "sfsim_atmo_surrogate_parameters", "sfsim_atmo_surrogate_gradients", "sfsim_atmo_query_surrogate",
-    "sfsim_atmo_query_coords",
+    "sfsim_atmo_query_coords", "sfsim_noise_worley", "sfsim_noise_perlin", "sfsim_noise_blue",
 )
 
 
@@ -96,6 +96,9 @@ def load(build: bool = False):
     L.sfsim_atmo_query_surrogate.argtypes = [vp, ctypes.c_longlong, vp, vp, vp, vp, ctypes.c_float,
                                              ctypes.POINTER(ctypes.c_longlong), vp]
     L.sfsim_atmo_query_coords.argtypes = [vp, ctypes.c_longlong, vp, vp, vp, vp, vp]
+    L.sfsim_noise_worley.argtypes = [ctypes.c_int, ctypes.c_int, vp, vp]
+    L.sfsim_noise_perlin.argtypes = [ctypes.c_int, ctypes.c_int, vp, vp]
+    L.sfsim_noise_blue.argtypes = [ctypes.c_int, ctypes.c_int, vp, ctypes.c_double, vp]
     L.sfsim_atmo_version.argtypes = []
     L.sfsim_atmo_version.restype = ctypes.c_char_p
     _lib = L

@@ -11,6 +11,7 @@
 #include <vector>
 
 #include "../../include/sfsim_atmo.h"
+#include "../../include/sfsim_noise.h"
 #include "atmo_device.cuh"
 #include "kernels.h"
 
@@ -1575,6 +1576,136 @@ int sfsim_atmo_query_surrogate(sfsim_atmo_context* ctx, long long n, const doubl
     if (!rc) rc = check_error_flag(S, st);
   }
   return rc;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Cloud-noise builders (include/sfsim_noise.h)
+// ---------------------------------------------------------------------------
+
+namespace {
+
+// Device allocations of one call, freed on every return path.
+struct DeviceScratch {
+  std::vector<void*> ptrs;
+  template <class T>
+  T* get(size_t count) {
+    void* p = nullptr;
+    if (cudaMalloc(&p, sizeof(T) * (count ? count : 1)) != cudaSuccess) {
+      cudaGetLastError();
+      return nullptr;
+    }
+    ptrs.push_back(p);
+    return static_cast<T*>(p);
+  }
+  ~DeviceScratch() {
+    for (void* p : ptrs) cudaFree(p);
+  }
+};
+
+int noise_prologue(cudaStream_t* st) {
+  int dev = 0, rc = 0;
+  if ((rc = current_device(&dev))) return rc;
+  if ((rc = ensure_stream(dev))) return rc;
+  *st = g_stream[dev];
+  return 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+int sfsim_noise_worley(int divisions, int size, const double* grid, float* out) {
+  if (!grid || !out) return fail(SFSIM_ATMO_ENULL, "NULL argument");
+  if (divisions < 1 || size < 1 || size % divisions != 0 || size > 1024)
+    return fail(SFSIM_ATMO_EINVAL, "need 1 <= divisions, size <= 1024 and size a multiple of divisions");
+  const long long nc = (long long)divisions * divisions * divisions, n = (long long)size * size * size;
+  for (long long c = 0; c < 3 * nc; c++)
+    if (!std::isfinite(grid[c])) return fail(SFSIM_ATMO_EINVAL, "grid points must be finite");
+  std::lock_guard<std::mutex> lock(g_mutex);
+  cudaStream_t st;
+  int rc = noise_prologue(&st);
+  if (rc) return rc;
+  DeviceScratch d;
+  double* g = d.get<double>(3 * nc);
+  float4* local = d.get<float4>(nc);
+  float* o = d.get<float>(n);
+  unsigned int* mx = d.get<unsigned int>(1);
+  if (!g || !local || !o || !mx) return fail(SFSIM_ATMO_ENOMEM, "Worley noise allocation failed");
+  CUDA_TRY(cudaMemcpyAsync(g, grid, sizeof(double) * 3 * nc, cudaMemcpyHostToDevice, st));
+  CUDA_TRY(cudaMemsetAsync(mx, 0, sizeof(unsigned int), st));
+  launch_worley(divisions, size, g, local, o, mx, st);
+  CUDA_TRY(cudaGetLastError());
+  CUDA_TRY(cudaMemcpyAsync(out, o, sizeof(float) * n, cudaMemcpyDeviceToHost, st));
+  CUDA_TRY(cudaStreamSynchronize(st));
+  return 0;
+}
+
+int sfsim_noise_perlin(int divisions, int size, const int* gradients, float* out) {
+  if (!gradients || !out) return fail(SFSIM_ATMO_ENULL, "NULL argument");
+  if (divisions < 1 || size < 1 || size > 1024) return fail(SFSIM_ATMO_EINVAL, "need divisions >= 1, 1 <= size <= 1024");
+  const long long nc = (long long)divisions * divisions * divisions, n = (long long)size * size * size;
+  for (long long c = 0; c < nc; c++)
+    if (gradients[c] < 0 || gradients[c] > 11) return fail(SFSIM_ATMO_EINVAL, "gradient indices must be in [0, 11]");
+  std::lock_guard<std::mutex> lock(g_mutex);
+  cudaStream_t st;
+  int rc = noise_prologue(&st);
+  if (rc) return rc;
+  DeviceScratch d;
+  int* gi = d.get<int>(nc);
+  float* o = d.get<float>(n);
+  unsigned int* range = d.get<unsigned int>(2);
+  if (!gi || !o || !range) return fail(SFSIM_ATMO_ENOMEM, "Perlin noise allocation failed");
+  const unsigned int init[2] = {0xFFFFFFFFu, 0u};
+  CUDA_TRY(cudaMemcpyAsync(gi, gradients, sizeof(int) * nc, cudaMemcpyHostToDevice, st));
+  CUDA_TRY(cudaMemcpyAsync(range, init, sizeof(init), cudaMemcpyHostToDevice, st));
+  launch_perlin(divisions, size, gi, o, range, st);
+  CUDA_TRY(cudaGetLastError());
+  CUDA_TRY(cudaMemcpyAsync(out, o, sizeof(float) * n, cudaMemcpyDeviceToHost, st));
+  CUDA_TRY(cudaStreamSynchronize(st));
+  return 0;
+}
+
+int sfsim_noise_blue(int m, int n, const int* seed, double sigma, int* dither) {
+  if (!seed || !dither) return fail(SFSIM_ATMO_ENULL, "NULL argument");
+  if (m < 2 || m > 512) return fail(SFSIM_ATMO_EINVAL, "m must be in [2, 512]");
+  const int total = m * m;
+  if (n < 1 || n > total / 2) return fail(SFSIM_ATMO_EINVAL, "n must be in [1, m*m/2]");
+  if (!(sigma > 0) || !std::isfinite(sigma)) return fail(SFSIM_ATMO_EINVAL, "sigma must be positive");
+  std::vector<unsigned char> seen(total, 0);
+  for (int t = 0; t < n; t++) {
+    if (seed[t] < 0 || seed[t] >= total || seen[seed[t]])
+      return fail(SFSIM_ATMO_EINVAL, "seed pixels must be distinct indices in [0, m*m)");
+    seen[seed[t]] = 1;
+  }
+  // Gauss weights by |dx|, |dy| with the host's exp, as density-function
+  // (bluenoise.clj:50-53) evaluates them
+  const int h = m / 2 + 1;
+  std::vector<double> table((size_t)h * h);
+  for (int y = 0; y < h; y++)
+    for (int x = 0; x < h; x++) table[(size_t)y * h + x] = std::exp(-((double)(x * x + y * y) / (2.0 * sigma * sigma)));
+  std::lock_guard<std::mutex> lock(g_mutex);
+  cudaStream_t st;
+  int rc = noise_prologue(&st);
+  if (rc) return rc;
+  DeviceScratch d;
+  int* sd = d.get<int>(n);
+  double* tb = d.get<double>(table.size());
+  double* dens = d.get<double>(total);
+  double* dens0 = d.get<double>(total);
+  unsigned char* mask = d.get<unsigned char>(total);
+  unsigned char* work = d.get<unsigned char>(total);
+  int* dith = d.get<int>(total);
+  if (!sd || !tb || !dens || !dens0 || !mask || !work || !dith) return fail(SFSIM_ATMO_ENOMEM, "blue noise allocation failed");
+  CUDA_TRY(cudaMemcpyAsync(sd, seed, sizeof(int) * n, cudaMemcpyHostToDevice, st));
+  CUDA_TRY(cudaMemcpyAsync(tb, table.data(), sizeof(double) * table.size(), cudaMemcpyHostToDevice, st));
+  if (launch_blue_noise(m, n, sd, sigma, tb, dens, dens0, mask, work, dith, st))
+    return fail(SFSIM_ATMO_ECUDA, "blue noise launch configuration failed");
+  CUDA_TRY(cudaGetLastError());
+  CUDA_TRY(cudaMemcpyAsync(dither, dith, sizeof(int) * total, cudaMemcpyDeviceToHost, st));
+  CUDA_TRY(cudaStreamSynchronize(st));
+  return 0;
 }
 
 }  // extern "C"

@@ -197,4 +197,15 @@ void launch_to_bf16(long long count, const float* w, int rows, int cols, __nv_bf
 void launch_gather_batch(long long n, unsigned long long seed, float node_frac, const float* poolA, long long na,
                          const float* poolB, long long nb, float* coords, float* target, cudaStream_t st);
 
+// ---- cloud-noise builders (k_noise.cu) ----
+// max_bits (one uint, zeroed) and range (two uints: 0xFFFFFFFF, 0) are scratch.
+void launch_worley(int divisions, int size, const double* grid, float4* local, float* out, unsigned int* max_bits,
+                   cudaStream_t st);
+void launch_perlin(int divisions, int size, const int* gradients, float* out, unsigned int* range, cudaStream_t st);
+// density, mask and work are used only when the state does not fit in
+// shared memory (blue_noise_smem sets use_smem false).
+size_t blue_noise_smem(int m, bool* use_smem);
+int launch_blue_noise(int m, int n, const int* seed, double sigma, const double* table, double* density,
+                      double* density0, unsigned char* mask, unsigned char* work, int* dither, cudaStream_t st);
+
 }  // namespace sfsim
