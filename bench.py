@@ -240,6 +240,7 @@ def run_ours(args):
 
     sweep = run_sweep(L, A, C) if args.extras else None
     queries = run_queries(C) if args.extras else None
+    noise_builders = run_noise() if args.extras else None
 
     if world > 1:
         dist.barrier()
@@ -268,6 +269,7 @@ def run_ours(args):
             "cpu_baseline": cpu,
             "sweep": sweep,
             "queries": queries,
+            "noise": noise_builders,
         }
         print(json.dumps(result), flush=True)
     if world > 1:
@@ -335,6 +337,49 @@ def query_error_stats(a, ref):
     q = torch.quantile(e[: 1 << 20].double(), torch.tensor([0.5, 0.9, 0.99], device=e.device, dtype=torch.float64))
     return {"median": float(q[0]), "p90": float(q[1]), "p99": float(q[2]), "max": float(e.max()),
             "frac_le_1e-3": float((e <= 1e-3).double().mean()), "frac_le_1e-2": float((e <= 1e-2).double().mean())}
+
+
+def run_noise():
+    """The cloud-noise build steps through the C ABI (host arrays in and out,
+    allocation and copies included) against the oracle's single-threaded C
+    restatement on the same random inputs, at the reference's default sizes
+    and at larger ones."""
+    import time as _t
+
+    import numpy as np
+
+    from oracle import oracle as O
+    from sfsim_gb300 import noise
+
+    def timed(fn, reps=3):
+        fn()
+        best = None
+        for _ in range(reps):
+            t0 = _t.perf_counter()
+            r = fn()
+            dt = _t.perf_counter() - t0
+            best = dt if best is None else min(best, dt)
+        return best * 1e3, r
+
+    out = {}
+    rng = np.random.default_rng(7)
+    for d, size in ((4, 16), (8, 128)):
+        grid = noise.random_point_grid(d, size, rng)
+        g_ms, g = timed(lambda: noise.worley_noise(d, size, grid=grid))
+        c_ms, c = timed(lambda: O.worley(d, size, grid), reps=1)
+        out[f"worley_{size}^3_div{d}"] = {"gpu_ms": g_ms, "cpu_oracle_ms": c_ms, "max_abs_diff": float(np.abs(g - c).max())}
+        grad = noise.random_gradient_grid(d, rng)
+        g_ms, g = timed(lambda: noise.perlin_noise(d, size, gradients=grad))
+        c_ms, c = timed(lambda: O.perlin(d, size, grad), reps=1)
+        out[f"perlin_{size}^3_div{d}"] = {"gpu_ms": g_ms, "cpu_oracle_ms": c_ms, "max_abs_diff": float(np.abs(g - c).max())}
+    for m in (64, 128):
+        pixels = rng.permutation(m * m)[: (m * m) // 10]
+        g_ms, g = timed(lambda: noise.blue_noise(m, sigma=1.5, seed_pixels=pixels), reps=2)
+        c_ms, c = timed(lambda: O.blue(m, pixels, 1.5), reps=1)
+        out[f"bluenoise_{m}x{m}"] = {"gpu_ms": g_ms, "cpu_oracle_ms": c_ms, "ranks_equal": bool(np.array_equal(g, c))}
+    out["note"] = ("GPU times through sfsim_noise_* with host buffers; CPU = the FP64 C oracle, one thread, "
+                   "same random inputs")
+    return out
 
 
 MLP_FLOPS_PER_QUERY = 2 * (192 * 256 + 3 * 256 * 256 + 256 * 4)
