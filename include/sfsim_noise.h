@@ -34,7 +34,7 @@ int sfsim_noise_perlin(int divisions, int size, const int* gradients, float* out
 
 /* Blue noise by void and cluster, replaces blue-noise
  * (src/clj/sfsim/bluenoise.clj:162-172).  seed: the n distinct pixel
- * indices in [0, m*m) that pick-n chose, 1 <= n <= m*m/2; sigma: the width of the Gauss
+ * indices in [0, m*m) that pick-n chose, 1 <= n <= m*m/2, 2 <= m <= 256; sigma: the width of the Gauss
  * density function.  dither: m*m ranks (the reference's dither array).  The
  * densities are FP64 with the reference's order of operations per pixel. */
 int sfsim_noise_blue(int m, int n, const int* seed, double sigma, int* dither);

@@ -1669,7 +1669,7 @@ int sfsim_noise_perlin(int divisions, int size, const int* gradients, float* out
 
 int sfsim_noise_blue(int m, int n, const int* seed, double sigma, int* dither) {
   if (!seed || !dither) return fail(SFSIM_ATMO_ENULL, "NULL argument");
-  if (m < 2 || m > 512) return fail(SFSIM_ATMO_EINVAL, "m must be in [2, 512]");
+  if (m < 2 || m > 256) return fail(SFSIM_ATMO_EINVAL, "m must be in [2, 256]");
   const int total = m * m;
   if (n < 1 || n > total / 2) return fail(SFSIM_ATMO_EINVAL, "n must be in [1, m*m/2]");
   if (!(sigma > 0) || !std::isfinite(sigma)) return fail(SFSIM_ATMO_EINVAL, "sigma must be positive");

@@ -150,53 +150,54 @@ __global__ void k_perlin_finish(long long n, const unsigned int* range, float* o
 }
 
 // ------------------------------------------------------------ blue noise
+//
+// The void-and-cluster steps are sequential: one CTA of 1024 threads runs
+// them (k_blue_seed, k_blue_phases, k_blue_phase3) with the state in shared
+// memory when it fits.  The full density sums (density-array), m^4 FP64
+// additions each, run between them on every SM (k_blue_density).
 
 constexpr int kBlueThreads = 1024;
 
 struct BlueArgs {
   int m;
   double sigma;
-  const int* seed;  // n pixel indices
+  const int* seed;       // n pixel indices
   int n;
-  const double* table;  // Gauss weights [|dy|][|dx|], (m/2 + 1)^2
-  double* density;      // m*m (shared memory when it fits, else this global array)
-  double* density0;     // m*m global scratch
-  unsigned char* mask;  // m*m global scratch (used when shared memory is too small)
-  unsigned char* work;
-  int* dither;          // m*m output
-  int use_smem;
+  const double* table;   // Gauss weights [|dy|][|dx|], (m/2 + 1)^2
+  double* density;       // m*m global scratch
+  double* density0;      // m*m: the density of the seed pattern
+  unsigned char* mask;   // m*m: the seed mask, then the seed pattern
+  unsigned char* work;   // m*m: the complement of the half-filled pattern
+  int* dither;           // m*m output ranks
+  int use_smem;          // the single-CTA kernels keep density and mask in shared memory
 };
 
-__device__ __forceinline__ int wrap_m(int x, int m) {
-  const int offset = m >> 1;
-  int r = (x + offset) % m;
-  if (r < 0) r += m;
-  return r - offset;
+// Order-preserving integer key of a double (no NaN; the densities are never
+// -0.0): comparisons and reductions run on the integer pipes, not FP64.
+__device__ __forceinline__ unsigned long long okey(double d) {
+  const unsigned long long u = (unsigned long long)__double_as_longlong(d);
+  return (u >> 63) ? ~u : (u | 0x8000000000000000ull);
 }
 
-// Best (value, index) under "larger value wins, equal values: larger index"
-// (max-key / min-key keep the last of equal elements); min searches negate.
+// Candidate (key, index) under "larger key wins, equal keys: larger index"
+// (max-key / min-key keep the last of equal elements); arg-min searches
+// complement the key.
 struct Best {
-  double v;
+  unsigned long long k;
   int i;
 };
 __device__ __forceinline__ Best better(Best a, Best b) {
   if (b.i < 0) return a;
   if (a.i < 0) return b;
-  if (b.v > a.v || (b.v == a.v && b.i > a.i)) return b;
+  if (b.k > a.k || (b.k == a.k && b.i > a.i)) return b;
   return a;
 }
 
-// Block-wide arg-extremum over pixels whose mask equals `want`: arg max of
-// density (sign +1) or arg min (sign -1).  All threads get the index.
-__device__ int block_arg(const double* density, const unsigned char* mask, int total, unsigned char want,
-                         double sign, Best* red) {
-  Best b{0.0, -1};
-  for (int p = threadIdx.x; p < total; p += kBlueThreads)
-    if (mask[p] == want) b = better(b, Best{sign * density[p], p});
+// Block-wide reduction of each thread's candidate; all threads get the index.
+__device__ int block_best(Best b, Best* red) {
   for (int o = 16; o > 0; o >>= 1) {
     Best c;
-    c.v = __shfl_xor_sync(0xffffffffu, b.v, o);
+    c.k = __shfl_xor_sync(0xffffffffu, b.k, o);
     c.i = __shfl_xor_sync(0xffffffffu, b.i, o);
     b = better(b, c);
   }
@@ -206,7 +207,7 @@ __device__ int block_arg(const double* density, const unsigned char* mask, int t
     Best c = red[threadIdx.x];
     for (int o = 16; o > 0; o >>= 1) {
       Best e;
-      e.v = __shfl_xor_sync(0xffffffffu, c.v, o);
+      e.k = __shfl_xor_sync(0xffffffffu, c.k, o);
       e.i = __shfl_xor_sync(0xffffffffu, c.i, o);
       c = better(c, e);
     }
@@ -214,7 +215,7 @@ __device__ int block_arg(const double* density, const unsigned char* mask, int t
   }
   __syncthreads();
   const int r = red[32].i;
-  __syncthreads();  // red is reused by the next search
+  __syncthreads();  // red is reused by the next reduction
   return r;
 }
 
@@ -222,117 +223,206 @@ __device__ __forceinline__ double weight(const double* table, int h, int dx, int
   return table[abs(dy) * h + abs(dx)];
 }
 
-// density-change (bluenoise.clj:99-109) of every pixel by +/- the weight of
-// its offset from `index`
-__device__ void change(double* density, int m, const double* table, int index, bool add) {
-  const int cy = index / m, cx = index % m, h = (m >> 1) + 1, total = m * m;
-  for (int p = threadIdx.x; p < total; p += kBlueThreads) {
-    const double f = weight(table, h, wrap_m(p % m - cx, m), wrap_m(p / m - cy, m));
-    density[p] = add ? density[p] + f : density[p] - f;
-  }
+// x - cx wrapped into [-m/2, m - m/2) (wrap, bluenoise.clj:72-76) for
+// |x - cx| < m
+__device__ __forceinline__ int wrap_near(int d, int m) {
+  const int half = m >> 1;
+  return d < -half ? d + m : d >= m - half ? d - m : d;
 }
 
-// density-array (bluenoise.clj:79-96): each pixel sums over the set pixels
-// in row-major order, as density-sample does
-__device__ void density_array(double* density, const unsigned char* mask, int m, const double* table) {
+// The pixels of this thread, p = threadIdx.x + k * kBlueThreads, walked with
+// their (x, y) so that the hot loop has no division.
+struct Walk {
+  int m, x0, y0, sx, sy;
+  __device__ explicit Walk(int m_) : m(m_) {
+    x0 = threadIdx.x % m_;
+    y0 = threadIdx.x / m_;
+    sx = kBlueThreads % m_;
+    sy = kBlueThreads / m_;
+  }
+};
+
+// Arg-extremum over pixels whose mask equals `want`, without changes: arg max
+// of the density, or arg min when `least`.
+__device__ int search(const double* density, const unsigned char* mask, int total, unsigned char want, bool least,
+                      Best* red) {
+  Best b{0ull, -1};
+  for (int p = threadIdx.x; p < total; p += kBlueThreads)
+    if (mask[p] == want) {
+      const unsigned long long k = okey(density[p]);
+      b = better(b, Best{least ? ~k : k, p});
+    }
+  return block_best(b, red);
+}
+
+// One step: mask[c] = mask_c and density-change (bluenoise.clj:99-109) by
+// +/- the weight of every pixel's offset from c; in the same pass the
+// arg-extremum of the next search over the updated pixels (mask == want).
+__device__ int step(double* density, unsigned char* mask, const Walk& w, int total, const double* table, int c,
+                    bool add, unsigned char mask_c, unsigned char want, bool least, Best* red) {
+  const int m = w.m, h = (m >> 1) + 1, cy = c / m, cx = c - cy * m;
+  Best b{0ull, -1};
+  int x = w.x0, y = w.y0;
+  for (int p = threadIdx.x; p < total; p += kBlueThreads) {
+    if (p == c) mask[p] = mask_c;
+    const double f = weight(table, h, wrap_near(x - cx, m), wrap_near(y - cy, m));
+    const double d = add ? __dadd_rn(density[p], f) : __dsub_rn(density[p], f);
+    density[p] = d;
+    if (mask[p] == want) {
+      const unsigned long long k = okey(d);
+      b = better(b, Best{least ? ~k : k, p});
+    }
+    x += w.sx;
+    y += w.sy;
+    if (x >= m) {
+      x -= m;
+      y += 1;
+    }
+  }
+  return block_best(b, red);
+}
+
+// density-array (bluenoise.clj:79-96) on every SM: pixel p sums the weights
+// of the set pixels in row-major order, as density-sample does.  One warp
+// per pixel row segment would reorder the sum; one thread per pixel keeps it.
+__global__ void k_blue_density(int m, const double* __restrict__ table, const unsigned char* __restrict__ mask,
+                               double* density) {
+  extern __shared__ __align__(16) unsigned char dsm[];
   const int h = (m >> 1) + 1, total = m * m;
-  for (int p = threadIdx.x; p < total; p += kBlueThreads) {
-    const int cy = p / m, cx = p % m;
-    double s = 0.0;
-    for (int y = 0; y < m; y++)
-      for (int x = 0; x < m; x++)
-        if (mask[y * m + x]) s += weight(table, h, wrap_m(x - cx, m), wrap_m(y - cy, m));
-    density[p] = s;
+  double* tb = reinterpret_cast<double*>(dsm);
+  unsigned char* mk = dsm + sizeof(double) * h * h;
+  for (int t = threadIdx.x; t < h * h; t += blockDim.x) tb[t] = table[t];
+  for (int t = threadIdx.x; t < total; t += blockDim.x) mk[t] = mask[t];
+  __syncthreads();
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= total) return;
+  const int cy = p / m, cx = p - cy * m;
+  double s = 0.0;
+  for (int y = 0; y < m; y++) {
+    const int wy = wrap_near(y - cy, m);
+    for (int x = 0; x < m; x++)
+      if (mk[y * m + x]) s = __dadd_rn(s, weight(tb, h, wrap_near(x - cx, m), wy));
   }
+  density[p] = s;
 }
 
-// One CTA runs the whole dithering: seed pattern, phases 1-3 (one arg search
-// and one density change per step, two block barriers each).
-__global__ void __launch_bounds__(kBlueThreads, 1) k_blue_noise(BlueArgs a) {
+// State of the single-CTA kernels: the table always in shared memory, the
+// density and a mask there too when they fit, else in global memory.
+struct BlueState {
+  double* table;
+  double* density;
+  unsigned char* mask;
+};
+
+__device__ BlueState blue_state(const BlueArgs& a, unsigned char* smem, double* g_density, unsigned char* g_mask) {
+  const int m = a.m, total = m * m, h = (m >> 1) + 1;
+  BlueState st;
+  st.table = reinterpret_cast<double*>(smem);
+  unsigned char* base = smem + sizeof(double) * h * h;
+  st.density = a.use_smem ? reinterpret_cast<double*>(base) : g_density;
+  st.mask = a.use_smem ? base + sizeof(double) * total : g_mask;
+  for (int t = threadIdx.x; t < h * h; t += kBlueThreads) st.table[t] = a.table[t];
+  return st;
+}
+
+// seed-pattern (bluenoise.clj:112-124) from a.mask with its density in
+// a.density: remove the tightest cluster, add the largest void, until they
+// coincide; the pattern is left in a.mask.
+__global__ void __launch_bounds__(kBlueThreads, 1) k_blue_seed(BlueArgs a) {
   extern __shared__ __align__(16) unsigned char smem[];
   __shared__ Best red[33];
-  const int m = a.m, total = m * m, h = (m >> 1) + 1;
-  double* table = reinterpret_cast<double*>(smem);
-  unsigned char* base = smem + sizeof(double) * h * h;
-  double* density = a.use_smem ? reinterpret_cast<double*>(base) : a.density;
-  unsigned char* mask = a.use_smem ? base + sizeof(double) * total : a.mask;
-  unsigned char* work = a.use_smem ? mask + total : a.work;
-  for (int t = threadIdx.x; t < h * h; t += kBlueThreads) table[t] = a.table[t];
-  for (int p = threadIdx.x; p < total; p += kBlueThreads) {
-    mask[p] = 0;
-    a.dither[p] = 0;
+  const int m = a.m, total = m * m;
+  const Walk w(m);
+  BlueState st = blue_state(a, smem, a.density, a.mask);
+  if (a.use_smem)
+    for (int p = threadIdx.x; p < total; p += kBlueThreads) {
+      st.density[p] = a.density[p];
+      st.mask[p] = a.mask[p];
+    }
+  __syncthreads();
+  int cluster = search(st.density, st.mask, total, 1, false, red);
+  for (int it = 0; it < total * 4 && cluster >= 0; it++) {  // the pattern settles long before this bound
+    const int vd = step(st.density, st.mask, w, total, st.table, cluster, false, 0, 0, true, red);
+    if (vd < 0) break;  // cannot happen for 1 <= n <= m*m/2
+    if (vd == cluster) {
+      if (threadIdx.x == 0) st.mask[vd] = 1;
+      break;
+    }
+    cluster = step(st.density, st.mask, w, total, st.table, vd, true, 1, 1, false, red);
   }
   __syncthreads();
-  for (int t = threadIdx.x; t < a.n; t += kBlueThreads) mask[a.seed[t]] = 1;
-  __syncthreads();
+  if (a.use_smem)
+    for (int p = threadIdx.x; p < total; p += kBlueThreads) a.mask[p] = st.mask[p];
+}
 
-  // seed-pattern (bluenoise.clj:112-124)
-  density_array(density, mask, m, table);
-  __syncthreads();
-  for (int it = 0; it < total * 4; it++) {  // the pattern settles long before this bound
-    const int cluster = block_arg(density, mask, total, 1, 1.0, red);
-    if (cluster < 0) break;  // no set pixel: cannot happen for 1 <= n <= m*m/2
-    if (threadIdx.x == 0) mask[cluster] = 0;
-    change(density, m, table, cluster, false);
-    __syncthreads();
-    const int vd = block_arg(density, mask, total, 0, -1.0, red);
-    if (vd < 0) break;
-    if (threadIdx.x == 0) mask[vd] = 1;
-    __syncthreads();
-    if (cluster == vd) break;
-    change(density, m, table, vd, true);
-    __syncthreads();
+// dither-phase1 and dither-phase2 (bluenoise.clj:127-154), both from the
+// seed pattern a.mask and its density a.density0: ranks n-1 .. 0 for the
+// removed clusters, n .. m*m/2 - 1 for the filled voids.  The complement of
+// the half-filled pattern is left in a.work for phase 3.
+__global__ void __launch_bounds__(kBlueThreads, 1) k_blue_phases(BlueArgs a) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  __shared__ Best red[33];
+  const int m = a.m, total = m * m;
+  const Walk w(m);
+  BlueState st = blue_state(a, smem, a.density, a.work);
+  for (int p = threadIdx.x; p < total; p += kBlueThreads) {
+    st.mask[p] = a.mask[p];
+    st.density[p] = a.density0[p];
   }
-  density_array(a.density0, mask, m, table);
   __syncthreads();
+  int c = search(st.density, st.mask, total, 1, false, red);
+  for (int r = a.n; r > 0 && c >= 0; r--) {
+    if (threadIdx.x == 0) a.dither[c] = r - 1;
+    c = step(st.density, st.mask, w, total, st.table, c, false, 0, 1, false, red);
+  }
+  __syncthreads();
+  for (int p = threadIdx.x; p < total; p += kBlueThreads) {
+    st.mask[p] = a.mask[p];
+    st.density[p] = a.density0[p];
+  }
+  __syncthreads();
+  c = search(st.density, st.mask, total, 0, true, red);
+  for (int r = a.n; r < total / 2 && c >= 0; r++) {
+    if (threadIdx.x == 0) a.dither[c] = r;
+    c = step(st.density, st.mask, w, total, st.table, c, true, 1, 0, true, red);
+  }
+  __syncthreads();
+  for (int p = threadIdx.x; p < total; p += kBlueThreads) a.work[p] = !st.mask[p];
+}
 
-  // phase 1 (bluenoise.clj:127-140) from the seed pattern
-  for (int p = threadIdx.x; p < total; p += kBlueThreads) {
-    work[p] = mask[p];
-    density[p] = a.density0[p];
-  }
-  __syncthreads();
-  for (int r = a.n; r > 0; r--) {
-    const int cluster = block_arg(density, work, total, 1, 1.0, red);
-    if (cluster < 0) break;
-    change(density, m, table, cluster, false);
-    if (threadIdx.x == 0) {
-      work[cluster] = 0;
-      a.dither[cluster] = r - 1;
+// dither-phase3 (bluenoise.clj:157-169) on the complement a.work with its
+// density a.density: ranks m*m/2 .. m*m - 1 for the removed clusters.
+__global__ void __launch_bounds__(kBlueThreads, 1) k_blue_phase3(BlueArgs a) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  __shared__ Best red[33];
+  const int m = a.m, total = m * m;
+  const Walk w(m);
+  BlueState st = blue_state(a, smem, a.density, a.work);
+  if (a.use_smem)
+    for (int p = threadIdx.x; p < total; p += kBlueThreads) {
+      st.mask[p] = a.work[p];
+      st.density[p] = a.density[p];
     }
-    __syncthreads();
-  }
-  // phase 2 (bluenoise.clj:143-154) from the seed pattern
-  for (int p = threadIdx.x; p < total; p += kBlueThreads) {
-    work[p] = mask[p];
-    density[p] = a.density0[p];
-  }
   __syncthreads();
-  for (int r = a.n; r < total / 2; r++) {
-    const int vd = block_arg(density, work, total, 0, -1.0, red);
-    if (vd < 0) break;
-    change(density, m, table, vd, true);
-    if (threadIdx.x == 0) {
-      work[vd] = 1;
-      a.dither[vd] = r;
-    }
-    __syncthreads();
+  int c = search(st.density, st.mask, total, 1, false, red);
+  for (int r = total / 2; r < total && c >= 0; r++) {
+    if (threadIdx.x == 0) a.dither[c] = r;
+    c = step(st.density, st.mask, w, total, st.table, c, false, 0, 1, false, red);
   }
-  // phase 3 (bluenoise.clj:157-169) on the complement
-  for (int p = threadIdx.x; p < total; p += kBlueThreads) work[p] = !work[p];
-  __syncthreads();
-  density_array(density, work, m, table);
-  __syncthreads();
-  for (int r = total / 2; r < total; r++) {
-    const int cluster = block_arg(density, work, total, 1, 1.0, red);
-    if (cluster < 0) break;
-    change(density, m, table, cluster, false);
-    if (threadIdx.x == 0) {
-      work[cluster] = 0;
-      a.dither[cluster] = r;
-    }
-    __syncthreads();
-  }
+}
+
+// scatter-mask (bluenoise.clj:39-43), first pass: clear the mask and the ranks
+__global__ void k_blue_clear(int total, unsigned char* mask, int* dither) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= total) return;
+  mask[t] = 0;
+  dither[t] = 0;
+}
+
+// second pass: set the n seed pixels
+__global__ void k_blue_seed_set(int n, const int* seed, unsigned char* mask) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < n) mask[seed[t]] = 1;
 }
 
 // ---------------------------------------------------------------- launches
@@ -358,7 +448,7 @@ void launch_perlin(int divisions, int size, const int* gradients, float* out, un
 size_t blue_noise_smem(int m, bool* use_smem) {
   const size_t h = (size_t)(m / 2 + 1);
   const size_t table = sizeof(double) * h * h;
-  const size_t all = table + sizeof(double) * (size_t)m * m + 2 * (size_t)m * m;
+  const size_t all = table + (sizeof(double) + 1) * (size_t)m * m;
   *use_smem = all <= 200 * 1024;
   return *use_smem ? all : table;
 }
@@ -379,9 +469,25 @@ int launch_blue_noise(int m, int n, const int* seed, double sigma, const double*
   bool use = false;
   const size_t smem = blue_noise_smem(m, &use);
   a.use_smem = use ? 1 : 0;
-  if (cudaFuncSetAttribute(k_blue_noise, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+  const int total = m * m, h = m / 2 + 1;
+  const size_t dsmem = sizeof(double) * h * h + (size_t)total;
+  if (dsmem > 220 * 1024) return -1;
+  if (cudaFuncSetAttribute(k_blue_seed, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess ||
+      cudaFuncSetAttribute(k_blue_phases, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess ||
+      cudaFuncSetAttribute(k_blue_phase3, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess ||
+      cudaFuncSetAttribute(k_blue_density, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dsmem) != cudaSuccess)
     return -1;
-  k_blue_noise<<<1, kBlueThreads, smem, st>>>(a);
+  const unsigned dblocks = (unsigned)((total + 255) / 256);
+  // the seed mask, its density, the seed pattern, its density, phases 1-2,
+  // the complement's density, phase 3
+  k_blue_clear<<<(unsigned)((total + 255) / 256), 256, 0, st>>>(total, mask, dither);
+  k_blue_seed_set<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(n, seed, mask);
+  k_blue_density<<<dblocks, 256, dsmem, st>>>(m, table, mask, density);
+  k_blue_seed<<<1, kBlueThreads, smem, st>>>(a);
+  k_blue_density<<<dblocks, 256, dsmem, st>>>(m, table, mask, density0);
+  k_blue_phases<<<1, kBlueThreads, smem, st>>>(a);
+  k_blue_density<<<dblocks, 256, dsmem, st>>>(m, table, work, density);
+  k_blue_phase3<<<1, kBlueThreads, smem, st>>>(a);
   return 0;
 }
 
