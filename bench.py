@@ -228,14 +228,29 @@ def run_ours(args):
     except Exception:
         pass
 
-    # --- roofline of the first-order kernel: SFU-bound
-    counts = (ctypes.c_ulonglong * 6)()
-    _lib.check(L.sfsim_atmo_census(ctypes.byref(cfg), counts, 6), "census")
-    ext_samples = counts[1]
+    # --- rooflines: point scatter (the largest stage, shared-memory gathers)
+    # and the first order (SFU exponentials)
+    counts = (ctypes.c_ulonglong * 9)()
+    _lib.check(L.sfsim_atmo_census(ctypes.byref(cfg), counts, 9), "census")
+    lit, climb = counts[0], counts[6]
+    dir_evals, ground_evals, first_evals = counts[3], counts[7], counts[8]
+    # per direction: the dS heading-row interpolation, 2 corners x RGB float
+    # (24 B); the first iteration's Mie row another 24 B; a ground direction's
+    # 4-corner dE gather 48 B
+    ps_bytes = 24 * dir_evals + 24 * first_evals + 48 * ground_evals
+    smem_peak = ctypes.c_double()
+    _lib.check(L.sfsim_atmo_smem_peak(ctypes.byref(smem_peak)), "smem_peak")
+    ps_ms = stages["point_scatter"]
+    ps_achieved = ps_bytes / (ps_ms * 1e-3) / 1e9
+    smem_peak_g = smem_peak.value / 1e9
     peak = ctypes.c_double()
     _lib.check(L.sfsim_atmo_sfu_peak(ctypes.byref(peak)), "sfu_peak")
     fo_ms = stages["first_order"]
-    achieved = 2.0 * ext_samples / (fo_ms * 1e-3) / 1e9  # two exponentials per extinction sample
+    # exponentials of the first-order stage: the descending sun rays
+    # integrated (2 per sample), 3 transmittances per lit sample, and the sun
+    # table's 2048 x 2048 nodes of S samples (2 each)
+    fo_ex2 = 2 * (lit - climb) * cfg.ray_steps + 3 * lit + 2 * 2048 * 2048 * cfg.ray_steps
+    fo_achieved = fo_ex2 / (fo_ms * 1e-3) / 1e9
     peak_g = peak.value / 1e9
 
     sweep = run_sweep(L, A, C) if args.extras else None
@@ -258,13 +273,23 @@ def run_ours(args):
                     "build_s": e2e_s / args.steps},
             "gpu_launches": launches * args.steps,
             "stage_ms": {k: round(v, 4) for k, v in stages.items()},
-            "roofline": {"bound": "sfu", "kernel": "k_first_order", "achieved": achieved, "peak": peak_g,
-                         "unit": "Gex2/s", "frac": achieved / peak_g if peak_g else None,
+            "roofline": {"bound": "smem", "kernel": "k_point_scatter", "achieved": ps_achieved,
+                         "peak": smem_peak_g, "unit": "GB/s", "frac": ps_achieved / smem_peak_g if smem_peak_g else None,
                          "traffic": None,
-                         "note": ("achieved = 2 exp per sun-ray extinction sample x census count / first-order "
-                                  "event time; peak = ex2.approx throughput measured live on this GPU by "
-                                  "sfsim_atmo_sfu_peak (no SFU figure in MEASURED_PEAKS.json)"),
-                         "ext_samples": ext_samples, "kernel_ms": fo_ms},
+                         "note": ("achieved = algorithmic shared-memory gather bytes of the point-scatter stage "
+                                  "(24 B per direction evaluation for the dS row, 24 B more in the first "
+                                  "iteration, 48 B per ground direction; census counts) / its event time; peak = "
+                                  "conflict-free shared-memory read bandwidth measured live on this GPU by "
+                                  "sfsim_atmo_smem_peak (no such figure in MEASURED_PEAKS.json); DRAM is not "
+                                  "the bound (the tables live in L2)"),
+                         "direction_evaluations": dir_evals, "kernel_ms": ps_ms},
+            "roofline_first_order": {"bound": "sfu", "kernel": "k_first_order", "achieved": fo_achieved,
+                                     "peak": peak_g, "unit": "Gex2/s", "frac": fo_achieved / peak_g if peak_g else None,
+                                     "note": ("exponentials of the stage: 2 per sample of the descending sun rays "
+                                              "integrated directly, 3 transmittances per lit sample, 2 per sample "
+                                              "of the sun table (2048^2 nodes); climbing sun rays are read from "
+                                              "the table; peak = ex2.approx throughput measured live"),
+                                     "lit_pairs": lit, "climbing_pairs": climb, "kernel_ms": fo_ms},
             "clocks": clk,
             "cpu_baseline": cpu,
             "sweep": sweep,

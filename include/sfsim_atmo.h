@@ -273,14 +273,24 @@ int sfsim_atmo_gemm_bf16(const void* A, const void* B, float* C, int M, int N, l
  * sun-ray integrals (node, ray-sample pairs with the sun above the sample's
  * horizon), [1] = their extinction samples, [2] = view-ray extinction
  * samples, [3] = point-scatter direction evaluations, [4] = ray-scatter
- * J lookups, [5] = surface-radiance direction evaluations.  Returns the
- * number of counts written (at most n). */
+ * J lookups, [5] = surface-radiance direction evaluations, [6] = the pairs
+ * of [0] whose sun ray climbs (FP32 builds read those optical depths from a
+ * table instead of integrating them), [7] = the point-scatter direction
+ * evaluations of [3] that end on the ground, [8] = those of the first
+ * iteration (which also reads the Mie strength).  Returns the number of
+ * counts written (at most n). */
 int sfsim_atmo_census(const sfsim_atmo_config* cfg, unsigned long long* counts, int n);
 
 /* Measures the SFU throughput of the current device (ex2.approx.f32
  * operations per second, best of 4 timed launches over all SMs), the
  * denominator of the quadrature kernels' roofline. */
 int sfsim_atmo_sfu_peak(double* ex2_per_second);
+
+/* Measured shared-memory read bandwidth of this GPU (bytes per second, all
+ * SMs, conflict-free 16-byte reads), the roofline denominator of the
+ * shared-memory-gather kernels (point scatter).  No counterpart in the
+ * reference. */
+int sfsim_atmo_smem_peak(double* bytes_per_second);
 
 /* Frees the cached scratch tables of the current device. */
 int sfsim_atmo_release(void);

@@ -26,7 +26,7 @@ EXPORTS = (
     "sfsim_atmo_context_tables", "sfsim_atmo_context_point_scatter_sum", "sfsim_atmo_query_table",
     "sfsim_atmo_query_direct", "sfsim_atmo_gemm_bf16", "sfsim_atmo_surrogate_train",
     "sfsim_atmo_surrogate_parameters", "sfsim_atmo_surrogate_gradients", "sfsim_atmo_query_surrogate",
-    "sfsim_atmo_query_coords", "sfsim_noise_worley", "sfsim_noise_perlin", "sfsim_noise_blue",
+    "sfsim_atmo_query_coords", "sfsim_atmo_smem_peak", "sfsim_noise_worley", "sfsim_noise_perlin", "sfsim_noise_blue",
 )
 
 
@@ -82,6 +82,7 @@ def load(build: bool = False):
     L.sfsim_atmo_last_error.restype = ctypes.c_char_p
     L.sfsim_atmo_census.argtypes = [_cfgp, ctypes.POINTER(ctypes.c_ulonglong), ctypes.c_int]
     L.sfsim_atmo_sfu_peak.argtypes = [ctypes.POINTER(ctypes.c_double)]
+    L.sfsim_atmo_smem_peak.argtypes = [ctypes.POINTER(ctypes.c_double)]
     vp = ctypes.c_void_p
     L.sfsim_atmo_context_create.argtypes = [_cfgp, ctypes.POINTER(vp)]
     L.sfsim_atmo_context_destroy.argtypes = [vp]

@@ -321,10 +321,11 @@ struct Work {
   Vec4<Real>*T, *E0, *dE[2], *Eacc[2];
   Vec4<Real>*S1R, *M, *J, *dS[2], *Sacc[2];
   float *oT, *oE, *oS, *oM;  // device outputs when the caller passes host buffers
+  float2* sun;               // sun-ray optical-depth tables (FP32 builds), or NULL
 };
 
 template <class Real>
-size_t carve(Work<Real>& w, char* base, const BuildDims& d, bool outputs) {
+size_t carve(Work<Real>& w, char* base, const BuildDims& d, bool outputs, bool sun_table = true) {
   Carver c{base};
   const long long B = d.B;
   w.params = c.take<AtmoParams>(B);
@@ -359,6 +360,7 @@ size_t carve(Work<Real>& w, char* base, const BuildDims& d, bool outputs) {
   } else {
     w.oT = w.oE = w.oS = w.oM = nullptr;
   }
+  w.sun = (sun_table && sizeof(Real) == sizeof(float)) ? c.take<float2>(B * (long long)kSunNR * kSunNM) : nullptr;
   return c.off + 256;
 }
 
@@ -433,7 +435,11 @@ int run_build(const Work<Real>& w, const BuildDims& d, float* oT, float* oE, flo
   launches++;
   tm.mark_end();
   tm.mark_begin(3);
-  launch_first_order<Real>(w.params, d, w.setup.rowinfo, w.setup.rows, w.setup.geom, w.S1R, w.M, st);
+  if (w.sun) {
+    launch_sun_table(w.params, d, w.sun, st);
+    launches++;
+  }
+  launch_first_order<Real>(w.params, d, w.setup.rowinfo, w.setup.rows, w.setup.geom, w.sun, w.S1R, w.M, st);
   launches++;
   tm.mark_end();
   CUDA_TRY(cudaGetLastError());
@@ -633,9 +639,9 @@ int census_impl(const sfsim_atmo_config& cfg, unsigned long long* out, int n) {
   std::vector<int> ring_end;
   sphere_directions(cfg.sphere_steps >> 1, cfg.sphere_steps, M_PI, dirs, ring_end);
   Work<Real> w;
-  size_t bytes = carve<Real>(w, nullptr, d, false);
+  size_t bytes = carve<Real>(w, nullptr, d, false, false);
   if ((rc = ensure_arena(dev, bytes + 256))) return rc;
-  carve<Real>(w, (char*)g_arena[dev].base, d, false);
+  carve<Real>(w, (char*)g_arena[dev].base, d, false, false);
   unsigned long long* dcount = reinterpret_cast<unsigned long long*>((char*)g_arena[dev].base + bytes);
   cudaStream_t st = g_stream[dev];
   CUDA_TRY(cudaMemcpyAsync(w.params, &hp, sizeof(AtmoParams), cudaMemcpyHostToDevice, st));
@@ -643,21 +649,32 @@ int census_impl(const sfsim_atmo_config& cfg, unsigned long long* out, int n) {
     CUDA_TRY(cudaMemcpyAsync(w.dirs, dirs.data(), sizeof(DirLocal) * dirs.size(), cudaMemcpyHostToDevice, st));
     CUDA_TRY(cudaMemcpyAsync(w.ring_end, ring_end.data(), sizeof(int) * ring_end.size(), cudaMemcpyHostToDevice, st));
   }
-  CUDA_TRY(cudaMemsetAsync(dcount, 0, sizeof(unsigned long long), st));
+  CUDA_TRY(cudaMemsetAsync(dcount, 0, 2 * sizeof(unsigned long long), st));
   launch_setup<Real>(w.params, d, w.dirs, w.ring_end, w.setup, st);
   launch_first_order_census<Real>(w.params, d, w.setup.rowinfo, w.setup.rows, w.setup.geom, dcount, st);
   CUDA_TRY(cudaGetLastError());
-  unsigned long long lit = 0;
-  CUDA_TRY(cudaMemcpyAsync(&lit, dcount, sizeof(lit), cudaMemcpyDeviceToHost, st));
+  unsigned long long cnt[2] = {0, 0};
+  CUDA_TRY(cudaMemcpyAsync(cnt, dcount, sizeof(cnt), cudaMemcpyDeviceToHost, st));
   CUDA_TRY(cudaStreamSynchronize(st));
+  const unsigned long long lit = cnt[0], climb = cnt[1];
+  // ground directions of the point-scatter sphere per height
+  std::vector<SphereDir<Real>> sd((size_t)d.n0 * (d.P + 1));
+  CUDA_TRY(cudaMemcpy(sd.data(), w.setup.sdirs, sizeof(SphereDir<Real>) * sd.size(), cudaMemcpyDeviceToHost));
+  unsigned long long ground = 0;
+  for (int i = 0; i < d.n0; i++)
+    for (int k = 0; k < d.P; k++) ground += sd[(size_t)i * d.P + k].surface ? 1 : 0;
   const unsigned long long S = (unsigned long long)d.S, it = (unsigned long long)d.iterations;
-  const unsigned long long vals[6] = {lit,
+  const unsigned long long per_height = (unsigned long long)d.n1 * d.n2 * d.n3;
+  const unsigned long long vals[9] = {lit,
                                       lit * S,
                                       (unsigned long long)d.rows() * S * S,
                                       (unsigned long long)d.n4() * d.P * it,
                                       (unsigned long long)d.n4() * S * it,
-                                      (unsigned long long)d.nE() * d.Ph * it};
-  int m = n < 6 ? n : 6;
+                                      (unsigned long long)d.nE() * d.Ph * it,
+                                      climb,
+                                      ground * per_height * it,
+                                      it > 0 ? (unsigned long long)d.n4() * d.P : 0ull};
+  int m = n < 9 ? n : 9;
   for (int i = 0; i < m; i++) out[i] = vals[i];
   return m;
 }
@@ -706,6 +723,41 @@ int sfsim_atmo_sfu_peak(double* ex2_per_second) {
   cudaEventDestroy(e1);
   CUDA_TRY(cudaFree(sink));
   *ex2_per_second = best;
+  return 0;
+}
+
+int sfsim_atmo_smem_peak(double* bytes_per_second) {
+  if (!bytes_per_second) return fail(SFSIM_ATMO_ENULL, "bytes_per_second is NULL");
+  std::lock_guard<std::mutex> lock(g_mutex);
+  int dev = 0;
+  int rc = current_device(&dev);
+  if (rc) return rc;
+  if ((rc = ensure_stream(dev))) return rc;
+  int sms = 0;
+  CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  const int blocks = sms, iters = 4096;
+  float* sink = nullptr;
+  CUDA_TRY(cudaMalloc(&sink, sizeof(float) * blocks));
+  cudaStream_t st = g_stream[dev];
+  cudaEvent_t e0, e1;
+  CUDA_TRY(cudaEventCreate(&e0));
+  CUDA_TRY(cudaEventCreate(&e1));
+  double best = 0;
+  for (int rep = 0; rep < 5 && !rc; rep++) {
+    CUDA_TRY(cudaEventRecord(e0, st));
+    if (launch_smem_probe(blocks, iters, sink, st)) rc = fail(SFSIM_ATMO_ECUDA, "shared-memory probe launch failed");
+    CUDA_TRY(cudaEventRecord(e1, st));
+    CUDA_TRY(cudaEventSynchronize(e1));
+    float ms = 0;
+    CUDA_TRY(cudaEventElapsedTime(&ms, e0, e1));
+    const double bytes = (double)blocks * 1024 * iters * 8 * 16;
+    if (rep > 0 && ms > 0) best = std::fmax(best, bytes / (ms * 1e-3));
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(sink);
+  if (rc) return rc;
+  *bytes_per_second = best;
   return 0;
 }
 
@@ -1214,7 +1266,7 @@ int build_static_impl(const sfsim_atmo_config& cfg, float* T, float* E, float* S
   BuildDims d = make_dims(cfg, 1);
   if ((rc = check_smem<Real>(d))) return rc;
   Work<Real> w;
-  const size_t bytes = carve<Real>(w, nullptr, d, false);
+  const size_t bytes = carve<Real>(w, nullptr, d, false, false);
   if (bytes > kStaticScratchBytes)
     return fail(SFSIM_ATMO_ETOOBIG, "the build needs " + std::to_string(bytes) +
                                         " bytes of scratch, more than the 67108864-byte static array");
@@ -1226,7 +1278,7 @@ int build_static_impl(const sfsim_atmo_config& cfg, float* T, float* E, float* S
   sphere_directions(cfg.ray_steps >> 2, cfg.ray_steps, M_PI / 2, hdirs, hring);
   void* base = nullptr;
   if ((rc = static_scratch_base(dev, &base))) return rc;
-  carve<Real>(w, (char*)base, d, false);
+  carve<Real>(w, (char*)base, d, false, false);
   // every scratch table is written before it is read, so nothing is cleared;
   // parameters and quadrature directions are copied in on the caller's stream
   CUDA_TRY(cudaMemcpyAsync(w.params, &hp, sizeof(AtmoParams), cudaMemcpyHostToDevice, st));

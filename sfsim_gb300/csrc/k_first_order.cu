@@ -15,6 +15,15 @@
 // samples, FP32, compensated sums), and the warp reduces the samples with
 // shuffles.  Shadowed samples form contiguous runs along a ray, so lanes of a
 // warp mostly agree on whether to integrate.
+//
+// FP32 builds read the sun ray's optical depths from a table when the ray
+// climbs (p_s.l >= 0): the same S-sample midpoint sums, evaluated by
+// k_sun_table on a 2048 x 2048 grid of (sqrt(q / q_top), the exit distance
+// between its zenith and horizontal values) and interpolated bilinearly.  A
+// climbing ray's integrand falls monotonically, so the sums are smooth in
+// those coordinates (transmittance error below 1e-5 at the grid's
+// resolution).  Descending rays pass a density peak that the S samples alias,
+// so they are integrated directly as before.
 #include "atmo_device.cuh"
 #include "kernels.h"
 
@@ -52,11 +61,73 @@ __device__ __forceinline__ Real warp_sum(Real v) {
   return v;
 }
 
+// ---- sun-ray optical-depth table (FP32 builds) ----
+
+// Node (i, j) of the table: q = (i / (NR - 1))^2 q_top and the exit distance
+// d = dmin + (j / (NM - 1)) (dh - dmin) between the zenith (dmin = top - r)
+// and horizontal (dh = sqrt(top^2 - r^2)) exits; p.l follows from
+// top^2 = r^2 + 2 d (p.l) + d^2.  Stored: dt * sum exp2 of the Rayleigh and
+// Mie exponents (dt = d / S), the quantities k_first_order integrates.
+__global__ void k_sun_table(const AtmoParams* params, int S, float2* table) {
+  const int b = blockIdx.y;
+  const AtmoParams& P = params[b];
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= kSunNR * kSunNM) return;
+  const int i = t / kSunNM, j = t - (t / kSunNM) * kSunNM;
+  const float Hh2 = P.f_Hh2, R2 = P.f_R * P.f_R, top = (float)P.top;
+  const float xr = (float)i / (float)(kSunNR - 1), xm = (float)j / (float)(kSunNM - 1);
+  const float q = xr * xr * Hh2;
+  const float cq = fmaxf(Hh2 - q, 0.0f);  // top^2 - r^2
+  const float r = sqrtf(R2 + q);
+  const float dmin = cq / (top + r), dh = sqrtf(cq);
+  const float dist = fmaf(xm, dh - dmin, dmin);
+  float2 out = make_float2(0.0f, 0.0f);
+  if (dist > 0.0f) {
+    const float bp = (cq - dist * dist) / (2.0f * dist);
+    constexpr int NP = Bulk<float>::kSunNP;
+    float hc[NP];
+#pragma unroll
+    for (int c = 0; c < NP; c++) hc[c] = Bulk<float>::hpr(P)[c];
+    const float dt = dist / (float)S;
+    float sr, smie;
+    sun_sums<float, NP>(q, bp, dt, S, hc, Bulk<float>::alpha(P), Bulk<float>::beta(P), Bulk<float>::hratio(P), sr,
+                        smie);
+    out = make_float2(dt * sr, dt * smie);
+  }
+  table[(long long)b * kSunNR * kSunNM + t] = out;
+}
+
+void launch_sun_table(const AtmoParams* params, const BuildDims& d, float2* table, cudaStream_t st) {
+  dim3 grid((unsigned)((kSunNR * kSunNM + 255) / 256), d.B);
+  k_sun_table<<<grid, 256, 0, st>>>(params, d.S, table);
+}
+
+// Bilinear lookup of the table at (q, exit distance) for a climbing ray.
+__device__ __forceinline__ float2 sun_lookup(const float2* __restrict__ tab, const AtmoParams& P, float q,
+                                             float texit) {
+  const float Hh2 = P.f_Hh2, R2 = P.f_R * P.f_R, top = (float)P.top;
+  const float qc = fminf(fmaxf(q, 0.0f), Hh2);
+  const float cq = Hh2 - qc;
+  const float r = sqrtf(R2 + qc);
+  const float dmin = cq / (top + r), dh = sqrtf(cq);
+  const float span = dh - dmin;
+  const float xm = span > 0.0f ? fminf(fmaxf((texit - dmin) / span, 0.0f), 1.0f) : 0.0f;
+  const float xr = sqrtf(qc / Hh2);
+  const float fi = xr * (float)(kSunNR - 1), fj = xm * (float)(kSunNM - 1);
+  const int i0 = min((int)fi, kSunNR - 2), j0 = min((int)fj, kSunNM - 2);
+  const float a = fi - (float)i0, c = fj - (float)j0;
+  const float2* row0 = tab + (long long)i0 * kSunNM + j0;
+  const float2 v00 = __ldg(row0), v01 = __ldg(row0 + 1), v10 = __ldg(row0 + kSunNM), v11 = __ldg(row0 + kSunNM + 1);
+  const float w00 = (1.0f - a) * (1.0f - c), w01 = (1.0f - a) * c, w10 = a * (1.0f - c), w11 = a * c;
+  return make_float2(w00 * v00.x + w01 * v01.x + w10 * v10.x + w11 * v11.x,
+                     w00 * v00.y + w01 * v01.y + w10 * v10.y + w11 * v11.y);
+}
+
 template <class Real, int WARPS>
 __global__ void __launch_bounds__(WARPS * 32, 4) k_first_order(const AtmoParams* params, BuildDims d,
                                                             const RowInfo* rowinfo, const RowSample<Real>* rows,
-                                                            const CellGeom<Real>* geom, Vec4<Real>* rayleigh,
-                                                            Vec4<Real>* mie) {
+                                                            const CellGeom<Real>* geom, const float2* sun_table,
+                                                            Vec4<Real>* rayleigh, Vec4<Real>* mie) {
   extern __shared__ unsigned char smem_raw[];
   FirstOrderSmem<Real>* sm = reinterpret_cast<FirstOrderSmem<Real>*>(smem_raw);
   const int b = blockIdx.y;
@@ -98,6 +169,7 @@ __global__ void __launch_bounds__(WARPS * 32, 4) k_first_order(const AtmoParams*
   const double stepsize = 1.0 / S;
   const Real rr = (Real)ri.r, D0 = (Real)ri.D[0], D1 = (Real)ri.D[1], D2 = (Real)ri.D[2];
   const long long node0 = (b * nrows + row) * ncell;
+  const float2* tab = sun_table ? sun_table + (long long)b * kSunNR * kSunNM : nullptr;
 
   for (int cell = warp; cell < ncell; cell += WARPS) {
     const CellGeom<Real> g = geom[node0 + cell];
@@ -114,12 +186,21 @@ __global__ void __launch_bounds__(WARPS * 32, 4) k_first_order(const AtmoParams*
         const Real root = Bulk<Real>::sqrt(disc);
         Real texit = bp >= Real(0) ? Bulk<Real>::div(-ctop, bp + root) : root - bp;
         texit = fmax(texit, Real(0));
-        const Real dt = texit * inv_steps;
-        Real sr, smie;
-        sun_sums<Real, NP>(q, bp, dt, S, hc, alpha, beta, ratio, sr, smie);
+        Real odr, odm;
+        if (std::is_same<Real, float>::value && tab && bp >= Real(0)) {
+          const float2 od = sun_lookup(tab, P, (float)q, (float)texit);
+          odr = (Real)od.x;
+          odm = (Real)od.y;
+        } else {
+          const Real dt = texit * inv_steps;
+          Real sr, smie;
+          sun_sums<Real, NP>(q, bp, dt, S, hc, alpha, beta, ratio, sr, smie);
+          odr = dt * sr;
+          odm = dt * smie;
+        }
 #pragma unroll
         for (int c = 0; c < 3; c++) {
-          const Real tau = sm[s].tau[c] + dt * (rext[c] * sr + mext[c] * smie);
+          const Real tau = sm[s].tau[c] + (rext[c] * odr + mext[c] * odm);
           const Real T = exp_neg(tau);
           accR[c] = fma(T, sm[s].er, accR[c]);
           accM[c] = fma(T, sm[s].em, accM[c]);
@@ -151,24 +232,26 @@ __global__ void __launch_bounds__(WARPS * 32, 4) k_first_order(const AtmoParams*
 
 template <class Real>
 void launch_first_order(const AtmoParams* params, const BuildDims& d, const RowInfo* rowinfo,
-                        const RowSample<Real>* rows, const CellGeom<Real>* geom, Vec4<Real>* rayleigh,
-                        Vec4<Real>* mie, cudaStream_t st) {
+                        const RowSample<Real>* rows, const CellGeom<Real>* geom, const float2* sun_table,
+                        Vec4<Real>* rayleigh, Vec4<Real>* mie, cudaStream_t st) {
   constexpr int WARPS = 8;
   size_t smem = sizeof(FirstOrderSmem<Real>) * d.S;
   dim3 grid((unsigned)d.rows(), d.B);
-  k_first_order<Real, WARPS><<<grid, WARPS * 32, smem, st>>>(params, d, rowinfo, rows, geom, rayleigh, mie);
+  k_first_order<Real, WARPS><<<grid, WARPS * 32, smem, st>>>(params, d, rowinfo, rows, geom, sun_table, rayleigh,
+                                                             mie);
 }
 
 template void launch_first_order<float>(const AtmoParams*, const BuildDims&, const RowInfo*,
-                                        const RowSample<float>*, const CellGeom<float>*, Vec4<float>*,
-                                        Vec4<float>*, cudaStream_t);
+                                        const RowSample<float>*, const CellGeom<float>*, const float2*,
+                                        Vec4<float>*, Vec4<float>*, cudaStream_t);
 template void launch_first_order<double>(const AtmoParams*, const BuildDims&, const RowInfo*,
-                                         const RowSample<double>*, const CellGeom<double>*, Vec4<double>*,
-                                         Vec4<double>*, cudaStream_t);
+                                         const RowSample<double>*, const CellGeom<double>*, const float2*,
+                                         Vec4<double>*, Vec4<double>*, cudaStream_t);
 
-// Work census of the first order: the number of (node, sample) pairs whose
-// sun is above the horizon, i.e. the sun-ray optical-depth integrals the
-// kernel above evaluates (each of S extinction samples).
+// Work census of the first order: count[0] = the (node, sample) pairs whose
+// sun is above the horizon (sun-ray optical depths the reference integrates,
+// each of S extinction samples), count[1] = those whose sun ray climbs
+// (p_s.l >= 0; FP32 builds read them from the sun table).
 template <class Real>
 __global__ void k_first_order_census(const AtmoParams* params, BuildDims d, const RowInfo* rowinfo,
                                      const RowSample<Real>* rows, const CellGeom<Real>* geom,
@@ -181,16 +264,24 @@ __global__ void k_first_order_census(const AtmoParams* params, BuildDims d, cons
   const RowSample<Real>* rs = rows + (b * nrows + row) * d.S;
   const int ncell = d.n2 * d.n3;
   const long long node0 = (b * nrows + row) * ncell;
-  unsigned long long local = 0;
+  unsigned long long local = 0, climb = 0;
   for (long long t = threadIdx.x; t < (long long)ncell * d.S; t += blockDim.x) {
     const int cell = (int)(t / d.S), s = (int)(t % d.S);
     const CellGeom<Real> g = geom[node0 + cell];
     const Real Dl = (Real)ri.D[0] * g.lx + (Real)ri.D[1] * g.ly + (Real)ri.D[2] * g.lz;
     const Real bp = fma(rs[s].us, Dl, (Real)ri.r * g.lx);
-    local += sun_visible<Real>(P, d, ri, bp, rs[s].q, cell, s) ? 1 : 0;
+    const bool lit = sun_visible<Real>(P, d, ri, bp, rs[s].q, cell, s);
+    local += lit ? 1 : 0;
+    climb += (lit && bp >= Real(0)) ? 1 : 0;
   }
-  for (int o = 16; o > 0; o >>= 1) local += __shfl_xor_sync(0xffffffffu, local, o);
-  if ((threadIdx.x & 31) == 0) atomicAdd(count, local);
+  for (int o = 16; o > 0; o >>= 1) {
+    local += __shfl_xor_sync(0xffffffffu, local, o);
+    climb += __shfl_xor_sync(0xffffffffu, climb, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomicAdd(count, local);
+    atomicAdd(count + 1, climb);
+  }
 }
 
 template <class Real>

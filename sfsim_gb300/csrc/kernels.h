@@ -32,8 +32,14 @@ void launch_surface_base(const AtmoParams* params, const BuildDims& d, Vec4<Real
 // First-order Rayleigh ray scatter and Mie strength (fused).
 template <class Real>
 void launch_first_order(const AtmoParams* params, const BuildDims& d, const RowInfo* rowinfo,
-                        const RowSample<Real>* rows, const CellGeom<Real>* geom, Vec4<Real>* rayleigh,
-                        Vec4<Real>* mie, cudaStream_t st);
+                        const RowSample<Real>* rows, const CellGeom<Real>* geom, const float2* sun_table,
+                        Vec4<Real>* rayleigh, Vec4<Real>* mie, cudaStream_t st);
+
+// Sun-ray optical-depth table of the FP32 first order: kSunNR x kSunNM
+// float2 per atmosphere (see k_first_order.cu).
+constexpr int kSunNR = 2048;
+constexpr int kSunNM = 2048;
+void launch_sun_table(const AtmoParams* params, const BuildDims& d, float2* table, cudaStream_t st);
 
 template <class Real>
 void launch_first_order_census(const AtmoParams* params, const BuildDims& d, const RowInfo* rowinfo,
@@ -42,6 +48,9 @@ void launch_first_order_census(const AtmoParams* params, const BuildDims& d, con
 
 // Throughput probe of the SFU: `iters` ex2.approx per chain, 8 chains per thread.
 void launch_sfu_probe(int blocks, int threads, int iters, float* sink, cudaStream_t st);
+// Throughput probe of shared-memory reads: blocks of 1024 threads, each
+// reading `iters` x 8 16-byte words.
+int launch_smem_probe(int blocks, int iters, float* sink, cudaStream_t st);
 
 // J = point scatter of (dS, dE); when `mie` is non-NULL dS is the first
 // iteration's rayleigh + mie * phase(mie, v.l).

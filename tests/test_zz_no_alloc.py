@@ -43,10 +43,13 @@ def test_static_build_matches_allocating_build(precision):
     first = _build(L.sfsim_atmo_build_static, cfg, stream)
     second = _build(L.sfsim_atmo_build_static, cfg, stream)
     torch.cuda.synchronize()
+    # the static build integrates every sun ray directly; the allocating FP32
+    # build reads the climbing ones from its sun table, within 2e-5
+    tol = 2e-5 if precision == C.FP32 else 1e-12
     for r, a, b in zip(ref, first, second):
         assert torch.isfinite(a).all() and torch.isfinite(b).all()
-        assert _rel(a, r) <= 1e-6
-        assert _rel(b, r) <= 1e-6
+        assert _rel(a, r) <= tol
+        assert torch.equal(a, b)
 
 
 def test_static_build_rejects_oversize():
