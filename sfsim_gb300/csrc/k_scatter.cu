@@ -58,6 +58,31 @@ __device__ __forceinline__ void gather_heading_row(const Vec4<Real>* t, const Bu
   mix3(e0, e1, s1, dst);
 }
 
+// Shared-memory rows of RGB texels, three values per texel.  (16-byte texels
+// were measured slower: a warp's lanes read few distinct texels of a row,
+// which scalar loads serve as broadcasts in one wavefront each, while 16-byte
+// loads take four.)
+template <class Real>
+struct TexelRow {
+  static constexpr int kStride = 3;
+  static __device__ __forceinline__ void load(const Real* base, int idx, Real* out) {
+    out[0] = base[3 * idx];
+    out[1] = base[3 * idx + 1];
+    out[2] = base[3 * idx + 2];
+  }
+  static __device__ __forceinline__ void store(Real* base, int idx, const Real* v) {
+    base[3 * idx] = v[0];
+    base[3 * idx + 1] = v[1];
+    base[3 * idx + 2] = v[2];
+  }
+};
+
+// Direction vector and quadrature weight of a SphereDir.
+template <class Real>
+__device__ __forceinline__ void load_dir(const SphereDir<Real>& D, Real& w0, Real& w1, Real& w2, Real& weight) {
+  w0 = D.w[0], w1 = D.w[1], w2 = D.w[2], weight = D.weight;
+}
+
 template <class Real, bool FIRST>
 __global__ void __launch_bounds__(256, 3) k_point_scatter(const AtmoParams* params, BuildDims d,
                                                           const RowInfo* rowinfo, const SphereDir<Real>* sdirs,
@@ -65,6 +90,8 @@ __global__ void __launch_bounds__(256, 3) k_point_scatter(const AtmoParams* para
                                                           const Vec4<Real>* Mt, const Vec4<Real>* dE,
                                                           Vec4<Real>* J, int nchunks) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
+  using TR = TexelRow<Real>;
+  constexpr int RS = TR::kStride;
   const int b = blockIdx.y;
   const int chunk = blockIdx.x % nchunks;
   const int ik = blockIdx.x / nchunks;
@@ -73,8 +100,8 @@ __global__ void __launch_bounds__(256, 3) k_point_scatter(const AtmoParams* para
   const int nrow = d.P * d.n3;
   SphereDir<Real>* dirs = reinterpret_cast<SphereDir<Real>*>(smem_raw);
   Real* rows = reinterpret_cast<Real*>(dirs + d.P);
-  Real* rowsM = rows + 3 * nrow;
-  Real* etab = rowsM + (FIRST ? 3 * nrow : 0);
+  Real* rowsM = rows + RS * nrow;
+  Real* etab = rowsM + (FIRST ? RS * nrow : 0);
 
   // the (i, k) coordinates, FP64 as in ray-scatter-forward
   const double r = index_to_radius(P, d.n0, (double)i);
@@ -92,16 +119,19 @@ __global__ void __launch_bounds__(256, 3) k_point_scatter(const AtmoParams* para
     const int w = t / d.n3, a = t - w * d.n3;
     const int u1 = src[w].u1, v1 = upper_index(u1, d.n1);
     const Real s1 = src[w].s1;
-    gather_heading_row(dS + base4, d, u0, v0, s0, u1, v1, s1, u2, v2, s2, a, rows + 3 * t);
-    if (FIRST) gather_heading_row(Mt + base4, d, u0, v0, s0, u1, v1, s1, u2, v2, s2, a, rowsM + 3 * t);
+    Real v[3];
+    gather_heading_row(dS + base4, d, u0, v0, s0, u1, v1, s1, u2, v2, s2, a, v);
+    TR::store(rows, t, v);
+    if (FIRST) {
+      gather_heading_row(Mt + base4, d, u0, v0, s0, u1, v1, s1, u2, v2, s2, a, v);
+      TR::store(rowsM, t, v);
+    }
   }
   const long long nE = d.nE();
   for (int t = threadIdx.x; t < nE; t += blockDim.x) {
     Real A[3];
     ld3(dE, b * nE + t, A);
-    etab[3 * t] = A[0];
-    etab[3 * t + 1] = A[1];
-    etab[3 * t + 2] = A[2];
+    TR::store(etab, t, A);
   }
   __syncthreads();
 
@@ -118,10 +148,9 @@ __global__ void __launch_bounds__(256, 3) k_point_scatter(const AtmoParams* para
   const PhaseCS<Real> phR(P.ray_g), phM(P.mie_g);
   const Real scale3 = Real(0.5) * Real(d.n3 - 1);
   const Real scaleE = (Real)((d.nE1 - 1) / (1 - exp(-3.6)));
-  const int n3x3 = 3 * d.n3;
-  // The phases depend on (j, direction) only.  When the n3 headings of one j
-  // fill aligned lane groups, each lane evaluates them for one direction of a
-  // batch of n3 and the group exchanges them by shuffles.
+  // The weighted phases depend on (j, direction) only.  When the n3 headings
+  // of one j fill aligned lane groups, each lane evaluates them for one
+  // direction of a batch of n3 and the group exchanges them by shuffles.
   const int G = d.n3;
   const bool share = (32 % G == 0) && (blockDim.x % G == 0);
   const int lane = threadIdx.x & 31;
@@ -131,44 +160,52 @@ __global__ void __launch_bounds__(256, 3) k_point_scatter(const AtmoParams* para
   Real accR[3] = {0, 0, 0}, accM[3] = {0, 0, 0}, cR[3] = {0, 0, 0}, cM[3] = {0, 0, 0};
   Real ringR[3] = {0, 0, 0}, ringM[3] = {0, 0, 0};
   const int step = share ? G : 1;
+  const int row_len = RS * d.n3;
   for (int w0 = 0; w0 < d.P; w0 += step) {
-    Real pRb = 0, pMb = 0;
+    Real wRb = 0, wMb = 0;
     if (share) {
       const int wb = w0 + gpos;
       if (wb < d.P) {
-        const Real mu_v = fma(sv, dirs[wb].w[0], cv * dirs[wb].w[1]);
-        pRb = phR(mu_v);
-        pMb = phM(mu_v);
+        Real x0, x1, x2, wt;
+        load_dir(dirs[wb], x0, x1, x2, wt);
+        const Real mu_v = fma(sv, x0, cv * x1);
+        wRb = wt * phR(mu_v);
+        wMb = wt * phM(mu_v);
       }
     }
     const int wend = min(w0 + step, d.P);
     for (int w = w0; w < wend; w++) {
       const SphereDir<Real>& D = dirs[w];
-      Real pR, pM;
+      Real x0, x1, x2, wt;
+      load_dir(D, x0, x1, x2, wt);
+      Real wR, wM;
       if (share) {
-        pR = __shfl_sync(0xffffffffu, pRb, gbase + (w - w0));
-        pM = __shfl_sync(0xffffffffu, pMb, gbase + (w - w0));
+        wR = __shfl_sync(0xffffffffu, wRb, gbase + (w - w0));
+        wM = __shfl_sync(0xffffffffu, wMb, gbase + (w - w0));
       } else {
-        const Real mu_v = fma(sv, D.w[0], cv * D.w[1]);
-        pR = phR(mu_v);
-        pM = phM(mu_v);
+        const Real mu_v = fma(sv, x0, cv * x1);
+        wR = wt * phR(mu_v);
+        wM = wt * phM(mu_v);
       }
-      const Real mu_l = fma(D.w[0], g.lx, fma(D.w[1], g.ly, D.w[2] * g.lz));
+      const Real mu_l = fma(x0, g.lx, fma(x1, g.ly, x2 * g.lz));
       // sun-angle coordinate of (omega, l) along the direction's heading row
       int u3;
       Real s3;
-      split_coord_r<Real>(scale3 * (Real(1) + mu_l), d.n3, &u3, &s3);
+      split_coord_r<Real>(fma(scale3, mu_l, scale3), d.n3, &u3, &s3);
       const int v3 = upper_index(u3, d.n3);
-      const Real* row = rows + w * n3x3;
-      Real X[3];
+      Real X[3], lo[3], hi[3];
+      const Real* row_w = rows + w * row_len;
+      TR::load(row_w, u3, lo);
+      TR::load(row_w, v3, hi);
 #pragma unroll
-      for (int c = 0; c < 3; c++) X[c] = fma(row[3 * v3 + c] - row[3 * u3 + c], s3, row[3 * u3 + c]);
+      for (int c = 0; c < 3; c++) X[c] = fma(hi[c] - lo[c], s3, lo[c]);
       if (FIRST) {
-        const Real* rowM = rowsM + w * n3x3;
         const Real ph = phM(mu_l);
+        const Real* rowM_w = rowsM + w * row_len;
+        TR::load(rowM_w, u3, lo);
+        TR::load(rowM_w, v3, hi);
 #pragma unroll
-        for (int c = 0; c < 3; c++)
-          X[c] = fma(fma(rowM[3 * v3 + c] - rowM[3 * u3 + c], s3, rowM[3 * u3 + c]), ph, X[c]);
+        for (int c = 0; c < 3; c++) X[c] = fma(fma(hi[c] - lo[c], s3, lo[c]), ph, X[c]);
       }
       if (D.surface) {
         const Real sg = fma(D.gdir[0], g.lx, fma(D.gdir[1], g.ly, D.gdir[2] * g.lz));
@@ -176,14 +213,15 @@ __global__ void __launch_bounds__(256, 3) k_point_scatter(const AtmoParams* para
         Real sE1;
         split_coord_r<Real>(sun_elevation_index_r<Real>(sg, scaleE), d.nE1, &uE1, &sE1);
         const int vE1 = upper_index(uE1, d.nE1), vE0 = upper_index(D.uE0, d.nE0);
-        Real Y[3];
-        mix4(etab + 3 * (D.uE0 * d.nE1 + uE1), etab + 3 * (D.uE0 * d.nE1 + vE1), etab + 3 * (vE0 * d.nE1 + uE1),
-             etab + 3 * (vE0 * d.nE1 + vE1), D.sE0, sE1, Y);
+        Real e00[3], e01[3], e10[3], e11[3], Y[3];
+        TR::load(etab, D.uE0 * d.nE1 + uE1, e00);
+        TR::load(etab, D.uE0 * d.nE1 + vE1, e01);
+        TR::load(etab, vE0 * d.nE1 + uE1, e10);
+        TR::load(etab, vE0 * d.nE1 + vE1, e11);
+        mix4(e00, e01, e10, e11, D.sE0, sE1, Y);
 #pragma unroll
         for (int c = 0; c < 3; c++) X[c] = fma(D.ground[c], Y[c], X[c]);
       }
-      const Real wR = D.weight * pR;
-      const Real wM = D.weight * pM;
 #pragma unroll
       for (int c = 0; c < 3; c++) {
         ringR[c] = fma(wR, X[c], ringR[c]);
