@@ -202,12 +202,12 @@ int sfsim_atmo_query_table(const sfsim_atmo_context* ctx, int kind, long long n,
 int sfsim_atmo_query_direct(const sfsim_atmo_context* ctx, long long n, const double* x,
                             const double* v, const double* l, float* out, void* stream);
 
-/* The surrogate's six coordinates in [0, 1] of (x, v, l): the table
+/* The surrogate's ten coordinates in [0, 1] of (x, v, l): the table
  * coordinates height, elevation, sun elevation and sun heading as
  * core/ray-scatter-forward.glsl forms them (FP32), with the table half chosen
  * by is_above_horizon; then (1 + sin of the sun elevation) / 2 without the
- * lookup's clamp, and the table half (0 upper, 1 lower).  coords is a DEVICE
- * [n][6]. */
+ * lookup's clamp, the table half (0 upper, 1 lower), and the four cell phases
+ * frac(coordinate * (size - 1)) of the lookup.  coords is a DEVICE [n][10]. */
 int sfsim_atmo_query_coords(const sfsim_atmo_context* ctx, long long n, const double* x, const double* v,
                             const double* l, float* coords, void* stream);
 
@@ -234,7 +234,7 @@ typedef struct sfsim_atmo_surrogate_config {
 int sfsim_atmo_surrogate_train(sfsim_atmo_context* ctx, const sfsim_atmo_surrogate_config* cfg,
                                float* loss_history);
 
-/* Parameter vector (FP32, W1 [256][192], b1, W2, b2, W3, b3, W4, b4 [256][256],
+/* Parameter vector (FP32, W1 [256][256], b1, W2, b2, W3, b3, W4, b4 [256][256],
  * W5 [4][256], b5 [4]): *count receives its length; `get` copies it out, `set`
  * replaces it (host arrays, either may be NULL).  Outputs 0-2 are corrections
  * r = log(value + 1e-7) - log(table + 1e-7) to the in-scatter lookup, output 3
@@ -242,7 +242,7 @@ int sfsim_atmo_surrogate_train(sfsim_atmo_context* ctx, const sfsim_atmo_surroga
 int sfsim_atmo_surrogate_parameters(sfsim_atmo_context* ctx, float* get, const float* set, long long* count);
 
 /* Loss (mean squared error of the corrections) and parameter gradients of
- * one batch (host coords [n][6], target corrections [n][3]; n a multiple of
+ * one batch (host coords [n][10], target corrections [n][3]; n a multiple of
  * 1024) without updating, for validation.  The gradients also carry the
  * Gaussian negative log-likelihood of the squared error under the predicted
  * variance, weighted 0.01. */

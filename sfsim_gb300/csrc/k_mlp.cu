@@ -18,10 +18,12 @@ __global__ void k_features(long long n, const float* __restrict__ coords, __nv_b
   const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (t >= n * kMlpIn / 2) return;
   const long long i = t / (kMlpIn / 2);
-  const int f = (int)(t % (kMlpIn / 2));  // d * 16 + k
-  const int d = f >> 4, k = f & 15;
+  const int f = (int)(t % (kMlpIn / 2));
+  int d;
+  float freq;
+  feature_pair(f, &d, &freq);
   float s, c;
-  sincospif(feature_frequency(k) * coords[i * kMlpCoords + d], &s, &c);
+  sincospif(freq * coords[i * kMlpCoords + d], &s, &c);
   const __nv_bfloat16 bs = __float2bfloat16(s), bc = __float2bfloat16(c);
   F[i * kMlpIn + 2 * f] = bs;
   F[i * kMlpIn + 2 * f + 1] = bc;

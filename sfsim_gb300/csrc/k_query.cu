@@ -273,8 +273,10 @@ void launch_query_table(const QueryTables& q, int kind, long long n, const float
 // The surrogate's coordinates of (p, d, l): the table coordinates as the
 // in-scatter lookup forms them (core/ray-scatter-forward.glsl order reversed
 // to height, elevation, sun elevation, sun heading) with the table half chosen
-// by the horizon test, then (1 + sin of the sun elevation) / 2 and the half
-// (0 upper, 1 lower).  idx receives the lookup's indices.
+// by the horizon test, then (1 + sin of the sun elevation) / 2, the half
+// (0 upper, 1 lower) and the four cell phases of the lookup
+// (interpolate-4d.glsl scales each coordinate by size - 1).  idx receives the
+// lookup's indices.
 __device__ __forceinline__ void network_coords(const GlslEnv& e, f3 p, f3 d, f3 l, float* u, float* idx) {
   const bool above = is_above_horizon_g(e, p, d);
   ray_scatter_forward_g(e, p, d, l, above, idx);
@@ -284,6 +286,13 @@ __device__ __forceinline__ void network_coords(const GlslEnv& e, f3 p, f3 d, f3 
   u[3] = idx[0];
   u[4] = fminf(fmaxf(0.5f * (1.0f + fdot(p, l) / sqrtf(fdot(p, p))), 0.0f), 1.0f);
   u[5] = above ? 0.0f : 1.0f;
+  const float size[4] = {(float)(e.height - 1), (float)(e.elevation - 1), (float)(e.light - 1),
+                         (float)(e.heading - 1)};
+#pragma unroll
+  for (int c = 0; c < 4; c++) {
+    const float x = u[c] * size[c];
+    u[kMlpSmooth + c] = x - floorf(x);
+  }
 }
 
 // The surrogate's coordinates of (x, v, l); the table value there (S + M
@@ -374,6 +383,7 @@ __global__ void k_node_pool(BuildDims d, float* pool) {
   const float sin_el = -(logf(1.0f - o[2] * (1.0f - expf(-3.6f))) + 0.6f) / 3.0f;
   o[4] = fminf(fmaxf(0.5f * (1.0f + sin_el), 0.0f), 1.0f);
   o[5] = o[1] > 0.5f ? 1.0f : 0.0f;
+  for (int c = 0; c < kMlpPhases; c++) o[kMlpSmooth + c] = 0.0f;  // a node sits on a cell corner
   for (int c = 0; c < 3; c++) o[kMlpCoords + c] = 0.0f;
 }
 
@@ -625,6 +635,32 @@ __device__ __forceinline__ float tanh_approx(float x) {
   return y;
 }
 
+// Sines and cosines of pi 2 (k + 1) t for the 8 harmonics of a cell phase t,
+// by the recurrences sin((k+1)a) = 2 cos(a) sin(ka) - sin((k-1)a) (and the
+// same for cos), as 2 x 8 BF16 at K columns col0 .. col0 + 15.
+__device__ __forceinline__ void write_phase_features(float t, unsigned char* A, int row, int col0) {
+  float s[8], c[8];
+  sincospif(2.0f * t, &s[0], &c[0]);
+  const float c2 = c[0] + c[0];
+  s[1] = c2 * s[0];
+  c[1] = fmaf(c2, c[0], -1.0f);
+#pragma unroll
+  for (int k = 2; k < 8; k++) {
+    s[k] = fmaf(c2, s[k - 1], -s[k - 2]);
+    c[k] = fmaf(c2, c[k - 1], -c[k - 2]);
+  }
+#pragma unroll
+  for (int q = 0; q < 2; q++) {
+    uint32_t w[4];
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+      const __nv_bfloat162 h = __floats2bfloat162_rn(s[4 * q + j], c[4 * q + j]);
+      w[j] = *reinterpret_cast<const uint32_t*>(&h);
+    }
+    *reinterpret_cast<uint4*>(A + tc::tile_offset(row, col0 + 8 * q, kMlpHidden)) = make_uint4(w[0], w[1], w[2], w[3]);
+  }
+}
+
 // Sines and cosines of pi f_k u for the 16 feature frequencies f_k = 2^(k/2):
 // sincospi at f_0 and f_1, the rest by exact angle doubling
 // (sin 2a = 2 sin a cos a, cos 2a = 1 - 2 sin^2 a), written as 4 x 8 BF16
@@ -762,7 +798,9 @@ __global__ void __launch_bounds__(kInferThreads, 1) k_surrogate_infer(InferArgs 
 #pragma unroll
       for (int c = 0; c < kMlpCoords; c++) u[c] = g.coords[kMlpCoords * qq + c];
 #pragma unroll
-      for (int dd = 0; dd < kMlpCoords; dd++) write_features(u[dd], A, row, 32 * dd);
+      for (int dd = 0; dd < kMlpSmooth; dd++) write_features(u[dd], A, row, 32 * dd);
+#pragma unroll
+      for (int dd = 0; dd < kMlpPhases; dd++) write_phase_features(u[kMlpSmooth + dd], A, row, 32 * kMlpSmooth + 16 * dd);
       tc::fence_async_smem();
       tc::fence_before();
       tc::mbar_arrive(act_bar);

@@ -167,14 +167,20 @@ struct GemmArgs {
 
 int launch_gemm_tn(const GemmArgs& g, int splits, cudaStream_t st);
 
-// ---- surrogate MLP: 6 coordinates -> 192 Fourier features -> 4 x 256 SiLU -> 4 ----
+// ---- surrogate MLP: 10 coordinates -> 256 Fourier features -> 4 x 256 SiLU -> 4 ----
 // Coordinates in [0, 1]: the four table coordinates (height, elevation, sun
 // elevation, sun heading), the sun elevation (1 + sin) / 2 without the
-// table's clamp at sin = -0.2, and 0 / 1 for the upper / lower table half.
+// table's clamp at sin = -0.2, 0 / 1 for the upper / lower table half, and
+// the four cell phases: the position inside the table cell along each axis
+// (frac(coordinate * (size - 1))), where the lookup's interpolation error
+// repeats.  The six smooth coordinates get 16 frequencies 2^(k/2) each, the
+// phases 8 harmonics 2 (k + 1) each (sin and cos of pi f u).
 // Outputs: r_c (c < 3), the correction log(value_c + eps) - log(table_c + eps)
 // to the table lookup, and s, the log of the expected squared error of r.
-constexpr int kMlpCoords = 6;
-constexpr int kMlpIn = 32 * kMlpCoords;
+constexpr int kMlpSmooth = 6;
+constexpr int kMlpPhases = 4;
+constexpr int kMlpCoords = kMlpSmooth + kMlpPhases;
+constexpr int kMlpIn = 32 * kMlpSmooth + 16 * kMlpPhases;
 constexpr int kPoolRow = kMlpCoords + 3;  // floats per training sample: coordinates, corrections
 constexpr int kMlpHidden = 256;
 constexpr int kMlpLayers = 4;
@@ -184,6 +190,17 @@ constexpr int kMlpOut = 4;
 constexpr float kFeatureSqrt2 = 1.41421356237309505f;
 __host__ __device__ __forceinline__ float feature_frequency(int k) {
   return (k & 1 ? kFeatureSqrt2 : 1.0f) * (float)(1 << (k >> 1));
+}
+// Feature pair f (0 .. kMlpIn/2 - 1): its coordinate and its frequency.
+__host__ __device__ __forceinline__ void feature_pair(int f, int* coord, float* freq) {
+  if (f < 16 * kMlpSmooth) {
+    *coord = f >> 4;
+    *freq = feature_frequency(f & 15);
+  } else {
+    const int g = f - 16 * kMlpSmooth;
+    *coord = kMlpSmooth + (g >> 3);
+    *freq = (float)(2 * ((g & 7) + 1));
+  }
 }
 
 void launch_features(long long n, const float* coords, __nv_bfloat16* F, __nv_bfloat16* FT, cudaStream_t st);

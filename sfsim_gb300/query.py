@@ -142,13 +142,14 @@ class Context:
         return out, nf.value
 
     def coords(self, x, v, l):
-        """The surrogate's coordinates [n, 6] in [0, 1] of the queries: the table coordinates (height,
-        elevation, sun elevation, heading), the unclamped sun elevation and the table half."""
+        """The surrogate's coordinates [n, 10] in [0, 1] of the queries: the table coordinates (height,
+        elevation, sun elevation, heading), the unclamped sun elevation, the table half and the four
+        cell phases of the lookup."""
         import torch
         x = x.contiguous().double()
         v = v.contiguous().double()
         l = l.contiguous().double()
-        out = torch.empty((x.shape[0], 6), dtype=torch.float32, device="cuda")
+        out = torch.empty((x.shape[0], 10), dtype=torch.float32, device="cuda")
         _lib.check(self._L.sfsim_atmo_query_coords(self._ptr, x.shape[0], x.data_ptr(), v.data_ptr(), l.data_ptr(),
                                                    out.data_ptr(), torch.cuda.current_stream().cuda_stream),
                    "query_coords")

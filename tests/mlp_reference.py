@@ -5,8 +5,9 @@ weight copies), so that its gradients check the GPU's forward and backward
 GEMMs."""
 import numpy as np
 
-N_COORDS = 6
-N_IN, N_HID = 32 * N_COORDS, 256
+N_SMOOTH, N_PHASES = 6, 4
+N_COORDS = N_SMOOTH + N_PHASES
+N_IN, N_HID = 32 * N_SMOOTH + 16 * N_PHASES, 256
 N_OUT = 4  # three log-space corrections to the table lookup and a log variance
 SHAPES = [(N_HID, N_IN), (N_HID, N_HID), (N_HID, N_HID), (N_HID, N_HID), (N_OUT, N_HID)]
 VAR_WEIGHT = 0.01
@@ -32,11 +33,17 @@ def unpack(params):
 
 
 def features(coords):
+    """Smooth coordinates: 16 frequencies 2^(k/2); cell phases: 8 harmonics 2 (k + 1);
+    sin and cos of pi f u, in coordinate order."""
+    n = coords.shape[0]
     k = np.arange(16)
     f = np.where(k % 2 == 1, np.float32(np.sqrt(2.0)), 1.0) * 2.0 ** (k // 2)
-    ang = np.pi * coords[:, :, None].astype(np.float64) * f[None, None, :]  # [n, 4, 16]
-    F = np.stack([np.sin(ang), np.cos(ang)], axis=-1).reshape(coords.shape[0], N_IN)
-    return F
+    ang = np.pi * coords[:, :N_SMOOTH, None].astype(np.float64) * f[None, None, :]
+    smooth = np.stack([np.sin(ang), np.cos(ang)], axis=-1).reshape(n, 32 * N_SMOOTH)
+    h = 2.0 * (np.arange(8) + 1)
+    angp = np.pi * coords[:, N_SMOOTH:, None].astype(np.float64) * h[None, None, :]
+    phase = np.stack([np.sin(angp), np.cos(angp)], axis=-1).reshape(n, 16 * N_PHASES)
+    return np.concatenate([smooth, phase], axis=1)
 
 
 def silu(z):

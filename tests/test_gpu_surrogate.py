@@ -21,7 +21,7 @@ def ctx():
 def test_gradients_match_reference(ctx):
     rng = np.random.default_rng(3)
     n = 2048
-    coords = rng.uniform(0, 1, (n, 6)).astype(np.float32)
+    coords = rng.uniform(0, 1, (n, 10)).astype(np.float32)
     targets = rng.normal(0, 0.5, (n, 3)).astype(np.float32)
     params = ctx.surrogate_parameters()
     loss, grads = ctx.surrogate_gradients(coords, targets)
