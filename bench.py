@@ -429,7 +429,7 @@ def surrogate_roofline(n, ms):
             "flops_per_query": MLP_FLOPS_PER_QUERY}
 
 
-def run_queries(C, steps=10000, batch=65536, direct_samples=1 << 25, lr=3e-3, huber_delta=0.02,
+def run_queries(C, steps=20000, batch=65536, direct_samples=1 << 25, lr=3e-3, huber_delta=0.02,
                 thresholds=(3e-2, 1e-2, 3e-3, 1e-3)):
     """2^24 random in-scatter queries (height uniform 0-100 km, view and sun
     uniform on the sphere) on the production tables: table lookup, direct

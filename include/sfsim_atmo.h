@@ -230,7 +230,9 @@ typedef struct sfsim_atmo_surrogate_config {
 } sfsim_atmo_surrogate_config;
 
 /* Trains (or continues training) the context's surrogate on the GPU;
- * loss_history (host, `steps` floats, may be NULL) receives each step's loss. */
+ * loss_history (host, `steps` floats, may be NULL) receives each step's loss.
+ * Returns SFSIM_ATMO_ENUMERIC when the run diverged (a non-finite last loss;
+ * learning rates above about 3e-3 can do that at batch 65536). */
 int sfsim_atmo_surrogate_train(sfsim_atmo_context* ctx, const sfsim_atmo_surrogate_config* cfg,
                                float* loss_history);
 

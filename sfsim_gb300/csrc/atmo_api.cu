@@ -1510,6 +1510,15 @@ int sfsim_atmo_surrogate_train(sfsim_atmo_context* ctx, const sfsim_atmo_surroga
       cudaMemcpyAsync(loss_history, hist, sizeof(float) * sc->steps, cudaMemcpyDeviceToHost, st) != cudaSuccess)
     rc = fail(SFSIM_ATMO_ECUDA, "loss history copy failed");
   if (!rc) rc = check_error_flag(S, st);
+  if (!rc && sc->steps > 0) {
+    // a diverged run (learning rate too high) leaves non-finite losses
+    float last = 0.0f;
+    if (cudaMemcpyAsync(&last, hist + sc->steps - 1, sizeof(float), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+        cudaStreamSynchronize(st) != cudaSuccess)
+      rc = fail(SFSIM_ATMO_ECUDA, "loss readback failed");
+    else if (!std::isfinite(last))
+      rc = fail(SFSIM_ATMO_ENUMERIC, "surrogate training diverged (non-finite loss); lower the learning rate");
+  }
   cudaStreamSynchronize(st);
   for (void* p : temps) cudaFree(p);
   if (!rc) S.trained_steps += sc->steps;
