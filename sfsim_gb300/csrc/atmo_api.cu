@@ -1585,12 +1585,13 @@ int sfsim_atmo_query_surrogate(sfsim_atmo_context* ctx, long long n, const doubl
   cudaStream_t st = (cudaStream_t)stream;
   const QueryTables q = context_tables(ctx);
   const bool fallback = threshold > 0;
-  unsigned char* mask = nullptr;
+  long long* list = nullptr;  // indices of the flagged queries
   unsigned long long* count = nullptr;
   if (fallback) {
-    if (cudaMalloc(&mask, n) != cudaSuccess || cudaMalloc(&count, sizeof(unsigned long long)) != cudaSuccess) {
-      if (mask) cudaFree(mask);
-      return fail(SFSIM_ATMO_ENOMEM, "fallback mask allocation failed");
+    if (cudaMalloc(&list, sizeof(long long) * (size_t)n) != cudaSuccess ||
+        cudaMalloc(&count, sizeof(unsigned long long)) != cudaSuccess) {
+      if (list) cudaFree(list);
+      return fail(SFSIM_ATMO_ENOMEM, "fallback list allocation failed");
     }
     CUDA_TRY(cudaMemsetAsync(count, 0, sizeof(unsigned long long), st));
   }
@@ -1619,19 +1620,22 @@ int sfsim_atmo_query_surrogate(sfsim_atmo_context* ctx, long long n, const doubl
     float* tab = S.qbuf + kMlpCoords * chunk;
     launch_query_coords(q, m, x + 3 * o, v + 3 * o, l + 3 * o, crd, tab, st);
     if (launch_surrogate_infer(m, crd, tab, S.packed, biases, S.w + S.lay.W[4], S.w + S.lay.b[4], kLogEps,
-                               fallback ? threshold : 0.0f, out + 3 * o, mask ? mask + o : nullptr, count, S.error,
-                               sms, st))
+                               fallback ? threshold : 0.0f, out + 3 * o, list, o, count, S.error, sms, st))
       rc = fail(SFSIM_ATMO_ECUDA, "surrogate inference launch configuration failed");
   }
-  if (!rc && fallback) launch_query_direct(ctx->params, ctx->dims, ctx->jsum, n, x, v, l, out, st, mask);
   if (!rc && cudaGetLastError() != cudaSuccess) rc = fail(SFSIM_ATMO_ECUDA, "surrogate query launch failed");
   if (fallback) {
+    // the flagged queries, compacted into `list`, go to the direct quadrature
     unsigned long long h = 0;
-    if (!rc && cudaMemcpyAsync(&h, count, sizeof(h), cudaMemcpyDeviceToHost, st) == cudaSuccess &&
-        cudaStreamSynchronize(st) == cudaSuccess && n_fallback)
-      *n_fallback = (long long)h;
+    if (!rc && (cudaMemcpyAsync(&h, count, sizeof(h), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+                cudaStreamSynchronize(st) != cudaSuccess))
+      rc = fail(SFSIM_ATMO_ECUDA, "fallback count readback failed");
+    if (!rc && h > (unsigned long long)n) rc = fail(SFSIM_ATMO_ECUDA, "fallback count out of range");
+    if (!rc) launch_query_direct(ctx->params, ctx->dims, ctx->jsum, (long long)h, x, v, l, out, st, list);
+    if (!rc && cudaGetLastError() != cudaSuccess) rc = fail(SFSIM_ATMO_ECUDA, "fallback launch failed");
+    if (!rc && n_fallback) *n_fallback = (long long)h;
     cudaStreamSynchronize(st);
-    cudaFree(mask);
+    cudaFree(list);
     cudaFree(count);
     // the call synchronised: report a wait that timed out in the inference kernel
     if (!rc) rc = check_error_flag(S, st);

@@ -428,15 +428,15 @@ __device__ __forceinline__ float elevation_coordinate_f(float q, float pv, float
   return 0.5f + limit_quot_f(a, rho + rho, -0.5f, 0.0f);
 }
 
-template <int WARPS>
-__global__ void __launch_bounds__(WARPS * 32) k_query_direct(const AtmoParams* params, BuildDims d,
-                                                             const Vec4<float>* Jsum, long long n, const double* X,
-                                                             const double* V, const double* Lt, float* out,
-                                                             const unsigned char* mask) {
+template <int WARPS, bool LIST>
+__global__ void __launch_bounds__(WARPS * 32, 2) k_query_direct(const AtmoParams* params, BuildDims d,
+                                                                const Vec4<float>* Jsum, long long n, const double* X,
+                                                                const double* V, const double* Lt, float* out,
+                                                                const long long* indices) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const long long qi = blockIdx.x * (long long)WARPS + warp;
-  if (qi >= n) return;
-  if (mask && !mask[qi]) return;
+  const long long wi = blockIdx.x * (long long)WARPS + warp;
+  if (wi >= n) return;
+  const long long qi = LIST ? indices[wi] : wi;
   const AtmoParams& P = params[0];
   const d3 x = mk3(X[3 * qi], X[3 * qi + 1], X[3 * qi + 2]);
   const d3 v = mk3(V[3 * qi], V[3 * qi + 1], V[3 * qi + 2]);
@@ -539,10 +539,14 @@ __global__ void __launch_bounds__(WARPS * 32) k_query_direct(const AtmoParams* p
 
 void launch_query_direct(const AtmoParams* params, const BuildDims& d, const Vec4<float>* Jsum, long long n,
                          const double* x, const double* v, const double* l, float* out, cudaStream_t st,
-                         const unsigned char* mask) {
+                         const long long* indices) {
+  if (n <= 0) return;
   constexpr int WARPS = 8;
   const unsigned blocks = (unsigned)((n + WARPS - 1) / WARPS);
-  k_query_direct<WARPS><<<blocks, WARPS * 32, 0, st>>>(params, d, Jsum, n, x, v, l, out, mask);
+  if (indices)
+    k_query_direct<WARPS, true><<<blocks, WARPS * 32, 0, st>>>(params, d, Jsum, n, x, v, l, out, indices);
+  else
+    k_query_direct<WARPS, false><<<blocks, WARPS * 32, 0, st>>>(params, d, Jsum, n, x, v, l, out, nullptr);
 }
 
 // ---------------------------------------------------------------------------
@@ -624,8 +628,9 @@ struct InferArgs {
   float* out;
   float log_var_limit;          // flag queries with s above this (2 log threshold), or +inf
   float eps;
-  unsigned char* mask;
-  unsigned long long* count;
+  long long* list;              // indices (plus index_offset) of the flagged queries, or NULL
+  long long index_offset;
+  unsigned long long* count;    // flagged queries so far (also the next free slot of list)
   int* error;
 };
 
@@ -870,11 +875,14 @@ __global__ void __launch_bounds__(kInferThreads, 1) k_surrogate_infer(InferArgs 
           g.out[3 * q + cc] = fmaxf((fmaxf(tv[cc], 0.0f) + g.eps) * expf(r) - g.eps, 0.0f);
         }
         flag = head[3] + s_w5[kMlpOut * kMlpHidden + 3] > g.log_var_limit;
-        if (g.mask) g.mask[q] = flag ? 1 : 0;
       }
       if (g.count) {
+        // one atomic per warp reserves the slots of its flagged queries
         const unsigned bal = __ballot_sync(0xffffffffu, flag);
-        if (lane == 0 && bal) atomicAdd(g.count, (unsigned long long)__popc(bal));
+        unsigned long long base = 0;
+        if (lane == 0 && bal) base = atomicAdd(g.count, (unsigned long long)__popc(bal));
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (flag && g.list) g.list[base + __popc(bal & ((1u << lane) - 1u))] = g.index_offset + q;
       }
     }
     if (!ok) {
@@ -894,8 +902,8 @@ void launch_pack_infer(const __nv_bfloat16* const* W, unsigned char* packed, cud
 
 int launch_surrogate_infer(long long n, const float* coords, const float* table, const unsigned char* packed,
                            const float* const* b, const float* W5, const float* b5, float eps, float threshold,
-                           float* out, unsigned char* mask, unsigned long long* count, int* error, int num_sms,
-                           cudaStream_t st) {
+                           float* out, long long* list, long long index_offset, unsigned long long* count, int* error,
+                           int num_sms, cudaStream_t st) {
   InferArgs g;
   g.n = n;
   g.coords = coords;
@@ -907,7 +915,8 @@ int launch_surrogate_infer(long long n, const float* coords, const float* table,
   g.out = out;
   g.log_var_limit = threshold > 0 ? 2.0f * logf(threshold) : INFINITY;
   g.eps = eps;
-  g.mask = mask;
+  g.list = list;
+  g.index_offset = index_offset;
   g.count = count;
   g.error = error;
   if (cudaFuncSetAttribute(k_surrogate_infer, cudaFuncAttributeMaxDynamicSharedMemorySize, kInferSmem) !=

@@ -107,9 +107,10 @@ void launch_query_table(const QueryTables& q, int kind, long long n, const float
 
 // Rendered in-scatter S + M phase(mie, v.l) at (x, v, l) by quadrature with
 // the order-summed point-scatter table Jsum (NULL: first order only).
+// With `indices`, warp w evaluates query indices[w] (n of them).
 void launch_query_direct(const AtmoParams* params, const BuildDims& d, const Vec4<float>* Jsum, long long n,
                          const double* x, const double* v, const double* l, float* out, cudaStream_t st,
-                         const unsigned char* mask = nullptr);
+                         const long long* indices = nullptr);
 
 // The surrogate's kMlpCoords coordinates of (x, v, l), the first four the
 // table coordinates as the in-scatter lookup forms them; the lookup's value
@@ -125,8 +126,8 @@ void launch_make_pool(long long n, const float* coords, const float* values, con
 // coordinates and table values (launch_query_coords); see k_query.cu.
 int launch_surrogate_infer(long long n, const float* coords, const float* table, const unsigned char* packed,
                            const float* const* b, const float* W5, const float* b5, float eps, float threshold,
-                           float* out, unsigned char* mask, unsigned long long* count, int* error, int num_sms,
-                           cudaStream_t st);
+                           float* out, long long* list, long long index_offset, unsigned long long* count, int* error,
+                           int num_sms, cudaStream_t st);
 // Packs the BF16 hidden-layer weights into the inference kernel's chunks.
 void launch_pack_infer(const __nv_bfloat16* const* W, unsigned char* packed, cudaStream_t st);
 // Bytes of the packed weight chunks the inference kernel streams.
