@@ -563,7 +563,9 @@ void launch_query_direct(const AtmoParams* params, const BuildDims& d, const Vec
 // the BF16 result back as the next layer's input; the last layer folds the
 // 256 -> 4 head in.  The value is (table + eps) exp(r) - eps, and a query whose
 // predicted squared error exp(s) exceeds threshold^2 is flagged for the direct
-// quadrature.  Warp 8 is the producer: one thread
+// quadrature.  The epilogue has 16 warps: two per group of 32 tensor-memory
+// lanes of each tile, one for each half of the columns (the second adds its
+// part of the head through shared memory).  Warp 16 is the producer: one thread
 // streams the 28 weight chunks of a group (256 rows x 32 K, 16 KB each,
 // pre-packed in the tensor cores' layout) through a five-stage shared-memory
 // ring with bulk TMA copies, and issues the tcgen05.mma of both tiles on each
@@ -581,13 +583,15 @@ constexpr int kInferChunksH = kMlpHidden / kInferKC;                  // hidden 
 constexpr int kInferChunks = kInferChunks0 + 3 * kInferChunksH;       // 28 per group
 constexpr int kInferStages = 5;
 constexpr int kInferTileBytes = 128 * kMlpHidden * 2;                 // 64 KB
-constexpr int kInferThreads = 288;
+constexpr int kInferEpilogueWarps = 16;  // 2 tiles x 4 lane quarters x 2 column halves
+constexpr int kInferThreads = 32 * kInferEpilogueWarps + 32;
 constexpr int kInferWaitLimit = 1 << 22;
 constexpr int kInferSmemRing = 2 * kInferTileBytes;
 constexpr int kInferSmemBias = kInferSmemRing + kInferStages * kInferChunkBytes;
 constexpr int kInferSmemHead = kInferSmemBias + 4 * kMlpHidden * 4;
 constexpr int kInferSmemBar = kInferSmemHead + (kMlpOut * kMlpHidden + 4) * 4;  // W5 (4 x 256) and b5
-constexpr int kInferSmem = kInferSmemBar + (2 * kInferStages + 2) * 8 + 16;
+constexpr int kInferSmemPart = kInferSmemBar + (2 * kInferStages + 3) * 8 + 16;  // head partial sums
+constexpr int kInferSmem = kInferSmemPart + 256 * kMlpOut * 4;
 
 size_t infer_packed_bytes() { return (size_t)kInferChunks * kInferChunkBytes; }
 
@@ -759,7 +763,9 @@ __global__ void __launch_bounds__(kInferThreads, 1) k_surrogate_infer(InferArgs 
   uint64_t* empty = full + kInferStages;
   uint64_t* acc_bar = empty + kInferStages;
   uint64_t* act_bar = acc_bar + 1;
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(act_bar + 1);
+  uint64_t* head_bar = act_bar + 1;  // the second column half's head parts are in s_part
+  float* s_part = reinterpret_cast<float*>(smem + kInferSmemPart);
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(head_bar + 1);
   volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
   const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
   const long long ngroups = (g.n + 255) / 256;
@@ -777,7 +783,8 @@ __global__ void __launch_bounds__(kInferThreads, 1) k_surrogate_infer(InferArgs 
       tc::mbar_init(&empty[s], 1);
     }
     tc::mbar_init(acc_bar, 1);
-    tc::mbar_init(act_bar, 256);
+    tc::mbar_init(act_bar, 32 * kInferEpilogueWarps);
+    tc::mbar_init(head_bar, 16 * kInferEpilogueWarps);
     *abort_flag = 0;
     tc::fence_mbar_init();
   }
@@ -786,26 +793,34 @@ __global__ void __launch_bounds__(kInferThreads, 1) k_surrogate_infer(InferArgs 
   tc::fence_after();
   const uint32_t tmem = *tmem_slot;
 
-  if (warp == 8) {
+  if (warp == kInferEpilogueWarps) {
     if (lane == 0) infer_producer(g, my_groups, smem, tmem, full, empty, acc_bar, act_bar, abort_flag);
     __syncwarp();
   } else {
-    const int tile = warp >> 2, row = (warp & 3) * 32 + lane;
+    // warp w: tensor-memory lanes 32 (w % 4) .., tile (w / 4) % 2, column half w / 8
+    const int tile = (warp >> 2) & 1, half = warp >> 3, row = (warp & 3) * 32 + lane;
+    const int col0 = half * (kMlpHidden / 2);
     unsigned char* A = smem + tile * kInferTileBytes;
-    const uint32_t trow = tmem + ((uint32_t)((warp & 3) * 32) << 16) + (uint32_t)(tile * kMlpHidden);
-    uint32_t acc_phase = 0;
+    const uint32_t trow = tmem + ((uint32_t)((warp & 3) * 32) << 16) + (uint32_t)(tile * kMlpHidden + col0);
+    float* part = s_part + (tile * 128 + row) * kMlpOut;
+    uint32_t acc_phase = 0, head_phase = 0;
     bool ok = true;
     for (long long gi = 0; gi < my_groups && ok; gi++) {
       const long long q = (blockIdx.x + gi * gridDim.x) * 256 + tile * 128 + row;
       const bool valid = q < g.n;
       const long long qq = valid ? q : g.n - 1;
-      float u[kMlpCoords];
+      // the features of a row split between its two threads: smooth
+      // coordinates 0-3, and smooth 4-5 with the four phases
+      if (half == 0) {
 #pragma unroll
-      for (int c = 0; c < kMlpCoords; c++) u[c] = g.coords[kMlpCoords * qq + c];
+        for (int dd = 0; dd < 4; dd++) write_features(g.coords[kMlpCoords * qq + dd], A, row, 32 * dd);
+      } else {
 #pragma unroll
-      for (int dd = 0; dd < kMlpSmooth; dd++) write_features(u[dd], A, row, 32 * dd);
+        for (int dd = 4; dd < kMlpSmooth; dd++) write_features(g.coords[kMlpCoords * qq + dd], A, row, 32 * dd);
 #pragma unroll
-      for (int dd = 0; dd < kMlpPhases; dd++) write_phase_features(u[kMlpSmooth + dd], A, row, 32 * kMlpSmooth + 16 * dd);
+        for (int dd = 0; dd < kMlpPhases; dd++)
+          write_phase_features(g.coords[kMlpCoords * qq + kMlpSmooth + dd], A, row, 32 * kMlpSmooth + 16 * dd);
+      }
       tc::fence_async_smem();
       tc::fence_before();
       tc::mbar_arrive(act_bar);
@@ -822,13 +837,14 @@ __global__ void __launch_bounds__(kInferThreads, 1) k_surrogate_infer(InferArgs 
         uint32_t rb[2][32];
         tc::tmem_ld32_async(trow, rb[0]);
         tc::tmem_wait_ld(rb[0]);
+        constexpr int kBlocks = kMlpHidden / 2 / 32;
 #pragma unroll
-        for (int blk = 0; blk < kMlpHidden / 32; blk++) {
-          if (blk + 1 < kMlpHidden / 32) tc::tmem_ld32_async(trow + (uint32_t)(32 * (blk + 1)), rb[(blk + 1) & 1]);
+        for (int blk = 0; blk < kBlocks; blk++) {
+          if (blk + 1 < kBlocks) tc::tmem_ld32_async(trow + (uint32_t)(32 * (blk + 1)), rb[(blk + 1) & 1]);
           const uint32_t* r = rb[blk & 1];
 #pragma unroll
           for (int i8 = 0; i8 < 4; i8++) {
-            const int n0 = 32 * blk + 8 * i8;
+            const int n0 = col0 + 32 * blk + 8 * i8;
             const float4 b0 = *reinterpret_cast<const float4*>(hb + n0);
             const float4 b1 = *reinterpret_cast<const float4*>(hb + n0 + 4);
             const float bb[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
@@ -857,7 +873,7 @@ __global__ void __launch_bounds__(kInferThreads, 1) k_surrogate_infer(InferArgs 
               }
             }
           }
-          if (blk + 1 < kMlpHidden / 32) tc::tmem_wait_ld(rb[(blk + 1) & 1]);
+          if (blk + 1 < kBlocks) tc::tmem_wait_ld(rb[(blk + 1) & 1]);
         }
         if (layer < 3) {
           tc::fence_async_smem();
@@ -866,6 +882,23 @@ __global__ void __launch_bounds__(kInferThreads, 1) k_surrogate_infer(InferArgs 
         }
       }
       if (!ok) break;
+      // the head: the second half hands its partial sums to the first
+      if (half == 1) {
+#pragma unroll
+        for (int cc = 0; cc < kMlpOut; cc++) part[cc] = head[cc];
+        tc::mbar_arrive(head_bar);
+        continue;
+      }
+      {
+        const bool done = tc::mbar_wait(head_bar, head_phase & 1, kInferWaitLimit);
+        head_phase++;
+        if (!__all_sync(0xffffffffu, done) || *abort_flag) {
+          ok = false;
+          break;
+        }
+#pragma unroll
+        for (int cc = 0; cc < kMlpOut; cc++) head[cc] += part[cc];
+      }
       bool flag = false;
       if (valid) {
         const float tv[3] = {g.table[3 * q], g.table[3 * q + 1], g.table[3 * q + 2]};
