@@ -160,7 +160,6 @@ constexpr int kBlueThreads = 1024;
 
 struct BlueArgs {
   int m;
-  double sigma;
   const int* seed;       // n pixel indices
   int n;
   const double* table;   // Gauss weights [|dy|][|dx|], (m/2 + 1)^2
@@ -457,8 +456,8 @@ int launch_blue_noise(int m, int n, const int* seed, double sigma, const double*
                       double* density0, unsigned char* mask, unsigned char* work, int* dither, cudaStream_t st) {
   BlueArgs a;
   a.m = m;
-  a.sigma = sigma;
   a.seed = seed;
+  (void)sigma;  // the Gauss weights arrive in `table`
   a.n = n;
   a.table = table;
   a.density = density;
