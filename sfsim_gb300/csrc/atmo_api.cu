@@ -250,6 +250,23 @@ int make_params(const sfsim_atmo_config& c, AtmoParams& P) {
   P.f_R = (float)P.R;
   P.f_Hh2 = (float)P.Hh2;
   P.f_mie_g = (float)P.mie_g;
+  P.f_top = (float)P.top;
+  const double gs[2] = {P.ray_g, P.mie_g};
+  for (int m = 0; m < 2; m++) {
+    const double g = gs[m];
+    double* ph = m ? P.d_phM : P.d_phR;
+    float* fph = m ? P.f_phM : P.f_phR;
+    ph[0] = 3.0 * (1.0 - g * g) / (8.0 * M_PI * (2.0 + g * g));
+    ph[1] = 1.0 + g * g;
+    ph[2] = -2.0 * g;
+    for (int k = 0; k < 3; k++) fph[k] = (float)ph[k];
+  }
+  for (int ch = 0; ch < 3; ch++) {
+    P.d_srcR[ch] = P.intensity[ch] * P.ray_base[ch];
+    P.d_srcM[ch] = P.intensity[ch] * P.mie_base[ch];
+    P.f_srcR[ch] = (float)P.d_srcR[ch];
+    P.f_srcM[ch] = (float)P.d_srcM[ch];
+  }
   return fit_height_polynomial(P);
 }
 
@@ -273,6 +290,10 @@ BuildDims make_dims(const sfsim_atmo_config& c, int B) {
   d.P = (int)v.size();
   sphere_directions(c.ray_steps >> 2, c.ray_steps, M_PI / 2, v, e);
   d.Ph = (int)v.size();
+  d.sun_scale = (d.n2 - 1) / (1 - std::exp(-3.6));
+  d.sun_scale_E = (d.nE1 - 1) / (1 - std::exp(-3.6));
+  d.f_sun_scale = (float)d.sun_scale;
+  d.f_sun_scale_E = (float)d.sun_scale_E;
   return d;
 }
 
@@ -339,6 +360,11 @@ size_t carve(Work<Real>& w, char* base, const BuildDims& d, bool outputs, bool s
   w.setup.rowinfo = c.take<RowInfo>(B * d.rows());
   w.setup.rows = c.take<RowSample<Real>>(B * d.rows() * d.S);
   w.setup.sdirs = c.take<SphereDir<Real>>(B * d.n0 * (long long)(d.P + 1));
+  w.setup.pdirs = c.take<SphereDir<Real>>(B * d.n0 * (long long)dir_row(d.P));
+  w.setup.pcount = c.take<int2>(B * d.n0);
+  w.setup.prow = c.take<PointRow<Real>>(B * d.n0 * d.n2);
+  w.setup.erow = c.take<SurfRow<Real>>(B * d.nE());
+  w.setup.hdir = c.take<HalfDir<Real>>(B * d.nE0 * (long long)d.Ph);
   w.T = c.take<Vec4<Real>>(B * d.nT());
   w.E0 = c.take<Vec4<Real>>(B * d.nE());
   for (int i = 0; i < 2; i++) {
@@ -423,8 +449,8 @@ int run_build(const Work<Real>& w, const BuildDims& d, float* oT, float* oE, flo
               Timer& tm, const sfsim_atmo_intermediates* inter, Vec4<float>* jsum = nullptr) {
   int launches = 0;
   tm.mark_begin(0);
-  launch_setup<Real>(w.params, d, w.dirs, w.ring_end, w.setup, st);
-  launches += 5;
+  launch_setup<Real>(w.params, d, w.dirs, w.ring_end, w.hdirs, w.setup, st);
+  launches += 9;
   tm.mark_end();
   tm.mark_begin(1);
   launch_transmittance<Real>(w.params, d, w.T, st);
@@ -461,8 +487,8 @@ int run_build(const Work<Real>& w, const BuildDims& d, float* oT, float* oE, flo
     Vec4<Real>* E_new = w.Eacc[it & 1];
     Vec4<Real>* S_new = w.Sacc[it & 1];
     tm.mark_begin(5);
-    if (launch_point_scatter<Real>(w.params, d, w.setup.rowinfo, w.setup.sdirs, w.setup.geom, dS_prev, M_first,
-                                   dE_prev, w.J, st))
+    if (launch_point_scatter<Real>(w.params, d, w.setup.rowinfo, w.setup.pdirs, w.setup.pcount, w.setup.prow,
+                                   w.setup.geom, dS_prev, M_first, dE_prev, w.J, st))
       return fail(SFSIM_ATMO_ECUDA, "point scatter launch configuration failed");
     launches++;
     tm.mark_end();
@@ -471,7 +497,7 @@ int run_build(const Work<Real>& w, const BuildDims& d, float* oT, float* oE, flo
       launches++;
     }
     tm.mark_begin(6);
-    launch_surface_radiance<Real>(w.params, d, w.hdirs, dS_prev, M_first, dE_new, st);
+    launch_surface_radiance<Real>(w.params, d, w.setup.erow, w.setup.hdir, dS_prev, M_first, dE_new, st);
     launches++;
     tm.mark_end();
     tm.mark_begin(7);
@@ -650,7 +676,7 @@ int census_impl(const sfsim_atmo_config& cfg, unsigned long long* out, int n) {
     CUDA_TRY(cudaMemcpyAsync(w.ring_end, ring_end.data(), sizeof(int) * ring_end.size(), cudaMemcpyHostToDevice, st));
   }
   CUDA_TRY(cudaMemsetAsync(dcount, 0, 2 * sizeof(unsigned long long), st));
-  launch_setup<Real>(w.params, d, w.dirs, w.ring_end, w.setup, st);
+  launch_setup<Real>(w.params, d, w.dirs, w.ring_end, w.hdirs, w.setup, st);
   launch_first_order_census<Real>(w.params, d, w.setup.rowinfo, w.setup.rows, w.setup.geom, dcount, st);
   CUDA_TRY(cudaGetLastError());
   unsigned long long cnt[2] = {0, 0};

@@ -305,6 +305,12 @@ struct Bulk<float> {
   static __device__ __forceinline__ float km(const AtmoParams& P) { return P.f_km; }
   static __device__ __forceinline__ float ray_ext(const AtmoParams& P, int c) { return P.f_ray_ext[c]; }
   static __device__ __forceinline__ float mie_ext(const AtmoParams& P, int c) { return P.f_mie_ext[c]; }
+  static __device__ __forceinline__ const float* phase_ray(const AtmoParams& P) { return P.f_phR; }
+  static __device__ __forceinline__ const float* phase_mie(const AtmoParams& P) { return P.f_phM; }
+  static __device__ __forceinline__ float src_ray(const AtmoParams& P, int c) { return P.f_srcR[c]; }
+  static __device__ __forceinline__ float src_mie(const AtmoParams& P, int c) { return P.f_srcM[c]; }
+  static __device__ __forceinline__ float sun_scale(const BuildDims& d) { return d.f_sun_scale; }
+  static __device__ __forceinline__ float sun_scale_E(const BuildDims& d) { return d.f_sun_scale_E; }
 };
 
 template <>
@@ -323,6 +329,45 @@ struct Bulk<double> {
   static __device__ __forceinline__ double km(const AtmoParams& P) { return P.d_km; }
   static __device__ __forceinline__ double ray_ext(const AtmoParams& P, int c) { return P.d_ray_ext[c]; }
   static __device__ __forceinline__ double mie_ext(const AtmoParams& P, int c) { return P.d_mie_ext[c]; }
+  static __device__ __forceinline__ const double* phase_ray(const AtmoParams& P) { return P.d_phR; }
+  static __device__ __forceinline__ const double* phase_mie(const AtmoParams& P) { return P.d_phM; }
+  static __device__ __forceinline__ double src_ray(const AtmoParams& P, int c) { return P.d_srcR[c]; }
+  static __device__ __forceinline__ double src_mie(const AtmoParams& P, int c) { return P.d_srcM[c]; }
+  static __device__ __forceinline__ double sun_scale(const BuildDims& d) { return d.sun_scale; }
+  static __device__ __forceinline__ double sun_scale_E(const BuildDims& d) { return d.sun_scale_E; }
+};
+
+// A view row's geometry in Real: the FP32 copies for FP32 kernels, so that
+// they convert nothing on the (slow) FP64 pipe.
+template <class Real>
+struct RowR {
+  Real r, sv, cv, D[3], Ls;
+};
+__device__ __forceinline__ void row_r(const RowInfo& ri, RowR<float>& o) {
+  o.r = ri.f_r, o.sv = ri.f_sv, o.cv = ri.f_cv, o.Ls = ri.f_Ls;
+  o.D[0] = ri.f_D[0], o.D[1] = ri.f_D[1], o.D[2] = ri.f_D[2];
+}
+__device__ __forceinline__ void row_r(const RowInfo& ri, RowR<double>& o) {
+  o.r = ri.r, o.sv = ri.sv, o.cv = ri.cv, o.Ls = ri.Ls;
+  o.D[0] = ri.D[0], o.D[1] = ri.D[1], o.D[2] = ri.D[2];
+}
+template <class Real>
+__device__ __forceinline__ RowR<Real> row_r(const RowInfo& ri) {
+  RowR<Real> o;
+  row_r(ri, o);
+  return o;
+}
+
+// Cornette-Shanks phase k (1 + mu^2) (a + b mu)^-3/2 from the host-computed
+// coefficients {k, a, b} of AtmoParams.
+template <class Real>
+struct PhaseCS {
+  Real k, a, b;
+  __device__ __forceinline__ explicit PhaseCS(const Real* c) : k(c[0]), a(c[1]), b(c[2]) {}
+  __device__ __forceinline__ Real operator()(Real mu) const {
+    const Real r = Bulk<Real>::rsqrt(fma(b, mu, a));
+    return k * fma(mu, mu, Real(1)) * (r * r * r);
+  }
 };
 
 template <class Real>

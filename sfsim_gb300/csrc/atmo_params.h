@@ -44,6 +44,14 @@ struct AtmoParams {
   float f_R, f_Hh2, f_mie_g;
   float f_bright_pi[3];               // brightness / pi
   float f_intensity[3];
+  // Cornette-Shanks phase as k (1 + mu^2) (a + b mu)^-3/2: {k, a, b} with
+  // k = 3 (1 - g^2) / (8 pi (2 + g^2)), a = 1 + g^2, b = -2 g
+  double d_phR[3], d_phM[3];
+  float f_phR[3], f_phM[3];
+  // intensity * scatter base, the first-order source factors
+  double d_srcR[3], d_srcM[3];
+  float f_srcR[3], f_srcM[3];
+  float f_top;
   int hpoly_n;                        // number of coefficients
 };
 
@@ -58,6 +66,10 @@ struct BuildDims {
   int P;                   // directions of integral-sphere(sphere_steps)
   int Ph;                  // directions of integral-half-sphere(ray_steps)
   int iterations;
+  // (size - 1) / (1 - exp(-3.6)) of the sun-elevation axes of the ray-scatter
+  // space (n2) and of the surface-radiance space (nE1)
+  double sun_scale, sun_scale_E;
+  float f_sun_scale, f_sun_scale_E;
   SFSIM_HD long long nT() const { return (long long)nT0 * nT1; }
   SFSIM_HD long long nE() const { return (long long)nE0 * nE1; }
   SFSIM_HD long long n4() const { return (long long)n0 * n1 * n2 * n3; }
@@ -102,14 +114,45 @@ struct alignas(4 * sizeof(Real)) CellGeom {
   Real lx, ly, lz, mu;
 };
 
-// Per view row (height i, elevation j) of the 4-D space, FP64.
+// Per view row (height i, elevation j) of the 4-D space, FP64, with FP32
+// copies for the FP32 kernels.
 struct RowInfo {
   double r;            // |x|, x = (r, 0, 0)
   double sv, cv;       // view direction (sv, cv, 0)
   double D[3];         // ray segment from x to its extremity
   double L;            // |D|
+  double Ls;           // L / ray steps
+  float f_r, f_sv, f_cv, f_D[3], f_Ls;
   int above;           // above-horizon flag of the node
-  int pad;
+};
+
+// Per (height i, sun elevation k) of the 4-D space, from FP64: the height
+// and sun-elevation coordinates of point scatter's dS lookups at x, and the
+// scattering coefficients beta(x) it multiplies its sums with.
+template <class Real>
+struct PointRow {
+  int u0, u2;
+  Real s0, s2;
+  Real bR[3], bM[3];
+};
+
+// Per node (height iE, sun elevation kE) of the surface-radiance space, from
+// FP64: the dS lookup's height and sun-elevation coordinates at x = (r, 0, 0)
+// and the terms of the elevation coordinate of (x, w) (atmosphere.clj:239-253):
+// H^2 - q, 2 rho + 2 H, r; and the light direction (lx, ly, 0).
+template <class Real>
+struct SurfRow {
+  int u0, u2;
+  Real s0, s2;
+  Real Hh2mq, den, rr, lx, ly;
+};
+
+// A direction of the surface-radiance half-sphere integral in world
+// coordinates at the height of row iE: its first two components and its
+// quadrature weight times w.n.
+template <class Real>
+struct HalfDir {
+  Real wx, wy, wgt;
 };
 
 // Per view row and ray sample s (p_s = x + D (s + 1/2)/S).

@@ -74,7 +74,7 @@ __global__ void k_sun_table(const AtmoParams* params, int S, float2* table) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= kSunNR * kSunNM) return;
   const int i = t / kSunNM, j = t - (t / kSunNM) * kSunNM;
-  const float Hh2 = P.f_Hh2, R2 = P.f_R * P.f_R, top = (float)P.top;
+  const float Hh2 = P.f_Hh2, R2 = P.f_R * P.f_R, top = P.f_top;
   const float xr = (float)i / (float)(kSunNR - 1), xm = (float)j / (float)(kSunNM - 1);
   const float q = xr * xr * Hh2;
   const float cq = fmaxf(Hh2 - q, 0.0f);  // top^2 - r^2
@@ -105,7 +105,7 @@ void launch_sun_table(const AtmoParams* params, const BuildDims& d, float2* tabl
 // Bilinear lookup of the table at (q, exit distance) for a climbing ray.
 __device__ __forceinline__ float2 sun_lookup(const float2* __restrict__ tab, const AtmoParams& P, float q,
                                              float texit) {
-  const float Hh2 = P.f_Hh2, R2 = P.f_R * P.f_R, top = (float)P.top;
+  const float Hh2 = P.f_Hh2, R2 = P.f_R * P.f_R, top = P.f_top;
   const float qc = fminf(fmaxf(q, 0.0f), Hh2);
   const float cq = Hh2 - qc;
   const float r = sqrtf(R2 + qc);
@@ -151,7 +151,7 @@ __global__ void __launch_bounds__(WARPS * 32, 4) k_first_order(const AtmoParams*
   const RowInfo ri = rowinfo[b * nrows + row];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int ncell = d.n2 * d.n3;
-  const Real Hh2 = (Real)P.Hh2;
+  const Real Hh2 = std::is_same<Real, float>::value ? (Real)P.f_Hh2 : (Real)P.Hh2;
   constexpr int NP = Bulk<Real>::kSunNP;
   const Real* hp = Bulk<Real>::hpr(P);
   Real hc[NP];
@@ -166,8 +166,9 @@ __global__ void __launch_bounds__(WARPS * 32, 4) k_first_order(const AtmoParams*
     mext[c] = Bulk<Real>::mie_ext(P, c);
   }
   const Real inv_steps = Real(1) / Real(S);
-  const double stepsize = 1.0 / S;
-  const Real rr = (Real)ri.r, D0 = (Real)ri.D[0], D1 = (Real)ri.D[1], D2 = (Real)ri.D[2];
+  const RowR<Real> rw = row_r<Real>(ri);
+  const Real rr = rw.r, D0 = rw.D[0], D1 = rw.D[1], D2 = rw.D[2];
+  const PhaseCS<Real> phase_ray(Bulk<Real>::phase_ray(P));
   const long long node0 = (b * nrows + row) * ncell;
   const float2* tab = sun_table ? sun_table + (long long)b * kSunNR * kSunNM : nullptr;
 
@@ -213,16 +214,16 @@ __global__ void __launch_bounds__(WARPS * 32, 4) k_first_order(const AtmoParams*
       accM[c] = warp_sum(accM[c]);
     }
     if (lane == 0) {
-      const Real wR = (Real)(ri.L * stepsize);
-      const Real phR = phase_cs<Real>((Real)P.ray_g, g.mu);
+      const Real wR = rw.Ls;
+      const Real phR = phase_ray(g.mu);
       Vec4<Real> o1, o2;
-      o1.x = wR * phR * (Real)(P.intensity[0] * P.ray_base[0]) * accR[0];
-      o1.y = wR * phR * (Real)(P.intensity[1] * P.ray_base[1]) * accR[1];
-      o1.z = wR * phR * (Real)(P.intensity[2] * P.ray_base[2]) * accR[2];
+      o1.x = wR * phR * Bulk<Real>::src_ray(P, 0) * accR[0];
+      o1.y = wR * phR * Bulk<Real>::src_ray(P, 1) * accR[1];
+      o1.z = wR * phR * Bulk<Real>::src_ray(P, 2) * accR[2];
       o1.w = 0;
-      o2.x = wR * (Real)(P.intensity[0] * P.mie_base[0]) * accM[0];
-      o2.y = wR * (Real)(P.intensity[1] * P.mie_base[1]) * accM[1];
-      o2.z = wR * (Real)(P.intensity[2] * P.mie_base[2]) * accM[2];
+      o2.x = wR * Bulk<Real>::src_mie(P, 0) * accM[0];
+      o2.y = wR * Bulk<Real>::src_mie(P, 1) * accM[1];
+      o2.z = wR * Bulk<Real>::src_mie(P, 2) * accM[2];
       o2.w = 0;
       rayleigh[node0 + cell] = o1;
       mie[node0 + cell] = o2;

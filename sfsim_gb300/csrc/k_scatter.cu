@@ -1,6 +1,9 @@
 // k_scatter.cu -- multiple-scattering passes of the atmosphere LUT build
 // (atmosphere_lut.clj:86-97): point scatter J, surface radiance dE, ray
 // scatter dS, and the re-interpolating accumulation of E and S.
+#include <cstddef>
+#include <type_traits>
+
 #include "atmo_device.cuh"
 #include "kernels.h"
 
@@ -18,22 +21,6 @@ namespace sfsim {
 // staged in shared memory.  One thread per node (elevation j, heading a);
 // directions, ground ends and T(x, ground) come from k_sphere_setup.
 // ---------------------------------------------------------------------------
-
-// Cornette-Shanks phase with its g-only factors hoisted:
-// phase = k (1 + mu^2) (a + b mu)^-3/2, k = 3(1-g^2)/(8 pi (2+g^2)), a = 1+g^2, b = -2g.
-template <class Real>
-struct PhaseCS {
-  Real k, a, b;
-  __device__ __forceinline__ PhaseCS(double g) {
-    k = (Real)(3.0 * (1.0 - g * g) / (8.0 * 3.14159265358979323846 * (2.0 + g * g)));
-    a = (Real)(1.0 + g * g);
-    b = (Real)(-2.0 * g);
-  }
-  __device__ __forceinline__ Real operator()(Real mu) const {
-    const Real r = Bulk<Real>::rsqrt(fma(b, mu, a));
-    return k * fma(mu, mu, Real(1)) * (r * r * r);
-  }
-};
 
 template <class Real>
 __device__ __forceinline__ void gather_heading_row(const Vec4<Real>* t, const BuildDims& d, int u0, int v0, Real s0,
@@ -77,55 +64,64 @@ struct TexelRow {
   }
 };
 
-// Direction vector and quadrature weight of a SphereDir.
+// Direction vector and quadrature weight of a SphereDir in shared memory:
+// one 16-byte broadcast load for FP32 entries.
 template <class Real>
-__device__ __forceinline__ void load_dir(const SphereDir<Real>& D, Real& w0, Real& w1, Real& w2, Real& weight) {
-  w0 = D.w[0], w1 = D.w[1], w2 = D.w[2], weight = D.weight;
+__device__ __forceinline__ void load_dir(const SphereDir<Real>& D, Real& x0, Real& x1, Real& x2, Real& weight) {
+  x0 = D.w[0], x1 = D.w[1], x2 = D.w[2], weight = D.weight;
+}
+template <>
+__device__ __forceinline__ void load_dir<float>(const SphereDir<float>& D, float& x0, float& x1, float& x2,
+                                                float& weight) {
+  static_assert(offsetof(SphereDir<float>, weight) == 12 && sizeof(SphereDir<float>) % 16 == 0, "layout");
+  const float4 v = *reinterpret_cast<const float4*>(&D);
+  x0 = v.x, x1 = v.y, x2 = v.z, weight = v.w;
 }
 
 template <class Real, bool FIRST>
 __global__ void __launch_bounds__(256, 3) k_point_scatter(const AtmoParams* params, BuildDims d,
-                                                          const RowInfo* rowinfo, const SphereDir<Real>* sdirs,
-                                                          const CellGeom<Real>* geom, const Vec4<Real>* dS,
-                                                          const Vec4<Real>* Mt, const Vec4<Real>* dE,
-                                                          Vec4<Real>* J, int nchunks) {
+                                                          const RowInfo* rowinfo, const SphereDir<Real>* pdirs,
+                                                          const int2* pcount, const PointRow<Real>* prow,
+                                                          const CellGeom<Real>* geom,
+                                                          const Vec4<Real>* dS, const Vec4<Real>* Mt,
+                                                          const Vec4<Real>* dE, Vec4<Real>* J, int nchunks) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   using TR = TexelRow<Real>;
   constexpr int RS = TR::kStride;
+  constexpr int DB = kDirBlock;
   const int b = blockIdx.y;
   const int chunk = blockIdx.x % nchunks;
   const int ik = blockIdx.x / nchunks;
   const int i = ik / d.n2, k = ik % d.n2;
   const AtmoParams& P = params[b];
-  const int nrow = d.P * d.n3;
+  const PointRow<Real>* prk = prow + ((long long)b * d.n0 + i) * d.n2 + k;
+  const int2 pc = pcount[(long long)b * d.n0 + i];
+  const int sky_end = pc.x, used = pc.y;
+  const int nrow = used * d.n3;
   SphereDir<Real>* dirs = reinterpret_cast<SphereDir<Real>*>(smem_raw);
-  Real* rows = reinterpret_cast<Real*>(dirs + d.P);
+  Real* rows = reinterpret_cast<Real*>(dirs + dir_row(d.P));
   Real* rowsM = rows + RS * nrow;
   Real* etab = rowsM + (FIRST ? RS * nrow : 0);
 
-  // the (i, k) coordinates, FP64 as in ray-scatter-forward
-  const double r = index_to_radius(P, d.n0, (double)i);
-  const double ss = index_to_sin_sun_elevation(d.n2, (double)k);
-  int u0, u2;
-  Real s0, s2;
-  split_coord<Real>(height_to_index(P, d.n0, r), d.n0, &u0, &s0);
-  split_coord<Real>(sun_elevation_to_index(d.n2, mk3(r, 0, 0), mk3(ss, 0, 0)), d.n2, &u2, &s2);
+  // the (i, k) coordinates of the dS lookups
+  const int u0 = prk->u0, u2 = prk->u2;
+  const Real s0 = prk->s0, s2 = prk->s2;
   const int v0 = upper_index(u0, d.n0), v2 = upper_index(u2, d.n2);
 
   const long long base4 = (long long)b * d.n4();
-  const SphereDir<Real>* src = sdirs + ((long long)b * d.n0 + i) * d.P;
-  for (int t = threadIdx.x; t < d.P; t += blockDim.x) dirs[t] = src[t];
+  const SphereDir<Real>* src = pdirs + ((long long)b * d.n0 + i) * dir_row(d.P);
+  for (int t = threadIdx.x; t < used; t += blockDim.x) dirs[t] = src[t];
   for (int t = threadIdx.x; t < nrow; t += blockDim.x) {
     const int w = t / d.n3, a = t - w * d.n3;
-    const int u1 = src[w].u1, v1 = upper_index(u1, d.n1);
-    const Real s1 = src[w].s1;
-    Real v[3];
-    gather_heading_row(dS + base4, d, u0, v0, s0, u1, v1, s1, u2, v2, s2, a, v);
-    TR::store(rows, t, v);
-    if (FIRST) {
-      gather_heading_row(Mt + base4, d, u0, v0, s0, u1, v1, s1, u2, v2, s2, a, v);
-      TR::store(rowsM, t, v);
+    Real v[3] = {0, 0, 0}, vm[3] = {0, 0, 0};
+    if (!src[w].pad) {
+      const int u1 = src[w].u1, v1 = upper_index(u1, d.n1);
+      const Real s1 = src[w].s1;
+      gather_heading_row(dS + base4, d, u0, v0, s0, u1, v1, s1, u2, v2, s2, a, v);
+      if (FIRST) gather_heading_row(Mt + base4, d, u0, v0, s0, u1, v1, s1, u2, v2, s2, a, vm);
     }
+    TR::store(rows, t, v);
+    if (FIRST) TR::store(rowsM, t, vm);
   }
   const long long nE = d.nE();
   for (int t = threadIdx.x; t < nE; t += blockDim.x) {
@@ -141,47 +137,46 @@ __global__ void __launch_bounds__(256, 3) k_point_scatter(const AtmoParams* para
   const bool valid = cell_raw < nslab;
   const int cell = valid ? cell_raw : nslab - 1;
   const int j = cell / d.n3, a = cell % d.n3;
-  const RowInfo ri = rowinfo[(long long)b * d.rows() + (long long)i * d.n1 + j];
-  const Real sv = (Real)ri.sv, cv = (Real)ri.cv;
+  const RowR<Real> rw = row_r<Real>(rowinfo[(long long)b * d.rows() + (long long)i * d.n1 + j]);
+  const Real sv = rw.sv, cv = rw.cv;
   const long long node = base4 + idx4(d, i, j, k, a);
   const CellGeom<Real> g = geom[node];
-  const PhaseCS<Real> phR(P.ray_g), phM(P.mie_g);
+  const PhaseCS<Real> phR(Bulk<Real>::phase_ray(P)), phM(Bulk<Real>::phase_mie(P));
   const Real scale3 = Real(0.5) * Real(d.n3 - 1);
-  const Real scaleE = (Real)((d.nE1 - 1) / (1 - exp(-3.6)));
+  const Real scaleE = Bulk<Real>::sun_scale_E(d);
   // The weighted phases depend on (j, direction) only.  When the n3 headings
-  // of one j fill aligned lane groups, each lane evaluates them for one
-  // direction of a batch of n3 and the group exchanges them by shuffles.
+  // of one j fill aligned lane groups of at least DB lanes, lane p of a group
+  // evaluates them for direction p of a block of DB and the group exchanges
+  // them by shuffles.
   const int G = d.n3;
-  const bool share = (32 % G == 0) && (blockDim.x % G == 0);
+  const bool share = G >= DB && (32 % G == 0) && (blockDim.x % G == 0);
   const int lane = threadIdx.x & 31;
   const int gbase = share ? (lane & ~(G - 1)) : lane;
   const int gpos = lane - gbase;
+  const int row_len = RS * d.n3;
 
   Real accR[3] = {0, 0, 0}, accM[3] = {0, 0, 0}, cR[3] = {0, 0, 0}, cM[3] = {0, 0, 0};
   Real ringR[3] = {0, 0, 0}, ringM[3] = {0, 0, 0};
-  const int step = share ? G : 1;
-  const int row_len = RS * d.n3;
-  for (int w0 = 0; w0 < d.P; w0 += step) {
+  // One block of DB directions starting at w0 (all sky or all ground),
+  // summed plainly into ringR/ringM.
+  auto dir_block = [&](int w0, auto ground) {
     Real wRb = 0, wMb = 0;
-    if (share) {
-      const int wb = w0 + gpos;
-      if (wb < d.P) {
-        Real x0, x1, x2, wt;
-        load_dir(dirs[wb], x0, x1, x2, wt);
-        const Real mu_v = fma(sv, x0, cv * x1);
-        wRb = wt * phR(mu_v);
-        wMb = wt * phM(mu_v);
-      }
+    if (share && gpos < DB) {
+      Real x0, x1, x2, wt;
+      load_dir(dirs[w0 + gpos], x0, x1, x2, wt);
+      const Real mu_v = fma(sv, x0, cv * x1);
+      wRb = wt * phR(mu_v);
+      wMb = wt * phM(mu_v);
     }
-    const int wend = min(w0 + step, d.P);
-    for (int w = w0; w < wend; w++) {
-      const SphereDir<Real>& D = dirs[w];
+#pragma unroll
+    for (int q = 0; q < DB; q++) {
+      const SphereDir<Real>& D = dirs[w0 + q];
       Real x0, x1, x2, wt;
       load_dir(D, x0, x1, x2, wt);
       Real wR, wM;
       if (share) {
-        wR = __shfl_sync(0xffffffffu, wRb, gbase + (w - w0));
-        wM = __shfl_sync(0xffffffffu, wMb, gbase + (w - w0));
+        wR = __shfl_sync(0xffffffffu, wRb, gbase + q);
+        wM = __shfl_sync(0xffffffffu, wMb, gbase + q);
       } else {
         const Real mu_v = fma(sv, x0, cv * x1);
         wR = wt * phR(mu_v);
@@ -194,20 +189,20 @@ __global__ void __launch_bounds__(256, 3) k_point_scatter(const AtmoParams* para
       split_coord_r<Real>(fma(scale3, mu_l, scale3), d.n3, &u3, &s3);
       const int v3 = upper_index(u3, d.n3);
       Real X[3], lo[3], hi[3];
-      const Real* row_w = rows + w * row_len;
+      const Real* row_w = rows + (w0 + q) * row_len;
       TR::load(row_w, u3, lo);
       TR::load(row_w, v3, hi);
 #pragma unroll
       for (int c = 0; c < 3; c++) X[c] = fma(hi[c] - lo[c], s3, lo[c]);
       if (FIRST) {
         const Real ph = phM(mu_l);
-        const Real* rowM_w = rowsM + w * row_len;
+        const Real* rowM_w = rowsM + (w0 + q) * row_len;
         TR::load(rowM_w, u3, lo);
         TR::load(rowM_w, v3, hi);
 #pragma unroll
         for (int c = 0; c < 3; c++) X[c] = fma(fma(hi[c] - lo[c], s3, lo[c]), ph, X[c]);
       }
-      if (D.surface) {
+      if (decltype(ground)::value) {
         const Real sg = fma(D.gdir[0], g.lx, fma(D.gdir[1], g.ly, D.gdir[2] * g.lz));
         int uE1;
         Real sE1;
@@ -227,38 +222,49 @@ __global__ void __launch_bounds__(256, 3) k_point_scatter(const AtmoParams* para
         ringR[c] = fma(wR, X[c], ringR[c]);
         ringM[c] = fma(wM, X[c], ringM[c]);
       }
-      if (D.pad) {  // last direction of a theta ring
-#pragma unroll
-        for (int c = 0; c < 3; c++) {
-          kahan_add(accR[c], cR[c], ringR[c]);
-          kahan_add(accM[c], cM[c], ringM[c]);
-          ringR[c] = 0;
-          ringM[c] = 0;
-        }
-      }
     }
+  };
+  // the partial sums of up to two blocks go to the compensated totals
+  auto flush = [&]() {
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+      kahan_add(accR[c], cR[c], ringR[c]);
+      kahan_add(accM[c], cM[c], ringM[c]);
+      ringR[c] = ringM[c] = 0;
+    }
+  };
+  for (int w0 = 0; w0 < sky_end; w0 += DB) {
+    dir_block(w0, std::false_type{});
+    if (w0 & DB) flush();
   }
+  flush();
+  for (int w0 = sky_end; w0 < used; w0 += DB) {
+    dir_block(w0, std::true_type{});
+    if ((w0 - sky_end) & DB) flush();
+  }
+  flush();
   if (!valid) return;
   // beta_c(x) (atmosphere.clj:42-47, 140-151)
-  const double h = r - P.R;
-  const double er = exp(-(h / P.ray_scale)), em = exp(-(h / P.mie_scale));
+  const PointRow<Real> pr = *prk;
   Vec4<Real> o;
-  o.x = (Real)(P.ray_base[0] * er) * accR[0] + (Real)(P.mie_base[0] * em) * accM[0];
-  o.y = (Real)(P.ray_base[1] * er) * accR[1] + (Real)(P.mie_base[1] * em) * accM[1];
-  o.z = (Real)(P.ray_base[2] * er) * accR[2] + (Real)(P.mie_base[2] * em) * accM[2];
+  o.x = pr.bR[0] * accR[0] + pr.bM[0] * accM[0];
+  o.y = pr.bR[1] * accR[1] + pr.bM[1] * accM[1];
+  o.z = pr.bR[2] * accR[2] + pr.bM[2] * accM[2];
   o.w = 0;
   J[node] = o;
 }
 
 template <class Real>
 size_t point_scatter_smem(const BuildDims& d, bool first) {
-  return sizeof(SphereDir<Real>) * d.P + sizeof(Real) * 3 * ((size_t)d.P * d.n3 * (first ? 2 : 1) + d.nE());
+  return sizeof(SphereDir<Real>) * dir_row(d.P) +
+         sizeof(Real) * 3 * ((size_t)dir_row(d.P) * d.n3 * (first ? 2 : 1) + d.nE());
 }
 
 template <class Real>
 int launch_point_scatter(const AtmoParams* params, const BuildDims& d, const RowInfo* rowinfo,
-                         const SphereDir<Real>* sdirs, const CellGeom<Real>* geom, const Vec4<Real>* dS,
-                         const Vec4<Real>* mie, const Vec4<Real>* dE, Vec4<Real>* J, cudaStream_t st) {
+                         const SphereDir<Real>* pdirs, const int2* pcount, const PointRow<Real>* prow,
+                         const CellGeom<Real>* geom, const Vec4<Real>* dS, const Vec4<Real>* mie,
+                         const Vec4<Real>* dE, Vec4<Real>* J, cudaStream_t st) {
   const int block = 256;
   const int nchunks = (d.n1 * d.n3 + block - 1) / block;
   const bool first = mie != nullptr;
@@ -268,13 +274,14 @@ int launch_point_scatter(const AtmoParams* params, const BuildDims& d, const Row
     if (cudaFuncSetAttribute(k_point_scatter<Real, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
         cudaSuccess)
       return -1;
-    k_point_scatter<Real, true><<<grid, block, smem, st>>>(params, d, rowinfo, sdirs, geom, dS, mie, dE, J, nchunks);
+    k_point_scatter<Real, true><<<grid, block, smem, st>>>(params, d, rowinfo, pdirs, pcount, prow, geom, dS, mie,
+                                                           dE, J, nchunks);
   } else {
     if (cudaFuncSetAttribute(k_point_scatter<Real, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)smem) != cudaSuccess)
       return -1;
-    k_point_scatter<Real, false><<<grid, block, smem, st>>>(params, d, rowinfo, sdirs, geom, dS, mie, dE, J,
-                                                            nchunks);
+    k_point_scatter<Real, false><<<grid, block, smem, st>>>(params, d, rowinfo, pdirs, pcount, prow, geom, dS,
+                                                            mie, dE, J, nchunks);
   }
   return 0;
 }
@@ -283,46 +290,39 @@ int launch_point_scatter(const AtmoParams* params, const BuildDims& d, const Row
 // Surface radiance dE (atmosphere.clj:225-230): integral over the upper half
 // sphere of dS(x, w, l, above) (w.n); the reference passes the ray steps as
 // the sphere steps (atmosphere_lut.clj:89).  One block per node, threads over
-// directions, FP64 coordinates (the work is small), block reduction.
+// directions, block reduction.  The per-node coordinates and the world-space
+// directions come from FP64 setup tables, so no thread uses the FP64 pipe.
 // ---------------------------------------------------------------------------
 
 template <class Real, bool FIRST>
 __global__ void __launch_bounds__(256) k_surface_radiance(const AtmoParams* params, BuildDims d,
-                                                          const DirLocal* hdirs, const Vec4<Real>* dS,
-                                                          const Vec4<Real>* Mt, Vec4<Real>* dE) {
+                                                          const SurfRow<Real>* erow, const HalfDir<Real>* hdir,
+                                                          const Vec4<Real>* dS, const Vec4<Real>* Mt,
+                                                          Vec4<Real>* dE) {
   __shared__ Real red[3][256];
   const int b = blockIdx.y;
   const long long node = blockIdx.x;
   const AtmoParams& P = params[b];
-  const int iE = (int)(node / d.nE1), kE = (int)(node % d.nE1);
-  // FP64 per node: x = (r, 0, 0), l = (sin, cos, 0), the frame, and the
-  // height and sun-elevation coordinates shared by every direction
-  const double r = index_to_radius(P, d.nE0, (double)iE);
-  const double ss = index_to_sin_sun_elevation(d.nE1, (double)kE);
-  const d3 x = mk3(r, 0, 0), l = mk3(ss, sqrt(dmax(0.0, 1 - sqr(ss))), 0);
-  const d3 n = mul3(x, 1.0 / mag3(x));
-  const d3 o1 = orthogonal(n);
-  const d3 o2 = cross3(n, o1);
-  int u[4];
-  Real s[4];
-  split_coord<Real>(height_to_index(P, d.n0, mag3(x)), d.n0, &u[0], &s[0]);
-  split_coord<Real>(sun_elevation_to_index(d.n2, x, l), d.n2, &u[2], &s[2]);
-  const double c0 = dmul(dsub(r, P.R), dadd(r, P.R));  // |x|^2 - R^2
+  const int iE = (int)(node / d.nE1);
+  // per node, from FP64 (k_surface_rows): x = (r, 0, 0), l = (lx, ly, 0) and
+  // the height and sun-elevation coordinates shared by every direction
+  const SurfRow<Real> er = erow[(long long)b * d.nE() + node];
+  int u[4] = {er.u0, 0, er.u2, 0};
+  Real s[4] = {er.s0, 0, er.s2, 0};
   // elevation coordinate of (x, w, above) (atmosphere.clj:239-253) in Real:
   // r sin_el = x.w, rho^2 = q, Delta + H^2 = (x.w)^2 + (H^2 - q) with both
   // terms non-negative, and r sin_el - sqrt(Delta + H^2) rewritten without
   // cancellation when x.w > 0
-  const Real q = (Real)c0, Hh2mq = (Real)dsub(P.Hh2, c0), rho = (Real)sqrt(dmax(0.0, c0));
-  const Real den = rho + rho + Real(2) * (Real)P.Hh, rr = (Real)r;
-  const Real lx = (Real)l.x, ly = (Real)l.y;
+  const Real Hh2mq = er.Hh2mq, den = er.den, rr = er.rr, lx = er.lx, ly = er.ly;
   const Real scale1 = Real(d.n1 - 1), scale3 = Real(0.5) * Real(d.n3 - 1);
   const Vec4<Real>* tS = dS + (long long)b * d.n4();
   const Vec4<Real>* tM = FIRST ? Mt + (long long)b * d.n4() : nullptr;
+  const HalfDir<Real>* hd = hdir + ((long long)b * d.nE0 + iE) * d.Ph;
+  const PhaseCS<Real> phase_mie(Bulk<Real>::phase_mie(P));
   Real acc[3] = {0, 0, 0}, cmp[3] = {0, 0, 0};
   for (int w = threadIdx.x; w < d.Ph; w += blockDim.x) {
-    const DirLocal qd = hdirs[w];
-    const d3 omega = to_world(n, o1, o2, qd);
-    const Real wx = (Real)omega.x, wy = (Real)omega.y;
+    const HalfDir<Real> qd = hd[w];
+    const Real wx = qd.wx, wy = qd.wy;
     const Real pv = rr * wx;
     const Real root = Bulk<Real>::sqrt(fma(pv, pv, Hh2mq));
     const Real a = pv > Real(0) ? -Hh2mq / (pv + root) : pv - root;
@@ -346,15 +346,14 @@ __global__ void __launch_bounds__(256) k_surface_radiance(const AtmoParams* para
     if (FIRST) {
       Real vm[3];
       interp4(tM, d, uu, sx, vm);
-      const Real ph = phase_cs<Real>((Real)P.mie_g, mu);
+      const Real ph = phase_mie(mu);
 #pragma unroll
       for (int c = 0; c < 3; c++) val[c] = fma(vm[c], ph, val[c]);
     }
-    const Real wgt = (Real)(qd.w * dot3(omega, n));
+    const Real wgt = qd.wgt;
 #pragma unroll
     for (int c = 0; c < 3; c++) kahan_add(acc[c], cmp[c], val[c] * wgt);
   }
-  (void)q;
 #pragma unroll
   for (int c = 0; c < 3; c++) red[c][threadIdx.x] = acc[c];
   __syncthreads();
@@ -376,13 +375,14 @@ __global__ void __launch_bounds__(256) k_surface_radiance(const AtmoParams* para
 }
 
 template <class Real>
-void launch_surface_radiance(const AtmoParams* params, const BuildDims& d, const DirLocal* half_dirs,
-                             const Vec4<Real>* dS, const Vec4<Real>* mie, Vec4<Real>* dE, cudaStream_t st) {
+void launch_surface_radiance(const AtmoParams* params, const BuildDims& d, const SurfRow<Real>* erow,
+                             const HalfDir<Real>* hdir, const Vec4<Real>* dS, const Vec4<Real>* mie,
+                             Vec4<Real>* dE, cudaStream_t st) {
   dim3 grid((unsigned)d.nE(), d.B);
   if (mie)
-    k_surface_radiance<Real, true><<<grid, 256, 0, st>>>(params, d, half_dirs, dS, mie, dE);
+    k_surface_radiance<Real, true><<<grid, 256, 0, st>>>(params, d, erow, hdir, dS, mie, dE);
   else
-    k_surface_radiance<Real, false><<<grid, 256, 0, st>>>(params, d, half_dirs, dS, mie, dE);
+    k_surface_radiance<Real, false><<<grid, 256, 0, st>>>(params, d, erow, hdir, dS, mie, dE);
 }
 
 // ---------------------------------------------------------------------------
@@ -396,18 +396,61 @@ void launch_surface_radiance(const AtmoParams* params, const BuildDims& d, const
 // T(x, p_s) comes from k_view_rows.
 // ---------------------------------------------------------------------------
 
+// Per-sample constants, laid out so that FP32 blocks read each group with
+// one 16-byte broadcast load: {T, us} and {inv_r, -, s0, s1} for the
+// nodes, {s0, s1} and the J offsets for the plane build.
 template <class Real>
 struct RaySample {
-  Real T[3];
-  Real us, inv_r, s0, s1;
+  Real T[3], us;
+  Real inv_r, unused, s0, s1;
   int p00, p01, p10, p11;  // J offsets of the four (height, elevation) planes
 };
 
+template <class Real>
+struct SampleView {
+  Real T[3], us, inv_r;
+  __device__ __forceinline__ SampleView(const RaySample<Real>& v) {
+    T[0] = v.T[0], T[1] = v.T[1], T[2] = v.T[2], us = v.us, inv_r = v.inv_r;
+  }
+};
+template <>
+struct SampleView<float> {
+  float T[3], us, inv_r;
+  __device__ __forceinline__ SampleView(const RaySample<float>& v) {
+    const float4 a = *reinterpret_cast<const float4*>(&v);
+    T[0] = a.x, T[1] = a.y, T[2] = a.z, us = a.w;
+    inv_r = v.inv_r;
+  }
+};
+
+template <class Real>
+struct SampleCorners {
+  int p[4];
+  Real s0, s1;
+  __device__ __forceinline__ SampleCorners(const RaySample<Real>& v) {
+    p[0] = v.p00, p[1] = v.p01, p[2] = v.p10, p[3] = v.p11, s0 = v.s0, s1 = v.s1;
+  }
+};
+template <>
+struct SampleCorners<float> {
+  int p[4];
+  float s0, s1;
+  __device__ __forceinline__ SampleCorners(const RaySample<float>& v) {
+    static_assert(sizeof(RaySample<float>) == 48 && offsetof(RaySample<float>, p00) == 32, "layout");
+    const int4 o = *reinterpret_cast<const int4*>(&v.p00);
+    const float2 f = *reinterpret_cast<const float2*>(&v.s0);
+    p[0] = o.x, p[1] = o.y, p[2] = o.z, p[3] = o.w, s0 = f.x, s1 = f.y;
+  }
+};
+
+// Four FP32 blocks fit in shared memory; the hint keeps ptxas from trading
+// registers for spills below that.
+constexpr int ray_scatter_min_blocks(size_t real_size) { return real_size == 4 ? 4 : 1; }
+
 template <class Real, int CH>
-__global__ void __launch_bounds__(256) k_ray_scatter(const AtmoParams* params, BuildDims d, const RowInfo* rowinfo,
-                                                     const RowSample<Real>* rows, const CellGeom<Real>* geom,
-                                                     const Remap4<Real>* remap, const Vec4<Real>* J,
-                                                     Vec4<Real>* dS) {
+__global__ void __launch_bounds__(256, ray_scatter_min_blocks(sizeof(Real)))
+    k_ray_scatter(const AtmoParams* params, BuildDims d, const RowInfo* rowinfo, const RowSample<Real>* rows,
+                  const CellGeom<Real>* geom, const Remap4<Real>* remap, const Vec4<Real>* J, Vec4<Real>* dS) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int b = blockIdx.y;
   const long long row = blockIdx.x;
@@ -419,8 +462,9 @@ __global__ void __launch_bounds__(256) k_ray_scatter(const AtmoParams* params, B
   const RowInfo ri = rowinfo[b * nrows + row];
   const Vec4<Real>* tJ = J + (long long)b * d.n4();
   const long long node0 = (b * nrows + row) * ncell;
-  const Real scale2 = (Real)((d.n2 - 1) / (1 - exp(-3.6)));
-  const Real rr = (Real)ri.r, D0 = (Real)ri.D[0], D1 = (Real)ri.D[1], D2 = (Real)ri.D[2];
+  const Real scale2 = Bulk<Real>::sun_scale(d);
+  const RowR<Real> rw = row_r<Real>(ri);
+  const Real rr = rw.r, D0 = rw.D[0], D1 = rw.D[1], D2 = rw.D[2];
   const int n3x3 = 3 * d.n3;
 
   for (int c0 = 0; c0 < ncell; c0 += blockDim.x) {
@@ -449,6 +493,7 @@ __global__ void __launch_bounds__(256) k_ray_scatter(const AtmoParams* params, B
         v.T[2] = exp_neg(q.tau[2]);
         v.us = q.us;
         v.inv_r = q.inv_r;
+        v.unused = 0;
         v.s0 = q.s0;
         v.s1 = q.s1;
         const int v0 = upper_index(q.u0, d.n0), v1 = upper_index(q.u1, d.n1);
@@ -460,15 +505,15 @@ __global__ void __launch_bounds__(256) k_ray_scatter(const AtmoParams* params, B
       }
       __syncthreads();
       for (int ch = 0; ch < nch; ch++) {
-        const RaySample<Real>& v = smp[ch];
+        const SampleCorners<Real> v(smp[ch]);
         for (int t = threadIdx.x; t < ncell; t += blockDim.x) {
           Real A[3], B[3], lo[3], hi[3];
-          ld3(tJ, (long long)v.p00 + t, A);
-          ld3(tJ, (long long)v.p01 + t, B);
+          ld3(tJ, (long long)v.p[0] + t, A);
+          ld3(tJ, (long long)v.p[1] + t, B);
 #pragma unroll
           for (int c = 0; c < 3; c++) lo[c] = fma(B[c] - A[c], v.s1, A[c]);
-          ld3(tJ, (long long)v.p10 + t, A);
-          ld3(tJ, (long long)v.p11 + t, B);
+          ld3(tJ, (long long)v.p[2] + t, A);
+          ld3(tJ, (long long)v.p[3] + t, B);
 #pragma unroll
           for (int c = 0; c < 3; c++) hi[c] = fma(B[c] - A[c], v.s1, A[c]);
           Real* dst = plane + 3 * (ch * ncell + t);
@@ -478,26 +523,32 @@ __global__ void __launch_bounds__(256) k_ray_scatter(const AtmoParams* params, B
       }
       __syncthreads();
       if (active) {
-#pragma unroll 2
-        for (int ch = 0; ch < nch; ch++) {
-          const Real sin_el = fma(smp[ch].us, Dl, b0) * smp[ch].inv_r;  // p_s.l / |p_s|
+        // samples alternate between two sums for independent FMA chains
+        auto sample = [&](int ch, Real(&a)[3]) {
+          const SampleView<Real> v(smp[ch]);
+          const Real sin_el = fma(v.us, Dl, b0) * v.inv_r;  // p_s.l / |p_s|
           int u2;
           Real s2;
           split_coord_r<Real>(sun_elevation_index_r<Real>(sin_el, scale2), d.n2, &u2, &s2);
           const Real* lo = plane + 3 * ch * ncell + u2 * n3x3;
           const Real* hi = u2 + 1 < d.n2 ? lo + n3x3 : lo;
-          Real* a = acc[ch & 1];
 #pragma unroll
           for (int c = 0; c < 3; c++) {
             const Real x0 = fma(lo[o3v + c] - lo[o3u + c], s3, lo[o3u + c]);
             const Real x1 = fma(hi[o3v + c] - hi[o3u + c], s3, hi[o3u + c]);
-            a[c] = fma(smp[ch].T[c], fma(x1 - x0, s2, x0), a[c]);
+            a[c] = fma(v.T[c], fma(x1 - x0, s2, x0), a[c]);
           }
+        };
+        int ch = 0;
+        for (; ch + 1 < nch; ch += 2) {
+          sample(ch, acc[0]);
+          sample(ch + 1, acc[1]);
         }
+        if (ch < nch) sample(ch, acc[0]);
       }
     }
     if (active) {
-      const Real w = (Real)(ri.L / d.S);
+      const Real w = rw.Ls;
       Vec4<Real> o;
       o.x = w * (acc[0][0] + acc[1][0]);
       o.y = w * (acc[0][1] + acc[1][1]);
@@ -670,10 +721,12 @@ void launch_export(long long n, const Vec4<Real>* tab, float* out, cudaStream_t 
 
 #define SFSIM_INSTANTIATE(Real)                                                                                     \
   template int launch_point_scatter<Real>(const AtmoParams*, const BuildDims&, const RowInfo*,                     \
-                                          const SphereDir<Real>*, const CellGeom<Real>*, const Vec4<Real>*,        \
-                                          const Vec4<Real>*, const Vec4<Real>*, Vec4<Real>*, cudaStream_t);        \
-  template void launch_surface_radiance<Real>(const AtmoParams*, const BuildDims&, const DirLocal*,                \
-                                              const Vec4<Real>*, const Vec4<Real>*, Vec4<Real>*, cudaStream_t);    \
+                                          const SphereDir<Real>*, const int2*, const PointRow<Real>*,              \
+                                          const CellGeom<Real>*, const Vec4<Real>*, const Vec4<Real>*,             \
+                                          const Vec4<Real>*, Vec4<Real>*, cudaStream_t);                           \
+  template void launch_surface_radiance<Real>(const AtmoParams*, const BuildDims&, const SurfRow<Real>*,          \
+                                              const HalfDir<Real>*, const Vec4<Real>*, const Vec4<Real>*,          \
+                                              Vec4<Real>*, cudaStream_t);                                          \
   template int launch_ray_scatter<Real>(const AtmoParams*, const BuildDims&, const RowInfo*, const RowSample<Real>*, \
                                         const CellGeom<Real>*, const Remap4<Real>*, const Vec4<Real>*,             \
                                         Vec4<Real>*, cudaStream_t);                                                \

@@ -171,8 +171,15 @@ __global__ void k_view_rows(const AtmoParams* params, BuildDims d, RowInfo* info
     ri.D[1] = D.y;
     ri.D[2] = D.z;
     ri.L = mag3(D);
+    ri.Ls = ri.L / d.S;
+    ri.f_r = (float)r;
+    ri.f_sv = (float)sv;
+    ri.f_cv = (float)cv;
+    ri.f_D[0] = (float)D.x;
+    ri.f_D[1] = (float)D.y;
+    ri.f_D[2] = (float)D.z;
+    ri.f_Ls = (float)ri.Ls;
     ri.above = above;
-    ri.pad = 0;
     info[b * nrows + row] = ri;
   }
   // sample point as integral-ray forms it (ray.clj:22-24)
@@ -246,6 +253,130 @@ __global__ void k_sphere_setup(const AtmoParams* params, BuildDims d, const DirL
   out[((long long)b * d.n0 + i) * d.P + w] = o;
 }
 
+// The sphere directions of one height row split into those that end in the
+// sky and those that end on the ground, order kept within each part, and
+// each part filled to a multiple of kDirBlock with zero-weight entries, so
+// that point scatter runs both parts in whole blocks of directions without
+// a branch per direction.  One warp per row.
+template <class Real>
+__global__ void k_sphere_partition(BuildDims d, const SphereDir<Real>* sdirs, SphereDir<Real>* pdirs,
+                                   int2* pcount) {
+  const int i = blockIdx.x, b = blockIdx.y, lane = threadIdx.x;
+  const long long row = (long long)b * d.n0 + i;
+  const SphereDir<Real>* src = sdirs + row * d.P;
+  SphereDir<Real>* dst = pdirs + row * dir_row(d.P);
+  int nsky = 0;
+  for (int t0 = 0; t0 < d.P; t0 += 32) {
+    const int t = t0 + lane;
+    nsky += __popc(__ballot_sync(0xffffffffu, t < d.P && !src[t].surface));
+  }
+  const int sky_end = (nsky + kDirBlock - 1) / kDirBlock * kDirBlock;
+  const int nground = d.P - nsky;
+  const int used = sky_end + (nground + kDirBlock - 1) / kDirBlock * kDirBlock;
+  const unsigned below = (1u << lane) - 1u;
+  int s = 0, g = 0;
+  for (int t0 = 0; t0 < d.P; t0 += 32) {
+    const int t = t0 + lane;
+    const bool in = t < d.P;
+    const bool sky = in && !src[t].surface;
+    const unsigned bs = __ballot_sync(0xffffffffu, sky), bg = __ballot_sync(0xffffffffu, in && !sky);
+    if (in) {
+      SphereDir<Real> e = src[t];
+      e.pad = 0;
+      dst[sky ? s + __popc(bs & below) : sky_end + g + __popc(bg & below)] = e;
+    }
+    s += __popc(bs);
+    g += __popc(bg);
+  }
+  SphereDir<Real> z;
+  for (int c = 0; c < 3; c++) z.w[c] = z.gdir[c] = z.ground[c] = 0;
+  z.weight = z.s1 = z.sE0 = 0;
+  z.u1 = z.uE0 = 0;
+  z.pad = 1;
+  for (int t = nsky + lane; t < sky_end; t += 32) {
+    z.surface = 0;
+    dst[t] = z;
+  }
+  for (int t = sky_end + nground + lane; t < used; t += 32) {
+    z.surface = 1;
+    dst[t] = z;
+  }
+  if (lane == 0) pcount[row] = make_int2(sky_end, used);
+}
+
+// Point-scatter constants per (height i, sun elevation k): the coordinates
+// of ray-scatter-forward (atmosphere.clj:203-222) at x = (r_i, 0, 0) with the
+// sun at elevation k, and beta_c(x) (atmosphere.clj:42-47, 140-151), in FP64
+// once here instead of in every thread of the point-scatter blocks.
+template <class Real>
+__global__ void k_point_rows(const AtmoParams* params, BuildDims d, PointRow<Real>* out) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int b = blockIdx.y;
+  if (t >= d.n0 * d.n2) return;
+  const AtmoParams& P = params[b];
+  const int i = t / d.n2, k = t % d.n2;
+  const double r = index_to_radius(P, d.n0, (double)i);
+  const double ss = index_to_sin_sun_elevation(d.n2, (double)k);
+  PointRow<Real> o;
+  split_coord<Real>(height_to_index(P, d.n0, r), d.n0, &o.u0, &o.s0);
+  split_coord<Real>(sun_elevation_to_index(d.n2, mk3(r, 0, 0), mk3(ss, 0, 0)), d.n2, &o.u2, &o.s2);
+  const double h = r - P.R;
+  const double er = exp(-(h / P.ray_scale)), em = exp(-(h / P.mie_scale));
+  for (int c = 0; c < 3; c++) {
+    o.bR[c] = (Real)(P.ray_base[c] * er);
+    o.bM[c] = (Real)(P.mie_base[c] * em);
+  }
+  out[(long long)b * d.n0 * d.n2 + t] = o;
+}
+
+// Surface-radiance constants per node (iE, kE), in FP64 as the per-node part
+// of k_surface_radiance needs them (atmosphere.clj:225-230, 239-253).
+template <class Real>
+__global__ void k_surface_rows(const AtmoParams* params, BuildDims d, SurfRow<Real>* out) {
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  const int b = blockIdx.y;
+  if (t >= d.nE()) return;
+  const AtmoParams& P = params[b];
+  const int iE = (int)(t / d.nE1), kE = (int)(t % d.nE1);
+  const double r = index_to_radius(P, d.nE0, (double)iE);
+  const double ss = index_to_sin_sun_elevation(d.nE1, (double)kE);
+  const d3 x = mk3(r, 0, 0), l = mk3(ss, sqrt(dmax(0.0, 1 - sqr(ss))), 0);
+  SurfRow<Real> o;
+  split_coord<Real>(height_to_index(P, d.n0, mag3(x)), d.n0, &o.u0, &o.s0);
+  split_coord<Real>(sun_elevation_to_index(d.n2, x, l), d.n2, &o.u2, &o.s2);
+  const double c0 = dmul(dsub(r, P.R), dadd(r, P.R));  // |x|^2 - R^2
+  const Real rho = (Real)sqrt(dmax(0.0, c0));
+  o.Hh2mq = (Real)dsub(P.Hh2, c0);
+  o.den = rho + rho + Real(2) * (Real)P.Hh;
+  o.rr = (Real)r;
+  o.lx = (Real)l.x;
+  o.ly = (Real)l.y;
+  out[(long long)b * d.nE() + t] = o;
+}
+
+// The half-sphere directions of surface radiance in world coordinates at
+// the height of row iE (x = (r, 0, 0), the frame of integral-half-sphere).
+template <class Real>
+__global__ void k_half_dirs(const AtmoParams* params, BuildDims d, const DirLocal* hdirs, HalfDir<Real>* out) {
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  const int b = blockIdx.y;
+  if (t >= (long long)d.nE0 * d.Ph) return;
+  const AtmoParams& P = params[b];
+  const int iE = (int)(t / d.Ph), w = (int)(t % d.Ph);
+  const double r = index_to_radius(P, d.nE0, (double)iE);
+  const d3 x = mk3(r, 0, 0);
+  const d3 n = mul3(x, 1.0 / mag3(x));
+  const d3 o1 = orthogonal(n);
+  const d3 o2 = cross3(n, o1);
+  const DirLocal qd = hdirs[w];
+  const d3 omega = to_world(n, o1, o2, qd);
+  HalfDir<Real> o;
+  o.wx = (Real)omega.x;
+  o.wy = (Real)omega.y;
+  o.wgt = (Real)(qd.w * dot3(omega, n));
+  out[(long long)b * d.nE0 * d.Ph + t] = o;
+}
+
 // ---------------------------------------------------------------------------
 // launchers
 // ---------------------------------------------------------------------------
@@ -254,13 +385,17 @@ static inline dim3 grid1(long long n, int block, int B) { return dim3((unsigned)
 
 template <class Real>
 void launch_setup(const AtmoParams* params, const BuildDims& d, const DirLocal* dirs, const int* ring_end,
-                  const SetupBuffers<Real>& o, cudaStream_t st) {
+                  const DirLocal* half_dirs, const SetupBuffers<Real>& o, cudaStream_t st) {
   const int blk = 128;
   k_remap4<Real><<<grid1(d.n4(), blk, d.B), blk, 0, st>>>(params, d, o.remapS, o.geom);
   k_remapT<Real><<<grid1(d.nT(), blk, d.B), blk, 0, st>>>(params, d, o.remapT);
   k_remapE<Real><<<grid1(d.nE(), blk, d.B), blk, 0, st>>>(params, d, o.remapE);
   k_view_rows<Real><<<grid1(d.rows() * d.S, blk, d.B), blk, 0, st>>>(params, d, o.rowinfo, o.rows);
   k_sphere_setup<Real><<<grid1((long long)d.n0 * d.P, blk, d.B), blk, 0, st>>>(params, d, dirs, ring_end, o.sdirs);
+  k_sphere_partition<Real><<<dim3(d.n0, d.B), 32, 0, st>>>(d, o.sdirs, o.pdirs, o.pcount);
+  k_point_rows<Real><<<grid1((long long)d.n0 * d.n2, blk, d.B), blk, 0, st>>>(params, d, o.prow);
+  k_surface_rows<Real><<<grid1(d.nE(), blk, d.B), blk, 0, st>>>(params, d, o.erow);
+  k_half_dirs<Real><<<grid1((long long)d.nE0 * d.Ph, blk, d.B), blk, 0, st>>>(params, d, half_dirs, o.hdir);
 }
 
 template <class Real>
@@ -276,9 +411,9 @@ void launch_surface_base(const AtmoParams* params, const BuildDims& d, Vec4<Real
 }
 
 template void launch_setup<float>(const AtmoParams*, const BuildDims&, const DirLocal*, const int*,
-                                  const SetupBuffers<float>&, cudaStream_t);
+                                  const DirLocal*, const SetupBuffers<float>&, cudaStream_t);
 template void launch_setup<double>(const AtmoParams*, const BuildDims&, const DirLocal*, const int*,
-                                   const SetupBuffers<double>&, cudaStream_t);
+                                   const DirLocal*, const SetupBuffers<double>&, cudaStream_t);
 template void launch_transmittance<float>(const AtmoParams*, const BuildDims&, Vec4<float>*, cudaStream_t);
 template void launch_transmittance<double>(const AtmoParams*, const BuildDims&, Vec4<double>*, cudaStream_t);
 template void launch_surface_base<float>(const AtmoParams*, const BuildDims&, Vec4<float>*, cudaStream_t);

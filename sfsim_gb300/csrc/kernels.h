@@ -17,11 +17,23 @@ struct SetupBuffers {
   RowInfo* rowinfo;
   RowSample<Real>* rows;
   SphereDir<Real>* sdirs;
+  // sdirs partitioned per height row: the directions that end in the sky,
+  // then those that end on the ground, each part filled to a multiple of
+  // kDirBlock with zero-weight entries (pad = 1); kDirRow entries per row,
+  // pcount = {first ground entry, entries used}
+  SphereDir<Real>* pdirs;
+  int2* pcount;
+  PointRow<Real>* prow;  // [B][n0][n2]
+  SurfRow<Real>* erow;   // [B][nE0][nE1]
+  HalfDir<Real>* hdir;   // [B][nE0][Ph]
 };
+
+constexpr int kDirBlock = 8;
+__host__ __device__ constexpr int dir_row(int P) { return P + 2 * kDirBlock; }
 
 template <class Real>
 void launch_setup(const AtmoParams* params, const BuildDims& d, const DirLocal* dirs, const int* ring_end,
-                  const SetupBuffers<Real>& o, cudaStream_t st);
+                  const DirLocal* half_dirs, const SetupBuffers<Real>& o, cudaStream_t st);
 
 template <class Real>
 void launch_transmittance(const AtmoParams* params, const BuildDims& d, Vec4<Real>* T, cudaStream_t st);
@@ -56,13 +68,15 @@ int launch_smem_probe(int blocks, int iters, float* sink, cudaStream_t st);
 // iteration's rayleigh + mie * phase(mie, v.l).
 template <class Real>
 int launch_point_scatter(const AtmoParams* params, const BuildDims& d, const RowInfo* rowinfo,
-                         const SphereDir<Real>* sdirs, const CellGeom<Real>* geom, const Vec4<Real>* dS,
+                         const SphereDir<Real>* pdirs, const int2* pcount, const PointRow<Real>* prow,
+                         const CellGeom<Real>* geom, const Vec4<Real>* dS,
                          const Vec4<Real>* mie, const Vec4<Real>* dE, Vec4<Real>* J, cudaStream_t st);
 
 // dE = surface radiance of dS (same first-iteration convention).
 template <class Real>
-void launch_surface_radiance(const AtmoParams* params, const BuildDims& d, const DirLocal* half_dirs,
-                             const Vec4<Real>* dS, const Vec4<Real>* mie, Vec4<Real>* dE, cudaStream_t st);
+void launch_surface_radiance(const AtmoParams* params, const BuildDims& d, const SurfRow<Real>* erow,
+                             const HalfDir<Real>* hdir, const Vec4<Real>* dS, const Vec4<Real>* mie,
+                             Vec4<Real>* dE, cudaStream_t st);
 
 // dS = ray scatter of J.
 template <class Real>
