@@ -251,6 +251,7 @@ int make_params(const sfsim_atmo_config& c, AtmoParams& P) {
   P.f_Hh2 = (float)P.Hh2;
   P.f_mie_g = (float)P.mie_g;
   P.f_top = (float)P.top;
+  P.f_Hh = (float)P.Hh;
   const double gs[2] = {P.ray_g, P.mie_g};
   for (int m = 0; m < 2; m++) {
     const double g = gs[m];
@@ -340,7 +341,8 @@ struct Work {
   DirLocal* hdirs;
   SetupBuffers<Real> setup;
   Vec4<Real>*T, *E0, *dE[2], *Eacc[2];
-  Vec4<Real>*S1R, *M, *J, *dS[2], *Sacc[2];
+  Vec4<Real>*S1R, *M, *dS[2], *Sacc[2];
+  Real* J;
   float *oT, *oE, *oS, *oM;  // device outputs when the caller passes host buffers
   float2* sun;               // sun-ray optical-depth tables (FP32 builds), or NULL
 };
@@ -358,6 +360,7 @@ size_t carve(Work<Real>& w, char* base, const BuildDims& d, bool outputs, bool s
   w.setup.remapT = c.take<Remap2<Real>>(B * d.nT());
   w.setup.remapE = c.take<Remap2<Real>>(B * d.nE());
   w.setup.rowinfo = c.take<RowInfo>(B * d.rows());
+  w.setup.rowmap = c.take<Remap2<Real>>(B * d.rows());
   w.setup.rows = c.take<RowSample<Real>>(B * d.rows() * d.S);
   w.setup.sdirs = c.take<SphereDir<Real>>(B * d.n0 * (long long)(d.P + 1));
   w.setup.pdirs = c.take<SphereDir<Real>>(B * d.n0 * (long long)dir_row(d.P));
@@ -373,7 +376,7 @@ size_t carve(Work<Real>& w, char* base, const BuildDims& d, bool outputs, bool s
   }
   w.S1R = c.take<Vec4<Real>>(B * d.n4());
   w.M = c.take<Vec4<Real>>(B * d.n4());
-  w.J = c.take<Vec4<Real>>(B * d.n4());
+  w.J = c.take<Real>(3 * B * d.n4());  // planar [atmosphere][channel][node]
   for (int i = 0; i < 2; i++) {
     w.dS[i] = c.take<Vec4<Real>>(B * d.n4());
     w.Sacc[i] = c.take<Vec4<Real>>(B * d.n4());
@@ -450,7 +453,7 @@ int run_build(const Work<Real>& w, const BuildDims& d, float* oT, float* oE, flo
   int launches = 0;
   tm.mark_begin(0);
   launch_setup<Real>(w.params, d, w.dirs, w.ring_end, w.hdirs, w.setup, st);
-  launches += 9;
+  launches += 10;
   tm.mark_end();
   tm.mark_begin(1);
   launch_transmittance<Real>(w.params, d, w.T, st);
@@ -493,7 +496,7 @@ int run_build(const Work<Real>& w, const BuildDims& d, float* oT, float* oE, flo
     launches++;
     tm.mark_end();
     if (jsum) {
-      launch_add_to_sum<Real>(d.B * d.n4(), w.J, jsum, it == 0, st);
+      launch_add_to_sum<Real>(d.n4(), d.B, w.J, jsum, it == 0, st);
       launches++;
     }
     tm.mark_begin(6);
@@ -514,7 +517,7 @@ int run_build(const Work<Real>& w, const BuildDims& d, float* oT, float* oE, flo
     CUDA_TRY(cudaGetLastError());
     if (inter) {
       if (inter->point_scatter)
-        launch_export<Real>(d.B * d.n4(), w.J, inter->point_scatter + (size_t)3 * d.B * d.n4() * it, st);
+        launch_export_planar<Real>(d.n4(), d.B, w.J, inter->point_scatter + (size_t)3 * d.B * d.n4() * it, st);
       if (inter->surface_delta)
         launch_export<Real>(d.B * d.nE(), dE_new, inter->surface_delta + (size_t)3 * d.B * d.nE() * it, st);
       if (inter->ray_scatter_delta)

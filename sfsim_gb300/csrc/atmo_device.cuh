@@ -358,6 +358,37 @@ __device__ __forceinline__ RowR<Real> row_r(const RowInfo& ri) {
   return o;
 }
 
+// Pairs of independent values with one instruction per operation: on
+// sm_100+ FFMA2/FADD2/FMUL2 (each lane rounded as the scalar operation),
+// plain pairs in FP64.
+template <class Real>
+struct Vec2Of;
+template <>
+struct Vec2Of<float> {
+  using T = float2;
+};
+template <>
+struct Vec2Of<double> {
+  using T = double2;
+};
+template <class Real>
+using V2 = typename Vec2Of<Real>::T;
+__device__ __forceinline__ float2 mk2(float a, float b) { return make_float2(a, b); }
+__device__ __forceinline__ double2 mk2(double a, double b) { return make_double2(a, b); }
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ double2 fma2(double2 a, double2 b, double2 c) {
+  return make_double2(fma(a.x, b.x, c.x), fma(a.y, b.y, c.y));
+}
+__device__ __forceinline__ double2 add2(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ double2 mul2(double2 a, double2 b) { return make_double2(a.x * b.x, a.y * b.y); }
+// b - a, exactly rounded (a * -1 is exact, the FMA rounds once)
+template <class V>
+__device__ __forceinline__ V sub2(V b, V a) {
+  return fma2(a, mk2(decltype(a.x)(-1), decltype(a.x)(-1)), b);
+}
+
 // Cornette-Shanks phase k (1 + mu^2) (a + b mu)^-3/2 from the host-computed
 // coefficients {k, a, b} of AtmoParams.
 template <class Real>
@@ -367,6 +398,11 @@ struct PhaseCS {
   __device__ __forceinline__ Real operator()(Real mu) const {
     const Real r = Bulk<Real>::rsqrt(fma(b, mu, a));
     return k * fma(mu, mu, Real(1)) * (r * r * r);
+  }
+  __device__ __forceinline__ V2<Real> pair(V2<Real> mu) const {
+    const V2<Real> t = fma2(mk2(b, b), mu, mk2(a, a));
+    const V2<Real> r = mk2(Bulk<Real>::rsqrt(t.x), Bulk<Real>::rsqrt(t.y));
+    return mul2(mul2(mk2(k, k), fma2(mu, mu, mk2(Real(1), Real(1)))), mul2(mul2(r, r), r));
   }
 };
 
@@ -438,19 +474,55 @@ __device__ __forceinline__ void sun_sums(Real q0, Real b, Real dt, int steps, co
   Real sr[4] = {0, 0, 0, 0}, sm[4] = {0, 0, 0, 0};
   Real f = 0;
   int n = 0;
-  for (; n + 4 <= steps; n += 4) {
+  if constexpr (std::is_same<Real, float>::value) {
+    // samples u = 0, 1 and u = 2, 3 as pairs of FP32 lanes (FFMA2/FMUL2/
+    // FADD2, each lane rounded as the scalar operation): the same values
+    // in half the instructions
+    float2 A2[2], B2[2], pr2[NP], s_r[2], s_m[2];
+    const float2 C2 = make_float2(C, C), al2 = make_float2(alpha, alpha), be2 = make_float2(beta, beta);
+    const float2 ra2 = make_float2(ratio, ratio), four = make_float2(4.0f, 4.0f);
 #pragma unroll
-    for (int u = 0; u < 4; u++) {
-      const Real q = fma(f, fma(f, C, Bu[u]), Au[u]);
-      const Real z = fma(q, alpha, beta);
-      Real p = pr[NP - 1];
+    for (int k = 0; k < NP; k++) pr2[k] = make_float2(pr[k], pr[k]);
 #pragma unroll
-      for (int k = NP - 2; k >= 0; k--) p = fma(p, z, pr[k]);
-      const Real xr = q * p;
-      sr[u] += Bulk<Real>::exp2(xr);
-      sm[u] += Bulk<Real>::exp2(xr * ratio);
+    for (int h = 0; h < 2; h++) {
+      A2[h] = make_float2(Au[2 * h], Au[2 * h + 1]);
+      B2[h] = make_float2(Bu[2 * h], Bu[2 * h + 1]);
+      s_r[h] = make_float2(0.0f, 0.0f);
+      s_m[h] = make_float2(0.0f, 0.0f);
     }
-    f += Real(4);
+    float2 f2 = make_float2(0.0f, 0.0f);
+    for (; n + 4 <= steps; n += 4) {
+#pragma unroll
+      for (int h = 0; h < 2; h++) {
+        const float2 q = __ffma2_rn(f2, __ffma2_rn(f2, C2, B2[h]), A2[h]);
+        const float2 z = __ffma2_rn(q, al2, be2);
+        float2 p = pr2[NP - 1];
+#pragma unroll
+        for (int k = NP - 2; k >= 0; k--) p = __ffma2_rn(p, z, pr2[k]);
+        const float2 xr = __fmul2_rn(q, p);
+        const float2 xm = __fmul2_rn(xr, ra2);
+        s_r[h] = __fadd2_rn(s_r[h], make_float2(Bulk<float>::exp2(xr.x), Bulk<float>::exp2(xr.y)));
+        s_m[h] = __fadd2_rn(s_m[h], make_float2(Bulk<float>::exp2(xm.x), Bulk<float>::exp2(xm.y)));
+      }
+      f2 = __fadd2_rn(f2, four);
+    }
+    sr[0] = s_r[0].x, sr[1] = s_r[0].y, sr[2] = s_r[1].x, sr[3] = s_r[1].y;
+    sm[0] = s_m[0].x, sm[1] = s_m[0].y, sm[2] = s_m[1].x, sm[3] = s_m[1].y;
+  } else {
+    for (; n + 4 <= steps; n += 4) {
+#pragma unroll
+      for (int u = 0; u < 4; u++) {
+        const Real q = fma(f, fma(f, C, Bu[u]), Au[u]);
+        const Real z = fma(q, alpha, beta);
+        Real p = pr[NP - 1];
+#pragma unroll
+        for (int k = NP - 2; k >= 0; k--) p = fma(p, z, pr[k]);
+        const Real xr = q * p;
+        sr[u] += Bulk<Real>::exp2(xr);
+        sm[u] += Bulk<Real>::exp2(xr * ratio);
+      }
+      f += Real(4);
+    }
   }
   for (; n < steps; n++) {
     const Real fn = Real(n);
@@ -558,6 +630,14 @@ __device__ __forceinline__ void ld3(const Vec4<Real>* t, long long i, Real o[3])
   o[2] = v.z;
 }
 
+// Texel i of a planar RGB table with `plane` entries per channel.
+template <class Real>
+__device__ __forceinline__ void ld3_planar(const Real* __restrict__ t, long long plane, long long i, Real o[3]) {
+  o[0] = t[i];
+  o[1] = t[i + plane];
+  o[2] = t[i + 2 * plane];
+}
+
 template <class Real>
 __device__ __forceinline__ void mix3(const Real* a, const Real* b, Real s, Real* o) {
 #pragma unroll
@@ -612,6 +692,16 @@ __device__ __forceinline__ Real sun_elevation_index_r(Real sin_el, Real scale) {
   const Real e = Bulk<Real>::exp2((Real(3) * sin_el + Real(0.6)) * Real(-1.4426950408889634));
   const Real r = (Real(1) - e) * scale;
   return r > Real(0) ? r : Real(0);
+}
+
+// sun_elevation_index_r for two values: the same operations per lane.
+template <class Real>
+__device__ __forceinline__ V2<Real> sun_elevation_index_r2(V2<Real> sin_el, Real scale) {
+  const V2<Real> z = mul2(fma2(mk2(Real(3), Real(3)), sin_el, mk2(Real(0.6), Real(0.6))),
+                          mk2(Real(-1.4426950408889634), Real(-1.4426950408889634)));
+  const V2<Real> e = mk2(Bulk<Real>::exp2(z.x), Bulk<Real>::exp2(z.y));
+  const V2<Real> r = mul2(sub2(mk2(Real(1), Real(1)), e), mk2(scale, scale));
+  return mk2(r.x > Real(0) ? r.x : Real(0), r.y > Real(0) ? r.y : Real(0));
 }
 
 }  // namespace sfsim

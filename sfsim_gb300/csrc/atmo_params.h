@@ -51,7 +51,7 @@ struct AtmoParams {
   // intensity * scatter base, the first-order source factors
   double d_srcR[3], d_srcM[3];
   float f_srcR[3], f_srcM[3];
-  float f_top;
+  float f_top, f_Hh;
   int hpoly_n;                        // number of coefficients
 };
 

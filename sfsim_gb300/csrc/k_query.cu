@@ -428,111 +428,139 @@ __device__ __forceinline__ float elevation_coordinate_f(float q, float pv, float
   return 0.5f + limit_quot_f(a, rho + rho, -0.5f, 0.0f);
 }
 
+// The FP64 part of one query's view ray (atmosphere.clj:192-198), computed
+// by one lane: GB300 runs FP64 at a small fraction of the FP32 rate, so a
+// warp sets up 32 queries side by side before it integrates them one by one.
+struct QueryRay {
+  double x[3], D[3], l[3];  // for the FP64 horizon test near the horizon
+  long long qi;
+  float root_top, root_gnd, c0, two_xD, DD, b0, Dl, mu, L, xv, s3;
+  int u3, above;
+};
+
 template <int WARPS, bool LIST>
 __global__ void __launch_bounds__(WARPS * 32, 2) k_query_direct(const AtmoParams* params, BuildDims d,
                                                                 const Vec4<float>* Jsum, long long n, const double* X,
                                                                 const double* V, const double* Lt, float* out,
                                                                 const long long* indices) {
+  __shared__ QueryRay rays[WARPS][32];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const long long wi = blockIdx.x * (long long)WARPS + warp;
-  if (wi >= n) return;
-  const long long qi = LIST ? indices[wi] : wi;
+  const long long base = (blockIdx.x * (long long)WARPS + warp) * 32;
+  if (base >= n) return;
   const AtmoParams& P = params[0];
-  const d3 x = mk3(X[3 * qi], X[3 * qi + 1], X[3 * qi + 2]);
-  const d3 v = mk3(V[3 * qi], V[3 * qi + 1], V[3 * qi + 2]);
-  const d3 l = mk3(Lt[3 * qi], Lt[3 * qi + 1], Lt[3 * qi + 2]);
   const int S = d.S;
-  // FP64 per query: the view ray (atmosphere.clj:192-198)
-  const int above = is_above_horizon(P, x, v);
-  const d3 e = above ? atmosphere_intersection(P, x, v) : surface_intersection(P, x, v);
-  const d3 D = sub3(e, x);
-  const double L = mag3(D);
-  const double xr = mag3(x);
-  const double c0 = dmul(dsub(xr, P.R), dadd(xr, P.R));
-  const double xv = dot3(x, v);
-  const double dperp2 = dsub(dot3(x, x), sqr(xv));  // squared distance of the line from the centre
-  const float root_top = (float)sqrt(dmax(0.0, dsub(P.top2, dperp2)));
-  const float root_gnd = (float)sqrt(dmax(0.0, dsub(P.R2, dperp2)));
-  const float fc0 = (float)c0, two_xD = (float)(2.0 * dot3(x, D)), DD = (float)dot3(D, D);
-  const float b0 = (float)dot3(x, l), Dl = (float)dot3(D, l), mu = (float)dot3(v, l);
-  const float fL = (float)L, fxv = (float)xv, Hh = (float)P.Hh, Hh2 = (float)P.Hh2;
+  if (base + lane < n) {
+    const long long qi = LIST ? indices[base + lane] : base + lane;
+    const d3 x = mk3(X[3 * qi], X[3 * qi + 1], X[3 * qi + 2]);
+    const d3 v = mk3(V[3 * qi], V[3 * qi + 1], V[3 * qi + 2]);
+    const d3 l = mk3(Lt[3 * qi], Lt[3 * qi + 1], Lt[3 * qi + 2]);
+    const int above = is_above_horizon(P, x, v);
+    const d3 e = above ? atmosphere_intersection(P, x, v) : surface_intersection(P, x, v);
+    const d3 D = sub3(e, x);
+    const double xr = mag3(x);
+    const double xv = dot3(x, v);
+    const double dperp2 = dsub(dot3(x, x), sqr(xv));  // squared distance of the line from the centre
+    QueryRay& R = rays[warp][lane];
+    R.x[0] = x.x, R.x[1] = x.y, R.x[2] = x.z;
+    R.D[0] = D.x, R.D[1] = D.y, R.D[2] = D.z;
+    R.l[0] = l.x, R.l[1] = l.y, R.l[2] = l.z;
+    R.qi = qi;
+    R.root_top = (float)sqrt(dmax(0.0, dsub(P.top2, dperp2)));
+    R.root_gnd = (float)sqrt(dmax(0.0, dsub(P.R2, dperp2)));
+    R.c0 = (float)dmul(dsub(xr, P.R), dadd(xr, P.R));
+    R.two_xD = (float)(2.0 * dot3(x, D));
+    R.DD = (float)dot3(D, D);
+    R.b0 = (float)dot3(x, l);
+    R.Dl = (float)dot3(D, l);
+    R.mu = (float)dot3(v, l);
+    R.L = (float)mag3(D);
+    R.xv = (float)xv;
+    R.above = above;
+    split_coord_r<float>(0.5f * (d.n3 - 1) * (1 + R.mu), d.n3, &R.u3, &R.s3);
+  }
+  __syncwarp();
+  const float Hh = P.f_Hh, Hh2 = P.f_Hh2;
   const float* hp = P.f_hpoly;
   const float* hr = P.f_hpr4;
-  const float scale2 = (float)((d.n2 - 1) / (1 - exp(-3.6)));
-  int u3;
-  float s3;
-  split_coord_r<float>(0.5f * (d.n3 - 1) * (1 + mu), d.n3, &u3, &s3);
-  float accR[3] = {0, 0, 0}, accM[3] = {0, 0, 0}, accJ[3] = {0, 0, 0};
-  for (int s = lane; s < S; s += 32) {
-    const float su = (s + 0.5f) / S;
-    // q and optical depth from x to p_s along the view ray
-    const float q = fmaf(su, fmaf(su, DD, two_xD), fc0);
-    float sr, sm;
-    optical_sums_u<float, 5>(fc0, two_xD * su, DD * su * su, 1.0f / S, S, hp, P.f_alpha, P.f_beta, P.f_kr, P.f_km,
-                             sr, sm);
-    const float segL = fL * su / S;
-    float taux[3];
+  const float scale2 = Bulk<float>::sun_scale(d);
+  const PhaseCS<float> phase_ray(P.f_phR), phase_mie(P.f_phM);
+  const int count = (int)(n - base < 32 ? n - base : 32);
+  for (int k = 0; k < count; k++) {
+    const QueryRay& R = rays[warp][k];
+    const float fc0 = R.c0, two_xD = R.two_xD, DD = R.DD, b0 = R.b0, Dl = R.Dl, fL = R.L, fxv = R.xv;
+    float accR[3] = {0, 0, 0}, accM[3] = {0, 0, 0}, accJ[3] = {0, 0, 0};
+    for (int s = lane; s < S; s += 32) {
+      const float su = (s + 0.5f) / S;
+      // q and optical depth from x to p_s along the view ray
+      const float q = fmaf(su, fmaf(su, DD, two_xD), fc0);
+      float sr, sm;
+      optical_sums_u<float, 5>(fc0, two_xD * su, DD * su * su, 1.0f / S, S, hp, P.f_alpha, P.f_beta, P.f_kr, P.f_km,
+                               sr, sm);
+      const float segL = fL * su / S;
+      float taux[3];
 #pragma unroll
-    for (int c = 0; c < 3; c++) taux[c] = segL * (P.f_ray_ext[c] * sr + P.f_mie_ext[c] * sm);
-    const float h = height_from_q<float, 5>(q, hp, P.f_alpha, P.f_beta);
-    const float er = Bulk<float>::exp2(h * P.f_kr), em = Bulk<float>::exp2(h * P.f_km);
-    // first order: the sun seen from p_s (atmosphere.clj:154-160)
-    const float bp = fmaf(su, Dl, b0);
-    bool lit = (bp >= 0.0f) || (bp * bp <= q);
-    const float m = bp * bp - q;
-    if ((bp < 4.0f) && (fabsf(m) < 1.0e8f || (bp > -4.0f && q < 1.0e8f))) {
-      const d3 p = add3(x, mul3(D, (0.5 + s) * (1.0 / S)));
-      lit = is_above_horizon(P, p, l);
-    }
-    if (lit) {
-      const float ctop = q - Hh2;
-      const float root = Bulk<float>::sqrt(fmaxf(bp * bp - ctop, 0.0f));
-      float texit = bp >= 0.0f ? Bulk<float>::div(-ctop, bp + root) : root - bp;
-      texit = fmaxf(texit, 0.0f);
-      const float dt = texit / S;
-      float tr, tm;
-      sun_sums<float, 4>(q, bp, dt, S, hr, P.f_alpha, P.f_beta, P.f_hratio, tr, tm);
+      for (int c = 0; c < 3; c++) taux[c] = segL * (P.f_ray_ext[c] * sr + P.f_mie_ext[c] * sm);
+      const float h = height_from_q<float, 5>(q, hp, P.f_alpha, P.f_beta);
+      const float er = Bulk<float>::exp2(h * P.f_kr), em = Bulk<float>::exp2(h * P.f_km);
+      // first order: the sun seen from p_s (atmosphere.clj:154-160)
+      const float bp = fmaf(su, Dl, b0);
+      bool lit = (bp >= 0.0f) || (bp * bp <= q);
+      const float m = bp * bp - q;
+      if ((bp < 4.0f) && (fabsf(m) < 1.0e8f || (bp > -4.0f && q < 1.0e8f))) {
+        const double t = (0.5 + s) * (1.0 / S);
+        const d3 p = add3(mk3(R.x[0], R.x[1], R.x[2]), mul3(mk3(R.D[0], R.D[1], R.D[2]), t));
+        lit = is_above_horizon(P, p, mk3(R.l[0], R.l[1], R.l[2]));
+      }
+      if (lit) {
+        const float ctop = q - Hh2;
+        const float root = Bulk<float>::sqrt(fmaxf(bp * bp - ctop, 0.0f));
+        float texit = bp >= 0.0f ? Bulk<float>::div(-ctop, bp + root) : root - bp;
+        texit = fmaxf(texit, 0.0f);
+        const float dt = texit / S;
+        float tr, tm;
+        sun_sums<float, 4>(q, bp, dt, S, hr, P.f_alpha, P.f_beta, P.f_hratio, tr, tm);
 #pragma unroll
-      for (int c = 0; c < 3; c++) {
-        const float T = exp_neg(taux[c] + dt * (P.f_ray_ext[c] * tr + P.f_mie_ext[c] * tm));
-        accR[c] = fmaf(T, er, accR[c]);
-        accM[c] = fmaf(T, em, accM[c]);
+        for (int c = 0; c < 3; c++) {
+          const float T = exp_neg(taux[c] + dt * (P.f_ray_ext[c] * tr + P.f_mie_ext[c] * tm));
+          accR[c] = fmaf(T, er, accR[c]);
+          accM[c] = fmaf(T, em, accM[c]);
+        }
+      }
+      // higher orders: J summed over the orders at forward(p_s, v, l, above)
+      if (Jsum) {
+        const float pr = sqrtf(P.f_R * P.f_R + q);
+        const float pv = fxv + su * fL;
+        int u[4];
+        float w[4];
+        split_coord_r<float>((d.n0 - 1) * (sqrtf(fmaxf(q, 0.0f)) / Hh), d.n0, &u[0], &w[0]);
+        split_coord_r<float>((d.n1 - 1) * elevation_coordinate_f(q, pv, R.root_top, R.root_gnd, Hh, R.above), d.n1,
+                             &u[1], &w[1]);
+        split_coord_r<float>(sun_elevation_index_r<float>(bp / pr, scale2), d.n2, &u[2], &w[2]);
+        u[3] = R.u3;
+        w[3] = R.s3;
+        float jv[3];
+        interp4<float>(Jsum, d, u, w, jv);
+#pragma unroll
+        for (int c = 0; c < 3; c++) accJ[c] = fmaf(exp_neg(taux[c]), jv[c], accJ[c]);
       }
     }
-    // higher orders: J summed over the orders at forward(p_s, v, l, above)
-    if (Jsum) {
-      const float pr = sqrtf(P.f_R * P.f_R + q);
-      const float pv = fxv + su * fL;
-      int u[4];
-      float w[4];
-      split_coord_r<float>((d.n0 - 1) * (sqrtf(fmaxf(q, 0.0f)) / Hh), d.n0, &u[0], &w[0]);
-      split_coord_r<float>((d.n1 - 1) * elevation_coordinate_f(q, pv, root_top, root_gnd, Hh, above), d.n1, &u[1],
-                           &w[1]);
-      split_coord_r<float>(sun_elevation_index_r<float>(bp / pr, scale2), d.n2, &u[2], &w[2]);
-      u[3] = u3;
-      w[3] = s3;
-      float jv[3];
-      interp4<float>(Jsum, d, u, w, jv);
-#pragma unroll
-      for (int c = 0; c < 3; c++) accJ[c] = fmaf(exp_neg(taux[c]), jv[c], accJ[c]);
-    }
-  }
-#pragma unroll
-  for (int c = 0; c < 3; c++) {
-    for (int o = 16; o > 0; o >>= 1) {
-      accR[c] += __shfl_xor_sync(0xffffffffu, accR[c], o);
-      accM[c] += __shfl_xor_sync(0xffffffffu, accM[c], o);
-      accJ[c] += __shfl_xor_sync(0xffffffffu, accJ[c], o);
-    }
-  }
-  if (lane == 0) {
-    const float w = fL / S;
-    const float phR = phase_cs<float>((float)P.ray_g, mu), phM = phase_cs<float>((float)P.mie_g, mu);
 #pragma unroll
     for (int c = 0; c < 3; c++) {
-      const float s1 = w * phR * (float)(P.intensity[c] * P.ray_base[c]) * accR[c];
-      const float m1 = w * (float)(P.intensity[c] * P.mie_base[c]) * accM[c];
-      out[3 * qi + c] = s1 + m1 * phM + w * accJ[c];
+      for (int o = 16; o > 0; o >>= 1) {
+        accR[c] += __shfl_xor_sync(0xffffffffu, accR[c], o);
+        accM[c] += __shfl_xor_sync(0xffffffffu, accM[c], o);
+        accJ[c] += __shfl_xor_sync(0xffffffffu, accJ[c], o);
+      }
+    }
+    if (lane == 0) {
+      const float w = fL / S;
+      const float phR = phase_ray(R.mu), phM = phase_mie(R.mu);
+#pragma unroll
+      for (int c = 0; c < 3; c++) {
+        const float s1 = w * phR * P.f_srcR[c] * accR[c];
+        const float m1 = w * P.f_srcM[c] * accM[c];
+        out[3 * R.qi + c] = s1 + m1 * phM + w * accJ[c];
+      }
     }
   }
 }
@@ -542,7 +570,7 @@ void launch_query_direct(const AtmoParams* params, const BuildDims& d, const Vec
                          const long long* indices) {
   if (n <= 0) return;
   constexpr int WARPS = 8;
-  const unsigned blocks = (unsigned)((n + WARPS - 1) / WARPS);
+  const unsigned blocks = (unsigned)((n + WARPS * 32 - 1) / (WARPS * 32));
   if (indices)
     k_query_direct<WARPS, true><<<blocks, WARPS * 32, 0, st>>>(params, d, Jsum, n, x, v, l, out, indices);
   else

@@ -64,29 +64,36 @@ struct TexelRow {
   }
 };
 
-// Direction vector and quadrature weight of a SphereDir in shared memory:
-// one 16-byte broadcast load for FP32 entries.
+// Shared-memory layout of point scatter for one (height i, sun elevation k)
+// pair, `used` directions (a multiple of kDirBlock):
+//   dirs  [kDirFields][used] Real: x0, x1, x2, weight, gdir0..2, ground0..2,
+//         sE0 of each direction (structure of arrays, so that two consecutive
+//         directions' components load as one pair);
+//   uE0   [used] int;
+//   rows  [used][n3 + 1][3] dS gathered along the heading axis, texel n3 a
+//         copy of texel n3 - 1 (and the Mie rows in the first iteration);
+//   etab  [nE0][nE1][3] the dE table.
+constexpr int kDirFields = 11;
+
 template <class Real>
-__device__ __forceinline__ void load_dir(const SphereDir<Real>& D, Real& x0, Real& x1, Real& x2, Real& weight) {
-  x0 = D.w[0], x1 = D.w[1], x2 = D.w[2], weight = D.weight;
-}
-template <>
-__device__ __forceinline__ void load_dir<float>(const SphereDir<float>& D, float& x0, float& x1, float& x2,
-                                                float& weight) {
-  static_assert(offsetof(SphereDir<float>, weight) == 12 && sizeof(SphereDir<float>) % 16 == 0, "layout");
-  const float4 v = *reinterpret_cast<const float4*>(&D);
-  x0 = v.x, x1 = v.y, x2 = v.z, weight = v.w;
+__device__ __forceinline__ V2<Real> ld2(const Real* p) {
+  return *reinterpret_cast<const V2<Real>*>(p);
 }
 
+// Three FP32 blocks of 256 share an SM (80 registers a thread); FP64 blocks
+// are register-bound anyway.
+constexpr int point_scatter_min_blocks(size_t real_size) { return real_size == 4 ? 3 : 1; }
+
 template <class Real, bool FIRST>
-__global__ void __launch_bounds__(256, 3) k_point_scatter(const AtmoParams* params, BuildDims d,
+__global__ void __launch_bounds__(256, point_scatter_min_blocks(sizeof(Real))) k_point_scatter(const AtmoParams* params, BuildDims d,
                                                           const RowInfo* rowinfo, const SphereDir<Real>* pdirs,
                                                           const int2* pcount, const PointRow<Real>* prow,
                                                           const CellGeom<Real>* geom,
                                                           const Vec4<Real>* dS, const Vec4<Real>* Mt,
-                                                          const Vec4<Real>* dE, Vec4<Real>* J, int nchunks) {
+                                                          const Vec4<Real>* dE, Real* J, int nchunks) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   using TR = TexelRow<Real>;
+  using R2 = V2<Real>;
   constexpr int RS = TR::kStride;
   constexpr int DB = kDirBlock;
   const int b = blockIdx.y;
@@ -98,10 +105,12 @@ __global__ void __launch_bounds__(256, 3) k_point_scatter(const AtmoParams* para
   const int2 pc = pcount[(long long)b * d.n0 + i];
   const int sky_end = pc.x, used = pc.y;
   const int nrow = used * d.n3;
-  SphereDir<Real>* dirs = reinterpret_cast<SphereDir<Real>*>(smem_raw);
-  Real* rows = reinterpret_cast<Real*>(dirs + dir_row(d.P));
-  Real* rowsM = rows + RS * nrow;
-  Real* etab = rowsM + (FIRST ? RS * nrow : 0);
+  const int rlen = d.n3 + 1;  // texels of a heading row, the last one a copy of texel n3 - 1
+  Real* dirs = reinterpret_cast<Real*>(smem_raw);
+  int* uE0s = reinterpret_cast<int*>(dirs + kDirFields * used);
+  Real* rows = reinterpret_cast<Real*>(smem_raw + (((size_t)used * (kDirFields * sizeof(Real) + sizeof(int)) + 15) & ~size_t(15)));
+  Real* rowsM = rows + RS * used * rlen;
+  Real* etab = rowsM + (FIRST ? RS * used * rlen : 0);
 
   // the (i, k) coordinates of the dS lookups
   const int u0 = prk->u0, u2 = prk->u2;
@@ -110,7 +119,14 @@ __global__ void __launch_bounds__(256, 3) k_point_scatter(const AtmoParams* para
 
   const long long base4 = (long long)b * d.n4();
   const SphereDir<Real>* src = pdirs + ((long long)b * d.n0 + i) * dir_row(d.P);
-  for (int t = threadIdx.x; t < used; t += blockDim.x) dirs[t] = src[t];
+  for (int t = threadIdx.x; t < used; t += blockDim.x) {
+    const SphereDir<Real> D = src[t];
+    const Real f[kDirFields] = {D.w[0],      D.w[1],      D.w[2],      D.weight,    D.gdir[0], D.gdir[1],
+                                D.gdir[2],   D.ground[0], D.ground[1], D.ground[2], D.sE0};
+#pragma unroll
+    for (int c = 0; c < kDirFields; c++) dirs[c * used + t] = f[c];
+    uE0s[t] = D.uE0;
+  }
   for (int t = threadIdx.x; t < nrow; t += blockDim.x) {
     const int w = t / d.n3, a = t - w * d.n3;
     Real v[3] = {0, 0, 0}, vm[3] = {0, 0, 0};
@@ -120,8 +136,13 @@ __global__ void __launch_bounds__(256, 3) k_point_scatter(const AtmoParams* para
       gather_heading_row(dS + base4, d, u0, v0, s0, u1, v1, s1, u2, v2, s2, a, v);
       if (FIRST) gather_heading_row(Mt + base4, d, u0, v0, s0, u1, v1, s1, u2, v2, s2, a, vm);
     }
-    TR::store(rows, t, v);
-    if (FIRST) TR::store(rowsM, t, vm);
+    const int o = w * rlen + a;
+    TR::store(rows, o, v);
+    if (FIRST) TR::store(rowsM, o, vm);
+    if (a == d.n3 - 1) {
+      TR::store(rows, o + 1, v);
+      if (FIRST) TR::store(rowsM, o + 1, vm);
+    }
   }
   const long long nE = d.nE();
   for (int t = threadIdx.x; t < nE; t += blockDim.x) {
@@ -153,74 +174,96 @@ __global__ void __launch_bounds__(256, 3) k_point_scatter(const AtmoParams* para
   const int lane = threadIdx.x & 31;
   const int gbase = share ? (lane & ~(G - 1)) : lane;
   const int gpos = lane - gbase;
-  const int row_len = RS * d.n3;
+  const int row_len = RS * rlen;
+  const R2 lx2 = mk2(g.lx, g.lx), ly2 = mk2(g.ly, g.ly), lz2 = mk2(g.lz, g.lz);
+  const R2 sv2 = mk2(sv, sv), cv2 = mk2(cv, cv), sc3 = mk2(scale3, scale3);
 
-  Real accR[3] = {0, 0, 0}, accM[3] = {0, 0, 0}, cR[3] = {0, 0, 0}, cM[3] = {0, 0, 0};
-  Real ringR[3] = {0, 0, 0}, ringM[3] = {0, 0, 0};
-  // One block of DB directions starting at w0 (all sky or all ground),
-  // summed plainly into ringR/ringM.
+  // compensated totals (x: Rayleigh, y: Mie) per channel, and the plain
+  // partial sums of the current directions (x: even, y: odd direction)
+  R2 acc[3], cmp[3], ringR[3], ringM[3];
+#pragma unroll
+  for (int c = 0; c < 3; c++) acc[c] = cmp[c] = ringR[c] = ringM[c] = mk2(Real(0), Real(0));
+  // One block of DB directions starting at w0 (all sky or all ground), two
+  // directions per step.
   auto dir_block = [&](int w0, auto ground) {
     Real wRb = 0, wMb = 0;
     if (share && gpos < DB) {
-      Real x0, x1, x2, wt;
-      load_dir(dirs[w0 + gpos], x0, x1, x2, wt);
-      const Real mu_v = fma(sv, x0, cv * x1);
-      wRb = wt * phR(mu_v);
-      wMb = wt * phM(mu_v);
+      const int wb = w0 + gpos;
+      const Real mu_v = fma(sv, dirs[wb], cv * dirs[used + wb]);
+      wRb = dirs[3 * used + wb] * phR(mu_v);
+      wMb = dirs[3 * used + wb] * phM(mu_v);
     }
 #pragma unroll
-    for (int q = 0; q < DB; q++) {
-      const SphereDir<Real>& D = dirs[w0 + q];
-      Real x0, x1, x2, wt;
-      load_dir(D, x0, x1, x2, wt);
-      Real wR, wM;
+    for (int q = 0; q < DB; q += 2) {
+      const int wa = w0 + q;
+      const R2 X0 = ld2(dirs + wa), X1 = ld2(dirs + used + wa), X2 = ld2(dirs + 2 * used + wa);
+      R2 wR, wM;
       if (share) {
-        wR = __shfl_sync(0xffffffffu, wRb, gbase + q);
-        wM = __shfl_sync(0xffffffffu, wMb, gbase + q);
+        wR = mk2(__shfl_sync(0xffffffffu, wRb, gbase + q), __shfl_sync(0xffffffffu, wRb, gbase + q + 1));
+        wM = mk2(__shfl_sync(0xffffffffu, wMb, gbase + q), __shfl_sync(0xffffffffu, wMb, gbase + q + 1));
       } else {
-        const Real mu_v = fma(sv, x0, cv * x1);
-        wR = wt * phR(mu_v);
-        wM = wt * phM(mu_v);
+        const R2 wt = ld2(dirs + 3 * used + wa);
+        const R2 mu_v = fma2(sv2, X0, mul2(cv2, X1));
+        wR = mul2(wt, phR.pair(mu_v));
+        wM = mul2(wt, phM.pair(mu_v));
       }
-      const Real mu_l = fma(x0, g.lx, fma(x1, g.ly, x2 * g.lz));
-      // sun-angle coordinate of (omega, l) along the direction's heading row
-      int u3;
-      Real s3;
-      split_coord_r<Real>(fma(scale3, mu_l, scale3), d.n3, &u3, &s3);
-      const int v3 = upper_index(u3, d.n3);
-      Real X[3], lo[3], hi[3];
-      const Real* row_w = rows + (w0 + q) * row_len;
-      TR::load(row_w, u3, lo);
-      TR::load(row_w, v3, hi);
+      const R2 mu_l = fma2(X0, lx2, fma2(X1, ly2, mul2(X2, lz2)));
+      // sun-angle coordinates of (omega, l) along the two directions' heading rows
+      const R2 c3 = fma2(sc3, mu_l, sc3);
+      int ua, ub;
+      Real sa, sb;
+      split_coord_r<Real>(c3.x, d.n3, &ua, &sa);
+      split_coord_r<Real>(c3.y, d.n3, &ub, &sb);
+      const R2 s3 = mk2(sa, sb);
+      // texels u and u + 1 (the row's copy of its last texel when u = n3 - 1, where s = 0)
+      const Real* ra = rows + wa * row_len + 3 * ua;
+      const Real* rb = rows + (wa + 1) * row_len + 3 * ub;
+      R2 X[3];
 #pragma unroll
-      for (int c = 0; c < 3; c++) X[c] = fma(hi[c] - lo[c], s3, lo[c]);
+      for (int c = 0; c < 3; c++) {
+        const R2 lo = mk2(ra[c], rb[c]), hi = mk2(ra[3 + c], rb[3 + c]);
+        X[c] = fma2(sub2(hi, lo), s3, lo);
+      }
       if (FIRST) {
-        const Real ph = phM(mu_l);
-        const Real* rowM_w = rowsM + (w0 + q) * row_len;
-        TR::load(rowM_w, u3, lo);
-        TR::load(rowM_w, v3, hi);
+        const R2 ph = phM.pair(mu_l);
+        const Real* ma = rowsM + wa * row_len + 3 * ua;
+        const Real* mb = rowsM + (wa + 1) * row_len + 3 * ub;
 #pragma unroll
-        for (int c = 0; c < 3; c++) X[c] = fma(fma(hi[c] - lo[c], s3, lo[c]), ph, X[c]);
+        for (int c = 0; c < 3; c++) {
+          const R2 lo = mk2(ma[c], mb[c]), hi = mk2(ma[3 + c], mb[3 + c]);
+          X[c] = fma2(fma2(sub2(hi, lo), s3, lo), ph, X[c]);
+        }
       }
       if (decltype(ground)::value) {
-        const Real sg = fma(D.gdir[0], g.lx, fma(D.gdir[1], g.ly, D.gdir[2] * g.lz));
-        int uE1;
-        Real sE1;
-        split_coord_r<Real>(sun_elevation_index_r<Real>(sg, scaleE), d.nE1, &uE1, &sE1);
-        const int vE1 = upper_index(uE1, d.nE1), vE0 = upper_index(D.uE0, d.nE0);
-        Real e00[3], e01[3], e10[3], e11[3], Y[3];
-        TR::load(etab, D.uE0 * d.nE1 + uE1, e00);
-        TR::load(etab, D.uE0 * d.nE1 + vE1, e01);
-        TR::load(etab, vE0 * d.nE1 + uE1, e10);
-        TR::load(etab, vE0 * d.nE1 + vE1, e11);
-        mix4(e00, e01, e10, e11, D.sE0, sE1, Y);
+        const R2 G0 = ld2(dirs + 4 * used + wa), G1 = ld2(dirs + 5 * used + wa), G2 = ld2(dirs + 6 * used + wa);
+        const R2 sg = fma2(G0, lx2, fma2(G1, ly2, mul2(G2, lz2)));
+        int ea, eb;
+        Real ta, tb;
+        split_coord_r<Real>(sun_elevation_index_r<Real>(sg.x, scaleE), d.nE1, &ea, &ta);
+        split_coord_r<Real>(sun_elevation_index_r<Real>(sg.y, scaleE), d.nE1, &eb, &tb);
+        const int fa = upper_index(ea, d.nE1), fb = upper_index(eb, d.nE1);
+        const int ha = uE0s[wa], hb = uE0s[wa + 1];
+        const int ka = upper_index(ha, d.nE0), kb = upper_index(hb, d.nE0);
+        const R2 sE1 = mk2(ta, tb), sE0 = ld2(dirs + 10 * used + wa);
+        const R2 one = mk2(Real(1), Real(1));
+        const R2 oi = sub2(one, sE1), oo = sub2(one, sE0);
+        const Real* e0a = etab + 3 * ha * d.nE1;
+        const Real* e1a = etab + 3 * ka * d.nE1;
+        const Real* e0b = etab + 3 * hb * d.nE1;
+        const Real* e1b = etab + 3 * kb * d.nE1;
 #pragma unroll
-        for (int c = 0; c < 3; c++) X[c] = fma(D.ground[c], Y[c], X[c]);
+        for (int c = 0; c < 3; c++) {
+          // mix4: height rows (uE0, vE0), sun-elevation columns (uE1, vE1)
+          const R2 lo = fma2(mk2(e0a[3 * fa + c], e0b[3 * fb + c]), sE1, mul2(mk2(e0a[3 * ea + c], e0b[3 * eb + c]), oi));
+          const R2 hi = fma2(mk2(e1a[3 * fa + c], e1b[3 * fb + c]), sE1, mul2(mk2(e1a[3 * ea + c], e1b[3 * eb + c]), oi));
+          const R2 Y = fma2(hi, sE0, mul2(lo, oo));
+          X[c] = fma2(ld2(dirs + (7 + c) * used + wa), Y, X[c]);
+        }
       }
 #pragma unroll
       for (int c = 0; c < 3; c++) {
-        ringR[c] = fma(wR, X[c], ringR[c]);
-        ringM[c] = fma(wM, X[c], ringM[c]);
+        ringR[c] = fma2(wR, X[c], ringR[c]);
+        ringM[c] = fma2(wM, X[c], ringM[c]);
       }
     }
   };
@@ -228,9 +271,12 @@ __global__ void __launch_bounds__(256, 3) k_point_scatter(const AtmoParams* para
   auto flush = [&]() {
 #pragma unroll
     for (int c = 0; c < 3; c++) {
-      kahan_add(accR[c], cR[c], ringR[c]);
-      kahan_add(accM[c], cM[c], ringM[c]);
-      ringR[c] = ringM[c] = 0;
+      const R2 x = mk2(ringR[c].x + ringR[c].y, ringM[c].x + ringM[c].y);
+      const R2 y = sub2(x, cmp[c]);
+      const R2 t = add2(acc[c], y);
+      cmp[c] = sub2(sub2(t, acc[c]), y);
+      acc[c] = t;
+      ringR[c] = ringM[c] = mk2(Real(0), Real(0));
     }
   };
   for (int w0 = 0; w0 < sky_end; w0 += DB) {
@@ -247,24 +293,28 @@ __global__ void __launch_bounds__(256, 3) k_point_scatter(const AtmoParams* para
   // beta_c(x) (atmosphere.clj:42-47, 140-151)
   const PointRow<Real> pr = *prk;
   Vec4<Real> o;
-  o.x = pr.bR[0] * accR[0] + pr.bM[0] * accM[0];
-  o.y = pr.bR[1] * accR[1] + pr.bM[1] * accM[1];
-  o.z = pr.bR[2] * accR[2] + pr.bM[2] * accM[2];
-  o.w = 0;
-  J[node] = o;
+  o.x = pr.bR[0] * acc[0].x + pr.bM[0] * acc[0].y;
+  o.y = pr.bR[1] * acc[1].x + pr.bM[1] * acc[1].y;
+  o.z = pr.bR[2] * acc[2].x + pr.bM[2] * acc[2].y;
+  // J planar, [atmosphere][channel][node], for the ray-scatter gathers
+  Real* Jb = J + (long long)b * 3 * d.n4() + (node - base4);
+  Jb[0] = o.x;
+  Jb[d.n4()] = o.y;
+  Jb[2 * d.n4()] = o.z;
 }
 
 template <class Real>
 size_t point_scatter_smem(const BuildDims& d, bool first) {
-  return sizeof(SphereDir<Real>) * dir_row(d.P) +
-         sizeof(Real) * 3 * ((size_t)dir_row(d.P) * d.n3 * (first ? 2 : 1) + d.nE());
+  const size_t n = dir_row(d.P);
+  return ((n * (kDirFields * sizeof(Real) + sizeof(int)) + 15) & ~size_t(15)) +
+         sizeof(Real) * 3 * (n * (d.n3 + 1) * (first ? 2 : 1) + d.nE());
 }
 
 template <class Real>
 int launch_point_scatter(const AtmoParams* params, const BuildDims& d, const RowInfo* rowinfo,
                          const SphereDir<Real>* pdirs, const int2* pcount, const PointRow<Real>* prow,
                          const CellGeom<Real>* geom, const Vec4<Real>* dS, const Vec4<Real>* mie,
-                         const Vec4<Real>* dE, Vec4<Real>* J, cudaStream_t st) {
+                         const Vec4<Real>* dE, Real* J, cudaStream_t st) {
   const int block = 256;
   const int nchunks = (d.n1 * d.n3 + block - 1) / block;
   const bool first = mie != nullptr;
@@ -396,51 +446,15 @@ void launch_surface_radiance(const AtmoParams* params, const BuildDims& d, const
 // T(x, p_s) comes from k_view_rows.
 // ---------------------------------------------------------------------------
 
-// Per-sample constants, laid out so that FP32 blocks read each group with
-// one 16-byte broadcast load: {T, us} and {inv_r, -, s0, s1} for the
-// nodes, {s0, s1} and the J offsets for the plane build.
-template <class Real>
-struct RaySample {
-  Real T[3], us;
-  Real inv_r, unused, s0, s1;
-  int p00, p01, p10, p11;  // J offsets of the four (height, elevation) planes
-};
-
-template <class Real>
-struct SampleView {
-  Real T[3], us, inv_r;
-  __device__ __forceinline__ SampleView(const RaySample<Real>& v) {
-    T[0] = v.T[0], T[1] = v.T[1], T[2] = v.T[2], us = v.us, inv_r = v.inv_r;
-  }
-};
-template <>
-struct SampleView<float> {
-  float T[3], us, inv_r;
-  __device__ __forceinline__ SampleView(const RaySample<float>& v) {
-    const float4 a = *reinterpret_cast<const float4*>(&v);
-    T[0] = a.x, T[1] = a.y, T[2] = a.z, us = a.w;
-    inv_r = v.inv_r;
-  }
-};
-
-template <class Real>
-struct SampleCorners {
-  int p[4];
-  Real s0, s1;
-  __device__ __forceinline__ SampleCorners(const RaySample<Real>& v) {
-    p[0] = v.p00, p[1] = v.p01, p[2] = v.p10, p[3] = v.p11, s0 = v.s0, s1 = v.s1;
-  }
-};
-template <>
-struct SampleCorners<float> {
-  int p[4];
-  float s0, s1;
-  __device__ __forceinline__ SampleCorners(const RaySample<float>& v) {
-    static_assert(sizeof(RaySample<float>) == 48 && offsetof(RaySample<float>, p00) == 32, "layout");
-    const int4 o = *reinterpret_cast<const int4*>(&v.p00);
-    const float2 f = *reinterpret_cast<const float2*>(&v.s0);
-    p[0] = o.x, p[1] = o.y, p[2] = o.z, p[3] = o.w, s0 = f.x, s1 = f.y;
-  }
+// Per-sample constants of one chunk of CH ray samples, as arrays so that two
+// consecutive samples' values load as one pair: T(x, p_s), (s + 1/2)/S and
+// 1/|p_s| for the nodes, the (height, elevation) fractions and the J offsets
+// of the four corner planes for the plane build.
+template <class Real, int CH>
+struct RayChunk {
+  Real T[3][CH];
+  Real us[CH], inv_r[CH], s0[CH], s1[CH];
+  int p[4][CH];
 };
 
 // Four FP32 blocks fit in shared memory; the hint keeps ptxas from trading
@@ -450,17 +464,20 @@ constexpr int ray_scatter_min_blocks(size_t real_size) { return real_size == 4 ?
 template <class Real, int CH>
 __global__ void __launch_bounds__(256, ray_scatter_min_blocks(sizeof(Real)))
     k_ray_scatter(const AtmoParams* params, BuildDims d, const RowInfo* rowinfo, const RowSample<Real>* rows,
-                  const CellGeom<Real>* geom, const Remap4<Real>* remap, const Vec4<Real>* J, Vec4<Real>* dS) {
+                  const CellGeom<Real>* geom, const Remap4<Real>* remap, const Real* J, Vec4<Real>* dS) {
+  static_assert(CH % 2 == 0, "samples go in pairs");
+  using R2 = V2<Real>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int b = blockIdx.y;
   const long long row = blockIdx.x;
   const long long nrows = d.rows();
   const int ncell = d.n2 * d.n3;
-  RaySample<Real>* smp = reinterpret_cast<RaySample<Real>*>(smem_raw);
-  Real* plane = reinterpret_cast<Real*>(smp + CH);
+  RayChunk<Real, CH>& sc = *reinterpret_cast<RayChunk<Real, CH>*>(smem_raw);
+  Real* plane = reinterpret_cast<Real*>(smem_raw + ((sizeof(RayChunk<Real, CH>) + 15) & ~size_t(15)));
   const RowSample<Real>* rs = rows + (b * nrows + row) * d.S;
   const RowInfo ri = rowinfo[b * nrows + row];
-  const Vec4<Real>* tJ = J + (long long)b * d.n4();
+  const long long n4 = d.n4();
+  const Real* tJ = J + (long long)b * 3 * n4;  // planar [channel][node]
   const long long node0 = (b * nrows + row) * ncell;
   const Real scale2 = Bulk<Real>::sun_scale(d);
   const RowR<Real> rw = row_r<Real>(ri);
@@ -481,52 +498,77 @@ __global__ void __launch_bounds__(256, ray_scatter_min_blocks(sizeof(Real)))
       o3v = 3 * upper_index(m.u[3], d.n3);
       s3 = m.s[3];
     }
-    Real acc[2][3] = {{0, 0, 0}, {0, 0, 0}};
+    const R2 b02 = mk2(b0, b0), Dl2 = mk2(Dl, Dl), s32 = mk2(s3, s3);
+    // x: even samples, y: odd samples (independent FMA chains)
+    R2 acc[3] = {mk2(Real(0), Real(0)), mk2(Real(0), Real(0)), mk2(Real(0), Real(0))};
     for (int sb = 0; sb < d.S; sb += CH) {
       const int nch = min(CH, d.S - sb);
       __syncthreads();
       if (threadIdx.x < nch) {
-        const RowSample<Real> q = rs[sb + threadIdx.x];
-        RaySample<Real> v;
-        v.T[0] = exp_neg(q.tau[0]);
-        v.T[1] = exp_neg(q.tau[1]);
-        v.T[2] = exp_neg(q.tau[2]);
-        v.us = q.us;
-        v.inv_r = q.inv_r;
-        v.unused = 0;
-        v.s0 = q.s0;
-        v.s1 = q.s1;
+        const int u = threadIdx.x;
+        const RowSample<Real> q = rs[sb + u];
+        sc.T[0][u] = exp_neg(q.tau[0]);
+        sc.T[1][u] = exp_neg(q.tau[1]);
+        sc.T[2][u] = exp_neg(q.tau[2]);
+        sc.us[u] = q.us;
+        sc.inv_r[u] = q.inv_r;
+        sc.s0[u] = q.s0;
+        sc.s1[u] = q.s1;
         const int v0 = upper_index(q.u0, d.n0), v1 = upper_index(q.u1, d.n1);
-        v.p00 = (q.u0 * d.n1 + q.u1) * ncell;
-        v.p01 = (q.u0 * d.n1 + v1) * ncell;
-        v.p10 = (v0 * d.n1 + q.u1) * ncell;
-        v.p11 = (v0 * d.n1 + v1) * ncell;
-        smp[threadIdx.x] = v;
+        sc.p[0][u] = (q.u0 * d.n1 + q.u1) * ncell;
+        sc.p[1][u] = (q.u0 * d.n1 + v1) * ncell;
+        sc.p[2][u] = (v0 * d.n1 + q.u1) * ncell;
+        sc.p[3][u] = (v0 * d.n1 + v1) * ncell;
       }
       __syncthreads();
-      for (int ch = 0; ch < nch; ch++) {
-        const SampleCorners<Real> v(smp[ch]);
+      // the plane of samples (ch, ch + 1): bilinear in (height, elevation)
+      for (int ch = 0; ch < nch; ch += 2) {
+        const bool two = ch + 1 < nch;
+        const int ch1 = two ? ch + 1 : ch;
+        const int pa[4] = {sc.p[0][ch], sc.p[1][ch], sc.p[2][ch], sc.p[3][ch]};
+        const int pb[4] = {sc.p[0][ch1], sc.p[1][ch1], sc.p[2][ch1], sc.p[3][ch1]};
+        const R2 s0 = mk2(sc.s0[ch], sc.s0[ch1]), s1 = mk2(sc.s1[ch], sc.s1[ch1]);
         for (int t = threadIdx.x; t < ncell; t += blockDim.x) {
-          Real A[3], B[3], lo[3], hi[3];
-          ld3(tJ, (long long)v.p[0] + t, A);
-          ld3(tJ, (long long)v.p[1] + t, B);
+          Real* dst0 = plane + 3 * (ch * ncell + t);
+          Real* dst1 = dst0 + 3 * ncell;
 #pragma unroll
-          for (int c = 0; c < 3; c++) lo[c] = fma(B[c] - A[c], v.s1, A[c]);
-          ld3(tJ, (long long)v.p[2] + t, A);
-          ld3(tJ, (long long)v.p[3] + t, B);
-#pragma unroll
-          for (int c = 0; c < 3; c++) hi[c] = fma(B[c] - A[c], v.s1, A[c]);
-          Real* dst = plane + 3 * (ch * ncell + t);
-#pragma unroll
-          for (int c = 0; c < 3; c++) dst[c] = fma(hi[c] - lo[c], v.s0, lo[c]);
+          for (int c = 0; c < 3; c++) {
+            const Real* tc = tJ + c * n4 + t;
+            const R2 A = mk2(tc[pa[0]], tc[pb[0]]), B = mk2(tc[pa[1]], tc[pb[1]]);
+            const R2 C = mk2(tc[pa[2]], tc[pb[2]]), E = mk2(tc[pa[3]], tc[pb[3]]);
+            const R2 lo = fma2(sub2(B, A), s1, A), hi = fma2(sub2(E, C), s1, C);
+            const R2 v = fma2(sub2(hi, lo), s0, lo);
+            dst0[c] = v.x;
+            if (two) dst1[c] = v.y;
+          }
         }
       }
       __syncthreads();
       if (active) {
-        // samples alternate between two sums for independent FMA chains
-        auto sample = [&](int ch, Real(&a)[3]) {
-          const SampleView<Real> v(smp[ch]);
-          const Real sin_el = fma(v.us, Dl, b0) * v.inv_r;  // p_s.l / |p_s|
+        int ch = 0;
+        for (; ch + 1 < nch; ch += 2) {
+          const R2 sin_el = mul2(fma2(ld2(sc.us + ch), Dl2, b02), ld2(sc.inv_r + ch));  // p_s.l / |p_s|
+          const R2 ie = sun_elevation_index_r2<Real>(sin_el, scale2);
+          int ua, ub;
+          Real sa, sb;
+          split_coord_r<Real>(ie.x, d.n2, &ua, &sa);
+          split_coord_r<Real>(ie.y, d.n2, &ub, &sb);
+          const R2 s2 = mk2(sa, sb);
+          const Real* loa = plane + 3 * ch * ncell + ua * n3x3;
+          const Real* hia = ua + 1 < d.n2 ? loa + n3x3 : loa;
+          const Real* lob = plane + 3 * (ch + 1) * ncell + ub * n3x3;
+          const Real* hib = ub + 1 < d.n2 ? lob + n3x3 : lob;
+#pragma unroll
+          for (int c = 0; c < 3; c++) {
+            const R2 lu = mk2(loa[o3u + c], lob[o3u + c]), lv = mk2(loa[o3v + c], lob[o3v + c]);
+            const R2 hu = mk2(hia[o3u + c], hib[o3u + c]), hv = mk2(hia[o3v + c], hib[o3v + c]);
+            const R2 x0 = fma2(sub2(lv, lu), s32, lu);
+            const R2 x1 = fma2(sub2(hv, hu), s32, hu);
+            acc[c] = fma2(ld2(sc.T[c] + ch), fma2(sub2(x1, x0), s2, x0), acc[c]);
+          }
+        }
+        if (ch < nch) {
+          const Real sin_el = fma(sc.us[ch], Dl, b0) * sc.inv_r[ch];
           int u2;
           Real s2;
           split_coord_r<Real>(sun_elevation_index_r<Real>(sin_el, scale2), d.n2, &u2, &s2);
@@ -536,23 +578,17 @@ __global__ void __launch_bounds__(256, ray_scatter_min_blocks(sizeof(Real)))
           for (int c = 0; c < 3; c++) {
             const Real x0 = fma(lo[o3v + c] - lo[o3u + c], s3, lo[o3u + c]);
             const Real x1 = fma(hi[o3v + c] - hi[o3u + c], s3, hi[o3u + c]);
-            a[c] = fma(v.T[c], fma(x1 - x0, s2, x0), a[c]);
+            acc[c].x = fma(sc.T[c][ch], fma(x1 - x0, s2, x0), acc[c].x);
           }
-        };
-        int ch = 0;
-        for (; ch + 1 < nch; ch += 2) {
-          sample(ch, acc[0]);
-          sample(ch + 1, acc[1]);
         }
-        if (ch < nch) sample(ch, acc[0]);
       }
     }
     if (active) {
       const Real w = rw.Ls;
       Vec4<Real> o;
-      o.x = w * (acc[0][0] + acc[1][0]);
-      o.y = w * (acc[0][1] + acc[1][1]);
-      o.z = w * (acc[0][2] + acc[1][2]);
+      o.x = w * (acc[0].x + acc[0].y);
+      o.y = w * (acc[1].x + acc[1].y);
+      o.z = w * (acc[2].x + acc[2].y);
       o.w = 0;
       dS[node0 + cell] = o;
     }
@@ -562,11 +598,11 @@ __global__ void __launch_bounds__(256, ray_scatter_min_blocks(sizeof(Real)))
 template <class Real>
 int launch_ray_scatter(const AtmoParams* params, const BuildDims& d, const RowInfo* rowinfo,
                        const RowSample<Real>* rows, const CellGeom<Real>* geom, const Remap4<Real>* remap,
-                       const Vec4<Real>* J, Vec4<Real>* dS, cudaStream_t st) {
+                       const Real* J, Vec4<Real>* dS, cudaStream_t st) {
   constexpr int CH = 16;
   const int ncell = d.n2 * d.n3;
   const int block = ncell >= 256 ? 256 : ((ncell + 31) / 32) * 32;
-  size_t smem = sizeof(RaySample<Real>) * CH + sizeof(Real) * 3 * (size_t)CH * ncell;
+  size_t smem = ((sizeof(RayChunk<Real, CH>) + 15) & ~size_t(15)) + sizeof(Real) * 3 * (size_t)CH * ncell;
   if (cudaFuncSetAttribute(k_ray_scatter<Real, CH>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
       cudaSuccess)
     return -1;
@@ -654,22 +690,22 @@ __global__ void k_output2(int n0, int n1, const Remap2<Real>* remap, const Vec4<
 }
 
 template <class Real>
-__global__ void k_add_to_sum(long long n, const Vec4<Real>* J, Vec4<float>* jsum, bool first) {
+__global__ void k_add_to_sum(long long n4, int B, const Real* J, Vec4<float>* jsum, bool first) {
   const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (t >= n) return;
-  const Vec4<Real> v = J[t];
+  if (t >= n4 * B) return;
+  const Real* src = J + (t / n4) * 3 * n4 + t % n4;
   Vec4<float> o;
   if (first) {
-    o.x = (float)v.x;
-    o.y = (float)v.y;
-    o.z = (float)v.z;
+    o.x = 0;
+    o.y = 0;
+    o.z = 0;
+    o.w = 0;
   } else {
     o = jsum[t];
-    o.x += (float)v.x;
-    o.y += (float)v.y;
-    o.z += (float)v.z;
   }
-  o.w = 0;
+  o.x += (float)src[0];
+  o.y += (float)src[n4];
+  o.z += (float)src[2 * n4];
   jsum[t] = o;
 }
 
@@ -710,8 +746,23 @@ void launch_output2(int B, int n0, int n1, const Remap2<Real>* remap, const Vec4
 }
 
 template <class Real>
-void launch_add_to_sum(long long n, const Vec4<Real>* J, Vec4<float>* jsum, bool first, cudaStream_t st) {
-  k_add_to_sum<Real><<<grid1(n, 256, 1), 256, 0, st>>>(n, J, jsum, first);
+void launch_add_to_sum(long long n4, int B, const Real* J, Vec4<float>* jsum, bool first, cudaStream_t st) {
+  k_add_to_sum<Real><<<grid1(n4 * B, 256, 1), 256, 0, st>>>(n4, B, J, jsum, first);
+}
+
+template <class Real>
+__global__ void k_export_planar(long long n4, int B, const Real* tab, float* out) {
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t >= n4 * B) return;
+  const Real* src = tab + (t / n4) * 3 * n4 + t % n4;
+  out[3 * t] = (float)src[0];
+  out[3 * t + 1] = (float)src[n4];
+  out[3 * t + 2] = (float)src[2 * n4];
+}
+
+template <class Real>
+void launch_export_planar(long long n4, int B, const Real* tab, float* out, cudaStream_t st) {
+  k_export_planar<Real><<<grid1(n4 * B, 256, 1), 256, 0, st>>>(n4, B, tab, out);
 }
 
 template <class Real>
@@ -723,13 +774,13 @@ void launch_export(long long n, const Vec4<Real>* tab, float* out, cudaStream_t 
   template int launch_point_scatter<Real>(const AtmoParams*, const BuildDims&, const RowInfo*,                     \
                                           const SphereDir<Real>*, const int2*, const PointRow<Real>*,              \
                                           const CellGeom<Real>*, const Vec4<Real>*, const Vec4<Real>*,             \
-                                          const Vec4<Real>*, Vec4<Real>*, cudaStream_t);                           \
+                                          const Vec4<Real>*, Real*, cudaStream_t);                                 \
   template void launch_surface_radiance<Real>(const AtmoParams*, const BuildDims&, const SurfRow<Real>*,          \
                                               const HalfDir<Real>*, const Vec4<Real>*, const Vec4<Real>*,          \
                                               Vec4<Real>*, cudaStream_t);                                          \
   template int launch_ray_scatter<Real>(const AtmoParams*, const BuildDims&, const RowInfo*, const RowSample<Real>*, \
-                                        const CellGeom<Real>*, const Remap4<Real>*, const Vec4<Real>*,             \
-                                        Vec4<Real>*, cudaStream_t);                                                \
+                                        const CellGeom<Real>*, const Remap4<Real>*, const Real*, Vec4<Real>*,      \
+                                        cudaStream_t);                                                             \
   template void launch_accumulate4<Real>(const BuildDims&, const Remap4<Real>*, const Vec4<Real>*,                 \
                                          const Vec4<Real>*, Vec4<Real>*, cudaStream_t);                            \
   template void launch_accumulate2<Real>(int, int, int, const Remap2<Real>*, const Vec4<Real>*, const Vec4<Real>*, \
@@ -738,7 +789,8 @@ void launch_export(long long n, const Vec4<Real>* tab, float* out, cudaStream_t 
                                      cudaStream_t);                                                                \
   template void launch_output2<Real>(int, int, int, const Remap2<Real>*, const Vec4<Real>*, float*, cudaStream_t);  \
   template void launch_export<Real>(long long, const Vec4<Real>*, float*, cudaStream_t);                           \
-  template void launch_add_to_sum<Real>(long long, const Vec4<Real>*, Vec4<float>*, bool, cudaStream_t);            \
+  template void launch_add_to_sum<Real>(long long, int, const Real*, Vec4<float>*, bool, cudaStream_t);           \
+  template void launch_export_planar<Real>(long long, int, const Real*, float*, cudaStream_t);                      \
   template size_t point_scatter_smem<Real>(const BuildDims&, bool);
 
 SFSIM_INSTANTIATE(float)

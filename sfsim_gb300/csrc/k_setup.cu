@@ -12,25 +12,66 @@ namespace sfsim {
 // atmosphere_lut.clj:94-101).  These kernels store that coordinate per node.
 // ---------------------------------------------------------------------------
 
+// Per view row (i, j), once: the row's geometry (RowInfo) and its height and
+// elevation coordinates, which every node and ray sample of the row shares.
 template <class Real>
-__global__ void k_remap4(const AtmoParams* params, BuildDims d, Remap4<Real>* out, CellGeom<Real>* geom) {
+__global__ void k_row_info(const AtmoParams* params, BuildDims d, RowInfo* info, Remap2<Real>* rowmap) {
+  const long long nrows = d.rows();
+  const long long row = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  const int b = blockIdx.y;
+  if (row >= nrows) return;
+  const AtmoParams& P = params[b];
+  const int j = (int)(row % d.n1), i = (int)(row / d.n1);
+  double r, sv, cv;
+  int above;
+  view_geometry(P, d, i, j, &r, &sv, &cv, &above);
+  const d3 x = mk3(r, 0, 0), v = mk3(sv, cv, 0);
+  const d3 e = above ? atmosphere_intersection(P, x, v) : surface_intersection(P, x, v);
+  const d3 D = sub3(e, x);
+  RowInfo ri;
+  ri.r = r;
+  ri.sv = sv;
+  ri.cv = cv;
+  ri.D[0] = D.x;
+  ri.D[1] = D.y;
+  ri.D[2] = D.z;
+  ri.L = mag3(D);
+  ri.Ls = ri.L / d.S;
+  ri.f_r = (float)r;
+  ri.f_sv = (float)sv;
+  ri.f_cv = (float)cv;
+  ri.f_D[0] = (float)D.x;
+  ri.f_D[1] = (float)D.y;
+  ri.f_D[2] = (float)D.z;
+  ri.f_Ls = (float)ri.Ls;
+  ri.above = above;
+  info[b * nrows + row] = ri;
+  Remap2<Real> m;
+  split_coord<Real>(height_to_index(P, d.n0, mag3(x)), d.n0, &m.u[0], &m.s[0]);
+  split_coord<Real>(elevation_to_index(P, d.n1, x, v, above), d.n1, &m.u[1], &m.s[1]);
+  rowmap[b * nrows + row] = m;
+}
+
+template <class Real>
+__global__ void k_remap4(const AtmoParams* params, BuildDims d, const RowInfo* info, const Remap2<Real>* rowmap,
+                         Remap4<Real>* out, CellGeom<Real>* geom) {
   const long long n4 = d.n4();
   const long long node = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   const int b = blockIdx.y;
   if (node >= n4) return;
-  const AtmoParams& P = params[b];
   int a = (int)(node % d.n3);
   int k = (int)((node / d.n3) % d.n2);
-  int j = (int)((node / ((long long)d.n3 * d.n2)) % d.n1);
-  int i = (int)(node / ((long long)d.n3 * d.n2 * d.n1));
-  double r, sv, cv;
-  int above;
-  view_geometry(P, d, i, j, &r, &sv, &cv, &above);
+  const long long row = node / ((long long)d.n3 * d.n2);
+  const RowInfo& ri = info[b * d.rows() + row];
+  const Remap2<Real> rm = rowmap[b * d.rows() + row];
+  const double r = ri.r, sv = ri.sv, cv = ri.cv;
   d3 x = mk3(r, 0, 0), v = mk3(sv, cv, 0);
   d3 l = light_direction(d, sv, cv, k, a);
   Remap4<Real> m;
-  split_coord<Real>(height_to_index(P, d.n0, mag3(x)), d.n0, &m.u[0], &m.s[0]);
-  split_coord<Real>(elevation_to_index(P, d.n1, x, v, above), d.n1, &m.u[1], &m.s[1]);
+  m.u[0] = rm.u[0];
+  m.s[0] = rm.s[0];
+  m.u[1] = rm.u[1];
+  m.s[1] = rm.s[1];
   split_coord<Real>(sun_elevation_to_index(d.n2, x, l), d.n2, &m.u[2], &m.s[2]);
   split_coord<Real>(sun_angle_to_index(d.n3, v, l), d.n3, &m.u[3], &m.s[3]);
   out[b * n4 + node] = m;
@@ -147,7 +188,7 @@ __global__ void k_surface_base(const AtmoParams* params, BuildDims d, Vec4<Real>
 // ---------------------------------------------------------------------------
 
 template <class Real>
-__global__ void k_view_rows(const AtmoParams* params, BuildDims d, RowInfo* info, RowSample<Real>* samples) {
+__global__ void k_view_rows(const AtmoParams* params, BuildDims d, const RowInfo* info, RowSample<Real>* samples) {
   const long long nrows = d.rows();
   const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   const int b = blockIdx.y;
@@ -155,33 +196,10 @@ __global__ void k_view_rows(const AtmoParams* params, BuildDims d, RowInfo* info
   const AtmoParams& P = params[b];
   const int s = (int)(t % d.S);
   const long long row = t / d.S;
-  const int j = (int)(row % d.n1), i = (int)(row / d.n1);
-  double r, sv, cv;
-  int above;
-  view_geometry(P, d, i, j, &r, &sv, &cv, &above);
-  d3 x = mk3(r, 0, 0), v = mk3(sv, cv, 0);
-  d3 e = above ? atmosphere_intersection(P, x, v) : surface_intersection(P, x, v);
-  d3 D = sub3(e, x);
-  if (s == 0) {
-    RowInfo ri;
-    ri.r = r;
-    ri.sv = sv;
-    ri.cv = cv;
-    ri.D[0] = D.x;
-    ri.D[1] = D.y;
-    ri.D[2] = D.z;
-    ri.L = mag3(D);
-    ri.Ls = ri.L / d.S;
-    ri.f_r = (float)r;
-    ri.f_sv = (float)sv;
-    ri.f_cv = (float)cv;
-    ri.f_D[0] = (float)D.x;
-    ri.f_D[1] = (float)D.y;
-    ri.f_D[2] = (float)D.z;
-    ri.f_Ls = (float)ri.Ls;
-    ri.above = above;
-    info[b * nrows + row] = ri;
-  }
+  const RowInfo& ri = info[b * nrows + row];
+  const int above = ri.above;
+  const d3 x = mk3(ri.r, 0, 0), v = mk3(ri.sv, ri.cv, 0);
+  const d3 D = mk3(ri.D[0], ri.D[1], ri.D[2]);
   // sample point as integral-ray forms it (ray.clj:22-24)
   double stepsize = 1.0 / d.S;
   double su = (0.5 + s) * stepsize;
@@ -387,7 +405,8 @@ template <class Real>
 void launch_setup(const AtmoParams* params, const BuildDims& d, const DirLocal* dirs, const int* ring_end,
                   const DirLocal* half_dirs, const SetupBuffers<Real>& o, cudaStream_t st) {
   const int blk = 128;
-  k_remap4<Real><<<grid1(d.n4(), blk, d.B), blk, 0, st>>>(params, d, o.remapS, o.geom);
+  k_row_info<Real><<<grid1(d.rows(), blk, d.B), blk, 0, st>>>(params, d, o.rowinfo, o.rowmap);
+  k_remap4<Real><<<grid1(d.n4(), blk, d.B), blk, 0, st>>>(params, d, o.rowinfo, o.rowmap, o.remapS, o.geom);
   k_remapT<Real><<<grid1(d.nT(), blk, d.B), blk, 0, st>>>(params, d, o.remapT);
   k_remapE<Real><<<grid1(d.nE(), blk, d.B), blk, 0, st>>>(params, d, o.remapE);
   k_view_rows<Real><<<grid1(d.rows() * d.S, blk, d.B), blk, 0, st>>>(params, d, o.rowinfo, o.rows);

@@ -15,6 +15,7 @@ struct SetupBuffers {
   Remap2<Real>* remapT;
   Remap2<Real>* remapE;
   RowInfo* rowinfo;
+  Remap2<Real>* rowmap;  // [B][rows]: height and elevation coordinates of each view row
   RowSample<Real>* rows;
   SphereDir<Real>* sdirs;
   // sdirs partitioned per height row: the directions that end in the sky,
@@ -64,13 +65,13 @@ void launch_sfu_probe(int blocks, int threads, int iters, float* sink, cudaStrea
 // reading `iters` x 8 16-byte words.
 int launch_smem_probe(int blocks, int iters, float* sink, cudaStream_t st);
 
-// J = point scatter of (dS, dE); when `mie` is non-NULL dS is the first
-// iteration's rayleigh + mie * phase(mie, v.l).
+// J = point scatter of (dS, dE), planar [atmosphere][channel][node]; when
+// `mie` is non-NULL dS is the first iteration's rayleigh + mie * phase(mie, v.l).
 template <class Real>
 int launch_point_scatter(const AtmoParams* params, const BuildDims& d, const RowInfo* rowinfo,
                          const SphereDir<Real>* pdirs, const int2* pcount, const PointRow<Real>* prow,
                          const CellGeom<Real>* geom, const Vec4<Real>* dS,
-                         const Vec4<Real>* mie, const Vec4<Real>* dE, Vec4<Real>* J, cudaStream_t st);
+                         const Vec4<Real>* mie, const Vec4<Real>* dE, Real* J, cudaStream_t st);
 
 // dE = surface radiance of dS (same first-iteration convention).
 template <class Real>
@@ -78,11 +79,11 @@ void launch_surface_radiance(const AtmoParams* params, const BuildDims& d, const
                              const HalfDir<Real>* hdir, const Vec4<Real>* dS, const Vec4<Real>* mie,
                              Vec4<Real>* dE, cudaStream_t st);
 
-// dS = ray scatter of J.
+// dS = ray scatter of J (planar [atmosphere][channel][node]).
 template <class Real>
 int launch_ray_scatter(const AtmoParams* params, const BuildDims& d, const RowInfo* rowinfo,
                        const RowSample<Real>* rows, const CellGeom<Real>* geom, const Remap4<Real>* remap,
-                       const Vec4<Real>* J, Vec4<Real>* dS, cudaStream_t st);
+                       const Real* J, Vec4<Real>* dS, cudaStream_t st);
 
 // out = re-interpolation of (a + b) at the node maps; b may be NULL and, for
 // the 2-D variant, a may be NULL.
@@ -147,9 +148,14 @@ void launch_pack_infer(const __nv_bfloat16* const* W, unsigned char* packed, cud
 // Bytes of the packed weight chunks the inference kernel streams.
 size_t infer_packed_bytes();
 
-// jsum = (first ? 0 : jsum) + J, converted to float.
+// jsum = (first ? 0 : jsum) + J, converted to float; J planar
+// [atmosphere][channel][node] with n4 nodes per atmosphere.
 template <class Real>
-void launch_add_to_sum(long long n, const Vec4<Real>* J, Vec4<float>* jsum, bool first, cudaStream_t st);
+void launch_add_to_sum(long long n4, int B, const Real* J, Vec4<float>* jsum, bool first, cudaStream_t st);
+
+// Float [atmosphere][node][channel] copy of a planar table.
+template <class Real>
+void launch_export_planar(long long n4, int B, const Real* tab, float* out, cudaStream_t st);
 
 // Plain-order float copy of an internal table (debug intermediates).
 template <class Real>
