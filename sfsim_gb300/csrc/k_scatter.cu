@@ -70,8 +70,9 @@ struct TexelRow {
 //         sE0 of each direction (structure of arrays, so that two consecutive
 //         directions' components load as one pair);
 //   uE0   [used] int;
-//   rows  [used][n3 + 1][3] dS gathered along the heading axis, texel n3 a
-//         copy of texel n3 - 1 (and the Mie rows in the first iteration);
+//   rows  [used][n3 + 2][3] dS gathered along the heading axis between
+//         copies of its first and last texel (and the Mie rows in the first
+//         iteration);
 //   etab  [nE0][nE1][3] the dE table.
 constexpr int kDirFields = 11;
 
@@ -105,10 +106,14 @@ __global__ void __launch_bounds__(256, point_scatter_min_blocks(sizeof(Real))) k
   const int2 pc = pcount[(long long)b * d.n0 + i];
   const int sky_end = pc.x, used = pc.y;
   const int nrow = used * d.n3;
-  const int rlen = d.n3 + 1;  // texels of a heading row, the last one a copy of texel n3 - 1
+  // texels of a heading row: a copy of texel 0, the n3 texels, a copy of
+  // texel n3 - 1, so that a sun-angle coordinate that rounding pushed just
+  // outside [0, n3 - 1] reads the edge texel without a clamp
+  const int rlen = d.n3 + 2;
   Real* dirs = reinterpret_cast<Real*>(smem_raw);
   int* uE0s = reinterpret_cast<int*>(dirs + kDirFields * used);
-  Real* rows = reinterpret_cast<Real*>(smem_raw + (((size_t)used * (kDirFields * sizeof(Real) + sizeof(int)) + 15) & ~size_t(15)));
+  const size_t dir_bytes = ((size_t)used * (kDirFields * sizeof(Real) + sizeof(int)) + 15) & ~size_t(15);
+  Real* rows = reinterpret_cast<Real*>(smem_raw + dir_bytes);
   Real* rowsM = rows + RS * used * rlen;
   Real* etab = rowsM + (FIRST ? RS * used * rlen : 0);
 
@@ -136,9 +141,13 @@ __global__ void __launch_bounds__(256, point_scatter_min_blocks(sizeof(Real))) k
       gather_heading_row(dS + base4, d, u0, v0, s0, u1, v1, s1, u2, v2, s2, a, v);
       if (FIRST) gather_heading_row(Mt + base4, d, u0, v0, s0, u1, v1, s1, u2, v2, s2, a, vm);
     }
-    const int o = w * rlen + a;
+    const int o = w * rlen + 1 + a;
     TR::store(rows, o, v);
     if (FIRST) TR::store(rowsM, o, vm);
+    if (a == 0) {
+      TR::store(rows, o - 1, v);
+      if (FIRST) TR::store(rowsM, o - 1, vm);
+    }
     if (a == d.n3 - 1) {
       TR::store(rows, o + 1, v);
       if (FIRST) TR::store(rowsM, o + 1, vm);
@@ -210,14 +219,15 @@ __global__ void __launch_bounds__(256, point_scatter_min_blocks(sizeof(Real))) k
       const R2 mu_l = fma2(X0, lx2, fma2(X1, ly2, mul2(X2, lz2)));
       // sun-angle coordinates of (omega, l) along the two directions' heading rows
       const R2 c3 = fma2(sc3, mu_l, sc3);
-      int ua, ub;
-      Real sa, sb;
-      split_coord_r<Real>(c3.x, d.n3, &ua, &sa);
-      split_coord_r<Real>(c3.y, d.n3, &ub, &sb);
-      const R2 s3 = mk2(sa, sb);
-      // texels u and u + 1 (the row's copy of its last texel when u = n3 - 1, where s = 0)
-      const Real* ra = rows + wa * row_len + 3 * ua;
-      const Real* rb = rows + (wa + 1) * row_len + 3 * ub;
+      // |mu| <= 1 up to rounding, so floor(c) lies in [-1, n3 - 1]: texels u
+      // and u + 1 of the padded row give the clamped interpolation exactly
+      // (at u = -1 both are texel 0, at u = n3 - 1 the weight s of the copy
+      // is rounding-small and both are texel n3 - 1)
+      const Real fa = floor(c3.x), fb = floor(c3.y);
+      const int ua = (int)fa, ub = (int)fb;
+      const R2 s3 = sub2(c3, mk2(fa, fb));
+      const Real* ra = rows + wa * row_len + 3 * (ua + 1);
+      const Real* rb = rows + (wa + 1) * row_len + 3 * (ub + 1);
       R2 X[3];
 #pragma unroll
       for (int c = 0; c < 3; c++) {
@@ -226,8 +236,8 @@ __global__ void __launch_bounds__(256, point_scatter_min_blocks(sizeof(Real))) k
       }
       if (FIRST) {
         const R2 ph = phM.pair(mu_l);
-        const Real* ma = rowsM + wa * row_len + 3 * ua;
-        const Real* mb = rowsM + (wa + 1) * row_len + 3 * ub;
+        const Real* ma = rowsM + wa * row_len + 3 * (ua + 1);
+        const Real* mb = rowsM + (wa + 1) * row_len + 3 * (ub + 1);
 #pragma unroll
         for (int c = 0; c < 3; c++) {
           const R2 lo = mk2(ma[c], mb[c]), hi = mk2(ma[3 + c], mb[3 + c]);
@@ -307,7 +317,7 @@ template <class Real>
 size_t point_scatter_smem(const BuildDims& d, bool first) {
   const size_t n = dir_row(d.P);
   return ((n * (kDirFields * sizeof(Real) + sizeof(int)) + 15) & ~size_t(15)) +
-         sizeof(Real) * 3 * (n * (d.n3 + 1) * (first ? 2 : 1) + d.nE());
+         sizeof(Real) * 3 * (n * (d.n3 + 2) * (first ? 2 : 1) + d.nE());
 }
 
 template <class Real>
