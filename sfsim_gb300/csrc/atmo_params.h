@@ -127,10 +127,13 @@ struct RowInfo {
 };
 
 // Per (height i, sun elevation k) of the 4-D space, from FP64: the height
-// and sun-elevation coordinates of point scatter's dS lookups at x, and the
-// scattering coefficients beta(x) it multiplies its sums with.
+// and sun-elevation coordinates of the dS lookups at x = (r_i, 0, 0) (also
+// those of every node (i, ., k, .), whose light direction has x.l = r_i sin),
+// and the scattering coefficients beta(x) point scatter multiplies its sums
+// with.
 template <class Real>
 struct PointRow {
+  double ss;  // sin of the sun elevation of index k (index-to-sin-sun-elevation)
   int u0, u2;
   Real s0, s2;
   Real bR[3], bM[3];

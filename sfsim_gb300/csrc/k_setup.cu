@@ -52,9 +52,13 @@ __global__ void k_row_info(const AtmoParams* params, BuildDims d, RowInfo* info,
   rowmap[b * nrows + row] = m;
 }
 
+// The height and elevation coordinates of a node are its row's (k_row_info);
+// its light direction l = index-to-sun-direction(v, sin(k), a) has
+// x.l = r sin(k) with x = (r, 0, 0), so its sun-elevation coordinate is the
+// (i, k) one of k_point_rows, which also holds sin(k).
 template <class Real>
 __global__ void k_remap4(const AtmoParams* params, BuildDims d, const RowInfo* info, const Remap2<Real>* rowmap,
-                         Remap4<Real>* out, CellGeom<Real>* geom) {
+                         const PointRow<Real>* prow, Remap4<Real>* out, CellGeom<Real>* geom) {
   const long long n4 = d.n4();
   const long long node = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   const int b = blockIdx.y;
@@ -62,17 +66,20 @@ __global__ void k_remap4(const AtmoParams* params, BuildDims d, const RowInfo* i
   int a = (int)(node % d.n3);
   int k = (int)((node / d.n3) % d.n2);
   const long long row = node / ((long long)d.n3 * d.n2);
+  const int i = (int)(row / d.n1);
   const RowInfo& ri = info[b * d.rows() + row];
   const Remap2<Real> rm = rowmap[b * d.rows() + row];
-  const double r = ri.r, sv = ri.sv, cv = ri.cv;
-  d3 x = mk3(r, 0, 0), v = mk3(sv, cv, 0);
-  d3 l = light_direction(d, sv, cv, k, a);
+  const PointRow<Real>& pk = prow[((long long)b * d.n0 + i) * d.n2 + k];
+  const double sv = ri.sv, cv = ri.cv;
+  const d3 v = mk3(sv, cv, 0);
+  const d3 l = index_to_sun_direction(d.n3, v, pk.ss, (double)a);
   Remap4<Real> m;
   m.u[0] = rm.u[0];
   m.s[0] = rm.s[0];
   m.u[1] = rm.u[1];
   m.s[1] = rm.s[1];
-  split_coord<Real>(sun_elevation_to_index(d.n2, x, l), d.n2, &m.u[2], &m.s[2]);
+  m.u[2] = pk.u2;
+  m.s[2] = pk.s2;
   split_coord<Real>(sun_angle_to_index(d.n3, v, l), d.n3, &m.u[3], &m.s[3]);
   out[b * n4 + node] = m;
   CellGeom<Real> g;
@@ -336,6 +343,7 @@ __global__ void k_point_rows(const AtmoParams* params, BuildDims d, PointRow<Rea
   const double r = index_to_radius(P, d.n0, (double)i);
   const double ss = index_to_sin_sun_elevation(d.n2, (double)k);
   PointRow<Real> o;
+  o.ss = ss;
   split_coord<Real>(height_to_index(P, d.n0, r), d.n0, &o.u0, &o.s0);
   split_coord<Real>(sun_elevation_to_index(d.n2, mk3(r, 0, 0), mk3(ss, 0, 0)), d.n2, &o.u2, &o.s2);
   const double h = r - P.R;
@@ -406,13 +414,14 @@ void launch_setup(const AtmoParams* params, const BuildDims& d, const DirLocal* 
                   const DirLocal* half_dirs, const SetupBuffers<Real>& o, cudaStream_t st) {
   const int blk = 128;
   k_row_info<Real><<<grid1(d.rows(), blk, d.B), blk, 0, st>>>(params, d, o.rowinfo, o.rowmap);
-  k_remap4<Real><<<grid1(d.n4(), blk, d.B), blk, 0, st>>>(params, d, o.rowinfo, o.rowmap, o.remapS, o.geom);
+  k_point_rows<Real><<<grid1((long long)d.n0 * d.n2, blk, d.B), blk, 0, st>>>(params, d, o.prow);
+  k_remap4<Real><<<grid1(d.n4(), blk, d.B), blk, 0, st>>>(params, d, o.rowinfo, o.rowmap, o.prow, o.remapS,
+                                                            o.geom);
   k_remapT<Real><<<grid1(d.nT(), blk, d.B), blk, 0, st>>>(params, d, o.remapT);
   k_remapE<Real><<<grid1(d.nE(), blk, d.B), blk, 0, st>>>(params, d, o.remapE);
   k_view_rows<Real><<<grid1(d.rows() * d.S, blk, d.B), blk, 0, st>>>(params, d, o.rowinfo, o.rows);
   k_sphere_setup<Real><<<grid1((long long)d.n0 * d.P, blk, d.B), blk, 0, st>>>(params, d, dirs, ring_end, o.sdirs);
   k_sphere_partition<Real><<<dim3(d.n0, d.B), 32, 0, st>>>(d, o.sdirs, o.pdirs, o.pcount);
-  k_point_rows<Real><<<grid1((long long)d.n0 * d.n2, blk, d.B), blk, 0, st>>>(params, d, o.prow);
   k_surface_rows<Real><<<grid1(d.nE(), blk, d.B), blk, 0, st>>>(params, d, o.erow);
   k_half_dirs<Real><<<grid1((long long)d.nE0 * d.Ph, blk, d.B), blk, 0, st>>>(params, d, half_dirs, o.hdir);
 }
