@@ -91,15 +91,19 @@ __global__ void __launch_bounds__(256, point_scatter_min_blocks(sizeof(Real))) k
                                                           const int2* pcount, const PointRow<Real>* prow,
                                                           const CellGeom<Real>* geom,
                                                           const Vec4<Real>* dS, const Vec4<Real>* Mt,
-                                                          const Vec4<Real>* dE, Real* J, int nchunks) {
+                                                          const Vec4<Real>* dE, Real* J, int nchunks,
+                                                          int chunks_per_block) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   using TR = TexelRow<Real>;
   using R2 = V2<Real>;
   constexpr int RS = TR::kStride;
   constexpr int DB = kDirBlock;
   const int b = blockIdx.y;
-  const int chunk = blockIdx.x % nchunks;
-  const int ik = blockIdx.x / nchunks;
+  // one (height i, sun elevation k) pair, chunks_per_block chunks of 256 of
+  // its (elevation, heading) nodes: the rows are gathered once for them all
+  const int nblk = (nchunks + chunks_per_block - 1) / chunks_per_block;
+  const int chunk0 = (blockIdx.x % nblk) * chunks_per_block;
+  const int ik = blockIdx.x / nblk;
   const int i = ik / d.n2, k = ik % d.n2;
   const AtmoParams& P = params[b];
   const PointRow<Real>* prk = prow + ((long long)b * d.n0 + i) * d.n2 + k;
@@ -161,156 +165,172 @@ __global__ void __launch_bounds__(256, point_scatter_min_blocks(sizeof(Real))) k
   }
   __syncthreads();
 
-  // a lane past the last node keeps running (it feeds the warp's shuffles) but stores nothing
-  const int nslab = d.n1 * d.n3;
-  const int cell_raw = chunk * blockDim.x + threadIdx.x;
-  const bool valid = cell_raw < nslab;
-  const int cell = valid ? cell_raw : nslab - 1;
-  const int j = cell / d.n3, a = cell % d.n3;
-  const RowR<Real> rw = row_r<Real>(rowinfo[(long long)b * d.rows() + (long long)i * d.n1 + j]);
-  const Real sv = rw.sv, cv = rw.cv;
-  const long long node = base4 + idx4(d, i, j, k, a);
-  const CellGeom<Real> g = geom[node];
-  const PhaseCS<Real> phR(Bulk<Real>::phase_ray(P)), phM(Bulk<Real>::phase_mie(P));
-  const Real scale3 = Real(0.5) * Real(d.n3 - 1);
-  const Real scaleE = Bulk<Real>::sun_scale_E(d);
-  // The weighted phases depend on (j, direction) only.  When the n3 headings
-  // of one j fill aligned lane groups of at least DB lanes, lane p of a group
-  // evaluates them for direction p of a block of DB and the group exchanges
-  // them by shuffles.
-  const int G = d.n3;
-  const bool share = G >= DB && (32 % G == 0) && (blockDim.x % G == 0);
-  const int lane = threadIdx.x & 31;
-  const int gbase = share ? (lane & ~(G - 1)) : lane;
-  const int gpos = lane - gbase;
-  const int row_len = RS * rlen;
-  const R2 lx2 = mk2(g.lx, g.lx), ly2 = mk2(g.ly, g.ly), lz2 = mk2(g.lz, g.lz);
-  const R2 sv2 = mk2(sv, sv), cv2 = mk2(cv, cv), sc3 = mk2(scale3, scale3);
+  for (int chunk = chunk0; chunk < min(chunk0 + chunks_per_block, nchunks); chunk++) {
+    // a lane past the last node keeps running (it feeds the warp's shuffles) but stores nothing
+    const int nslab = d.n1 * d.n3;
+    const int cell_raw = chunk * blockDim.x + threadIdx.x;
+    const bool valid = cell_raw < nslab;
+    const int cell = valid ? cell_raw : nslab - 1;
+    const int j = cell / d.n3, a = cell % d.n3;
+    const RowR<Real> rw = row_r<Real>(rowinfo[(long long)b * d.rows() + (long long)i * d.n1 + j]);
+    const Real sv = rw.sv, cv = rw.cv;
+    const long long node = base4 + idx4(d, i, j, k, a);
+    const CellGeom<Real> g = geom[node];
+    const PhaseCS<Real> phR(Bulk<Real>::phase_ray(P)), phM(Bulk<Real>::phase_mie(P));
+    const Real scale3 = Real(0.5) * Real(d.n3 - 1);
+    const Real scaleE = Bulk<Real>::sun_scale_E(d);
+    // The weighted phases depend on (j, direction) only.  When the n3 headings
+    // of one j fill aligned lane groups of at least DB lanes, lane p of a group
+    // evaluates them for direction p of a block of DB and the group exchanges
+    // them by shuffles.
+    const int G = d.n3;
+    const bool share = G >= DB && (32 % G == 0) && (blockDim.x % G == 0);
+    const int lane = threadIdx.x & 31;
+    const int gbase = share ? (lane & ~(G - 1)) : lane;
+    const int gpos = lane - gbase;
+    const int row_len = RS * rlen;
+    const R2 lx2 = mk2(g.lx, g.lx), ly2 = mk2(g.ly, g.ly), lz2 = mk2(g.lz, g.lz);
+    const R2 sv2 = mk2(sv, sv), cv2 = mk2(cv, cv), sc3 = mk2(scale3, scale3);
 
-  // compensated totals (x: Rayleigh, y: Mie) per channel, and the plain
-  // partial sums of the current directions (x: even, y: odd direction)
-  R2 acc[3], cmp[3], ringR[3], ringM[3];
-#pragma unroll
-  for (int c = 0; c < 3; c++) acc[c] = cmp[c] = ringR[c] = ringM[c] = mk2(Real(0), Real(0));
-  // One block of DB directions starting at w0 (all sky or all ground), two
-  // directions per step.
-  auto dir_block = [&](int w0, auto ground) {
-    Real wRb = 0, wMb = 0;
-    if (share && gpos < DB) {
-      const int wb = w0 + gpos;
-      const Real mu_v = fma(sv, dirs[wb], cv * dirs[used + wb]);
-      wRb = dirs[3 * used + wb] * phR(mu_v);
-      wMb = dirs[3 * used + wb] * phM(mu_v);
-    }
-#pragma unroll
-    for (int q = 0; q < DB; q += 2) {
-      const int wa = w0 + q;
-      const R2 X0 = ld2(dirs + wa), X1 = ld2(dirs + used + wa), X2 = ld2(dirs + 2 * used + wa);
-      R2 wR, wM;
-      if (share) {
-        wR = mk2(__shfl_sync(0xffffffffu, wRb, gbase + q), __shfl_sync(0xffffffffu, wRb, gbase + q + 1));
-        wM = mk2(__shfl_sync(0xffffffffu, wMb, gbase + q), __shfl_sync(0xffffffffu, wMb, gbase + q + 1));
-      } else {
-        const R2 wt = ld2(dirs + 3 * used + wa);
-        const R2 mu_v = fma2(sv2, X0, mul2(cv2, X1));
-        wR = mul2(wt, phR.pair(mu_v));
-        wM = mul2(wt, phM.pair(mu_v));
+    // compensated totals (x: Rayleigh, y: Mie) per channel, and the plain
+    // partial sums of the current directions (x: even, y: odd direction)
+    R2 acc[3], cmp[3], ringR[3], ringM[3];
+  #pragma unroll
+    for (int c = 0; c < 3; c++) acc[c] = cmp[c] = ringR[c] = ringM[c] = mk2(Real(0), Real(0));
+    // One block of DB directions starting at w0 (all sky or all ground), two
+    // directions per step.
+    auto dir_block = [&](int w0, auto ground) {
+      Real wRb = 0, wMb = 0;
+      if (share && gpos < DB) {
+        const int wb = w0 + gpos;
+        const Real mu_v = fma(sv, dirs[wb], cv * dirs[used + wb]);
+        wRb = dirs[3 * used + wb] * phR(mu_v);
+        wMb = dirs[3 * used + wb] * phM(mu_v);
       }
-      const R2 mu_l = fma2(X0, lx2, fma2(X1, ly2, mul2(X2, lz2)));
-      // sun-angle coordinates of (omega, l) along the two directions' heading rows
-      const R2 c3 = fma2(sc3, mu_l, sc3);
-      // |mu| <= 1 up to rounding, so floor(c) lies in [-1, n3 - 1]: texels u
-      // and u + 1 of the padded row give the clamped interpolation exactly
-      // (at u = -1 both are texel 0, at u = n3 - 1 the weight s of the copy
-      // is rounding-small and both are texel n3 - 1)
-      const Real fa = floor(c3.x), fb = floor(c3.y);
-      const int ua = (int)fa, ub = (int)fb;
-      const R2 s3 = sub2(c3, mk2(fa, fb));
-      const Real* ra = rows + wa * row_len + 3 * (ua + 1);
-      const Real* rb = rows + (wa + 1) * row_len + 3 * (ub + 1);
-      R2 X[3];
-#pragma unroll
-      for (int c = 0; c < 3; c++) {
-        const R2 lo = mk2(ra[c], rb[c]), hi = mk2(ra[3 + c], rb[3 + c]);
-        X[c] = fma2(sub2(hi, lo), s3, lo);
-      }
-      if (FIRST) {
-        const R2 ph = phM.pair(mu_l);
-        const Real* ma = rowsM + wa * row_len + 3 * (ua + 1);
-        const Real* mb = rowsM + (wa + 1) * row_len + 3 * (ub + 1);
-#pragma unroll
+  #pragma unroll
+      for (int q = 0; q < DB; q += 2) {
+        const int wa = w0 + q;
+        const R2 X0 = ld2(dirs + wa), X1 = ld2(dirs + used + wa), X2 = ld2(dirs + 2 * used + wa);
+        R2 wR, wM;
+        if (share) {
+          wR = mk2(__shfl_sync(0xffffffffu, wRb, gbase + q), __shfl_sync(0xffffffffu, wRb, gbase + q + 1));
+          wM = mk2(__shfl_sync(0xffffffffu, wMb, gbase + q), __shfl_sync(0xffffffffu, wMb, gbase + q + 1));
+        } else {
+          const R2 wt = ld2(dirs + 3 * used + wa);
+          const R2 mu_v = fma2(sv2, X0, mul2(cv2, X1));
+          wR = mul2(wt, phR.pair(mu_v));
+          wM = mul2(wt, phM.pair(mu_v));
+        }
+        const R2 mu_l = fma2(X0, lx2, fma2(X1, ly2, mul2(X2, lz2)));
+        // sun-angle coordinates of (omega, l) along the two directions' heading rows
+        const R2 c3 = fma2(sc3, mu_l, sc3);
+        // |mu| <= 1 up to rounding, so floor(c) lies in [-1, n3 - 1]: texels u
+        // and u + 1 of the padded row give the clamped interpolation exactly
+        // (at u = -1 both are texel 0, at u = n3 - 1 the weight s of the copy
+        // is rounding-small and both are texel n3 - 1)
+        const Real fa = floor(c3.x), fb = floor(c3.y);
+        const int ua = (int)fa, ub = (int)fb;
+        const R2 s3 = sub2(c3, mk2(fa, fb));
+        const Real* ra = rows + wa * row_len + 3 * (ua + 1);
+        const Real* rb = rows + (wa + 1) * row_len + 3 * (ub + 1);
+        R2 X[3];
+  #pragma unroll
         for (int c = 0; c < 3; c++) {
-          const R2 lo = mk2(ma[c], mb[c]), hi = mk2(ma[3 + c], mb[3 + c]);
-          X[c] = fma2(fma2(sub2(hi, lo), s3, lo), ph, X[c]);
+          const R2 lo = mk2(ra[c], rb[c]), hi = mk2(ra[3 + c], rb[3 + c]);
+          X[c] = fma2(sub2(hi, lo), s3, lo);
+        }
+        if (FIRST) {
+          const R2 ph = phM.pair(mu_l);
+          const Real* ma = rowsM + wa * row_len + 3 * (ua + 1);
+          const Real* mb = rowsM + (wa + 1) * row_len + 3 * (ub + 1);
+  #pragma unroll
+          for (int c = 0; c < 3; c++) {
+            const R2 lo = mk2(ma[c], mb[c]), hi = mk2(ma[3 + c], mb[3 + c]);
+            X[c] = fma2(fma2(sub2(hi, lo), s3, lo), ph, X[c]);
+          }
+        }
+        if (decltype(ground)::value) {
+          const R2 G0 = ld2(dirs + 4 * used + wa), G1 = ld2(dirs + 5 * used + wa), G2 = ld2(dirs + 6 * used + wa);
+          const R2 sg = fma2(G0, lx2, fma2(G1, ly2, mul2(G2, lz2)));
+          int ea, eb;
+          Real ta, tb;
+          split_coord_r<Real>(sun_elevation_index_r<Real>(sg.x, scaleE), d.nE1, &ea, &ta);
+          split_coord_r<Real>(sun_elevation_index_r<Real>(sg.y, scaleE), d.nE1, &eb, &tb);
+          const int fa = upper_index(ea, d.nE1), fb = upper_index(eb, d.nE1);
+          const int ha = uE0s[wa], hb = uE0s[wa + 1];
+          const int ka = upper_index(ha, d.nE0), kb = upper_index(hb, d.nE0);
+          const R2 sE1 = mk2(ta, tb), sE0 = ld2(dirs + 10 * used + wa);
+          const R2 one = mk2(Real(1), Real(1));
+          const R2 oi = sub2(one, sE1);
+          const Real* e0a = etab + 3 * ha * d.nE1;
+          const Real* e0b = etab + 3 * hb * d.nE1;
+          if (sE0.x == Real(0) && sE0.y == Real(0)) {
+            // the vE0 row has weight 0: mix4 reduces to its uE0 row exactly
+            // (the same for every lane: both directions are the warp's)
+  #pragma unroll
+            for (int c = 0; c < 3; c++) {
+              const R2 Y = fma2(mk2(e0a[3 * fa + c], e0b[3 * fb + c]), sE1, mul2(mk2(e0a[3 * ea + c], e0b[3 * eb + c]), oi));
+              X[c] = fma2(ld2(dirs + (7 + c) * used + wa), Y, X[c]);
+            }
+          } else {
+            const R2 oo = sub2(one, sE0);
+            const Real* e1a = etab + 3 * ka * d.nE1;
+            const Real* e1b = etab + 3 * kb * d.nE1;
+  #pragma unroll
+            for (int c = 0; c < 3; c++) {
+              // mix4: height rows (uE0, vE0), sun-elevation columns (uE1, vE1)
+              const R2 lo =
+                  fma2(mk2(e0a[3 * fa + c], e0b[3 * fb + c]), sE1, mul2(mk2(e0a[3 * ea + c], e0b[3 * eb + c]), oi));
+              const R2 hi =
+                  fma2(mk2(e1a[3 * fa + c], e1b[3 * fb + c]), sE1, mul2(mk2(e1a[3 * ea + c], e1b[3 * eb + c]), oi));
+              const R2 Y = fma2(hi, sE0, mul2(lo, oo));
+              X[c] = fma2(ld2(dirs + (7 + c) * used + wa), Y, X[c]);
+            }
+          }
+        }
+  #pragma unroll
+        for (int c = 0; c < 3; c++) {
+          ringR[c] = fma2(wR, X[c], ringR[c]);
+          ringM[c] = fma2(wM, X[c], ringM[c]);
         }
       }
-      if (decltype(ground)::value) {
-        const R2 G0 = ld2(dirs + 4 * used + wa), G1 = ld2(dirs + 5 * used + wa), G2 = ld2(dirs + 6 * used + wa);
-        const R2 sg = fma2(G0, lx2, fma2(G1, ly2, mul2(G2, lz2)));
-        int ea, eb;
-        Real ta, tb;
-        split_coord_r<Real>(sun_elevation_index_r<Real>(sg.x, scaleE), d.nE1, &ea, &ta);
-        split_coord_r<Real>(sun_elevation_index_r<Real>(sg.y, scaleE), d.nE1, &eb, &tb);
-        const int fa = upper_index(ea, d.nE1), fb = upper_index(eb, d.nE1);
-        const int ha = uE0s[wa], hb = uE0s[wa + 1];
-        const int ka = upper_index(ha, d.nE0), kb = upper_index(hb, d.nE0);
-        const R2 sE1 = mk2(ta, tb), sE0 = ld2(dirs + 10 * used + wa);
-        const R2 one = mk2(Real(1), Real(1));
-        const R2 oi = sub2(one, sE1), oo = sub2(one, sE0);
-        const Real* e0a = etab + 3 * ha * d.nE1;
-        const Real* e1a = etab + 3 * ka * d.nE1;
-        const Real* e0b = etab + 3 * hb * d.nE1;
-        const Real* e1b = etab + 3 * kb * d.nE1;
-#pragma unroll
-        for (int c = 0; c < 3; c++) {
-          // mix4: height rows (uE0, vE0), sun-elevation columns (uE1, vE1)
-          const R2 lo = fma2(mk2(e0a[3 * fa + c], e0b[3 * fb + c]), sE1, mul2(mk2(e0a[3 * ea + c], e0b[3 * eb + c]), oi));
-          const R2 hi = fma2(mk2(e1a[3 * fa + c], e1b[3 * fb + c]), sE1, mul2(mk2(e1a[3 * ea + c], e1b[3 * eb + c]), oi));
-          const R2 Y = fma2(hi, sE0, mul2(lo, oo));
-          X[c] = fma2(ld2(dirs + (7 + c) * used + wa), Y, X[c]);
-        }
-      }
-#pragma unroll
+    };
+    // the partial sums of up to two blocks go to the compensated totals
+    auto flush = [&]() {
+  #pragma unroll
       for (int c = 0; c < 3; c++) {
-        ringR[c] = fma2(wR, X[c], ringR[c]);
-        ringM[c] = fma2(wM, X[c], ringM[c]);
+        const R2 x = mk2(ringR[c].x + ringR[c].y, ringM[c].x + ringM[c].y);
+        const R2 y = sub2(x, cmp[c]);
+        const R2 t = add2(acc[c], y);
+        cmp[c] = sub2(sub2(t, acc[c]), y);
+        acc[c] = t;
+        ringR[c] = ringM[c] = mk2(Real(0), Real(0));
       }
+    };
+    for (int w0 = 0; w0 < sky_end; w0 += DB) {
+      dir_block(w0, std::false_type{});
+      if (w0 & DB) flush();
     }
-  };
-  // the partial sums of up to two blocks go to the compensated totals
-  auto flush = [&]() {
-#pragma unroll
-    for (int c = 0; c < 3; c++) {
-      const R2 x = mk2(ringR[c].x + ringR[c].y, ringM[c].x + ringM[c].y);
-      const R2 y = sub2(x, cmp[c]);
-      const R2 t = add2(acc[c], y);
-      cmp[c] = sub2(sub2(t, acc[c]), y);
-      acc[c] = t;
-      ringR[c] = ringM[c] = mk2(Real(0), Real(0));
+    flush();
+    for (int w0 = sky_end; w0 < used; w0 += DB) {
+      dir_block(w0, std::true_type{});
+      if ((w0 - sky_end) & DB) flush();
     }
-  };
-  for (int w0 = 0; w0 < sky_end; w0 += DB) {
-    dir_block(w0, std::false_type{});
-    if (w0 & DB) flush();
+    flush();
+    if (valid) {
+      // beta_c(x) (atmosphere.clj:42-47, 140-151)
+      const PointRow<Real> pr = *prk;
+      Vec4<Real> o;
+      o.x = pr.bR[0] * acc[0].x + pr.bM[0] * acc[0].y;
+      o.y = pr.bR[1] * acc[1].x + pr.bM[1] * acc[1].y;
+      o.z = pr.bR[2] * acc[2].x + pr.bM[2] * acc[2].y;
+      // J planar, [atmosphere][channel][node], for the ray-scatter gathers
+      Real* Jb = J + (long long)b * 3 * d.n4() + (node - base4);
+      Jb[0] = o.x;
+      Jb[d.n4()] = o.y;
+      Jb[2 * d.n4()] = o.z;
+    }
   }
-  flush();
-  for (int w0 = sky_end; w0 < used; w0 += DB) {
-    dir_block(w0, std::true_type{});
-    if ((w0 - sky_end) & DB) flush();
-  }
-  flush();
-  if (!valid) return;
-  // beta_c(x) (atmosphere.clj:42-47, 140-151)
-  const PointRow<Real> pr = *prk;
-  Vec4<Real> o;
-  o.x = pr.bR[0] * acc[0].x + pr.bM[0] * acc[0].y;
-  o.y = pr.bR[1] * acc[1].x + pr.bM[1] * acc[1].y;
-  o.z = pr.bR[2] * acc[2].x + pr.bM[2] * acc[2].y;
-  // J planar, [atmosphere][channel][node], for the ray-scatter gathers
-  Real* Jb = J + (long long)b * 3 * d.n4() + (node - base4);
-  Jb[0] = o.x;
-  Jb[d.n4()] = o.y;
-  Jb[2 * d.n4()] = o.z;
 }
 
 template <class Real>
@@ -327,21 +347,25 @@ int launch_point_scatter(const AtmoParams* params, const BuildDims& d, const Row
                          const Vec4<Real>* dE, Real* J, cudaStream_t st) {
   const int block = 256;
   const int nchunks = (d.n1 * d.n3 + block - 1) / block;
+  // two chunks per block halve the row gathers; one when that would leave
+  // fewer blocks than about eight waves of three per SM
+  const int cpb = (long long)d.n0 * d.n2 * ((nchunks + 1) / 2) * d.B >= 8 * 3 * 152 ? 2 : 1;
+  const int nblk = (nchunks + cpb - 1) / cpb;
   const bool first = mie != nullptr;
   size_t smem = point_scatter_smem<Real>(d, first);
-  dim3 grid((unsigned)(d.n0 * d.n2 * nchunks), d.B);
+  dim3 grid((unsigned)(d.n0 * d.n2 * nblk), d.B);
   if (first) {
     if (cudaFuncSetAttribute(k_point_scatter<Real, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
         cudaSuccess)
       return -1;
     k_point_scatter<Real, true><<<grid, block, smem, st>>>(params, d, rowinfo, pdirs, pcount, prow, geom, dS, mie,
-                                                           dE, J, nchunks);
+                                                           dE, J, nchunks, cpb);
   } else {
     if (cudaFuncSetAttribute(k_point_scatter<Real, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)smem) != cudaSuccess)
       return -1;
     k_point_scatter<Real, false><<<grid, block, smem, st>>>(params, d, rowinfo, pdirs, pcount, prow, geom, dS,
-                                                            mie, dE, J, nchunks);
+                                                            mie, dE, J, nchunks, cpb);
   }
   return 0;
 }

@@ -279,7 +279,8 @@ __global__ void k_sphere_setup(const AtmoParams* params, BuildDims d, const DirL
 }
 
 // The sphere directions of one height row split into those that end in the
-// sky and those that end on the ground, order kept within each part, and
+// sky and those that end on the ground (the latter with an exactly-zero
+// ground height coordinate first), order kept within each part, and
 // each part filled to a multiple of kDirBlock with zero-weight entries, so
 // that point scatter runs both parts in whole blocks of directions without
 // a branch per direction.  One warp per row.
@@ -290,27 +291,37 @@ __global__ void k_sphere_partition(BuildDims d, const SphereDir<Real>* sdirs, Sp
   const long long row = (long long)b * d.n0 + i;
   const SphereDir<Real>* src = sdirs + row * d.P;
   SphereDir<Real>* dst = pdirs + row * dir_row(d.P);
-  int nsky = 0;
+  // three groups, order kept within each: sky, ground with the ground
+  // point's height coordinate exactly 0 (most of them: only its lower E row
+  // has weight), other ground
+  int nsky = 0, nflat = 0;
   for (int t0 = 0; t0 < d.P; t0 += 32) {
     const int t = t0 + lane;
-    nsky += __popc(__ballot_sync(0xffffffffu, t < d.P && !src[t].surface));
+    const bool in = t < d.P;
+    nsky += __popc(__ballot_sync(0xffffffffu, in && !src[t].surface));
+    nflat += __popc(__ballot_sync(0xffffffffu, in && src[t].surface && src[t].sE0 == Real(0)));
   }
   const int sky_end = (nsky + kDirBlock - 1) / kDirBlock * kDirBlock;
   const int nground = d.P - nsky;
   const int used = sky_end + (nground + kDirBlock - 1) / kDirBlock * kDirBlock;
   const unsigned below = (1u << lane) - 1u;
-  int s = 0, g = 0;
+  int s = 0, f = 0, g = 0;
   for (int t0 = 0; t0 < d.P; t0 += 32) {
     const int t = t0 + lane;
     const bool in = t < d.P;
     const bool sky = in && !src[t].surface;
-    const unsigned bs = __ballot_sync(0xffffffffu, sky), bg = __ballot_sync(0xffffffffu, in && !sky);
+    const bool flat = in && !sky && src[t].sE0 == Real(0);
+    const unsigned bs = __ballot_sync(0xffffffffu, sky), bf = __ballot_sync(0xffffffffu, flat);
+    const unsigned bg = __ballot_sync(0xffffffffu, in && !sky && !flat);
     if (in) {
       SphereDir<Real> e = src[t];
       e.pad = 0;
-      dst[sky ? s + __popc(bs & below) : sky_end + g + __popc(bg & below)] = e;
+      const int pos = sky ? s + __popc(bs & below)
+                          : (flat ? sky_end + f + __popc(bf & below) : sky_end + nflat + g + __popc(bg & below));
+      dst[pos] = e;
     }
     s += __popc(bs);
+    f += __popc(bf);
     g += __popc(bg);
   }
   SphereDir<Real> z;

@@ -53,6 +53,25 @@ def test_small_build_matches_oracle(small_oracle, precision):
         assert_close(gpu[key], small_oracle[key], tol, key)
 
 
+@pytest.mark.parametrize("precision", [C.FP64, C.FP32])
+def test_odd_shapes_match_oracle(precision):
+    """Odd table sizes: 5 headings (each lane evaluates its own phases, and
+    3 * n3 is odd), odd elevation and sun-elevation counts, an odd ray-step
+    count (a ray-scatter chunk ends on an unpaired sample) and 13 sphere
+    steps (41 directions: the sky and ground parts end in padded blocks)."""
+    cfg = C.make_config(height=100000.0, transmittance_shape=(9, 17), surface_radiance_shape=(5, 11),
+                        ray_scatter_shape=(5, 9, 7, 5), ray_steps=21, sphere_steps=13, iterations=2,
+                        precision=precision)
+    ref = O.build(cfg, intermediates=True)
+    gpu = A.build(cfg, intermediates=True)
+    tol = TOL[precision]
+    for it in range(cfg.iterations):
+        assert_close(gpu["point_scatter"][it], ref["point_scatter"][it], tol, f"point_scatter[{it}]")
+        assert_close(gpu["ray_scatter_delta"][it], ref["ray_scatter_delta"][it], tol, f"ray_scatter_delta[{it}]")
+    for key in ("transmittance", "surface_radiance", "ray_scatter", "mie_strength"):
+        assert_close(gpu[key], ref[key], tol, key)
+
+
 def test_zero_iterations_and_shader_tables():
     """iterations = 0 (E stays 0) at the reference shader-test shapes (12^4, 10 steps)."""
     cfg = C.shader_test()
