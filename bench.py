@@ -230,14 +230,15 @@ def run_ours(args):
 
     # --- rooflines: point scatter (the largest stage, shared-memory gathers)
     # and the first order (SFU exponentials)
-    counts = (ctypes.c_ulonglong * 9)()
-    _lib.check(L.sfsim_atmo_census(ctypes.byref(cfg), counts, 9), "census")
+    counts = (ctypes.c_ulonglong * 10)()
+    _lib.check(L.sfsim_atmo_census(ctypes.byref(cfg), counts, 10), "census")
     lit, climb = counts[0], counts[6]
-    dir_evals, ground_evals, first_evals = counts[3], counts[7], counts[8]
+    dir_evals, ground_evals, first_evals, flat_evals = counts[3], counts[7], counts[8], counts[9]
     # per direction: the dS heading-row interpolation, 2 corners x RGB float
     # (24 B); the first iteration's Mie row another 24 B; a ground direction's
-    # 4-corner dE gather 48 B
-    ps_bytes = 24 * dir_evals + 24 * first_evals + 48 * ground_evals
+    # dE gather 48 B (4 corners), or 24 B when its lower height row alone has
+    # weight
+    ps_bytes = 24 * dir_evals + 24 * first_evals + 48 * (ground_evals - flat_evals) + 24 * flat_evals
     smem_peak = ctypes.c_double()
     _lib.check(L.sfsim_atmo_smem_peak(ctypes.byref(smem_peak)), "smem_peak")
     ps_ms = stages["point_scatter"]
@@ -278,7 +279,8 @@ def run_ours(args):
                          "traffic": None,
                          "note": ("achieved = algorithmic shared-memory gather bytes of the point-scatter stage "
                                   "(24 B per direction evaluation for the dS row, 24 B more in the first "
-                                  "iteration, 48 B per ground direction; census counts) / its event time; peak = "
+                                  "iteration, 48 B per ground direction, 24 B when one dE height row has all the "
+                                  "weight; census counts) / its event time; peak = "
                                   "conflict-free shared-memory read bandwidth measured live on this GPU by "
                                   "sfsim_atmo_smem_peak (no such figure in MEASURED_PEAKS.json); DRAM is not "
                                   "the bound (the tables live in L2)"),

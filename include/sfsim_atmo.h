@@ -279,7 +279,9 @@ int sfsim_atmo_gemm_bf16(const void* A, const void* B, float* C, int M, int N, l
  * of [0] whose sun ray climbs (FP32 builds read those optical depths from a
  * table instead of integrating them), [7] = the point-scatter direction
  * evaluations of [3] that end on the ground, [8] = those of the first
- * iteration (which also reads the Mie strength).  Returns the number of
+ * iteration (which also reads the Mie strength), [9] = those of [7] whose
+ * ground point has height coordinate exactly 0 in the surface-radiance
+ * table (their dE lookup reads one height row).  Returns the number of
  * counts written (at most n). */
 int sfsim_atmo_census(const sfsim_atmo_config* cfg, unsigned long long* counts, int n);
 

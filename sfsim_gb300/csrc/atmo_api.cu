@@ -689,21 +689,26 @@ int census_impl(const sfsim_atmo_config& cfg, unsigned long long* out, int n) {
   // ground directions of the point-scatter sphere per height
   std::vector<SphereDir<Real>> sd((size_t)d.n0 * (d.P + 1));
   CUDA_TRY(cudaMemcpy(sd.data(), w.setup.sdirs, sizeof(SphereDir<Real>) * sd.size(), cudaMemcpyDeviceToHost));
-  unsigned long long ground = 0;
+  unsigned long long ground = 0, flat = 0;
   for (int i = 0; i < d.n0; i++)
-    for (int k = 0; k < d.P; k++) ground += sd[(size_t)i * d.P + k].surface ? 1 : 0;
+    for (int k = 0; k < d.P; k++) {
+      const SphereDir<Real>& e = sd[(size_t)i * d.P + k];
+      ground += e.surface ? 1 : 0;
+      flat += (e.surface && e.sE0 == Real(0)) ? 1 : 0;
+    }
   const unsigned long long S = (unsigned long long)d.S, it = (unsigned long long)d.iterations;
   const unsigned long long per_height = (unsigned long long)d.n1 * d.n2 * d.n3;
-  const unsigned long long vals[9] = {lit,
-                                      lit * S,
-                                      (unsigned long long)d.rows() * S * S,
-                                      (unsigned long long)d.n4() * d.P * it,
-                                      (unsigned long long)d.n4() * S * it,
-                                      (unsigned long long)d.nE() * d.Ph * it,
-                                      climb,
-                                      ground * per_height * it,
-                                      it > 0 ? (unsigned long long)d.n4() * d.P : 0ull};
-  int m = n < 9 ? n : 9;
+  const unsigned long long vals[10] = {lit,
+                                       lit * S,
+                                       (unsigned long long)d.rows() * S * S,
+                                       (unsigned long long)d.n4() * d.P * it,
+                                       (unsigned long long)d.n4() * S * it,
+                                       (unsigned long long)d.nE() * d.Ph * it,
+                                       climb,
+                                       ground * per_height * it,
+                                       it > 0 ? (unsigned long long)d.n4() * d.P : 0ull,
+                                       flat * per_height * it};
+  int m = n < 10 ? n : 10;
   for (int i = 0; i < m; i++) out[i] = vals[i];
   return m;
 }
