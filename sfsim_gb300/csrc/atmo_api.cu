@@ -343,6 +343,7 @@ struct Work {
   Vec4<Real>*T, *E0, *dE[2], *Eacc[2];
   Vec4<Real>*S1R, *M, *dS[2], *Sacc[2];
   Real* J;
+  Real* hrows;  // point scatter's heading rows per (height, sun elevation)
   float *oT, *oE, *oS, *oM;  // device outputs when the caller passes host buffers
   float2* sun;               // sun-ray optical-depth tables (FP32 builds), or NULL
 };
@@ -377,6 +378,7 @@ size_t carve(Work<Real>& w, char* base, const BuildDims& d, bool outputs, bool s
   w.S1R = c.take<Vec4<Real>>(B * d.n4());
   w.M = c.take<Vec4<Real>>(B * d.n4());
   w.J = c.take<Real>(3 * B * d.n4());  // planar [atmosphere][channel][node]
+  w.hrows = c.take<Real>(B * d.n0 * d.n2 * heading_rows_stride(d));
   for (int i = 0; i < 2; i++) {
     w.dS[i] = c.take<Vec4<Real>>(B * d.n4());
     w.Sacc[i] = c.take<Vec4<Real>>(B * d.n4());
@@ -491,9 +493,9 @@ int run_build(const Work<Real>& w, const BuildDims& d, float* oT, float* oE, flo
     Vec4<Real>* S_new = w.Sacc[it & 1];
     tm.mark_begin(5);
     if (launch_point_scatter<Real>(w.params, d, w.setup.rowinfo, w.setup.pdirs, w.setup.pcount, w.setup.prow,
-                                   w.setup.geom, dS_prev, M_first, dE_prev, w.J, st))
+                                   w.setup.geom, dS_prev, M_first, dE_prev, w.hrows, w.J, st))
       return fail(SFSIM_ATMO_ECUDA, "point scatter launch configuration failed");
-    launches++;
+    launches += 2;
     tm.mark_end();
     if (jsum) {
       launch_add_to_sum<Real>(d.n4(), d.B, w.J, jsum, it == 0, st);

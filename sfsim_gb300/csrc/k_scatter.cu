@@ -64,6 +64,60 @@ struct TexelRow {
   }
 };
 
+// The heading rows of one (height i, sun elevation k) pair: for each of the
+// `used` partitioned directions, dS (and in the first iteration the Mie
+// strength) gathered along the heading axis at the pair's height and
+// sun-elevation coordinates and the direction's elevation coordinate, n3
+// texels between copies of the first and last (rows, then rowsM).
+template <class Real, bool FIRST>
+__device__ __forceinline__ void heading_rows(const BuildDims& d, const SphereDir<Real>* src, int used,
+                                             const Vec4<Real>* dS, const Vec4<Real>* Mt, const PointRow<Real>& pk,
+                                             Real* rows, int t0, int nt) {
+  using TR = TexelRow<Real>;
+  const int rlen = d.n3 + 2;
+  Real* rowsM = rows + TR::kStride * used * rlen;
+  const int u0 = pk.u0, u2 = pk.u2;
+  const Real s0 = pk.s0, s2 = pk.s2;
+  const int v0 = upper_index(u0, d.n0), v2 = upper_index(u2, d.n2);
+  for (int t = t0; t < used * d.n3; t += nt) {
+    const int w = t / d.n3, a = t - w * d.n3;
+    Real v[3] = {0, 0, 0}, vm[3] = {0, 0, 0};
+    if (!src[w].pad) {
+      const int u1 = src[w].u1, v1 = upper_index(u1, d.n1);
+      const Real s1 = src[w].s1;
+      gather_heading_row(dS, d, u0, v0, s0, u1, v1, s1, u2, v2, s2, a, v);
+      if (FIRST) gather_heading_row(Mt, d, u0, v0, s0, u1, v1, s1, u2, v2, s2, a, vm);
+    }
+    const int o = w * rlen + 1 + a;
+    TR::store(rows, o, v);
+    if (FIRST) TR::store(rowsM, o, vm);
+    if (a == 0) {
+      TR::store(rows, o - 1, v);
+      if (FIRST) TR::store(rowsM, o - 1, vm);
+    }
+    if (a == d.n3 - 1) {
+      TR::store(rows, o + 1, v);
+      if (FIRST) TR::store(rowsM, o + 1, vm);
+    }
+  }
+}
+
+// The rows of every (i, k) pair into the global row table, once per
+// iteration, so that the point-scatter blocks of a pair copy them instead
+// of each gathering them.
+template <class Real, bool FIRST>
+__global__ void __launch_bounds__(256) k_heading_rows(BuildDims d, const SphereDir<Real>* pdirs, const int2* pcount,
+                                                      const PointRow<Real>* prow, const Vec4<Real>* dS,
+                                                      const Vec4<Real>* Mt, Real* hrows) {
+  const int b = blockIdx.y;
+  const int i = blockIdx.x / d.n2, k = blockIdx.x % d.n2;
+  const long long pair = ((long long)b * d.n0 + i) * d.n2 + k;
+  const SphereDir<Real>* src = pdirs + ((long long)b * d.n0 + i) * dir_row(d.P);
+  const long long base4 = (long long)b * d.n4();
+  heading_rows<Real, FIRST>(d, src, pcount[(long long)b * d.n0 + i].y, dS + base4, FIRST ? Mt + base4 : nullptr,
+                            prow[pair], hrows + pair * heading_rows_stride(d), threadIdx.x, blockDim.x);
+}
+
 // Shared-memory layout of point scatter for one (height i, sun elevation k)
 // pair, `used` directions (a multiple of kDirBlock):
 //   dirs  [kDirFields][used] Real: x0, x1, x2, weight, gdir0..2, ground0..2,
@@ -81,6 +135,12 @@ __device__ __forceinline__ V2<Real> ld2(const Real* p) {
   return *reinterpret_cast<const V2<Real>*>(p);
 }
 
+// Blocks per (height, sun elevation) pair when each evaluates `cpb` of the
+// pair's `nchunks` chunks of 256 nodes; the launch and the kernel share it.
+__host__ __device__ __forceinline__ int point_scatter_blocks_per_pair(int nchunks, int cpb) {
+  return (nchunks + cpb - 1) / cpb;
+}
+
 // Three FP32 blocks of 256 share an SM (80 registers a thread); FP64 blocks
 // are register-bound anyway.
 constexpr int point_scatter_min_blocks(size_t real_size) { return real_size == 4 ? 3 : 1; }
@@ -90,9 +150,8 @@ __global__ void __launch_bounds__(256, point_scatter_min_blocks(sizeof(Real))) k
                                                           const RowInfo* rowinfo, const SphereDir<Real>* pdirs,
                                                           const int2* pcount, const PointRow<Real>* prow,
                                                           const CellGeom<Real>* geom,
-                                                          const Vec4<Real>* dS, const Vec4<Real>* Mt,
-                                                          const Vec4<Real>* dE, Real* J, int nchunks,
-                                                          int chunks_per_block) {
+                                                          const Real* hrows, const Vec4<Real>* dE, Real* J,
+                                                          int nchunks, int chunks_per_block) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   using TR = TexelRow<Real>;
   using R2 = V2<Real>;
@@ -101,15 +160,15 @@ __global__ void __launch_bounds__(256, point_scatter_min_blocks(sizeof(Real))) k
   const int b = blockIdx.y;
   // one (height i, sun elevation k) pair, chunks_per_block chunks of 256 of
   // its (elevation, heading) nodes: the rows are gathered once for them all
-  const int nblk = (nchunks + chunks_per_block - 1) / chunks_per_block;
+  const int nblk = point_scatter_blocks_per_pair(nchunks, chunks_per_block);
   const int chunk0 = (blockIdx.x % nblk) * chunks_per_block;
   const int ik = blockIdx.x / nblk;
+  if (ik >= d.n0 * d.n2) return;  // the grid is n0 * n2 * nblk blocks; nothing beyond
   const int i = ik / d.n2, k = ik % d.n2;
   const AtmoParams& P = params[b];
   const PointRow<Real>* prk = prow + ((long long)b * d.n0 + i) * d.n2 + k;
   const int2 pc = pcount[(long long)b * d.n0 + i];
   const int sky_end = pc.x, used = pc.y;
-  const int nrow = used * d.n3;
   // texels of a heading row: a copy of texel 0, the n3 texels, a copy of
   // texel n3 - 1, so that a sun-angle coordinate that rounding pushed just
   // outside [0, n3 - 1] reads the edge texel without a clamp
@@ -121,11 +180,6 @@ __global__ void __launch_bounds__(256, point_scatter_min_blocks(sizeof(Real))) k
   Real* rowsM = rows + RS * used * rlen;
   Real* etab = rowsM + (FIRST ? RS * used * rlen : 0);
 
-  // the (i, k) coordinates of the dS lookups
-  const int u0 = prk->u0, u2 = prk->u2;
-  const Real s0 = prk->s0, s2 = prk->s2;
-  const int v0 = upper_index(u0, d.n0), v2 = upper_index(u2, d.n2);
-
   const long long base4 = (long long)b * d.n4();
   const SphereDir<Real>* src = pdirs + ((long long)b * d.n0 + i) * dir_row(d.P);
   for (int t = threadIdx.x; t < used; t += blockDim.x) {
@@ -136,26 +190,14 @@ __global__ void __launch_bounds__(256, point_scatter_min_blocks(sizeof(Real))) k
     for (int c = 0; c < kDirFields; c++) dirs[c * used + t] = f[c];
     uE0s[t] = D.uE0;
   }
-  for (int t = threadIdx.x; t < nrow; t += blockDim.x) {
-    const int w = t / d.n3, a = t - w * d.n3;
-    Real v[3] = {0, 0, 0}, vm[3] = {0, 0, 0};
-    if (!src[w].pad) {
-      const int u1 = src[w].u1, v1 = upper_index(u1, d.n1);
-      const Real s1 = src[w].s1;
-      gather_heading_row(dS + base4, d, u0, v0, s0, u1, v1, s1, u2, v2, s2, a, v);
-      if (FIRST) gather_heading_row(Mt + base4, d, u0, v0, s0, u1, v1, s1, u2, v2, s2, a, vm);
-    }
-    const int o = w * rlen + 1 + a;
-    TR::store(rows, o, v);
-    if (FIRST) TR::store(rowsM, o, vm);
-    if (a == 0) {
-      TR::store(rows, o - 1, v);
-      if (FIRST) TR::store(rowsM, o - 1, vm);
-    }
-    if (a == d.n3 - 1) {
-      TR::store(rows, o + 1, v);
-      if (FIRST) TR::store(rowsM, o + 1, vm);
-    }
+  {
+    // the pair's heading rows from the row table (k_heading_rows), 16 bytes
+    // a thread at a time: a multiple of 24 values, both ends 16-byte aligned
+    const int4* hs = reinterpret_cast<const int4*>(hrows + (((long long)b * d.n0 + i) * d.n2 + k) *
+                                                                heading_rows_stride(d));
+    int4* hd = reinterpret_cast<int4*>(rows);
+    const int n16 = (int)((FIRST ? 2 : 1) * (size_t)RS * used * rlen * sizeof(Real) / 16);
+    for (int t = threadIdx.x; t < n16; t += blockDim.x) hd[t] = hs[t];
   }
   const long long nE = d.nE();
   for (int t = threadIdx.x; t < nE; t += blockDim.x) {
@@ -344,28 +386,28 @@ template <class Real>
 int launch_point_scatter(const AtmoParams* params, const BuildDims& d, const RowInfo* rowinfo,
                          const SphereDir<Real>* pdirs, const int2* pcount, const PointRow<Real>* prow,
                          const CellGeom<Real>* geom, const Vec4<Real>* dS, const Vec4<Real>* mie,
-                         const Vec4<Real>* dE, Real* J, cudaStream_t st) {
+                         const Vec4<Real>* dE, Real* hrows, Real* J, cudaStream_t st) {
   const int block = 256;
   const int nchunks = (d.n1 * d.n3 + block - 1) / block;
-  // two chunks per block halve the row gathers; one when that would leave
-  // fewer blocks than about eight waves of three per SM
-  const int cpb = (long long)d.n0 * d.n2 * ((nchunks + 1) / 2) * d.B >= 8 * 3 * 152 ? 2 : 1;
-  const int nblk = (nchunks + cpb - 1) / cpb;
+  const int cpb = 2;
   const bool first = mie != nullptr;
   size_t smem = point_scatter_smem<Real>(d, first);
-  dim3 grid((unsigned)(d.n0 * d.n2 * nblk), d.B);
+  const dim3 rgrid((unsigned)(d.n0 * d.n2), d.B);
+  dim3 grid((unsigned)(d.n0 * d.n2 * point_scatter_blocks_per_pair(nchunks, cpb)), d.B);
   if (first) {
     if (cudaFuncSetAttribute(k_point_scatter<Real, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
         cudaSuccess)
       return -1;
-    k_point_scatter<Real, true><<<grid, block, smem, st>>>(params, d, rowinfo, pdirs, pcount, prow, geom, dS, mie,
-                                                           dE, J, nchunks, cpb);
+    k_heading_rows<Real, true><<<rgrid, block, 0, st>>>(d, pdirs, pcount, prow, dS, mie, hrows);
+    k_point_scatter<Real, true><<<grid, block, smem, st>>>(params, d, rowinfo, pdirs, pcount, prow, geom, hrows, dE,
+                                                           J, nchunks, cpb);
   } else {
     if (cudaFuncSetAttribute(k_point_scatter<Real, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)smem) != cudaSuccess)
       return -1;
-    k_point_scatter<Real, false><<<grid, block, smem, st>>>(params, d, rowinfo, pdirs, pcount, prow, geom, dS,
-                                                            mie, dE, J, nchunks, cpb);
+    k_heading_rows<Real, false><<<rgrid, block, 0, st>>>(d, pdirs, pcount, prow, dS, nullptr, hrows);
+    k_point_scatter<Real, false><<<grid, block, smem, st>>>(params, d, rowinfo, pdirs, pcount, prow, geom, hrows,
+                                                            dE, J, nchunks, cpb);
   }
   return 0;
 }
@@ -808,7 +850,7 @@ void launch_export(long long n, const Vec4<Real>* tab, float* out, cudaStream_t 
   template int launch_point_scatter<Real>(const AtmoParams*, const BuildDims&, const RowInfo*,                     \
                                           const SphereDir<Real>*, const int2*, const PointRow<Real>*,              \
                                           const CellGeom<Real>*, const Vec4<Real>*, const Vec4<Real>*,             \
-                                          const Vec4<Real>*, Real*, cudaStream_t);                                 \
+                                          const Vec4<Real>*, Real*, Real*, cudaStream_t);                          \
   template void launch_surface_radiance<Real>(const AtmoParams*, const BuildDims&, const SurfRow<Real>*,          \
                                               const HalfDir<Real>*, const Vec4<Real>*, const Vec4<Real>*,          \
                                               Vec4<Real>*, cudaStream_t);                                          \

@@ -32,6 +32,13 @@ struct SetupBuffers {
 constexpr int kDirBlock = 8;
 __host__ __device__ constexpr int dir_row(int P) { return P + 2 * kDirBlock; }
 
+// Reals of one (height, sun elevation) pair's heading rows in point
+// scatter's global row table: the dS and Mie rows of every partitioned
+// direction, n3 + 2 RGB texels each; a multiple of 48.
+__host__ __device__ inline long long heading_rows_stride(const BuildDims& d) {
+  return 2LL * ((dir_row(d.P) + 7) / 8 * 8) * (d.n3 + 2) * 3;
+}
+
 template <class Real>
 void launch_setup(const AtmoParams* params, const BuildDims& d, const DirLocal* dirs, const int* ring_end,
                   const DirLocal* half_dirs, const SetupBuffers<Real>& o, cudaStream_t st);
@@ -67,11 +74,12 @@ int launch_smem_probe(int blocks, int iters, float* sink, cudaStream_t st);
 
 // J = point scatter of (dS, dE), planar [atmosphere][channel][node]; when
 // `mie` is non-NULL dS is the first iteration's rayleigh + mie * phase(mie, v.l).
+// hrows: scratch for the heading rows, B * n0 * n2 * heading_rows_stride(d) Reals.
 template <class Real>
 int launch_point_scatter(const AtmoParams* params, const BuildDims& d, const RowInfo* rowinfo,
                          const SphereDir<Real>* pdirs, const int2* pcount, const PointRow<Real>* prow,
                          const CellGeom<Real>* geom, const Vec4<Real>* dS,
-                         const Vec4<Real>* mie, const Vec4<Real>* dE, Real* J, cudaStream_t st);
+                         const Vec4<Real>* mie, const Vec4<Real>* dE, Real* hrows, Real* J, cudaStream_t st);
 
 // dE = surface radiance of dS (same first-iteration convention).
 template <class Real>
