@@ -533,9 +533,9 @@ struct RayChunk {
   int p[4][CH];
 };
 
-// Four FP32 blocks fit in shared memory; the hint keeps ptxas from trading
-// registers for spills below that.
-constexpr int ray_scatter_min_blocks(size_t real_size) { return real_size == 4 ? 4 : 1; }
+// Three FP32 blocks per SM: 80 registers a thread hold the plane build's
+// cached J corners without spills (four blocks at 64 registers spilled).
+constexpr int ray_scatter_min_blocks(size_t real_size) { return real_size == 4 ? 3 : 1; }
 
 template <class Real, int CH>
 __global__ void __launch_bounds__(256, ray_scatter_min_blocks(sizeof(Real)))
@@ -577,6 +577,9 @@ __global__ void __launch_bounds__(256, ray_scatter_min_blocks(sizeof(Real)))
     const R2 b02 = mk2(b0, b0), Dl2 = mk2(Dl, Dl), s32 = mk2(s3, s3);
     // x: even samples, y: odd samples (independent FMA chains)
     R2 acc[3] = {mk2(Real(0), Real(0)), mk2(Real(0), Real(0)), mk2(Real(0), Real(0))};
+    // the plane build's cached J corners of the last even and odd samples
+    Real ca[12], cb[12];
+    int key_a = -1, key_b = -1;
     for (int sb = 0; sb < d.S; sb += CH) {
       const int nch = min(CH, d.S - sb);
       __syncthreads();
@@ -598,6 +601,56 @@ __global__ void __launch_bounds__(256, ray_scatter_min_blocks(sizeof(Real)))
       }
       __syncthreads();
       // the plane of samples (ch, ch + 1): bilinear in (height, elevation)
+      if (ncell <= (int)blockDim.x) {
+        // one cell per thread: its J corner values stay in registers while
+        // consecutive samples share their (height, elevation) corners (the
+        // first corner's offset identifies all four); about half the pairs do
+        if (threadIdx.x < ncell) {
+          const int t = threadIdx.x;
+          for (int ch = 0; ch < nch; ch += 2) {
+            const bool two = ch + 1 < nch;
+            const int ch1 = two ? ch + 1 : ch;
+            const int pa = sc.p[0][ch], pb = sc.p[0][ch1];
+            auto load = [&](int s, Real (&v)[12]) {
+              const int q[4] = {sc.p[0][s], sc.p[1][s], sc.p[2][s], sc.p[3][s]};
+#pragma unroll
+              for (int c = 0; c < 3; c++)
+#pragma unroll
+                for (int m = 0; m < 4; m++) v[4 * c + m] = tJ[c * n4 + t + q[m]];
+            };
+            if (pa != key_a) {
+              if (pa == key_b) {
+#pragma unroll
+                for (int m = 0; m < 12; m++) ca[m] = cb[m];
+              } else {
+                load(ch, ca);
+              }
+              key_a = pa;
+            }
+            if (pb != key_b) {
+              if (pb == key_a) {
+#pragma unroll
+                for (int m = 0; m < 12; m++) cb[m] = ca[m];
+              } else {
+                load(ch1, cb);
+              }
+              key_b = pb;
+            }
+            const R2 s0 = mk2(sc.s0[ch], sc.s0[ch1]), s1 = mk2(sc.s1[ch], sc.s1[ch1]);
+            Real* dst0 = plane + 3 * (ch * ncell + t);
+            Real* dst1 = dst0 + 3 * ncell;
+#pragma unroll
+            for (int c = 0; c < 3; c++) {
+              const R2 A = mk2(ca[4 * c], cb[4 * c]), B = mk2(ca[4 * c + 1], cb[4 * c + 1]);
+              const R2 C = mk2(ca[4 * c + 2], cb[4 * c + 2]), E = mk2(ca[4 * c + 3], cb[4 * c + 3]);
+              const R2 lo = fma2(sub2(B, A), s1, A), hi = fma2(sub2(E, C), s1, C);
+              const R2 v = fma2(sub2(hi, lo), s0, lo);
+              dst0[c] = v.x;
+              if (two) dst1[c] = v.y;
+            }
+          }
+        }
+      } else
       for (int ch = 0; ch < nch; ch += 2) {
         const bool two = ch + 1 < nch;
         const int ch1 = two ? ch + 1 : ch;
