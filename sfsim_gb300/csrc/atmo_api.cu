@@ -97,10 +97,8 @@ bool same_layout(const sfsim_atmo_config& a, const sfsim_atmo_config& b) {
 // Directions of spherical-integral (sphere.clj:62-93): theta rings at
 // midpoints, ceil(sin theta * phi_steps) phi midpoints per ring, weight
 // (cos(theta - d) - cos(theta + d)) * 2 pi / ring steps.
-void sphere_directions(int theta_steps, int phi_steps, double range, std::vector<DirLocal>& out,
-                       std::vector<int>& ring_end) {
+void sphere_directions(int theta_steps, int phi_steps, double range, std::vector<DirLocal>& out) {
   out.clear();
-  ring_end.clear();
   if (theta_steps <= 0) return;
   const double delta2 = range / theta_steps / 2;
   for (int k = 0; k < theta_steps; k++) {
@@ -112,7 +110,6 @@ void sphere_directions(int theta_steps, int phi_steps, double range, std::vector
       const double phi = 2 * M_PI * ((0.5 + i) / ringsteps);
       out.push_back(DirLocal{std::cos(theta), std::sin(theta) * std::cos(phi), std::sin(theta) * std::sin(phi),
                              factor * weight});
-      ring_end.push_back(i == ringsteps - 1);
     }
   }
 }
@@ -286,10 +283,9 @@ BuildDims make_dims(const sfsim_atmo_config& c, int B) {
   d.sphere_steps = c.sphere_steps;
   d.iterations = c.iterations;
   std::vector<DirLocal> v;
-  std::vector<int> e;
-  sphere_directions(c.sphere_steps >> 1, c.sphere_steps, M_PI, v, e);
+  sphere_directions(c.sphere_steps >> 1, c.sphere_steps, M_PI, v);
   d.P = (int)v.size();
-  sphere_directions(c.ray_steps >> 2, c.ray_steps, M_PI / 2, v, e);
+  sphere_directions(c.ray_steps >> 2, c.ray_steps, M_PI / 2, v);
   d.Ph = (int)v.size();
   d.sun_scale = (d.n2 - 1) / (1 - std::exp(-3.6));
   d.sun_scale_E = (d.nE1 - 1) / (1 - std::exp(-3.6));
@@ -337,7 +333,6 @@ template <class Real>
 struct Work {
   AtmoParams* params;
   DirLocal* dirs;
-  int* ring_end;
   DirLocal* hdirs;
   SetupBuffers<Real> setup;
   Vec4<Real>*T, *E0, *dE[2], *Eacc[2];
@@ -354,7 +349,6 @@ size_t carve(Work<Real>& w, char* base, const BuildDims& d, bool outputs, bool s
   const long long B = d.B;
   w.params = c.take<AtmoParams>(B);
   w.dirs = c.take<DirLocal>(d.P + 1);
-  w.ring_end = c.take<int>(d.P + 1);
   w.hdirs = c.take<DirLocal>(d.Ph + 1);
   w.setup.remapS = c.take<Remap4<Real>>(B * d.n4());
   w.setup.geom = c.take<CellGeom<Real>>(B * d.n4());
@@ -365,6 +359,7 @@ size_t carve(Work<Real>& w, char* base, const BuildDims& d, bool outputs, bool s
   w.setup.rows = c.take<RowSample<Real>>(B * d.rows() * d.S);
   w.setup.sdirs = c.take<SphereDir<Real>>(B * d.n0 * (long long)(d.P + 1));
   w.setup.pdirs = c.take<SphereDir<Real>>(B * d.n0 * (long long)dir_row(d.P));
+  w.setup.dimage = c.take<unsigned char>(B * d.n0 * dir_image_stride(d, sizeof(Real)));
   w.setup.pcount = c.take<int2>(B * d.n0);
   w.setup.prow = c.take<PointRow<Real>>(B * d.n0 * d.n2);
   w.setup.erow = c.take<SurfRow<Real>>(B * d.nE());
@@ -454,7 +449,7 @@ int run_build(const Work<Real>& w, const BuildDims& d, float* oT, float* oE, flo
               Timer& tm, const sfsim_atmo_intermediates* inter, Vec4<float>* jsum = nullptr) {
   int launches = 0;
   tm.mark_begin(0);
-  launch_setup<Real>(w.params, d, w.dirs, w.ring_end, w.hdirs, w.setup, st);
+  launch_setup<Real>(w.params, d, w.dirs, w.hdirs, w.setup, st);
   launches += 10;
   tm.mark_end();
   tm.mark_begin(1);
@@ -492,7 +487,8 @@ int run_build(const Work<Real>& w, const BuildDims& d, float* oT, float* oE, flo
     Vec4<Real>* E_new = w.Eacc[it & 1];
     Vec4<Real>* S_new = w.Sacc[it & 1];
     tm.mark_begin(5);
-    if (launch_point_scatter<Real>(w.params, d, w.setup.rowinfo, w.setup.pdirs, w.setup.pcount, w.setup.prow,
+    if (launch_point_scatter<Real>(w.params, d, w.setup.rowinfo, w.setup.pdirs, w.setup.dimage, w.setup.pcount,
+                                   w.setup.prow,
                                    w.setup.geom, dS_prev, M_first, dE_prev, w.hrows, w.J, st))
       return fail(SFSIM_ATMO_ECUDA, "point scatter launch configuration failed");
     launches += 2;
@@ -572,9 +568,8 @@ int build_impl(const sfsim_atmo_config* cfgs, int B, float* T, float* E, float* 
   for (int b = 0; b < B; b++)
     if ((rc = make_params(cfgs[b], hp[b]))) return rc;
   std::vector<DirLocal> dirs, hdirs;
-  std::vector<int> ring_end, hring;
-  sphere_directions(cfgs[0].sphere_steps >> 1, cfgs[0].sphere_steps, M_PI, dirs, ring_end);
-  sphere_directions(cfgs[0].ray_steps >> 2, cfgs[0].ray_steps, M_PI / 2, hdirs, hring);
+  sphere_directions(cfgs[0].sphere_steps >> 1, cfgs[0].sphere_steps, M_PI, dirs);
+  sphere_directions(cfgs[0].ray_steps >> 2, cfgs[0].ray_steps, M_PI / 2, hdirs);
 
   Work<Real> w;
   size_t bytes = carve<Real>(w, nullptr, d, host_out);
@@ -585,7 +580,6 @@ int build_impl(const sfsim_atmo_config* cfgs, int B, float* T, float* E, float* 
   CUDA_TRY(cudaMemcpyAsync(w.params, hp.data(), sizeof(AtmoParams) * B, cudaMemcpyHostToDevice, st));
   if (!dirs.empty()) {
     CUDA_TRY(cudaMemcpyAsync(w.dirs, dirs.data(), sizeof(DirLocal) * dirs.size(), cudaMemcpyHostToDevice, st));
-    CUDA_TRY(cudaMemcpyAsync(w.ring_end, ring_end.data(), sizeof(int) * ring_end.size(), cudaMemcpyHostToDevice, st));
   }
   if (!hdirs.empty())
     CUDA_TRY(cudaMemcpyAsync(w.hdirs, hdirs.data(), sizeof(DirLocal) * hdirs.size(), cudaMemcpyHostToDevice, st));
@@ -667,8 +661,7 @@ int census_impl(const sfsim_atmo_config& cfg, unsigned long long* out, int n) {
   AtmoParams hp;
   if ((rc = make_params(cfg, hp))) return rc;
   std::vector<DirLocal> dirs;
-  std::vector<int> ring_end;
-  sphere_directions(cfg.sphere_steps >> 1, cfg.sphere_steps, M_PI, dirs, ring_end);
+  sphere_directions(cfg.sphere_steps >> 1, cfg.sphere_steps, M_PI, dirs);
   Work<Real> w;
   size_t bytes = carve<Real>(w, nullptr, d, false, false);
   if ((rc = ensure_arena(dev, bytes + 256))) return rc;
@@ -678,10 +671,9 @@ int census_impl(const sfsim_atmo_config& cfg, unsigned long long* out, int n) {
   CUDA_TRY(cudaMemcpyAsync(w.params, &hp, sizeof(AtmoParams), cudaMemcpyHostToDevice, st));
   if (!dirs.empty()) {
     CUDA_TRY(cudaMemcpyAsync(w.dirs, dirs.data(), sizeof(DirLocal) * dirs.size(), cudaMemcpyHostToDevice, st));
-    CUDA_TRY(cudaMemcpyAsync(w.ring_end, ring_end.data(), sizeof(int) * ring_end.size(), cudaMemcpyHostToDevice, st));
   }
   CUDA_TRY(cudaMemsetAsync(dcount, 0, 2 * sizeof(unsigned long long), st));
-  launch_setup<Real>(w.params, d, w.dirs, w.ring_end, w.hdirs, w.setup, st);
+  launch_setup<Real>(w.params, d, w.dirs, w.hdirs, w.setup, st);
   launch_first_order_census<Real>(w.params, d, w.setup.rowinfo, w.setup.rows, w.setup.geom, dcount, st);
   CUDA_TRY(cudaGetLastError());
   unsigned long long cnt[2] = {0, 0};
@@ -942,9 +934,8 @@ int context_build(sfsim_atmo_context* c) {
   AtmoParams hp;
   if ((rc = make_params(cfg, hp))) return rc;
   std::vector<DirLocal> dirs, hdirs;
-  std::vector<int> ring_end, hring;
-  sphere_directions(cfg.sphere_steps >> 1, cfg.sphere_steps, M_PI, dirs, ring_end);
-  sphere_directions(cfg.ray_steps >> 2, cfg.ray_steps, M_PI / 2, hdirs, hring);
+  sphere_directions(cfg.sphere_steps >> 1, cfg.sphere_steps, M_PI, dirs);
+  sphere_directions(cfg.ray_steps >> 2, cfg.ray_steps, M_PI / 2, hdirs);
   Work<Real> w;
   const size_t wbytes = carve<Real>(w, nullptr, d, true);
   const size_t total = wbytes + sizeof(Vec4<float>) * (size_t)d.n4() + 256;
@@ -961,7 +952,6 @@ int context_build(sfsim_atmo_context* c) {
   CUDA_TRY(cudaMemcpyAsync(w.params, &hp, sizeof(AtmoParams), cudaMemcpyHostToDevice, st));
   if (!dirs.empty()) {
     CUDA_TRY(cudaMemcpyAsync(w.dirs, dirs.data(), sizeof(DirLocal) * dirs.size(), cudaMemcpyHostToDevice, st));
-    CUDA_TRY(cudaMemcpyAsync(w.ring_end, ring_end.data(), sizeof(int) * ring_end.size(), cudaMemcpyHostToDevice, st));
   }
   if (!hdirs.empty())
     CUDA_TRY(cudaMemcpyAsync(w.hdirs, hdirs.data(), sizeof(DirLocal) * hdirs.size(), cudaMemcpyHostToDevice, st));
@@ -1309,9 +1299,8 @@ int build_static_impl(const sfsim_atmo_config& cfg, float* T, float* E, float* S
   AtmoParams hp;
   if ((rc = make_params(cfg, hp))) return rc;
   std::vector<DirLocal> dirs, hdirs;
-  std::vector<int> ring_end, hring;
-  sphere_directions(cfg.sphere_steps >> 1, cfg.sphere_steps, M_PI, dirs, ring_end);
-  sphere_directions(cfg.ray_steps >> 2, cfg.ray_steps, M_PI / 2, hdirs, hring);
+  sphere_directions(cfg.sphere_steps >> 1, cfg.sphere_steps, M_PI, dirs);
+  sphere_directions(cfg.ray_steps >> 2, cfg.ray_steps, M_PI / 2, hdirs);
   void* base = nullptr;
   if ((rc = static_scratch_base(dev, &base))) return rc;
   carve<Real>(w, (char*)base, d, false, false);
@@ -1320,7 +1309,6 @@ int build_static_impl(const sfsim_atmo_config& cfg, float* T, float* E, float* S
   CUDA_TRY(cudaMemcpyAsync(w.params, &hp, sizeof(AtmoParams), cudaMemcpyHostToDevice, st));
   if (!dirs.empty()) {
     CUDA_TRY(cudaMemcpyAsync(w.dirs, dirs.data(), sizeof(DirLocal) * dirs.size(), cudaMemcpyHostToDevice, st));
-    CUDA_TRY(cudaMemcpyAsync(w.ring_end, ring_end.data(), sizeof(int) * ring_end.size(), cudaMemcpyHostToDevice, st));
   }
   if (!hdirs.empty())
     CUDA_TRY(cudaMemcpyAsync(w.hdirs, hdirs.data(), sizeof(DirLocal) * hdirs.size(), cudaMemcpyHostToDevice, st));

@@ -181,7 +181,7 @@ struct SphereDir {
   int surface;         // 1: the direction ends on the ground
   int u1;              // elevation coordinate of (x, omega, !surface)
   int uE0;             // height coordinate of the ground point in the surface space
-  int pad;
+  int pad;             // 1: a zero-weight filler of the partitioned lists
   Real s1, sE0;
 };
 

@@ -128,7 +128,6 @@ __global__ void __launch_bounds__(256) k_heading_rows(BuildDims d, const SphereD
 //         copies of its first and last texel (and the Mie rows in the first
 //         iteration);
 //   etab  [nE0][nE1][3] the dE table.
-constexpr int kDirFields = 11;
 
 template <class Real>
 __device__ __forceinline__ V2<Real> ld2(const Real* p) {
@@ -148,7 +147,8 @@ constexpr int point_scatter_min_blocks(size_t real_size) { return real_size == 4
 template <class Real, bool FIRST>
 __global__ void __launch_bounds__(256, point_scatter_min_blocks(sizeof(Real))) k_point_scatter(const AtmoParams* params, BuildDims d,
                                                           const RowInfo* rowinfo, const SphereDir<Real>* pdirs,
-                                                          const int2* pcount, const PointRow<Real>* prow,
+                                                          const unsigned char* dimage, const int2* pcount,
+                                                          const PointRow<Real>* prow,
                                                           const CellGeom<Real>* geom,
                                                           const Real* hrows, const Vec4<Real>* dE, Real* J,
                                                           int nchunks, int chunks_per_block) {
@@ -175,20 +175,18 @@ __global__ void __launch_bounds__(256, point_scatter_min_blocks(sizeof(Real))) k
   const int rlen = d.n3 + 2;
   Real* dirs = reinterpret_cast<Real*>(smem_raw);
   int* uE0s = reinterpret_cast<int*>(dirs + kDirFields * used);
-  const size_t dir_bytes = ((size_t)used * (kDirFields * sizeof(Real) + sizeof(int)) + 15) & ~size_t(15);
+  const size_t dir_bytes = dir_image_bytes(used, sizeof(Real));
   Real* rows = reinterpret_cast<Real*>(smem_raw + dir_bytes);
   Real* rowsM = rows + RS * used * rlen;
   Real* etab = rowsM + (FIRST ? RS * used * rlen : 0);
 
   const long long base4 = (long long)b * d.n4();
-  const SphereDir<Real>* src = pdirs + ((long long)b * d.n0 + i) * dir_row(d.P);
-  for (int t = threadIdx.x; t < used; t += blockDim.x) {
-    const SphereDir<Real> D = src[t];
-    const Real f[kDirFields] = {D.w[0],      D.w[1],      D.w[2],      D.weight,    D.gdir[0], D.gdir[1],
-                                D.gdir[2],   D.ground[0], D.ground[1], D.ground[2], D.sE0};
-#pragma unroll
-    for (int c = 0; c < kDirFields; c++) dirs[c * used + t] = f[c];
-    uE0s[t] = D.uE0;
+  {
+    // the height's direction arrays, prepared by k_sphere_partition
+    const int4* ds = reinterpret_cast<const int4*>(dimage + ((long long)b * d.n0 + i) *
+                                                                dir_image_stride(d, sizeof(Real)));
+    int4* dd = reinterpret_cast<int4*>(smem_raw);
+    for (int t = threadIdx.x; t < (int)(dir_bytes / 16); t += blockDim.x) dd[t] = ds[t];
   }
   {
     // the pair's heading rows from the row table (k_heading_rows), 16 bytes
@@ -384,9 +382,9 @@ size_t point_scatter_smem(const BuildDims& d, bool first) {
 
 template <class Real>
 int launch_point_scatter(const AtmoParams* params, const BuildDims& d, const RowInfo* rowinfo,
-                         const SphereDir<Real>* pdirs, const int2* pcount, const PointRow<Real>* prow,
-                         const CellGeom<Real>* geom, const Vec4<Real>* dS, const Vec4<Real>* mie,
-                         const Vec4<Real>* dE, Real* hrows, Real* J, cudaStream_t st) {
+                         const SphereDir<Real>* pdirs, const unsigned char* dimage, const int2* pcount,
+                         const PointRow<Real>* prow, const CellGeom<Real>* geom, const Vec4<Real>* dS,
+                         const Vec4<Real>* mie, const Vec4<Real>* dE, Real* hrows, Real* J, cudaStream_t st) {
   const int block = 256;
   const int nchunks = (d.n1 * d.n3 + block - 1) / block;
   const int cpb = 2;
@@ -399,15 +397,15 @@ int launch_point_scatter(const AtmoParams* params, const BuildDims& d, const Row
         cudaSuccess)
       return -1;
     k_heading_rows<Real, true><<<rgrid, block, 0, st>>>(d, pdirs, pcount, prow, dS, mie, hrows);
-    k_point_scatter<Real, true><<<grid, block, smem, st>>>(params, d, rowinfo, pdirs, pcount, prow, geom, hrows, dE,
-                                                           J, nchunks, cpb);
+    k_point_scatter<Real, true><<<grid, block, smem, st>>>(params, d, rowinfo, pdirs, dimage, pcount, prow, geom,
+                                                           hrows, dE, J, nchunks, cpb);
   } else {
     if (cudaFuncSetAttribute(k_point_scatter<Real, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)smem) != cudaSuccess)
       return -1;
     k_heading_rows<Real, false><<<rgrid, block, 0, st>>>(d, pdirs, pcount, prow, dS, nullptr, hrows);
-    k_point_scatter<Real, false><<<grid, block, smem, st>>>(params, d, rowinfo, pdirs, pcount, prow, geom, hrows,
-                                                            dE, J, nchunks, cpb);
+    k_point_scatter<Real, false><<<grid, block, smem, st>>>(params, d, rowinfo, pdirs, dimage, pcount, prow, geom,
+                                                            hrows, dE, J, nchunks, cpb);
   }
   return 0;
 }
@@ -901,9 +899,9 @@ void launch_export(long long n, const Vec4<Real>* tab, float* out, cudaStream_t 
 
 #define SFSIM_INSTANTIATE(Real)                                                                                     \
   template int launch_point_scatter<Real>(const AtmoParams*, const BuildDims&, const RowInfo*,                     \
-                                          const SphereDir<Real>*, const int2*, const PointRow<Real>*,              \
-                                          const CellGeom<Real>*, const Vec4<Real>*, const Vec4<Real>*,             \
-                                          const Vec4<Real>*, Real*, Real*, cudaStream_t);                          \
+                                          const SphereDir<Real>*, const unsigned char*, const int2*,               \
+                                          const PointRow<Real>*, const CellGeom<Real>*, const Vec4<Real>*,         \
+                                          const Vec4<Real>*, const Vec4<Real>*, Real*, Real*, cudaStream_t);       \
   template void launch_surface_radiance<Real>(const AtmoParams*, const BuildDims&, const SurfRow<Real>*,          \
                                               const HalfDir<Real>*, const Vec4<Real>*, const Vec4<Real>*,          \
                                               Vec4<Real>*, cudaStream_t);                                          \

@@ -235,7 +235,7 @@ __global__ void k_view_rows(const AtmoParams* params, BuildDims d, const RowInfo
 // ---------------------------------------------------------------------------
 
 template <class Real>
-__global__ void k_sphere_setup(const AtmoParams* params, BuildDims d, const DirLocal* dirs, const int* ring_end,
+__global__ void k_sphere_setup(const AtmoParams* params, BuildDims d, const DirLocal* dirs,
                                SphereDir<Real>* out) {
   const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   const int b = blockIdx.y;
@@ -256,7 +256,7 @@ __global__ void k_sphere_setup(const AtmoParams* params, BuildDims d, const DirL
   o.w[2] = (Real)omega.z;
   o.weight = (Real)dirs[w].w;
   o.surface = surface;
-  o.pad = ring_end[w];
+  o.pad = 0;
   split_coord<Real>(elevation_to_index(P, d.n1, x, omega, !surface), d.n1, &o.u1, &o.s1);
   if (surface) {
     Real tau[3];
@@ -286,7 +286,7 @@ __global__ void k_sphere_setup(const AtmoParams* params, BuildDims d, const DirL
 // a branch per direction.  One warp per row.
 template <class Real>
 __global__ void k_sphere_partition(BuildDims d, const SphereDir<Real>* sdirs, SphereDir<Real>* pdirs,
-                                   int2* pcount) {
+                                   int2* pcount, unsigned char* dimage) {
   const int i = blockIdx.x, b = blockIdx.y, lane = threadIdx.x;
   const long long row = (long long)b * d.n0 + i;
   const SphereDir<Real>* src = sdirs + row * d.P;
@@ -338,6 +338,18 @@ __global__ void k_sphere_partition(BuildDims d, const SphereDir<Real>* sdirs, Sp
     dst[t] = z;
   }
   if (lane == 0) pcount[row] = make_int2(sky_end, used);
+  // point scatter's shared-memory image of the list: each field as an array
+  __syncwarp();
+  Real* img = reinterpret_cast<Real*>(dimage + row * dir_image_stride(d, sizeof(Real)));
+  int* img_u = reinterpret_cast<int*>(img + kDirFields * used);
+  for (int t = lane; t < used; t += 32) {
+    const SphereDir<Real> e = dst[t];
+    const Real f[kDirFields] = {e.w[0],      e.w[1],      e.w[2],      e.weight,    e.gdir[0], e.gdir[1],
+                                e.gdir[2],   e.ground[0], e.ground[1], e.ground[2], e.sE0};
+#pragma unroll
+    for (int c = 0; c < kDirFields; c++) img[c * used + t] = f[c];
+    img_u[t] = e.uE0;
+  }
 }
 
 // Point-scatter constants per (height i, sun elevation k): the coordinates
@@ -421,7 +433,7 @@ __global__ void k_half_dirs(const AtmoParams* params, BuildDims d, const DirLoca
 static inline dim3 grid1(long long n, int block, int B) { return dim3((unsigned)((n + block - 1) / block), B); }
 
 template <class Real>
-void launch_setup(const AtmoParams* params, const BuildDims& d, const DirLocal* dirs, const int* ring_end,
+void launch_setup(const AtmoParams* params, const BuildDims& d, const DirLocal* dirs,
                   const DirLocal* half_dirs, const SetupBuffers<Real>& o, cudaStream_t st) {
   const int blk = 128;
   k_row_info<Real><<<grid1(d.rows(), blk, d.B), blk, 0, st>>>(params, d, o.rowinfo, o.rowmap);
@@ -431,8 +443,8 @@ void launch_setup(const AtmoParams* params, const BuildDims& d, const DirLocal* 
   k_remapT<Real><<<grid1(d.nT(), blk, d.B), blk, 0, st>>>(params, d, o.remapT);
   k_remapE<Real><<<grid1(d.nE(), blk, d.B), blk, 0, st>>>(params, d, o.remapE);
   k_view_rows<Real><<<grid1(d.rows() * d.S, blk, d.B), blk, 0, st>>>(params, d, o.rowinfo, o.rows);
-  k_sphere_setup<Real><<<grid1((long long)d.n0 * d.P, blk, d.B), blk, 0, st>>>(params, d, dirs, ring_end, o.sdirs);
-  k_sphere_partition<Real><<<dim3(d.n0, d.B), 32, 0, st>>>(d, o.sdirs, o.pdirs, o.pcount);
+  k_sphere_setup<Real><<<grid1((long long)d.n0 * d.P, blk, d.B), blk, 0, st>>>(params, d, dirs, o.sdirs);
+  k_sphere_partition<Real><<<dim3(d.n0, d.B), 32, 0, st>>>(d, o.sdirs, o.pdirs, o.pcount, o.dimage);
   k_surface_rows<Real><<<grid1(d.nE(), blk, d.B), blk, 0, st>>>(params, d, o.erow);
   k_half_dirs<Real><<<grid1((long long)d.nE0 * d.Ph, blk, d.B), blk, 0, st>>>(params, d, half_dirs, o.hdir);
 }
@@ -449,10 +461,10 @@ void launch_surface_base(const AtmoParams* params, const BuildDims& d, Vec4<Real
   k_surface_base<Real><<<grid1(d.nE(), blk, d.B), blk, 0, st>>>(params, d, E0);
 }
 
-template void launch_setup<float>(const AtmoParams*, const BuildDims&, const DirLocal*, const int*,
-                                  const DirLocal*, const SetupBuffers<float>&, cudaStream_t);
-template void launch_setup<double>(const AtmoParams*, const BuildDims&, const DirLocal*, const int*,
-                                   const DirLocal*, const SetupBuffers<double>&, cudaStream_t);
+template void launch_setup<float>(const AtmoParams*, const BuildDims&, const DirLocal*, const DirLocal*,
+                                  const SetupBuffers<float>&, cudaStream_t);
+template void launch_setup<double>(const AtmoParams*, const BuildDims&, const DirLocal*, const DirLocal*,
+                                   const SetupBuffers<double>&, cudaStream_t);
 template void launch_transmittance<float>(const AtmoParams*, const BuildDims&, Vec4<float>*, cudaStream_t);
 template void launch_transmittance<double>(const AtmoParams*, const BuildDims&, Vec4<double>*, cudaStream_t);
 template void launch_surface_base<float>(const AtmoParams*, const BuildDims&, Vec4<float>*, cudaStream_t);

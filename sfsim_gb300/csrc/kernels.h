@@ -24,6 +24,9 @@ struct SetupBuffers {
   // pcount = {first ground entry, entries used}
   SphereDir<Real>* pdirs;
   int2* pcount;
+  // point scatter's shared-memory image of each height's partitioned
+  // directions (dir_image_bytes per height): the fields as arrays, then uE0
+  unsigned char* dimage;
   PointRow<Real>* prow;  // [B][n0][n2]
   SurfRow<Real>* erow;   // [B][nE0][nE1]
   HalfDir<Real>* hdir;   // [B][nE0][Ph]
@@ -31,6 +34,18 @@ struct SetupBuffers {
 
 constexpr int kDirBlock = 8;
 __host__ __device__ constexpr int dir_row(int P) { return P + 2 * kDirBlock; }
+
+// Fields per direction in point scatter's shared direction arrays: x0, x1,
+// x2, weight, gdir0..2, ground0..2, sE0 (then uE0 as ints).
+constexpr int kDirFields = 11;
+// Bytes of the direction image of `used` directions, a multiple of 16.
+__host__ __device__ inline size_t dir_image_bytes(int used, size_t real_size) {
+  return ((size_t)used * (kDirFields * real_size + sizeof(int)) + 15) & ~size_t(15);
+}
+// Room per height in the global images: the most partitioned directions.
+__host__ __device__ inline size_t dir_image_stride(const BuildDims& d, size_t real_size) {
+  return dir_image_bytes((dir_row(d.P) + 7) / 8 * 8, real_size);
+}
 
 // Reals of one (height, sun elevation) pair's heading rows in point
 // scatter's global row table: the dS and Mie rows of every partitioned
@@ -40,7 +55,7 @@ __host__ __device__ inline long long heading_rows_stride(const BuildDims& d) {
 }
 
 template <class Real>
-void launch_setup(const AtmoParams* params, const BuildDims& d, const DirLocal* dirs, const int* ring_end,
+void launch_setup(const AtmoParams* params, const BuildDims& d, const DirLocal* dirs,
                   const DirLocal* half_dirs, const SetupBuffers<Real>& o, cudaStream_t st);
 
 template <class Real>
@@ -77,8 +92,8 @@ int launch_smem_probe(int blocks, int iters, float* sink, cudaStream_t st);
 // hrows: scratch for the heading rows, B * n0 * n2 * heading_rows_stride(d) Reals.
 template <class Real>
 int launch_point_scatter(const AtmoParams* params, const BuildDims& d, const RowInfo* rowinfo,
-                         const SphereDir<Real>* pdirs, const int2* pcount, const PointRow<Real>* prow,
-                         const CellGeom<Real>* geom, const Vec4<Real>* dS,
+                         const SphereDir<Real>* pdirs, const unsigned char* dimage, const int2* pcount,
+                         const PointRow<Real>* prow, const CellGeom<Real>* geom, const Vec4<Real>* dS,
                          const Vec4<Real>* mie, const Vec4<Real>* dE, Real* hrows, Real* J, cudaStream_t st);
 
 // dE = surface radiance of dS (same first-iteration convention).
