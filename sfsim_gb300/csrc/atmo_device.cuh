@@ -426,29 +426,6 @@ __device__ __forceinline__ Real height_from_q(Real q, const Real* c, Real alpha,
   return q * p;
 }
 
-// Sums of exp(-h/H_rayleigh) and exp(-h/H_mie) over the midpoint samples
-// t_n = (n + 1/2) dt of a ray with q(t) = q0 + t (two_b + t), where
-// two_b = 2 p.d for a unit direction d.  Compensated sums.
-template <class Real, int NP>
-__device__ __forceinline__ void optical_sums(Real q0, Real two_b, Real dt, int steps, const Real* c, Real alpha,
-                                             Real beta, Real kr, Real km, Real& sum_r, Real& sum_m) {
-  Real sr = 0, cr = 0, sm = 0, cm = 0;
-  Real half = Real(0.5) * dt;
-  Real fn = 0;
-  for (int n = 0; n < steps; n++) {
-    Real t = fma(fn, dt, half);
-    Real q = fma(t, two_b + t, q0);
-    Real h = height_from_q<Real, NP>(q, c, alpha, beta);
-    Real er = Bulk<Real>::exp2(h * kr);
-    Real em = Bulk<Real>::exp2(h * km);
-    kahan_add(sr, cr, er);
-    kahan_add(sm, cm, em);
-    fn += Real(1);
-  }
-  sum_r = sr;
-  sum_m = sm;
-}
-
 // Sums of exp(-h/H_rayleigh) and exp(-h/H_mie) over the midpoint samples of
 // the sun ray, in the form the first-order kernel needs most often.  With
 // t_n = (n + 1/2) dt, q(t_n) = A + n (B + n C), A = q0 + dt (b + dt/4),
@@ -585,34 +562,6 @@ __device__ __forceinline__ Real exp_neg(Real tau) {
   return Bulk<Real>::exp2(tau * Real(-1.4426950408889634));
 }
 
-// Cornette-Shanks phase (atmosphere.clj:56-61); g = 0 gives Rayleigh.
-template <class Real>
-__device__ __forceinline__ Real phase_cs(Real g, Real mu) {
-  Real g2 = g * g;
-  Real base = (Real(1) + g2) - Real(2) * g * mu;
-  Real num = Real(3) * (Real(1) - g2) * (Real(1) + mu * mu);
-  Real den = Real(8) * Real(3.14159265358979323846) * (Real(2) + g2);
-  Real rs = Bulk<Real>::rsqrt(base);
-  return num / den * (rs * rs * rs);
-}
-
-template <class Real>
-__device__ __forceinline__ Real phase_rayleigh(Real mu) {
-  return Real(3.0 / (16.0 * 3.14159265358979323846)) * (Real(1) + mu * mu);
-}
-
-// Bilinear mix of four RGB texels (interpolate.clj:81-98 order: inner dimension first).
-template <class Real>
-__device__ __forceinline__ void mix4(const Real* a, const Real* b, const Real* c, const Real* d, Real s_outer,
-                                     Real s_inner, Real out[3]) {
-#pragma unroll
-  for (int ch = 0; ch < 3; ch++) {
-    Real lo = a[ch] * (Real(1) - s_inner) + b[ch] * s_inner;
-    Real hi = c[ch] * (Real(1) - s_inner) + d[ch] * s_inner;
-    out[ch] = lo * (Real(1) - s_outer) + hi * s_outer;
-  }
-}
-
 // ---------------------------------------------------------------------------
 // Table gathers
 // ---------------------------------------------------------------------------
@@ -628,14 +577,6 @@ __device__ __forceinline__ void ld3(const Vec4<Real>* t, long long i, Real o[3])
   o[0] = v.x;
   o[1] = v.y;
   o[2] = v.z;
-}
-
-// Texel i of a planar RGB table with `plane` entries per channel.
-template <class Real>
-__device__ __forceinline__ void ld3_planar(const Real* __restrict__ t, long long plane, long long i, Real o[3]) {
-  o[0] = t[i];
-  o[1] = t[i + plane];
-  o[2] = t[i + 2 * plane];
 }
 
 template <class Real>

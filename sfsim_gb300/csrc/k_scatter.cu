@@ -305,7 +305,7 @@ __global__ void __launch_bounds__(256, point_scatter_min_blocks(sizeof(Real))) k
           const Real* e0a = etab + 3 * ha * d.nE1;
           const Real* e0b = etab + 3 * hb * d.nE1;
           if (sE0.x == Real(0) && sE0.y == Real(0)) {
-            // the vE0 row has weight 0: mix4 reduces to its uE0 row exactly
+            // the vE0 row has weight 0: the bilinear mix is its uE0 row exactly
             // (the same for every lane: both directions are the warp's)
   #pragma unroll
             for (int c = 0; c < 3; c++) {
@@ -318,7 +318,7 @@ __global__ void __launch_bounds__(256, point_scatter_min_blocks(sizeof(Real))) k
             const Real* e1b = etab + 3 * kb * d.nE1;
   #pragma unroll
             for (int c = 0; c < 3; c++) {
-              // mix4: height rows (uE0, vE0), sun-elevation columns (uE1, vE1)
+              // bilinear in height rows (uE0, vE0) and sun-elevation columns (uE1, vE1)
               const R2 lo =
                   fma2(mk2(e0a[3 * fa + c], e0b[3 * fb + c]), sE1, mul2(mk2(e0a[3 * ea + c], e0b[3 * eb + c]), oi));
               const R2 hi =
