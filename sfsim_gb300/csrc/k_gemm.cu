@@ -13,7 +13,9 @@
 // epilogue, two per group of 32 tensor-memory lanes (one per half of the
 // columns): they read the finished accumulator (tcgen05.ld, the next 32
 // columns in flight while the current ones are written) and apply the
-// epilogue while the MMAs of the next tile run into the other accumulator.
+// epilogue while the MMAs of the next tile run into the other accumulator;
+// full 32 x 32 blocks pass their row-major input and outputs through a
+// per-warp shared-memory tile so that global accesses are row-contiguous.
 // Every wait is bounded; on timeout the CTA records an error, drains its
 // copies and MMAs and returns.
 #include <cuda.h>
@@ -70,6 +72,88 @@ struct GemmKernelArgs {
   int tiles_m, splits;
   long long kper;  // K per split, a multiple of kGemmBK
 };
+
+// Per epilogue warp: a 32 x 32 staging tile (row stride 33 words) that turns
+// the lane-per-row layout of the tensor-memory loads into row-contiguous
+// global accesses.
+constexpr int kGemmStageWords = 32 * 33;
+
+// The 32 x 32 block of rows m0 .. m0 + 31 (lane = row), columns n0 .. n0 + 31,
+// with every row and column inside the output and 16-byte aligned rows: the
+// SiLU' input is read, and the SiLU' and BF16 row-major outputs written, a
+// whole row segment at a time through the warp's staging tile.  Returns
+// false (nothing done) when the block does not qualify.
+__device__ __forceinline__ bool gemm_epilogue32_staged(const GemmArgs& g, const uint32_t* r, int m0, int n0,
+                                                       float* sg) {
+  const int lane = threadIdx.x & 31;
+  const bool fits = m0 + 32 <= g.M && n0 + 32 <= g.N && (g.N % 4) == 0 && !g.Cacc && !g.Cf32 &&
+                    (!g.dact || (reinterpret_cast<uintptr_t>(g.dact) & 15) == 0) &&
+                    (!g.Dsilu || (reinterpret_cast<uintptr_t>(g.Dsilu) & 15) == 0) &&
+                    (!g.Hbf16 || ((g.ldh % 8) == 0 && (reinterpret_cast<uintptr_t>(g.Hbf16) & 15) == 0));
+  if (!fits) return false;
+  float z[32];
+#pragma unroll
+  for (int i = 0; i < 32; i++) z[i] = __uint_as_float(r[i]) * g.alpha;
+  if (g.bias) {
+#pragma unroll
+    for (int i = 0; i < 32; i++) z[i] += g.bias[n0 + i];
+  }
+  // row segments of 32 floats: lane l moves 16 bytes of row 4k + l / 8
+  const int rq = lane >> 3, c4 = 4 * (lane & 7);
+  if (g.dact) {
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+      const int row = 4 * k + rq;
+      const float4 v = *reinterpret_cast<const float4*>(g.dact + (long long)(m0 + row) * g.N + n0 + c4);
+      float* d = sg + row * 33 + c4;
+      d[0] = v.x, d[1] = v.y, d[2] = v.z, d[3] = v.w;
+    }
+    __syncwarp();
+#pragma unroll
+    for (int i = 0; i < 32; i++) z[i] *= sg[lane * 33 + i];
+    __syncwarp();
+  }
+  if (g.Dsilu) {
+#pragma unroll
+    for (int i = 0; i < 32; i++) sg[lane * 33 + i] = dsilu(z[i]);
+    __syncwarp();
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+      const int row = 4 * k + rq;
+      const float* d = sg + row * 33 + c4;
+      *reinterpret_cast<float4*>(g.Dsilu + (long long)(m0 + row) * g.N + n0 + c4) = make_float4(d[0], d[1], d[2], d[3]);
+    }
+    __syncwarp();
+  }
+  if (g.Hbf16 || g.HTbf16) {
+    __nv_bfloat16 h[32];
+#pragma unroll
+    for (int i = 0; i < 32; i++) h[i] = __float2bfloat16(g.silu ? silu(z[i]) : z[i]);
+    if (g.Hbf16) {
+      // 16 packed pairs per row; lane l moves 16 bytes of row 8k + l / 4
+      uint32_t* s32 = reinterpret_cast<uint32_t*>(sg);
+      const uint32_t* hp = reinterpret_cast<const uint32_t*>(h);
+#pragma unroll
+      for (int i = 0; i < 16; i++) s32[lane * 17 + i] = hp[i];
+      __syncwarp();
+      const int rr = lane >> 2, q4 = 4 * (lane & 3);
+#pragma unroll
+      for (int k = 0; k < 4; k++) {
+        const int row = 8 * k + rr;
+        const uint32_t* d = s32 + row * 17 + q4;
+        *reinterpret_cast<uint4*>(g.Hbf16 + (long long)(m0 + row) * g.ldh + n0 + 2 * q4) =
+            make_uint4(d[0], d[1], d[2], d[3]);
+      }
+      __syncwarp();
+    }
+    if (g.HTbf16) {
+      const int m = m0 + lane;
+#pragma unroll
+      for (int i = 0; i < 32; i++) g.HTbf16[(long long)(n0 + i) * g.ldht + m] = h[i];
+    }
+  }
+  return true;
+}
 
 // 32 columns of the epilogue for row m, columns n0 .. n0 + 31.
 __device__ __forceinline__ void gemm_epilogue32(const GemmArgs& g, const uint32_t* r, int m, int n0) {
@@ -165,6 +249,7 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
   uint64_t* drain = tempty + 2;
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(drain + 1);
   volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
+  float* staging = reinterpret_cast<float*>(smem + S * stage_bytes + 1024);  // [8 epilogue warps][32 * 33]
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const uint32_t ncols = a.nt <= 32 ? 32 : a.nt <= 64 ? 64 : a.nt <= 128 ? 128 : 256;  // per accumulator
   const long long ntiles = (long long)a.tiles_m * a.splits;
@@ -270,6 +355,11 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
       }
       tc::fence_after();
       const int m = tm * 128 + q * 32 + lane;
+      const int m0 = tm * 128 + q * 32;
+      float* sg = staging + (warp - 2) * kGemmStageWords;
+      auto epilogue = [&](const uint32_t* r, int n0) {
+        if (!__all_sync(0xffffffffu, gemm_epilogue32_staged(a.g, r, m0, n0, sg))) gemm_epilogue32(a.g, r, m, n0);
+      };
       const uint32_t trow = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(b * ncols);
       const int nall = (a.nt + 31) / 32, nh = (nall + 1) / 2;
       const int b0 = half * nh, b1 = min(nall, b0 + nh);
@@ -279,11 +369,11 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
         tc::tmem_wait_ld(rb[0]);
         for (int blk = b0; blk < b1; blk += 2) {
           if (blk + 1 < b1) tc::tmem_ld32_async(trow + (uint32_t)(32 * (blk + 1)), rb[1]);
-          gemm_epilogue32(a.g, rb[0], m, 32 * blk);
+          epilogue(rb[0], 32 * blk);
           if (blk + 1 < b1) {
             tc::tmem_wait_ld(rb[1]);
             if (blk + 2 < b1) tc::tmem_ld32_async(trow + (uint32_t)(32 * (blk + 2)), rb[0]);
-            gemm_epilogue32(a.g, rb[1], m, 32 * (blk + 1));
+            epilogue(rb[1], 32 * (blk + 1));
             if (blk + 2 < b1) tc::tmem_wait_ld(rb[0]);
           }
         }
@@ -352,9 +442,11 @@ int launch_gemm_tn(const GemmArgs& g, int splits, cudaStream_t st) {
   const int stage_bytes = kGemmTileA + a.nt * kGemmBK * 2;
   const long long kchunks = a.kper / kGemmBK;
   a.stages = (int)std::min<long long>(std::min(kGemmSmemBudget / stage_bytes, 8), std::max<long long>(kchunks, 2));
+  // the epilogue warps' staging tiles after the stages and the barriers
+  const size_t staging = (size_t)(kGemmEpilogueThreads / 32) * kGemmStageWords * sizeof(float);
   CUtensorMap mapA, mapB;
   if (!make_map(&mapA, g.A, g.M, g.K, g.lda, 128) || !make_map(&mapB, g.B, g.N, g.K, g.ldb, a.nt)) return -1;
-  size_t smem = 1024 + (size_t)a.stages * stage_bytes + (2 * a.stages + 5) * 8 + 16;
+  size_t smem = 1024 + (size_t)a.stages * stage_bytes + 1024 + staging;
   // two 256-column accumulators take all of an SM's tensor memory: one CTA per SM
   if (a.nt > 128) smem = std::max<size_t>(smem, 120 * 1024);
   if (cudaFuncSetAttribute(k_gemm_tn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
