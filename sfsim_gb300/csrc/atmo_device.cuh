@@ -586,24 +586,50 @@ __device__ __forceinline__ void mix3(const Real* a, const Real* b, Real s, Real*
 }
 
 // Clamped quadrilinear interpolation of a 4-D table (interpolate.clj:87-98:
-// the innermost dimension is mixed first).
-template <class Real>
+// the innermost dimension is mixed first).  With SKIP, a dimension whose
+// fraction is exactly 0 gives its upper corners weight 0, and
+// mix3(a, b, 0) = a exactly for finite b, so those corners are not loaded:
+// for the re-interpolation maps, which are integers in most dimensions of
+// most nodes (elsewhere the tests cost more than they save).
+template <class Real, bool SKIP = false>
 __device__ inline void interp4(const Vec4<Real>* t, const BuildDims& d, const int* u, const Real* s, Real out[3]) {
   const int v[4] = {upper_index(u[0], d.n0), upper_index(u[1], d.n1), upper_index(u[2], d.n2),
                     upper_index(u[3], d.n3)};
+  const bool two[4] = {!SKIP || s[0] != Real(0), !SKIP || s[1] != Real(0), !SKIP || s[2] != Real(0),
+                       !SKIP || s[3] != Real(0)};
   Real rh[2][3];
 #pragma unroll
   for (int h = 0; h < 2; h++) {
     Real re[2][3];
+    if (h == 1 && !two[0]) {
+#pragma unroll
+      for (int c = 0; c < 3; c++) rh[1][c] = rh[0][c];
+      continue;
+    }
 #pragma unroll
     for (int e = 0; e < 2; e++) {
       Real rk[2][3];
+      if (e == 1 && !two[1]) {
+#pragma unroll
+        for (int c = 0; c < 3; c++) re[1][c] = re[0][c];
+        continue;
+      }
 #pragma unroll
       for (int k = 0; k < 2; k++) {
         Real A[3], B[3];
+        if (k == 1 && !two[2]) {
+#pragma unroll
+          for (int c = 0; c < 3; c++) rk[1][c] = rk[0][c];
+          continue;
+        }
         const int ih = h ? v[0] : u[0], ie = e ? v[1] : u[1], ik = k ? v[2] : u[2];
         ld3(t, idx4(d, ih, ie, ik, u[3]), A);
-        ld3(t, idx4(d, ih, ie, ik, v[3]), B);
+        if (two[3]) {
+          ld3(t, idx4(d, ih, ie, ik, v[3]), B);
+        } else {
+#pragma unroll
+          for (int c = 0; c < 3; c++) B[c] = A[c];
+        }
         mix3(A, B, s[3], rk[k]);
       }
       mix3(rk[0], rk[1], s[2], re[e]);

@@ -26,22 +26,33 @@ template <class Real>
 __device__ __forceinline__ void gather_heading_row(const Vec4<Real>* t, const BuildDims& d, int u0, int v0, Real s0,
                                                    int u1, int v1, Real s1, int u2, int v2, Real s2, int a,
                                                    Real* dst) {
-  Real A[3], B[3], lo[3], hi[3], e0[3], e1[3];
-  // height and sun elevation first, then elevation
-  ld3(t, idx4(d, u0, u1, u2, a), A);
-  ld3(t, idx4(d, u0, u1, v2, a), B);
-  mix3(A, B, s2, lo);
-  ld3(t, idx4(d, v0, u1, u2, a), A);
-  ld3(t, idx4(d, v0, u1, v2, a), B);
-  mix3(A, B, s2, hi);
-  mix3(lo, hi, s0, e0);
-  ld3(t, idx4(d, u0, v1, u2, a), A);
-  ld3(t, idx4(d, u0, v1, v2, a), B);
-  mix3(A, B, s2, lo);
-  ld3(t, idx4(d, v0, v1, u2, a), A);
-  ld3(t, idx4(d, v0, v1, v2, a), B);
-  mix3(A, B, s2, hi);
-  mix3(lo, hi, s0, e1);
+  // height and sun elevation first, then elevation; a corner whose weight
+  // is exactly 0 is not loaded (mix3(x, y, 0) = x exactly)
+  auto pair = [&](int h, int e, Real* out) {  // mixed over the sun elevation
+    Real A[3], B[3];
+    ld3(t, idx4(d, h, e, u2, a), A);
+    if (s2 != Real(0)) {
+      ld3(t, idx4(d, h, e, v2, a), B);
+      mix3(A, B, s2, out);
+    } else {
+#pragma unroll
+      for (int c = 0; c < 3; c++) out[c] = A[c];
+    }
+  };
+  auto row = [&](int e, Real* out) {  // mixed over the height
+    Real lo[3], hi[3];
+    pair(u0, e, lo);
+    if (s0 != Real(0)) {
+      pair(v0, e, hi);
+      mix3(lo, hi, s0, out);
+    } else {
+#pragma unroll
+      for (int c = 0; c < 3; c++) out[c] = lo[c];
+    }
+  };
+  Real e0[3], e1[3];
+  row(u1, e0);
+  row(v1, e1);
   mix3(e0, e1, s1, dst);
 }
 
@@ -410,6 +421,10 @@ int launch_point_scatter(const AtmoParams* params, const BuildDims& d, const Row
   return 0;
 }
 
+// Threads per surface-radiance node: 128 lets about seven blocks share an
+// SM, so the 1024 nodes of the production tables run in about one wave.
+constexpr int kSurfaceThreads = 128;
+
 // ---------------------------------------------------------------------------
 // Surface radiance dE (atmosphere.clj:225-230): integral over the upper half
 // sphere of dS(x, w, l, above) (w.n); the reference passes the ray steps as
@@ -419,11 +434,11 @@ int launch_point_scatter(const AtmoParams* params, const BuildDims& d, const Row
 // ---------------------------------------------------------------------------
 
 template <class Real, bool FIRST>
-__global__ void __launch_bounds__(256) k_surface_radiance(const AtmoParams* params, BuildDims d,
+__global__ void __launch_bounds__(kSurfaceThreads) k_surface_radiance(const AtmoParams* params, BuildDims d,
                                                           const SurfRow<Real>* erow, const HalfDir<Real>* hdir,
                                                           const Vec4<Real>* dS, const Vec4<Real>* Mt,
                                                           Vec4<Real>* dE) {
-  __shared__ Real red[3][256];
+  __shared__ Real red[3][kSurfaceThreads];
   const int b = blockIdx.y;
   const long long node = blockIdx.x;
   const AtmoParams& P = params[b];
@@ -504,9 +519,9 @@ void launch_surface_radiance(const AtmoParams* params, const BuildDims& d, const
                              Vec4<Real>* dE, cudaStream_t st) {
   dim3 grid((unsigned)d.nE(), d.B);
   if (mie)
-    k_surface_radiance<Real, true><<<grid, 256, 0, st>>>(params, d, erow, hdir, dS, mie, dE);
+    k_surface_radiance<Real, true><<<grid, kSurfaceThreads, 0, st>>>(params, d, erow, hdir, dS, mie, dE);
   else
-    k_surface_radiance<Real, false><<<grid, 256, 0, st>>>(params, d, erow, hdir, dS, mie, dE);
+    k_surface_radiance<Real, false><<<grid, kSurfaceThreads, 0, st>>>(params, d, erow, hdir, dS, mie, dE);
 }
 
 // ---------------------------------------------------------------------------
@@ -751,8 +766,8 @@ __global__ void k_accumulate4(BuildDims d, const Remap4<Real>* remap, const Vec4
   if (node >= n4) return;
   const Remap4<Real> m = remap[b * n4 + node];
   Real va[3], vb[3] = {0, 0, 0};
-  interp4(A + b * n4, d, m.u, m.s, va);
-  if (Bt) interp4(Bt + b * n4, d, m.u, m.s, vb);
+  interp4<Real, true>(A + b * n4, d, m.u, m.s, va);
+  if (Bt) interp4<Real, true>(Bt + b * n4, d, m.u, m.s, vb);
   Vec4<Real> o;
   o.x = va[0] + vb[0];
   o.y = va[1] + vb[1];
@@ -789,7 +804,7 @@ __global__ void k_output4(BuildDims d, const Remap4<Real>* remap, const Vec4<Rea
   if (node >= n4) return;
   const Remap4<Real> m = remap[b * n4 + node];
   Real v[3];
-  interp4(tab + b * n4, d, m.u, m.s, v);
+  interp4<Real, true>(tab + b * n4, d, m.u, m.s, v);
   const int a = (int)(node % d.n3);
   const int k = (int)((node / d.n3) % d.n2);
   const int j = (int)((node / ((long long)d.n3 * d.n2)) % d.n1);
