@@ -538,8 +538,26 @@ __device__ __forceinline__ void optical_sums_u(Real c0, Real two_xd, Real dd, Re
   sum_m = sm;
 }
 
-// Optical depth (RGB) of a segment from x to x + D, x and D in FP64, with
-// `steps` midpoint samples (ray.clj:19-30 with atmosphere.clj:114-125).
+// Optical depth (RGB) of a segment from x to x + D with `steps` midpoint
+// samples (ray.clj:19-30 with atmosphere.clj:114-125), from the segment's
+// FP64 invariants: c0 = |x|^2 - R^2, x.D, D.D and L = |D| (a view row's
+// sample segments are the row's segment scaled).
+template <class Real>
+__device__ inline void segment_depth_q(const AtmoParams& P, double c0, double xD, double DD, double L, int steps,
+                                       Real tau[3]) {
+  if (!(L > 0.0)) {
+    tau[0] = tau[1] = tau[2] = 0;
+    return;
+  }
+  Real sr, sm;
+  optical_sums_u<Real, 5>((Real)c0, (Real)(2.0 * xD), (Real)DD, (Real)(1.0 / steps), steps, Bulk<Real>::hpoly(P),
+                          Bulk<Real>::alpha(P), Bulk<Real>::beta(P), Bulk<Real>::kr(P), Bulk<Real>::km(P), sr, sm);
+  Real a = (Real)(L / steps);
+#pragma unroll
+  for (int ch = 0; ch < 3; ch++) tau[ch] = a * (Bulk<Real>::ray_ext(P, ch) * sr + Bulk<Real>::mie_ext(P, ch) * sm);
+}
+
+// The same for x and D in FP64.
 template <class Real>
 __device__ inline void segment_depth(const AtmoParams& P, d3 x, d3 D, int steps, Real tau[3]) {
   double L = mag3(D);

@@ -1,5 +1,7 @@
 // k_setup.cu -- node maps, transmittance and surface-base tables, per-row ray
 // samples and per-height sphere directions of the atmosphere LUT build.
+#include <type_traits>
+
 #include "atmo_device.cuh"
 #include "kernels.h"
 
@@ -214,9 +216,17 @@ __global__ void k_view_rows(const AtmoParams* params, BuildDims d, const RowInfo
   double pr = mag3(p);
   double h = pr - P.R;
   RowSample<Real> o;
-  segment_depth<Real>(P, x, sub3(p, x), d.S, o.tau);
-  o.er = (Real)exp(-(h / P.ray_scale));
-  o.em = (Real)exp(-(h / P.mie_scale));
+  // T(x, p_s): the segment x -> p_s is the row's segment D scaled by su
+  const double c0 = dmul(dsub(ri.r, P.R), dadd(ri.r, P.R));
+  segment_depth_q<Real>(P, c0, su * (ri.r * D.x), su * su * dot3(D, D), su * ri.L, d.S, o.tau);
+  if (std::is_same<Real, float>::value) {
+    // the densities exp(-h/H) as the FP32 integrands form them
+    o.er = (Real)Bulk<float>::exp2((float)h * P.f_kr);
+    o.em = (Real)Bulk<float>::exp2((float)h * P.f_km);
+  } else {
+    o.er = (Real)exp(-(h / P.ray_scale));
+    o.em = (Real)exp(-(h / P.mie_scale));
+  }
   o.q = (Real)((pr - P.R) * (pr + P.R));
   o.us = (Real)su;
   o.inv_r = (Real)(1.0 / pr);
