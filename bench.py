@@ -256,6 +256,7 @@ def run_ours(args):
 
     sweep = run_sweep(L, A, C) if args.extras else None
     queries = run_queries(C) if args.extras else None
+    queries_cond = run_cond_queries(C) if args.extras else None
     noise_builders = run_noise() if args.extras else None
 
     if world > 1:
@@ -296,6 +297,7 @@ def run_ours(args):
             "cpu_baseline": cpu,
             "sweep": sweep,
             "queries": queries,
+            "queries_conditioned": queries_cond,
             "noise": noise_builders,
         }
         print(json.dumps(result), flush=True)
@@ -313,6 +315,7 @@ def run_sweep(L, A, C):
     """64 atmospheres drawn from the sweep distribution, shapes 16x128x16x8, 4
     iterations, built in one batched pass; device time from the stage events."""
     import time as _t
+    import numpy as np
     cfgs = C.parameter_sweep(64)
     read = A.stage_timings(True)
     A.build_batch(cfgs[:2])  # warm-up
@@ -324,8 +327,20 @@ def run_sweep(L, A, C):
     n4 = 1
     for v in cfgs[0].ray_scatter_shape:
         n4 *= v
+    # per-table error of the FP32 tables against the FP64 path of the same
+    # kernels on the same 64 atmospheres (outside the timed region)
+    got = A.build_batch(cfgs)
+    ref = A.build_batch(C.parameter_sweep(64, precision=C.FP64))
+    err = {}
+    for k in ("transmittance", "surface_radiance", "ray_scatter", "mie_strength"):
+        g = got[k].reshape(len(cfgs), -1).astype(np.float64)
+        r = ref[k].reshape(len(cfgs), -1).astype(np.float64)
+        floor = 1e-6 * np.maximum(np.abs(r).max(axis=1, keepdims=True), 1e-300)
+        e = np.abs(g - r) / np.maximum(np.abs(r), floor)
+        err[k] = {"max": float(e.max()), "mean": float(e.mean())}
     return {"atmospheres": len(cfgs), "shape": list(cfgs[0].ray_scatter_shape), "iterations": cfgs[0].iterations,
-            "device_s": dev_ms * 1e-3, "e2e_s": wall, "cells_per_s": len(cfgs) * n4 / (dev_ms * 1e-3)}
+            "device_s": dev_ms * 1e-3, "e2e_s": wall, "cells_per_s": len(cfgs) * n4 / (dev_ms * 1e-3),
+            "err_vs_fp64": err}
 
 
 def _random_queries(n, R, H, seed):
@@ -361,7 +376,8 @@ def query_error_stats(a, ref):
     import torch
     floor = 1e-6 * ref.abs().max()
     e = ((a - ref).abs() / torch.maximum(ref.abs(), floor)).max(dim=1).values
-    q = torch.quantile(e[: 1 << 20].double(), torch.tensor([0.5, 0.9, 0.99], device=e.device, dtype=torch.float64))
+    sample = e[:: max(1, e.numel() >> 20)].double()  # quantile takes at most 2^24 values
+    q = torch.quantile(sample, torch.tensor([0.5, 0.9, 0.99], device=e.device, dtype=torch.float64))
     return {"median": float(q[0]), "p90": float(q[1]), "p99": float(q[2]), "max": float(e.max()),
             "frac_le_1e-3": float((e <= 1e-3).double().mean()), "frac_le_1e-2": float((e <= 1e-2).double().mean())}
 
@@ -473,6 +489,72 @@ def run_queries(C, steps=20000, batch=65536, direct_samples=1 << 25, lr=3e-3, hu
                                             "err": query_error_stats(fb, direct), "vs_direct": t_direct / t_fb}
     ctx.close()
     return r
+
+
+def run_cond_queries(C, n_train=32, n_held_out=8, steps=10000, batch=65536, direct_samples=1 << 20, lr=3e-3,
+                     huber_delta=0.02, threshold=3e-2):
+    """The conditioned surrogate: trained on 32 atmospheres of the parameter
+    sweep (tables 16x128x16x8, 4 iterations; 2^20 direct samples each, 2^25 in
+    all), queried on 8 held-out atmospheres drawn from the same distribution
+    with another seed, 2^21 queries each (height uniform 0-100 km, view and sun
+    uniform); errors relative to each atmosphere's direct quadrature."""
+    import time as _t
+
+    import torch
+
+    from sfsim_gb300.query import ConditionedSurrogate, Context
+    train_cfgs = C.parameter_sweep(n_train)
+    held_cfgs = C.parameter_sweep(n_held_out, seed=C.SWEEP_SEED + 1)
+    t0 = _t.perf_counter()
+    train_ctx = [Context(c) for c in train_cfgs]
+    torch.cuda.synchronize()
+    build_s = _t.perf_counter() - t0
+    cs = ConditionedSurrogate(seed=1)
+    t0 = _t.perf_counter()
+    hist = cs.train(train_ctx, steps=steps, batch=batch, direct_samples=direct_samples, node_fraction=0.0, lr=lr,
+                    seed=1, huber_delta=huber_delta)
+    torch.cuda.synchronize()
+    train_s = _t.perf_counter() - t0
+    for c in train_ctx:
+        c.close()
+    n = 1 << 21
+    ms = {"table": 0.0, "direct": 0.0, "surrogate": 0.0, "fallback": 0.0}
+    parts = {"table": [], "direct": [], "surrogate": [], "fallback": []}
+    flagged = 0
+    for k, cfg in enumerate(held_cfgs):
+        ctx = Context(cfg)
+        x, v, l = _random_queries(n, cfg.radius, cfg.height, 100 + k)
+        x32, v32, l32 = x.float(), v.float(), l.float()
+        out = torch.empty((n, 3), dtype=torch.float32, device="cuda")
+        t, r = _timed(lambda: ctx.table(4, x32, v32, l32, out=out).clone())
+        ms["table"] += t
+        parts["table"].append(r)
+        t, r = _timed(lambda: ctx.direct(x, v, l, out=out).clone(), reps=1)
+        ms["direct"] += t
+        parts["direct"].append(r)
+        t, (r, _) = _timed(lambda: cs.query(ctx, x, v, l, out=out))
+        ms["surrogate"] += t
+        parts["surrogate"].append(r.clone())
+        t, (r, nf) = _timed(lambda: cs.query(ctx, x, v, l, threshold=threshold, out=out), reps=1)
+        ms["fallback"] += t
+        parts["fallback"].append(r.clone())
+        flagged += nf
+        ctx.close()
+    cat = {k: torch.cat(v) for k, v in parts.items()}
+    total = n * len(held_cfgs)
+    qps = lambda t: total / (t * 1e-3)  # noqa: E731
+    cs.close()
+    return {"train_atmospheres": n_train, "held_out_atmospheres": n_held_out, "shape": list(train_cfgs[0].ray_scatter_shape),
+            "n": total, "train_steps": steps, "train_batch": batch, "direct_samples": direct_samples * n_train,
+            "lr": lr, "huber_delta": huber_delta, "context_builds_s": build_s, "train_s": train_s,
+            "train_loss_first": float(hist[:10].mean()), "train_loss_last": float(hist[-100:].mean()),
+            "table": {"qps": qps(ms["table"]), "err": query_error_stats(cat["table"], cat["direct"])},
+            "direct": {"qps": qps(ms["direct"])},
+            "surrogate": {"qps": qps(ms["surrogate"]), "err": query_error_stats(cat["surrogate"], cat["direct"]),
+                          "vs_direct": ms["direct"] / ms["surrogate"]},
+            f"surrogate_fallback_{threshold:g}": {"qps": qps(ms["fallback"]), "fallback_fraction": flagged / total,
+                                                  "err": query_error_stats(cat["fallback"], cat["direct"]),
+                                                  "vs_direct": ms["direct"] / ms["fallback"]}}
 
 
 # ---------------------------------------------------------------------------

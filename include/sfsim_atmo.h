@@ -264,6 +264,53 @@ int sfsim_atmo_query_surrogate(sfsim_atmo_context* ctx, long long n, const doubl
                                const double* l, float* out, float threshold, long long* n_fallback,
                                void* stream);
 
+/* ---- Conditioned surrogate ------------------------------------------------
+ * One network for a family of atmospheres: the surrogate above whose first
+ * layer also takes eight inputs describing the atmosphere (z1 = W1 F + b1 +
+ * U g with U [256][8]).  It is trained on several contexts at once and
+ * corrects the table lookup of any context, including atmospheres it was not
+ * trained on.  No counterpart in the reference. */
+typedef struct sfsim_atmo_cond_surrogate sfsim_atmo_cond_surrogate;
+
+/* The eight inputs g of an atmosphere, each about [-1, 1] over the
+ * parameter sweep: log2 of the Rayleigh coefficients (RGB) relative to
+ * (5.8, 13.5, 33.1)e-6 /m, log2 of the red Mie coefficient relative to
+ * 2e-5 /m, (Rayleigh scale height - 8 km) / 2 km, (Mie scale height -
+ * 1.4 km) / 0.6 km, (Mie g - 0.725) / 0.125, (radius - 5000 km) / 2000 km;
+ * each clamped to [-8, 8].  Host-only. */
+int sfsim_atmo_condition_inputs(const sfsim_atmo_config* cfg, float* inputs);
+
+/* Creates an untrained conditioned surrogate on the current device
+ * (Xavier-uniform weights from `seed`, U zero). */
+int sfsim_atmo_cond_surrogate_create(unsigned long long seed, sfsim_atmo_cond_surrogate** out);
+int sfsim_atmo_cond_surrogate_destroy(sfsim_atmo_cond_surrogate* cs);
+
+/* Trains on n_ctx (1..256) FP32 contexts sharing one ray-scatter shape.  Each
+ * batch row picks a context uniformly, then a sample of it as
+ * sfsim_atmo_surrogate_train draws one; `direct_samples` counts per context. */
+int sfsim_atmo_cond_surrogate_train(sfsim_atmo_cond_surrogate* cs, sfsim_atmo_context* const* ctxs, int n_ctx,
+                                    const sfsim_atmo_surrogate_config* cfg, float* loss_history);
+
+/* Parameter vector: the surrogate's (sfsim_atmo_surrogate_parameters) followed
+ * by U [256][8]. */
+int sfsim_atmo_cond_surrogate_parameters(sfsim_atmo_cond_surrogate* cs, float* get, const float* set,
+                                         long long* count);
+
+/* Loss and gradients of one batch as sfsim_atmo_surrogate_gradients, row i
+ * belonging to group groups[i] < n_groups whose eight inputs are
+ * inputs[groups[i]][0..7] (host arrays). */
+int sfsim_atmo_cond_surrogate_gradients(sfsim_atmo_cond_surrogate* cs, long long n, const float* coords,
+                                        const int* groups, int n_groups, const float* inputs, const float* targets,
+                                        float* loss, float* grads);
+
+/* Rendered in-scatter of the atmosphere `ctx` as sfsim_atmo_query_surrogate
+ * computes it, with the conditioned network at ctx's inputs (folded into the
+ * first-layer bias, so the fused kernel is the same).  Calls on one
+ * surrogate are ordered on one stream. */
+int sfsim_atmo_query_cond_surrogate(sfsim_atmo_cond_surrogate* cs, const sfsim_atmo_context* ctx, long long n,
+                                    const double* x, const double* v, const double* l, float* out, float threshold,
+                                    long long* n_fallback, void* stream);
+
 /* The surrogate's tensor-core GEMM, exposed for validation: C = A * B^T with
  * A [M][K] and B [N][K] row-major bf16 DEVICE arrays and C [M][N] float,
  * FP32 accumulation on tcgen05 tensor cores.  N <= 256; K a multiple of

@@ -27,6 +27,9 @@ EXPORTS = (
     "sfsim_atmo_query_direct", "sfsim_atmo_gemm_bf16", "sfsim_atmo_surrogate_train",
     "sfsim_atmo_surrogate_parameters", "sfsim_atmo_surrogate_gradients", "sfsim_atmo_query_surrogate",
     "sfsim_atmo_query_coords", "sfsim_atmo_smem_peak", "sfsim_noise_worley", "sfsim_noise_perlin", "sfsim_noise_blue",
+    "sfsim_atmo_condition_inputs", "sfsim_atmo_cond_surrogate_create", "sfsim_atmo_cond_surrogate_destroy",
+    "sfsim_atmo_cond_surrogate_train", "sfsim_atmo_cond_surrogate_parameters", "sfsim_atmo_cond_surrogate_gradients",
+    "sfsim_atmo_query_cond_surrogate",
 )
 
 
@@ -97,6 +100,14 @@ def load(build: bool = False):
     L.sfsim_atmo_query_surrogate.argtypes = [vp, ctypes.c_longlong, vp, vp, vp, vp, ctypes.c_float,
                                              ctypes.POINTER(ctypes.c_longlong), vp]
     L.sfsim_atmo_query_coords.argtypes = [vp, ctypes.c_longlong, vp, vp, vp, vp, vp]
+    L.sfsim_atmo_condition_inputs.argtypes = [_cfgp, vp]
+    L.sfsim_atmo_cond_surrogate_create.argtypes = [ctypes.c_ulonglong, ctypes.POINTER(vp)]
+    L.sfsim_atmo_cond_surrogate_destroy.argtypes = [vp]
+    L.sfsim_atmo_cond_surrogate_train.argtypes = [vp, vp, ctypes.c_int, ctypes.POINTER(SurrogateConfig), vp]
+    L.sfsim_atmo_cond_surrogate_parameters.argtypes = [vp, vp, vp, ctypes.POINTER(ctypes.c_longlong)]
+    L.sfsim_atmo_cond_surrogate_gradients.argtypes = [vp, ctypes.c_longlong, vp, vp, ctypes.c_int, vp, vp, vp, vp]
+    L.sfsim_atmo_query_cond_surrogate.argtypes = [vp, vp, ctypes.c_longlong, vp, vp, vp, vp, ctypes.c_float,
+                                                  ctypes.POINTER(ctypes.c_longlong), vp]
     L.sfsim_noise_worley.argtypes = [ctypes.c_int, ctypes.c_int, vp, vp]
     L.sfsim_noise_perlin.argtypes = [ctypes.c_int, ctypes.c_int, vp, vp]
     L.sfsim_noise_blue.argtypes = [ctypes.c_int, ctypes.c_int, vp, ctypes.c_double, vp]

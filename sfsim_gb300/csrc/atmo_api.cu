@@ -984,11 +984,13 @@ constexpr float kLogEps = 1e-7f;     // corrections are log(value + kLogEps) - l
 constexpr float kVarWeight = 0.01f;  // weight of the variance output's gradient in the shared layers
 constexpr long long kQueryChunk = 1 << 22;  // surrogate queries per lookup + inference pass
 
-// parameter offsets (floats) in the concatenated FP32 vector
+// parameter offsets (floats) in the concatenated FP32 vector; a conditioned
+// network appends U [kMlpHidden][cond], the first layer's weights of the
+// atmosphere inputs
 struct MlpLayout {
-  long long W[5], b[5], total;
-  int in[5], out[5];
-  MlpLayout() {
+  long long W[5], b[5], U, total;
+  int in[5], out[5], cond;
+  explicit MlpLayout(int cond_inputs = 0) {
     const int ins[5] = {kMlpIn, kMlpHidden, kMlpHidden, kMlpHidden, kMlpHidden};
     const int outs[5] = {kMlpHidden, kMlpHidden, kMlpHidden, kMlpHidden, kMlpOut};
     long long o = 0;
@@ -1000,12 +1002,15 @@ struct MlpLayout {
       b[l] = o;
       o += outs[l];
     }
-    total = o;
+    cond = cond_inputs;
+    U = o;
+    total = o + (long long)kMlpHidden * cond;
   }
 };
 
 struct Surrogate {
   MlpLayout lay;
+  explicit Surrogate(int cond) : lay(cond) {}
   long long batch = 0;             // rows of the activation buffers
   float *w = nullptr, *g = nullptr, *m = nullptr, *v = nullptr;  // master weights, grads, Adam moments
   __nv_bfloat16 *wb[4] = {}, *wbt[4] = {};  // BF16 W_l [out][in] and W_l^T [in][out]
@@ -1018,6 +1023,12 @@ struct Surrogate {
   long long qcap = 0;               // queries qbuf holds
   int* error = nullptr;
   int trained_steps = 0;
+  // conditioned network: the groups' atmosphere inputs G [groups][kCondInputs],
+  // their first-layer row biases U g [groups][kMlpHidden], each row's group,
+  // and for queries the first-layer bias b1 + U g of the queried atmosphere
+  int groups = 0;
+  float *G = nullptr, *cbias = nullptr, *qbias = nullptr, *qG = nullptr;
+  int* group = nullptr;
   std::vector<void*> allocs;
   float* alloc_f(size_t n) {
     void* p = nullptr;
@@ -1062,10 +1073,10 @@ void init_weights(const MlpLayout& lay, unsigned long long seed, std::vector<flo
   }
 }
 
-int surrogate_alloc(sfsim_atmo_context* c, long long batch, unsigned long long seed) {
-  if (!c->sur) {
-    c->sur = new Surrogate();
-    Surrogate& S = *c->sur;
+int surrogate_alloc(Surrogate*& sur, int cond, long long batch, unsigned long long seed) {
+  if (!sur) {
+    sur = new Surrogate(cond);
+    Surrogate& S = *sur;
     const long long P = S.lay.total;
     S.w = S.alloc_f(P);
     S.g = S.alloc_f(P);
@@ -1083,6 +1094,13 @@ int surrogate_alloc(sfsim_atmo_context* c, long long batch, unsigned long long s
     S.packed = reinterpret_cast<unsigned char*>(S.alloc_h(infer_packed_bytes() / 2));
     if (!S.w || !S.g || !S.m || !S.v || !S.loss || !S.wb[3] || !S.wbt[3] || !S.packed)
       return fail(SFSIM_ATMO_ENOMEM, "surrogate allocation failed");
+    if (cond) {
+      S.G = S.alloc_f((size_t)kMaxCondGroups * kCondInputs);
+      S.cbias = S.alloc_f((size_t)kMaxCondGroups * kMlpHidden);
+      S.qbias = S.alloc_f(kMlpHidden);
+      S.qG = S.alloc_f(kCondInputs);
+      if (!S.G || !S.cbias || !S.qbias || !S.qG) return fail(SFSIM_ATMO_ENOMEM, "surrogate allocation failed");
+    }
     std::vector<float> h;
     init_weights(S.lay, seed, h);
     CUDA_TRY(cudaMemcpy(S.w, h.data(), sizeof(float) * P, cudaMemcpyHostToDevice));
@@ -1094,7 +1112,7 @@ int surrogate_alloc(sfsim_atmo_context* c, long long batch, unsigned long long s
                      S.wbt[l], 0);
     CUDA_TRY(cudaGetLastError());
   }
-  Surrogate& S = *c->sur;
+  Surrogate& S = *sur;
   if (S.batch < batch) {
     // activation buffers for `batch` rows
     auto drop = [&](void* p) {
@@ -1106,7 +1124,7 @@ int surrogate_alloc(sfsim_atmo_context* c, long long batch, unsigned long long s
           return;
         }
     };
-    drop(S.coords); drop(S.target); drop(S.out); drop(S.dout); drop(S.F); drop(S.FT);
+    drop(S.coords); drop(S.target); drop(S.out); drop(S.dout); drop(S.F); drop(S.FT); drop(S.group);
     for (int l = 0; l < 4; l++) {
       drop(S.H[l]); drop(S.HT[l]); drop(S.dZ[l]); drop(S.dZT[l]); drop(S.dsilu[l]);
     }
@@ -1116,7 +1134,15 @@ int surrogate_alloc(sfsim_atmo_context* c, long long batch, unsigned long long s
     S.dout = S.alloc_f(kMlpOut * batch);
     S.F = S.alloc_h(kMlpIn * batch);
     S.FT = S.alloc_h(kMlpIn * batch);
-    bool okay = S.coords && S.target && S.out && S.dout && S.F && S.FT;
+    S.group = nullptr;
+    if (S.lay.cond) {
+      void* p = nullptr;
+      if (cudaMalloc(&p, sizeof(int) * (size_t)batch) == cudaSuccess) {
+        S.allocs.push_back(p);
+        S.group = (int*)p;
+      }
+    }
+    bool okay = S.coords && S.target && S.out && S.dout && S.F && S.FT && (!S.lay.cond || S.group);
     for (int l = 0; l < 4 && okay; l++) {
       S.H[l] = S.alloc_h(kMlpHidden * batch);
       S.HT[l] = S.alloc_h(kMlpHidden * batch);
@@ -1138,6 +1164,7 @@ int surrogate_alloc(sfsim_atmo_context* c, long long batch, unsigned long long s
 // backward pass needs.  Leaves the kMlpOut outputs per row in S.out.
 int surrogate_forward(Surrogate& S, long long n, bool train, cudaStream_t st) {
   launch_features(n, S.coords, S.F, train ? S.FT : nullptr, st);
+  if (S.lay.cond) launch_cond_bias(S.groups, S.w + S.lay.U, S.G, nullptr, S.cbias, st);
   const __nv_bfloat16* prev = S.F;
   for (int l = 0; l < 4; l++) {
     GemmArgs g = {};
@@ -1150,6 +1177,10 @@ int surrogate_forward(Surrogate& S, long long n, bool train, cudaStream_t st) {
     g.K = S.lay.in[l];
     g.alpha = 1.0f;
     g.bias = S.w + S.lay.b[l];
+    if (l == 0 && S.lay.cond) {
+      g.row_bias = S.cbias;
+      g.row_group = S.group;
+    }
     g.Dsilu = train ? S.dsilu[l] : nullptr;
     g.silu = 1;
     g.Hbf16 = S.H[l];
@@ -1191,6 +1222,7 @@ int surrogate_backward(Surrogate& S, long long n, float huber, cudaStream_t st) 
     g.error = S.error;
     if (launch_gemm_tn(g, splits, st)) return fail(SFSIM_ATMO_ECUDA, "weight-gradient GEMM launch failed");
     launch_bias_grad(n, S.lay.out[l], S.dZT[l], S.g + S.lay.b[l], st);
+    if (l == 0 && S.lay.cond) launch_cond_grad(n, S.dZT[0], S.group, S.groups, S.G, S.g + S.lay.U, st);
     if (l > 0) {
       // dZ_{l-1} = (dZ_l W_l) * SiLU'(z_{l-1}): A = dZ_l [n][out], B = W_l^T [in][out]
       GemmArgs h = {};
@@ -1223,6 +1255,11 @@ void surrogate_adam(Surrogate& S, float lr, int step, cudaStream_t st) {
                 S.lay.out[l], S.lay.in[l], l < 4 ? S.wb[l] : nullptr, l < 4 ? S.wbt[l] : nullptr, st);
     launch_adam(S.lay.out[l], S.w + S.lay.b[l], S.g + S.lay.b[l], S.m + S.lay.b[l], S.v + S.lay.b[l], lr, b1, b2,
                 eps, step, 1, S.lay.out[l], nullptr, nullptr, st);
+  }
+  if (S.lay.cond) {
+    const long long nu = (long long)kMlpHidden * S.lay.cond;
+    launch_adam(nu, S.w + S.lay.U, S.g + S.lay.U, S.m + S.lay.U, S.v + S.lay.U, lr, b1, b2, eps, step, kMlpHidden,
+                S.lay.cond, nullptr, nullptr, st);
   }
 }
 
@@ -1493,37 +1530,28 @@ int surrogate_pools(sfsim_atmo_context* c, long long n_direct, unsigned long lon
   return 0;
 }
 
-}  // namespace
-
-extern "C" {
-
-int sfsim_atmo_surrogate_train(sfsim_atmo_context* ctx, const sfsim_atmo_surrogate_config* sc, float* loss_history) {
-  if (!ctx || !sc) return fail(SFSIM_ATMO_ENULL, "NULL argument");
-  if (ctx->cfg.precision != SFSIM_ATMO_FP32) return fail(SFSIM_ATMO_EINVAL, "the surrogate needs an FP32 context");
+int check_train_config(const sfsim_atmo_surrogate_config* sc) {
   if (sc->steps < 0 || sc->batch < 1024 || sc->batch % 1024 != 0 || sc->direct_samples < 0 ||
       !(sc->node_fraction >= 0 && sc->node_fraction <= 1) || !(sc->lr > 0) || !(sc->huber_delta >= 0))
     return fail(SFSIM_ATMO_EINVAL,
                 "steps >= 0, batch a positive multiple of 1024, lr > 0, node_fraction in [0, 1], huber_delta >= 0");
-  std::lock_guard<std::mutex> lock(g_mutex);
-  int cur = 0;
-  CUDA_TRY(cudaGetDevice(&cur));
-  if (cur != ctx->dev) return fail(SFSIM_ATMO_EINVAL, "the context belongs to another device");
-  int rc = surrogate_alloc(ctx, sc->batch, sc->seed);
-  if (rc) return rc;
-  Surrogate& S = *ctx->sur;
-  cudaStream_t st = g_stream[ctx->dev];
-  std::vector<void*> temps;
-  float *node_pool = nullptr, *direct_pool = nullptr;
+  return 0;
+}
+
+// The Adam steps of one training call (cosine-decayed learning rate); `gather`
+// fills S.coords and S.target (and S.group) for step t.  `rc` carries an
+// error of the caller's set-up, in which case nothing runs.  Frees `temps`.
+template <class Gather>
+int run_training(Surrogate& S, const sfsim_atmo_surrogate_config* sc, int rc, Gather gather, float* loss_history,
+                 std::vector<void*>& temps, cudaStream_t st) {
   float* hist = nullptr;
-  rc = surrogate_pools(ctx, sc->direct_samples, sc->seed, &node_pool, &direct_pool, temps, st);
   if (!rc && cudaMalloc(&hist, sizeof(float) * std::max(1, sc->steps)) != cudaSuccess)
     rc = fail(SFSIM_ATMO_ENOMEM, "loss history allocation failed");
   if (hist) temps.push_back(hist);
   const long long n = sc->batch;
   for (int t = 0; t < sc->steps && !rc; t++) {
     const float lr = sc->lr * 0.5f * (1.0f + std::cos(3.14159265358979f * (float)t / (float)sc->steps));
-    launch_gather_batch(n, sc->seed * 0x9E3779B97F4A7C15ull + (unsigned long long)t, sc->node_fraction, node_pool,
-                        ctx->dims.n4(), direct_pool, sc->direct_samples, S.coords, S.target, st);
+    gather(t);
     if ((rc = surrogate_forward(S, n, true, st))) break;
     if ((rc = surrogate_backward(S, n, sc->huber_delta, st))) break;
     surrogate_adam(S, lr, S.trained_steps + t + 1, st);
@@ -1545,8 +1573,37 @@ int sfsim_atmo_surrogate_train(sfsim_atmo_context* ctx, const sfsim_atmo_surroga
   }
   cudaStreamSynchronize(st);
   for (void* p : temps) cudaFree(p);
+  temps.clear();
   if (!rc) S.trained_steps += sc->steps;
   return rc;
+}
+
+}  // namespace
+
+extern "C" {
+
+int sfsim_atmo_surrogate_train(sfsim_atmo_context* ctx, const sfsim_atmo_surrogate_config* sc, float* loss_history) {
+  if (!ctx || !sc) return fail(SFSIM_ATMO_ENULL, "NULL argument");
+  if (ctx->cfg.precision != SFSIM_ATMO_FP32) return fail(SFSIM_ATMO_EINVAL, "the surrogate needs an FP32 context");
+  int rc = check_train_config(sc);
+  if (rc) return rc;
+  std::lock_guard<std::mutex> lock(g_mutex);
+  int cur = 0;
+  CUDA_TRY(cudaGetDevice(&cur));
+  if (cur != ctx->dev) return fail(SFSIM_ATMO_EINVAL, "the context belongs to another device");
+  rc = surrogate_alloc(ctx->sur, 0, sc->batch, sc->seed);
+  if (rc) return rc;
+  Surrogate& S = *ctx->sur;
+  cudaStream_t st = g_stream[ctx->dev];
+  std::vector<void*> temps;
+  float *node_pool = nullptr, *direct_pool = nullptr;
+  rc = surrogate_pools(ctx, sc->direct_samples, sc->seed, &node_pool, &direct_pool, temps, st);
+  const long long na = ctx->dims.n4();
+  auto gather = [&](int t) {
+    launch_gather_batch(sc->batch, sc->seed * 0x9E3779B97F4A7C15ull + (unsigned long long)t, sc->node_fraction,
+                        node_pool, na, direct_pool, sc->direct_samples, S.coords, S.target, st);
+  };
+  return run_training(S, sc, rc, gather, loss_history, temps, st);
 }
 
 int sfsim_atmo_surrogate_parameters(sfsim_atmo_context* ctx, float* get, const float* set, long long* count) {
@@ -1555,7 +1612,7 @@ int sfsim_atmo_surrogate_parameters(sfsim_atmo_context* ctx, float* get, const f
   if (count) *count = lay.total;
   if (!get && !set) return 0;
   std::lock_guard<std::mutex> lock(g_mutex);
-  int rc = surrogate_alloc(ctx, 1024, 1);
+  int rc = surrogate_alloc(ctx->sur, 0, 1024, 1);
   if (rc) return rc;
   Surrogate& S = *ctx->sur;
   if (set) {
@@ -1573,7 +1630,7 @@ int sfsim_atmo_surrogate_gradients(sfsim_atmo_context* ctx, long long n, const f
   if (!ctx || !coords || !targets) return fail(SFSIM_ATMO_ENULL, "NULL argument");
   if (n < 1024 || n % 1024 != 0) return fail(SFSIM_ATMO_EINVAL, "n must be a positive multiple of 1024");
   std::lock_guard<std::mutex> lock(g_mutex);
-  int rc = surrogate_alloc(ctx, n, 1);
+  int rc = surrogate_alloc(ctx->sur, 0, n, 1);
   if (rc) return rc;
   Surrogate& S = *ctx->sur;
   cudaStream_t st = g_stream[ctx->dev];
@@ -1597,16 +1654,16 @@ int sfsim_atmo_query_coords(const sfsim_atmo_context* ctx, long long n, const do
   return 0;
 }
 
-int sfsim_atmo_query_surrogate(sfsim_atmo_context* ctx, long long n, const double* x, const double* v,
-                               const double* l, float* out, float threshold, long long* n_fallback, void* stream) {
-  if (!ctx || !x || !v || !l || !out) return fail(SFSIM_ATMO_ENULL, "NULL argument");
-  if (!ctx->sur) return fail(SFSIM_ATMO_EINVAL, "the context has no trained surrogate");
-  if (n < 0) return fail(SFSIM_ATMO_EINVAL, "n must be non-negative");
-  if (n_fallback) *n_fallback = 0;
-  if (n == 0) return 0;
-  std::lock_guard<std::mutex> lock(g_mutex);
-  Surrogate& S = *ctx->sur;
-  cudaStream_t st = (cudaStream_t)stream;
+}  // extern "C"
+
+namespace {
+
+// Surrogate queries of the atmosphere `ctx` (its tables, and its quadrature
+// for the fallback) with the network S, whose first-layer bias is `bias0`.
+// The caller holds g_mutex.
+int surrogate_query(Surrogate& S, const float* bias0, const sfsim_atmo_context* ctx, long long n, const double* x,
+                    const double* v, const double* l, float* out, float threshold, long long* n_fallback,
+                    cudaStream_t st) {
   const QueryTables q = context_tables(ctx);
   const bool fallback = threshold > 0;
   long long* list = nullptr;  // indices of the flagged queries
@@ -1621,6 +1678,7 @@ int sfsim_atmo_query_surrogate(sfsim_atmo_context* ctx, long long n, const doubl
   }
   const float* biases[4];
   for (int i = 0; i < 4; i++) biases[i] = S.w + S.lay.b[i];
+  biases[0] = bias0;
   int rc = 0, sms = 0;
   CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->dev));
   // queries go through in chunks: the lookup kernel forms coordinates and
@@ -1665,6 +1723,236 @@ int sfsim_atmo_query_surrogate(sfsim_atmo_context* ctx, long long n, const doubl
     if (!rc) rc = check_error_flag(S, st);
   }
   return rc;
+}
+
+
+}  // namespace
+
+extern "C" {
+
+int sfsim_atmo_query_surrogate(sfsim_atmo_context* ctx, long long n, const double* x, const double* v,
+                               const double* l, float* out, float threshold, long long* n_fallback, void* stream) {
+  if (!ctx || !x || !v || !l || !out) return fail(SFSIM_ATMO_ENULL, "NULL argument");
+  if (!ctx->sur) return fail(SFSIM_ATMO_EINVAL, "the context has no trained surrogate");
+  if (n < 0) return fail(SFSIM_ATMO_EINVAL, "n must be non-negative");
+  if (n_fallback) *n_fallback = 0;
+  if (n == 0) return 0;
+  std::lock_guard<std::mutex> lock(g_mutex);
+  Surrogate& S = *ctx->sur;
+  return surrogate_query(S, S.w + S.lay.b[0], ctx, n, x, v, l, out, threshold, n_fallback, (cudaStream_t)stream);
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Conditioned surrogate: one network for many atmospheres, whose first layer
+// also takes kCondInputs inputs describing the atmosphere.  Trained on several
+// contexts at once; queried on any context (also one it never saw), whose
+// table it corrects.
+// ---------------------------------------------------------------------------
+
+struct sfsim_atmo_cond_surrogate {
+  int dev;
+  unsigned long long seed;
+  Surrogate* sur;
+};
+
+namespace {
+
+// The atmosphere inputs, each about [-1, 1] over the parameter sweep: log2 of
+// the Rayleigh coefficients (RGB) and of the Mie coefficient (red) relative
+// to Earth's, the two scale heights, the Mie asymmetry and the radius.
+void condition_inputs(const sfsim_atmo_config& c, float* g) {
+  auto lg = [](double a, double ref) { return std::log2(std::max(a, 1e-30) / ref); };
+  const double v[kCondInputs] = {lg(c.rayleigh.scatter_base[0], 5.8e-6), lg(c.rayleigh.scatter_base[1], 13.5e-6),
+                                 lg(c.rayleigh.scatter_base[2], 33.1e-6), lg(c.mie.scatter_base[0], 2e-5),
+                                 (c.rayleigh.scatter_scale - 8000.0) / 2000.0, (c.mie.scatter_scale - 1400.0) / 600.0,
+                                 (c.mie.scatter_g - 0.725) / 0.125,        (c.radius - 5.0e6) / 2.0e6};
+  for (int p = 0; p < kCondInputs; p++) g[p] = (float)std::min(8.0, std::max(-8.0, v[p]));
+}
+
+int cond_prologue(sfsim_atmo_cond_surrogate* cs) {
+  int cur = 0;
+  CUDA_TRY(cudaGetDevice(&cur));
+  if (cur != cs->dev) return fail(SFSIM_ATMO_EINVAL, "the surrogate belongs to another device");
+  return ensure_stream(cs->dev);
+}
+
+}  // namespace
+
+extern "C" {
+
+int sfsim_atmo_condition_inputs(const sfsim_atmo_config* cfg, float* inputs) {
+  if (!cfg || !inputs) return fail(SFSIM_ATMO_ENULL, "NULL argument");
+  condition_inputs(*cfg, inputs);
+  return 0;
+}
+
+int sfsim_atmo_cond_surrogate_create(unsigned long long seed, sfsim_atmo_cond_surrogate** out) {
+  if (!out) return fail(SFSIM_ATMO_ENULL, "out is NULL");
+  *out = nullptr;
+  std::lock_guard<std::mutex> lock(g_mutex);
+  int dev = 0, rc = current_device(&dev);
+  if (rc) return rc;
+  if ((rc = ensure_stream(dev))) return rc;
+  sfsim_atmo_cond_surrogate* cs = new sfsim_atmo_cond_surrogate();
+  cs->dev = dev;
+  cs->seed = seed;
+  cs->sur = nullptr;
+  if ((rc = surrogate_alloc(cs->sur, kCondInputs, 1024, seed))) {
+    if (cs->sur) {
+      cs->sur->free_all();
+      delete cs->sur;
+    }
+    delete cs;
+    return rc;
+  }
+  *out = cs;
+  return 0;
+}
+
+int sfsim_atmo_cond_surrogate_destroy(sfsim_atmo_cond_surrogate* cs) {
+  if (!cs) return 0;
+  int cur = 0;
+  cudaGetDevice(&cur);
+  cudaSetDevice(cs->dev);
+  if (cs->sur) {
+    cs->sur->free_all();
+    delete cs->sur;
+  }
+  cudaSetDevice(cur);
+  delete cs;
+  return 0;
+}
+
+int sfsim_atmo_cond_surrogate_train(sfsim_atmo_cond_surrogate* cs, sfsim_atmo_context* const* ctxs, int n_ctx,
+                                    const sfsim_atmo_surrogate_config* sc, float* loss_history) {
+  if (!cs || !ctxs || !sc) return fail(SFSIM_ATMO_ENULL, "NULL argument");
+  if (n_ctx < 1 || n_ctx > kMaxCondGroups)
+    return fail(SFSIM_ATMO_EINVAL, "n_ctx must be in [1, " + std::to_string(kMaxCondGroups) + "]");
+  int rc = check_train_config(sc);
+  if (rc) return rc;
+  for (int a = 0; a < n_ctx; a++) {
+    const sfsim_atmo_context* c = ctxs[a];
+    if (!c) return fail(SFSIM_ATMO_ENULL, "a context is NULL");
+    if (c->cfg.precision != SFSIM_ATMO_FP32) return fail(SFSIM_ATMO_EINVAL, "the surrogate needs FP32 contexts");
+    if (c->dev != cs->dev) return fail(SFSIM_ATMO_EINVAL, "a context belongs to another device");
+    if (c->dims.n4() != ctxs[0]->dims.n4())
+      return fail(SFSIM_ATMO_EINVAL, "the contexts must share their ray-scatter shape");
+  }
+  std::lock_guard<std::mutex> lock(g_mutex);
+  if ((rc = cond_prologue(cs))) return rc;
+  if ((rc = surrogate_alloc(cs->sur, kCondInputs, sc->batch, cs->seed))) return rc;
+  Surrogate& S = *cs->sur;
+  cudaStream_t st = g_stream[cs->dev];
+  std::vector<void*> temps;
+  // per atmosphere: its inputs and its two pools (table nodes, direct samples)
+  std::vector<float> G((size_t)n_ctx * kCondInputs);
+  std::vector<const float*> pa(n_ctx), pb(n_ctx);
+  for (int a = 0; a < n_ctx && !rc; a++) {
+    condition_inputs(ctxs[a]->cfg, G.data() + (size_t)a * kCondInputs);
+    float *node_pool = nullptr, *direct_pool = nullptr;
+    rc = surrogate_pools(ctxs[a], sc->direct_samples, sc->seed * 7919ull + (unsigned long long)a, &node_pool,
+                         &direct_pool, temps, st);
+    pa[a] = node_pool;
+    pb[a] = direct_pool;
+  }
+  const float** dp = nullptr;
+  if (!rc) {
+    void* p = nullptr;
+    if (cudaMalloc(&p, sizeof(float*) * 2 * (size_t)n_ctx) != cudaSuccess) {
+      rc = fail(SFSIM_ATMO_ENOMEM, "pool table allocation failed");
+    } else {
+      temps.push_back(p);
+      dp = (const float**)p;
+      std::vector<const float*> both(pa);
+      both.insert(both.end(), pb.begin(), pb.end());
+      if (cudaMemcpyAsync(dp, both.data(), sizeof(float*) * 2 * (size_t)n_ctx, cudaMemcpyHostToDevice, st) !=
+              cudaSuccess ||
+          cudaMemcpyAsync(S.G, G.data(), sizeof(float) * G.size(), cudaMemcpyHostToDevice, st) != cudaSuccess ||
+          cudaStreamSynchronize(st) != cudaSuccess)
+        rc = fail(SFSIM_ATMO_ECUDA, "pool table copy failed");
+    }
+  }
+  S.groups = n_ctx;
+  const long long na = ctxs[0]->dims.n4();
+  auto gather = [&](int t) {
+    launch_gather_batch_groups(sc->batch, sc->seed * 0x9E3779B97F4A7C15ull + (unsigned long long)t,
+                               sc->node_fraction, n_ctx, dp, na, dp + n_ctx, sc->direct_samples, S.coords, S.target,
+                               S.group, st);
+  };
+  return run_training(S, sc, rc, gather, loss_history, temps, st);
+}
+
+int sfsim_atmo_cond_surrogate_parameters(sfsim_atmo_cond_surrogate* cs, float* get, const float* set,
+                                         long long* count) {
+  if (!cs) return fail(SFSIM_ATMO_ENULL, "surrogate is NULL");
+  const MlpLayout lay(kCondInputs);
+  if (count) *count = lay.total;
+  if (!get && !set) return 0;
+  std::lock_guard<std::mutex> lock(g_mutex);
+  int rc = cond_prologue(cs);
+  if (rc) return rc;
+  Surrogate& S = *cs->sur;
+  if (set) {
+    CUDA_TRY(cudaMemcpy(S.w, set, sizeof(float) * lay.total, cudaMemcpyHostToDevice));
+    for (int l = 0; l < 4; l++)
+      launch_to_bf16((long long)lay.in[l] * lay.out[l], S.w + lay.W[l], lay.out[l], lay.in[l], S.wb[l], S.wbt[l], 0);
+    CUDA_TRY(cudaDeviceSynchronize());
+  }
+  if (get) CUDA_TRY(cudaMemcpy(get, S.w, sizeof(float) * lay.total, cudaMemcpyDeviceToHost));
+  return 0;
+}
+
+int sfsim_atmo_cond_surrogate_gradients(sfsim_atmo_cond_surrogate* cs, long long n, const float* coords,
+                                        const int* groups, int n_groups, const float* inputs, const float* targets,
+                                        float* loss, float* grads) {
+  if (!cs || !coords || !groups || !inputs || !targets) return fail(SFSIM_ATMO_ENULL, "NULL argument");
+  if (n < 1024 || n % 1024 != 0) return fail(SFSIM_ATMO_EINVAL, "n must be a positive multiple of 1024");
+  if (n_groups < 1 || n_groups > kMaxCondGroups)
+    return fail(SFSIM_ATMO_EINVAL, "n_groups must be in [1, " + std::to_string(kMaxCondGroups) + "]");
+  for (long long i = 0; i < n; i++)
+    if (groups[i] < 0 || groups[i] >= n_groups) return fail(SFSIM_ATMO_EINVAL, "a group index is out of range");
+  std::lock_guard<std::mutex> lock(g_mutex);
+  int rc = cond_prologue(cs);
+  if (rc) return rc;
+  if ((rc = surrogate_alloc(cs->sur, kCondInputs, n, cs->seed))) return rc;
+  Surrogate& S = *cs->sur;
+  cudaStream_t st = g_stream[cs->dev];
+  S.groups = n_groups;
+  CUDA_TRY(cudaMemcpyAsync(S.coords, coords, sizeof(float) * kMlpCoords * n, cudaMemcpyHostToDevice, st));
+  CUDA_TRY(cudaMemcpyAsync(S.target, targets, sizeof(float) * 3 * n, cudaMemcpyHostToDevice, st));
+  CUDA_TRY(cudaMemcpyAsync(S.group, groups, sizeof(int) * n, cudaMemcpyHostToDevice, st));
+  CUDA_TRY(cudaMemcpyAsync(S.G, inputs, sizeof(float) * kCondInputs * n_groups, cudaMemcpyHostToDevice, st));
+  if ((rc = surrogate_forward(S, n, true, st))) return rc;
+  if ((rc = surrogate_backward(S, n, 0.0f, st))) return rc;
+  if (loss) CUDA_TRY(cudaMemcpyAsync(loss, S.loss, sizeof(float), cudaMemcpyDeviceToHost, st));
+  if (grads) CUDA_TRY(cudaMemcpyAsync(grads, S.g, sizeof(float) * S.lay.total, cudaMemcpyDeviceToHost, st));
+  CUDA_TRY(cudaStreamSynchronize(st));
+  return check_error_flag(S, st);
+}
+
+int sfsim_atmo_query_cond_surrogate(sfsim_atmo_cond_surrogate* cs, const sfsim_atmo_context* ctx, long long n,
+                                    const double* x, const double* v, const double* l, float* out, float threshold,
+                                    long long* n_fallback, void* stream) {
+  if (!cs || !ctx || !x || !v || !l || !out) return fail(SFSIM_ATMO_ENULL, "NULL argument");
+  if (ctx->cfg.precision != SFSIM_ATMO_FP32) return fail(SFSIM_ATMO_EINVAL, "the surrogate needs an FP32 context");
+  if (ctx->dev != cs->dev) return fail(SFSIM_ATMO_EINVAL, "the context belongs to another device");
+  if (n < 0) return fail(SFSIM_ATMO_EINVAL, "n must be non-negative");
+  if (n_fallback) *n_fallback = 0;
+  if (n == 0) return 0;
+  std::lock_guard<std::mutex> lock(g_mutex);
+  int rc = cond_prologue(cs);
+  if (rc) return rc;
+  Surrogate& S = *cs->sur;
+  cudaStream_t st = (cudaStream_t)stream;
+  // first-layer bias of this atmosphere: b1 + U g
+  float g[kCondInputs];
+  condition_inputs(ctx->cfg, g);
+  CUDA_TRY(cudaMemcpyAsync(S.qG, g, sizeof(g), cudaMemcpyHostToDevice, st));
+  launch_cond_bias(1, S.w + S.lay.U, S.qG, S.w + S.lay.b[0], S.qbias, st);
+  CUDA_TRY(cudaGetLastError());
+  return surrogate_query(S, S.qbias, ctx, n, x, v, l, out, threshold, n_fallback, st);
 }
 
 }  // extern "C"

@@ -89,6 +89,7 @@ __device__ __forceinline__ bool gemm_epilogue32_staged(const GemmArgs& g, const 
   const bool fits = m0 + 32 <= g.M && n0 + 32 <= g.N && (g.N % 4) == 0 && !g.Cacc && !g.Cf32 &&
                     (!g.dact || (reinterpret_cast<uintptr_t>(g.dact) & 15) == 0) &&
                     (!g.Dsilu || (reinterpret_cast<uintptr_t>(g.Dsilu) & 15) == 0) &&
+                    (!g.row_bias || (reinterpret_cast<uintptr_t>(g.row_bias) & 15) == 0) &&
                     (!g.Hbf16 || ((g.ldh % 8) == 0 && (reinterpret_cast<uintptr_t>(g.Hbf16) & 15) == 0));
   if (!fits) return false;
   float z[32];
@@ -97,6 +98,14 @@ __device__ __forceinline__ bool gemm_epilogue32_staged(const GemmArgs& g, const 
   if (g.bias) {
 #pragma unroll
     for (int i = 0; i < 32; i++) z[i] += g.bias[n0 + i];
+  }
+  if (g.row_bias) {
+    const float4* rb = reinterpret_cast<const float4*>(g.row_bias + (long long)g.row_group[m0 + lane] * g.N + n0);
+#pragma unroll
+    for (int i = 0; i < 8; i++) {
+      const float4 b = rb[i];
+      z[4 * i] += b.x, z[4 * i + 1] += b.y, z[4 * i + 2] += b.z, z[4 * i + 3] += b.w;
+    }
   }
   // row segments of 32 floats: lane l moves 16 bytes of row 4k + l / 8
   const int rq = lane >> 3, c4 = 4 * (lane & 7);
@@ -171,6 +180,12 @@ __device__ __forceinline__ void gemm_epilogue32(const GemmArgs& g, const uint32_
 #pragma unroll
       for (int i = 0; i < 8; i++)
         if (nb + i < g.N) z[i] += g.bias[nb + i];
+    }
+    if (g.row_bias) {
+      const float* rb = g.row_bias + (long long)g.row_group[m] * g.N;
+#pragma unroll
+      for (int i = 0; i < 8; i++)
+        if (nb + i < g.N) z[i] += rb[nb + i];
     }
     if (g.dact) {
       const float* src = g.dact + (long long)m * g.N + nb;

@@ -193,6 +193,59 @@ __global__ void k_gather_batch(long long n, unsigned long long seed, float node_
   for (int c = 0; c < 3; c++) target[i * 3 + c] = src[kMlpCoords + c];
 }
 
+// Conditioned batches: the group (atmosphere) of row i is drawn uniformly,
+// then the row from that group's pool A (table nodes) or pool B (direct
+// samples) as k_gather_batch does.
+__global__ void k_gather_batch_groups(long long n, unsigned long long seed, float node_frac, int groups,
+                                      const float* const* __restrict__ poolsA, long long na,
+                                      const float* const* __restrict__ poolsB, long long nb,
+                                      float* __restrict__ coords, float* __restrict__ target,
+                                      int* __restrict__ group) {
+  const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const unsigned long long h = mix64(seed ^ (unsigned long long)i * 0x2545F4914F6CDD1Dull);
+  const int a = (int)(mix64(h + 2) % (unsigned long long)groups);
+  const bool fromA = nb == 0 || ((h >> 40) & 0xFFFFFF) < (unsigned long long)(node_frac * 16777216.0f);
+  const float* src = fromA ? poolsA[a] + kPoolRow * (long long)(mix64(h) % (unsigned long long)na)
+                           : poolsB[a] + kPoolRow * (long long)(mix64(h + 1) % (unsigned long long)nb);
+#pragma unroll
+  for (int c = 0; c < kMlpCoords; c++) coords[i * kMlpCoords + c] = src[c];
+#pragma unroll
+  for (int c = 0; c < 3; c++) target[i * 3 + c] = src[kMlpCoords + c];
+  group[i] = a;
+}
+
+// C[a][j] = b1[j] + sum_p U[j][p] G[a][p]: one thread per (a, j).
+__global__ void k_cond_bias(int groups, const float* __restrict__ U, const float* __restrict__ G,
+                            const float* __restrict__ b1, float* __restrict__ C) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= groups * kMlpHidden) return;
+  const int a = t / kMlpHidden, j = t % kMlpHidden;
+  float z = b1 ? b1[j] : 0.0f;
+#pragma unroll
+  for (int p = 0; p < kCondInputs; p++) z = fmaf(U[j * kCondInputs + p], G[a * kCondInputs + p], z);
+  C[t] = z;
+}
+
+// dU[j][p] += sum_a s_a G[a][p] with s_a = sum over the rows i of group a of
+// dZT[j][i]: one block per hidden unit j, the per-group sums in shared memory.
+__global__ void k_cond_grad(long long n, const __nv_bfloat16* __restrict__ dZT, const int* __restrict__ group,
+                            int groups, const float* __restrict__ G, float* __restrict__ dU) {
+  __shared__ float acc[kMaxCondGroups];
+  const int j = blockIdx.x;
+  for (int a = threadIdx.x; a < groups; a += blockDim.x) acc[a] = 0.0f;
+  __syncthreads();
+  for (long long i = threadIdx.x; i < n; i += blockDim.x)
+    atomicAdd(&acc[group[i]], __bfloat162float(dZT[(long long)j * n + i]));
+  __syncthreads();
+  if (threadIdx.x < kCondInputs) {
+    const int p = threadIdx.x;
+    float s = 0.0f;
+    for (int a = 0; a < groups; a++) s = fmaf(acc[a], G[a * kCondInputs + p], s);
+    dU[j * kCondInputs + p] += s;
+  }
+}
+
 static inline unsigned grid_for(long long n, int blk) { return (unsigned)((n + blk - 1) / blk); }
 
 void launch_features(long long n, const float* coords, __nv_bfloat16* F, __nv_bfloat16* FT, cudaStream_t st) {
@@ -228,6 +281,20 @@ void launch_to_bf16(long long count, const float* w, int rows, int cols, __nv_bf
 void launch_gather_batch(long long n, unsigned long long seed, float node_frac, const float* poolA, long long na,
                          const float* poolB, long long nb, float* coords, float* target, cudaStream_t st) {
   k_gather_batch<<<grid_for(n, 256), 256, 0, st>>>(n, seed, node_frac, poolA, na, poolB, nb, coords, target);
+}
+
+void launch_gather_batch_groups(long long n, unsigned long long seed, float node_frac, int groups,
+                                const float* const* poolsA, long long na, const float* const* poolsB, long long nb,
+                                float* coords, float* target, int* group, cudaStream_t st) {
+  k_gather_batch_groups<<<grid_for(n, 256), 256, 0, st>>>(n, seed, node_frac, groups, poolsA, na, poolsB, nb, coords,
+                                                          target, group);
+}
+void launch_cond_bias(int groups, const float* U, const float* G, const float* b1, float* C, cudaStream_t st) {
+  k_cond_bias<<<grid_for((long long)groups * kMlpHidden, 256), 256, 0, st>>>(groups, U, G, b1, C);
+}
+void launch_cond_grad(long long n, const __nv_bfloat16* dZT, const int* group, int groups, const float* G, float* dU,
+                      cudaStream_t st) {
+  k_cond_grad<<<kMlpHidden, 256, 0, st>>>(n, dZT, group, groups, G, dU);
 }
 
 }  // namespace sfsim

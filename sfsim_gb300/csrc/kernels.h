@@ -196,6 +196,8 @@ struct GemmArgs {
   long long K;
   float alpha;
   const float* bias;  // [N] added after alpha, or NULL
+  const float* row_bias;  // [groups][N] added by row: row_bias[row_group[m]][n], or NULL
+  const int* row_group;   // [M] group of each row (with row_bias)
   const float* dact;  // [M][N] multiplier applied after the bias, or NULL
   float* Cf32;        // [M][ldc] or NULL
   long long ldc;
@@ -266,6 +268,24 @@ void launch_to_bf16(long long count, const float* w, int rows, int cols, __nv_bf
                     cudaStream_t st);
 void launch_gather_batch(long long n, unsigned long long seed, float node_frac, const float* poolA, long long na,
                          const float* poolB, long long nb, float* coords, float* target, cudaStream_t st);
+
+// ---- conditioned surrogate: kCondInputs atmosphere inputs per group ----
+// The inputs enter the first layer linearly: z1 = W1 F + b1 + U g, U
+// [kMlpHidden][kCondInputs], so per group of rows (one atmosphere) U g is a
+// constant row bias.
+constexpr int kCondInputs = 8;
+constexpr int kMaxCondGroups = 256;
+// C[a][j] = (b1 ? b1[j] : 0) + sum_p U[j][p] G[a][p], a < groups.
+void launch_cond_bias(int groups, const float* U, const float* G, const float* b1, float* C, cudaStream_t st);
+// dU[j][p] += sum_a (sum_{i: group[i] = a} dZT[j][i]) G[a][p].
+void launch_cond_grad(long long n, const __nv_bfloat16* dZT, const int* group, int groups, const float* G, float* dU,
+                      cudaStream_t st);
+// Batch of n rows from `groups` pairs of pools (poolsA[a]: na rows,
+// poolsB[a]: nb rows; device arrays of device pointers): each row picks its
+// group uniformly, then pool A with probability node_frac; group[i] records it.
+void launch_gather_batch_groups(long long n, unsigned long long seed, float node_frac, int groups,
+                                const float* const* poolsA, long long na, const float* const* poolsB, long long nb,
+                                float* coords, float* target, int* group, cudaStream_t st);
 
 // ---- cloud-noise builders (k_noise.cu) ----
 // max_bits (one uint, zeroed) and range (two uints: 0xFFFFFFFF, 0) are scratch.

@@ -6,6 +6,7 @@ methods take and return torch CUDA tensors of shape [n, 3]:
   table(kind, a, b, light)  the lookups sfsim's shaders perform
                             (resources/shaders/atmosphere/*.glsl)
   direct(x, v, l)           rendered in-scatter S + M phase by direct quadrature
+`ConditionedSurrogate` is one surrogate network for a family of atmospheres.
 """
 from __future__ import annotations
 
@@ -166,6 +167,95 @@ class Context:
         _lib.check(self._L.sfsim_atmo_query_direct(self._ptr, n, x.data_ptr(), v.data_ptr(), l.data_ptr(),
                                                    out.data_ptr(), st), "query_direct")
         return out
+
+
+def condition_inputs(cfg: AtmoConfig):
+    """The conditioned surrogate's eight inputs of an atmosphere (numpy float32)."""
+    import numpy as np
+    L = _lib.load()
+    out = np.zeros(8, np.float32)
+    _lib.check(L.sfsim_atmo_condition_inputs(ctypes.byref(cfg), out.ctypes.data), "condition_inputs")
+    return out
+
+
+class ConditionedSurrogate:
+    """One surrogate network for a family of atmospheres: the eight inputs of
+    `condition_inputs` join the first layer.  `train(contexts, ...)` trains it on
+    several built atmospheres; `query(ctx, x, v, l)` corrects any context's
+    table lookup (torch CUDA tensors in and out, as Context.surrogate)."""
+
+    def __init__(self, seed: int = 1):
+        self._L = _lib.load()
+        self._ptr = ctypes.c_void_p()
+        _lib.check(self._L.sfsim_atmo_cond_surrogate_create(seed, ctypes.byref(self._ptr)), "cond_surrogate_create")
+
+    def close(self):
+        if self._ptr:
+            self._L.sfsim_atmo_cond_surrogate_destroy(self._ptr)
+            self._ptr = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def train(self, contexts, steps=2000, batch=65536, direct_samples=1 << 18, node_fraction=0.0, lr=1e-3, seed=1,
+              huber_delta=0.0):
+        """Trains on the contexts (a list of Context sharing one ray-scatter
+        shape; direct_samples per context); returns the per-step losses."""
+        import numpy as np
+        c = _lib.SurrogateConfig(steps, batch, direct_samples, node_fraction, lr, seed, huber_delta)
+        arr = (ctypes.c_void_p * len(contexts))(*[ctx._ptr.value for ctx in contexts])
+        hist = np.zeros(max(steps, 1), np.float32)
+        _lib.check(self._L.sfsim_atmo_cond_surrogate_train(self._ptr, arr, len(contexts), ctypes.byref(c),
+                                                           hist.ctypes.data), "cond_surrogate_train")
+        return hist[:steps]
+
+    def parameters(self, set_to=None):
+        import numpy as np
+        n = ctypes.c_longlong()
+        _lib.check(self._L.sfsim_atmo_cond_surrogate_parameters(self._ptr, None, None, ctypes.byref(n)), "parameters")
+        out = np.zeros(n.value, np.float32)
+        src = None
+        if set_to is not None:
+            src = np.ascontiguousarray(set_to, dtype=np.float32)
+            assert src.size == n.value
+        _lib.check(self._L.sfsim_atmo_cond_surrogate_parameters(self._ptr, out.ctypes.data,
+                                                                src.ctypes.data if src is not None else None,
+                                                                ctypes.byref(n)), "parameters")
+        return out
+
+    def gradients(self, coords, groups, inputs, targets):
+        """Loss and parameter gradients of one batch (numpy in, numpy out)."""
+        import numpy as np
+        coords = np.ascontiguousarray(coords, dtype=np.float32)
+        groups = np.ascontiguousarray(groups, dtype=np.int32)
+        inputs = np.ascontiguousarray(inputs, dtype=np.float32)
+        targets = np.ascontiguousarray(targets, dtype=np.float32)
+        grads = np.zeros(self.parameters().size, np.float32)
+        loss = np.zeros(1, np.float32)
+        _lib.check(self._L.sfsim_atmo_cond_surrogate_gradients(self._ptr, coords.shape[0], coords.ctypes.data,
+                                                               groups.ctypes.data, inputs.shape[0], inputs.ctypes.data,
+                                                               targets.ctypes.data, loss.ctypes.data,
+                                                               grads.ctypes.data), "cond_gradients")
+        return float(loss[0]), grads
+
+    def query(self, ctx, x, v, l, threshold=0.0, out=None):
+        """Rendered in-scatter of ctx's atmosphere from its table lookup
+        corrected by the network; returns (out, number recomputed)."""
+        import torch
+        x = x.contiguous().double()
+        v = v.contiguous().double()
+        l = l.contiguous().double()
+        n = x.shape[0]
+        out = out if out is not None else torch.empty((n, 3), dtype=torch.float32, device="cuda")
+        nf = ctypes.c_longlong()
+        st = torch.cuda.current_stream().cuda_stream
+        _lib.check(self._L.sfsim_atmo_query_cond_surrogate(self._ptr, ctx._ptr, n, x.data_ptr(), v.data_ptr(),
+                                                           l.data_ptr(), out.data_ptr(), threshold, ctypes.byref(nf),
+                                                           st), "query_cond_surrogate")
+        return out, nf.value
 
 
 def _cuda_copy(dst: int, src: int, nbytes: int) -> None:

@@ -55,10 +55,25 @@ def dsilu(z):
     return s * (1 + z * (1 - s))
 
 
-def loss_and_grads(params, coords, targets, var_weight=VAR_WEIGHT):
+N_COND = 8  # atmosphere inputs of the conditioned network
+
+
+def cond_term(params, groups, inputs):
+    """First-layer term U g of each row of a conditioned network (U [256][8]
+    after the plain parameters), or 0 for a plain parameter vector."""
+    n_plain = sum(r * c + r for (r, c) in SHAPES)
+    if params.size == n_plain:
+        return 0.0
+    U = params[n_plain:].reshape(N_HID, N_COND).astype(np.float64)
+    return inputs.astype(np.float64)[groups] @ U.T
+
+
+def loss_and_grads(params, coords, targets, var_weight=VAR_WEIGHT, groups=None, inputs=None):
     """Mean squared error of the corrections (the reported loss) with the
     Gaussian negative log-likelihood of the squared error under the predicted
-    variance exp(s) added to the gradients, weighted by var_weight."""
+    variance exp(s) added to the gradients, weighted by var_weight.  With
+    `groups` and `inputs` the network is the conditioned one: row i adds
+    U inputs[groups[i]] to the first layer."""
     layers = unpack(params)
     n = coords.shape[0]
     H = [bf16(features(coords))]
@@ -66,6 +81,8 @@ def loss_and_grads(params, coords, targets, var_weight=VAR_WEIGHT):
     for l in range(4):
         W, b = layers[l]
         z = H[-1] @ bf16(W).T + b
+        if l == 0 and groups is not None:
+            z = z + cond_term(params, groups, inputs)
         Z.append(z)
         H.append(bf16(silu(z)))
     W5, b5 = layers[4]
@@ -81,26 +98,34 @@ def loss_and_grads(params, coords, targets, var_weight=VAR_WEIGHT):
     dZ = bf16((dout @ W5) * dsilu(Z[3]))
     g = [None] * 5
     g[4] = (dW5, db5)
+    dU = None
     for l in range(3, -1, -1):
         W, b = layers[l]
         dW = dZ.T @ H[l]
         db = dZ.sum(axis=0)
         g[l] = (dW, db)
+        if l == 0 and groups is not None:
+            dU = dZ.T @ inputs.astype(np.float64)[groups]
         if l > 0:
             dZ = bf16((dZ @ bf16(W)) * dsilu(Z[l - 1]))
     for (dW, db) in g:
         grads.append(dW.ravel())
         grads.append(db.ravel())
+    if dU is not None:
+        grads.append(dU.ravel())
     return loss, np.concatenate(grads)
 
 
-def forward(params, coords):
+def forward(params, coords, inputs=None):
     """Network outputs [n][4] (three corrections, log variance) for coords
-    [n][4], with the GPU's BF16 roundings."""
+    [n][4], with the GPU's BF16 roundings; `inputs` [8] are the atmosphere
+    inputs of a conditioned network."""
     layers = unpack(params)
     H = bf16(features(coords))
     for l in range(4):
         W, b = layers[l]
+        if l == 0 and inputs is not None:
+            b = b + cond_term(params, np.zeros(1, np.int64), np.asarray(inputs)[None, :])[0]
         H = bf16(silu(H @ bf16(W).T + b))
     W5, b5 = layers[4]
     return H @ W5.T + b5

@@ -98,3 +98,22 @@ def test_batch_layout_mismatch_rejected(lib):
     x = np.zeros(10, np.float32)
     p = x.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
     assert lib.sfsim_atmo_build_batch(arr, 2, p, p, p, p) == -1
+
+
+def test_condition_inputs(lib):
+    """The conditioned surrogate's atmosphere inputs (host-only): Earth's
+    coefficients give 0 in the coefficient inputs, the sweep's ranges map to
+    about [-1, 1]."""
+    from sfsim_gb300.query import condition_inputs
+    g = condition_inputs(C.production())
+    assert g.shape == (8,)
+    np.testing.assert_allclose(g[:4], 0.0, atol=1e-6)
+    np.testing.assert_allclose(g[4:], [0.0, (1200.0 - 1400.0) / 600.0, (0.76 - 0.725) / 0.125,
+                                       (6378e3 - 5e6) / 2e6], rtol=1e-6, atol=1e-6)
+    for cfg in C.parameter_sweep(64):
+        g = condition_inputs(cfg)
+        assert np.all(np.abs(g) <= 1.0 + 1e-5), g
+        ref = [np.log2(cfg.rayleigh.scatter_base[0] / 5.8e-6), np.log2(cfg.mie.scatter_base[0] / 2e-5),
+               (cfg.radius - 5e6) / 2e6]
+        np.testing.assert_allclose([g[0], g[3], g[7]], ref, rtol=1e-5, atol=1e-6)
+    assert lib.sfsim_atmo_condition_inputs(None, None) == -6
