@@ -516,17 +516,17 @@ __device__ __forceinline__ void sun_sums(Real q0, Real b, Real dt, int steps, co
   sum_m = (sm[0] + sm[1]) + (sm[2] + sm[3]);
 }
 
-// Same sums for a segment parameterised by u in [0, 1]:
-// q(u) = c0 + u (two_xd + u dd) with two_xd = 2 x.D, dd = D.D.
+// Same sums for a segment parameterised by u in [0, 1], with the height
+// coordinate written as q = A + w (B + w C) in w = u - u0: the samples are
+// w_n = w0 + n du.
 template <class Real, int NP>
-__device__ __forceinline__ void optical_sums_u(Real c0, Real two_xd, Real dd, Real du, int steps, const Real* c,
+__device__ __forceinline__ void optical_sums_w(Real A, Real B, Real C, Real w0, Real du, int steps, const Real* c,
                                                Real alpha, Real beta, Real kr, Real km, Real& sum_r, Real& sum_m) {
   Real sr = 0, cr = 0, sm = 0, cm = 0;
-  Real half = Real(0.5) * du;
   Real fn = 0;
   for (int n = 0; n < steps; n++) {
-    Real u = fma(fn, du, half);
-    Real q = fma(u, fma(u, dd, two_xd), c0);
+    Real w = fma(fn, du, w0);
+    Real q = fma(w, fma(w, C, B), A);
     Real h = height_from_q<Real, NP>(q, c, alpha, beta);
     Real er = Bulk<Real>::exp2(h * kr);
     Real em = Bulk<Real>::exp2(h * km);
@@ -536,6 +536,43 @@ __device__ __forceinline__ void optical_sums_u(Real c0, Real two_xd, Real dd, Re
   }
   sum_r = sr;
   sum_m = sm;
+}
+
+// q(u) = c0 + u (two_xd + u dd) with two_xd = 2 x.D, dd = D.D.
+template <class Real, int NP>
+__device__ __forceinline__ void optical_sums_u(Real c0, Real two_xd, Real dd, Real du, int steps, const Real* c,
+                                               Real alpha, Real beta, Real kr, Real km, Real& sum_r, Real& sum_m) {
+  optical_sums_w<Real, NP>(c0, two_xd, dd, Real(0.5) * du, du, steps, c, alpha, beta, kr, km, sum_r, sum_m);
+}
+
+// The height form of the segment x -> x + D from its FP64 invariants c0 =
+// |x|^2 - R^2, x.D and D.D.  Plain: q = c0 + u (2 x.D + u D.D).  About the
+// closest approach u* = -x.D / D.D: q = qmin + D.D (u - u*)^2 with qmin = c0 -
+// (x.D)^2 / D.D computed in FP64.  A grazing segment (|qmin| < c0) takes the
+// second form: the plain one rounds c0 and x.D to Real, an error of about
+// 1e-7 c0 in q at every sample, which near the tangent point is a height
+// offset of millimetres where the density is largest (a systematic 1e-5 in
+// the optical depth of a Mie-dense grazing ray); about u* the samples keep
+// their heights to 1e-7 of the height above qmin, and rounding u* only shifts
+// all samples together.  Steeper segments keep the plain form, which does not
+// cancel there.
+struct QForm {
+  double A, B, C, w0;
+};
+__device__ __forceinline__ QForm segment_q_form(double c0, double xD, double DD, double du) {
+  QForm f;
+  f.C = DD;
+  const double qmin = DD > 0.0 ? c0 - xD * xD / DD : c0;
+  if (DD > 0.0 && fabs(qmin) < c0) {
+    f.A = qmin;
+    f.B = 0.0;
+    f.w0 = 0.5 * du + xD / DD;  // u_0 - u* with u_0 = du / 2
+  } else {
+    f.A = c0;
+    f.B = 2.0 * xD;
+    f.w0 = 0.5 * du;
+  }
+  return f;
 }
 
 // Optical depth (RGB) of a segment from x to x + D with `steps` midpoint
@@ -549,8 +586,10 @@ __device__ inline void segment_depth_q(const AtmoParams& P, double c0, double xD
     tau[0] = tau[1] = tau[2] = 0;
     return;
   }
+  const double du = 1.0 / steps;
+  const QForm f = segment_q_form(c0, xD, DD, du);
   Real sr, sm;
-  optical_sums_u<Real, 5>((Real)c0, (Real)(2.0 * xD), (Real)DD, (Real)(1.0 / steps), steps, Bulk<Real>::hpoly(P),
+  optical_sums_w<Real, 5>((Real)f.A, (Real)f.B, (Real)f.C, (Real)f.w0, (Real)du, steps, Bulk<Real>::hpoly(P),
                           Bulk<Real>::alpha(P), Bulk<Real>::beta(P), Bulk<Real>::kr(P), Bulk<Real>::km(P), sr, sm);
   Real a = (Real)(L / steps);
 #pragma unroll
@@ -560,19 +599,8 @@ __device__ inline void segment_depth_q(const AtmoParams& P, double c0, double xD
 // The same for x and D in FP64.
 template <class Real>
 __device__ inline void segment_depth(const AtmoParams& P, d3 x, d3 D, int steps, Real tau[3]) {
-  double L = mag3(D);
-  if (!(L > 0.0)) {
-    tau[0] = tau[1] = tau[2] = 0;
-    return;
-  }
-  double c0 = (mag3(x) - P.R) * (mag3(x) + P.R);
-  Real sr, sm;
-  optical_sums_u<Real, 5>((Real)c0, (Real)(2.0 * dot3(x, D)), (Real)dot3(D, D), (Real)(1.0 / steps), steps,
-                          Bulk<Real>::hpoly(P), Bulk<Real>::alpha(P), Bulk<Real>::beta(P), Bulk<Real>::kr(P),
-                          Bulk<Real>::km(P), sr, sm);
-  Real a = (Real)(L / steps);
-#pragma unroll
-  for (int ch = 0; ch < 3; ch++) tau[ch] = a * (Bulk<Real>::ray_ext(P, ch) * sr + Bulk<Real>::mie_ext(P, ch) * sm);
+  const double c0 = (mag3(x) - P.R) * (mag3(x) + P.R);
+  segment_depth_q<Real>(P, c0, dot3(x, D), dot3(D, D), mag3(D), steps, tau);
 }
 
 template <class Real>

@@ -477,7 +477,21 @@ __global__ void __launch_bounds__(kSurfaceThreads) k_surface_radiance(const Atmo
         lq = aa < Real(0) ? (aa > bb * Real(-0.5) ? aa / bb : Real(-0.5)) : Real(0);
       }
     }
-    split_coord_r<Real>(scale1 * (Real(0.5) - lq), d.n1, &uu[1], &sx[1]);
+    {
+      // (n1 - 1)(1/2 - lq) with the exact base (n1 - 1)/2 split off: the
+      // fraction keeps the precision of the part above it, -(n1 - 1) lq,
+      // which is small for the rays near the horizon that carry the most
+      // light (in FP32 the whole coordinate near n1/2 resolves only ~1e-5 of
+      // a texel there, and the table is steep)
+      const Real t = ((d.n1 - 1) & 1 ? Real(0.5) : Real(0)) - scale1 * lq;
+      const Real ft = floor(t);
+      uu[1] = ((d.n1 - 1) >> 1) + (int)ft;
+      sx[1] = t - ft;
+      if (uu[1] >= d.n1 - 1) {
+        uu[1] = d.n1 - 1;
+        sx[1] = Real(0);
+      }
+    }
     const Real mu = fma(wx, lx, wy * ly);  // w.l, l.z = 0
     split_coord_r<Real>(scale3 * (Real(1) + mu), d.n3, &uu[3], &sx[3]);
     Real val[3];
