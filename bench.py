@@ -34,6 +34,9 @@ sys.path.insert(0, ROOT)
 
 METRIC = "LUT build s & ray-scatter queries/s: plain vs surrogate at stated rel err"
 UNIT = "ray-scatter cells/s (full multi-order LUT build)"
+# DRAM bytes read + written per k_point_scatter launch of the production
+# build, mean over its five launches (ncu, profiles/dram_traffic_production_build.md)
+PS_DRAM_BYTES_PER_LAUNCH = 89_700_000
 WORKLOAD = ("production LUT build: T 255x255, E 16x64, S/M 32x255x32x8 RGB, 5 iterations, "
             "128 ray steps, sphere steps 32 (336 directions), R 6378 km, H 100 km")
 
@@ -277,14 +280,16 @@ def run_ours(args):
             "stage_ms": {k: round(v, 4) for k, v in stages.items()},
             "roofline": {"bound": "smem", "kernel": "k_point_scatter", "achieved": ps_achieved,
                          "peak": smem_peak_g, "unit": "GB/s", "frac": ps_achieved / smem_peak_g if smem_peak_g else None,
-                         "traffic": None,
+                         "traffic": PS_DRAM_BYTES_PER_LAUNCH,
                          "note": ("achieved = algorithmic shared-memory gather bytes of the point-scatter stage "
                                   "(24 B per direction evaluation for the dS row, 24 B more in the first "
                                   "iteration, 48 B per ground direction, 24 B when one dE height row has all the "
                                   "weight; census counts) / its event time; peak = "
                                   "conflict-free shared-memory read bandwidth measured live on this GPU by "
                                   "sfsim_atmo_smem_peak (no such figure in MEASURED_PEAKS.json); DRAM is not "
-                                  "the bound (the tables live in L2)"),
+                                  "the bound (the tables live in L2); traffic = DRAM bytes read + written per "
+                                  "point-scatter launch, mean of the build's five launches in one ncu capture of "
+                                  "this workload (profiles/dram_traffic_production_build.md)"),
                          "direction_evaluations": dir_evals, "kernel_ms": ps_ms},
             "roofline_first_order": {"bound": "sfu", "kernel": "k_first_order", "achieved": fo_achieved,
                                      "peak": peak_g, "unit": "Gex2/s", "frac": fo_achieved / peak_g if peak_g else None,
