@@ -70,6 +70,38 @@ def test_validate_shapes(lib):
     assert lib.sfsim_atmo_validate(ctypes.byref(c)) == -1
 
 
+def test_validate_limits(lib):
+    """The remaining configuration checks, all on the host: a ray-scatter table
+    over 2^31 nodes, non-finite or negative physical values, surface radiance
+    without its ray_steps/4 rings, and the step limits."""
+    def code(**kw):
+        c = C.production()
+        for k, v in kw.items():
+            if k == "shape":
+                for i, x in enumerate(v):
+                    c.ray_scatter_shape[i] = x
+            elif k in ("mie_base", "ray_scale"):
+                if k == "mie_base":
+                    c.mie.scatter_base[0] = v
+                else:
+                    c.rayleigh.scatter_scale = v
+            else:
+                setattr(c, k, v)
+        return lib.sfsim_atmo_validate(ctypes.byref(c))
+    assert code() == 0
+    assert code(shape=(2048, 1024, 32, 33)) == -7          # 2^31 + 2^26 nodes
+    assert code(shape=(2048, 1024, 32, 32)) == 0           # exactly 2^31
+    assert code(radius=float("nan")) == -1
+    assert code(height=float("inf")) == -1
+    assert code(mie_base=-1e-6) == -1
+    assert code(ray_scale=0.0) == -1
+    assert code(ray_steps=3) == -1                         # iterations > 0 need 4 rings' worth
+    assert code(ray_steps=3, iterations=0) == 0
+    assert code(ray_steps=4097) == -1
+    assert code(sphere_steps=1025) == -1
+    assert code(iterations=65) == -1
+
+
 def test_null_outputs(lib):
     c = C.small_fp64()
     assert lib.sfsim_atmo_build(ctypes.byref(c), None, None, None, None) == -6

@@ -241,3 +241,18 @@ def test_sweep_fp32_vs_fp64():
     for key in ("transmittance", "surface_radiance", "ray_scatter", "mie_strength"):
         for n in range(64):
             assert_close(g32[key][n], g64[key][n], 1e-4, f"{key}[{n}]")
+
+
+def test_unsupported_shape_reported():
+    """A sun-elevation x heading plane too large for shared memory is refused
+    with SFSIM_ATMO_ESHAPE before anything is allocated or launched, and the
+    library stays usable."""
+    from sfsim_gb300 import _lib
+    cfg = C.small_fp64(precision=C.FP32)
+    for i, v in enumerate((4, 8, 64, 64)):
+        cfg.ray_scatter_shape[i] = v
+    with pytest.raises(_lib.AtmoError) as e:
+        A.build(cfg)
+    assert e.value.code == -5
+    ok = A.build(C.small_fp64(precision=C.FP32))
+    assert np.isfinite(ok["ray_scatter"]).all()
