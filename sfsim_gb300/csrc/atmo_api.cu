@@ -18,6 +18,8 @@
 namespace sfsim {
 template <class Real>
 size_t point_scatter_smem(const BuildDims& d, bool first);
+template <class Real>
+size_t ray_scatter_smem(const BuildDims& d);
 }
 
 using namespace sfsim;
@@ -298,7 +300,7 @@ template <class Real>
 int check_smem(const BuildDims& d) {
   if (point_scatter_smem<Real>(d, true) > kMaxSmem)
     return fail(SFSIM_ATMO_ESHAPE, "elevation x heading slab of point scatter exceeds shared memory");
-  if (sizeof(Real) * 3 * 16 * (size_t)d.n2 * d.n3 + 16 * 64 > kMaxSmem)
+  if (ray_scatter_smem<Real>(d) > kMaxSmem)
     return fail(SFSIM_ATMO_ESHAPE, "sun elevation x heading plane of ray scatter exceeds shared memory");
   return 0;
 }

@@ -751,14 +751,24 @@ __global__ void __launch_bounds__(256, ray_scatter_min_blocks(sizeof(Real)))
   }
 }
 
+constexpr int kRayChunk = 16;  // ray samples per chunk of k_ray_scatter
+
+// Dynamic shared memory of k_ray_scatter: the chunk's constants and one
+// plane of n2 x n3 RGB texels per sample.
+template <class Real>
+size_t ray_scatter_smem(const BuildDims& d) {
+  return ((sizeof(RayChunk<Real, kRayChunk>) + 15) & ~size_t(15)) +
+         sizeof(Real) * 3 * (size_t)kRayChunk * d.n2 * d.n3;
+}
+
 template <class Real>
 int launch_ray_scatter(const AtmoParams* params, const BuildDims& d, const RowInfo* rowinfo,
                        const RowSample<Real>* rows, const CellGeom<Real>* geom, const Remap4<Real>* remap,
                        const Real* J, Vec4<Real>* dS, cudaStream_t st) {
-  constexpr int CH = 16;
+  constexpr int CH = kRayChunk;
   const int ncell = d.n2 * d.n3;
   const int block = ncell >= 256 ? 256 : ((ncell + 31) / 32) * 32;
-  size_t smem = ((sizeof(RayChunk<Real, CH>) + 15) & ~size_t(15)) + sizeof(Real) * 3 * (size_t)CH * ncell;
+  const size_t smem = ray_scatter_smem<Real>(d);
   if (cudaFuncSetAttribute(k_ray_scatter<Real, CH>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
       cudaSuccess)
     return -1;
@@ -947,7 +957,8 @@ void launch_export(long long n, const Vec4<Real>* tab, float* out, cudaStream_t 
   template void launch_export<Real>(long long, const Vec4<Real>*, float*, cudaStream_t);                           \
   template void launch_add_to_sum<Real>(long long, int, const Real*, Vec4<float>*, bool, cudaStream_t);           \
   template void launch_export_planar<Real>(long long, int, const Real*, float*, cudaStream_t);                      \
-  template size_t point_scatter_smem<Real>(const BuildDims&, bool);
+  template size_t point_scatter_smem<Real>(const BuildDims&, bool);                                                 \
+  template size_t ray_scatter_smem<Real>(const BuildDims&);
 
 SFSIM_INSTANTIATE(float)
 SFSIM_INSTANTIATE(double)
