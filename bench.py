@@ -260,6 +260,7 @@ def run_ours(args):
     sweep = run_sweep(L, A, C) if args.extras else None
     queries = run_queries(C) if args.extras else None
     queries_cond = run_cond_queries(C) if args.extras else None
+    small_graph = run_small_graph(A, C) if args.extras else None
     noise_builders = run_noise() if args.extras else None
 
     if world > 1:
@@ -303,6 +304,7 @@ def run_ours(args):
             "sweep": sweep,
             "queries": queries,
             "queries_conditioned": queries_cond,
+            "small_build_graph": small_graph,
             "noise": noise_builders,
         }
         print(json.dumps(result), flush=True)
@@ -346,6 +348,47 @@ def run_sweep(L, A, C):
     return {"atmospheres": len(cfgs), "shape": list(cfgs[0].ray_scatter_shape), "iterations": cfgs[0].iterations,
             "device_s": dev_ms * 1e-3, "e2e_s": wall, "cells_per_s": len(cfgs) * n4 / (dev_ms * 1e-3),
             "err_vs_fp64": err}
+
+
+def run_small_graph(A, C, reps=200):
+    """The small FP64 and FP32 builds (8x16x8x4, 64 ray steps, 2 iterations),
+    where launch overhead matters: device time per build through
+    build_device, and through a plan's build captured once into a CUDA graph
+    and replayed (CUDA events around `reps` back-to-back builds)."""
+    import torch
+    out = {}
+    for name, prec in (("fp64", C.FP64), ("fp32", C.FP32)):
+        cfg = C.small_fp64(precision=prec)
+        tensors = [torch.empty(s, dtype=torch.float32, device="cuda") for s in A.table_shapes(cfg)]
+        plan = A.Plan(cfg)
+        side = torch.cuda.Stream()
+        side.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.stream(side):
+            for _ in range(3):
+                plan.build(tensors, stream=side)
+                A.build_device(cfg, tensors, stream=side)
+        torch.cuda.current_stream().wait_stream(side)
+        torch.cuda.synchronize()
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g):
+            plan.build(tensors, stream=torch.cuda.current_stream())
+        torch.cuda.synchronize()
+
+        def timed(fn):
+            s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            fn()
+            torch.cuda.synchronize()
+            s.record()
+            for _ in range(reps):
+                fn()
+            e.record()
+            torch.cuda.synchronize()
+            return s.elapsed_time(e) / reps
+        out[name] = {"build_device_ms": timed(lambda: A.build_device(cfg, tensors)),
+                     "graph_replay_ms": timed(g.replay), "reps": reps}
+        del g
+        plan.close()
+    return out
 
 
 def _random_queries(n, R, H, seed):

@@ -107,23 +107,38 @@ int sfsim_atmo_build_device(const sfsim_atmo_config* cfg, float* transmittance,
                             float* mie_strength, void* stream);
 
 /* As sfsim_atmo_build_device, but allocates nothing.  No counterpart in the
- * reference: it is for callers that cannot call cudaMalloc, such as code
- * inside a CUDA-graph capture, or engines whose own allocator owns all device
- * memory.  All scratch tables live in one static device array of 64 MiB
+ * reference: it is for callers that cannot call cudaMalloc, such as engines
+ * whose own allocator owns all device memory.  It copies the parameters and
+ * quadrature directions from host memory on every call, so a CUDA graph must
+ * not capture it (the captured copies would read host memory that no longer
+ * holds them); capture sfsim_atmo_plan_build instead.  All scratch tables
+ * live in one static device array of 64 MiB
  * (67108864 bytes) that every GPU loading the library holds until the process
  * exits; a configuration that needs more (roughly 3e5 ray-scatter cells in
  * FP32, half that in FP64; the small FP64 case and the 12^4 shader-test
  * tables fit, the production tables do not) is rejected with
  * SFSIM_ATMO_ETOOBIG and a message naming the bytes it needs.  Outputs are
  * DEVICE pointers, work is queued on `stream`, and the call returns once it is
- * queued.  The first call on a device looks up the array's device address
- * (cudaGetSymbolAddress); make that first call before any stream capture.
- * Every call uses the same array, so calls that overlap on the GPU (different
+ * queued.  Every call uses the same array, so calls that overlap on the GPU (different
  * streams, or different host threads) race and corrupt each other; order them
  * on one stream.  Stage timings are not recorded. */
 int sfsim_atmo_build_static(const sfsim_atmo_config* cfg, float* transmittance,
                             float* surface_radiance, float* ray_scatter,
                             float* mie_strength, void* stream);
+
+/* Plans: a build prepared once for one configuration on the current device
+ * (its scratch allocated, its parameters and quadrature directions uploaded;
+ * synchronous).  sfsim_atmo_plan_build then only launches kernels on
+ * `stream` into DEVICE outputs in the .scatter layout: no allocation, copy or
+ * synchronisation, so it may run inside a CUDA stream capture, and the
+ * captured graph rebuilds the tables on every launch.  Asynchronous.  Builds
+ * of one plan share its scratch: order them on one stream.  No counterpart in
+ * the reference. */
+typedef struct sfsim_atmo_plan sfsim_atmo_plan;
+int sfsim_atmo_plan_create(const sfsim_atmo_config* cfg, sfsim_atmo_plan** plan);
+int sfsim_atmo_plan_build(sfsim_atmo_plan* plan, float* transmittance, float* surface_radiance,
+                          float* ray_scatter, float* mie_strength, void* stream);
+int sfsim_atmo_plan_destroy(sfsim_atmo_plan* plan);
 
 /* Builds `n` independent atmospheres that share shapes, steps, iterations and
  * precision (they may differ in every physical parameter) in one pass of

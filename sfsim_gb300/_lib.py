@@ -29,7 +29,7 @@ EXPORTS = (
     "sfsim_atmo_query_coords", "sfsim_atmo_smem_peak", "sfsim_noise_worley", "sfsim_noise_perlin", "sfsim_noise_blue",
     "sfsim_atmo_condition_inputs", "sfsim_atmo_cond_surrogate_create", "sfsim_atmo_cond_surrogate_destroy",
     "sfsim_atmo_cond_surrogate_train", "sfsim_atmo_cond_surrogate_parameters", "sfsim_atmo_cond_surrogate_gradients",
-    "sfsim_atmo_query_cond_surrogate",
+    "sfsim_atmo_query_cond_surrogate", "sfsim_atmo_plan_create", "sfsim_atmo_plan_build", "sfsim_atmo_plan_destroy",
 )
 
 
@@ -101,6 +101,9 @@ def load(build: bool = False):
                                              ctypes.POINTER(ctypes.c_longlong), vp]
     L.sfsim_atmo_query_coords.argtypes = [vp, ctypes.c_longlong, vp, vp, vp, vp, vp]
     L.sfsim_atmo_condition_inputs.argtypes = [_cfgp, vp]
+    L.sfsim_atmo_plan_create.argtypes = [_cfgp, ctypes.POINTER(vp)]
+    L.sfsim_atmo_plan_build.argtypes = [vp, vp, vp, vp, vp, vp]
+    L.sfsim_atmo_plan_destroy.argtypes = [vp]
     L.sfsim_atmo_cond_surrogate_create.argtypes = [ctypes.c_ulonglong, ctypes.POINTER(vp)]
     L.sfsim_atmo_cond_surrogate_destroy.argtypes = [vp]
     L.sfsim_atmo_cond_surrogate_train.argtypes = [vp, vp, ctypes.c_int, ctypes.POINTER(SurrogateConfig), vp]

@@ -88,6 +88,38 @@ def build_device(cfg: AtmoConfig, tensors=None, stream=None):
     return tensors
 
 
+class Plan:
+    """A build prepared once (sfsim_atmo_plan_*): `build(tensors, stream)`
+    only launches kernels, so it can be captured into a torch CUDA graph and
+    replayed."""
+
+    def __init__(self, cfg: AtmoConfig):
+        self.cfg = cfg.copy()
+        self._L = _lib.load()
+        self._ptr = ctypes.c_void_p()
+        _lib.check(self._L.sfsim_atmo_plan_create(ctypes.byref(self.cfg), ctypes.byref(self._ptr)), "plan_create")
+
+    def build(self, tensors=None, stream=None):
+        import torch
+        if tensors is None:
+            tensors = [torch.empty(s, dtype=torch.float32, device="cuda") for s in table_shapes(self.cfg)]
+        st = stream if stream is not None else torch.cuda.current_stream()
+        _lib.check(self._L.sfsim_atmo_plan_build(self._ptr, *[t.data_ptr() for t in tensors],
+                                                 ctypes.c_void_p(st.cuda_stream)), "plan_build")
+        return tensors
+
+    def close(self):
+        if self._ptr:
+            self._L.sfsim_atmo_plan_destroy(self._ptr)
+            self._ptr = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 def spit_floats(path: str, data: np.ndarray) -> None:
     """util.clj:236-240: raw little-endian float32."""
     np.ascontiguousarray(data, dtype="<f4").tofile(path)

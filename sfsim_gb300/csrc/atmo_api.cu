@@ -1360,6 +1360,103 @@ int build_static_impl(const sfsim_atmo_config& cfg, float* T, float* E, float* S
 
 }  // namespace
 
+// ---------------------------------------------------------------------------
+// Plans: a build prepared once (scratch allocated, parameters and quadrature
+// directions uploaded) so that the build itself only launches kernels and can
+// be captured into a CUDA graph and replayed.
+// ---------------------------------------------------------------------------
+
+struct sfsim_atmo_plan {
+  int dev;
+  sfsim_atmo_config cfg;
+  BuildDims dims;
+  void* mem;
+  Work<float> wf;
+  Work<double> wd;
+};
+
+namespace {
+
+template <class Real>
+int plan_prepare(sfsim_atmo_plan* p, Work<Real>& w) {
+  int rc = 0;
+  const sfsim_atmo_config& cfg = p->cfg;
+  BuildDims d = make_dims(cfg, 1);
+  if ((rc = check_smem<Real>(d))) return rc;
+  AtmoParams hp;
+  if ((rc = make_params(cfg, hp))) return rc;
+  std::vector<DirLocal> dirs, hdirs;
+  sphere_directions(cfg.sphere_steps >> 1, cfg.sphere_steps, M_PI, dirs);
+  sphere_directions(cfg.ray_steps >> 2, cfg.ray_steps, M_PI / 2, hdirs);
+  const size_t bytes = carve<Real>(w, nullptr, d, false);
+  cudaError_t e = cudaMalloc(&p->mem, bytes);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    p->mem = nullptr;
+    return fail(SFSIM_ATMO_ENOMEM, std::string("cudaMalloc of the plan failed: ") + cudaGetErrorString(e));
+  }
+  carve<Real>(w, (char*)p->mem, d, false);
+  CUDA_TRY(cudaMemcpy(w.params, &hp, sizeof(AtmoParams), cudaMemcpyHostToDevice));
+  if (!dirs.empty()) CUDA_TRY(cudaMemcpy(w.dirs, dirs.data(), sizeof(DirLocal) * dirs.size(), cudaMemcpyHostToDevice));
+  if (!hdirs.empty())
+    CUDA_TRY(cudaMemcpy(w.hdirs, hdirs.data(), sizeof(DirLocal) * hdirs.size(), cudaMemcpyHostToDevice));
+  p->dims = d;
+  return 0;
+}
+
+}  // namespace
+
+extern "C" int sfsim_atmo_plan_create(const sfsim_atmo_config* cfg, sfsim_atmo_plan** out) {
+  if (!out) return fail(SFSIM_ATMO_ENULL, "out is NULL");
+  *out = nullptr;
+  int rc = validate(cfg);
+  if (rc) return rc;
+  std::lock_guard<std::mutex> lock(g_mutex);
+  int dev = 0;
+  if ((rc = current_device(&dev))) return rc;
+  if ((rc = ensure_stream(dev))) return rc;
+  sfsim_atmo_plan* p = new sfsim_atmo_plan();
+  p->dev = dev;
+  p->cfg = *cfg;
+  p->mem = nullptr;
+  rc = cfg->precision == SFSIM_ATMO_FP64 ? plan_prepare<double>(p, p->wd) : plan_prepare<float>(p, p->wf);
+  if (rc) {
+    if (p->mem) cudaFree(p->mem);
+    delete p;
+    return rc;
+  }
+  *out = p;
+  return 0;
+}
+
+extern "C" int sfsim_atmo_plan_build(sfsim_atmo_plan* p, float* T, float* E, float* S, float* M, void* stream) {
+  if (!p) return fail(SFSIM_ATMO_ENULL, "plan is NULL");
+  if (!T || !E || !S || !M) return fail(SFSIM_ATMO_ENULL, "an output pointer is NULL");
+  std::lock_guard<std::mutex> lock(g_mutex);
+  int cur = 0;
+  CUDA_TRY(cudaGetDevice(&cur));
+  if (cur != p->dev) return fail(SFSIM_ATMO_EINVAL, "the plan belongs to another device");
+  Timer tm;
+  tm.dev = p->dev;
+  tm.st = (cudaStream_t)stream;
+  tm.n = 512;  // a full event list: no stage timings, nothing but kernel launches
+  if (p->cfg.precision == SFSIM_ATMO_FP64)
+    return run_build<double>(p->wd, p->dims, T, E, S, M, (cudaStream_t)stream, tm, nullptr);
+  return run_build<float>(p->wf, p->dims, T, E, S, M, (cudaStream_t)stream, tm, nullptr);
+}
+
+extern "C" int sfsim_atmo_plan_destroy(sfsim_atmo_plan* p) {
+  if (!p) return 0;
+  int cur = 0;
+  cudaGetDevice(&cur);
+  cudaSetDevice(p->dev);
+  cudaError_t e = p->mem ? cudaFree(p->mem) : cudaSuccess;
+  cudaSetDevice(cur);
+  delete p;
+  if (e != cudaSuccess) return fail(SFSIM_ATMO_ECUDA, std::string("cudaFree: ") + cudaGetErrorString(e));
+  return 0;
+}
+
 extern "C" int sfsim_atmo_build_static(const sfsim_atmo_config* cfg, float* T, float* E, float* S, float* M,
                                        void* stream) {
   int rc = validate(cfg);
