@@ -83,6 +83,7 @@ constexpr int kGemmStageWords = 32 * 33;
 // SiLU' input is read, and the SiLU' and BF16 row-major outputs written, a
 // whole row segment at a time through the warp's staging tile.  Returns
 // false (nothing done) when the block does not qualify.
+template <bool ROWB>
 __device__ __forceinline__ bool gemm_epilogue32_staged(const GemmArgs& g, const uint32_t* r, int m0, int n0,
                                                        float* sg) {
   const int lane = threadIdx.x & 31;
@@ -99,7 +100,7 @@ __device__ __forceinline__ bool gemm_epilogue32_staged(const GemmArgs& g, const 
 #pragma unroll
     for (int i = 0; i < 32; i++) z[i] += g.bias[n0 + i];
   }
-  if (g.row_bias) {
+  if (ROWB) {
     const float4* rb = reinterpret_cast<const float4*>(g.row_bias + (long long)g.row_group[m0 + lane] * g.N + n0);
 #pragma unroll
     for (int i = 0; i < 8; i++) {
@@ -165,6 +166,7 @@ __device__ __forceinline__ bool gemm_epilogue32_staged(const GemmArgs& g, const 
 }
 
 // 32 columns of the epilogue for row m, columns n0 .. n0 + 31.
+template <bool ROWB>
 __device__ __forceinline__ void gemm_epilogue32(const GemmArgs& g, const uint32_t* r, int m, int n0) {
   const bool row_ok = m < g.M;
   if (!row_ok) return;
@@ -181,7 +183,7 @@ __device__ __forceinline__ void gemm_epilogue32(const GemmArgs& g, const uint32_
       for (int i = 0; i < 8; i++)
         if (nb + i < g.N) z[i] += g.bias[nb + i];
     }
-    if (g.row_bias) {
+    if (ROWB) {
       const float* rb = g.row_bias + (long long)g.row_group[m] * g.N;
 #pragma unroll
       for (int i = 0; i < 8; i++)
@@ -250,6 +252,9 @@ __device__ __forceinline__ void gemm_epilogue32(const GemmArgs& g, const uint32_
   }
 }
 
+// ROWB: the epilogue adds the per-row-group bias (the conditioned surrogate's
+// first layer); a separate instantiation keeps the other GEMMs' registers.
+template <bool ROWB>
 __global__ void __launch_bounds__(kGemmThreads, 1)
     k_gemm_tn(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB, GemmKernelArgs a) {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
@@ -373,7 +378,8 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
       const int m0 = tm * 128 + q * 32;
       float* sg = staging + (warp - 2) * kGemmStageWords;
       auto epilogue = [&](const uint32_t* r, int n0) {
-        if (!__all_sync(0xffffffffu, gemm_epilogue32_staged(a.g, r, m0, n0, sg))) gemm_epilogue32(a.g, r, m, n0);
+        if (!__all_sync(0xffffffffu, gemm_epilogue32_staged<ROWB>(a.g, r, m0, n0, sg)))
+          gemm_epilogue32<ROWB>(a.g, r, m, n0);
       };
       const uint32_t trow = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(b * ncols);
       const int nall = (a.nt + 31) / 32, nh = (nall + 1) / 2;
@@ -464,14 +470,16 @@ int launch_gemm_tn(const GemmArgs& g, int splits, cudaStream_t st) {
   size_t smem = 1024 + (size_t)a.stages * stage_bytes + 1024 + staging;
   // two 256-column accumulators take all of an SM's tensor memory: one CTA per SM
   if (a.nt > 128) smem = std::max<size_t>(smem, 120 * 1024);
-  if (cudaFuncSetAttribute(k_gemm_tn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+  if (g.row_bias && !g.row_group) return -1;
+  auto* kernel = g.row_bias ? k_gemm_tn<true> : k_gemm_tn<false>;
+  if (cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
     return -1;
   int dev = 0, sms = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
     return -1;
   const long long ntiles = (long long)a.tiles_m * splits;
   const unsigned grid = (unsigned)std::min<long long>(ntiles, sms);
-  k_gemm_tn<<<grid, kGemmThreads, smem, st>>>(mapA, mapB, a);
+  kernel<<<grid, kGemmThreads, smem, st>>>(mapA, mapB, a);
   return 0;
 }
 
