@@ -540,7 +540,7 @@ def run_queries(C, steps=20000, batch=65536, direct_samples=1 << 25, lr=3e-3, hu
 
 
 def run_cond_queries(C, n_train=32, n_held_out=8, steps=10000, batch=65536, direct_samples=1 << 20, lr=3e-3,
-                     huber_delta=0.02, threshold=3e-2):
+                     huber_delta=0.02, thresholds=(3e-2, 1e-3)):
     """The conditioned surrogate: trained on 32 atmospheres of the parameter
     sweep (tables 16x128x16x8, 4 iterations; 2^20 direct samples each, 2^25 in
     all), queried on 8 held-out atmospheres drawn from the same distribution
@@ -566,9 +566,12 @@ def run_cond_queries(C, n_train=32, n_held_out=8, steps=10000, batch=65536, dire
     for c in train_ctx:
         c.close()
     n = 1 << 21
-    ms = {"table": 0.0, "direct": 0.0, "surrogate": 0.0, "fallback": 0.0}
-    parts = {"table": [], "direct": [], "surrogate": [], "fallback": []}
-    flagged = 0
+    ms = {"table": 0.0, "direct": 0.0, "surrogate": 0.0}
+    parts = {"table": [], "direct": [], "surrogate": []}
+    for thr in thresholds:
+        ms[thr] = 0.0
+        parts[thr] = []
+    flagged = {thr: 0 for thr in thresholds}
     for k, cfg in enumerate(held_cfgs):
         ctx = Context(cfg)
         x, v, l = _random_queries(n, cfg.radius, cfg.height, 100 + k)
@@ -583,26 +586,29 @@ def run_cond_queries(C, n_train=32, n_held_out=8, steps=10000, batch=65536, dire
         t, (r, _) = _timed(lambda: cs.query(ctx, x, v, l, out=out))
         ms["surrogate"] += t
         parts["surrogate"].append(r.clone())
-        t, (r, nf) = _timed(lambda: cs.query(ctx, x, v, l, threshold=threshold, out=out), reps=1)
-        ms["fallback"] += t
-        parts["fallback"].append(r.clone())
-        flagged += nf
+        for thr in thresholds:
+            t, (r, nf) = _timed(lambda: cs.query(ctx, x, v, l, threshold=thr, out=out), reps=1)
+            ms[thr] += t
+            parts[thr].append(r.clone())
+            flagged[thr] += nf
         ctx.close()
     cat = {k: torch.cat(v) for k, v in parts.items()}
     total = n * len(held_cfgs)
     qps = lambda t: total / (t * 1e-3)  # noqa: E731
     cs.close()
-    return {"train_atmospheres": n_train, "held_out_atmospheres": n_held_out, "shape": list(train_cfgs[0].ray_scatter_shape),
+    r = {"train_atmospheres": n_train, "held_out_atmospheres": n_held_out, "shape": list(train_cfgs[0].ray_scatter_shape),
             "n": total, "train_steps": steps, "train_batch": batch, "direct_samples": direct_samples * n_train,
             "lr": lr, "huber_delta": huber_delta, "context_builds_s": build_s, "train_s": train_s,
             "train_loss_first": float(hist[:10].mean()), "train_loss_last": float(hist[-100:].mean()),
             "table": {"qps": qps(ms["table"]), "err": query_error_stats(cat["table"], cat["direct"])},
             "direct": {"qps": qps(ms["direct"])},
             "surrogate": {"qps": qps(ms["surrogate"]), "err": query_error_stats(cat["surrogate"], cat["direct"]),
-                          "vs_direct": ms["direct"] / ms["surrogate"]},
-            f"surrogate_fallback_{threshold:g}": {"qps": qps(ms["fallback"]), "fallback_fraction": flagged / total,
-                                                  "err": query_error_stats(cat["fallback"], cat["direct"]),
-                                                  "vs_direct": ms["direct"] / ms["fallback"]}}
+                          "vs_direct": ms["direct"] / ms["surrogate"]}}
+    for thr in thresholds:
+        r[f"surrogate_fallback_{thr:g}"] = {"qps": qps(ms[thr]), "fallback_fraction": flagged[thr] / total,
+                                            "err": query_error_stats(cat[thr], cat["direct"]),
+                                            "vs_direct": ms["direct"] / ms[thr]}
+    return r
 
 
 # ---------------------------------------------------------------------------

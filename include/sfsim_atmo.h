@@ -227,12 +227,14 @@ int sfsim_atmo_query_coords(const sfsim_atmo_context* ctx, long long n, const do
                             const double* l, float* coords, void* stream);
 
 /* ---- Surrogate of the rendered in-scatter ----------------------------------
- * An MLP over the four table coordinates in [0, 1] (height, elevation, sun
- * elevation, sun heading, as the in-scatter lookup forms them): 16-frequency
- * sin/cos features per coordinate (128) -> 4 x 256 SiLU -> 3 outputs, the
- * log of (S + M phase + 1e-8).  BF16 weights and activations, FP32
- * accumulation and master weights; the hidden layers run on tcgen05 tensor
- * cores in the forward and both backward GEMMs.  No counterpart in the
+ * An MLP over ten coordinates in [0, 1] of a query (sfsim_atmo_query_coords:
+ * the four table coordinates as the in-scatter lookup forms them, the
+ * unclamped sun elevation, the table half and the four cell phases): sin/cos
+ * Fourier features (256) -> 4 x 256 SiLU -> 4 outputs, three log-space
+ * corrections to the table lookup and the log of their expected squared
+ * error (sfsim_atmo_surrogate_parameters).  BF16 weights and activations,
+ * FP32 accumulation and master weights; the hidden layers run on tcgen05
+ * tensor cores in the forward and both backward GEMMs.  No counterpart in the
  * reference. */
 typedef struct sfsim_atmo_surrogate_config {
   int steps;                /* Adam steps */

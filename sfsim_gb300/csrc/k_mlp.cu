@@ -1,9 +1,12 @@
 // k_mlp.cu -- CUDA-core kernels of the ray-scatter surrogate: a Fourier-
-// feature MLP over the four table coordinates (height, elevation, sun
-// elevation, sun heading; each in [0, 1]) with 4 x 256 SiLU hidden layers and
-// 3 log-RGB outputs.  The hidden-layer GEMMs run on the tensor cores
-// (k_gemm.cu); these kernels do the features, the 256 -> 3 head, the loss,
-// bias gradients, Adam and the sampling of training batches.
+// feature MLP over ten coordinates of a query (the four table coordinates,
+// the unclamped sun elevation, the table half and the four cell phases; each
+// in [0, 1]) with 4 x 256 SiLU hidden layers and 4 outputs (three log-space
+// corrections to the table lookup, the log of their expected squared error).
+// The hidden-layer GEMMs run on the tensor cores (k_gemm.cu); these kernels
+// do the features, the 256 -> 4 head, the loss, bias gradients, Adam, the
+// sampling of training batches, and the conditioned network's atmosphere
+// term.
 #include <cuda_bf16.h>
 
 #include "atmo_device.cuh"

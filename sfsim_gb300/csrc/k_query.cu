@@ -594,7 +594,7 @@ void launch_query_direct(const AtmoParams* params, const BuildDims& d, const Vec
 // quadrature.  The epilogue has 16 warps: two per group of 32 tensor-memory
 // lanes of each tile, one for each half of the columns (the second adds its
 // part of the head through shared memory).  Warp 16 is the producer: one thread
-// streams the 28 weight chunks of a group (256 rows x 32 K, 16 KB each,
+// streams the 32 weight chunks of a group (256 rows x 32 K, 16 KB each,
 // pre-packed in the tensor cores' layout) through a five-stage shared-memory
 // ring with bulk TMA copies, and issues the tcgen05.mma of both tiles on each
 // chunk (one weight fetch serves 256 queries) into two 128 x 256 FP32
@@ -608,7 +608,7 @@ constexpr int kInferKC = 32;                                          // K per w
 constexpr int kInferChunkBytes = kMlpHidden * kInferKC * 2;           // 16 KB
 constexpr int kInferChunks0 = kMlpIn / kInferKC;                      // layer 0
 constexpr int kInferChunksH = kMlpHidden / kInferKC;                  // hidden layers
-constexpr int kInferChunks = kInferChunks0 + 3 * kInferChunksH;       // 28 per group
+constexpr int kInferChunks = kInferChunks0 + 3 * kInferChunksH;       // 32 per group
 constexpr int kInferStages = 5;
 constexpr int kInferTileBytes = 128 * kMlpHidden * 2;                 // 64 KB
 constexpr int kInferEpilogueWarps = 16;  // 2 tiles x 4 lane quarters x 2 column halves
