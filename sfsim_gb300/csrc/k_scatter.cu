@@ -606,7 +606,7 @@ __global__ void __launch_bounds__(256, ray_scatter_min_blocks(sizeof(Real)))
     R2 acc[3] = {mk2(Real(0), Real(0)), mk2(Real(0), Real(0)), mk2(Real(0), Real(0))};
     // the plane build's cached J corners of the last even and odd samples
     Real ca[12], cb[12];
-    int key_a = -1, key_b = -1;
+    int key_a = -1, key_b = -1, a1 = -1, a2 = -1, b1 = -1, b2 = -1;  // keys and corners 1, 2 of the caches
     for (int sb = 0; sb < d.S; sb += CH) {
       const int nch = min(CH, d.S - sb);
       __syncthreads();
@@ -638,19 +638,54 @@ __global__ void __launch_bounds__(256, ray_scatter_min_blocks(sizeof(Real)))
             const bool two = ch + 1 < nch;
             const int ch1 = two ? ch + 1 : ch;
             const int pa = sc.p[0][ch], pb = sc.p[0][ch1];
-            auto load = [&](int s, Real (&v)[12]) {
-              const int q[4] = {sc.p[0][s], sc.p[1][s], sc.p[2][s], sc.p[3][s]};
+            // sample s's corners into v from the previous sample's cache src
+            // (offsets k0 = its key, k1, k2): a step of one cell along one
+            // axis carries two corners over, the other two are loaded
+            auto refill = [&](int s, Real (&v)[12], const Real (&src)[12], int k0, int k1, int k2, int& o1,
+                              int& o2) {
+              const int q0 = sc.p[0][s], q1 = sc.p[1][s], q2 = sc.p[2][s], q3 = sc.p[3][s];
+              const Real* tt = tJ + t;
+              if (q0 == k1) {  // elevation + 1: corners 1, 3 become 0, 2
 #pragma unroll
-              for (int c = 0; c < 3; c++)
+                for (int c = 0; c < 3; c++) {
+                  v[4 * c] = src[4 * c + 1], v[4 * c + 2] = src[4 * c + 3];
+                  v[4 * c + 1] = tt[c * n4 + q1], v[4 * c + 3] = tt[c * n4 + q3];
+                }
+              } else if (q1 == k0) {  // elevation - 1: corners 0, 2 become 1, 3
 #pragma unroll
-                for (int m = 0; m < 4; m++) v[4 * c + m] = tJ[c * n4 + t + q[m]];
+                for (int c = 0; c < 3; c++) {
+                  v[4 * c + 1] = src[4 * c], v[4 * c + 3] = src[4 * c + 2];
+                  v[4 * c] = tt[c * n4 + q0], v[4 * c + 2] = tt[c * n4 + q2];
+                }
+              } else if (q0 == k2) {  // height + 1: corners 2, 3 become 0, 1
+#pragma unroll
+                for (int c = 0; c < 3; c++) {
+                  v[4 * c] = src[4 * c + 2], v[4 * c + 1] = src[4 * c + 3];
+                  v[4 * c + 2] = tt[c * n4 + q2], v[4 * c + 3] = tt[c * n4 + q3];
+                }
+              } else if (q2 == k0) {  // height - 1: corners 0, 1 become 2, 3
+#pragma unroll
+                for (int c = 0; c < 3; c++) {
+                  v[4 * c + 2] = src[4 * c], v[4 * c + 3] = src[4 * c + 1];
+                  v[4 * c] = tt[c * n4 + q0], v[4 * c + 1] = tt[c * n4 + q1];
+                }
+              } else {
+#pragma unroll
+                for (int c = 0; c < 3; c++) {
+                  v[4 * c] = tt[c * n4 + q0], v[4 * c + 1] = tt[c * n4 + q1];
+                  v[4 * c + 2] = tt[c * n4 + q2], v[4 * c + 3] = tt[c * n4 + q3];
+                }
+              }
+              o1 = q1;
+              o2 = q2;
             };
             if (pa != key_a) {
               if (pa == key_b) {
 #pragma unroll
                 for (int m = 0; m < 12; m++) ca[m] = cb[m];
+                a1 = b1, a2 = b2;
               } else {
-                load(ch, ca);
+                refill(ch, ca, cb, key_b, b1, b2, a1, a2);
               }
               key_a = pa;
             }
@@ -658,8 +693,9 @@ __global__ void __launch_bounds__(256, ray_scatter_min_blocks(sizeof(Real)))
               if (pb == key_a) {
 #pragma unroll
                 for (int m = 0; m < 12; m++) cb[m] = ca[m];
+                b1 = a1, b2 = a2;
               } else {
-                load(ch1, cb);
+                refill(ch1, cb, ca, key_a, a1, a2, b1, b2);
               }
               key_b = pb;
             }
