@@ -318,6 +318,10 @@ constexpr int kMaxDevices = 64;
 Arena g_arena[kMaxDevices];
 cudaStream_t g_stream[kMaxDevices];
 cudaEvent_t g_events[kMaxDevices][2 * 512];
+// host-output builds: a second stream copies the transmittance and Mie
+// tables to the host while the scattering iterations still run
+cudaStream_t g_copy_stream[kMaxDevices];
+cudaEvent_t g_early_done[kMaxDevices];
 
 struct Carver {
   char* base;
@@ -421,6 +425,8 @@ int ensure_arena(int dev, size_t bytes) {
 
 int ensure_stream(int dev) {
   if (!g_stream[dev]) {
+    CUDA_TRY(cudaStreamCreateWithFlags(&g_copy_stream[dev], cudaStreamNonBlocking));
+    CUDA_TRY(cudaEventCreateWithFlags(&g_early_done[dev], cudaEventDisableTiming));
     CUDA_TRY(cudaStreamCreateWithFlags(&g_stream[dev], cudaStreamNonBlocking));
     for (int i = 0; i < 2 * 512; i++) CUDA_TRY(cudaEventCreate(&g_events[dev][i]));
   }
@@ -448,7 +454,8 @@ struct Timer {
 // device memory; outputs are device pointers in the .scatter layout.
 template <class Real>
 int run_build(const Work<Real>& w, const BuildDims& d, float* oT, float* oE, float* oS, float* oM, cudaStream_t st,
-              Timer& tm, const sfsim_atmo_intermediates* inter, Vec4<float>* jsum = nullptr) {
+              Timer& tm, const sfsim_atmo_intermediates* inter, Vec4<float>* jsum = nullptr,
+              cudaEvent_t early_done = nullptr) {
   int launches = 0;
   tm.mark_begin(0);
   launch_setup<Real>(w.params, d, w.dirs, w.hdirs, w.setup, st);
@@ -470,6 +477,14 @@ int run_build(const Work<Real>& w, const BuildDims& d, float* oT, float* oE, flo
   launch_first_order<Real>(w.params, d, w.setup.rowinfo, w.setup.rows, w.setup.geom, w.sun, w.S1R, w.M, st);
   launches++;
   tm.mark_end();
+  // the transmittance and Mie-strength tables are final here: their outputs
+  // (and, for host outputs, their copies) need not wait for the iterations
+  tm.mark_begin(9);
+  launch_output2<Real>(d.B, d.nT0, d.nT1, w.setup.remapT, w.T, oT, st);
+  launch_output4<Real>(d, w.setup.remapS, w.M, oM, st);
+  launches += 2;
+  tm.mark_end();
+  if (early_done) CUDA_TRY(cudaEventRecord(early_done, st));
   CUDA_TRY(cudaGetLastError());
   if (inter) {
     if (inter->transmittance_nodes) launch_export<Real>(d.B * d.nT(), w.T, inter->transmittance_nodes, st);
@@ -530,11 +545,9 @@ int run_build(const Work<Real>& w, const BuildDims& d, float* oT, float* oE, flo
     E_prev = E_new;
   }
   tm.mark_begin(9);
-  launch_output2<Real>(d.B, d.nT0, d.nT1, w.setup.remapT, w.T, oT, st);
   launch_output2<Real>(d.B, d.nE0, d.nE1, w.setup.remapE, E_prev, oE, st);
   launch_output4<Real>(d, w.setup.remapS, S_prev, oS, st);
-  launch_output4<Real>(d, w.setup.remapS, w.M, oM, st);
-  launches += 4;
+  launches += 2;
   tm.mark_end();
   CUDA_TRY(cudaGetLastError());
   g_launches = launches;
@@ -618,16 +631,23 @@ int build_impl(const sfsim_atmo_config* cfgs, int B, float* T, float* E, float* 
   tm.dev = dev;
   tm.st = st;
   float *dT = host_out ? w.oT : T, *dE = host_out ? w.oE : E, *dS = host_out ? w.oS : S, *dM = host_out ? w.oM : M;
-  rc = run_build<Real>(w, d, dT, dE, dS, dM, st, tm, inter ? &dinter : nullptr);
+  rc = run_build<Real>(w, d, dT, dE, dS, dM, st, tm, inter ? &dinter : nullptr, nullptr,
+                       host_out ? g_early_done[dev] : nullptr);
   if (rc) {
     if (staging) cudaFree(staging);
     return rc;
   }
   if (host_out) {
-    CUDA_TRY(cudaMemcpyAsync(T, w.oT, sizeof(float) * 3 * B * d.nT(), cudaMemcpyDeviceToHost, st));
+    // T and M copy on the second stream once their outputs are written (the
+    // whole build is queued first, so a copy into pageable memory, which
+    // blocks the host, cannot hold back the launches)
+    cudaStream_t cs = g_copy_stream[dev];
+    CUDA_TRY(cudaStreamWaitEvent(cs, g_early_done[dev], 0));
+    CUDA_TRY(cudaMemcpyAsync(T, w.oT, sizeof(float) * 3 * B * d.nT(), cudaMemcpyDeviceToHost, cs));
+    CUDA_TRY(cudaMemcpyAsync(M, w.oM, sizeof(float) * 3 * B * d.n4(), cudaMemcpyDeviceToHost, cs));
     CUDA_TRY(cudaMemcpyAsync(E, w.oE, sizeof(float) * 3 * B * d.nE(), cudaMemcpyDeviceToHost, st));
     CUDA_TRY(cudaMemcpyAsync(S, w.oS, sizeof(float) * 3 * B * d.n4(), cudaMemcpyDeviceToHost, st));
-    CUDA_TRY(cudaMemcpyAsync(M, w.oM, sizeof(float) * 3 * B * d.n4(), cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaStreamSynchronize(cs));
   }
   for (size_t i = 0; i < copies.size(); i++)
     CUDA_TRY(cudaMemcpyAsync(copies[i].second, copies[i].first, copy_bytes[i], cudaMemcpyDeviceToHost, st));
