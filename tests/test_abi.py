@@ -149,3 +149,21 @@ def test_condition_inputs(lib):
                (cfg.radius - 5e6) / 2e6]
         np.testing.assert_allclose([g[0], g[3], g[7]], ref, rtol=1e-5, atol=1e-6)
     assert lib.sfsim_atmo_condition_inputs(None, None) == -6
+
+
+def test_no_gpu_new_entry_points_report_enodev(lib):
+    """Plans and conditioned surrogates report ENODEV without a GPU, like the
+    builds, and leave their out-pointer NULL."""
+    torch = pytest.importorskip("torch")
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    c = C.small_fp64()
+    p = ctypes.c_void_p(1)
+    assert lib.sfsim_atmo_plan_create(ctypes.byref(c), ctypes.byref(p)) == -4
+    assert not p.value
+    q = ctypes.c_void_p(1)
+    assert lib.sfsim_atmo_cond_surrogate_create(1, ctypes.byref(q)) == -4
+    assert not q.value
+    assert lib.sfsim_atmo_plan_build(None, None, None, None, None, None) == -6
+    assert lib.sfsim_atmo_plan_destroy(None) == 0
+    assert lib.sfsim_atmo_cond_surrogate_destroy(None) == 0
