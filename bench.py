@@ -35,8 +35,11 @@ sys.path.insert(0, ROOT)
 METRIC = "LUT build s & ray-scatter queries/s: plain vs surrogate at stated rel err"
 UNIT = "ray-scatter cells/s (full multi-order LUT build)"
 # DRAM bytes read + written per k_point_scatter launch of the production
-# build, mean over its five launches (ncu, profiles/dram_traffic_production_build.md)
+# build, mean over its five launches in one ncu capture of this workload
+# (dram__bytes_read.sum + dram__bytes_write.sum); ncu does not run here, so the
+# figure is a recorded capture, not a measurement of this run
 PS_DRAM_BYTES_PER_LAUNCH = 89_700_000
+TABLES = ("transmittance", "surface_radiance", "ray_scatter", "mie_strength")
 WORKLOAD = ("production LUT build: T 255x255, E 16x64, S/M 32x255x32x8 RGB, 5 iterations, "
             "128 ray steps, sphere steps 32 (336 directions), R 6378 km, H 100 km")
 
@@ -134,6 +137,20 @@ def flush_l2(buf):
     buf.add_(1.0)
 
 
+def table_errors(got, ref):
+    """Max and mean relative error per table, |g - r| / max(|r|, 1e-6 max|r|)
+    (the floor keeps cells that are ~0 from dominating), as the parity tests
+    measure it."""
+    import numpy as np
+    out = {}
+    for k in TABLES:
+        g = np.asarray(got[k], dtype=np.float64)
+        r = np.asarray(ref[k], dtype=np.float64)
+        e = np.abs(g - r) / np.maximum(np.abs(r), 1e-6 * max(np.abs(r).max(), 1e-300))
+        out[k] = {"max": float(e.max()), "mean": float(e.mean())}
+    return out
+
+
 def run_ours(args):
     import torch
     import torch.distributed as dist
@@ -221,15 +238,17 @@ def run_ours(args):
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         e2e_s = float(t.item())
     e2e = world * n4 * args.steps / e2e_s
-    d2h = sum(t.numel() * 4 for t in host_out)
-    import numpy as np  # noqa: F401
-    params_bytes = 0
-    try:
-        # parameters and quadrature directions are the only host-to-device data
-        from sfsim_gb300.config import AtmoConfig  # noqa: F401
-        params_bytes = 1024 + 32 * (336 + 2 * 2608)
-    except Exception:
-        pass
+    # the bytes the library copied in the last build: parameters and
+    # quadrature directions in, the four tables out
+    h2d_b, d2h_b = ctypes.c_ulonglong(), ctypes.c_ulonglong()
+    _lib.check(L.sfsim_atmo_last_transfer_bytes(ctypes.byref(h2d_b), ctypes.byref(d2h_b)), "transfer bytes")
+    params_bytes, d2h = h2d_b.value, d2h_b.value
+    assert d2h == sum(t.numel() * 4 for t in host_out)
+
+    # --- per-table error of the production tables against the FP64 path of
+    # the same kernels (outside the timed regions)
+    err_fp64 = table_errors({k: t.numpy() for k, t in zip(TABLES, host_out)},
+                            A.build(C.production(precision=C.FP64)))
 
     # --- rooflines: point scatter (the largest stage, shared-memory gathers)
     # and the first order (SFU exponentials)
@@ -267,7 +286,14 @@ def run_ours(args):
         dist.barrier()
     result = None
     if rank == 0:
-        cpu = cpu_baseline(cfg, args.cpu_sample_s) if world == 1 else None
+        cpu, err_oracle = None, None
+        if world == 1:
+            # the CPU leg evaluates its sampled nodes from the GPU build's own
+            # previous-order tables and reports their agreement
+            inter = A.build(cfg, intermediates=True)
+            cpu = cpu_baseline(cfg, args.cpu_sample_s, inter)
+            err_oracle = cpu.pop("err_vs_gpu")
+            del inter
         result = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": max(args.warmup, 3), "ms_per_step": total_ms / args.steps, "higher_is_better": True,
@@ -282,6 +308,7 @@ def run_ours(args):
             "roofline": {"bound": "smem", "kernel": "k_point_scatter", "achieved": ps_achieved,
                          "peak": smem_peak_g, "unit": "GB/s", "frac": ps_achieved / smem_peak_g if smem_peak_g else None,
                          "traffic": PS_DRAM_BYTES_PER_LAUNCH,
+                         "traffic_source": "ncu capture of this workload (recorded figure, not measured in this run)",
                          "note": ("achieved = algorithmic shared-memory gather bytes of the point-scatter stage "
                                   "(24 B per direction evaluation for the dS row, 24 B more in the first "
                                   "iteration, 48 B per ground direction, 24 B when one dE height row has all the "
@@ -290,7 +317,7 @@ def run_ours(args):
                                   "sfsim_atmo_smem_peak (no such figure in MEASURED_PEAKS.json); DRAM is not "
                                   "the bound (the tables live in L2); traffic = DRAM bytes read + written per "
                                   "point-scatter launch, mean of the build's five launches in one ncu capture of "
-                                  "this workload (profiles/dram_traffic_production_build.md)"),
+                                  "this workload"),
                          "direction_evaluations": dir_evals, "kernel_ms": ps_ms},
             "roofline_first_order": {"bound": "sfu", "kernel": "k_first_order", "achieved": fo_achieved,
                                      "peak": peak_g, "unit": "Gex2/s", "frac": fo_achieved / peak_g if peak_g else None,
@@ -300,6 +327,9 @@ def run_ours(args):
                                               "the table; peak = ex2.approx throughput measured live"),
                                      "lit_pairs": lit, "climbing_pairs": climb, "kernel_ms": fo_ms},
             "clocks": clk,
+            "err_vs_fp64": {"tables": err_fp64, "against": ("the FP64 production build of the same kernels "
+                                                            "(every cell)")},
+            "err_vs_oracle": err_oracle,
             "cpu_baseline": cpu,
             "sweep": sweep,
             "queries": queries,
@@ -615,59 +645,111 @@ def run_cond_queries(C, n_train=32, n_held_out=8, steps=10000, batch=65536, dire
 # CPU baseline: the FP64 restatement of the reference (oracle/), all host threads
 # ---------------------------------------------------------------------------
 
-def cpu_sample(cfg, seconds: float, threads: int, seed: int = 0):
+def cpu_sample(cfg, seconds: float, threads: int, seed: int = 0, inter=None, min_nodes: int = 256):
     """Times sampled nodes of each build stage with `threads` host threads and
-    extrapolates the whole build by node counts.  Returns (build_s, detail)."""
+    extrapolates the whole build by node counts.  Returns (build_s, detail,
+    errors).
+
+    Without `inter` the nodes read synthetic previous-order tables (the work
+    per node does not depend on the values).  With `inter`, the GPU build's
+    intermediate tables of the same configuration, every node of every
+    iteration is evaluated from the GPU's own previous-order tables, as the
+    parity tests do, at least `min_nodes` seeded nodes per stage and
+    iteration, and `errors` holds the relative error of the GPU's value at
+    those nodes (max over RGB, floor 1e-6 of the GPU table's largest value)."""
     import concurrent.futures
 
     import numpy as np
 
     from oracle import oracle as O
 
-    s = cfg.shapes()[2]
-    e = cfg.shapes()[1]
+    t_shape, e_shape, s = cfg.shapes()
     n4 = int(np.prod(s))
     rng = np.random.default_rng(seed)
-    # synthetic previous-order tables: the work per node does not depend on the values
-    tab4 = rng.uniform(0.0, 1e-2, size=tuple(s) + (3,))
-    tab2 = rng.uniform(0.0, 1e-1, size=tuple(e) + (3,))
-
-    def nodes(n):
-        return [tuple(int(rng.integers(0, m)) for m in s) for _ in range(n)]
-
-    stages = {
-        "first_order": lambda nd: O.first_order_node(cfg, *nd),
-        "point_scatter": lambda nd: O.point_scatter_node(cfg, tab4, tab2, *nd),
-        "ray_scatter": lambda nd: O.ray_scatter_node(cfg, tab4, *nd),
-    }
-    per_node = {}
-    budget = seconds / len(stages)
-    with concurrent.futures.ThreadPoolExecutor(max_workers=threads) as ex:
-        for name, fn in stages.items():
-            done, t0 = 0, time.perf_counter()
-            while time.perf_counter() - t0 < budget:
-                batch = nodes(threads * 2)
-                list(ex.map(fn, batch))
-                done += len(batch)
-            per_node[name] = (time.perf_counter() - t0) / done  # wall seconds per node at `threads`
     it = cfg.iterations
+
+    def nodes(shape, n):
+        return [tuple(int(rng.integers(0, m)) for m in shape) for _ in range(n)]
+
+    if inter is None:
+        tab4 = rng.uniform(0.0, 1e-2, size=tuple(s) + (3,))
+        tab2 = rng.uniform(0.0, 1e-1, size=tuple(e_shape) + (3,))
+        tasks = [("first_order", None, lambda nd: O.first_order_node(cfg, *nd), None, s),
+                 ("point_scatter", None, lambda nd: O.point_scatter_node(cfg, tab4, tab2, *nd), None, s),
+                 ("ray_scatter", None, lambda nd: O.ray_scatter_node(cfg, tab4, *nd), None, s)]
+    else:
+        f64 = lambda a: np.ascontiguousarray(a, dtype=np.float64)  # noqa: E731
+        S1R, M = f64(inter["rayleigh_first"]), f64(inter["mie_first"])
+        tasks = [("first_order", None, lambda nd: np.concatenate(O.first_order_node(cfg, *nd)),
+                  lambda nd: np.concatenate([S1R[nd], M[nd]]), s)]
+        for k in range(it):
+            dS_prev = S1R if k == 0 else f64(inter["ray_scatter_delta"][k - 1])
+            dE_prev = f64(inter["surface_base"] if k == 0 else inter["surface_delta"][k - 1])
+            mf = M if k == 0 else None
+            J, dS, dE = f64(inter["point_scatter"][k]), inter["ray_scatter_delta"][k], inter["surface_delta"][k]
+            tasks.append(("point_scatter", k,
+                          lambda nd, a=dS_prev, b=dE_prev, c=mf: O.point_scatter_node(cfg, a, b, *nd, mie_first=c),
+                          lambda nd, J=J: J[nd], s))
+            tasks.append(("ray_scatter", k, lambda nd, J=J: O.ray_scatter_node(cfg, J, *nd),
+                          lambda nd, dS=dS: dS[nd], s))
+            tasks.append(("surface_radiance", k,
+                          lambda nd, a=dS_prev, c=mf: O.surface_radiance_node(cfg, a, *nd, mie_first=c),
+                          lambda nd, dE=dE: dE[nd], e_shape))
+    timed = ("first_order", "point_scatter", "ray_scatter")
+    per_stage = {name: sum(1 for t in tasks if t[0] == name) for name in timed}
+    spent, done = {n: 0.0 for n in timed}, {n: 0 for n in timed}
+    errors = {}
+    with concurrent.futures.ThreadPoolExecutor(max_workers=threads) as ex:
+        for name, order, fn, gpu_value, shape in tasks:
+            budget = seconds / len(timed) / per_stage.get(name, 1)
+            count, errs, t0 = 0, [], time.perf_counter()
+            while count < (min_nodes if gpu_value is not None else 1) or \
+                    (name in timed and time.perf_counter() - t0 < budget):
+                batch = nodes(shape, threads * 2)
+                vals = list(ex.map(fn, batch))
+                count += len(batch)
+                if gpu_value is not None:
+                    for nd, v in zip(batch, vals):
+                        errs.append((np.asarray(gpu_value(nd), dtype=np.float64), np.asarray(v, dtype=np.float64)))
+            if name in timed:
+                spent[name] += time.perf_counter() - t0
+                done[name] += count
+            if gpu_value is not None:
+                g = np.array([a for a, _ in errs])
+                r = np.array([b for _, b in errs])
+                if name == "first_order":  # Rayleigh and Mie, each against its own table's largest value
+                    scale = np.repeat([np.abs(inter["rayleigh_first"]).max(), np.abs(inter["mie_first"]).max()], 3)
+                else:
+                    scale = np.abs({"point_scatter": inter["point_scatter"], "ray_scatter": inter["ray_scatter_delta"],
+                                    "surface_radiance": inter["surface_delta"]}[name][order]).max()
+                e = (np.abs(g - r) / np.maximum(np.abs(r), 1e-6 * np.maximum(scale, 1e-300))).max(axis=1)
+                key = name if order is None else f"{name}[{order}]"
+                errors[key] = {"max": float(e.max()), "mean": float(e.mean()), "nodes": int(len(e))}
+    per_node = {n: spent[n] / max(done[n], 1) for n in timed}  # wall seconds per node at `threads`
     build_s = n4 * (per_node["first_order"] + it * (per_node["point_scatter"] + per_node["ray_scatter"]))
-    return build_s, per_node
+    return build_s, per_node, errors
 
 
-def cpu_baseline(cfg, seconds: float):
+def cpu_baseline(cfg, seconds: float, inter=None):
     threads = os.cpu_count() or 1
     n4 = 1
     for v in cfg.ray_scatter_shape:
         n4 *= v
-    build_s, per_node = cpu_sample(cfg, seconds, threads)
-    return {"value": n4 / build_s, "unit": UNIT, "cores": threads, "kind": "port",
-            "build_s_extrapolated": build_s,
-            "sample": (f"FP64 C restatement of the reference (oracle/atmo_oracle.c), {threads} threads, "
-                       f"~{seconds:.0f} s of seeded random nodes of the first-order, point-scatter and "
-                       f"ray-scatter stages, extrapolated by node counts (2D tables and re-interpolation "
-                       f"passes, <1% of the work, not counted)"),
-            "seconds_per_node": per_node}
+    build_s, per_node, errors = cpu_sample(cfg, seconds, threads, inter=inter)
+    out = {"value": n4 / build_s, "unit": UNIT, "cores": threads, "kind": "port",
+           "build_s_extrapolated": build_s,
+           "sample": (f"FP64 C restatement of the reference (oracle/atmo_oracle.c), {threads} threads, "
+                      f"~{seconds:.0f} s of seeded random nodes of the first-order, point-scatter and "
+                      f"ray-scatter stages, extrapolated by node counts (2D tables and re-interpolation "
+                      f"passes, <1% of the work, not counted)"),
+           "seconds_per_node": per_node}
+    if inter is not None:
+        worst = max(v["max"] for v in errors.values())
+        out["err_vs_gpu"] = {"stages": errors, "max": worst,
+                             "against": ("the oracle at seeded nodes of every stage and iteration, each evaluated "
+                                         "from the GPU build's own previous-order tables (the nodes the CPU "
+                                         "baseline times)")}
+    return out
 
 
 def run_reference(args):
@@ -686,7 +768,7 @@ def run_reference(args):
     vals = []
     t0 = time.perf_counter()
     for k in range(args.steps):
-        build_s, _ = cpu_sample(cfg, per_step, threads, seed=k)
+        build_s, _, _ = cpu_sample(cfg, per_step, threads, seed=k)
         vals.append(n4 / build_s)
     wall = time.perf_counter() - t0
     value = statistics.median(vals)

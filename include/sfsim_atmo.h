@@ -106,22 +106,27 @@ int sfsim_atmo_build_device(const sfsim_atmo_config* cfg, float* transmittance,
                             float* surface_radiance, float* ray_scatter,
                             float* mie_strength, void* stream);
 
-/* As sfsim_atmo_build_device, but allocates nothing.  No counterpart in the
- * reference: it is for callers that cannot call cudaMalloc, such as engines
- * whose own allocator owns all device memory.  It copies the parameters and
- * quadrature directions from host memory on every call, so a CUDA graph must
- * not capture it (the captured copies would read host memory that no longer
- * holds them); capture sfsim_atmo_plan_build instead.  All scratch tables
- * live in one static device array of 64 MiB
+/* A build that allocates nothing.  No counterpart in the reference.  It is
+ * for callers that cannot call cudaMalloc: engines whose own allocator
+ * reserves all device memory at start-up, or that run under a fixed device
+ * budget, where a library that allocates on its own would fail or break the
+ * budget.  All scratch tables live in one static device array of 64 MiB
  * (67108864 bytes) that every GPU loading the library holds until the process
  * exits; a configuration that needs more (roughly 3e5 ray-scatter cells in
  * FP32, half that in FP64; the small FP64 case and the 12^4 shader-test
  * tables fit, the production tables do not) is rejected with
- * SFSIM_ATMO_ETOOBIG and a message naming the bytes it needs.  Outputs are
- * DEVICE pointers, work is queued on `stream`, and the call returns once it is
- * queued.  Every call uses the same array, so calls that overlap on the GPU (different
- * streams, or different host threads) race and corrupt each other; order them
- * on one stream.  Stage timings are not recorded. */
+ * SFSIM_ATMO_ETOOBIG and a message naming the bytes it needs.  The first call
+ * on a device looks up the array's device address (cudaGetSymbolAddress, with
+ * that device current); make that first call before any stream capture.  The
+ * parameters and quadrature directions are copied from host memory on every
+ * call.  Outputs are DEVICE pointers, work is queued on `stream`, and the call
+ * returns once it is queued.  Every call uses the same array, so calls that
+ * overlap on the GPU (different streams, or different host threads) race and
+ * corrupt each other; order them on one stream.  FP64 builds equal
+ * sfsim_atmo_build_device's bit for bit.  FP32 builds integrate every sun ray
+ * directly, where sfsim_atmo_build_device reads the climbing sun rays from a
+ * table, so their tables agree within 2e-5 relative, not bit for bit.  Stage
+ * timings are not recorded. */
 int sfsim_atmo_build_static(const sfsim_atmo_config* cfg, float* transmittance,
                             float* surface_radiance, float* ray_scatter,
                             float* mie_strength, void* stream);
@@ -177,6 +182,13 @@ int sfsim_atmo_last_timings(double* ms, int n);
 
 /* Number of kernel launches of the last build. */
 int sfsim_atmo_last_launch_count(void);
+
+/* Bytes the last build copied from host to device (its parameters and
+ * quadrature directions) and from device to host (the four tables of
+ * sfsim_atmo_build, plus the intermediates of sfsim_atmo_build_debug).  A plan
+ * build copies nothing.  Either pointer may be NULL.  No counterpart in the
+ * reference. */
+int sfsim_atmo_last_transfer_bytes(unsigned long long* h2d, unsigned long long* d2h);
 
 /* ---- Queries of a built atmosphere ---------------------------------------
  * A context builds the four tables of `cfg` on the current device and keeps
@@ -334,6 +346,27 @@ int sfsim_atmo_query_cond_surrogate(sfsim_atmo_cond_surrogate* cs, const sfsim_a
  * 64 * splits; splits > 1 divides K over CTAs and sums into C atomically. */
 int sfsim_atmo_gemm_bf16(const void* A, const void* B, float* C, int M, int N, long long K, int splits,
                          void* stream);
+
+/* Poll limit of every mbarrier wait in the tensor-core kernels (the
+ * surrogate's training GEMMs and its fused inference).  A wait that is not
+ * satisfied within `polls` polls gives up: the CTA records an error, tells
+ * its other warps to stop (their waits give up too), waits for the copies
+ * and MMAs it has in flight, frees its tensor memory and returns; the next
+ * synchronising call (training, gradients, a query with a threshold) returns
+ * SFSIM_ATMO_ECUDA.  polls <= 0 restores the default, 4194304.  Returns the
+ * limit that was in force.  Applies to launches after the call.  No
+ * counterpart in the reference. */
+long long sfsim_atmo_set_wait_limit(long long polls);
+
+/* Self-test of that timeout path, for validation: launches the GEMM kernel of
+ * sfsim_atmo_gemm_bf16 once (one CTA, 128 x 256 x 4096 zero operands that it
+ * allocates) with its epilogue first waiting `polls` polls (1 .. 1000000) on
+ * an mbarrier that nothing arrives on, and synchronises.  That wait gives up
+ * and the kernel returns through the path above, so the call returns
+ * SFSIM_ATMO_ECUDA with a message naming the timed-out wait; the device and
+ * the library stay usable.  A return of 0 would mean the wait did not time
+ * out.  No counterpart in the reference. */
+int sfsim_atmo_wait_selftest(int polls);
 
 /* Work census of one build (no tables are written).  counts[0] = first-order
  * sun-ray integrals (node, ray-sample pairs with the sun above the sample's

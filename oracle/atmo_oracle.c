@@ -1382,10 +1382,30 @@ static float elevation_to_index_f(const glsl_env* e, f3 point, f3 direction, int
   return 0.5f + limit_quot_f(point_radius * sin_elevation + sqrtf(delta > 0 ? delta : 0), 2 * rho, -0.5f, 0.0f);
 }
 
+/* GLSL's exp() is implementation-defined; the CUDA lookups use their own
+ * exponential, restated here with the same single-precision operations in the
+ * same order so that both sides return the same bits: Cody and Waite's
+ * reduction y = k ln2 + r (ln 2 split into the 16-bit head 45426/65536 and its
+ * remainder), the degree-7 Taylor polynomial of exp(r) by Horner's rule, and
+ * the exact scaling by 2^k. */
+static float exp_cw(float y) {
+  float k = rintf(y * 1.44269504088896341f);
+  float r = (y - k * 0.693145751953125f) - k * 1.42860682030941723e-6f;
+  float p = 1.0f / 5040.0f;
+  p = p * r + 1.0f / 720.0f;
+  p = p * r + 1.0f / 120.0f;
+  p = p * r + 1.0f / 24.0f;
+  p = p * r + 1.0f / 6.0f;
+  p = p * r + 0.5f;
+  p = p * r + 1.0f;
+  p = p * r + 1.0f;
+  return ldexpf(p, (int)k);
+}
+
 /* core/sun-elevation-to-index.glsl, core/sun-angle-to-index.glsl */
 static float sun_elevation_to_index_f(f3 point, f3 light) {
   float sin_elevation = fdot(point, light) / flen(point);
-  float r = (1 - expf(-3 * sin_elevation - 0.6f)) / (1 - expf(-3.6f));
+  float r = (1 - exp_cw(-3 * sin_elevation - 0.6f)) / (1 - exp_cw(-3.6f));
   return r > 0 ? r : 0;
 }
 static float sun_angle_to_index_f(f3 direction, f3 light) { return 0.5f * (1 + fdot(direction, light)); }
@@ -1452,9 +1472,10 @@ static f3 interpolate_4d_f(const float* tex, int size_w, int size_z, int size_y,
               fadd(fmulf(sq, (1 - fz) * fw), fmulf(tq, fz * fw)));
 }
 
-/* atmosphere/phase-function.glsl */
+/* atmosphere/phase-function.glsl; pow(t, 1.5) as t * sqrt(t) */
 static float phase_f(float g, float mu) {
-  return 3 * (1 - g * g) * (1 + mu * mu) / (8 * (float)M_PI * (2 + g * g) * powf(1 + g * g - 2 * g * mu, 1.5f));
+  float t = 1 + g * g - 2 * g * mu;
+  return 3 * (1 - g * g) * (1 + mu * mu) / (8 * (float)M_PI * (2 + g * g) * (t * sqrtf(t)));
 }
 
 /* core/transmittance-forward.glsl: (elevation, height) */
@@ -1551,4 +1572,26 @@ void oracle_glsl_query(const oracle_glsl_tables* t, int kind, const float* light
     default: r = in_scatter_query_f(&e, L, P, Q); break;
   }
   out[0] = r.x; out[1] = r.y; out[2] = r.z;
+}
+
+/* n queries at once (light, p, q and out [n][3]); above (may be NULL)
+ * receives is-above-horizon(p, q) of each query, the test that chooses the
+ * table half in kinds 0, 2 and 4. */
+void oracle_glsl_query_batch(const oracle_glsl_tables* t, int kind, long n, const float* light, const float* p,
+                             const float* q, float* out, int* above) {
+  glsl_env e = {t->radius, t->max_height, t->t_height_size, t->t_elevation_size, t->height_size, t->elevation_size,
+                t->light_elevation_size, t->heading_size, t->transmittance, t->ray_scatter, t->mie_strength,
+                t->weight_bits};
+  for (long i = 0; i < n; i++) {
+    oracle_glsl_query(t, kind, light + 3 * i, p + 3 * i, q + 3 * i, out + 3 * i);
+    if (above) {
+      f3 P = F(p[3 * i], p[3 * i + 1], p[3 * i + 2]), Q = F(q[3 * i], q[3 * i + 1], q[3 * i + 2]);
+      f3 d = Q;
+      if (kind == 0 || kind == 2) {
+        float dist = flen(fsub(Q, P));
+        d = dist > 0 ? fmulf(fsub(Q, P), 1.0f / dist) : Q;
+      }
+      above[i] = is_above_horizon_f(&e, P, d);
+    }
+  }
 }

@@ -75,6 +75,8 @@ typedef struct {
 
 void oracle_glsl_query(const oracle_glsl_tables* t, int kind, const float* light, const float* p, const float* q,
                        float* out);
+void oracle_glsl_query_batch(const oracle_glsl_tables* t, int kind, long n, const float* light, const float* p,
+                             const float* q, float* out, int* above);
 
 #ifdef __cplusplus
 }

@@ -427,6 +427,34 @@ def glsl_query(tables: dict, kind: int, light, p, q, weight_bits: int = 0):
     return np.array(o[:], dtype=np.float64)
 
 
+def glsl_query_batch(tables: dict, kind: int, light, p, q, weight_bits: int = 0):
+    """glsl_query over n queries at once.  light, p and q are [n][3] arrays
+    that are rounded to float32 first (the inputs the CUDA lookups receive);
+    returns (float32 [n][3] results, bool [n] is-above-horizon of each query)."""
+    T = np.ascontiguousarray(tables["transmittance"], dtype=np.float32)
+    S = np.ascontiguousarray(tables["ray_scatter"], dtype=np.float32)
+    M = np.ascontiguousarray(tables["mie_strength"], dtype=np.float32)
+    t = GlslTables()
+    t.radius = tables["radius"]
+    t.max_height = tables["max_height"]
+    t.t_height_size, t.t_elevation_size = tables["transmittance_shape"]
+    (t.height_size, t.elevation_size, t.light_elevation_size, t.heading_size) = tables["ray_scatter_shape"]
+    t.transmittance = T.ctypes.data_as(_fp)
+    t.ray_scatter = S.ctypes.data_as(_fp)
+    t.mie_strength = M.ctypes.data_as(_fp)
+    t.weight_bits = weight_bits
+    f32 = [np.ascontiguousarray(np.asarray(a, dtype=np.float32).reshape(-1, 3)) for a in (light, p, q)]
+    n = f32[1].shape[0]
+    out = np.empty((n, 3), dtype=np.float32)
+    above = np.empty(n, dtype=np.int32)
+    L = lib()
+    L.oracle_glsl_query_batch.argtypes = [ctypes.POINTER(GlslTables), ctypes.c_int, ctypes.c_long, _fp, _fp, _fp,
+                                          _fp, _ip]
+    L.oracle_glsl_query_batch(ctypes.byref(t), kind, n, *[a.ctypes.data_as(_fp) for a in f32],
+                              out.ctypes.data_as(_fp), above.ctypes.data_as(_ip))
+    return out, above.astype(bool)
+
+
 # --- cloud-noise builders (noise_oracle.c) ----------------------------------------
 
 def worley(divisions: int, size: int, grid):

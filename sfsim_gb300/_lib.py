@@ -30,6 +30,7 @@ EXPORTS = (
     "sfsim_atmo_condition_inputs", "sfsim_atmo_cond_surrogate_create", "sfsim_atmo_cond_surrogate_destroy",
     "sfsim_atmo_cond_surrogate_train", "sfsim_atmo_cond_surrogate_parameters", "sfsim_atmo_cond_surrogate_gradients",
     "sfsim_atmo_query_cond_surrogate", "sfsim_atmo_plan_create", "sfsim_atmo_plan_build", "sfsim_atmo_plan_destroy",
+    "sfsim_atmo_set_wait_limit", "sfsim_atmo_wait_selftest", "sfsim_atmo_last_transfer_bytes",
 )
 
 
@@ -114,6 +115,10 @@ def load(build: bool = False):
     L.sfsim_noise_worley.argtypes = [ctypes.c_int, ctypes.c_int, vp, vp]
     L.sfsim_noise_perlin.argtypes = [ctypes.c_int, ctypes.c_int, vp, vp]
     L.sfsim_noise_blue.argtypes = [ctypes.c_int, ctypes.c_int, vp, ctypes.c_double, vp]
+    L.sfsim_atmo_set_wait_limit.argtypes = [ctypes.c_longlong]
+    L.sfsim_atmo_set_wait_limit.restype = ctypes.c_longlong
+    L.sfsim_atmo_wait_selftest.argtypes = [ctypes.c_int]
+    L.sfsim_atmo_last_transfer_bytes.argtypes = [ctypes.POINTER(ctypes.c_ulonglong)] * 2
     L.sfsim_atmo_version.argtypes = []
     L.sfsim_atmo_version.restype = ctypes.c_char_p
     _lib = L

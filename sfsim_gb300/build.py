@@ -18,6 +18,9 @@ OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libsfsim_atmo.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"] + ARCH
+# k_lookup.cu restates the shaders' FP32 lookups operation by operation, as the
+# oracle does: no multiply-add contraction there
+FILE_FLAGS = {"k_lookup.cu": ["-fmad=false"]}
 
 
 def nvcc() -> str:
@@ -33,7 +36,7 @@ def sources():
 
 def _compile(src: str) -> str:
     obj = os.path.join(OUT_DIR, os.path.basename(src)[:-3] + ".o")
-    cmd = [nvcc(), *NVCC_FLAGS, "-c", src, "-o", obj]
+    cmd = [nvcc(), *NVCC_FLAGS, *FILE_FLAGS.get(os.path.basename(src), []), "-c", src, "-o", obj]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"nvcc failed on {src}:\n{r.stdout}\n{r.stderr}")

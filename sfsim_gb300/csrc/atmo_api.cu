@@ -3,6 +3,7 @@
 // generate-atmosphere-luts (src/clj/sfsim/atmosphere_lut.clj:43-105).
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -35,6 +36,8 @@ int g_launches = 0;
 constexpr int kStages = 10;
 double g_stage_ms[kStages];
 int g_have_timings = 0;
+// bytes the last build copied host -> device and device -> host
+unsigned long long g_h2d_bytes = 0, g_d2h_bytes = 0;
 
 int fail(int code, const std::string& msg) {
   g_last_error = msg;
@@ -592,6 +595,8 @@ int build_impl(const sfsim_atmo_config* cfgs, int B, float* T, float* E, float* 
   carve<Real>(w, (char*)g_arena[dev].base, d, host_out);
 
   cudaStream_t st = host_out ? g_stream[dev] : user_stream;
+  g_h2d_bytes = sizeof(AtmoParams) * B + sizeof(DirLocal) * (dirs.size() + hdirs.size());
+  g_d2h_bytes = host_out ? sizeof(float) * 3 * B * (d.nT() + d.nE() + 2 * d.n4()) : 0;
   CUDA_TRY(cudaMemcpyAsync(w.params, hp.data(), sizeof(AtmoParams) * B, cudaMemcpyHostToDevice, st));
   if (!dirs.empty()) {
     CUDA_TRY(cudaMemcpyAsync(w.dirs, dirs.data(), sizeof(DirLocal) * dirs.size(), cudaMemcpyHostToDevice, st));
@@ -649,8 +654,10 @@ int build_impl(const sfsim_atmo_config* cfgs, int B, float* T, float* E, float* 
     CUDA_TRY(cudaMemcpyAsync(S, w.oS, sizeof(float) * 3 * B * d.n4(), cudaMemcpyDeviceToHost, st));
     CUDA_TRY(cudaStreamSynchronize(cs));
   }
-  for (size_t i = 0; i < copies.size(); i++)
+  for (size_t i = 0; i < copies.size(); i++) {
     CUDA_TRY(cudaMemcpyAsync(copies[i].second, copies[i].first, copy_bytes[i], cudaMemcpyDeviceToHost, st));
+    g_d2h_bytes += copy_bytes[i];
+  }
   if (host_out || inter) CUDA_TRY(cudaStreamSynchronize(st));
   if (staging) CUDA_TRY(cudaFree(staging));
   collect_timings(tm);
@@ -890,6 +897,12 @@ int sfsim_atmo_last_timings(double* ms, int n) {
 }
 
 int sfsim_atmo_last_launch_count(void) { return g_launches; }
+
+int sfsim_atmo_last_transfer_bytes(unsigned long long* h2d, unsigned long long* d2h) {
+  if (h2d) *h2d = g_h2d_bytes;
+  if (d2h) *d2h = g_d2h_bytes;
+  return 0;
+}
 
 int sfsim_atmo_release(void) {
   std::lock_guard<std::mutex> lock(g_mutex);
@@ -1311,12 +1324,13 @@ int check_error_flag(Surrogate& S, cudaStream_t st) {
 }
 
 // ---------------------------------------------------------------------------
-// Allocation-free build.  Some callers cannot call cudaMalloc: code running
-// inside a CUDA-graph capture or under a memory budget fixed at start-up, or
-// engines whose allocator owns every device byte.  For them this entry point
-// builds the tables with all scratch in one fixed device array that the
-// library declares at file scope.  The array (kStaticScratchBytes, 64 MiB) is
-// held on every GPU that loads the library until the process exits.
+// Allocation-free build.  Some callers cannot call cudaMalloc: engines whose
+// allocator reserves every device byte at start-up, or that run under a fixed
+// device budget.  For them this entry point builds the tables with all
+// scratch in one fixed device array that the library declares at file scope.
+// The array (kStaticScratchBytes, 64 MiB) is held on every GPU that loads the
+// library until the process exits.  Every call shares it and it keeps the
+// last call's contents, so calls that overlap on the GPU race.
 // ---------------------------------------------------------------------------
 
 namespace {
@@ -1365,6 +1379,8 @@ int build_static_impl(const sfsim_atmo_config& cfg, float* T, float* E, float* S
   carve<Real>(w, (char*)base, d, false, false);
   // every scratch table is written before it is read, so nothing is cleared;
   // parameters and quadrature directions are copied in on the caller's stream
+  g_h2d_bytes = sizeof(AtmoParams) + sizeof(DirLocal) * (dirs.size() + hdirs.size());
+  g_d2h_bytes = 0;
   CUDA_TRY(cudaMemcpyAsync(w.params, &hp, sizeof(AtmoParams), cudaMemcpyHostToDevice, st));
   if (!dirs.empty()) {
     CUDA_TRY(cudaMemcpyAsync(w.dirs, dirs.data(), sizeof(DirLocal) * dirs.size(), cudaMemcpyHostToDevice, st));
@@ -1375,6 +1391,7 @@ int build_static_impl(const sfsim_atmo_config& cfg, float* T, float* E, float* S
   tm.dev = dev;
   tm.st = st;
   tm.n = 512;  // a full event list: this entry point records no stage timings
+  g_have_timings = 0;  // so sfsim_atmo_last_timings reports none for this build
   return run_build<Real>(w, d, T, E, S, M, st, tm, nullptr);
 }
 
@@ -1460,6 +1477,8 @@ extern "C" int sfsim_atmo_plan_build(sfsim_atmo_plan* p, float* T, float* E, flo
   tm.dev = p->dev;
   tm.st = (cudaStream_t)stream;
   tm.n = 512;  // a full event list: no stage timings, nothing but kernel launches
+  g_have_timings = 0;
+  g_h2d_bytes = g_d2h_bytes = 0;
   if (p->cfg.precision == SFSIM_ATMO_FP64)
     return run_build<double>(p->wd, p->dims, T, E, S, M, (cudaStream_t)stream, tm, nullptr);
   return run_build<float>(p->wf, p->dims, T, E, S, M, (cudaStream_t)stream, tm, nullptr);
@@ -1600,6 +1619,77 @@ extern "C" int sfsim_atmo_gemm_bf16(const void* A, const void* B, float* C, int 
   if (splits > 1) CUDA_TRY(cudaMemsetAsync(C, 0, sizeof(float) * (size_t)M * N, (cudaStream_t)stream));
   if (launch_gemm_tn(g, splits, (cudaStream_t)stream)) return fail(SFSIM_ATMO_ECUDA, "GEMM launch configuration failed");
   CUDA_TRY(cudaGetLastError());
+  return 0;
+}
+
+// ---------------------------------------------------------------------------
+// Bounded waits of the tensor-core kernels
+// ---------------------------------------------------------------------------
+
+namespace {
+std::atomic<int> g_wait_limit{kDefaultWaitLimit};
+}
+
+int sfsim::wait_limit() { return g_wait_limit.load(std::memory_order_relaxed); }
+
+extern "C" long long sfsim_atmo_set_wait_limit(long long polls) {
+  const int v = polls <= 0 ? kDefaultWaitLimit : (int)std::min<long long>(polls, 0x7fffffffLL);
+  return g_wait_limit.exchange(v);
+}
+
+extern "C" int sfsim_atmo_wait_selftest(int polls) {
+  if (polls < 1 || polls > 1000000) return fail(SFSIM_ATMO_EINVAL, "polls must be in 1 .. 1000000");
+  std::lock_guard<std::mutex> lock(g_mutex);
+  int dev = 0;
+  int rc = current_device(&dev);
+  if (rc) return rc;
+  if ((rc = ensure_stream(dev))) return rc;
+  const int M = 128, N = 256;
+  const long long K = 4096;
+  void *A = nullptr, *B = nullptr;
+  float* C = nullptr;
+  int* err = nullptr;
+  auto release = [&] {
+    cudaFree(A);
+    cudaFree(B);
+    cudaFree(C);
+    cudaFree(err);
+  };
+  if (cudaMalloc(&A, sizeof(__nv_bfloat16) * M * K) != cudaSuccess ||
+      cudaMalloc(&B, sizeof(__nv_bfloat16) * N * K) != cudaSuccess ||
+      cudaMalloc(&C, sizeof(float) * M * N) != cudaSuccess || cudaMalloc(&err, sizeof(int)) != cudaSuccess) {
+    cudaGetLastError();
+    release();
+    return fail(SFSIM_ATMO_ENOMEM, "self-test operands could not be allocated");
+  }
+  cudaStream_t st = g_stream[dev];
+  int h = 0;
+  cudaError_t e = cudaMemsetAsync(A, 0, sizeof(__nv_bfloat16) * M * K, st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(B, 0, sizeof(__nv_bfloat16) * N * K, st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(err, 0, sizeof(int), st);
+  GemmArgs g = {};
+  g.A = (const __nv_bfloat16*)A;
+  g.lda = K;
+  g.B = (const __nv_bfloat16*)B;
+  g.ldb = K;
+  g.M = M;
+  g.N = N;
+  g.K = K;
+  g.alpha = 1.0f;
+  g.Cf32 = C;
+  g.ldc = N;
+  g.error = err;
+  g.stall_polls = polls;
+  if (e == cudaSuccess && launch_gemm_tn(g, 1, st)) e = cudaErrorInvalidConfiguration;
+  if (e == cudaSuccess) e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&h, err, sizeof(int), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  release();
+  if (e != cudaSuccess) return fail(SFSIM_ATMO_ECUDA, std::string("wait self-test: ") + cudaGetErrorString(e));
+  if (h)
+    return fail(SFSIM_ATMO_ECUDA, "a tensor-core wait timed out after " + std::to_string(polls) +
+                                      " polls (self-test: the GEMM epilogue waited on a barrier that nothing "
+                                      "arrives on)");
   return 0;
 }
 

@@ -72,6 +72,20 @@ __host__ __device__ inline double limit_quot(double a, double b, double lower, d
   return upper;
 }
 
+// core/limit-quot.glsl, the FP32 form of limit_quot the shaders use
+__device__ __forceinline__ float limit_quot_f(float a, float b, float lower, float upper) {
+  if (a == 0.0f) return 0.0f;
+  if (b < 0) {
+    a = -a;
+    b = -b;
+  }
+  if (a < b * upper) {
+    if (a > b * lower) return a / b;
+    return lower;
+  }
+  return upper;
+}
+
 // sphere.clj:46-59; returns distance + length of the chosen branch pieces.
 struct Isect {
   double distance, length;

@@ -16,8 +16,12 @@
 // epilogue while the MMAs of the next tile run into the other accumulator;
 // full 32 x 32 blocks pass their row-major input and outputs through a
 // per-warp shared-memory tile so that global accesses are row-contiguous.
-// Every wait is bounded; on timeout the CTA records an error, drains its
-// copies and MMAs and returns.
+// Every wait is bounded by a poll limit set at run time
+// (sfsim_atmo_set_wait_limit); on timeout the CTA records an error, tells its
+// other roles through a shared-memory flag (their waits give up when they see
+// it), waits for its copies and MMAs in flight, frees its tensor memory and
+// returns.  A self-test mode (stall_polls > 0) makes the epilogue first wait
+// on a barrier that nothing arrives on, so that exactly that path runs.
 #include <cuda.h>
 #include <cuda_bf16.h>
 #include <stdint.h>
@@ -32,7 +36,6 @@
 namespace sfsim {
 
 constexpr int kGemmBK = 64;                 // K per stage: one 128-byte swizzle atom of bf16
-constexpr int kGemmWaitLimit = 1 << 22;
 constexpr int kGemmThreads = 320;  // producer, MMA, 8 epilogue warps
 constexpr int kGemmEpilogueThreads = 256;
 constexpr int kGemmSmemBudget = 192 * 1024;  // stages
@@ -71,6 +74,7 @@ struct GemmKernelArgs {
   int stages;
   int tiles_m, splits;
   long long kper;  // K per split, a multiple of kGemmBK
+  int wait_limit;  // polls per mbarrier wait
 };
 
 // Per epilogue warp: a 32 x 32 staging tile (row stride 33 words) that turns
@@ -267,7 +271,8 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
   uint64_t* tfull = empty + S;   // [2] accumulator ready
   uint64_t* tempty = tfull + 2;  // [2] accumulator drained by the epilogue
   uint64_t* drain = tempty + 2;
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(drain + 1);
+  uint64_t* stall = drain + 1;   // self-test: nothing arrives on it
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(stall + 1);
   volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
   float* staging = reinterpret_cast<float*>(smem + S * stage_bytes + 1024);  // [8 epilogue warps][32 * 33]
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -287,6 +292,7 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
       tc::mbar_init(&tempty[b], kGemmEpilogueThreads);
     }
     tc::mbar_init(drain, 1);
+    tc::mbar_init(stall, 1);
     *abort_flag = 0;
     tc::fence_mbar_init();
   }
@@ -305,9 +311,12 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
         const int tm = (int)(tile % a.tiles_m), split = (int)(tile / a.tiles_m);
         for (int kc = 0; kc < kchunks; kc++, issued++) {
           const int s = (int)(issued % S);
-          if (issued >= S &&
-              !(ok = tc::mbar_wait(&empty[s], (uint32_t)(((issued - S) / S) & 1), kGemmWaitLimit) && !*abort_flag))
+          if (*abort_flag ||
+              (issued >= S &&
+               !tc::mbar_wait_or_abort(&empty[s], (uint32_t)(((issued - S) / S) & 1), a.wait_limit, abort_flag))) {
+            ok = false;
             break;
+          }
           unsigned char* st = smem + s * stage_bytes;
           tc::mbar_expect_tx(&full[s], (uint32_t)stage_bytes);
           const int k = (int)(split * a.kper + (long long)kc * kGemmBK);
@@ -319,9 +328,10 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
         *abort_flag = 1;
         if (a.g.error) atomicExch(a.g.error, 1);
       }
-      // copies in flight land before the CTA leaves: wait for the last S issued
+      // copies in flight land before the CTA leaves: wait for the last S
+      // issued (under the full limit, whatever the flag says)
       for (long long k = issued > S ? issued - S : 0; k < issued; k++)
-        tc::mbar_wait(&full[k % S], (uint32_t)((k / S) & 1), kGemmWaitLimit);
+        tc::mbar_wait(&full[k % S], (uint32_t)((k / S) & 1), a.wait_limit);
     }
     __syncwarp();
   } else if (warp == 1) {
@@ -334,13 +344,16 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
       for (long long ti = 0; ti < my_tiles && ok; ti++) {
         const int b = (int)(ti & 1);
         if (ti >= 2 &&
-            !(ok = tc::mbar_wait(&tempty[b], (uint32_t)(((ti - 2) >> 1) & 1), kGemmWaitLimit) && !*abort_flag))
+            !(ok = tc::mbar_wait_or_abort(&tempty[b], (uint32_t)(((ti - 2) >> 1) & 1), a.wait_limit, abort_flag) &&
+                   !*abort_flag))
           break;
         tc::fence_after();
         const uint32_t d = tmem + (uint32_t)(b * ncols);
         for (int kc = 0; kc < kchunks; kc++, c++) {
           const int s = (int)(c % S);
-          if (!(ok = tc::mbar_wait(&full[s], (uint32_t)((c / S) & 1), kGemmWaitLimit) && !*abort_flag)) break;
+          if (!(ok = tc::mbar_wait_or_abort(&full[s], (uint32_t)((c / S) & 1), a.wait_limit, abort_flag) &&
+                     !*abort_flag))
+            break;
           tc::fence_after();
           const uint32_t sa = base + s * stage_bytes, sb = sa + kGemmTileA;
 #pragma unroll
@@ -356,7 +369,7 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
       }
       // every MMA issued by this thread completes before the CTA leaves
       tc::commit(drain);
-      tc::mbar_wait(drain, 0, kGemmWaitLimit);
+      tc::mbar_wait(drain, 0, a.wait_limit);
     }
     __syncwarp();
   } else {
@@ -364,11 +377,16 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
     // of its half
     const int q = warp & 3, half = (warp - 2) >> 2;
     bool ok = true;
+    if (a.g.stall_polls > 0) {
+      // self-test of the timeout path: a wait that cannot succeed
+      const bool done = tc::mbar_wait(stall, 0, a.g.stall_polls);
+      ok = __all_sync(0xffffffffu, done);
+    }
     for (long long ti = 0; ti < my_tiles && ok; ti++) {
       const long long tile = blockIdx.x + ti * gridDim.x;
       const int tm = (int)(tile % a.tiles_m);
       const int b = (int)(ti & 1);
-      bool done = tc::mbar_wait(&tfull[b], (uint32_t)((ti >> 1) & 1), kGemmWaitLimit);
+      bool done = tc::mbar_wait_or_abort(&tfull[b], (uint32_t)((ti >> 1) & 1), a.wait_limit, abort_flag);
       if (!__all_sync(0xffffffffu, done) || *abort_flag) {
         ok = false;
         break;
@@ -460,6 +478,7 @@ int launch_gemm_tn(const GemmArgs& g, int splits, cudaStream_t st) {
   a.splits = splits;
   a.tiles_m = (g.M + 127) / 128;
   a.kper = g.K / splits;
+  a.wait_limit = g.wait_limit > 0 ? g.wait_limit : wait_limit();
   const int stage_bytes = kGemmTileA + a.nt * kGemmBK * 2;
   const long long kchunks = a.kper / kGemmBK;
   a.stages = (int)std::min<long long>(std::min(kGemmSmemBudget / stage_bytes, 8), std::max<long long>(kchunks, 2));

@@ -1,12 +1,9 @@
-// k_query.cu -- queries of a built atmosphere at arbitrary points:
-//  * the table lookups sfsim's shaders perform (resources/shaders/atmosphere/
-//    transmittance-track.glsl, transmittance-outer.glsl, ray-scatter-track.glsl,
-//    ray-scatter-outer.glsl with core/interpolate-2d.glsl, interpolate-4d.glsl
-//    and the core/*-to-index.glsl maps), restated in FP32 as the GLSL computes
-//    them, on the .scatter tables;
+// k_query.cu -- queries of a built atmosphere at arbitrary points (the table
+// lookups themselves live in k_lookup.cu):
 //  * the rendered in-scatter S + M phase(mie, v.l) at (x, v, l) by direct
 //    quadrature: the first order integrated at the point (atmosphere.clj:
-//    154-200) plus ray scatter of the summed point-scatter tables.
+//    154-200) plus ray scatter of the summed point-scatter tables;
+//  * the surrogate's training pools and its fused tensor-core inference.
 #include <cuda_bf16.h>
 
 #include "atmo_device.cuh"
@@ -14,314 +11,6 @@
 #include "tc.cuh"
 
 namespace sfsim {
-
-// ---------------------------------------------------------------------------
-// GLSL restatement (FP32)
-// ---------------------------------------------------------------------------
-
-struct f3 {
-  float x, y, z;
-};
-__device__ __forceinline__ f3 F3(float x, float y, float z) { return f3{x, y, z}; }
-__device__ __forceinline__ float fdot(f3 a, f3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
-__device__ __forceinline__ f3 fsub(f3 a, f3 b) { return F3(a.x - b.x, a.y - b.y, a.z - b.z); }
-__device__ __forceinline__ f3 fadd(f3 a, f3 b) { return F3(a.x + b.x, a.y + b.y, a.z + b.z); }
-__device__ __forceinline__ f3 fmul(f3 a, float s) { return F3(a.x * s, a.y * s, a.z * s); }
-__device__ __forceinline__ f3 femul(f3 a, f3 b) { return F3(a.x * b.x, a.y * b.y, a.z * b.z); }
-
-// core/limit-quot.glsl
-__device__ __forceinline__ float limit_quot_f(float a, float b, float lower, float upper) {
-  if (a == 0.0f) return 0.0f;
-  if (b < 0) {
-    a = -a;
-    b = -b;
-  }
-  if (a < b * upper) {
-    if (a > b * lower) return a / b;
-    return lower;
-  }
-  return upper;
-}
-
-// core/horizon-distance.glsl
-__device__ __forceinline__ float horizon_distance_f(float ground_radius, float radius_sqr) {
-  return sqrtf(fmaxf(0.0f, radius_sqr - ground_radius * ground_radius));
-}
-
-struct GlslEnv {
-  float radius, max_height;
-  int t_height, t_elevation;           // transmittance table
-  int height, elevation, light, heading;  // 4-D tables
-  const float* T;                      // width t_elevation, height t_height
-  const float* S;                      // width elevation*heading, height height*light
-  const float* M;
-  int weight_bits;                     // 0: exact weights; 8: GL 8-bit fixed-point filtering
-  float mie_g;
-};
-
-// core/height-to-index.glsl (normalised)
-__device__ __forceinline__ float height_to_index_g(const GlslEnv& e, f3 p) {
-  const float top = e.radius + e.max_height;
-  return horizon_distance_f(e.radius, fdot(p, p)) / horizon_distance_f(e.radius, top * top);
-}
-
-// core/elevation-to-index.glsl
-__device__ __forceinline__ float elevation_to_index_g(const GlslEnv& e, f3 p, f3 d, bool above) {
-  const float pr = sqrtf(fdot(p, p));
-  const float sin_el = fdot(p, d) / pr;
-  const float rho = horizon_distance_f(e.radius, pr * pr);
-  const float delta = pr * pr * sin_el * sin_el - rho * rho;
-  if (above) {
-    const float top = e.radius + e.max_height;
-    const float h = sqrtf(top * top - e.radius * e.radius);
-    return 0.5f - limit_quot_f(pr * sin_el - sqrtf(fmaxf(0.0f, delta + h * h)), 2 * rho + 2 * h, -0.5f, 0.0f);
-  }
-  return 0.5f + limit_quot_f(pr * sin_el + sqrtf(fmaxf(0.0f, delta)), 2 * rho, -0.5f, 0.0f);
-}
-
-// core/sun-elevation-to-index.glsl, core/sun-angle-to-index.glsl
-__device__ __forceinline__ float sun_elevation_to_index_g(f3 p, f3 l) {
-  const float s = fdot(p, l) / sqrtf(fdot(p, p));
-  return fmaxf(0.0f, (1 - expf(-3 * s - 0.6f)) / (1 - expf(-3.6f)));
-}
-__device__ __forceinline__ float sun_angle_to_index_g(f3 d, f3 l) { return 0.5f * (1 + fdot(d, l)); }
-
-// core/is-above-horizon.glsl
-__device__ __forceinline__ bool is_above_horizon_g(const GlslEnv& e, f3 p, f3 d) {
-  const float dist = sqrtf(fdot(p, p));
-  const float s = fdot(d, p);
-  return s >= 0 || s * s <= dist * dist - e.radius * e.radius;
-}
-
-// texture() with GL_LINEAR and CLAMP_TO_EDGE on an RGB float texture at
-// texel coordinates (x, y) = uv * size - 0.5
-__device__ __forceinline__ float q_weight(float f, int bits) {
-  if (!bits) return f;
-  const float s = (float)(1 << bits);
-  return floorf(f * s + 0.5f) / s;
-}
-
-__device__ __forceinline__ f3 texel(const float* t, int w, int h, int x, int y) {
-  x = min(max(x, 0), w - 1);
-  y = min(max(y, 0), h - 1);
-  const float* p = t + 3 * ((long long)y * w + x);
-  return F3(p[0], p[1], p[2]);
-}
-
-__device__ __forceinline__ f3 texture_g(const float* t, int w, int h, float u, float v, int bits) {
-  const float x = u * w - 0.5f, y = v * h - 0.5f;
-  const float x0 = floorf(x), y0 = floorf(y);
-  const float fx = q_weight(x - x0, bits), fy = q_weight(y - y0, bits);
-  const int ix = (int)x0, iy = (int)y0;
-  const f3 a = texel(t, w, h, ix, iy), b = texel(t, w, h, ix + 1, iy);
-  const f3 c = texel(t, w, h, ix, iy + 1), d = texel(t, w, h, ix + 1, iy + 1);
-  const f3 top = fadd(fmul(a, 1 - fx), fmul(b, fx));
-  const f3 bot = fadd(fmul(c, 1 - fx), fmul(d, fx));
-  return fadd(fmul(top, 1 - fy), fmul(bot, fy));
-}
-
-// core/interpolate-2d.glsl + convert-2d-index.glsl; idx = (x, y)
-__device__ __forceinline__ f3 interpolate_2d_g(const float* t, int size_y, int size_x, float ix, float iy, int bits) {
-  const float u = (ix * (size_x - 1) + 0.5f) / size_x;
-  const float v = (iy * (size_y - 1) + 0.5f) / size_y;
-  return texture_g(t, size_x, size_y, u, v, bits);
-}
-
-// core/interpolate-4d.glsl + make-2d-index-from-4d.glsl; idx = (x, y, z, w)
-__device__ __forceinline__ f3 interpolate_4d_g(const float* t, int size_w, int size_z, int size_y, int size_x,
-                                               const float* idx, int bits) {
-  const float px = idx[0] * (size_x - 1), py = idx[1] * (size_y - 1);
-  const float pz = idx[2] * (size_z - 1), pw = idx[3] * (size_w - 1);
-  const float fz = pz - floorf(pz), fw = pw - floorf(pw);
-  const float zf = floorf(pz), wf = floorf(pw);
-  const float dx = (float)(size_x * size_z), dy = (float)(size_y * size_w);
-  const float z1 = fminf(zf + 1, (float)(size_z - 1)), w1 = fminf(wf + 1, (float)(size_w - 1));
-  const float s = (0.5f + px + zf * size_x) / dx, tt = (0.5f + px + z1 * size_x) / dx;
-  const float p = (0.5f + py + wf * size_y) / dy, q = (0.5f + py + w1 * size_y) / dy;
-  const int W = size_x * size_z, H = size_y * size_w;
-  const f3 sp = texture_g(t, W, H, s, p, bits), tp = texture_g(t, W, H, tt, p, bits);
-  const f3 sq = texture_g(t, W, H, s, q, bits), tq = texture_g(t, W, H, tt, q, bits);
-  return fadd(fadd(fmul(sp, (1 - fz) * (1 - fw)), fmul(tp, fz * (1 - fw))),
-              fadd(fmul(sq, (1 - fz) * fw), fmul(tq, fz * fw)));
-}
-
-// atmosphere/phase-function.glsl
-__device__ __forceinline__ float phase_g(float g, float mu) {
-  return 3 * (1 - g * g) * (1 + mu * mu) / (8 * 3.14159265358979323846f * (2 + g * g) * powf(1 + g * g - 2 * g * mu, 1.5f));
-}
-
-__device__ __forceinline__ void transmittance_forward_g(const GlslEnv& e, f3 p, f3 d, bool above, float* out) {
-  out[0] = elevation_to_index_g(e, p, d, above);
-  out[1] = height_to_index_g(e, p);
-}
-
-// atmosphere/transmittance-track.glsl
-__device__ f3 transmittance_track_g(const GlslEnv& e, f3 p, f3 q) {
-  const float dist = sqrtf(fdot(fsub(q, p), fsub(q, p)));
-  if (dist > 0) {
-    const f3 d = fmul(fsub(q, p), 1.0f / dist);
-    const bool above = is_above_horizon_g(e, p, d);
-    float a[2], b[2];
-    transmittance_forward_g(e, p, d, above, a);
-    transmittance_forward_g(e, q, d, above, b);
-    const f3 t1 = interpolate_2d_g(e.T, e.t_height, e.t_elevation, a[0], a[1], e.weight_bits);
-    const f3 t2 = interpolate_2d_g(e.T, e.t_height, e.t_elevation, b[0], b[1], e.weight_bits);
-    return F3(t1.x / t2.x, t1.y / t2.y, t1.z / t2.z);
-  }
-  return F3(1, 1, 1);
-}
-
-// atmosphere/transmittance-outer.glsl
-__device__ f3 transmittance_outer_g(const GlslEnv& e, f3 p, f3 d) {
-  float a[2];
-  transmittance_forward_g(e, p, d, true, a);
-  return interpolate_2d_g(e.T, e.t_height, e.t_elevation, a[0], a[1], e.weight_bits);
-}
-
-// core/ray-scatter-forward.glsl: (sun angle, sun elevation, elevation, height)
-__device__ __forceinline__ void ray_scatter_forward_g(const GlslEnv& e, f3 p, f3 d, f3 l, bool above, float* out) {
-  out[0] = sun_angle_to_index_g(d, l);
-  out[1] = sun_elevation_to_index_g(p, l);
-  out[2] = elevation_to_index_g(e, p, d, above);
-  out[3] = height_to_index_g(e, p);
-}
-
-__device__ __forceinline__ f3 in_scatter_g(const GlslEnv& e, const float* idx, float mu) {
-  const f3 s = interpolate_4d_g(e.S, e.height, e.elevation, e.light, e.heading, idx, e.weight_bits);
-  const f3 m = interpolate_4d_g(e.M, e.height, e.elevation, e.light, e.heading, idx, e.weight_bits);
-  return fadd(s, fmul(m, phase_g(e.mie_g, mu)));
-}
-
-// atmosphere/ray-scatter-track.glsl
-__device__ f3 ray_scatter_track_g(const GlslEnv& e, f3 l, f3 p, f3 q) {
-  const float dist = sqrtf(fdot(fsub(q, p), fsub(q, p)));
-  if (dist > 0) {
-    const f3 d = fmul(fsub(q, p), 1.0f / dist);
-    const bool above = is_above_horizon_g(e, p, d);
-    const float mu = fdot(d, l);
-    float ip[4], iq[4];
-    ray_scatter_forward_g(e, p, d, l, above, ip);
-    const f3 sp = in_scatter_g(e, ip, mu);
-    ray_scatter_forward_g(e, q, d, l, above, iq);
-    const f3 sq = in_scatter_g(e, iq, mu);
-    const f3 t = transmittance_track_g(e, p, q);
-    return fsub(sp, femul(t, sq));
-  }
-  return F3(0, 0, 0);
-}
-
-// atmosphere/ray-scatter-outer.glsl
-__device__ f3 ray_scatter_outer_g(const GlslEnv& e, f3 l, f3 p, f3 d) {
-  float idx[4];
-  ray_scatter_forward_g(e, p, d, l, true, idx);
-  return in_scatter_g(e, idx, fdot(d, l));
-}
-
-// In-scatter of the tables at (p, d, l) with the horizon test choosing the
-// table half, the lookup the rendered in-scatter comparison uses.
-__device__ f3 in_scatter_at_g(const GlslEnv& e, f3 l, f3 p, f3 d) {
-  float idx[4];
-  ray_scatter_forward_g(e, p, d, l, is_above_horizon_g(e, p, d), idx);
-  return in_scatter_g(e, idx, fdot(d, l));
-}
-
-__global__ void k_query_table(GlslEnv e, int kind, long long n, const float* A, const float* Bv, const float* L,
-                              float* out) {
-  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (t >= n) return;
-  const f3 a = F3(A[3 * t], A[3 * t + 1], A[3 * t + 2]);
-  const f3 b = F3(Bv[3 * t], Bv[3 * t + 1], Bv[3 * t + 2]);
-  const f3 l = L ? F3(L[3 * t], L[3 * t + 1], L[3 * t + 2]) : F3(0, 0, 1);
-  f3 r;
-  switch (kind) {
-    case 0: r = transmittance_track_g(e, a, b); break;
-    case 1: r = transmittance_outer_g(e, a, b); break;
-    case 2: r = ray_scatter_track_g(e, l, a, b); break;
-    case 3: r = ray_scatter_outer_g(e, l, a, b); break;
-    default: r = in_scatter_at_g(e, l, a, b); break;
-  }
-  out[3 * t] = r.x;
-  out[3 * t + 1] = r.y;
-  out[3 * t + 2] = r.z;
-}
-
-static GlslEnv make_env(const QueryTables& q, int weight_bits) {
-  GlslEnv e;
-  e.radius = q.radius;
-  e.max_height = q.max_height;
-  e.t_height = q.t_height;
-  e.t_elevation = q.t_elevation;
-  e.height = q.height;
-  e.elevation = q.elevation;
-  e.light = q.light;
-  e.heading = q.heading;
-  e.T = q.T;
-  e.S = q.S;
-  e.M = q.M;
-  e.weight_bits = weight_bits;
-  e.mie_g = q.mie_g;
-  return e;
-}
-
-void launch_query_table(const QueryTables& q, int kind, long long n, const float* a, const float* b, const float* l,
-                        float* out, int weight_bits, cudaStream_t st) {
-  const GlslEnv e = make_env(q, weight_bits);
-  const int blk = 128;
-  k_query_table<<<(unsigned)((n + blk - 1) / blk), blk, 0, st>>>(e, kind, n, a, b, l, out);
-}
-
-// The surrogate's coordinates of (p, d, l): the table coordinates as the
-// in-scatter lookup forms them (core/ray-scatter-forward.glsl order reversed
-// to height, elevation, sun elevation, sun heading) with the table half chosen
-// by the horizon test, then (1 + sin of the sun elevation) / 2, the half
-// (0 upper, 1 lower) and the four cell phases of the lookup
-// (interpolate-4d.glsl scales each coordinate by size - 1).  idx receives the
-// lookup's indices.
-__device__ __forceinline__ void network_coords(const GlslEnv& e, f3 p, f3 d, f3 l, float* u, float* idx) {
-  const bool above = is_above_horizon_g(e, p, d);
-  ray_scatter_forward_g(e, p, d, l, above, idx);
-  u[0] = idx[3];
-  u[1] = idx[2];
-  u[2] = idx[1];
-  u[3] = idx[0];
-  u[4] = fminf(fmaxf(0.5f * (1.0f + fdot(p, l) / sqrtf(fdot(p, p))), 0.0f), 1.0f);
-  u[5] = above ? 0.0f : 1.0f;
-  const float size[4] = {(float)(e.height - 1), (float)(e.elevation - 1), (float)(e.light - 1),
-                         (float)(e.heading - 1)};
-#pragma unroll
-  for (int c = 0; c < 4; c++) {
-    const float x = u[c] * size[c];
-    u[kMlpSmooth + c] = x - floorf(x);
-  }
-}
-
-// The surrogate's coordinates of (x, v, l); the table value there (S + M
-// phase) as a by-product when `table` is set.
-__global__ void k_query_coords(GlslEnv e, long long n, const double* X, const double* V, const double* L,
-                               float* coords, float* table) {
-  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (t >= n) return;
-  const f3 p = F3((float)X[3 * t], (float)X[3 * t + 1], (float)X[3 * t + 2]);
-  const f3 d = F3((float)V[3 * t], (float)V[3 * t + 1], (float)V[3 * t + 2]);
-  const f3 l = F3((float)L[3 * t], (float)L[3 * t + 1], (float)L[3 * t + 2]);
-  float idx[4], u[kMlpCoords];
-  network_coords(e, p, d, l, u, idx);
-#pragma unroll
-  for (int c = 0; c < kMlpCoords; c++) coords[kMlpCoords * t + c] = u[c];
-  if (table) {
-    const f3 r = in_scatter_g(e, idx, fdot(d, l));
-    table[3 * t] = r.x;
-    table[3 * t + 1] = r.y;
-    table[3 * t + 2] = r.z;
-  }
-}
-
-void launch_query_coords(const QueryTables& q, long long n, const double* x, const double* v, const double* l,
-                         float* coords, float* table, cudaStream_t st) {
-  const GlslEnv e = make_env(q, 0);
-  const int blk = 128;
-  k_query_coords<<<(unsigned)((n + blk - 1) / blk), blk, 0, st>>>(e, n, x, v, l, coords, table);
-}
 
 __device__ __forceinline__ unsigned long long hash64(unsigned long long z) {
   z += 0x9E3779B97F4A7C15ull;
@@ -600,8 +289,9 @@ void launch_query_direct(const AtmoParams* params, const BuildDims& d, const Vec
 // chunk (one weight fetch serves 256 queries) into two 128 x 256 FP32
 // accumulators in tensor memory (all 512 columns).  Stages are released by
 // tcgen05.commit, layers handed over by two mbarriers (accumulator complete,
-// activations written).  Every wait is bounded: on timeout the CTA records an
-// error, lets its copies and MMAs drain and returns.
+// activations written).  Every wait is bounded by the run-time poll limit
+// (sfsim_atmo_set_wait_limit): on timeout the CTA records an error, lets its
+// copies and MMAs drain and returns.
 // ---------------------------------------------------------------------------
 
 constexpr int kInferKC = 32;                                          // K per weight chunk
@@ -613,7 +303,6 @@ constexpr int kInferStages = 5;
 constexpr int kInferTileBytes = 128 * kMlpHidden * 2;                 // 64 KB
 constexpr int kInferEpilogueWarps = 16;  // 2 tiles x 4 lane quarters x 2 column halves
 constexpr int kInferThreads = 32 * kInferEpilogueWarps + 32;
-constexpr int kInferWaitLimit = 1 << 22;
 constexpr int kInferSmemRing = 2 * kInferTileBytes;
 constexpr int kInferSmemBias = kInferSmemRing + kInferStages * kInferChunkBytes;
 constexpr int kInferSmemHead = kInferSmemBias + 4 * kMlpHidden * 4;
@@ -664,6 +353,7 @@ struct InferArgs {
   long long index_offset;
   unsigned long long* count;    // flagged queries so far (also the next free slot of list)
   int* error;
+  int wait_limit;               // polls per mbarrier wait
 };
 
 __device__ __forceinline__ float tanh_approx(float x) {
@@ -744,14 +434,14 @@ __device__ __forceinline__ void infer_producer(const InferArgs& g, long long my_
   bool ok = true;
   for (long long gi = 0; gi < my_groups && ok; gi++) {
     for (int layer = 0; layer < 4 && ok; layer++) {
-      ok = tc::mbar_wait(act_bar, act_phase & 1, kInferWaitLimit) && !*abort_flag;
+      ok = tc::mbar_wait(act_bar, act_phase & 1, g.wait_limit) && !*abort_flag;
       act_phase++;
       if (!ok) break;
       tc::fence_after();
       const int nk = layer == 0 ? kInferChunks0 : kInferChunksH;
       for (int j = 0; j < nk; j++, c++) {
         const int s = (int)(c % kInferStages);
-        if (!(ok = tc::mbar_wait(&full[s], (uint32_t)((c / kInferStages) & 1), kInferWaitLimit))) break;
+        if (!(ok = tc::mbar_wait(&full[s], (uint32_t)((c / kInferStages) & 1), g.wait_limit))) break;
         tc::fence_after();
         const uint32_t w0 = w_base + s * kInferChunkBytes;
 #pragma unroll
@@ -765,7 +455,7 @@ __device__ __forceinline__ void infer_producer(const InferArgs& g, long long my_
         tc::commit(&empty[s]);
         if (c >= 1 && issued < total) {  // refill the stage of the previous chunk
           const long long p = c - 1;
-          if (!(ok = tc::mbar_wait(&empty[p % kInferStages], (uint32_t)((p / kInferStages) & 1), kInferWaitLimit)))
+          if (!(ok = tc::mbar_wait(&empty[p % kInferStages], (uint32_t)((p / kInferStages) & 1), g.wait_limit)))
             break;
           issue(issued++);
         }
@@ -778,8 +468,8 @@ __device__ __forceinline__ void infer_producer(const InferArgs& g, long long my_
     if (g.error) atomicExch(g.error, 1);
     // let the copies in flight land and the issued MMAs finish before the CTA leaves
     for (long long k = c; k < issued; k++)
-      tc::mbar_wait(&full[k % kInferStages], (uint32_t)((k / kInferStages) & 1), kInferWaitLimit);
-    if (c >= 1) tc::mbar_wait(&empty[(c - 1) % kInferStages], (uint32_t)(((c - 1) / kInferStages) & 1), kInferWaitLimit);
+      tc::mbar_wait(&full[k % kInferStages], (uint32_t)((k / kInferStages) & 1), g.wait_limit);
+    if (c >= 1) tc::mbar_wait(&empty[(c - 1) % kInferStages], (uint32_t)(((c - 1) / kInferStages) & 1), g.wait_limit);
   }
 }
 
@@ -854,7 +544,7 @@ __global__ void __launch_bounds__(kInferThreads, 1) k_surrogate_infer(InferArgs 
       tc::mbar_arrive(act_bar);
       float head[kMlpOut] = {};
       for (int layer = 0; layer < 4; layer++) {
-        bool done = tc::mbar_wait(acc_bar, acc_phase & 1, kInferWaitLimit);
+        bool done = tc::mbar_wait(acc_bar, acc_phase & 1, g.wait_limit);
         acc_phase++;
         if (!__all_sync(0xffffffffu, done) || *abort_flag) {
           ok = false;
@@ -918,7 +608,7 @@ __global__ void __launch_bounds__(kInferThreads, 1) k_surrogate_infer(InferArgs 
         continue;
       }
       {
-        const bool done = tc::mbar_wait(head_bar, head_phase & 1, kInferWaitLimit);
+        const bool done = tc::mbar_wait(head_bar, head_phase & 1, g.wait_limit);
         head_phase++;
         if (!__all_sync(0xffffffffu, done) || *abort_flag) {
           ok = false;
@@ -980,6 +670,7 @@ int launch_surrogate_infer(long long n, const float* coords, const float* table,
   g.index_offset = index_offset;
   g.count = count;
   g.error = error;
+  g.wait_limit = wait_limit();
   if (cudaFuncSetAttribute(k_surrogate_infer, cudaFuncAttributeMaxDynamicSharedMemorySize, kInferSmem) !=
       cudaSuccess)
     return -1;

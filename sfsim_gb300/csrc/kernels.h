@@ -187,6 +187,11 @@ void launch_export(long long n, const Vec4<Real>* tab, float* out, cudaStream_t 
 // Tensor-core GEMM C[m][n] = alpha * sum_k A[m][k] B[n][k] (BF16 in, FP32
 // accumulate) with the epilogue the surrogate MLP needs.  M any, N <= 256,
 // K a multiple of 64 * splits; split > 1 only with the Cacc output.
+// Poll limit of the tensor-core kernels' mbarrier waits: kDefaultWaitLimit
+// unless sfsim_atmo_set_wait_limit changed it.
+constexpr int kDefaultWaitLimit = 1 << 22;
+int wait_limit();
+
 struct GemmArgs {
   const __nv_bfloat16* A;
   long long lda;
@@ -209,6 +214,8 @@ struct GemmArgs {
   __nv_bfloat16* HTbf16;  // transposed [N][ldht] or NULL
   long long ldht;
   int* error;         // set to 1 when a wait times out
+  int wait_limit;     // polls per mbarrier wait; 0: wait_limit()
+  int stall_polls;    // > 0: self-test, the epilogue first waits this many polls on a barrier nothing arrives on
 };
 
 int launch_gemm_tn(const GemmArgs& g, int splits, cudaStream_t st);

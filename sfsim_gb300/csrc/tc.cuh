@@ -63,6 +63,25 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* mbar, uint32_t parity, int l
   return false;
 }
 
+// Bounded wait that also gives up once *abort is set (read every 16 polls),
+// so that a timeout in one role of a CTA ends the other roles' waits.
+__device__ __forceinline__ bool mbar_wait_or_abort(uint64_t* mbar, uint32_t parity, int limit, volatile int* abort) {
+  const uint32_t addr = smem_u32(mbar);
+  for (int i = 0; i < limit; i++) {
+    uint32_t done;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.b32 %0, 1, 0, p;\n\t}"
+        : "=r"(done)
+        : "r"(addr), "r"(parity)
+        : "memory");
+    if (done) return true;
+    if ((i & 15) == 15 && *abort) return false;
+  }
+  return false;
+}
+
 __device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 __device__ __forceinline__ void fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }

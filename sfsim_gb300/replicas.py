@@ -42,12 +42,3 @@ def gather_objects(obj):
     dist.all_gather_object(out, obj)
     return out
 
-
-def build_sweep_share(cfgs, rank: int, world: int):
-    """Builds this rank's share of a parameter sweep on its GPU in one batched
-    pass; returns (indices, tables)."""
-    from .atmosphere_lut import build_batch
-    idx = shard_indices(len(cfgs), rank, world)
-    if not idx:
-        return idx, None
-    return idx, build_batch([cfgs[i] for i in idx])
