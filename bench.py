@@ -38,7 +38,7 @@ UNIT = "ray-scatter cells/s (full multi-order LUT build)"
 # build, mean over its five launches in one ncu capture of this workload
 # (dram__bytes_read.sum + dram__bytes_write.sum); ncu does not run here, so the
 # figure is a recorded capture, not a measurement of this run
-PS_DRAM_BYTES_PER_LAUNCH = 89_700_000
+PS_DRAM_BYTES_PER_LAUNCH = 90_150_000
 TABLES = ("transmittance", "surface_radiance", "ray_scatter", "mie_strength")
 WORKLOAD = ("production LUT build: T 255x255, E 16x64, S/M 32x255x32x8 RGB, 5 iterations, "
             "128 ray steps, sphere steps 32 (336 directions), R 6378 km, H 100 km")
@@ -275,6 +275,12 @@ def run_ours(args):
     fo_ex2 = 2 * (lit - climb) * cfg.ray_steps + 3 * lit + 2 * 2048 * 2048 * cfg.ray_steps
     fo_achieved = fo_ex2 / (fo_ms * 1e-3) / 1e9
     peak_g = peak.value / 1e9
+    # ray scatter: per (node, ray sample) the bilinear gather from the
+    # sample's [sun elevation][heading] plane in shared memory reads 4 RGB
+    # texels (48 B); every iteration gathers at every node and sample
+    rs_ms = stages["ray_scatter"]
+    rs_bytes = 48 * n4 * cfg.ray_steps * cfg.iterations
+    rs_achieved = rs_bytes / (rs_ms * 1e-3) / 1e9
 
     sweep = run_sweep(L, A, C) if args.extras else None
     queries = run_queries(C) if args.extras else None
@@ -326,6 +332,13 @@ def run_ours(args):
                                               "of the sun table (2048^2 nodes); climbing sun rays are read from "
                                               "the table; peak = ex2.approx throughput measured live"),
                                      "lit_pairs": lit, "climbing_pairs": climb, "kernel_ms": fo_ms},
+            "roofline_ray_scatter": {"bound": "smem", "kernel": "k_ray_scatter", "achieved": rs_achieved,
+                                     "peak": smem_peak_g, "unit": "GB/s",
+                                     "frac": rs_achieved / smem_peak_g if smem_peak_g else None,
+                                     "note": ("achieved = shared-memory plane gather bytes of the stage (4 RGB "
+                                              "texels, 48 B, per node and ray sample, every iteration) / its event "
+                                              "time; peak = the live conflict-free shared-memory read bandwidth"),
+                                     "node_samples": n4 * cfg.ray_steps * cfg.iterations, "kernel_ms": rs_ms},
             "clocks": clk,
             "err_vs_fp64": {"tables": err_fp64, "against": ("the FP64 production build of the same kernels "
                                                             "(every cell)")},

@@ -122,10 +122,12 @@ def _check_table_queries(cfg, ctx, seed):
             report[(kind, bits)] = float(np.mean(np.all(gpu == ref, axis=1)))
         # queries where the FP32 horizon test (both restatements) and the FP64
         # test on the same inputs choose different table halves: listed, and
-        # checked above like every other query
+        # checked above like every other query.  The edge queries (from 4096
+        # on) look within microradians of the horizon, so many of them flip;
+        # among the random ones flips are rare.
         d = b32 if kind in (1, 3, 4) else (b32 - a32) / np.linalg.norm(b32 - a32, axis=1, keepdims=True)
         flips = np.nonzero(above != _fp64_above(cfg, a32, d))[0]
-        assert flips.size <= 0.01 * len(a32), (kind, flips.size)
+        assert np.sum(flips < 4096) <= 0.01 * 4096, (kind, flips.tolist())
     return report
 
 
