@@ -373,8 +373,10 @@ int sfsim_atmo_wait_selftest(int polls);
  * horizon), [1] = their extinction samples, [2] = view-ray extinction
  * samples, [3] = point-scatter direction evaluations, [4] = ray-scatter
  * J lookups, [5] = surface-radiance direction evaluations, [6] = the pairs
- * of [0] whose sun ray climbs (FP32 builds read those optical depths from a
- * table instead of integrating them), [7] = the point-scatter direction
+ * of [0] whose sun ray climbs (FP32 builds of at least about 1.5e5
+ * ray-scatter cells read the optical depths of every pair of [0] from two
+ * tables, one for climbing and one for descending sun rays, instead of
+ * integrating them; smaller builds integrate them), [7] = the point-scatter direction
  * evaluations of [3] that end on the ground, [8] = those of the first
  * iteration (which also reads the Mie strength), [9] = those of [7] whose
  * ground point has height coordinate exactly 0 in the surface-radiance

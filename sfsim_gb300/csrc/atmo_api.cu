@@ -254,6 +254,12 @@ int make_params(const sfsim_atmo_config& c, AtmoParams& P) {
   P.f_mie_g = (float)P.mie_g;
   P.f_top = (float)P.top;
   P.f_Hh = (float)P.Hh;
+  P.f_H = (float)P.H;
+  // the descending sun rays' distance to their perigee is tabulated in
+  // asinh(d / s): about linear within s of the perigee, where the Mie density
+  // peak lies (it spans sqrt(2 R H_mie)), logarithmic beyond
+  P.f_desc_s = (float)(1.2 * std::sqrt(2.0 * P.R * P.mie_scale));
+  P.f_desc_inv_s = 1.0f / P.f_desc_s;
   const double gs[2] = {P.ray_g, P.mie_g};
   for (int m = 0; m < 2; m++) {
     const double g = gs[m];
@@ -352,6 +358,13 @@ struct Work {
   float2* sun;               // sun-ray optical-depth tables (FP32 builds), or NULL
 };
 
+// The sun-ray tables cost kSunTableLen nodes of S samples per atmosphere;
+// integrating the lit sun rays directly costs S samples for each lit
+// (node, ray sample) pair, about a third of all pairs.  Small builds (the
+// 8x16x8x4 case) integrate directly, larger ones (the production and sweep
+// tables) read the tables.
+inline bool sun_tables_pay(const BuildDims& d) { return (double)d.n4() * d.S / 3.0 > (double)kSunTableLen; }
+
 template <class Real>
 size_t carve(Work<Real>& w, char* base, const BuildDims& d, bool outputs, bool sun_table = true) {
   Carver c{base};
@@ -395,7 +408,8 @@ size_t carve(Work<Real>& w, char* base, const BuildDims& d, bool outputs, bool s
   } else {
     w.oT = w.oE = w.oS = w.oM = nullptr;
   }
-  w.sun = (sun_table && sizeof(Real) == sizeof(float)) ? c.take<float2>(B * (long long)kSunNR * kSunNM) : nullptr;
+  w.sun = (sun_table && sizeof(Real) == sizeof(float) && sun_tables_pay(d)) ? c.take<float2>(B * kSunTableLen)
+                                                                             : nullptr;
   return c.off + 256;
 }
 

@@ -52,6 +52,9 @@ struct AtmoParams {
   double d_srcR[3], d_srcM[3];
   float f_srcR[3], f_srcM[3];
   float f_top, f_Hh;
+  // descending sun-ray table of the FP32 first order: atmosphere height and
+  // the distance scale s of its asinh coordinate (and 1 / s)
+  float f_H, f_desc_s, f_desc_inv_s;
   int hpoly_n;                        // number of coefficients
 };
 
