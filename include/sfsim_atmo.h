@@ -124,9 +124,10 @@ int sfsim_atmo_build_device(const sfsim_atmo_config* cfg, float* transmittance,
  * overlap on the GPU (different streams, or different host threads) race and
  * corrupt each other; order them on one stream.  FP64 builds equal
  * sfsim_atmo_build_device's bit for bit.  FP32 builds integrate every sun ray
- * directly, where sfsim_atmo_build_device reads the climbing sun rays from a
- * table, so their tables agree within 2e-5 relative, not bit for bit.  Stage
- * timings are not recorded. */
+ * directly; sfsim_atmo_build_device does the same for builds whose
+ * ray-scatter cells times ray steps stay below 3 x 2^21 (then the tables are
+ * equal) and reads the sun rays from a table above that size, where the two
+ * agree within 2e-5 relative.  Stage timings are not recorded. */
 int sfsim_atmo_build_static(const sfsim_atmo_config* cfg, float* transmittance,
                             float* surface_radiance, float* ray_scatter,
                             float* mie_strength, void* stream);
@@ -373,10 +374,10 @@ int sfsim_atmo_wait_selftest(int polls);
  * horizon), [1] = their extinction samples, [2] = view-ray extinction
  * samples, [3] = point-scatter direction evaluations, [4] = ray-scatter
  * J lookups, [5] = surface-radiance direction evaluations, [6] = the pairs
- * of [0] whose sun ray climbs (FP32 builds of at least about 1.5e5
- * ray-scatter cells read the optical depths of every pair of [0] from two
- * tables, one for climbing and one for descending sun rays, instead of
- * integrating them; smaller builds integrate them), [7] = the point-scatter direction
+ * of [0] whose sun ray climbs (FP32 builds whose ray-scatter cells times ray
+ * steps exceed 3 x 2^21 read the optical depths of every pair of [0] from a
+ * table instead of integrating them; smaller builds integrate them), [7] =
+ * the point-scatter direction
  * evaluations of [3] that end on the ground, [8] = those of the first
  * iteration (which also reads the Mie strength), [9] = those of [7] whose
  * ground point has height coordinate exactly 0 in the surface-radiance

@@ -6,10 +6,10 @@ budget.  Its scratch is a fixed static device array inside the library.  This
 test calls it twice in a row through the C ABI and checks both results
 against the allocating entry point, sfsim_atmo_build_device.  FP64 builds run
 the same kernels and must agree within 1e-12 relative (bit for bit in
-practice).  FP32 builds must agree within 2e-5: the allocating FP32 build
-reads the climbing sun rays' optical depths from its sun table, the static
-build integrates every sun ray directly.  The two static calls must agree bit
-for bit.  The file name sorts last so that a run stopping at its first failure
+practice).  FP32 builds must agree within 2e-5: an allocating FP32 build of
+a larger configuration reads the sun rays' optical depths from a table where
+the static build integrates every sun ray directly (at this test's size both
+integrate directly).  The two static calls must agree bit for bit.  The file name sorts last so that a run stopping at its first failure
 has run every other test before this one.
 """
 import ctypes
@@ -46,8 +46,9 @@ def test_static_build_matches_allocating_build(precision):
     first = _build(L.sfsim_atmo_build_static, cfg, stream)
     second = _build(L.sfsim_atmo_build_static, cfg, stream)
     torch.cuda.synchronize()
-    # the static build integrates every sun ray directly; the allocating FP32
-    # build reads the climbing ones from its sun table, within 2e-5
+    # the static build integrates every sun ray directly; an allocating FP32
+    # build above the sun table's size threshold reads them from the table,
+    # within 2e-5
     tol = 2e-5 if precision == C.FP32 else 1e-12
     for r, a, b in zip(ref, first, second):
         assert torch.isfinite(a).all() and torch.isfinite(b).all()
