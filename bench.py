@@ -40,7 +40,7 @@ UNIT = "ray-scatter cells/s (full multi-order LUT build)"
 # figure is a recorded capture, not a measurement of this run
 PS_DRAM_BYTES_PER_LAUNCH = 90_150_000
 TABLES = ("transmittance", "surface_radiance", "ray_scatter", "mie_strength")
-SUN_TABLE_NODES = 512 * 4096  # the sun-ray table of the FP32 first order
+SUN_TABLE_NODES = 2048 * 2048 + 1024 * 2048  # climbing and descending sun-ray tables of the FP32 first order
 WORKLOAD = ("production LUT build: T 255x255, E 16x64, S/M 32x255x32x8 RGB, 5 iterations, "
             "128 ray steps, sphere steps 32 (336 directions), R 6378 km, H 100 km")
 
@@ -270,11 +270,12 @@ def run_ours(args):
     peak = ctypes.c_double()
     _lib.check(L.sfsim_atmo_sfu_peak(ctypes.byref(peak)), "sfu_peak")
     fo_ms = stages["first_order"]
-    # exponentials of the first-order stage: 3 transmittances and 2 for the
-    # sun-table lookup (the log of a mean density) per lit (node, sample)
-    # pair, and the table's 512 x 4096 nodes of S samples (2 each); the FP32
-    # production build reads every sun ray's optical depths from the table
-    fo_ex2 = 5 * lit + 2 * SUN_TABLE_NODES * cfg.ray_steps
+    # exponentials of the first-order stage: 3 transmittances per lit
+    # (node, sample) pair, 2 more per descending sun ray (its lookup is the
+    # log of a mean density), and the sun tables' 2048 x 2048 + 1024 x 2048
+    # nodes of S samples (2 each); the FP32 production build reads every sun
+    # ray's optical depths from these tables
+    fo_ex2 = 3 * lit + 2 * (lit - climb) + 2 * SUN_TABLE_NODES * cfg.ray_steps
     fo_achieved = fo_ex2 / (fo_ms * 1e-3) / 1e9
     peak_g = peak.value / 1e9
     # ray scatter: per (node, ray sample) the bilinear gather from the
@@ -329,11 +330,11 @@ def run_ours(args):
                          "direction_evaluations": dir_evals, "kernel_ms": ps_ms},
             "roofline_first_order": {"bound": "sfu", "kernel": "k_first_order", "achieved": fo_achieved,
                                      "peak": peak_g, "unit": "Gex2/s", "frac": fo_achieved / peak_g if peak_g else None,
-                                     "note": ("exponentials of the stage: 3 transmittances and 2 for the sun-table "
-                                              "lookup per lit sample, 2 per sample of the sun table (512 x 4096 "
-                                              "nodes); every sun ray's optical depths are read from the table, so "
-                                              "the stage is bound by the table's L1 gathers, not the SFU; peak = "
-                                              "ex2.approx throughput measured live"),
+                                     "note": ("exponentials of the stage: 3 transmittances per lit sample, 2 per "
+                                              "descending sun-ray lookup, 2 per sample of the sun tables (2048 x 2048 "
+                                              "climbing + 1024 x 2048 descending nodes); every sun ray's optical "
+                                              "depths are read from the tables, so the stage is bound by the tables' "
+                                              "L1 gathers, not the SFU; peak = ex2.approx throughput measured live"),
                                      "lit_pairs": lit, "climbing_pairs": climb, "kernel_ms": fo_ms},
             "roofline_ray_scatter": {"bound": "smem", "kernel": "k_ray_scatter", "achieved": rs_achieved,
                                      "peak": smem_peak_g, "unit": "GB/s",

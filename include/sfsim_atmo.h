@@ -125,9 +125,9 @@ int sfsim_atmo_build_device(const sfsim_atmo_config* cfg, float* transmittance,
  * corrupt each other; order them on one stream.  FP64 builds equal
  * sfsim_atmo_build_device's bit for bit.  FP32 builds integrate every sun ray
  * directly; sfsim_atmo_build_device does the same for builds whose
- * ray-scatter cells times ray steps stay below 3 x 2^21 (then the tables are
- * equal) and reads the sun rays from a table above that size, where the two
- * agree within 2e-5 relative.  Stage timings are not recorded. */
+ * ray-scatter cells times ray steps stay below about 1.9e7 (then the tables
+ * are equal) and reads the sun rays from tables above that size, where the
+ * two agree within 2e-5 relative.  Stage timings are not recorded. */
 int sfsim_atmo_build_static(const sfsim_atmo_config* cfg, float* transmittance,
                             float* surface_radiance, float* ray_scatter,
                             float* mie_strength, void* stream);
@@ -375,9 +375,10 @@ int sfsim_atmo_wait_selftest(int polls);
  * samples, [3] = point-scatter direction evaluations, [4] = ray-scatter
  * J lookups, [5] = surface-radiance direction evaluations, [6] = the pairs
  * of [0] whose sun ray climbs (FP32 builds whose ray-scatter cells times ray
- * steps exceed 3 x 2^21 read the optical depths of every pair of [0] from a
- * table instead of integrating them; smaller builds integrate them), [7] =
- * the point-scatter direction
+ * steps exceed about 1.9e7 read the optical depths of every pair of [0] from
+ * two tables, one for climbing and one for descending sun rays, instead of
+ * integrating them; smaller builds integrate them), [7] = the point-scatter
+ * direction
  * evaluations of [3] that end on the ground, [8] = those of the first
  * iteration (which also reads the Mie strength), [9] = those of [7] whose
  * ground point has height coordinate exactly 0 in the surface-radiance

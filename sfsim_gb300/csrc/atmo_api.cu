@@ -355,15 +355,15 @@ struct Work {
   Real* J;
   Real* hrows;  // point scatter's heading rows per (height, sun elevation)
   float *oT, *oE, *oS, *oM;  // device outputs when the caller passes host buffers
-  float2* sun;               // sun-ray optical-depth table (FP32 builds), or NULL
+  float2* sun;               // sun-ray optical-depth tables (FP32 builds), or NULL
 };
 
-// The sun-ray table costs kSunNX * kSunNY nodes of S samples per atmosphere;
+// The sun-ray tables cost kSunTableLen nodes of S samples per atmosphere;
 // integrating the lit sun rays directly costs S samples for each lit
 // (node, ray sample) pair, about a third of all pairs.  Small builds (the
 // 8x16x8x4 case) integrate directly, larger ones (the production and sweep
-// tables) read the table.
-inline bool sun_tables_pay(const BuildDims& d) { return (double)d.n4() * d.S / 3.0 > (double)kSunNX * kSunNY; }
+// tables) read the tables.
+inline bool sun_tables_pay(const BuildDims& d) { return (double)d.n4() * d.S / 3.0 > (double)kSunTableLen; }
 
 template <class Real>
 size_t carve(Work<Real>& w, char* base, const BuildDims& d, bool outputs, bool sun_table = true) {

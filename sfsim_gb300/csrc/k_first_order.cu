@@ -16,23 +16,22 @@
 // shuffles.  Shadowed samples form contiguous runs along a ray, so lanes of a
 // warp mostly agree on whether to integrate.
 //
-// FP32 builds of production size read every sun ray's optical depths from a
-// table of the same S-sample midpoint sums, evaluated by k_sun_table.  A sun
-// ray from p along l is fixed by its perigee height h* (q* = |p|^2 - R^2 -
-// (p.l)^2) and the signed distance d = -(p.l) from p to the perigee: d > 0
-// for a descending ray, d <= 0 for one that climbs, |d| <= dmax, the half
-// chord from the perigee to the top; the ray leaves after d + dmax.  The
-// 512 x 4096 grid covers (h* / H, asinh(d / s) / asinh(dmax / s)) with
-// s = 1.2 sqrt(2 R H_mie), so the nodes crowd within a few s of the perigee,
-// where the Mie density peaks.  It stores log2 of the mean density along the
-// ray (sum / S); a lookup interpolates that bilinearly and multiplies
-// 2^(interpolated) by the exit distance.  The logarithm is nearly linear in
-// h*, and the mean stays finite for the rays of zero length (starting at the
-// exit, or with the perigee at the top).  A numpy model of the same sums
-// (FP32 storage included) put the optical-depth error at <= 4.4e-6 over
-// Earth, the reference's 35 km atmosphere and the sweep's extremes (radius
-// 3000 and 7000 km, Mie scale heights 0.8 and 2 km); interpolating the sums
-// themselves gave 4e-3 for descending rays.
+// FP32 builds read every sun ray's optical depths from two tables of the
+// same S-sample midpoint sums, both evaluated by k_sun_table:
+//  * a climbing ray (p_s.l >= 0) from a 2048 x 2048 grid of (sqrt(q / q_top),
+//    the exit distance between its zenith and horizontal values), sums
+//    interpolated bilinearly: its integrand falls monotonically, so the sums
+//    are smooth in those coordinates (transmittance error below 1e-5);
+//  * a descending ray (p_s.l < 0) from a 1024 x 2048 grid of (perigee height
+//    / H, asinh(d / s) / asinh(dmax / s)), d the distance from p_s to the
+//    perigee, dmax that from the perigee to the exit, s = 1.2 sqrt(2 R H_mie).
+//    What is stored is log2 of the mean density along the ray, sum / S, whose
+//    bilinear interpolation is smooth even at the perigee's density peak and
+//    stays finite for the short rays near the top; the optical depth is the
+//    exit distance times 2^interpolated.  A numpy model of the same sums put
+//    the optical-depth error at <= 3e-6 (FP32 storage included) over Earth,
+//    the reference's 35 km atmosphere and the sweep's extremes (radius 3000
+//    and 7000 km, Mie scale heights 0.8 and 2 km).
 #include "atmo_device.cuh"
 #include "kernels.h"
 
@@ -72,25 +71,25 @@ __device__ __forceinline__ Real warp_sum(Real v) {
 
 // ---- sun-ray optical-depth table (FP32 builds) ----
 
-// Node (i, j): perigee height h* = (i / (NX - 1)) H, q* = h* (2 R + h*),
-// dmax = sqrt(q_top - q*), d = s sinh(y asinh(dmax / s)) with
-// y = 2 j / (NY - 1) - 1; the ray starts at q = q* + d^2 with p.l = -d.
-// Stored: log2 of sum / S for Rayleigh and Mie.  A ray of length zero (the
-// top row, the column y = -1) has all S samples at its start, so the mean is
-// the density there.  Layout: float4 (node (i, j), node (i + 1, j)) at
-// i * NY + j for i < NX - 1, so that a lookup's four corners come in two
-// adjacent 16-byte loads; each node is written into two pairs.
-__global__ void k_sun_table(const AtmoParams* params, int S, float2* table) {
-  const int b = blockIdx.y;
-  const AtmoParams& P = params[b];
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= kSunNX * kSunNY) return;
-  const int i = t / kSunNY, j = t - (t / kSunNY) * kSunNY;
-  const float hs = (float)i / (float)(kSunNX - 1) * P.f_H;
+// Node (i, j) of the table: q = (i / (NR - 1))^2 q_top and the exit distance
+// d = dmin + (j / (NM - 1)) (dh - dmin) between the zenith (dmin = top - r)
+// and horizontal (dh = sqrt(top^2 - r^2)) exits; p.l follows from
+// top^2 = r^2 + 2 d (p.l) + d^2.  Stored: dt * sum exp2 of the Rayleigh and
+// Mie exponents (dt = d / S), the quantities k_first_order integrates.
+//
+// Descending rays, node (i, j) at kSunNR * kSunNM + i * kDescNY + j: perigee
+// height h* = (i / (NX - 1)) H (q* = h* (2 R + h*)), dmax = sqrt(q_top - q*),
+// the distance d = s sinh((j / (NY - 1)) asinh(dmax / s)) before the perigee;
+// the ray starts at q = q* + d^2 with p.l = -d and leaves after d + dmax.
+// Stored: log2 of sum / S for Rayleigh and Mie (the row h* = H holds the
+// density at the top: all S samples of a zero-length ray sit at its start).
+__device__ __forceinline__ void desc_table_node(const AtmoParams& P, int S, int i, int j, float2* out) {
+  const float Hh2 = P.f_Hh2;
+  const float hs = (float)i / (float)(kDescNX - 1) * P.f_H;
   const float qs = hs * (2.0f * P.f_R + hs);
-  const float dmax = sqrtf(fmaxf(P.f_Hh2 - qs, 0.0f));
-  const float y = 2.0f * (float)j / (float)(kSunNY - 1) - 1.0f;
-  const float d = fminf(fmaxf(P.f_desc_s * sinhf(y * asinhf(dmax * P.f_desc_inv_s)), -dmax), dmax);
+  const float dmax = sqrtf(fmaxf(Hh2 - qs, 0.0f));
+  const float y = (float)j / (float)(kDescNY - 1);
+  const float d = fminf(P.f_desc_s * sinhf(y * asinhf(dmax * P.f_desc_inv_s)), dmax);
   const float q0 = fmaf(d, d, qs);
   const float dt = (d + dmax) / (float)S;
   constexpr int NP = Bulk<float>::kSunNP;
@@ -102,36 +101,88 @@ __global__ void k_sun_table(const AtmoParams* params, int S, float2* table) {
                       smie);
   // 2^-126 keeps the logarithm finite where the density underflows
   const float inv_s = 1.0f / (float)S;
-  const float2 v = make_float2(log2f(fmaxf(sr * inv_s, 1.17549435e-38f)), log2f(fmaxf(smie * inv_s, 1.17549435e-38f)));
-  float2* tab = table + (long long)b * kSunTableLen;
-  if (i < kSunNX - 1) tab[2LL * ((long long)i * kSunNY + j)] = v;
-  if (i > 0) tab[2LL * ((long long)(i - 1) * kSunNY + j) + 1] = v;
+  *out = make_float2(log2f(fmaxf(sr * inv_s, 1.17549435e-38f)), log2f(fmaxf(smie * inv_s, 1.17549435e-38f)));
+}
+
+__global__ void k_sun_table(const AtmoParams* params, int S, float2* table) {
+  const int b = blockIdx.y;
+  const AtmoParams& P = params[b];
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t >= kSunTableLen) return;
+  if (t >= (long long)kSunNR * kSunNM) {
+    const int u = (int)(t - (long long)kSunNR * kSunNM);
+    desc_table_node(P, S, u / kDescNY, u - (u / kDescNY) * kDescNY, table + (long long)b * kSunTableLen + t);
+    return;
+  }
+  const int i = (int)t / kSunNM, j = (int)t - ((int)t / kSunNM) * kSunNM;
+  const float Hh2 = P.f_Hh2, R2 = P.f_R * P.f_R, top = P.f_top;
+  const float xr = (float)i / (float)(kSunNR - 1), xm = (float)j / (float)(kSunNM - 1);
+  const float q = xr * xr * Hh2;
+  const float cq = fmaxf(Hh2 - q, 0.0f);  // top^2 - r^2
+  const float r = sqrtf(R2 + q);
+  const float dmin = cq / (top + r), dh = sqrtf(cq);
+  const float dist = fmaf(xm, dh - dmin, dmin);
+  float2 out = make_float2(0.0f, 0.0f);
+  if (dist > 0.0f) {
+    const float bp = (cq - dist * dist) / (2.0f * dist);
+    constexpr int NP = Bulk<float>::kSunNP;
+    float hc[NP];
+#pragma unroll
+    for (int c = 0; c < NP; c++) hc[c] = Bulk<float>::hpr(P)[c];
+    const float dt = dist / (float)S;
+    float sr, smie;
+    sun_sums<float, NP>(q, bp, dt, S, hc, Bulk<float>::alpha(P), Bulk<float>::beta(P), Bulk<float>::hratio(P), sr,
+                        smie);
+    out = make_float2(dt * sr, dt * smie);
+  }
+  table[(long long)b * kSunTableLen + t] = out;
 }
 
 void launch_sun_table(const AtmoParams* params, const BuildDims& d, float2* table, cudaStream_t st) {
-  dim3 grid((unsigned)((kSunNX * kSunNY + 255) / 256), d.B);
+  dim3 grid((unsigned)((kSunTableLen + 255) / 256), d.B);
   k_sun_table<<<grid, 256, 0, st>>>(params, d.S, table);
 }
 
-// Optical depths of the sun ray from q = |p|^2 - R^2 with bp = p.l and exit
-// distance texit, from the table.
-__device__ __forceinline__ float2 sun_lookup(const float2* __restrict__ tab, const AtmoParams& P, float q, float bp,
+// Bilinear lookup of the table at (q, exit distance) for a climbing ray.
+__device__ __forceinline__ float2 sun_lookup(const float2* __restrict__ tab, const AtmoParams& P, float q,
                                              float texit) {
+  const float Hh2 = P.f_Hh2, R2 = P.f_R * P.f_R, top = P.f_top;
+  const float qc = fminf(fmaxf(q, 0.0f), Hh2);
+  const float cq = Hh2 - qc;
+  const float r = sqrtf(R2 + qc);
+  const float dmin = cq / (top + r), dh = sqrtf(cq);
+  const float span = dh - dmin;
+  const float xm = span > 0.0f ? fminf(fmaxf((texit - dmin) / span, 0.0f), 1.0f) : 0.0f;
+  const float xr = sqrtf(qc / Hh2);
+  const float fi = xr * (float)(kSunNR - 1), fj = xm * (float)(kSunNM - 1);
+  const int i0 = min((int)fi, kSunNR - 2), j0 = min((int)fj, kSunNM - 2);
+  const float a = fi - (float)i0, c = fj - (float)j0;
+  const float2* row0 = tab + (long long)i0 * kSunNM + j0;
+  const float2 v00 = __ldg(row0), v01 = __ldg(row0 + 1), v10 = __ldg(row0 + kSunNM), v11 = __ldg(row0 + kSunNM + 1);
+  const float w00 = (1.0f - a) * (1.0f - c), w01 = (1.0f - a) * c, w10 = a * (1.0f - c), w11 = a * c;
+  return make_float2(w00 * v00.x + w01 * v01.x + w10 * v10.x + w11 * v11.x,
+                     w00 * v00.y + w01 * v01.y + w10 * v10.y + w11 * v11.y);
+}
+
+// Optical depths of a descending ray (bp = p.l < 0) from q = |p|^2 - R^2 and
+// its exit distance texit = d + dmax, from the descending table.
+__device__ __forceinline__ float2 sun_lookup_desc(const float2* __restrict__ tab, const AtmoParams& P, float q,
+                                                  float bp, float texit) {
   const float R = P.f_R;
   const float qs = fmaxf(fmaf(-bp, bp, q), 0.0f);
   const float hs = qs / (R + sqrtf(fmaf(R, R, qs)));
   const float dmax = sqrtf(fmaxf(P.f_Hh2 - qs, 0.0f));
   const float den = asinhf(dmax * P.f_desc_inv_s);
   const float x = fminf(hs / P.f_H, 1.0f);
-  const float y = den > 0.0f ? fminf(fmaxf(asinhf(-bp * P.f_desc_inv_s) / den, -1.0f), 1.0f) : 0.0f;
-  const float fi = x * (float)(kSunNX - 1), fj = (y + 1.0f) * (0.5f * (float)(kSunNY - 1));
-  const int i0 = min((int)fi, kSunNX - 2), j0 = min((int)fj, kSunNY - 2);
+  const float y = den > 0.0f ? fminf(asinhf(-bp * P.f_desc_inv_s) / den, 1.0f) : 0.0f;
+  const float fi = x * (float)(kDescNX - 1), fj = y * (float)(kDescNY - 1);
+  const int i0 = min((int)fi, kDescNX - 2), j0 = min((int)fj, kDescNY - 2);
   const float a = fi - (float)i0, c = fj - (float)j0;
-  const float4* pair = reinterpret_cast<const float4*>(tab) + (long long)i0 * kSunNY + j0;
-  const float4 e0 = __ldg(pair), e1 = __ldg(pair + 1);  // (v00, v10), (v01, v11)
+  const float2* row0 = tab + (long long)i0 * kDescNY + j0;
+  const float2 v00 = __ldg(row0), v01 = __ldg(row0 + 1), v10 = __ldg(row0 + kDescNY), v11 = __ldg(row0 + kDescNY + 1);
   const float w00 = (1.0f - a) * (1.0f - c), w01 = (1.0f - a) * c, w10 = a * (1.0f - c), w11 = a * c;
-  const float lr = w00 * e0.x + w01 * e1.x + w10 * e0.z + w11 * e1.z;
-  const float lm = w00 * e0.y + w01 * e1.y + w10 * e0.w + w11 * e1.w;
+  const float lr = w00 * v00.x + w01 * v01.x + w10 * v10.x + w11 * v11.x;
+  const float lm = w00 * v00.y + w01 * v01.y + w10 * v10.y + w11 * v11.y;
   return make_float2(texit * Bulk<float>::exp2(lr), texit * Bulk<float>::exp2(lm));
 }
 
@@ -201,7 +252,9 @@ __global__ void __launch_bounds__(WARPS * 32, 4) k_first_order(const AtmoParams*
         texit = fmax(texit, Real(0));
         Real odr, odm;
         if (std::is_same<Real, float>::value && tab) {
-          const float2 od = sun_lookup(tab, P, (float)q, (float)bp, (float)texit);
+          const float2 od = bp >= Real(0) ? sun_lookup(tab, P, (float)q, (float)texit)
+                                          : sun_lookup_desc(tab + (long long)kSunNR * kSunNM, P, (float)q, (float)bp,
+                                                            (float)texit);
           odr = (Real)od.x;
           odm = (Real)od.y;
         } else {

@@ -70,13 +70,14 @@ void launch_first_order(const AtmoParams* params, const BuildDims& d, const RowI
                         const RowSample<Real>* rows, const CellGeom<Real>* geom, const float2* sun_table,
                         Vec4<Real>* rayleigh, Vec4<Real>* mie, cudaStream_t st);
 
-// Sun-ray optical-depth table of the FP32 first order: kSunNX x kSunNY nodes
-// of two floats per atmosphere, stored as (kSunNX - 1) x kSunNY float4 that
-// pair each node with the one of the next row (see k_first_order.cu);
-// kSunTableLen counts float2 units.
-constexpr int kSunNX = 512;
-constexpr int kSunNY = 4096;
-constexpr long long kSunTableLen = 2LL * (kSunNX - 1) * kSunNY;
+// Sun-ray optical-depth tables of the FP32 first order, per atmosphere: the
+// climbing rays' kSunNR x kSunNM float2, then the descending rays' kDescNX x
+// kDescNY float2 (see k_first_order.cu).
+constexpr int kSunNR = 2048;
+constexpr int kSunNM = 2048;
+constexpr int kDescNX = 1024;
+constexpr int kDescNY = 2048;
+constexpr long long kSunTableLen = (long long)kSunNR * kSunNM + (long long)kDescNX * kDescNY;
 void launch_sun_table(const AtmoParams* params, const BuildDims& d, float2* table, cudaStream_t st);
 
 template <class Real>
