@@ -12,10 +12,11 @@ tables inside the timed region.
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
 With N > 1 (torchrun) every rank builds its own LUT: the path has no exchange
-step, so this is N replicas ("scaling": "weak").  `--impl reference` times the
-FP64 CPU restatement of the reference's algorithm (oracle/) on the host cores
-over a bounded sample of nodes and extrapolates to the whole build by the
-node counts.
+step, so this is N replicas ("scaling": "weak").  `--impl reference` times
+complete builds of the FP64 CPU restatement of the reference's algorithm
+(oracle/) on the host cores, with the workload's steps, iterations and
+physics at a 16x15x4x4 ray-scatter table, and reports their cells per
+second.
 """
 from __future__ import annotations
 
@@ -747,29 +748,72 @@ def cpu_sample(cfg, seconds: float, threads: int, seed: int = 0, inter=None, min
     return build_s, per_node, errors
 
 
+CHECK_SHAPE = (16, 15, 4, 4)  # ray-scatter shape of the CPU baseline's complete build
+
+
+def small_config(cfg):
+    """cfg with its tables reduced to a 16x15x4x4 ray-scatter table (T 16x15, E
+    16x16) and everything else (steps, iterations, physics) kept."""
+    small = cfg.copy()
+    for i, v in enumerate(CHECK_SHAPE):
+        small.ray_scatter_shape[i] = v
+    small.transmittance_shape[0], small.transmittance_shape[1] = 16, 15
+    small.surface_radiance_shape[0], small.surface_radiance_shape[1] = 16, 16
+    return small
+
+
+def cpu_full_build(cfg, threads):
+    """Wall seconds of one complete oracle build of small_config(cfg) on
+    `threads` host threads (threaded over its 16 heights, as the reference's
+    pmap is over dimension 0), and its ray-scatter cell count."""
+    from oracle import oracle as O
+    small = small_config(cfg)
+    t0 = time.perf_counter()
+    O.build(small, nthreads=threads)
+    n4 = 1
+    for v in CHECK_SHAPE:
+        n4 *= v
+    return time.perf_counter() - t0, n4
+
+
 def cpu_baseline(cfg, seconds: float, inter=None):
+    """The CPU baseline: complete FP64 oracle builds of the workload's steps,
+    iterations and physics at a 16x15x4x4 ray-scatter table on all host
+    threads, scaled to the workload's table by cell count (the work per cell
+    does not depend on the table's shape).  The per-node sampler is reported
+    beside it as a cross-check and, with `inter`, yields the GPU's errors at
+    the sampled nodes."""
     threads = os.cpu_count() or 1
     n4 = 1
     for v in cfg.ray_scatter_shape:
         n4 *= v
-    build_s, per_node, errors = cpu_sample(cfg, seconds, threads, inter=inter)
+    t_small, n_small = min((cpu_full_build(cfg, threads) for _ in range(2)), key=lambda r: r[0])
+    build_s = t_small * n4 / n_small
+    sampled_s, per_node, errors = cpu_sample(cfg, seconds, threads, inter=inter)
     out = {"value": n4 / build_s, "unit": UNIT, "cores": threads, "kind": "port",
            "build_s_extrapolated": build_s,
-           "sample": (f"FP64 C restatement of the reference (oracle/atmo_oracle.c), {threads} threads, "
-                      f"~{seconds:.0f} s of seeded random nodes of the first-order, point-scatter and "
-                      f"ray-scatter stages, extrapolated by node counts (2D tables and re-interpolation "
-                      f"passes, <1% of the work, not counted)"),
-           "seconds_per_node": per_node}
+           "sample": (f"FP64 C restatement of the reference (oracle/atmo_oracle.c), {threads} threads: complete "
+                      f"builds with the workload's steps, iterations and physics at a 16x15x4x4 ray-scatter "
+                      f"table ({t_small:.2f} s, best of 2), scaled by cell count to {n4} cells"),
+           "full_build_s_small": t_small,
+           "per_node_sampler": {"build_s_extrapolated": sampled_s, "seconds_per_node": per_node,
+                                "note": ("seeded random nodes of the first-order, point-scatter and ray-scatter "
+                                         "stages timed one node at a time; overestimates the complete build "
+                                         "(per-call set-up, Python threads)")}}
     if inter is not None:
         worst = max(v["max"] for v in errors.values())
         out["err_vs_gpu"] = {"stages": errors, "max": worst,
                              "against": ("the oracle at seeded nodes of every stage and iteration, each evaluated "
-                                         "from the GPU build's own previous-order tables (the nodes the CPU "
-                                         "baseline times)")}
+                                         "from the GPU build's own previous-order tables")}
     return out
 
 
 def run_reference(args):
+    """The reference arm: each step is one complete FP64 oracle build at a
+    16x15x4x4 ray-scatter table with the workload's steps, iterations and
+    physics on all host threads; value = its ray-scatter cells per second,
+    the rate the workload's table is built at (the work per cell does not
+    depend on the table's shape)."""
     rank, world, local = dist_env()
     if rank != 0:
         return None
@@ -779,14 +823,14 @@ def run_reference(args):
     n4 = 1
     for v in cfg.ray_scatter_shape:
         n4 *= v
-    per_step = max(args.cpu_sample_s / 5.0, 2.0)
-    for w in range(max(args.warmup, 3)):
-        cpu_sample(cfg, 1.0, threads, seed=100 + w)
-    vals = []
+    for _ in range(max(args.warmup, 3)):
+        cpu_full_build(C.shader_test(), threads)
+    vals, times = [], []
     t0 = time.perf_counter()
-    for k in range(args.steps):
-        build_s, _, _ = cpu_sample(cfg, per_step, threads, seed=k)
-        vals.append(n4 / build_s)
+    for _ in range(args.steps):
+        t, n_small = cpu_full_build(cfg, threads)
+        times.append(t)
+        vals.append(n_small / t)
     wall = time.perf_counter() - t0
     value = statistics.median(vals)
     result = {
@@ -796,10 +840,11 @@ def run_reference(args):
         "config": {"workload": WORKLOAD, "cells_per_build": n4, "parallelism": "host threads"},
         "build_s": n4 / value,
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
-                         "sample": (f"each step: ~{per_step:.0f} s of seeded random nodes of the first-order, "
-                                    f"point-scatter and ray-scatter stages of the FP64 C restatement "
+                         "sample": (f"each step: one complete build of the FP64 C restatement "
                                     f"(oracle/atmo_oracle.c; the Clojure reference needs a JVM that is not "
-                                    f"installed), extrapolated to the whole build by node counts")},
+                                    f"installed) with the workload's steps, iterations and physics at a "
+                                    f"16x15x4x4 ray-scatter table ({statistics.median(times):.2f} s), whose cells "
+                                    f"per second are the rate of the {n4}-cell table")},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(result), flush=True)

@@ -15,24 +15,50 @@
 namespace sfsim {
 
 // F[i][32 d + 2 k] = sin(pi f_k u_d), F[i][32 d + 2 k + 1] = cos(pi f_k u_d);
-// also the transpose FT[128][n] when requested.
+// also the transpose FT[256][n] when requested.  A block computes the
+// features of 32 rows into shared memory, then writes F row by row and FT
+// as 32 consecutive entries (64 bytes) of each transposed row.
+constexpr int kFeatTile = 32;
 __global__ void k_features(long long n, const float* __restrict__ coords, __nv_bfloat16* __restrict__ F,
                            __nv_bfloat16* __restrict__ FT) {
-  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (t >= n * kMlpIn / 2) return;
-  const long long i = t / (kMlpIn / 2);
-  const int f = (int)(t % (kMlpIn / 2));
-  int d;
-  float freq;
-  feature_pair(f, &d, &freq);
-  float s, c;
-  sincospif(freq * coords[i * kMlpCoords + d], &s, &c);
-  const __nv_bfloat16 bs = __float2bfloat16(s), bc = __float2bfloat16(c);
-  F[i * kMlpIn + 2 * f] = bs;
-  F[i * kMlpIn + 2 * f + 1] = bc;
-  if (FT) {
-    FT[(long long)(2 * f) * n + i] = bs;
-    FT[(long long)(2 * f + 1) * n + i] = bc;
+  __shared__ __align__(16) __nv_bfloat16 tile[kFeatTile][kMlpIn + 8];
+  const long long i0 = blockIdx.x * (long long)kFeatTile;
+  const int rows = (int)min((long long)kFeatTile, n - i0);
+  for (int e = threadIdx.x; e < rows * (kMlpIn / 2); e += blockDim.x) {
+    const int r = e / (kMlpIn / 2), f = e % (kMlpIn / 2);
+    const long long i = i0 + r;
+    int d;
+    float freq;
+    feature_pair(f, &d, &freq);
+    float sv, cv;
+    sincospif(freq * coords[i * kMlpCoords + d], &sv, &cv);
+    __nv_bfloat162 pr;
+    pr.x = __float2bfloat16(sv);
+    pr.y = __float2bfloat16(cv);
+    *reinterpret_cast<__nv_bfloat162*>(&tile[r][2 * f]) = pr;
+    *reinterpret_cast<__nv_bfloat162*>(F + i * kMlpIn + 2 * f) = pr;
+  }
+  if (!FT) return;
+  __syncthreads();
+  for (int c = threadIdx.x; c < kMlpIn; c += blockDim.x) {
+    __nv_bfloat16* dst = FT + (long long)c * n + i0;
+    if (rows == kFeatTile && (n & 7) == 0) {
+      // i0 is a multiple of 32 and n of 8: the row segment is 16-byte aligned
+#pragma unroll
+      for (int q = 0; q < kFeatTile / 8; q++) {
+        uint32_t w[4];
+#pragma unroll
+        for (int e = 0; e < 4; e++) {
+          __nv_bfloat162 pr;
+          pr.x = tile[8 * q + 2 * e][c];
+          pr.y = tile[8 * q + 2 * e + 1][c];
+          w[e] = *reinterpret_cast<const uint32_t*>(&pr);
+        }
+        reinterpret_cast<uint4*>(dst)[q] = make_uint4(w[0], w[1], w[2], w[3]);
+      }
+    } else {
+      for (int r = 0; r < rows; r++) dst[r] = tile[r][c];
+    }
   }
 }
 
@@ -87,33 +113,61 @@ __global__ void k_loss_grad(long long n, const float* __restrict__ out, const fl
 static_assert(kMlpOut == 4, "the head kernels read rows of dout as float4");
 
 // Backward of the head: dZ4[i][j] = (sum_c dout[i][c] W5[c][j]) * dsilu4[i][j]
-// (BF16, also transposed), and dW5 += dout^T H4, db5 += sum dout.
+// (BF16, also transposed), and dW5 += dout^T H4, db5 += sum dout.  Thread j
+// of a block handles hidden unit j over the block's rows, 32 rows at a time:
+// the tile of 32 x 256 BF16 gradients passes through shared memory so that
+// each thread writes 32 consecutive entries of one transposed row (64 bytes)
+// instead of 32 scattered 2-byte values.  The rows of a block start at a
+// multiple of 32 (n is a multiple of 1024).
+constexpr int kHeadTile = 32;
 __global__ void k_head_backward(long long n, const float* __restrict__ dout, const __nv_bfloat16* __restrict__ H,
                                 const float* __restrict__ W5, const float* __restrict__ dsilu,
                                 __nv_bfloat16* __restrict__ dZ, __nv_bfloat16* __restrict__ dZT,
                                 float* __restrict__ dW5, float* __restrict__ db5) {
   __shared__ float sW[kMlpOut * kMlpHidden];
+  // [row][unit], 8 BF16 of padding a row: column reads hit 16 banks, one word per lane pair
+  __shared__ __align__(16) __nv_bfloat16 tile[kHeadTile][kMlpHidden + 8];
   for (int t = threadIdx.x; t < kMlpOut * kMlpHidden; t += blockDim.x) sW[t] = W5[t];
   __syncthreads();
-  // thread = hidden unit j; the block walks a range of rows
   const int j = threadIdx.x;  // blockDim.x == kMlpHidden
-  const long long rows_per_block = (n + gridDim.x - 1) / gridDim.x;
-  const long long r0 = blockIdx.x * rows_per_block, r1 = min(n, r0 + rows_per_block);
+  const long long tiles = n / kHeadTile;
+  const long long tiles_per_block = (tiles + gridDim.x - 1) / gridDim.x;
+  const long long t0 = blockIdx.x * tiles_per_block, t1 = min(tiles, t0 + tiles_per_block);
   float gw[kMlpOut] = {}, gb[kMlpOut] = {};
-  for (long long i = r0; i < r1; i++) {
-    const float4 d = *reinterpret_cast<const float4*>(dout + i * kMlpOut);
-    const float dd[kMlpOut] = {d.x, d.y, d.z, d.w};
-    const float h = __bfloat162float(H[i * kMlpHidden + j]);
-    float dh = 0;
+  for (long long tl = t0; tl < t1; tl++) {
+    const long long i0 = tl * kHeadTile;
+    for (int ii = 0; ii < kHeadTile; ii++) {
+      const long long i = i0 + ii;
+      const float4 d = *reinterpret_cast<const float4*>(dout + i * kMlpOut);
+      const float dd[kMlpOut] = {d.x, d.y, d.z, d.w};
+      const float h = __bfloat162float(H[i * kMlpHidden + j]);
+      float dh = 0;
 #pragma unroll
-    for (int c = 0; c < kMlpOut; c++) {
-      gw[c] = fmaf(dd[c], h, gw[c]);
-      gb[c] += dd[c];
-      dh = fmaf(dd[c], sW[c * kMlpHidden + j], dh);
+      for (int c = 0; c < kMlpOut; c++) {
+        gw[c] = fmaf(dd[c], h, gw[c]);
+        gb[c] += dd[c];
+        dh = fmaf(dd[c], sW[c * kMlpHidden + j], dh);
+      }
+      const __nv_bfloat16 dz = __float2bfloat16(dh * dsilu[i * kMlpHidden + j]);
+      dZ[i * kMlpHidden + j] = dz;
+      tile[ii][j] = dz;
     }
-    const __nv_bfloat16 dz = __float2bfloat16(dh * dsilu[i * kMlpHidden + j]);
-    dZ[i * kMlpHidden + j] = dz;
-    dZT[(long long)j * n + i] = dz;
+    __syncthreads();
+    // transposed row j, entries i0 .. i0 + 31: four 16-byte stores
+    uint4* dst = reinterpret_cast<uint4*>(dZT + (long long)j * n + i0);
+#pragma unroll
+    for (int q = 0; q < kHeadTile / 8; q++) {
+      uint32_t w[4];
+#pragma unroll
+      for (int e = 0; e < 4; e++) {
+        __nv_bfloat162 pr;
+        pr.x = tile[8 * q + 2 * e][j];
+        pr.y = tile[8 * q + 2 * e + 1][j];
+        w[e] = *reinterpret_cast<const uint32_t*>(&pr);
+      }
+      dst[q] = make_uint4(w[0], w[1], w[2], w[3]);
+    }
+    __syncthreads();
   }
 #pragma unroll
   for (int c = 0; c < kMlpOut; c++) atomicAdd(dW5 + c * kMlpHidden + j, gw[c]);
@@ -123,19 +177,33 @@ __global__ void k_head_backward(long long n, const float* __restrict__ dout, con
   }
 }
 
-// db[j] += sum_i dZT[j][i] (the transposed gradients make the rows contiguous)
+// db[j] += sum_i dZT[j][i] (the transposed gradients make the rows
+// contiguous); kBiasSplit blocks share a row, each reading 8 BF16 at a time,
+// and add their partial sums atomically.  n is a multiple of 1024.
+constexpr int kBiasSplit = 8;
 __global__ void k_bias_grad(long long n, int width, const __nv_bfloat16* __restrict__ dZT, float* __restrict__ db) {
-  const int j = blockIdx.x;
+  const int j = blockIdx.x / kBiasSplit, part = blockIdx.x % kBiasSplit;
+  const long long n8 = n / 8;
+  const uint4* row = reinterpret_cast<const uint4*>(dZT + (long long)j * n);
   float s = 0;
-  for (long long i = threadIdx.x; i < n; i += blockDim.x) s += __bfloat162float(dZT[(long long)j * n + i]);
-  __shared__ float red[256];
-  red[threadIdx.x] = s;
-  __syncthreads();
-  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
-    if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
-    __syncthreads();
+  for (long long v = part * (long long)blockDim.x + threadIdx.x; v < n8; v += (long long)kBiasSplit * blockDim.x) {
+    const uint4 q = row[v];
+    const uint32_t w[4] = {q.x, q.y, q.z, q.w};
+#pragma unroll
+    for (int e = 0; e < 4; e++) {
+      const float2 f = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&w[e]));
+      s += f.x + f.y;
+    }
   }
-  if (threadIdx.x == 0) db[j] += red[0];
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  __shared__ float red[32];
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    s = threadIdx.x < (int)(blockDim.x >> 5) ? red[threadIdx.x] : 0.0f;
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (threadIdx.x == 0) atomicAdd(db + j, s);
+  }
   (void)width;
 }
 
@@ -252,7 +320,7 @@ __global__ void k_cond_grad(long long n, const __nv_bfloat16* __restrict__ dZT, 
 static inline unsigned grid_for(long long n, int blk) { return (unsigned)((n + blk - 1) / blk); }
 
 void launch_features(long long n, const float* coords, __nv_bfloat16* F, __nv_bfloat16* FT, cudaStream_t st) {
-  k_features<<<grid_for(n * kMlpIn / 2, 256), 256, 0, st>>>(n, coords, F, FT);
+  k_features<<<(unsigned)((n + kFeatTile - 1) / kFeatTile), 256, 0, st>>>(n, coords, F, FT);
 }
 void launch_head_forward(long long n, const __nv_bfloat16* H, const float* W5, const float* b5, float* out,
                          cudaStream_t st) {
@@ -265,11 +333,11 @@ void launch_loss_grad(long long n, const float* out, const float* target, float 
 void launch_head_backward(long long n, const float* dout, const __nv_bfloat16* H, const float* W5,
                           const float* dsilu, __nv_bfloat16* dZ, __nv_bfloat16* dZT, float* dW5, float* db5,
                           cudaStream_t st) {
-  const int blocks = (int)min(1024LL, (n + 63) / 64);
+  const int blocks = (int)min(1024LL, (n / kHeadTile + 1) / 2);
   k_head_backward<<<blocks, kMlpHidden, 0, st>>>(n, dout, H, W5, dsilu, dZ, dZT, dW5, db5);
 }
 void launch_bias_grad(long long n, int width, const __nv_bfloat16* dZT, float* db, cudaStream_t st) {
-  k_bias_grad<<<width, 256, 0, st>>>(n, width, dZT, db);
+  k_bias_grad<<<width * kBiasSplit, 256, 0, st>>>(n, width, dZT, db);
 }
 void launch_adam(long long count, float* w, const float* g, float* m, float* v, float lr, float beta1, float beta2,
                  float eps, int step, int rows, int cols, __nv_bfloat16* wb, __nv_bfloat16* wbt, cudaStream_t st) {
