@@ -290,6 +290,7 @@ def run_ours(args):
     queries = run_queries(C) if args.extras else None
     queries_cond = run_cond_queries(C) if args.extras else None
     small_graph = run_small_graph(A, C) if args.extras else None
+    ref_prod = run_reference_production(A, C) if args.extras else None
     noise_builders = run_noise() if args.extras else None
 
     if world > 1:
@@ -353,6 +354,7 @@ def run_ours(args):
             "queries": queries,
             "queries_conditioned": queries_cond,
             "small_build_graph": small_graph,
+            "reference_production_build": ref_prod,
             "noise": noise_builders,
         }
         print(json.dumps(result), flush=True)
@@ -396,6 +398,42 @@ def run_sweep(L, A, C):
     return {"atmospheres": len(cfgs), "shape": list(cfgs[0].ray_scatter_shape), "iterations": cfgs[0].iterations,
             "device_s": dev_ms * 1e-3, "e2e_s": wall, "cells_per_s": len(cfgs) * n4 / (dev_ms * 1e-3),
             "err_vs_fp64": err}
+
+
+def run_reference_production(A, C, reps=10):
+    """The build sfsim's own `clj -T:build atmosphere-lut` runs (the
+    reference's settings: 35 km atmosphere, T 64x255, E 16x63, S/M
+    32x127x32x8, 100 ray steps, sphere steps 15, 5 iterations) in FP32:
+    device time per build (CUDA events, L2 flushed between builds) and end to
+    end through sfsim_atmo_build with pinned host buffers."""
+    import torch
+    cfg = C.reference_production()
+    dev = [torch.empty(s, dtype=torch.float32, device="cuda") for s in A.table_shapes(cfg)]
+    host = [torch.empty(s, dtype=torch.float32, pin_memory=True) for s in A.table_shapes(cfg)]
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
+    for _ in range(3):
+        A.build_device(cfg, dev)
+    torch.cuda.synchronize()
+    ms = []
+    for _ in range(reps):
+        flush.add_(1.0)
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s.record()
+        A.build_device(cfg, dev)
+        e.record()
+        torch.cuda.synchronize()
+        ms.append(s.elapsed_time(e))
+    L = A._lib.load()
+    fp = ctypes.POINTER(ctypes.c_float)
+    A._lib.check(L.sfsim_atmo_build(ctypes.byref(cfg), *[ctypes.cast(t.data_ptr(), fp) for t in host]), "build")
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        A._lib.check(L.sfsim_atmo_build(ctypes.byref(cfg), *[ctypes.cast(t.data_ptr(), fp) for t in host]), "build")
+    e2e = (time.perf_counter() - t0) / reps
+    n4 = 1
+    for v in cfg.ray_scatter_shape:
+        n4 *= v
+    return {"config": cfg.describe(), "cells": n4, "device_ms": statistics.median(ms), "e2e_ms": e2e * 1e3}
 
 
 def run_small_graph(A, C, reps=200):
