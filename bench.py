@@ -621,8 +621,74 @@ def run_queries(C, steps=20000, batch=65536, direct_samples=1 << 25, lr=3e-3, hu
         t_fb, (fb, nf) = _timed(lambda: ctx.surrogate(x, v, l, threshold=thr, out=out), reps=1)
         r[f"surrogate_fallback_{thr:g}"] = {"qps": qps(t_fb), "fallback_fraction": nf / n,
                                             "err": query_error_stats(fb, direct), "vs_direct": t_direct / t_fb}
+    r["c4_recipe_baseline"] = c4_recipe_baseline(ctx, cfg, x[: 1 << 21], v[: 1 << 21], l[: 1 << 21],
+                                                 direct[: 1 << 21], steps=steps, batch=batch)
     ctx.close()
     return r
+
+
+def c4_recipe_baseline(ctx, cfg, x, v, l, direct, steps, batch, n_direct=1 << 23, seed=1):
+    """The surrogate recipe as first specified, the baseline the product's
+    correction network replaced: the four table coordinates -> 16 sin/cos
+    Fourier frequencies each (128 features) -> 4 x 256 SiLU -> 3 log-RGB
+    values, predicted outright; Adam, learning rate 1e-3 with cosine decay,
+    batches of 65536 drawing 75% table nodes (the node's S + M phase) and 25%
+    uniform points integrated by the direct quadrature.  Fitted with torch
+    (TF32 matmuls, FP32 weights) as a baseline only; errors on the given
+    queries against the direct quadrature."""
+    import torch
+    eps = 1e-7
+    g = torch.Generator(device="cuda").manual_seed(seed)
+    T, E, S2, M2 = ctx.tables()
+    n0, n1, n2, n3 = cfg.ray_scatter_shape
+    S = S2.view(n0, n2, n1, n3, 3).permute(0, 2, 1, 3, 4).reshape(-1, 3)
+    M = M2.view(n0, n2, n1, n3, 3).permute(0, 2, 1, 3, 4).reshape(-1, 3)
+    idx = torch.stack(torch.meshgrid(*[torch.arange(m, device="cuda") for m in (n0, n1, n2, n3)], indexing="ij"),
+                      -1).reshape(-1, 4).float()
+    node_u = idx / torch.tensor([n0 - 1, n1 - 1, n2 - 1, n3 - 1], device="cuda", dtype=torch.float32)
+    mu = 2.0 * node_u[:, 3] - 1.0
+    gm = 0.76
+    phase = 3 * (1 - gm * gm) * (1 + mu * mu) / (8 * torch.pi * (2 + gm * gm) * (1 + gm * gm - 2 * gm * mu) ** 1.5)
+    node_t = torch.log((S + M * phase[:, None]).clamp(min=0) + eps)
+    dx, dv, dl = _random_queries(n_direct, cfg.radius, cfg.height, 11)
+    dir_u = ctx.coords(dx, dv, dl)[:, :4].contiguous()
+    dir_t = torch.log(ctx.direct(dx, dv, dl).clamp(min=0) + eps)
+    del dx, dv, dl
+    k = torch.arange(16, device="cuda")
+    freq = torch.where(k % 2 == 1, torch.tensor(2 ** 0.5, device="cuda"), torch.tensor(1.0, device="cuda")) * 2.0 ** (k // 2)
+
+    def features(u):
+        a = torch.pi * u[:, :, None] * freq[None, None, :]
+        return torch.stack([torch.sin(a), torch.cos(a)], -1).reshape(u.shape[0], 128)
+
+    torch.manual_seed(seed)
+    layers = [torch.nn.Linear(128, 256), torch.nn.SiLU()]
+    for _ in range(3):
+        layers += [torch.nn.Linear(256, 256), torch.nn.SiLU()]
+    net = torch.nn.Sequential(*layers, torch.nn.Linear(256, 3)).cuda()
+    opt = torch.optim.Adam(net.parameters(), lr=1e-3)
+    sched = torch.optim.lr_scheduler.CosineAnnealingLR(opt, steps)
+    tf32 = torch.backends.cuda.matmul.allow_tf32
+    torch.backends.cuda.matmul.allow_tf32 = True
+    nn_ = batch * 3 // 4
+    for _ in range(steps):
+        a = torch.randint(0, node_u.shape[0], (nn_,), device="cuda", generator=g)
+        b = torch.randint(0, dir_u.shape[0], (batch - nn_,), device="cuda", generator=g)
+        u = torch.cat([node_u[a], dir_u[b]])
+        t = torch.cat([node_t[a], dir_t[b]])
+        loss = torch.nn.functional.mse_loss(net(features(u)), t)
+        opt.zero_grad(set_to_none=True)
+        loss.backward()
+        opt.step()
+        sched.step()
+    with torch.no_grad():
+        u = ctx.coords(x, v, l)[:, :4].contiguous()
+        pred = torch.cat([torch.exp(net(features(u[i:i + (1 << 18)]))) - eps for i in range(0, u.shape[0], 1 << 18)])
+    torch.backends.cuda.matmul.allow_tf32 = tf32
+    return {"err": query_error_stats(pred.clamp(min=0), direct), "n": int(u.shape[0]), "steps": steps,
+            "note": ("the first surrogate recipe (4 coordinates, 128 Fourier features, 4 x 256 SiLU, 3 log-RGB "
+                     "outright, 75% table nodes, lr 1e-3 cosine), fitted in torch as the baseline the "
+                     "correction network replaced; not the product")}
 
 
 def run_cond_queries(C, n_train=32, n_held_out=8, steps=10000, batch=65536, direct_samples=1 << 20, lr=3e-3,
