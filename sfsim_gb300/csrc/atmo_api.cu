@@ -1298,18 +1298,18 @@ int surrogate_backward(Surrogate& S, long long n, float huber, cudaStream_t st) 
 
 void surrogate_adam(Surrogate& S, float lr, int step, cudaStream_t st) {
   const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
-  for (int l = 0; l < 5; l++) {
-    const long long nw = (long long)S.lay.in[l] * S.lay.out[l];
-    launch_adam(nw, S.w + S.lay.W[l], S.g + S.lay.W[l], S.m + S.lay.W[l], S.v + S.lay.W[l], lr, b1, b2, eps, step,
-                S.lay.out[l], S.lay.in[l], l < 4 ? S.wb[l] : nullptr, l < 4 ? S.wbt[l] : nullptr, st);
-    launch_adam(S.lay.out[l], S.w + S.lay.b[l], S.g + S.lay.b[l], S.m + S.lay.b[l], S.v + S.lay.b[l], lr, b1, b2,
-                eps, step, 1, S.lay.out[l], nullptr, nullptr, st);
+  // one launch over every parameter (W_l, b_l, and U of a conditioned
+  // network), refreshing the BF16 copies of the four hidden-layer matrices
+  AdamMatrices mats;
+  mats.n = 4;
+  for (int l = 0; l < 4; l++) {
+    mats.start[l] = S.lay.W[l];
+    mats.rows[l] = S.lay.out[l];
+    mats.cols[l] = S.lay.in[l];
+    mats.wb[l] = S.wb[l];
+    mats.wbt[l] = S.wbt[l];
   }
-  if (S.lay.cond) {
-    const long long nu = (long long)kMlpHidden * S.lay.cond;
-    launch_adam(nu, S.w + S.lay.U, S.g + S.lay.U, S.m + S.lay.U, S.v + S.lay.U, lr, b1, b2, eps, step, kMlpHidden,
-                S.lay.cond, nullptr, nullptr, st);
-  }
+  launch_adam_all(S.lay.total, S.w, S.g, S.m, S.v, lr, b1, b2, eps, step, mats, st);
 }
 
 QueryTables context_tables(const sfsim_atmo_context* ctx) {

@@ -62,17 +62,35 @@ __global__ void k_features(long long n, const float* __restrict__ coords, __nv_b
   }
 }
 
-// out[i][c] = sum_j H[i][j] W5[c][j] + b5[c], c < kMlpOut; one warp per row.
+// out[i][c] = sum_j H[i][j] W5[c][j] + b5[c], c < kMlpOut; one warp per row,
+// each lane one 16-byte load of eight BF16 (kMlpHidden == 256), W5 staged in
+// shared memory.
+static_assert(kMlpHidden == 256, "k_head_forward reads a row as 32 lanes x 8 BF16");
 __global__ void k_head_forward(long long n, const __nv_bfloat16* __restrict__ H, const float* __restrict__ W5,
                                const float* __restrict__ b5, float* __restrict__ out) {
+  __shared__ float sW[kMlpOut * kMlpHidden];
+  for (int t = threadIdx.x; t < kMlpOut * kMlpHidden; t += blockDim.x) sW[t] = W5[t];
+  __syncthreads();
   const long long row = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (row >= n) return;
-  float acc[kMlpOut] = {};
-  for (int j = lane; j < kMlpHidden; j += 32) {
-    const float h = __bfloat162float(H[row * kMlpHidden + j]);
+  const uint4 q = *reinterpret_cast<const uint4*>(H + row * kMlpHidden + 8 * lane);
+  const uint32_t wq[4] = {q.x, q.y, q.z, q.w};
+  float h[8];
 #pragma unroll
-    for (int c = 0; c < kMlpOut; c++) acc[c] = fmaf(h, W5[c * kMlpHidden + j], acc[c]);
+  for (int e = 0; e < 4; e++) {
+    const float2 f = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&wq[e]));
+    h[2 * e] = f.x;
+    h[2 * e + 1] = f.y;
+  }
+  float acc[kMlpOut];
+#pragma unroll
+  for (int c = 0; c < kMlpOut; c++) {
+    const float* w = sW + c * kMlpHidden + 8 * lane;
+    float a = 0;
+#pragma unroll
+    for (int e = 0; e < 8; e++) a = fmaf(h[e], w[e], a);
+    acc[c] = a;
   }
 #pragma unroll
   for (int c = 0; c < kMlpOut; c++) {
@@ -136,6 +154,7 @@ __global__ void k_head_backward(long long n, const float* __restrict__ dout, con
   float gw[kMlpOut] = {}, gb[kMlpOut] = {};
   for (long long tl = t0; tl < t1; tl++) {
     const long long i0 = tl * kHeadTile;
+#pragma unroll 8
     for (int ii = 0; ii < kHeadTile; ii++) {
       const long long i = i0 + ii;
       const float4 d = *reinterpret_cast<const float4*>(dout + i * kMlpOut);
@@ -205,6 +224,34 @@ __global__ void k_bias_grad(long long n, int width, const __nv_bfloat16* __restr
     if (threadIdx.x == 0) atomicAdd(db + j, s);
   }
   (void)width;
+}
+
+// Adam with bias correction over the whole parameter vector [0, count) in one
+// launch; the elements of the weight matrices listed in `mats` also refresh
+// their BF16 copy [rows][cols] and its transpose.
+__global__ void k_adam_all(long long count, float* __restrict__ w, const float* __restrict__ g,
+                           float* __restrict__ m, float* __restrict__ v, float lr, float beta1, float beta2, float eps,
+                           float c1, float c2, AdamMatrices mats) {
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t >= count) return;
+  const float gt = g[t];
+  const float mt = beta1 * m[t] + (1 - beta1) * gt;
+  const float vt = beta2 * v[t] + (1 - beta2) * gt * gt;
+  m[t] = mt;
+  v[t] = vt;
+  const float mhat = mt / c1, vhat = vt / c2;
+  const float wt = w[t] - lr * mhat / (sqrtf(vhat) + eps);
+  w[t] = wt;
+#pragma unroll
+  for (int k = 0; k < AdamMatrices::kMax; k++) {
+    if (k >= mats.n) break;
+    const long long o = t - mats.start[k];
+    if (o >= 0 && o < (long long)mats.rows[k] * mats.cols[k]) {
+      const int r = (int)(o / mats.cols[k]), c = (int)(o % mats.cols[k]);
+      mats.wb[k][o] = __float2bfloat16(wt);
+      mats.wbt[k][(long long)c * mats.rows[k] + r] = __float2bfloat16(wt);
+    }
+  }
 }
 
 // Adam with bias correction on FP32 master weights; refreshes the BF16
@@ -344,6 +391,11 @@ void launch_adam(long long count, float* w, const float* g, float* m, float* v, 
   const float c1 = 1.0f - powf(beta1, (float)step), c2 = 1.0f - powf(beta2, (float)step);
   k_adam<<<grid_for(count, 256), 256, 0, st>>>(count, w, g, m, v, lr, beta1, beta2, eps, c1, c2, rows, cols, wb,
                                                 wbt);
+}
+void launch_adam_all(long long count, float* w, const float* g, float* m, float* v, float lr, float beta1, float beta2,
+                     float eps, int step, const AdamMatrices& mats, cudaStream_t st) {
+  const float c1 = 1.0f - powf(beta1, (float)step), c2 = 1.0f - powf(beta2, (float)step);
+  k_adam_all<<<grid_for(count, 256), 256, 0, st>>>(count, w, g, m, v, lr, beta1, beta2, eps, c1, c2, mats);
 }
 void launch_to_bf16(long long count, const float* w, int rows, int cols, __nv_bfloat16* wb, __nv_bfloat16* wbt,
                     cudaStream_t st) {

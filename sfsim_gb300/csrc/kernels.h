@@ -273,6 +273,19 @@ void launch_head_backward(long long n, const float* dout, const __nv_bfloat16* H
                           const float* dsilu, __nv_bfloat16* dZ, __nv_bfloat16* dZT, float* dW5, float* db5,
                           cudaStream_t st);
 void launch_bias_grad(long long n, int width, const __nv_bfloat16* dZT, float* db, cudaStream_t st);
+// The weight matrices whose BF16 copies (and transposes) an Adam step over
+// the whole parameter vector refreshes: matrix k occupies [start, start +
+// rows * cols) of the vector.
+struct AdamMatrices {
+  static constexpr int kMax = 4;
+  int n;
+  long long start[kMax];
+  int rows[kMax], cols[kMax];
+  __nv_bfloat16* wb[kMax];
+  __nv_bfloat16* wbt[kMax];
+};
+void launch_adam_all(long long count, float* w, const float* g, float* m, float* v, float lr, float beta1, float beta2,
+                     float eps, int step, const AdamMatrices& mats, cudaStream_t st);
 void launch_adam(long long count, float* w, const float* g, float* m, float* v, float lr, float beta1, float beta2,
                  float eps, int step, int rows, int cols, __nv_bfloat16* wb, __nv_bfloat16* wbt, cudaStream_t st);
 void launch_to_bf16(long long count, const float* w, int rows, int cols, __nv_bfloat16* wb, __nv_bfloat16* wbt,

@@ -166,6 +166,21 @@ def test_production_fp32_vs_fp64(production_fp32):
         assert_close(g32[key], g64[key], 1e-4, key)
 
 
+def test_reference_production_fp32_vs_fp64():
+    """The reference's own settings (atmosphere_lut.clj:20-63: 35 km
+    atmosphere, T 64x255, E 16x63, S/M 32x127x32x8, 100 ray steps, 15 sphere
+    steps, 5 iterations), the build `clj -T:build atmosphere-lut` runs: every
+    cell of the FP32 path within 1e-4 of the FP64 path.  Its density at the
+    top of the atmosphere is not negligible, which tests the sun tables near
+    the top."""
+    g32 = A.build(C.reference_production())
+    cfg64 = C.reference_production()
+    cfg64.precision = C.FP64
+    g64 = A.build(cfg64)
+    for key in ("transmittance", "surface_radiance", "ray_scatter", "mie_strength"):
+        assert_close(g32[key], g64[key], 1e-4, key)
+
+
 def test_production_properties(production_fp32):
     """Size-independent properties of the full tables."""
     cfg, g = production_fp32
