@@ -260,6 +260,18 @@ int make_params(const sfsim_atmo_config& c, AtmoParams& P) {
   // peak lies (it spans sqrt(2 R H_mie)), logarithmic beyond
   P.f_desc_s = (float)(1.2 * std::sqrt(2.0 * P.R * P.mie_scale));
   P.f_desc_inv_s = 1.0f / P.f_desc_s;
+  // Near the top of the climbing sun-ray table the sums fall to zero like
+  // sqrt(q_top - q), which bilinear interpolation follows badly: a numpy model
+  // put the optical-depth error of the last row at about 0.18 times the
+  // Rayleigh density at the top relative to the ground (2.2e-3 in a 35 km
+  // atmosphere), 1e-5 eight rows down.  Where that density exceeds 2e-5 the
+  // rays starting in the top eight rows are integrated directly; elsewhere
+  // (the 100 km atmospheres) the whole table is read.
+  {
+    const double top_density = std::exp(-P.H / P.ray_scale);
+    const double x = (double)(kSunNR - 9) / (double)(kSunNR - 1);
+    P.f_sun_qlim = top_density > 2e-5 ? (float)(P.Hh2 * x * x) : 3.0e38f;
+  }
   const double gs[2] = {P.ray_g, P.mie_g};
   for (int m = 0; m < 2; m++) {
     const double g = gs[m];

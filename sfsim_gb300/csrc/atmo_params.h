@@ -55,6 +55,9 @@ struct AtmoParams {
   // descending sun-ray table of the FP32 first order: atmosphere height and
   // the distance scale s of its asinh coordinate (and 1 / s)
   float f_H, f_desc_s, f_desc_inv_s;
+  // climbing sun rays from q >= f_sun_qlim are integrated directly (the top
+  // rows of the climbing table where the density at the top matters)
+  float f_sun_qlim;
   int hpoly_n;                        // number of coefficients
 };
 

@@ -22,7 +22,8 @@
 //    the exit distance between its zenith and horizontal values), sums
 //    interpolated bilinearly: its integrand falls monotonically, so the sums
 //    are smooth in those coordinates (transmittance error below 1e-5), except
-//    in the top eight rows, whose rays are integrated directly;
+//    in the top eight rows of an atmosphere dense at the top (the reference's
+//    35 km one), whose rays are integrated directly;
 //  * a descending ray (p_s.l < 0) from a 1024 x 2048 grid of (perigee height
 //    / H, asinh(d / s) / asinh(dmax / s)), d the distance from p_s to the
 //    perigee, dmax that from the perigee to the exit, s = 1.2 sqrt(2 R H_mie).
@@ -216,12 +217,10 @@ __global__ void __launch_bounds__(WARPS * 32, 4) k_first_order(const AtmoParams*
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int ncell = d.n2 * d.n3;
   const Real Hh2 = std::is_same<Real, float>::value ? (Real)P.f_Hh2 : (Real)P.Hh2;
-  // Climbing rays from the top eight rows of the climbing table are
-  // integrated directly: there the exit distance, and with it the sums, goes
-  // to zero like sqrt(q_top - q), which bilinear interpolation follows badly
-  // (optical-depth errors up to 2e-3 in the last row of a 35 km atmosphere,
-  // whose density at the top is not negligible; 1e-5 eight rows down).
-  const Real qlim = Hh2 * (Real(kSunNR - 9) / Real(kSunNR - 1)) * (Real(kSunNR - 9) / Real(kSunNR - 1));
+  // climbing rays from the top rows of the climbing table, where its
+  // interpolation fails for atmospheres dense at the top, are integrated
+  // directly (AtmoParams::f_sun_qlim)
+  const Real qlim = (Real)P.f_sun_qlim;
   constexpr int NP = Bulk<Real>::kSunNP;
   const Real* hp = Bulk<Real>::hpr(P);
   Real hc[NP];
