@@ -235,6 +235,26 @@ def test_device_build_matches_host_build():
         assert np.array_equal(t.cpu().numpy(), host[key]), key
 
 
+def test_transfer_bytes_reported():
+    """sfsim_atmo_last_transfer_bytes: a host-output build copies its
+    parameters and quadrature directions in and the four tables out; a
+    device-output build copies nothing out."""
+    import ctypes
+    import torch
+    from sfsim_gb300 import _lib
+    L = _lib.load()
+    cfg = C.small_fp64(precision=C.FP32)
+    A.build(cfg)
+    h2d, d2h = ctypes.c_ulonglong(), ctypes.c_ulonglong()
+    L.sfsim_atmo_last_transfer_bytes(ctypes.byref(h2d), ctypes.byref(d2h))
+    assert d2h.value == 4 * sum(cfg.table_sizes())
+    assert 0 < h2d.value < 1 << 20
+    A.build_device(cfg)
+    torch.cuda.synchronize()
+    L.sfsim_atmo_last_transfer_bytes(ctypes.byref(h2d), ctypes.byref(d2h))
+    assert d2h.value == 0 and h2d.value > 0
+
+
 def test_generate_files(tmp_path):
     cfg = C.small_fp64(precision=C.FP32)
     paths = A.generate_atmosphere_luts(str(tmp_path), cfg)
