@@ -127,9 +127,16 @@ __device__ __forceinline__ bool gemm_epilogue32_staged(const GemmArgs& g, const 
     for (int i = 0; i < 32; i++) z[i] *= sg[lane * 33 + i];
     __syncwarp();
   }
+  // with SiLU' requested, the logistic s of each z serves both SiLU' and
+  // SiLU (z s): one exponential and one reciprocal per element
+  const bool silu_done = g.Dsilu && g.silu;
   if (g.Dsilu) {
 #pragma unroll
-    for (int i = 0; i < 32; i++) sg[lane * 33 + i] = dsilu(z[i]);
+    for (int i = 0; i < 32; i++) {
+      const float sgm = 1.0f / (1.0f + __expf(-z[i]));
+      sg[lane * 33 + i] = sgm * (1.0f + z[i] * (1.0f - sgm));
+      if (g.silu) z[i] *= sgm;
+    }
     __syncwarp();
 #pragma unroll
     for (int k = 0; k < 8; k++) {
@@ -142,7 +149,7 @@ __device__ __forceinline__ bool gemm_epilogue32_staged(const GemmArgs& g, const 
   if (g.Hbf16 || g.HTbf16) {
     __nv_bfloat16 h[32];
 #pragma unroll
-    for (int i = 0; i < 32; i++) h[i] = __float2bfloat16(g.silu ? silu(z[i]) : z[i]);
+    for (int i = 0; i < 32; i++) h[i] = __float2bfloat16(g.silu && !silu_done ? silu(z[i]) : z[i]);
     if (g.Hbf16) {
       // 16 packed pairs per row; lane l moves 16 bytes of row 8k + l / 4
       uint32_t* s32 = reinterpret_cast<uint32_t*>(sg);
@@ -219,24 +226,29 @@ __device__ __forceinline__ void gemm_epilogue32(const GemmArgs& g, const uint32_
       for (int i = 0; i < 8; i++)
         if (nb + i < g.N) g.Cf32[(long long)m * g.ldc + nb + i] = z[i];
     }
+    const bool silu_done = g.Dsilu && g.silu;
     if (g.Dsilu) {
       float* dst = g.Dsilu + (long long)m * g.N + nb;
-      if (full8 && (g.N % 4 == 0) && (reinterpret_cast<uintptr_t>(g.Dsilu) & 15) == 0) {
-        float d[8];
+      float d[8];
 #pragma unroll
-        for (int i = 0; i < 8; i++) d[i] = dsilu(z[i]);
+      for (int i = 0; i < 8; i++) {
+        const float sgm = 1.0f / (1.0f + __expf(-z[i]));
+        d[i] = sgm * (1.0f + z[i] * (1.0f - sgm));
+        if (g.silu) z[i] *= sgm;
+      }
+      if (full8 && (g.N % 4 == 0) && (reinterpret_cast<uintptr_t>(g.Dsilu) & 15) == 0) {
         *reinterpret_cast<float4*>(dst) = make_float4(d[0], d[1], d[2], d[3]);
         *reinterpret_cast<float4*>(dst + 4) = make_float4(d[4], d[5], d[6], d[7]);
       } else {
 #pragma unroll
         for (int i = 0; i < 8; i++)
-          if (nb + i < g.N) dst[i] = dsilu(z[i]);
+          if (nb + i < g.N) dst[i] = d[i];
       }
     }
     if (g.Hbf16 || g.HTbf16) {
       __nv_bfloat16 h[8];
 #pragma unroll
-      for (int i = 0; i < 8; i++) h[i] = __float2bfloat16(g.silu ? silu(z[i]) : z[i]);
+      for (int i = 0; i < 8; i++) h[i] = __float2bfloat16(g.silu && !silu_done ? silu(z[i]) : z[i]);
       if (g.Hbf16) {
         __nv_bfloat16* dst = g.Hbf16 + (long long)m * g.ldh + nb;
         if (full8 && (g.ldh % 8 == 0) && (reinterpret_cast<uintptr_t>(g.Hbf16) & 15) == 0) {
