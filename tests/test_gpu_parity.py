@@ -134,20 +134,21 @@ def test_production_first_order_nodes(production_fp32):
 
 def test_production_order_steps(production_fp32):
     """Each order's J, dS and dE at production size, one step at a time: the
-    oracle evaluates sampled nodes from the GPU's previous-order tables."""
+    oracle evaluates sampled nodes (6 fixed and 24 seeded ones per order,
+    every order) from the GPU's previous-order tables."""
     cfg, gpu = production_fp32
     s = cfg.shapes()[2]
     S1R = gpu["rayleigh_first"].astype(np.float64)
     M = gpu["mie_first"].astype(np.float64)
     dE_prev = gpu["surface_base"].astype(np.float64)
-    for it in (0, 1, cfg.iterations - 1):
+    for it in range(cfg.iterations):
         if it == 0:
             dS_prev, mf = S1R, M
         else:
             dS_prev, mf = gpu["ray_scatter_delta"][it - 1].astype(np.float64), None
             dE_prev = gpu["surface_delta"][it - 1].astype(np.float64)
         J = gpu["point_scatter"][it].astype(np.float64)
-        for (i, j, k, a) in _nodes(s, 6, 10 + it):
+        for (i, j, k, a) in _nodes(s, 24, 10 + it):
             jo = O.point_scatter_node(cfg, dS_prev, dE_prev, i, j, k, a, mie_first=mf)
             assert_close(J[i, j, k, a], jo, 1e-4, f"J[{it}]{(i, j, k, a)}")
             so = O.ray_scatter_node(cfg, J, i, j, k, a)
