@@ -167,3 +167,31 @@ def test_no_gpu_new_entry_points_report_enodev(lib):
     assert lib.sfsim_atmo_plan_build(None, None, None, None, None, None) == -6
     assert lib.sfsim_atmo_plan_destroy(None) == 0
     assert lib.sfsim_atmo_cond_surrogate_destroy(None) == 0
+
+
+@pytest.mark.gpu
+def test_native_caller_matches_python(tmp_path):
+    """tests/abi_build.c, compiled against include/sfsim_atmo.h and linked with
+    the library the way a native host would, builds the small FP32 tables;
+    they equal the tables built through the Python binding bit for bit."""
+    import shutil
+    import subprocess
+
+    from sfsim_gb300 import atmosphere_lut as A
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if not cc:
+        pytest.skip("no C compiler")
+    lib_dir = os.path.dirname(_lib.LIB_PATH)
+    exe = str(tmp_path / "abi_build")
+    subprocess.run([cc, "-std=c99", "-Wall", "-Werror", "-I", os.path.join(ROOT, "include"),
+                    os.path.join(ROOT, "tests", "abi_build.c"), "-L", lib_dir, "-lsfsim_atmo",
+                    "-Wl,-rpath," + lib_dir, "-o", exe], check=True)
+    out = str(tmp_path / "tables.bin")
+    r = subprocess.run([exe, out], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    native = np.fromfile(out, dtype=np.float32)
+    ref = A.build(C.small_fp64(precision=C.FP32))
+    py = np.concatenate([ref[k].ravel() for k in ("transmittance", "surface_radiance", "ray_scatter",
+                                                  "mie_strength")])
+    assert native.shape == py.shape
+    assert np.array_equal(native, py)
