@@ -621,13 +621,13 @@ def run_queries(C, steps=20000, batch=65536, direct_samples=1 << 25, lr=3e-3, hu
         t_fb, (fb, nf) = _timed(lambda: ctx.surrogate(x, v, l, threshold=thr, out=out), reps=1)
         r[f"surrogate_fallback_{thr:g}"] = {"qps": qps(t_fb), "fallback_fraction": nf / n,
                                             "err": query_error_stats(fb, direct), "vs_direct": t_direct / t_fb}
-    r["c4_recipe_baseline"] = c4_recipe_baseline(ctx, cfg, x[: 1 << 21], v[: 1 << 21], l[: 1 << 21],
+    r["first_recipe_baseline"] = first_recipe_baseline(ctx, cfg, x[: 1 << 21], v[: 1 << 21], l[: 1 << 21],
                                                  direct[: 1 << 21], steps=steps, batch=batch)
     ctx.close()
     return r
 
 
-def c4_recipe_baseline(ctx, cfg, x, v, l, direct, steps, batch, n_direct=1 << 23, seed=1):
+def first_recipe_baseline(ctx, cfg, x, v, l, direct, steps, batch, n_direct=1 << 23, seed=1):
     """The surrogate recipe as first specified, the baseline the product's
     correction network replaced: the four table coordinates -> 16 sin/cos
     Fourier frequencies each (128 features) -> 4 x 256 SiLU -> 3 log-RGB
