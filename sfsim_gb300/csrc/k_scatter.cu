@@ -547,6 +547,13 @@ void launch_surface_radiance(const AtmoParams* params, const BuildDims& d, const
 // gathers bilinearly from the plane at its own sun-elevation coordinate
 // (from p_s.l) and sun-angle coordinate (v.l, constant along the ray).
 // T(x, p_s) comes from k_view_rows.
+//
+// The planes are stored column by column: texel (sun elevation r, heading a)
+// at a * C + r, three values each, with C = n2 + 4 at n2 = 32.  A warp of
+// the plane build then stores 4 sun elevations x 8 headings to 32 distinct
+// banks, and the gather's loads (a warp's 32 nodes read rows spread by
+// their own sun elevations in up to 8 heading columns) meet fewer bank
+// conflicts than with rows of 24 values.
 // ---------------------------------------------------------------------------
 
 // Per-sample constants of one chunk of CH ray samples, as arrays so that two
@@ -560,11 +567,36 @@ struct RayChunk {
   int p[4][CH];
 };
 
+// Texels of one heading column of a ray-scatter plane (see above): n2, plus
+// the padding that makes the column stride 4 modulo 32 where that costs at
+// most a quarter more.
+__host__ __device__ constexpr int ray_plane_column(int n2) {
+  return ((4 - n2) % 32 + 32) % 32 <= n2 / 4 ? n2 + ((4 - n2) % 32 + 32) % 32 : n2;
+}
+
+// Bytes of the CH planes of one chunk (a multiple of 16 for even CH).
+template <class Real, int CH>
+__host__ __device__ constexpr size_t ray_plane_bytes(const BuildDims& d) {
+  return sizeof(Real) * 3 * (size_t)CH * ray_plane_column(d.n2) * d.n3;
+}
+
+// The view row's samples (k_view_rows) are copied into shared memory once
+// per block when they take at most this many bytes, so that each chunk's
+// constants come from there instead of a global-memory round trip.
+constexpr size_t kRayStageBytes = 16384;
+template <class Real>
+__host__ __device__ constexpr bool ray_stage_rows(int S) {
+  return (size_t)S * sizeof(RowSample<Real>) <= kRayStageBytes;
+}
+
 // Three FP32 blocks per SM: 80 registers a thread hold the plane build's
 // cached J corners without spills (four blocks at 64 registers spilled).
 constexpr int ray_scatter_min_blocks(size_t real_size) { return real_size == 4 ? 3 : 1; }
 
-template <class Real, int CH>
+// WIDE: a row has more cells than the block has threads, and the plane build
+// walks them blockDim.x apart; a separate instantiation, so that the
+// one-cell-per-thread build keeps its registers.
+template <class Real, int CH, bool WIDE>
 __global__ void __launch_bounds__(256, ray_scatter_min_blocks(sizeof(Real)))
     k_ray_scatter(const AtmoParams* params, BuildDims d, const RowInfo* rowinfo, const RowSample<Real>* rows,
                   const CellGeom<Real>* geom, const Remap4<Real>* remap, const Real* J, Vec4<Real>* dS) {
@@ -578,6 +610,26 @@ __global__ void __launch_bounds__(256, ray_scatter_min_blocks(sizeof(Real)))
   RayChunk<Real, CH>& sc = *reinterpret_cast<RayChunk<Real, CH>*>(smem_raw);
   Real* plane = reinterpret_cast<Real*>(smem_raw + ((sizeof(RayChunk<Real, CH>) + 15) & ~size_t(15)));
   const RowSample<Real>* rs = rows + (b * nrows + row) * d.S;
+  if (ray_stage_rows<Real>(d.S)) {
+    // 16-byte words where the row's samples start on a 16-byte boundary and
+    // fill whole words (S = 128: 6656 bytes a row), else 4-byte words
+    // (sizeof(RowSample<float>) is 52); the stage itself is 16-byte aligned.
+    // The first chunk's barrier publishes the copy.
+    static_assert(sizeof(RowSample<Real>) % 4 == 0, "rows are copied in 4-byte words");
+    RowSample<Real>* stage = reinterpret_cast<RowSample<Real>*>(
+        reinterpret_cast<unsigned char*>(plane) + ray_plane_bytes<Real, CH>(d));
+    const size_t bytes = d.S * sizeof(RowSample<Real>);
+    if ((reinterpret_cast<size_t>(rs) & 15) == 0 && bytes % 16 == 0) {
+      const int4* g = reinterpret_cast<const int4*>(rs);
+      int4* sd = reinterpret_cast<int4*>(stage);
+      for (int w = threadIdx.x; w < (int)(bytes / 16); w += blockDim.x) sd[w] = g[w];
+    } else {
+      const int* g = reinterpret_cast<const int*>(rs);
+      int* sd = reinterpret_cast<int*>(stage);
+      for (int w = threadIdx.x; w < (int)(bytes / 4); w += blockDim.x) sd[w] = g[w];
+    }
+    rs = stage;
+  }
   const RowInfo ri = rowinfo[b * nrows + row];
   const long long n4 = d.n4();
   const Real* tJ = J + (long long)b * 3 * n4;  // planar [channel][node]
@@ -585,7 +637,8 @@ __global__ void __launch_bounds__(256, ray_scatter_min_blocks(sizeof(Real)))
   const Real scale2 = Bulk<Real>::sun_scale(d);
   const RowR<Real> rw = row_r<Real>(ri);
   const Real rr = rw.r, D0 = rw.D[0], D1 = rw.D[1], D2 = rw.D[2];
-  const int n3x3 = 3 * d.n3;
+  const int col = ray_plane_column(d.n2);  // texels of a heading column
+  const int pl3 = 3 * d.n3 * col;           // values of a plane
 
   for (int c0 = 0; c0 < ncell; c0 += blockDim.x) {
     const int cell = c0 + threadIdx.x;
@@ -597,8 +650,8 @@ __global__ void __launch_bounds__(256, ray_scatter_min_blocks(sizeof(Real)))
       b0 = rr * g.lx;
       Dl = fma(D0, g.lx, fma(D1, g.ly, D2 * g.lz));
       const Remap4<Real> m = remap[node0 + cell];  // its sun-angle coordinate is that of (v, l)
-      o3u = 3 * m.u[3];
-      o3v = 3 * upper_index(m.u[3], d.n3);
+      o3u = 3 * col * m.u[3];
+      o3v = 3 * col * upper_index(m.u[3], d.n3);
       s3 = m.s[3];
     }
     const R2 b02 = mk2(b0, b0), Dl2 = mk2(Dl, Dl), s32 = mk2(s3, s3);
@@ -628,12 +681,13 @@ __global__ void __launch_bounds__(256, ray_scatter_min_blocks(sizeof(Real)))
       }
       __syncthreads();
       // the plane of samples (ch, ch + 1): bilinear in (height, elevation)
-      if (ncell <= (int)blockDim.x) {
+      if constexpr (!WIDE) {
         // one cell per thread: its J corner values stay in registers while
         // consecutive samples share their (height, elevation) corners (the
         // first corner's offset identifies all four); about half the pairs do
         if (threadIdx.x < ncell) {
           const int t = threadIdx.x;
+          const int st3 = 3 * ((t % d.n3) * col + t / d.n3);  // texel (k = t / n3, a = t mod n3)
           for (int ch = 0; ch < nch; ch += 2) {
             const bool two = ch + 1 < nch;
             const int ch1 = two ? ch + 1 : ch;
@@ -700,8 +754,8 @@ __global__ void __launch_bounds__(256, ray_scatter_min_blocks(sizeof(Real)))
               key_b = pb;
             }
             const R2 s0 = mk2(sc.s0[ch], sc.s0[ch1]), s1 = mk2(sc.s1[ch], sc.s1[ch1]);
-            Real* dst0 = plane + 3 * (ch * ncell + t);
-            Real* dst1 = dst0 + 3 * ncell;
+            Real* dst0 = plane + ch * pl3 + st3;
+            Real* dst1 = dst0 + pl3;
 #pragma unroll
             for (int c = 0; c < 3; c++) {
               const R2 A = mk2(ca[4 * c], cb[4 * c]), B = mk2(ca[4 * c + 1], cb[4 * c + 1]);
@@ -713,25 +767,27 @@ __global__ void __launch_bounds__(256, ray_scatter_min_blocks(sizeof(Real)))
             }
           }
         }
-      } else
-      for (int ch = 0; ch < nch; ch += 2) {
-        const bool two = ch + 1 < nch;
-        const int ch1 = two ? ch + 1 : ch;
-        const int pa[4] = {sc.p[0][ch], sc.p[1][ch], sc.p[2][ch], sc.p[3][ch]};
-        const int pb[4] = {sc.p[0][ch1], sc.p[1][ch1], sc.p[2][ch1], sc.p[3][ch1]};
-        const R2 s0 = mk2(sc.s0[ch], sc.s0[ch1]), s1 = mk2(sc.s1[ch], sc.s1[ch1]);
+      } else {
         for (int t = threadIdx.x; t < ncell; t += blockDim.x) {
-          Real* dst0 = plane + 3 * (ch * ncell + t);
-          Real* dst1 = dst0 + 3 * ncell;
+          const int st3 = 3 * ((t % d.n3) * col + t / d.n3);
+          for (int ch = 0; ch < nch; ch += 2) {
+            const bool two = ch + 1 < nch;
+            const int ch1 = two ? ch + 1 : ch;
+            const int pa[4] = {sc.p[0][ch], sc.p[1][ch], sc.p[2][ch], sc.p[3][ch]};
+            const int pb[4] = {sc.p[0][ch1], sc.p[1][ch1], sc.p[2][ch1], sc.p[3][ch1]};
+            const R2 s0 = mk2(sc.s0[ch], sc.s0[ch1]), s1 = mk2(sc.s1[ch], sc.s1[ch1]);
+            Real* dst0 = plane + ch * pl3 + st3;
+            Real* dst1 = dst0 + pl3;
 #pragma unroll
-          for (int c = 0; c < 3; c++) {
-            const Real* tc = tJ + c * n4 + t;
-            const R2 A = mk2(tc[pa[0]], tc[pb[0]]), B = mk2(tc[pa[1]], tc[pb[1]]);
-            const R2 C = mk2(tc[pa[2]], tc[pb[2]]), E = mk2(tc[pa[3]], tc[pb[3]]);
-            const R2 lo = fma2(sub2(B, A), s1, A), hi = fma2(sub2(E, C), s1, C);
-            const R2 v = fma2(sub2(hi, lo), s0, lo);
-            dst0[c] = v.x;
-            if (two) dst1[c] = v.y;
+            for (int c = 0; c < 3; c++) {
+              const Real* tc = tJ + c * n4 + t;
+              const R2 A = mk2(tc[pa[0]], tc[pb[0]]), B = mk2(tc[pa[1]], tc[pb[1]]);
+              const R2 C = mk2(tc[pa[2]], tc[pb[2]]), E = mk2(tc[pa[3]], tc[pb[3]]);
+              const R2 lo = fma2(sub2(B, A), s1, A), hi = fma2(sub2(E, C), s1, C);
+              const R2 v = fma2(sub2(hi, lo), s0, lo);
+              dst0[c] = v.x;
+              if (two) dst1[c] = v.y;
+            }
           }
         }
       }
@@ -746,10 +802,10 @@ __global__ void __launch_bounds__(256, ray_scatter_min_blocks(sizeof(Real)))
           split_coord_r<Real>(ie.x, d.n2, &ua, &sa);
           split_coord_r<Real>(ie.y, d.n2, &ub, &sb);
           const R2 s2 = mk2(sa, sb);
-          const Real* loa = plane + 3 * ch * ncell + ua * n3x3;
-          const Real* hia = ua + 1 < d.n2 ? loa + n3x3 : loa;
-          const Real* lob = plane + 3 * (ch + 1) * ncell + ub * n3x3;
-          const Real* hib = ub + 1 < d.n2 ? lob + n3x3 : lob;
+          const Real* loa = plane + ch * pl3 + 3 * ua;
+          const Real* hia = ua + 1 < d.n2 ? loa + 3 : loa;
+          const Real* lob = plane + (ch + 1) * pl3 + 3 * ub;
+          const Real* hib = ub + 1 < d.n2 ? lob + 3 : lob;
 #pragma unroll
           for (int c = 0; c < 3; c++) {
             const R2 lu = mk2(loa[o3u + c], lob[o3u + c]), lv = mk2(loa[o3v + c], lob[o3v + c]);
@@ -764,8 +820,8 @@ __global__ void __launch_bounds__(256, ray_scatter_min_blocks(sizeof(Real)))
           int u2;
           Real s2;
           split_coord_r<Real>(sun_elevation_index_r<Real>(sin_el, scale2), d.n2, &u2, &s2);
-          const Real* lo = plane + 3 * ch * ncell + u2 * n3x3;
-          const Real* hi = u2 + 1 < d.n2 ? lo + n3x3 : lo;
+          const Real* lo = plane + ch * pl3 + 3 * u2;
+          const Real* hi = u2 + 1 < d.n2 ? lo + 3 : lo;
 #pragma unroll
           for (int c = 0; c < 3; c++) {
             const Real x0 = fma(lo[o3v + c] - lo[o3u + c], s3, lo[o3u + c]);
@@ -789,12 +845,13 @@ __global__ void __launch_bounds__(256, ray_scatter_min_blocks(sizeof(Real)))
 
 constexpr int kRayChunk = 16;  // ray samples per chunk of k_ray_scatter
 
-// Dynamic shared memory of k_ray_scatter: the chunk's constants and one
-// plane of n2 x n3 RGB texels per sample.
+// Dynamic shared memory of k_ray_scatter: the chunk's constants, one plane
+// of n3 heading columns of RGB texels per sample, and the staged row
+// samples.
 template <class Real>
 size_t ray_scatter_smem(const BuildDims& d) {
-  return ((sizeof(RayChunk<Real, kRayChunk>) + 15) & ~size_t(15)) +
-         sizeof(Real) * 3 * (size_t)kRayChunk * d.n2 * d.n3;
+  return ((sizeof(RayChunk<Real, kRayChunk>) + 15) & ~size_t(15)) + ray_plane_bytes<Real, kRayChunk>(d) +
+         (ray_stage_rows<Real>(d.S) ? (size_t)d.S * sizeof(RowSample<Real>) : 0);
 }
 
 template <class Real>
@@ -805,11 +862,10 @@ int launch_ray_scatter(const AtmoParams* params, const BuildDims& d, const RowIn
   const int ncell = d.n2 * d.n3;
   const int block = ncell >= 256 ? 256 : ((ncell + 31) / 32) * 32;
   const size_t smem = ray_scatter_smem<Real>(d);
-  if (cudaFuncSetAttribute(k_ray_scatter<Real, CH>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
-      cudaSuccess)
-    return -1;
+  auto kernel = ncell > block ? k_ray_scatter<Real, CH, true> : k_ray_scatter<Real, CH, false>;
+  if (cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return -1;
   dim3 grid((unsigned)d.rows(), d.B);
-  k_ray_scatter<Real, CH><<<grid, block, smem, st>>>(params, d, rowinfo, rows, geom, remap, J, dS);
+  kernel<<<grid, block, smem, st>>>(params, d, rowinfo, rows, geom, remap, J, dS);
   return 0;
 }
 
