@@ -72,6 +72,32 @@ def test_odd_shapes_match_oracle(precision):
         assert_close(gpu[key], ref[key], tol, key)
 
 
+def wide_config(precision):
+    return C.make_config(height=100000.0, transmittance_shape=(7, 9), surface_radiance_shape=(4, 6),
+                         ray_scatter_shape=(3, 5, 20, 14), ray_steps=150, sphere_steps=8, iterations=1,
+                         precision=precision)
+
+
+@pytest.fixture(scope="module")
+def wide_oracle():
+    return O.build(wide_config(C.FP64), intermediates=True)
+
+
+@pytest.mark.parametrize("precision", [C.FP64, C.FP32])
+def test_wide_rows_and_long_rays_match_oracle(wide_oracle, precision):
+    """A view row of 20 x 14 = 280 nodes (more than a ray-scatter block's 256
+    threads: the plane build walks its cells) and 150 ray steps (more than
+    the 128 samples whose constants a block keeps at once: they are formed
+    chunk by chunk from the staged row samples)."""
+    ref = wide_oracle
+    gpu = A.build(wide_config(precision), intermediates=True)
+    tol = TOL[precision]
+    assert_close(gpu["point_scatter"][0], ref["point_scatter"][0], tol, "point_scatter[0]")
+    assert_close(gpu["ray_scatter_delta"][0], ref["ray_scatter_delta"][0], tol, "ray_scatter_delta[0]")
+    for key in ("transmittance", "surface_radiance", "ray_scatter", "mie_strength"):
+        assert_close(gpu[key], ref[key], tol, key)
+
+
 def test_zero_iterations_and_shader_tables():
     """iterations = 0 (E stays 0) at the reference shader-test shapes (12^4, 10 steps)."""
     cfg = C.shader_test()
