@@ -548,12 +548,14 @@ void launch_surface_radiance(const AtmoParams* params, const BuildDims& d, const
 // (from p_s.l) and sun-angle coordinate (v.l, constant along the ray).
 // T(x, p_s) comes from k_view_rows.
 //
-// The planes are stored column by column: texel (sun elevation r, heading a)
-// at a * C + r, three values each, with C = n2 + 4 at n2 = 32.  A warp of
-// the plane build then stores 4 sun elevations x 8 headings to 32 distinct
-// banks, and the gather's loads (a warp's 32 nodes read rows spread by
-// their own sun elevations in up to 8 heading columns) meet fewer bank
-// conflicts than with rows of 24 values.
+// Plane layout (three values a texel).  With 32 sun elevations (the
+// production shapes) the planes are stored column by column, texel
+// (sun elevation r, heading a) at a * 36 + r: a warp of the plane build then
+// stores 4 sun elevations x 8 headings to 32 distinct banks, and the
+// gather's loads (a warp's 32 nodes read rows spread by their own sun
+// elevations in up to 8 heading columns) meet a third fewer bank conflicts
+// than with rows of 24 values.  Other shapes keep rows (texel at r * n3 + a):
+// at 16 sun elevations a CPU model of the gathers finds rows best.
 // ---------------------------------------------------------------------------
 
 // Per-sample constants of one chunk of CH ray samples, as arrays so that two
@@ -567,17 +569,17 @@ struct RayChunk {
   int p[4][CH];
 };
 
-// Texels of one heading column of a ray-scatter plane (see above): n2, plus
-// the padding that makes the column stride 4 modulo 32 where that costs at
-// most a quarter more.
-__host__ __device__ constexpr int ray_plane_column(int n2) {
-  return ((4 - n2) % 32 + 32) % 32 <= n2 / 4 ? n2 + ((4 - n2) % 32 + 32) % 32 : n2;
+// Column-major planes (see above) for multiples of 32 sun elevations, with
+// columns of n2 + 4 texels; rows of n3 texels otherwise.
+__host__ __device__ constexpr bool ray_plane_by_column(int n2) { return n2 % 32 == 0; }
+__host__ __device__ constexpr int ray_plane_texels(const BuildDims& d) {
+  return ray_plane_by_column(d.n2) ? (d.n2 + 4) * d.n3 : d.n2 * d.n3;
 }
 
 // Bytes of the CH planes of one chunk (a multiple of 16 for even CH).
 template <class Real, int CH>
 __host__ __device__ constexpr size_t ray_plane_bytes(const BuildDims& d) {
-  return sizeof(Real) * 3 * (size_t)CH * ray_plane_column(d.n2) * d.n3;
+  return sizeof(Real) * 3 * (size_t)CH * ray_plane_texels(d);
 }
 
 // The view row's samples (k_view_rows) are copied into shared memory once
@@ -595,8 +597,8 @@ constexpr int ray_scatter_min_blocks(size_t real_size) { return real_size == 4 ?
 
 // WIDE: a row has more cells than the block has threads, and the plane build
 // walks them blockDim.x apart; a separate instantiation, so that the
-// one-cell-per-thread build keeps its registers.
-template <class Real, int CH, bool WIDE>
+// one-cell-per-thread build keeps its registers.  COLS: column-major planes.
+template <class Real, int CH, bool WIDE, bool COLS>
 __global__ void __launch_bounds__(256, ray_scatter_min_blocks(sizeof(Real)))
     k_ray_scatter(const AtmoParams* params, BuildDims d, const RowInfo* rowinfo, const RowSample<Real>* rows,
                   const CellGeom<Real>* geom, const Remap4<Real>* remap, const Real* J, Vec4<Real>* dS) {
@@ -637,8 +639,11 @@ __global__ void __launch_bounds__(256, ray_scatter_min_blocks(sizeof(Real)))
   const Real scale2 = Bulk<Real>::sun_scale(d);
   const RowR<Real> rw = row_r<Real>(ri);
   const Real rr = rw.r, D0 = rw.D[0], D1 = rw.D[1], D2 = rw.D[2];
-  const int col = ray_plane_column(d.n2);  // texels of a heading column
-  const int pl3 = 3 * d.n3 * col;           // values of a plane
+  // values between texels one sun elevation (row3) and one heading (col3)
+  // apart, and of a plane; one of the steps is a constant
+  const int row3 = COLS ? 3 : 3 * d.n3;
+  const int col3 = COLS ? 3 * (d.n2 + 4) : 3;
+  const int pl3 = 3 * ray_plane_texels(d);
 
   for (int c0 = 0; c0 < ncell; c0 += blockDim.x) {
     const int cell = c0 + threadIdx.x;
@@ -650,8 +655,8 @@ __global__ void __launch_bounds__(256, ray_scatter_min_blocks(sizeof(Real)))
       b0 = rr * g.lx;
       Dl = fma(D0, g.lx, fma(D1, g.ly, D2 * g.lz));
       const Remap4<Real> m = remap[node0 + cell];  // its sun-angle coordinate is that of (v, l)
-      o3u = 3 * col * m.u[3];
-      o3v = 3 * col * upper_index(m.u[3], d.n3);
+      o3u = col3 * m.u[3];
+      o3v = col3 * upper_index(m.u[3], d.n3);
       s3 = m.s[3];
     }
     const R2 b02 = mk2(b0, b0), Dl2 = mk2(Dl, Dl), s32 = mk2(s3, s3);
@@ -687,7 +692,7 @@ __global__ void __launch_bounds__(256, ray_scatter_min_blocks(sizeof(Real)))
         // first corner's offset identifies all four); about half the pairs do
         if (threadIdx.x < ncell) {
           const int t = threadIdx.x;
-          const int st3 = 3 * ((t % d.n3) * col + t / d.n3);  // texel (k = t / n3, a = t mod n3)
+          const int st3 = COLS ? (t % d.n3) * col3 + 3 * (t / d.n3) : 3 * t;  // texel (k = t / n3, a = t mod n3)
           for (int ch = 0; ch < nch; ch += 2) {
             const bool two = ch + 1 < nch;
             const int ch1 = two ? ch + 1 : ch;
@@ -769,7 +774,7 @@ __global__ void __launch_bounds__(256, ray_scatter_min_blocks(sizeof(Real)))
         }
       } else {
         for (int t = threadIdx.x; t < ncell; t += blockDim.x) {
-          const int st3 = 3 * ((t % d.n3) * col + t / d.n3);
+          const int st3 = COLS ? (t % d.n3) * col3 + 3 * (t / d.n3) : 3 * t;
           for (int ch = 0; ch < nch; ch += 2) {
             const bool two = ch + 1 < nch;
             const int ch1 = two ? ch + 1 : ch;
@@ -802,10 +807,10 @@ __global__ void __launch_bounds__(256, ray_scatter_min_blocks(sizeof(Real)))
           split_coord_r<Real>(ie.x, d.n2, &ua, &sa);
           split_coord_r<Real>(ie.y, d.n2, &ub, &sb);
           const R2 s2 = mk2(sa, sb);
-          const Real* loa = plane + ch * pl3 + 3 * ua;
-          const Real* hia = ua + 1 < d.n2 ? loa + 3 : loa;
-          const Real* lob = plane + (ch + 1) * pl3 + 3 * ub;
-          const Real* hib = ub + 1 < d.n2 ? lob + 3 : lob;
+          const Real* loa = plane + ch * pl3 + row3 * ua;
+          const Real* hia = ua + 1 < d.n2 ? loa + row3 : loa;
+          const Real* lob = plane + (ch + 1) * pl3 + row3 * ub;
+          const Real* hib = ub + 1 < d.n2 ? lob + row3 : lob;
 #pragma unroll
           for (int c = 0; c < 3; c++) {
             const R2 lu = mk2(loa[o3u + c], lob[o3u + c]), lv = mk2(loa[o3v + c], lob[o3v + c]);
@@ -820,8 +825,8 @@ __global__ void __launch_bounds__(256, ray_scatter_min_blocks(sizeof(Real)))
           int u2;
           Real s2;
           split_coord_r<Real>(sun_elevation_index_r<Real>(sin_el, scale2), d.n2, &u2, &s2);
-          const Real* lo = plane + ch * pl3 + 3 * u2;
-          const Real* hi = u2 + 1 < d.n2 ? lo + 3 : lo;
+          const Real* lo = plane + ch * pl3 + row3 * u2;
+          const Real* hi = u2 + 1 < d.n2 ? lo + row3 : lo;
 #pragma unroll
           for (int c = 0; c < 3; c++) {
             const Real x0 = fma(lo[o3v + c] - lo[o3u + c], s3, lo[o3u + c]);
@@ -862,7 +867,11 @@ int launch_ray_scatter(const AtmoParams* params, const BuildDims& d, const RowIn
   const int ncell = d.n2 * d.n3;
   const int block = ncell >= 256 ? 256 : ((ncell + 31) / 32) * 32;
   const size_t smem = ray_scatter_smem<Real>(d);
-  auto kernel = ncell > block ? k_ray_scatter<Real, CH, true> : k_ray_scatter<Real, CH, false>;
+  auto pick = [&](auto cols) {
+    constexpr bool C = decltype(cols)::value;
+    return ncell > block ? k_ray_scatter<Real, CH, true, C> : k_ray_scatter<Real, CH, false, C>;
+  };
+  auto kernel = ray_plane_by_column(d.n2) ? pick(std::true_type{}) : pick(std::false_type{});
   if (cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return -1;
   dim3 grid((unsigned)d.rows(), d.B);
   kernel<<<grid, block, smem, st>>>(params, d, rowinfo, rows, geom, remap, J, dS);

@@ -72,25 +72,37 @@ def test_odd_shapes_match_oracle(precision):
         assert_close(gpu[key], ref[key], tol, key)
 
 
-def wide_config(precision):
+WIDE_SHAPES = [(3, 5, 20, 14), (2, 5, 32, 9)]
+
+
+def wide_config(shape, precision):
     return C.make_config(height=100000.0, transmittance_shape=(7, 9), surface_radiance_shape=(4, 6),
-                         ray_scatter_shape=(3, 5, 20, 14), ray_steps=150, sphere_steps=8, iterations=1,
+                         ray_scatter_shape=shape, ray_steps=150, sphere_steps=8, iterations=1,
                          precision=precision)
 
 
 @pytest.fixture(scope="module")
 def wide_oracle():
-    return O.build(wide_config(C.FP64), intermediates=True)
+    cache = {}
+
+    def get(shape):
+        if shape not in cache:
+            cache[shape] = O.build(wide_config(shape, C.FP64), intermediates=True)
+        return cache[shape]
+    return get
 
 
+@pytest.mark.parametrize("shape", WIDE_SHAPES)
 @pytest.mark.parametrize("precision", [C.FP64, C.FP32])
-def test_wide_rows_and_long_rays_match_oracle(wide_oracle, precision):
-    """A view row of 20 x 14 = 280 nodes (more than a ray-scatter block's 256
-    threads: the plane build walks its cells) and 150 ray steps (more than
-    the 128 samples whose constants a block keeps at once: they are formed
-    chunk by chunk from the staged row samples)."""
-    ref = wide_oracle
-    gpu = A.build(wide_config(precision), intermediates=True)
+def test_wide_rows_and_long_rays_match_oracle(wide_oracle, shape, precision):
+    """View rows of 20 x 14 = 280 and 32 x 9 = 288 nodes (more than a
+    ray-scatter block's 256 threads: the plane build walks its cells; 32 sun
+    elevations store the planes by heading column, 20 by sun-elevation row)
+    and 150 ray steps (more than the 128 samples whose constants a block
+    keeps at once: they are formed chunk by chunk from the staged row
+    samples)."""
+    ref = wide_oracle(shape)
+    gpu = A.build(wide_config(shape, precision), intermediates=True)
     tol = TOL[precision]
     assert_close(gpu["point_scatter"][0], ref["point_scatter"][0], tol, "point_scatter[0]")
     assert_close(gpu["ray_scatter_delta"][0], ref["ray_scatter_delta"][0], tol, "ray_scatter_delta[0]")
