@@ -45,6 +45,7 @@ extern "C" {
 #define SFSIM_ATMO_ENULL        -6  /* a required pointer is NULL */
 #define SFSIM_ATMO_ETOOBIG      -7  /* a size exceeds a fixed capacity */
 #define SFSIM_ATMO_ENUMERIC     -8  /* a result contains NaN or Inf */
+#define SFSIM_ATMO_ESTOPPED     -9  /* an iteration callback stopped the build */
 
 /* Arithmetic of the bulk integrands.  Ray-sphere intersections and the table
  * parameterisations always run in FP64. */
@@ -171,6 +172,50 @@ typedef struct sfsim_atmo_intermediates {
 int sfsim_atmo_build_debug(const sfsim_atmo_config* cfg, float* transmittance,
                            float* surface_radiance, float* ray_scatter,
                            float* mie_strength, const sfsim_atmo_intermediates* inter);
+
+/* The state of a build between two iterations: the four tables the loop of
+ * atmosphere_lut.clj:86-97 carries from one iteration to the next (the last
+ * iteration's ray-scatter and surface-radiance deltas and both sums so far),
+ * as the build holds them.  Each table is one record of four values (RGB
+ * and an unused fourth) per node, in [height][elevation][sun elevation]
+ * [sun heading] order (4-D) or [height][sun elevation] (2-D), of the build's
+ * precision: float for SFSIM_ATMO_FP32, double for SFSIM_ATMO_FP64.  They
+ * are node values, before the outputs' re-interpolation, so a state saved by
+ * one build resumes another build of the same config with the same results
+ * as an uninterrupted build.  (The reference keeps no such state: a failed
+ * run restarts from the first iteration.) */
+typedef struct sfsim_atmo_iteration_state {
+  int iteration;            /* iterations done, 1 .. iterations */
+  void* ray_scatter_delta;  /* dS of that iteration: ray_scatter nodes x 4 values */
+  void* surface_delta;      /* dE of that iteration: surface_radiance nodes x 4 */
+  void* ray_scatter_sum;    /* S so far, the first-order Rayleigh term included */
+  void* surface_sum;        /* E so far */
+} sfsim_atmo_iteration_state;
+
+/* Bytes of each 4-D and each 2-D table of an iteration state of `cfg`. */
+int sfsim_atmo_iteration_state_bytes(const sfsim_atmo_config* cfg, size_t* ray_scatter_bytes,
+                                     size_t* surface_bytes);
+
+/* Called after each iteration with the state in host memory; a nonzero
+ * return stops the build, which then returns SFSIM_ATMO_ESTOPPED without
+ * writing its outputs.  It runs while the library holds its build lock, so
+ * it must not call the library's build entry points. */
+typedef int (*sfsim_atmo_iteration_fn)(const sfsim_atmo_iteration_state* state, void* user);
+
+/* As sfsim_atmo_build (HOST outputs), with a state per iteration and resume.
+ * resume:   NULL, or a state saved by an earlier build of the same config
+ *           (iteration in 1 .. iterations); the build redoes the set-up and
+ *           the first order (milliseconds) and continues with the next
+ *           iteration.
+ * state:    NULL, or caller-owned host buffers that receive the state after
+ *           each iteration; `iteration` is set before on_iteration (which
+ *           may be NULL) is called with it.  It may share `resume`'s buffers.
+ * Each state costs a device-to-host copy of two 4-D and two 2-D tables and a
+ * stream synchronisation. */
+int sfsim_atmo_build_resumable(const sfsim_atmo_config* cfg, const sfsim_atmo_iteration_state* resume,
+                               sfsim_atmo_iteration_state* state, sfsim_atmo_iteration_fn on_iteration,
+                               void* user, float* transmittance, float* surface_radiance,
+                               float* ray_scatter, float* mie_strength);
 
 /* Device time of each stage of the last build, in ms, measured with CUDA
  * events on the build stream when timing is enabled.  Stage order: set-up

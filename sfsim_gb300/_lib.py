@@ -31,6 +31,7 @@ EXPORTS = (
     "sfsim_atmo_cond_surrogate_train", "sfsim_atmo_cond_surrogate_parameters", "sfsim_atmo_cond_surrogate_gradients",
     "sfsim_atmo_query_cond_surrogate", "sfsim_atmo_plan_create", "sfsim_atmo_plan_build", "sfsim_atmo_plan_destroy",
     "sfsim_atmo_set_wait_limit", "sfsim_atmo_wait_selftest", "sfsim_atmo_last_transfer_bytes",
+    "sfsim_atmo_iteration_state_bytes", "sfsim_atmo_build_resumable",
 )
 
 
@@ -43,6 +44,15 @@ class SurrogateConfig(ctypes.Structure):
 class Intermediates(ctypes.Structure):
     _fields_ = [(n, _fp) for n in ("transmittance_nodes", "surface_base", "rayleigh_first", "mie_first",
                                    "point_scatter", "surface_delta", "ray_scatter_delta")]
+
+
+class IterationState(ctypes.Structure):
+    """sfsim_atmo_iteration_state: the four tables carried from one iteration to the next."""
+    _fields_ = [("iteration", ctypes.c_int), ("ray_scatter_delta", ctypes.c_void_p), ("surface_delta", ctypes.c_void_p),
+                ("ray_scatter_sum", ctypes.c_void_p), ("surface_sum", ctypes.c_void_p)]
+
+
+ITERATION_FN = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.POINTER(IterationState), ctypes.c_void_p)
 
 
 class AtmoError(RuntimeError):
@@ -119,6 +129,9 @@ def load(build: bool = False):
     L.sfsim_atmo_set_wait_limit.restype = ctypes.c_longlong
     L.sfsim_atmo_wait_selftest.argtypes = [ctypes.c_int]
     L.sfsim_atmo_last_transfer_bytes.argtypes = [ctypes.POINTER(ctypes.c_ulonglong)] * 2
+    L.sfsim_atmo_iteration_state_bytes.argtypes = [_cfgp, ctypes.POINTER(ctypes.c_size_t), ctypes.POINTER(ctypes.c_size_t)]
+    L.sfsim_atmo_build_resumable.argtypes = [_cfgp, ctypes.POINTER(IterationState), ctypes.POINTER(IterationState), ITERATION_FN,
+                                          ctypes.c_void_p, _fp, _fp, _fp, _fp]
     L.sfsim_atmo_version.argtypes = []
     L.sfsim_atmo_version.restype = ctypes.c_char_p
     _lib = L

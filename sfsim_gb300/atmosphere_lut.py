@@ -61,6 +61,78 @@ def build(cfg: AtmoConfig | None = None, intermediates: bool = False):
     return out
 
 
+STATE_TABLES = ("ray_scatter_delta", "surface_delta", "ray_scatter_sum", "surface_sum")
+
+
+def empty_iteration_state(cfg: AtmoConfig) -> dict:
+    """Host buffers of one iteration state (sfsim_atmo_iteration_state): node
+    records of four values in the build's precision, 4-D tables
+    [h][el][sun el][heading][4], 2-D tables [h][sun el][4]."""
+    from .config import FP64
+    dt = np.float64 if cfg.precision == FP64 else np.float32
+    _, e, s = cfg.shapes()
+    return {"ray_scatter_delta": np.zeros(s + (4,), dt), "surface_delta": np.zeros(e + (4,), dt),
+            "ray_scatter_sum": np.zeros(s + (4,), dt), "surface_sum": np.zeros(e + (4,), dt)}
+
+
+def _state_struct(iteration: int, tables: dict) -> "_lib.IterationState":
+    return _lib.IterationState(iteration, *[tables[k].ctypes.data for k in STATE_TABLES])
+
+
+def build_resumable(cfg: AtmoConfig, resume: tuple | None = None, on_iteration=None):
+    """Builds the four tables with a state after every iteration
+    (sfsim_atmo_build_resumable).  `resume`: (iteration, tables) saved from
+    an earlier build of the same config; the build continues after that
+    iteration.  `on_iteration(iteration, tables)` sees each iteration's state
+    (arrays the next iteration overwrites: copy what you keep) and stops the
+    build by returning True (AtmoError with code SFSIM_ATMO_ESTOPPED); an
+    exception it raises stops the build and is raised again here."""
+    L = _lib.load()
+    _lib.check(L.sfsim_atmo_validate(ctypes.byref(cfg)), "sfsim_atmo_validate")
+    sT, sE, sS, sM = table_shapes(cfg)
+    out = {"transmittance": np.empty(sT, np.float32), "surface_radiance": np.empty(sE, np.float32),
+           "ray_scatter": np.empty(sS, np.float32), "mie_strength": np.empty(sM, np.float32)}
+    rs = None
+    if resume is not None:
+        iteration, tables = resume
+        want = empty_iteration_state(cfg)
+        tables = {k: np.ascontiguousarray(tables[k], dtype=want[k].dtype) for k in STATE_TABLES}
+        for k in STATE_TABLES:
+            if tables[k].shape != want[k].shape:
+                raise ValueError(f"resume table {k} has shape {tables[k].shape}, the config needs {want[k].shape}")
+        rs = _state_struct(int(iteration), tables)
+    state_tables = empty_iteration_state(cfg) if on_iteration is not None else None
+    st = _state_struct(0, state_tables) if state_tables is not None else None
+    raised = []
+
+    def hook(p, _user):
+        try:
+            return 1 if on_iteration(p.contents.iteration, state_tables) else 0
+        except BaseException as e:  # it cannot cross the C ABI: stop the build, raise it below
+            raised.append(e)
+            return 1
+    fn = _lib.ITERATION_FN(hook) if on_iteration is not None else _lib.ITERATION_FN()
+    rc = L.sfsim_atmo_build_resumable(ctypes.byref(cfg), ctypes.byref(rs) if rs is not None else None,
+                                      ctypes.byref(st) if st is not None else None, fn, None,
+                                      *[_fptr(out[k]) for k in ("transmittance", "surface_radiance",
+                                                                "ray_scatter", "mie_strength")])
+    if raised:
+        raise raised[0]
+    _lib.check(rc, "sfsim_atmo_build_resumable")
+    return out
+
+
+def save_iteration_state(path: str, iteration: int, tables: dict) -> None:
+    """Writes an iteration state to an .npz file."""
+    np.savez(path, iteration=np.int64(iteration), **{k: tables[k] for k in STATE_TABLES})
+
+
+def load_iteration_state(path: str) -> tuple:
+    """Reads an iteration state written by save_iteration_state: (iteration, tables)."""
+    with np.load(path) as z:
+        return int(z["iteration"]), {k: z[k].copy() for k in STATE_TABLES}
+
+
 def build_batch(cfgs):
     """Builds len(cfgs) atmospheres sharing shapes and steps in one batched pass."""
     L = _lib.load()

@@ -60,7 +60,7 @@ def build_library(force: bool = False, verbose: bool = False) -> str:
     with concurrent.futures.ThreadPoolExecutor(max_workers=min(len(srcs), os.cpu_count() or 4)) as ex:
         objs = list(ex.map(_compile, srcs))
     tmp = LIB + ".tmp"
-    cmd = [nvcc(), "-shared", *ARCH, "-o", tmp, *objs, "-lcudart"]
+    cmd = [nvcc(), "-shared", *ARCH, "-o", tmp, *objs, "-lcudart", "-ldl"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")

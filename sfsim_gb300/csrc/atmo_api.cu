@@ -2,6 +2,7 @@
 // validation, parameter set-up, the device workspace and the order loop of
 // generate-atmosphere-luts (src/clj/sfsim/atmosphere_lut.clj:43-105).
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include <atomic>
 #include <cmath>
@@ -35,6 +36,10 @@ bool g_timing = false;
 int g_launches = 0;
 constexpr int kStages = 10;
 double g_stage_ms[kStages];
+// stage names of the timings and of the NVTX ranges
+const char* const kStageNames[kStages] = {"set-up",    "transmittance",    "surface base", "first order",
+                                          "reserved",  "point scatter",    "surface radiance",
+                                          "ray scatter", "accumulate", "output"};
 int g_have_timings = 0;
 // bytes the last build copied host -> device and device -> host
 unsigned long long g_h2d_bytes = 0, g_d2h_bytes = 0;
@@ -463,20 +468,49 @@ int ensure_stream(int dev) {
 }
 
 // Stage timing with events on the build stream.
+// Stage boundaries of a build: CUDA events on the build stream when timing
+// is enabled, and always an NVTX range per stage ("sfsim first order",
+// "sfsim iteration 3 ray scatter", ...), so that a profiler can select one
+// stage of one iteration (ncu --nvtx --nvtx-include "sfsim iteration 3 ray scatter/").
 struct Timer {
   int dev;
   cudaStream_t st;
   int n = 0;
   int stage_of[512];
+  int iteration = 0;  // iteration of the stages that follow (1-based); 0 outside the loop
+  int open = 0;   // NVTX ranges pushed and not yet popped
   void mark_begin(int stage) {
+    char name[64];
+    if (iteration > 0)
+      snprintf(name, sizeof name, "sfsim iteration %d %s", iteration, kStageNames[stage]);
+    else
+      snprintf(name, sizeof name, "sfsim %s", kStageNames[stage]);
+    nvtxRangePushA(name);
+    open++;
     if (!g_timing || n >= 511) return;
     stage_of[n / 2] = stage;
     cudaEventRecord(g_events[dev][n++], st);
   }
   void mark_end() {
+    if (open > 0) {
+      nvtxRangePop();
+      open--;
+    }
     if (!g_timing || n % 2 == 0) return;
     cudaEventRecord(g_events[dev][n++], st);
   }
+  ~Timer() {
+    for (; open > 0; open--) nvtxRangePop();  // a stage left by an error return
+  }
+};
+
+// Per-iteration state of sfsim_atmo_build_resumable: where to resume, where
+// to copy each iteration's state, and whom to tell.
+struct IterationHooks {
+  const sfsim_atmo_iteration_state* resume;
+  sfsim_atmo_iteration_state* state;
+  sfsim_atmo_iteration_fn on_iteration;
+  void* user;
 };
 
 // The order loop of atmosphere_lut.clj:86-97 with every table resident in
@@ -484,7 +518,7 @@ struct Timer {
 template <class Real>
 int run_build(const Work<Real>& w, const BuildDims& d, float* oT, float* oE, float* oS, float* oM, cudaStream_t st,
               Timer& tm, const sfsim_atmo_intermediates* inter, Vec4<float>* jsum = nullptr,
-              cudaEvent_t early_done = nullptr) {
+              cudaEvent_t early_done = nullptr, const IterationHooks* hooks = nullptr) {
   int launches = 0;
   tm.mark_begin(0);
   launch_setup<Real>(w.params, d, w.dirs, w.hdirs, w.setup, st);
@@ -527,7 +561,30 @@ int run_build(const Work<Real>& w, const BuildDims& d, float* oT, float* oE, flo
   const Vec4<Real>* dE_prev = w.E0;
   const Vec4<Real>* S_prev = w.S1R;
   const Vec4<Real>* E_prev = nullptr;  // E = constantly 0
-  for (int it = 0; it < d.iterations; it++) {
+  const size_t state4 = sizeof(Vec4<Real>) * d.B * d.n4(), state2 = sizeof(Vec4<Real>) * d.B * d.nE();
+  int it0 = 0;
+  if (hooks && hooks->resume) {
+    // the state after iteration k into the buffers iteration k wrote
+    const sfsim_atmo_iteration_state& r = *hooks->resume;
+    const int k = r.iteration;
+    Vec4<Real>* rdS = w.dS[(k - 1) & 1];
+    Vec4<Real>* rdE = w.dE[(k - 1) & 1];
+    Vec4<Real>* rS = w.Sacc[(k - 1) & 1];
+    Vec4<Real>* rE = w.Eacc[(k - 1) & 1];
+    CUDA_TRY(cudaMemcpyAsync(rdS, r.ray_scatter_delta, state4, cudaMemcpyHostToDevice, st));
+    CUDA_TRY(cudaMemcpyAsync(rdE, r.surface_delta, state2, cudaMemcpyHostToDevice, st));
+    CUDA_TRY(cudaMemcpyAsync(rS, r.ray_scatter_sum, state4, cudaMemcpyHostToDevice, st));
+    CUDA_TRY(cudaMemcpyAsync(rE, r.surface_sum, state2, cudaMemcpyHostToDevice, st));
+    g_h2d_bytes += 2 * (state4 + state2);
+    dS_prev = rdS;
+    dE_prev = rdE;
+    S_prev = rS;
+    E_prev = rE;
+    M_first = nullptr;
+    it0 = k;
+  }
+  for (int it = it0; it < d.iterations; it++) {
+    tm.iteration = it + 1;
     Vec4<Real>* dE_new = w.dE[it & 1];
     Vec4<Real>* dS_new = w.dS[it & 1];
     Vec4<Real>* E_new = w.Eacc[it & 1];
@@ -572,7 +629,20 @@ int run_build(const Work<Real>& w, const BuildDims& d, float* oT, float* oE, flo
     dE_prev = dE_new;
     S_prev = S_new;
     E_prev = E_new;
+    if (hooks && hooks->state) {
+      sfsim_atmo_iteration_state& o = *hooks->state;
+      CUDA_TRY(cudaMemcpyAsync(o.ray_scatter_delta, dS_new, state4, cudaMemcpyDeviceToHost, st));
+      CUDA_TRY(cudaMemcpyAsync(o.surface_delta, dE_new, state2, cudaMemcpyDeviceToHost, st));
+      CUDA_TRY(cudaMemcpyAsync(o.ray_scatter_sum, S_new, state4, cudaMemcpyDeviceToHost, st));
+      CUDA_TRY(cudaMemcpyAsync(o.surface_sum, E_new, state2, cudaMemcpyDeviceToHost, st));
+      CUDA_TRY(cudaStreamSynchronize(st));
+      g_d2h_bytes += 2 * (state4 + state2);
+      o.iteration = it + 1;
+      if (hooks->on_iteration && hooks->on_iteration(&o, hooks->user))
+        return fail(SFSIM_ATMO_ESTOPPED, "the iteration callback stopped the build after iteration " + std::to_string(it + 1));
+    }
   }
+  tm.iteration = 0;
   tm.mark_begin(9);
   launch_output2<Real>(d.B, d.nE0, d.nE1, w.setup.remapE, E_prev, oE, st);
   launch_output4<Real>(d, w.setup.remapS, S_prev, oS, st);
@@ -601,7 +671,7 @@ void collect_timings(Timer& tm) {
 // memory on `user_stream`.
 template <class Real>
 int build_impl(const sfsim_atmo_config* cfgs, int B, float* T, float* E, float* S, float* M, bool host_out,
-               cudaStream_t user_stream, const sfsim_atmo_intermediates* inter) {
+               cudaStream_t user_stream, const sfsim_atmo_intermediates* inter, const IterationHooks* hooks = nullptr) {
   int dev = 0;
   int rc = current_device(&dev);
   if (rc) return rc;
@@ -663,7 +733,7 @@ int build_impl(const sfsim_atmo_config* cfgs, int B, float* T, float* E, float* 
   tm.st = st;
   float *dT = host_out ? w.oT : T, *dE = host_out ? w.oE : E, *dS = host_out ? w.oS : S, *dM = host_out ? w.oM : M;
   rc = run_build<Real>(w, d, dT, dE, dS, dM, st, tm, inter ? &dinter : nullptr, nullptr,
-                       host_out ? g_early_done[dev] : nullptr);
+                       host_out ? g_early_done[dev] : nullptr, hooks);
   if (rc) {
     if (staging) cudaFree(staging);
     return rc;
@@ -910,6 +980,39 @@ int sfsim_atmo_build_debug(const sfsim_atmo_config* cfg, float* T, float* E, flo
   return dispatch(cfg, 1, T, E, S, M, true, nullptr, inter);
 }
 
+int sfsim_atmo_iteration_state_bytes(const sfsim_atmo_config* cfg, size_t* s_bytes, size_t* e_bytes) {
+  if (!cfg) return fail(SFSIM_ATMO_ENULL, "config is NULL");
+  int rc = validate(cfg);
+  if (rc) return rc;
+  const size_t rec = 4 * (cfg->precision == SFSIM_ATMO_FP64 ? sizeof(double) : sizeof(float));
+  const int* s = cfg->ray_scatter_shape;
+  if (s_bytes) *s_bytes = rec * (size_t)s[0] * s[1] * s[2] * s[3];
+  if (e_bytes) *e_bytes = rec * (size_t)cfg->surface_radiance_shape[0] * cfg->surface_radiance_shape[1];
+  return 0;
+}
+
+int sfsim_atmo_build_resumable(const sfsim_atmo_config* cfg, const sfsim_atmo_iteration_state* resume,
+                            sfsim_atmo_iteration_state* state, sfsim_atmo_iteration_fn on_iteration, void* user, float* T,
+                            float* E, float* S, float* M) {
+  if (!cfg) return fail(SFSIM_ATMO_ENULL, "config is NULL");
+  if (!T || !E || !S || !M) return fail(SFSIM_ATMO_ENULL, "an output pointer is NULL");
+  int rc = validate(cfg);
+  if (rc) return rc;
+  auto complete = [](const sfsim_atmo_iteration_state* o) {
+    return o->ray_scatter_delta && o->surface_delta && o->ray_scatter_sum && o->surface_sum;
+  };
+  if (resume) {
+    if (!complete(resume)) return fail(SFSIM_ATMO_ENULL, "a table of the resume state is NULL");
+    if (resume->iteration < 1 || resume->iteration > cfg->iterations)
+      return fail(SFSIM_ATMO_EINVAL, "the resume iteration must be in [1, iterations]");
+  }
+  if (state && !complete(state)) return fail(SFSIM_ATMO_ENULL, "a table of the state buffers is NULL");
+  const IterationHooks hooks{resume, state, on_iteration, user};
+  std::lock_guard<std::mutex> lock(g_mutex);
+  if (cfg->precision == SFSIM_ATMO_FP64) return build_impl<double>(cfg, 1, T, E, S, M, true, nullptr, nullptr, &hooks);
+  return build_impl<float>(cfg, 1, T, E, S, M, true, nullptr, nullptr, &hooks);
+}
+
 int sfsim_atmo_set_timing(int enabled) {
   g_timing = enabled != 0;
   return 0;
@@ -956,6 +1059,7 @@ const char* sfsim_atmo_strerror(int code) {
     case SFSIM_ATMO_ENULL: return "NULL pointer argument";
     case SFSIM_ATMO_ETOOBIG: return "size exceeds a fixed capacity";
     case SFSIM_ATMO_ENUMERIC: return "result contains NaN or Inf";
+    case SFSIM_ATMO_ESTOPPED: return "stopped by the iteration callback";
     default: return "unknown error";
   }
 }

@@ -107,8 +107,37 @@ def test_null_outputs(lib):
     assert lib.sfsim_atmo_build(ctypes.byref(c), None, None, None, None) == -6
 
 
+def test_iteration_state_bytes(lib):
+    c = C.production()
+    s, e = ctypes.c_size_t(), ctypes.c_size_t()
+    assert lib.sfsim_atmo_iteration_state_bytes(ctypes.byref(c), ctypes.byref(s), ctypes.byref(e)) == 0
+    assert s.value == 4 * 4 * 32 * 255 * 32 * 8 and e.value == 4 * 4 * 16 * 64
+    c.precision = C.FP64
+    assert lib.sfsim_atmo_iteration_state_bytes(ctypes.byref(c), ctypes.byref(s), ctypes.byref(e)) == 0
+    assert s.value == 8 * 4 * 32 * 255 * 32 * 8
+
+
+def test_build_resumable_rejects_bad_states(lib):
+    """Resume states are checked on the host before any device work: an
+    iteration outside [1, iterations] and a missing table are refused."""
+    c = C.small_fp64()
+    buf = (ctypes.c_double * 16)()
+    full = lambda it: _lib.IterationState(it, *[ctypes.addressof(buf)] * 4)
+    outs = [(ctypes.c_float * 4)() for _ in range(4)]
+    fp = [ctypes.cast(o, ctypes.POINTER(ctypes.c_float)) for o in outs]
+    none = _lib.ITERATION_FN()
+    for it in (0, -1, c.iterations + 1):
+        st = full(it)
+        assert lib.sfsim_atmo_build_resumable(ctypes.byref(c), ctypes.byref(st), None, none, None, *fp) == -1
+    st = full(1)
+    st.surface_sum = None
+    assert lib.sfsim_atmo_build_resumable(ctypes.byref(c), ctypes.byref(st), None, none, None, *fp) == -6
+    assert lib.sfsim_atmo_build_resumable(ctypes.byref(c), None, ctypes.byref(st), none, None, *fp) == -6
+    assert lib.sfsim_atmo_build_resumable(ctypes.byref(c), None, None, none, None, fp[0], None, fp[2], fp[3]) == -6
+
+
 def test_strerror(lib):
-    for code in range(0, -9, -1):
+    for code in range(0, -10, -1):
         assert lib.sfsim_atmo_strerror(code)
     assert lib.sfsim_atmo_version().startswith(b"sfsim-atmo-gb300")
 
