@@ -2413,14 +2413,20 @@ int sfsim_noise_blue(int m, int n, const int* seed, double sigma, int* dither) {
   unsigned char* mask = d.get<unsigned char>(total);
   unsigned char* work = d.get<unsigned char>(total);
   int* dith = d.get<int>(total);
-  if (!sd || !tb || !dens || !dens0 || !mask || !work || !dith) return fail(SFSIM_ATMO_ENOMEM, "blue noise allocation failed");
+  int* err = d.get<int>(1);
+  if (!sd || !tb || !dens || !dens0 || !mask || !work || !dith || !err)
+    return fail(SFSIM_ATMO_ENOMEM, "blue noise allocation failed");
   CUDA_TRY(cudaMemcpyAsync(sd, seed, sizeof(int) * n, cudaMemcpyHostToDevice, st));
   CUDA_TRY(cudaMemcpyAsync(tb, table.data(), sizeof(double) * table.size(), cudaMemcpyHostToDevice, st));
-  if (launch_blue_noise(m, n, sd, sigma, tb, dens, dens0, mask, work, dith, st))
+  CUDA_TRY(cudaMemsetAsync(err, 0, sizeof(int), st));
+  if (launch_blue_noise(m, n, sd, sigma, tb, dens, dens0, mask, work, dith, err, st))
     return fail(SFSIM_ATMO_ECUDA, "blue noise launch configuration failed");
   CUDA_TRY(cudaGetLastError());
+  int herr = 0;
   CUDA_TRY(cudaMemcpyAsync(dither, dith, sizeof(int) * total, cudaMemcpyDeviceToHost, st));
+  CUDA_TRY(cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, st));
   CUDA_TRY(cudaStreamSynchronize(st));
+  if (herr) return fail(SFSIM_ATMO_ECUDA, "blue noise: a wait between the cluster's CTAs timed out");
   return 0;
 }
 

@@ -169,6 +169,8 @@ struct BlueArgs {
   unsigned char* work;   // m*m: the complement of the half-filled pattern
   int* dither;           // m*m output ranks
   int use_smem;          // the single-CTA kernels keep density and mask in shared memory
+  int* error;            // set to 1 when a cluster wait gave up
+  int wait_limit;        // polls per cluster wait
 };
 
 // Order-preserving integer key of a double (no NaN; the densities are never
@@ -410,6 +412,275 @@ __global__ void __launch_bounds__(kBlueThreads, 1) k_blue_phase3(BlueArgs a) {
   }
 }
 
+// ------------------------------------------- blue noise on a CTA cluster
+//
+// The same steps with the pixels split over a cluster of kBlueCluster CTAs
+// (one per SM): each CTA keeps the density and mask of its m*m / kBlueCluster
+// pixels in shared memory and updates them; a step's arg-extremum is a block
+// reduction per CTA, after which every CTA sends its candidate to every
+// other (stores into their shared memory and a release-arrive on their
+// mbarrier) and takes the best of the kBlueCluster candidates.  All CTAs
+// reduce the same candidates in the same order, so they pick the same pixel
+// and take the same branches.  The candidates of step s sit in buffer s & 1:
+// no CTA can be a whole step ahead of another, as a step ends only after
+// every CTA's candidate for it has arrived.  Waits are bounded: a CTA that
+// gives up records the error, and the others then give up too, as its
+// candidates stop coming; all meet at the final cluster barrier.
+
+constexpr int kBlueCluster = 8;
+constexpr int kBlueCThreads = 512;
+
+struct BlueCluster {
+  int m, total, own, p0, rank;  // pixels [p0, p0 + own) are this CTA's
+  double* table;
+  double* density;
+  unsigned char* mask;
+  Best (*slot)[kBlueCluster];   // [2][kBlueCluster] candidates by step parity
+  uint64_t* bar;                // [2]
+  Best* red;                    // [2][33] reduction scratch by step parity
+  int* fail;                    // shared flag: a wait gave up
+  int step;
+  int wait_limit;
+};
+
+__device__ __forceinline__ uint32_t cl_smem(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ uint32_t cl_map(uint32_t addr, int rank) {
+  uint32_t r;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(addr), "r"(rank));
+  return r;
+}
+__device__ __forceinline__ void cl_sync() {
+  asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+
+// The best candidate of the whole cluster; every thread gets its index, or
+// -1 when a wait gave up (then every later step returns -1 at once).  The
+// reduction scratch alternates by step parity, so one barrier less a step.
+__device__ int cluster_best(BlueCluster& c, Best b) {
+  const int buf = c.step & 1;
+  Best* red = c.red + 33 * buf;
+  for (int o = 16; o > 0; o >>= 1) {
+    Best e;
+    e.k = __shfl_xor_sync(0xffffffffu, b.k, o);
+    e.i = __shfl_xor_sync(0xffffffffu, b.i, o);
+    b = better(b, e);
+  }
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = b;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    const int lane = threadIdx.x;
+    Best e = lane < (int)(blockDim.x >> 5) ? red[lane] : Best{0ull, -1};
+    for (int o = 16; o > 0; o >>= 1) {
+      Best f;
+      f.k = __shfl_xor_sync(0xffffffffu, e.k, o);
+      f.i = __shfl_xor_sync(0xffffffffu, e.i, o);
+      e = better(e, f);
+    }
+    // every lane holds the CTA's candidate; lane r sends it to CTA r (slot
+    // [buf][rank], then a release-arrive on its barrier [buf])
+    const bool failed = *c.fail != 0;
+    const uint32_t sb = cl_smem(&c.bar[buf]);
+    if (!failed && lane < kBlueCluster) {
+      asm volatile("st.shared::cluster.u64 [%0], %1;" ::"r"(cl_map(cl_smem(&c.slot[buf][c.rank].k), lane)),
+                   "l"(e.k)
+                   : "memory");
+      asm volatile("st.shared::cluster.u32 [%0], %1;" ::"r"(cl_map(cl_smem(&c.slot[buf][c.rank].i), lane)), "r"(e.i)
+                   : "memory");
+      asm volatile("mbarrier.arrive.release.cluster.shared::cluster.b64 _, [%0];" ::"r"(cl_map(sb, lane)) : "memory");
+    }
+    // all kBlueCluster candidates of this step, then their best
+    bool done = failed;
+    if (!failed) {
+      const uint32_t parity = (uint32_t)((c.step >> 1) & 1);
+      for (int i = 0; i < c.wait_limit && !done; i++) {
+        uint32_t ok;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\t"
+            "mbarrier.try_wait.parity.acquire.cluster.shared::cta.b64 p, [%1], %2;\n\t"
+            "selp.b32 %0, 1, 0, p;\n\t}"
+            : "=r"(ok)
+            : "r"(sb), "r"(parity)
+            : "memory");
+        done = ok != 0;
+      }
+    }
+    const bool ok = __all_sync(0xffffffffu, done) && !failed;
+    Best g = ok && lane < kBlueCluster ? c.slot[buf][lane] : Best{0ull, -1};
+    for (int o = kBlueCluster / 2; o > 0; o >>= 1) {
+      Best f;
+      f.k = __shfl_xor_sync(0xffffffffu, g.k, o);
+      f.i = __shfl_xor_sync(0xffffffffu, g.i, o);
+      g = better(g, f);
+    }
+    if (lane == 0) {
+      if (!ok) *c.fail = 1;
+      red[32] = ok ? g : Best{0ull, -1};
+    }
+  }
+  __syncthreads();
+  c.step++;
+  return red[32].i;
+}
+
+// Arg-extremum over the cluster's pixels whose mask equals `want`.
+__device__ int cluster_search(BlueCluster& c, unsigned char want, bool least) {
+  Best b{0ull, -1};
+  for (int q = threadIdx.x; q < c.own; q += blockDim.x)
+    if (c.mask[q] == want) {
+      const unsigned long long k = okey(c.density[q]);
+      b = better(b, Best{least ? ~k : k, c.p0 + q});
+    }
+  return cluster_best(c, b);
+}
+
+// One step as `step` above on this CTA's pixels: mask[pc] = mask_c (by its
+// owner) and the density change of every pixel by +/- the weight of its
+// offset from pc, then the cluster's arg-extremum of the next search.
+__device__ int cluster_step(BlueCluster& c, int pc, bool add, unsigned char mask_c, unsigned char want, bool least) {
+  const int m = c.m, h = (m >> 1) + 1, cy = pc / m, cx = pc - cy * m;
+  Best b{0ull, -1};
+  const int first = c.p0 + threadIdx.x;
+  int y = first / m, x = first - y * m;
+  const int sy = blockDim.x / m, sx = blockDim.x - sy * m;
+  for (int q = threadIdx.x; q < c.own; q += blockDim.x) {
+    const int p = c.p0 + q;
+    if (p == pc) c.mask[q] = mask_c;
+    const double f = weight(c.table, h, wrap_near(x - cx, m), wrap_near(y - cy, m));
+    const double d = add ? __dadd_rn(c.density[q], f) : __dsub_rn(c.density[q], f);
+    c.density[q] = d;
+    if (c.mask[q] == want) {
+      const unsigned long long k = okey(d);
+      b = better(b, Best{least ? ~k : k, p});
+    }
+    x += sx;
+    y += sy;
+    if (x >= m) {
+      x -= m;
+      y += 1;
+    }
+  }
+  return cluster_best(c, b);
+}
+
+// Shared memory of a cluster CTA: the Gauss table, the CTA's densities and
+// mask, the candidate slots, barriers and reduction scratch.
+__host__ __device__ inline size_t blue_cluster_smem(int m) {
+  const size_t h = (size_t)(m / 2 + 1), own = (size_t)m * m / kBlueCluster;
+  return ((sizeof(double) * (h * h + own) + own + 15) & ~size_t(15));
+}
+
+// Static part of a cluster CTA's shared memory.
+struct BlueClusterShared {
+  Best slot[2][kBlueCluster];
+  uint64_t bar[2];
+  Best red[2][33];
+  int fail;
+};
+
+__device__ BlueCluster blue_cluster_setup(const BlueArgs& a, unsigned char* smem, BlueClusterShared& sh,
+                                          const double* g_density, const unsigned char* g_mask) {
+  BlueCluster c;
+  c.m = a.m;
+  c.total = a.m * a.m;
+  c.own = c.total / kBlueCluster;
+  asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(c.rank));
+  c.p0 = c.rank * c.own;
+  const int h = (a.m >> 1) + 1;
+  c.table = reinterpret_cast<double*>(smem);
+  c.density = c.table + h * h;
+  c.mask = reinterpret_cast<unsigned char*>(c.density + c.own);
+  c.slot = sh.slot;
+  c.bar = sh.bar;
+  c.red = &sh.red[0][0];
+  c.fail = &sh.fail;
+  c.step = 0;
+  c.wait_limit = a.wait_limit;
+  for (int t = threadIdx.x; t < h * h; t += blockDim.x) c.table[t] = a.table[t];
+  for (int q = threadIdx.x; q < c.own; q += blockDim.x) {
+    c.density[q] = g_density[c.p0 + q];
+    c.mask[q] = g_mask[c.p0 + q];
+  }
+  if (threadIdx.x == 0) {
+    sh.fail = 0;
+    for (int b = 0; b < 2; b++)
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(cl_smem(&sh.bar[b])), "r"(kBlueCluster) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  // every CTA's barriers are initialised before any candidate is sent
+  cl_sync();
+  return c;
+}
+
+// The CTA's pixels of the mask back to `g_mask` (inverted when `invert`),
+// then the final cluster barrier: no CTA leaves while another may still
+// write into its shared memory; a wait that gave up is reported.
+__device__ void blue_cluster_finish(const BlueArgs& a, BlueCluster& c, unsigned char* g_mask, bool invert) {
+  __syncthreads();
+  if (g_mask)
+    for (int q = threadIdx.x; q < c.own; q += blockDim.x) g_mask[c.p0 + q] = invert ? !c.mask[q] : c.mask[q];
+  if (threadIdx.x == 0 && *c.fail && a.error) atomicExch(a.error, 1);
+  cl_sync();
+}
+
+__global__ void __cluster_dims__(kBlueCluster, 1, 1) __launch_bounds__(kBlueCThreads, 1)
+    k_blue_seed_cl(BlueArgs a) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  __shared__ BlueClusterShared sh;
+  BlueCluster c = blue_cluster_setup(a, smem, sh, a.density, a.mask);
+  const int total = c.total;
+  int cluster = cluster_search(c, 1, false);
+  for (int it = 0; it < total * 4 && cluster >= 0; it++) {  // the pattern settles long before this bound
+    const int vd = cluster_step(c, cluster, false, 0, 0, true);
+    if (vd < 0) break;
+    if (vd == cluster) {
+      if (vd >= c.p0 && vd < c.p0 + c.own && threadIdx.x == 0) c.mask[vd - c.p0] = 1;
+      break;
+    }
+    cluster = cluster_step(c, vd, true, 1, 1, false);
+  }
+  blue_cluster_finish(a, c, a.mask, false);
+}
+
+__global__ void __cluster_dims__(kBlueCluster, 1, 1) __launch_bounds__(kBlueCThreads, 1)
+    k_blue_phases_cl(BlueArgs a) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  __shared__ BlueClusterShared sh;
+  BlueCluster c = blue_cluster_setup(a, smem, sh, a.density0, a.mask);
+  const int total = c.total;
+  int pc = cluster_search(c, 1, false);
+  for (int r = a.n; r > 0 && pc >= 0; r--) {
+    if (c.rank == 0 && threadIdx.x == 0) a.dither[pc] = r - 1;
+    pc = cluster_step(c, pc, false, 0, 1, false);
+  }
+  // back to the seed pattern and its density for phase 2
+  __syncthreads();
+  for (int q = threadIdx.x; q < c.own; q += blockDim.x) {
+    c.density[q] = a.density0[c.p0 + q];
+    c.mask[q] = a.mask[c.p0 + q];
+  }
+  __syncthreads();
+  pc = cluster_search(c, 0, true);
+  for (int r = a.n; r < total / 2 && pc >= 0; r++) {
+    if (c.rank == 0 && threadIdx.x == 0) a.dither[pc] = r;
+    pc = cluster_step(c, pc, true, 1, 0, true);
+  }
+  blue_cluster_finish(a, c, a.work, true);
+}
+
+__global__ void __cluster_dims__(kBlueCluster, 1, 1) __launch_bounds__(kBlueCThreads, 1)
+    k_blue_phase3_cl(BlueArgs a) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  __shared__ BlueClusterShared sh;
+  BlueCluster c = blue_cluster_setup(a, smem, sh, a.density, a.work);
+  const int total = c.total;
+  int pc = cluster_search(c, 1, false);
+  for (int r = total / 2; r < total && pc >= 0; r++) {
+    if (c.rank == 0 && threadIdx.x == 0) a.dither[pc] = r;
+    pc = cluster_step(c, pc, false, 0, 1, false);
+  }
+  blue_cluster_finish(a, c, nullptr, false);
+}
+
 // scatter-mask (bluenoise.clj:39-43), first pass: clear the mask and the ranks
 __global__ void k_blue_clear(int total, unsigned char* mask, int* dither) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -452,8 +723,18 @@ size_t blue_noise_smem(int m, bool* use_smem) {
   return *use_smem ? all : table;
 }
 
+// The cluster kernels serve tables whose pixels split evenly over the
+// cluster, from 2048 pixels (below that one CTA's reductions are as fast)
+// while a CTA's share, the Gauss table and the static part fit in 227 KB.
+bool blue_noise_on_cluster(int m) {
+  const int total = m * m;
+  return total % kBlueCluster == 0 && total >= 2048 &&
+         blue_cluster_smem(m) + sizeof(BlueClusterShared) <= 227 * 1024;
+}
+
 int launch_blue_noise(int m, int n, const int* seed, double sigma, const double* table, double* density,
-                      double* density0, unsigned char* mask, unsigned char* work, int* dither, cudaStream_t st) {
+                      double* density0, unsigned char* mask, unsigned char* work, int* dither, int* error,
+                      cudaStream_t st) {
   BlueArgs a;
   a.m = m;
   a.seed = seed;
@@ -465,6 +746,8 @@ int launch_blue_noise(int m, int n, const int* seed, double sigma, const double*
   a.mask = mask;
   a.work = work;
   a.dither = dither;
+  a.error = error;
+  a.wait_limit = wait_limit();
   bool use = false;
   const size_t smem = blue_noise_smem(m, &use);
   a.use_smem = use ? 1 : 0;
@@ -476,17 +759,35 @@ int launch_blue_noise(int m, int n, const int* seed, double sigma, const double*
       cudaFuncSetAttribute(k_blue_phase3, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess ||
       cudaFuncSetAttribute(k_blue_density, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dsmem) != cudaSuccess)
     return -1;
+  const bool cl = blue_noise_on_cluster(m);
+  const size_t csmem = blue_cluster_smem(m);
+  if (cl && (cudaFuncSetAttribute(k_blue_seed_cl, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)csmem) !=
+                 cudaSuccess ||
+             cudaFuncSetAttribute(k_blue_phases_cl, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)csmem) !=
+                 cudaSuccess ||
+             cudaFuncSetAttribute(k_blue_phase3_cl, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)csmem) !=
+                 cudaSuccess))
+    return -1;
   const unsigned dblocks = (unsigned)((total + 255) / 256);
   // the seed mask, its density, the seed pattern, its density, phases 1-2,
   // the complement's density, phase 3
   k_blue_clear<<<(unsigned)((total + 255) / 256), 256, 0, st>>>(total, mask, dither);
   k_blue_seed_set<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(n, seed, mask);
   k_blue_density<<<dblocks, 256, dsmem, st>>>(m, table, mask, density);
-  k_blue_seed<<<1, kBlueThreads, smem, st>>>(a);
+  if (cl)
+    k_blue_seed_cl<<<kBlueCluster, kBlueCThreads, csmem, st>>>(a);
+  else
+    k_blue_seed<<<1, kBlueThreads, smem, st>>>(a);
   k_blue_density<<<dblocks, 256, dsmem, st>>>(m, table, mask, density0);
-  k_blue_phases<<<1, kBlueThreads, smem, st>>>(a);
+  if (cl)
+    k_blue_phases_cl<<<kBlueCluster, kBlueCThreads, csmem, st>>>(a);
+  else
+    k_blue_phases<<<1, kBlueThreads, smem, st>>>(a);
   k_blue_density<<<dblocks, 256, dsmem, st>>>(m, table, work, density);
-  k_blue_phase3<<<1, kBlueThreads, smem, st>>>(a);
+  if (cl)
+    k_blue_phase3_cl<<<kBlueCluster, kBlueCThreads, csmem, st>>>(a);
+  else
+    k_blue_phase3<<<1, kBlueThreads, smem, st>>>(a);
   return 0;
 }
 
