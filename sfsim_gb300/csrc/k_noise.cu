@@ -414,28 +414,29 @@ __global__ void __launch_bounds__(kBlueThreads, 1) k_blue_phase3(BlueArgs a) {
 
 // ------------------------------------------- blue noise on a CTA cluster
 //
-// The same steps with the pixels split over a cluster of kBlueCluster CTAs
-// (one per SM): each CTA keeps the density and mask of its m*m / kBlueCluster
-// pixels in shared memory and updates them; a step's arg-extremum is a block
-// reduction per CTA, after which every CTA sends its candidate to every
-// other (stores into their shared memory and a release-arrive on their
-// mbarrier) and takes the best of the kBlueCluster candidates.  All CTAs
-// reduce the same candidates in the same order, so they pick the same pixel
-// and take the same branches.  The candidates of step s sit in buffer s & 1:
+// The same steps with the pixels split over a cluster of nc CTAs (8, or 16
+// where the GPU can place such clusters and the table is large; one CTA per
+// SM): each CTA keeps the density and mask of its m*m / nc pixels in shared
+// memory and updates them; a step's arg-extremum is a block reduction per
+// CTA, after which every CTA sends its candidate to every other (stores into
+// their shared memory and a release-arrive on their mbarrier), and every
+// warp of every CTA takes the best of the nc candidates.  All reduce the same
+// candidates, and the order is total, so they pick the same pixel and take
+// the same branches.  The candidates of step s sit in buffer s & 1:
 // no CTA can be a whole step ahead of another, as a step ends only after
 // every CTA's candidate for it has arrived.  Waits are bounded: a CTA that
 // gives up records the error, and the others then give up too, as its
 // candidates stop coming; all meet at the final cluster barrier.
 
-constexpr int kBlueCluster = 8;
+constexpr int kBlueClusterMax = 16;
 constexpr int kBlueCThreads = 512;
 
 struct BlueCluster {
-  int m, total, own, p0, rank;  // pixels [p0, p0 + own) are this CTA's
+  int m, total, own, p0, rank, nc;  // pixels [p0, p0 + own) are this CTA's, of nc CTAs
   double* table;
   double* density;
   unsigned char* mask;
-  Best (*slot)[kBlueCluster];   // [2][kBlueCluster] candidates by step parity
+  Best (*slot)[kBlueClusterMax];  // [2][nc] candidates by step parity
   uint64_t* bar;                // [2]
   Best* red;                    // [2][33] reduction scratch by step parity
   int* fail;                    // shared flag: a wait gave up
@@ -454,10 +455,13 @@ __device__ __forceinline__ void cl_sync() {
 }
 
 // The best candidate of the whole cluster; every thread gets its index, or
-// -1 when a wait gave up (then every later step returns -1 at once).  The
-// reduction scratch alternates by step parity, so one barrier less a step.
+// -1 when a wait gave up (then every later step returns -1 at once).  Warp 0
+// exchanges and reduces the candidates and the block barrier after it hands
+// every thread the same answer, so the CTA takes one branch even when a wait
+// gives up.  The reduction scratch alternates by step parity, so no second
+// barrier is needed before the next step writes it.
 __device__ int cluster_best(BlueCluster& c, Best b) {
-  const int buf = c.step & 1;
+  const int buf = c.step & 1, lane = threadIdx.x & 31;
   Best* red = c.red + 33 * buf;
   for (int o = 16; o > 0; o >>= 1) {
     Best e;
@@ -465,10 +469,9 @@ __device__ int cluster_best(BlueCluster& c, Best b) {
     e.i = __shfl_xor_sync(0xffffffffu, b.i, o);
     b = better(b, e);
   }
-  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = b;
+  if (lane == 0) red[threadIdx.x >> 5] = b;
   __syncthreads();
   if (threadIdx.x < 32) {
-    const int lane = threadIdx.x;
     Best e = lane < (int)(blockDim.x >> 5) ? red[lane] : Best{0ull, -1};
     for (int o = 16; o > 0; o >>= 1) {
       Best f;
@@ -480,7 +483,7 @@ __device__ int cluster_best(BlueCluster& c, Best b) {
     // [buf][rank], then a release-arrive on its barrier [buf])
     const bool failed = *c.fail != 0;
     const uint32_t sb = cl_smem(&c.bar[buf]);
-    if (!failed && lane < kBlueCluster) {
+    if (!failed && lane < c.nc) {
       asm volatile("st.shared::cluster.u64 [%0], %1;" ::"r"(cl_map(cl_smem(&c.slot[buf][c.rank].k), lane)),
                    "l"(e.k)
                    : "memory");
@@ -488,7 +491,7 @@ __device__ int cluster_best(BlueCluster& c, Best b) {
                    : "memory");
       asm volatile("mbarrier.arrive.release.cluster.shared::cluster.b64 _, [%0];" ::"r"(cl_map(sb, lane)) : "memory");
     }
-    // all kBlueCluster candidates of this step, then their best
+    // all nc candidates of this step, then their best
     bool done = failed;
     if (!failed) {
       const uint32_t parity = (uint32_t)((c.step >> 1) & 1);
@@ -505,8 +508,8 @@ __device__ int cluster_best(BlueCluster& c, Best b) {
       }
     }
     const bool ok = __all_sync(0xffffffffu, done) && !failed;
-    Best g = ok && lane < kBlueCluster ? c.slot[buf][lane] : Best{0ull, -1};
-    for (int o = kBlueCluster / 2; o > 0; o >>= 1) {
+    Best g = ok && lane < c.nc ? c.slot[buf][lane] : Best{0ull, -1};
+    for (int o = kBlueClusterMax / 2; o > 0; o >>= 1) {
       Best f;
       f.k = __shfl_xor_sync(0xffffffffu, g.k, o);
       f.i = __shfl_xor_sync(0xffffffffu, g.i, o);
@@ -564,14 +567,14 @@ __device__ int cluster_step(BlueCluster& c, int pc, bool add, unsigned char mask
 
 // Shared memory of a cluster CTA: the Gauss table, the CTA's densities and
 // mask, the candidate slots, barriers and reduction scratch.
-__host__ __device__ inline size_t blue_cluster_smem(int m) {
-  const size_t h = (size_t)(m / 2 + 1), own = (size_t)m * m / kBlueCluster;
+__host__ __device__ inline size_t blue_cluster_smem(int m, int nc) {
+  const size_t h = (size_t)(m / 2 + 1), own = (size_t)m * m / nc;
   return ((sizeof(double) * (h * h + own) + own + 15) & ~size_t(15));
 }
 
 // Static part of a cluster CTA's shared memory.
 struct BlueClusterShared {
-  Best slot[2][kBlueCluster];
+  Best slot[2][kBlueClusterMax];
   uint64_t bar[2];
   Best red[2][33];
   int fail;
@@ -582,8 +585,9 @@ __device__ BlueCluster blue_cluster_setup(const BlueArgs& a, unsigned char* smem
   BlueCluster c;
   c.m = a.m;
   c.total = a.m * a.m;
-  c.own = c.total / kBlueCluster;
   asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(c.rank));
+  asm volatile("mov.u32 %0, %%cluster_nctarank;" : "=r"(c.nc));
+  c.own = c.total / c.nc;
   c.p0 = c.rank * c.own;
   const int h = (a.m >> 1) + 1;
   c.table = reinterpret_cast<double*>(smem);
@@ -603,7 +607,7 @@ __device__ BlueCluster blue_cluster_setup(const BlueArgs& a, unsigned char* smem
   if (threadIdx.x == 0) {
     sh.fail = 0;
     for (int b = 0; b < 2; b++)
-      asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(cl_smem(&sh.bar[b])), "r"(kBlueCluster) : "memory");
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(cl_smem(&sh.bar[b])), "r"(c.nc) : "memory");
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   // every CTA's barriers are initialised before any candidate is sent
@@ -622,7 +626,7 @@ __device__ void blue_cluster_finish(const BlueArgs& a, BlueCluster& c, unsigned 
   cl_sync();
 }
 
-__global__ void __cluster_dims__(kBlueCluster, 1, 1) __launch_bounds__(kBlueCThreads, 1)
+__global__ void __launch_bounds__(kBlueCThreads, 1)
     k_blue_seed_cl(BlueArgs a) {
   extern __shared__ __align__(16) unsigned char smem[];
   __shared__ BlueClusterShared sh;
@@ -641,7 +645,7 @@ __global__ void __cluster_dims__(kBlueCluster, 1, 1) __launch_bounds__(kBlueCThr
   blue_cluster_finish(a, c, a.mask, false);
 }
 
-__global__ void __cluster_dims__(kBlueCluster, 1, 1) __launch_bounds__(kBlueCThreads, 1)
+__global__ void __launch_bounds__(kBlueCThreads, 1)
     k_blue_phases_cl(BlueArgs a) {
   extern __shared__ __align__(16) unsigned char smem[];
   __shared__ BlueClusterShared sh;
@@ -667,7 +671,7 @@ __global__ void __cluster_dims__(kBlueCluster, 1, 1) __launch_bounds__(kBlueCThr
   blue_cluster_finish(a, c, a.work, true);
 }
 
-__global__ void __cluster_dims__(kBlueCluster, 1, 1) __launch_bounds__(kBlueCThreads, 1)
+__global__ void __launch_bounds__(kBlueCThreads, 1)
     k_blue_phase3_cl(BlueArgs a) {
   extern __shared__ __align__(16) unsigned char smem[];
   __shared__ BlueClusterShared sh;
@@ -723,13 +727,43 @@ size_t blue_noise_smem(int m, bool* use_smem) {
   return *use_smem ? all : table;
 }
 
-// The cluster kernels serve tables whose pixels split evenly over the
-// cluster, from 2048 pixels (below that one CTA's reductions are as fast)
-// while a CTA's share, the Gauss table and the static part fit in 227 KB.
-bool blue_noise_on_cluster(int m) {
+// CTAs of the blue-noise cluster for an m x m table, 0 where the single-CTA
+// kernels serve it.  The cluster kernels take tables whose pixels split
+// evenly over the cluster, from 2048 pixels (below that one CTA's
+// reductions are as fast), while a CTA's share, the Gauss table and the
+// static part fit in 227 KB; 16 CTAs from 16384 pixels where the GPU can
+// place such clusters (a non-portable size), else 8.
+int blue_noise_cluster_size(int m) {
   const int total = m * m;
-  return total % kBlueCluster == 0 && total >= 2048 &&
-         blue_cluster_smem(m) + sizeof(BlueClusterShared) <= 227 * 1024;
+  auto fits = [&](int nc) {
+    return total % nc == 0 && blue_cluster_smem(m, nc) + sizeof(BlueClusterShared) <= 227 * 1024;
+  };
+  if (total < 2048) return 0;
+  if (total >= 16384 && fits(16)) {
+    const size_t smem = blue_cluster_smem(m, 16);
+    void (*kernels[3])(BlueArgs) = {k_blue_seed_cl, k_blue_phases_cl, k_blue_phase3_cl};
+    bool ok = true;
+    for (auto k : kernels) {
+      ok = ok && cudaFuncSetAttribute(k, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess &&
+           cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) == cudaSuccess;
+      cudaLaunchConfig_t cfg = {};
+      cudaLaunchAttribute attr;
+      attr.id = cudaLaunchAttributeClusterDimension;
+      attr.val.clusterDim.x = 16;
+      attr.val.clusterDim.y = 1;
+      attr.val.clusterDim.z = 1;
+      cfg.gridDim = dim3(16);
+      cfg.blockDim = dim3(kBlueCThreads);
+      cfg.dynamicSmemBytes = smem;
+      cfg.attrs = &attr;
+      cfg.numAttrs = 1;
+      int clusters = 0;
+      ok = ok && cudaOccupancyMaxActiveClusters(&clusters, k, &cfg) == cudaSuccess && clusters >= 1;
+    }
+    cudaGetLastError();  // a refused query leaves no error behind
+    if (ok) return 16;
+  }
+  return fits(8) ? 8 : 0;
 }
 
 int launch_blue_noise(int m, int n, const int* seed, double sigma, const double* table, double* density,
@@ -759,35 +793,54 @@ int launch_blue_noise(int m, int n, const int* seed, double sigma, const double*
       cudaFuncSetAttribute(k_blue_phase3, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess ||
       cudaFuncSetAttribute(k_blue_density, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dsmem) != cudaSuccess)
     return -1;
-  const bool cl = blue_noise_on_cluster(m);
-  const size_t csmem = blue_cluster_smem(m);
-  if (cl && (cudaFuncSetAttribute(k_blue_seed_cl, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)csmem) !=
+  const int nc = blue_noise_cluster_size(m);
+  const size_t csmem = nc ? blue_cluster_smem(m, nc) : 0;
+  if (nc && (cudaFuncSetAttribute(k_blue_seed_cl, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)csmem) !=
                  cudaSuccess ||
              cudaFuncSetAttribute(k_blue_phases_cl, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)csmem) !=
                  cudaSuccess ||
              cudaFuncSetAttribute(k_blue_phase3_cl, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)csmem) !=
                  cudaSuccess))
     return -1;
+  // one cluster of nc CTAs
+  auto on_cluster = [&](void (*k)(BlueArgs)) {
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute attr;
+    attr.id = cudaLaunchAttributeClusterDimension;
+    attr.val.clusterDim.x = nc;
+    attr.val.clusterDim.y = 1;
+    attr.val.clusterDim.z = 1;
+    cfg.gridDim = dim3(nc);
+    cfg.blockDim = dim3(kBlueCThreads);
+    cfg.dynamicSmemBytes = csmem;
+    cfg.stream = st;
+    cfg.attrs = &attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, k, a) == cudaSuccess;
+  };
   const unsigned dblocks = (unsigned)((total + 255) / 256);
   // the seed mask, its density, the seed pattern, its density, phases 1-2,
   // the complement's density, phase 3
   k_blue_clear<<<(unsigned)((total + 255) / 256), 256, 0, st>>>(total, mask, dither);
   k_blue_seed_set<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(n, seed, mask);
   k_blue_density<<<dblocks, 256, dsmem, st>>>(m, table, mask, density);
-  if (cl)
-    k_blue_seed_cl<<<kBlueCluster, kBlueCThreads, csmem, st>>>(a);
-  else
+  if (nc) {
+    if (!on_cluster(k_blue_seed_cl)) return -1;
+  } else {
     k_blue_seed<<<1, kBlueThreads, smem, st>>>(a);
+  }
   k_blue_density<<<dblocks, 256, dsmem, st>>>(m, table, mask, density0);
-  if (cl)
-    k_blue_phases_cl<<<kBlueCluster, kBlueCThreads, csmem, st>>>(a);
-  else
+  if (nc) {
+    if (!on_cluster(k_blue_phases_cl)) return -1;
+  } else {
     k_blue_phases<<<1, kBlueThreads, smem, st>>>(a);
+  }
   k_blue_density<<<dblocks, 256, dsmem, st>>>(m, table, work, density);
-  if (cl)
-    k_blue_phase3_cl<<<kBlueCluster, kBlueCThreads, csmem, st>>>(a);
-  else
+  if (nc) {
+    if (!on_cluster(k_blue_phase3_cl)) return -1;
+  } else {
     k_blue_phase3<<<1, kBlueThreads, smem, st>>>(a);
+  }
   return 0;
 }
 

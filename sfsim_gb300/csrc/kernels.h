@@ -318,11 +318,11 @@ void launch_worley(int divisions, int size, const double* grid, float4* local, f
 void launch_perlin(int divisions, int size, const int* gradients, float* out, unsigned int* range, cudaStream_t st);
 // density, mask and work are used only when the state does not fit in
 // shared memory (blue_noise_smem sets use_smem false).  Tables of at least
-// 2048 pixels that split evenly over 8 CTAs run on a CTA cluster
-// (blue_noise_on_cluster); `error` (device int, zeroed by the caller) is set
-// when one of its bounded waits gave up.
+// 2048 pixels that split evenly over 8 (or 16) CTAs run on a CTA cluster
+// (blue_noise_cluster_size); `error` (device int, zeroed by the caller) is
+// set when one of its bounded waits gave up.
 size_t blue_noise_smem(int m, bool* use_smem);
-bool blue_noise_on_cluster(int m);
+int blue_noise_cluster_size(int m);
 int launch_blue_noise(int m, int n, const int* seed, double sigma, const double* table, double* density,
                       double* density0, unsigned char* mask, unsigned char* work, int* dither, int* error,
                       cudaStream_t st);
