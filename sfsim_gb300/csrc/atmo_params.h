@@ -143,6 +143,8 @@ struct PointRow {
   int u0, u2;
   Real s0, s2;
   Real bR[3], bM[3];
+  Real gA;    // r ss / R: with x = (r, 0, 0), a ground point g = x + t omega (|g| = R) has
+              // g.l / |g| = gA + (t / R) (omega . l), since l has first component ss
 };
 
 // Per node (height iE, sun elevation kE) of the surface-radiance space, from
@@ -182,7 +184,8 @@ template <class Real>
 struct SphereDir {
   Real w[3];           // direction omega in world coordinates
   Real weight;         // quadrature weight (ring factor * 2 pi / ring steps)
-  Real gdir[3];        // unit vector of the ground point (surface directions)
+  Real tR;             // ground distance / R (surface directions): the ground point's sin of the
+                       // sun elevation is gA + tR (omega . l), gA of the (height, sun elevation) row
   Real ground[3];      // T(x, g) * brightness / pi (surface directions)
   int surface;         // 1: the direction ends on the ground
   int u1;              // elevation coordinate of (x, omega, !surface)

@@ -131,8 +131,8 @@ __global__ void __launch_bounds__(256) k_heading_rows(BuildDims d, const SphereD
 
 // Shared-memory layout of point scatter for one (height i, sun elevation k)
 // pair, `used` directions (a multiple of kDirBlock):
-//   dirs  [kDirFields][used] Real: x0, x1, x2, weight, gdir0..2, ground0..2,
-//         sE0 of each direction (structure of arrays, so that two consecutive
+//   dirs  [kDirFields][used] Real: x0, x1, x2, weight, tR, ground0..2, sE0
+//         of each direction (structure of arrays, so that two consecutive
 //         directions' components load as one pair);
 //   uE0   [used] int;
 //   rows  [used][n3 + 2][3] dS gathered along the heading axis between
@@ -242,6 +242,8 @@ __global__ void __launch_bounds__(256, point_scatter_min_blocks(sizeof(Real))) k
     const int row_len = RS * rlen;
     const R2 lx2 = mk2(g.lx, g.lx), ly2 = mk2(g.ly, g.ly), lz2 = mk2(g.lz, g.lz);
     const R2 sv2 = mk2(sv, sv), cv2 = mk2(cv, cv), sc3 = mk2(scale3, scale3);
+    const Real gA = prk->gA;
+    const R2 gA2 = mk2(gA, gA);
 
     // compensated totals (x: Rayleigh, y: Mie) per channel, and the plain
     // partial sums of the current directions (x: even, y: odd direction)
@@ -301,8 +303,8 @@ __global__ void __launch_bounds__(256, point_scatter_min_blocks(sizeof(Real))) k
           }
         }
         if (decltype(ground)::value) {
-          const R2 G0 = ld2(dirs + 4 * used + wa), G1 = ld2(dirs + 5 * used + wa), G2 = ld2(dirs + 6 * used + wa);
-          const R2 sg = fma2(G0, lx2, fma2(G1, ly2, mul2(G2, lz2)));
+          // the ground point's sin of the sun elevation, g.l / |g| = gA + tR (omega . l)
+          const R2 sg = fma2(ld2(dirs + 4 * used + wa), mu_l, gA2);
           int ea, eb;
           Real ta, tb;
           split_coord_r<Real>(sun_elevation_index_r<Real>(sg.x, scaleE), d.nE1, &ea, &ta);
@@ -310,7 +312,7 @@ __global__ void __launch_bounds__(256, point_scatter_min_blocks(sizeof(Real))) k
           const int fa = upper_index(ea, d.nE1), fb = upper_index(eb, d.nE1);
           const int ha = uE0s[wa], hb = uE0s[wa + 1];
           const int ka = upper_index(ha, d.nE0), kb = upper_index(hb, d.nE0);
-          const R2 sE1 = mk2(ta, tb), sE0 = ld2(dirs + 10 * used + wa);
+          const R2 sE1 = mk2(ta, tb), sE0 = ld2(dirs + 8 * used + wa);
           const R2 one = mk2(Real(1), Real(1));
           const R2 oi = sub2(one, sE1);
           const Real* e0a = etab + 3 * ha * d.nE1;
@@ -321,7 +323,7 @@ __global__ void __launch_bounds__(256, point_scatter_min_blocks(sizeof(Real))) k
   #pragma unroll
             for (int c = 0; c < 3; c++) {
               const R2 Y = fma2(mk2(e0a[3 * fa + c], e0b[3 * fb + c]), sE1, mul2(mk2(e0a[3 * ea + c], e0b[3 * eb + c]), oi));
-              X[c] = fma2(ld2(dirs + (7 + c) * used + wa), Y, X[c]);
+              X[c] = fma2(ld2(dirs + (5 + c) * used + wa), Y, X[c]);
             }
           } else {
             const R2 oo = sub2(one, sE0);
@@ -335,7 +337,7 @@ __global__ void __launch_bounds__(256, point_scatter_min_blocks(sizeof(Real))) k
               const R2 hi =
                   fma2(mk2(e1a[3 * fa + c], e1b[3 * fb + c]), sE1, mul2(mk2(e1a[3 * ea + c], e1b[3 * eb + c]), oi));
               const R2 Y = fma2(hi, sE0, mul2(lo, oo));
-              X[c] = fma2(ld2(dirs + (7 + c) * used + wa), Y, X[c]);
+              X[c] = fma2(ld2(dirs + (5 + c) * used + wa), Y, X[c]);
             }
           }
         }

@@ -273,15 +273,11 @@ __global__ void k_sphere_setup(const AtmoParams* params, BuildDims d, const DirL
     segment_depth<Real>(P, x, sub3(g, x), d.S, tau);
     double gr = mag3(g);
     for (int c = 0; c < 3; c++) o.ground[c] = exp_neg(tau[c]) * (Real)(P.brightness[c] / M_PI);
-    o.gdir[0] = (Real)(g.x / gr);
-    o.gdir[1] = (Real)(g.y / gr);
-    o.gdir[2] = (Real)(g.z / gr);
+    o.tR = (Real)(mag3(sub3(g, x)) / P.R);
     split_coord<Real>(height_to_index(P, d.nE0, gr), d.nE0, &o.uE0, &o.sE0);
   } else {
-    for (int c = 0; c < 3; c++) {
-      o.ground[c] = 0;
-      o.gdir[c] = 0;
-    }
+    for (int c = 0; c < 3; c++) o.ground[c] = 0;
+    o.tR = 0;
     o.uE0 = 0;
     o.sE0 = 0;
   }
@@ -335,7 +331,8 @@ __global__ void k_sphere_partition(BuildDims d, const SphereDir<Real>* sdirs, Sp
     g += __popc(bg);
   }
   SphereDir<Real> z;
-  for (int c = 0; c < 3; c++) z.w[c] = z.gdir[c] = z.ground[c] = 0;
+  for (int c = 0; c < 3; c++) z.w[c] = z.ground[c] = 0;
+  z.tR = 0;
   z.weight = z.s1 = z.sE0 = 0;
   z.u1 = z.uE0 = 0;
   z.pad = 1;
@@ -354,8 +351,8 @@ __global__ void k_sphere_partition(BuildDims d, const SphereDir<Real>* sdirs, Sp
   int* img_u = reinterpret_cast<int*>(img + kDirFields * used);
   for (int t = lane; t < used; t += 32) {
     const SphereDir<Real> e = dst[t];
-    const Real f[kDirFields] = {e.w[0],      e.w[1],      e.w[2],      e.weight,    e.gdir[0], e.gdir[1],
-                                e.gdir[2],   e.ground[0], e.ground[1], e.ground[2], e.sE0};
+    const Real f[kDirFields] = {e.w[0],      e.w[1],      e.w[2],      e.weight, e.tR,
+                                e.ground[0], e.ground[1], e.ground[2], e.sE0};
 #pragma unroll
     for (int c = 0; c < kDirFields; c++) img[c * used + t] = f[c];
     img_u[t] = e.uE0;
@@ -377,6 +374,7 @@ __global__ void k_point_rows(const AtmoParams* params, BuildDims d, PointRow<Rea
   const double ss = index_to_sin_sun_elevation(d.n2, (double)k);
   PointRow<Real> o;
   o.ss = ss;
+  o.gA = (Real)(r * ss / P.R);
   split_coord<Real>(height_to_index(P, d.n0, r), d.n0, &o.u0, &o.s0);
   split_coord<Real>(sun_elevation_to_index(d.n2, mk3(r, 0, 0), mk3(ss, 0, 0)), d.n2, &o.u2, &o.s2);
   const double h = r - P.R;

@@ -36,8 +36,8 @@ constexpr int kDirBlock = 8;
 __host__ __device__ constexpr int dir_row(int P) { return P + 2 * kDirBlock; }
 
 // Fields per direction in point scatter's shared direction arrays: x0, x1,
-// x2, weight, gdir0..2, ground0..2, sE0 (then uE0 as ints).
-constexpr int kDirFields = 11;
+// x2, weight, tR, ground0..2, sE0 (then uE0 as ints).
+constexpr int kDirFields = 9;
 // Bytes of the direction image of `used` directions, a multiple of 16.
 __host__ __device__ inline size_t dir_image_bytes(int used, size_t real_size) {
   return ((size_t)used * (kDirFields * real_size + sizeof(int)) + 15) & ~size_t(15);
