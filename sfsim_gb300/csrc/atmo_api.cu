@@ -372,7 +372,7 @@ struct Work {
   Real* J;
   Real* hrows;  // point scatter's heading rows per (height, sun elevation)
   float *oT, *oE, *oS, *oM;  // device outputs when the caller passes host buffers
-  float4* sun;               // sun-ray optical-depth tables, paired texels (FP32 builds), or NULL
+  unsigned char* sun;        // sun-ray optical-depth tables, kSunTableBytes per atmosphere (FP32 builds), or NULL
 };
 
 // The sun-ray tables cost kSunTableLen nodes of S samples per atmosphere;
@@ -425,7 +425,7 @@ size_t carve(Work<Real>& w, char* base, const BuildDims& d, bool outputs, bool s
   } else {
     w.oT = w.oE = w.oS = w.oM = nullptr;
   }
-  w.sun = (sun_table && sizeof(Real) == sizeof(float) && sun_tables_pay(d)) ? c.take<float4>(B * kSunTableLen)
+  w.sun = (sun_table && sizeof(Real) == sizeof(float) && sun_tables_pay(d)) ? c.take<unsigned char>(B * kSunTableBytes)
                                                                              : nullptr;
   return c.off + 256;
 }

@@ -34,8 +34,8 @@
 //    the optical-depth error at <= 3e-6 (FP32 storage included) over Earth,
 //    the reference's 35 km atmosphere and the sweep's extremes (radius 3000
 //    and 7000 km, Mie scale heights 0.8 and 2 km).
-// Both tables hold paired texels (store_paired), one aligned 16-byte load
-// per row of a bilinear lookup.
+// A table of paired texels (kSunPairClimb, kSunPairDesc) is read with one
+// aligned 16-byte load per row of a bilinear lookup.
 #include "atmo_device.cuh"
 #include "kernels.h"
 
@@ -108,30 +108,56 @@ __device__ __forceinline__ void desc_table_node(const AtmoParams& P, int S, int 
   *out = make_float2(log2f(fmaxf(sr * inv_s, 1.17549435e-38f)), log2f(fmaxf(smie * inv_s, 1.17549435e-38f)));
 }
 
-// Node value v of table row entry t (column j of a row of `width`) into its
-// paired layout: entry t holds (v(j), v(j + 1)) as one 16-byte float4, so a
-// bilinear lookup reads each of its two rows with one aligned load from one
-// 32-byte sector; v goes to entry t's first half and entry t - 1's second
-// (the last entry of a row repeats v there, never read).
-__device__ __forceinline__ void store_paired(float4* tab, long long t, int j, int width, float2 v) {
-  float2* e = reinterpret_cast<float2*>(tab + t);
-  e[0] = v;
-  if (j > 0) e[-1] = v;
-  if (j == width - 1) e[1] = v;
+// Node value v at column j (of `width`) of entry `idx` of a table.  Paired:
+// entry idx holds (v(j), v(j + 1)) as one 16-byte float4, so a bilinear
+// lookup reads each of its two rows with one aligned load from one 32-byte
+// sector; v goes to entry idx's first half and entry idx - 1's second (the
+// last entry of a row repeats v there, never read).  Otherwise entry idx is v.
+template <bool PAIRED>
+__device__ __forceinline__ void store_node(unsigned char* tab, long long idx, int j, int width, float2 v) {
+  if (PAIRED) {
+    float2* e = reinterpret_cast<float2*>(reinterpret_cast<float4*>(tab) + idx);
+    e[0] = v;
+    if (j > 0) e[-1] = v;
+    if (j == width - 1) e[1] = v;
+  } else {
+    reinterpret_cast<float2*>(tab)[idx] = v;
+  }
 }
 
-__global__ void k_sun_table(const AtmoParams* params, int S, float4* table) {
+// The four texels of the bilinear footprint at entry idx of a table of rows
+// of `width`.
+template <bool PAIRED>
+__device__ __forceinline__ void load_footprint(const unsigned char* tab, long long idx, int width, float2& v00,
+                                               float2& v01, float2& v10, float2& v11) {
+  if (PAIRED) {
+    const float4* p = reinterpret_cast<const float4*>(tab) + idx;
+    const float4 e0 = __ldg(p), e1 = __ldg(p + width);
+    v00 = make_float2(e0.x, e0.y);
+    v01 = make_float2(e0.z, e0.w);
+    v10 = make_float2(e1.x, e1.y);
+    v11 = make_float2(e1.z, e1.w);
+  } else {
+    const float2* p = reinterpret_cast<const float2*>(tab) + idx;
+    v00 = __ldg(p);
+    v01 = __ldg(p + 1);
+    v10 = __ldg(p + width);
+    v11 = __ldg(p + width + 1);
+  }
+}
+
+__global__ void k_sun_table(const AtmoParams* params, int S, unsigned char* table) {
   const int b = blockIdx.y;
   const AtmoParams& P = params[b];
   const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (t >= kSunTableLen) return;
-  float4* tab = table + (long long)b * kSunTableLen;
+  unsigned char* tab = table + (size_t)b * kSunTableBytes;
   if (t >= (long long)kSunNR * kSunNM) {
     const int u = (int)(t - (long long)kSunNR * kSunNM);
     const int i = u / kDescNY, j = u - i * kDescNY;
     float2 v;
     desc_table_node(P, S, i, j, &v);
-    store_paired(tab, t, j, kDescNY, v);
+    store_node<kSunPairDesc>(tab + kSunClimbBytes, u, j, kDescNY, v);
     return;
   }
   const int i = (int)t / kSunNM, j = (int)t - ((int)t / kSunNM) * kSunNM;
@@ -155,16 +181,16 @@ __global__ void k_sun_table(const AtmoParams* params, int S, float4* table) {
                         smie);
     out = make_float2(dt * sr, dt * smie);
   }
-  store_paired(tab, t, j, kSunNM, out);
+  store_node<kSunPairClimb>(tab, t, j, kSunNM, out);
 }
 
-void launch_sun_table(const AtmoParams* params, const BuildDims& d, float4* table, cudaStream_t st) {
+void launch_sun_table(const AtmoParams* params, const BuildDims& d, unsigned char* table, cudaStream_t st) {
   dim3 grid((unsigned)((kSunTableLen + 255) / 256), d.B);
   k_sun_table<<<grid, 256, 0, st>>>(params, d.S, table);
 }
 
 // Bilinear lookup of the table at (q, exit distance) for a climbing ray.
-__device__ __forceinline__ float2 sun_lookup(const float4* __restrict__ tab, const AtmoParams& P, float q,
+__device__ __forceinline__ float2 sun_lookup(const unsigned char* __restrict__ tab, const AtmoParams& P, float q,
                                              float texit) {
   const float Hh2 = P.f_Hh2, R2 = P.f_R * P.f_R, top = P.f_top;
   const float qc = fminf(fmaxf(q, 0.0f), Hh2);
@@ -177,10 +203,8 @@ __device__ __forceinline__ float2 sun_lookup(const float4* __restrict__ tab, con
   const float fi = xr * (float)(kSunNR - 1), fj = xm * (float)(kSunNM - 1);
   const int i0 = min((int)fi, kSunNR - 2), j0 = min((int)fj, kSunNM - 2);
   const float a = fi - (float)i0, c = fj - (float)j0;
-  const float4* row0 = tab + (long long)i0 * kSunNM + j0;
-  const float4 e0 = __ldg(row0), e1 = __ldg(row0 + kSunNM);
-  const float2 v00 = make_float2(e0.x, e0.y), v01 = make_float2(e0.z, e0.w);
-  const float2 v10 = make_float2(e1.x, e1.y), v11 = make_float2(e1.z, e1.w);
+  float2 v00, v01, v10, v11;
+  load_footprint<kSunPairClimb>(tab, (long long)i0 * kSunNM + j0, kSunNM, v00, v01, v10, v11);
   const float w00 = (1.0f - a) * (1.0f - c), w01 = (1.0f - a) * c, w10 = a * (1.0f - c), w11 = a * c;
   return make_float2(w00 * v00.x + w01 * v01.x + w10 * v10.x + w11 * v11.x,
                      w00 * v00.y + w01 * v01.y + w10 * v10.y + w11 * v11.y);
@@ -188,8 +212,8 @@ __device__ __forceinline__ float2 sun_lookup(const float4* __restrict__ tab, con
 
 // Optical depths of a descending ray (bp = p.l < 0) from q = |p|^2 - R^2 and
 // its exit distance texit = d + dmax, from the descending table.
-__device__ __forceinline__ float2 sun_lookup_desc(const float4* __restrict__ tab, const AtmoParams& P, float q,
-                                                  float bp, float texit) {
+__device__ __forceinline__ float2 sun_lookup_desc(const unsigned char* __restrict__ tab, const AtmoParams& P,
+                                                  float q, float bp, float texit) {
   const float R = P.f_R;
   const float qs = fmaxf(fmaf(-bp, bp, q), 0.0f);
   const float hs = qs / (R + sqrtf(fmaf(R, R, qs)));
@@ -200,10 +224,8 @@ __device__ __forceinline__ float2 sun_lookup_desc(const float4* __restrict__ tab
   const float fi = x * (float)(kDescNX - 1), fj = y * (float)(kDescNY - 1);
   const int i0 = min((int)fi, kDescNX - 2), j0 = min((int)fj, kDescNY - 2);
   const float a = fi - (float)i0, c = fj - (float)j0;
-  const float4* row0 = tab + (long long)i0 * kDescNY + j0;
-  const float4 e0 = __ldg(row0), e1 = __ldg(row0 + kDescNY);
-  const float2 v00 = make_float2(e0.x, e0.y), v01 = make_float2(e0.z, e0.w);
-  const float2 v10 = make_float2(e1.x, e1.y), v11 = make_float2(e1.z, e1.w);
+  float2 v00, v01, v10, v11;
+  load_footprint<kSunPairDesc>(tab, (long long)i0 * kDescNY + j0, kDescNY, v00, v01, v10, v11);
   const float w00 = (1.0f - a) * (1.0f - c), w01 = (1.0f - a) * c, w10 = a * (1.0f - c), w11 = a * c;
   const float lr = w00 * v00.x + w01 * v01.x + w10 * v10.x + w11 * v11.x;
   const float lm = w00 * v00.y + w01 * v01.y + w10 * v10.y + w11 * v11.y;
@@ -213,7 +235,7 @@ __device__ __forceinline__ float2 sun_lookup_desc(const float4* __restrict__ tab
 template <class Real, int WARPS>
 __global__ void __launch_bounds__(WARPS * 32, 4) k_first_order(const AtmoParams* params, BuildDims d,
                                                             const RowInfo* rowinfo, const RowSample<Real>* rows,
-                                                            const CellGeom<Real>* geom, const float4* sun_table,
+                                                            const CellGeom<Real>* geom, const unsigned char* sun_table,
                                                             Vec4<Real>* rayleigh, Vec4<Real>* mie) {
   extern __shared__ unsigned char smem_raw[];
   FirstOrderSmem<Real>* sm = reinterpret_cast<FirstOrderSmem<Real>*>(smem_raw);
@@ -261,7 +283,7 @@ __global__ void __launch_bounds__(WARPS * 32, 4) k_first_order(const AtmoParams*
   const Real rr = rw.r, D0 = rw.D[0], D1 = rw.D[1], D2 = rw.D[2];
   const PhaseCS<Real> phase_ray(Bulk<Real>::phase_ray(P));
   const long long node0 = (b * nrows + row) * ncell;
-  const float4* tab = sun_table ? sun_table + (long long)b * kSunTableLen : nullptr;
+  const unsigned char* tab = sun_table ? sun_table + (size_t)b * kSunTableBytes : nullptr;
 
   for (int cell = warp; cell < ncell; cell += WARPS) {
     const CellGeom<Real> g = geom[node0 + cell];
@@ -281,7 +303,7 @@ __global__ void __launch_bounds__(WARPS * 32, 4) k_first_order(const AtmoParams*
         Real odr, odm;
         if (std::is_same<Real, float>::value && tab && (bp < Real(0) || q < qlim)) {
           const float2 od = bp >= Real(0) ? sun_lookup(tab, P, (float)q, (float)texit)
-                                          : sun_lookup_desc(tab + (long long)kSunNR * kSunNM, P, (float)q, (float)bp,
+                                          : sun_lookup_desc(tab + kSunClimbBytes, P, (float)q, (float)bp,
                                                             (float)texit);
           odr = (Real)od.x;
           odm = (Real)od.y;
@@ -326,7 +348,7 @@ __global__ void __launch_bounds__(WARPS * 32, 4) k_first_order(const AtmoParams*
 
 template <class Real>
 void launch_first_order(const AtmoParams* params, const BuildDims& d, const RowInfo* rowinfo,
-                        const RowSample<Real>* rows, const CellGeom<Real>* geom, const float4* sun_table,
+                        const RowSample<Real>* rows, const CellGeom<Real>* geom, const unsigned char* sun_table,
                         Vec4<Real>* rayleigh, Vec4<Real>* mie, cudaStream_t st) {
   constexpr int WARPS = 8;
   size_t smem = sizeof(FirstOrderSmem<Real>) * d.S;
@@ -336,10 +358,10 @@ void launch_first_order(const AtmoParams* params, const BuildDims& d, const RowI
 }
 
 template void launch_first_order<float>(const AtmoParams*, const BuildDims&, const RowInfo*,
-                                        const RowSample<float>*, const CellGeom<float>*, const float4*,
+                                        const RowSample<float>*, const CellGeom<float>*, const unsigned char*,
                                         Vec4<float>*, Vec4<float>*, cudaStream_t);
 template void launch_first_order<double>(const AtmoParams*, const BuildDims&, const RowInfo*,
-                                         const RowSample<double>*, const CellGeom<double>*, const float4*,
+                                         const RowSample<double>*, const CellGeom<double>*, const unsigned char*,
                                          Vec4<double>*, Vec4<double>*, cudaStream_t);
 
 // Work census of the first order: count[0] = the (node, sample) pairs whose

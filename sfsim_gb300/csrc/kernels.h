@@ -67,7 +67,7 @@ void launch_surface_base(const AtmoParams* params, const BuildDims& d, Vec4<Real
 // First-order Rayleigh ray scatter and Mie strength (fused).
 template <class Real>
 void launch_first_order(const AtmoParams* params, const BuildDims& d, const RowInfo* rowinfo,
-                        const RowSample<Real>* rows, const CellGeom<Real>* geom, const float4* sun_table,
+                        const RowSample<Real>* rows, const CellGeom<Real>* geom, const unsigned char* sun_table,
                         Vec4<Real>* rayleigh, Vec4<Real>* mie, cudaStream_t st);
 
 // Sun-ray optical-depth tables of the FP32 first order, per atmosphere: the
@@ -78,7 +78,16 @@ constexpr int kSunNM = 2048;
 constexpr int kDescNX = 1024;
 constexpr int kDescNY = 2048;
 constexpr long long kSunTableLen = (long long)kSunNR * kSunNM + (long long)kDescNX * kDescNY;
-void launch_sun_table(const AtmoParams* params, const BuildDims& d, float4* table, cudaStream_t st);
+// Bytes of the tables per atmosphere: the climbing table's rows, then the
+// descending table's.  A table of paired texels holds (v(j), v(j + 1)) per
+// entry, 16 bytes; otherwise v(j), 8 bytes.  Pairing the climbing table
+// (most lookups) halves its L1 sectors; pairing the descending one too made
+// the tables (96 MB) spill from L2 and gained nothing.
+constexpr bool kSunPairClimb = true, kSunPairDesc = false;
+constexpr size_t kSunClimbBytes = (size_t)kSunNR * kSunNM * (kSunPairClimb ? 16 : 8);
+constexpr size_t kSunDescBytes = (size_t)kDescNX * kDescNY * (kSunPairDesc ? 16 : 8);
+constexpr size_t kSunTableBytes = kSunClimbBytes + kSunDescBytes;
+void launch_sun_table(const AtmoParams* params, const BuildDims& d, unsigned char* table, cudaStream_t st);
 
 template <class Real>
 void launch_first_order_census(const AtmoParams* params, const BuildDims& d, const RowInfo* rowinfo,
