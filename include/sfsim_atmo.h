@@ -268,6 +268,24 @@ int sfsim_atmo_query_table(const sfsim_atmo_context* ctx, int kind, long long n,
                            const float* b, const float* light, float* out, int weight_bits,
                            void* stream);
 
+/* Attenuation of light along view rays as sfsim's shaders compute it from the
+ * tables (resources/shaders/atmosphere/, FP32, weights as in
+ * sfsim_atmo_query_table), one RGBA result per query in out [n][4]:
+ *   kind 0  attenuation-outer.glsl   attenuation_outer(light, p, d, s[0], incoming.rgb);
+ *           alpha = incoming.a
+ *   kind 1  attenuation-track.glsl   attenuation_track(light, p, d, (s[0], s[1]), incoming)
+ *           (p the ray origin, d its direction, s the segment's start and length)
+ *   kind 2  attenuation-point.glsl   attenuation_point(p, incoming) with the shader's
+ *           uniforms origin = d (the eye) and light_direction = light
+ *   kind 3  transmittance-point.glsl transmittance_point(p), uniform light_direction
+ *           = light; alpha = 1
+ * DEVICE arrays: light, p, d [n][3]; s [n][2]; incoming [n][4] (d, s and incoming
+ * may be NULL where the kind does not read them).  `amplification` is the
+ * shaders' uniform of that name. */
+int sfsim_atmo_query_attenuation(const sfsim_atmo_context* ctx, int kind, long long n, const float* light,
+                                 const float* p, const float* d, const float* s, const float* incoming,
+                                 float amplification, float* out, int weight_bits, void* stream);
+
 /* Rendered in-scatter S + M phase(mie g, v.l) at position x, unit view v and
  * unit sun l (FP64 inputs) by direct quadrature, without the 4-D table: the
  * first order integrated at the point as atmosphere.clj:154-200 does, plus

@@ -1555,6 +1555,123 @@ static f3 in_scatter_query_f(const glsl_env* e, f3 light, f3 point, f3 direction
   return in_scatter_at_f(e, idx, fdot(direction, light));
 }
 
+/* core/ray-hypersphere.glsl instantiated as ray_sphere (shaders.clj:18-20):
+ * out = (distance to the entry, clipped at 0, and length inside) */
+static void ray_sphere_f(f3 centre, float radius, f3 origin, f3 direction, float* out) {
+  f3 pos = fsub(origin, centre);
+  float direction_sqr = fdot(direction, direction);
+  float direction_pos = fdot(direction, pos);
+  float discriminant = direction_pos * direction_pos - direction_sqr * (fdot(pos, pos) - radius * radius);
+  if (discriminant > 0) {
+    float half_length = sqrtf(discriminant) / direction_sqr;
+    float middle = -fdot(direction, pos) / direction_sqr;
+    out[0] = middle - half_length;
+    out[1] = 2 * half_length;
+    if (out[0] < 0) {
+      out[1] = fmaxf(0.0f, out[1] + out[0]);
+      out[0] = 0;
+    }
+  } else {
+    out[0] = 0;
+    out[1] = 0;
+  }
+}
+
+/* core/limit-interval.glsl */
+static void limit_interval_f(float* interval, float limit) {
+  float end = fminf(interval[0] + interval[1], limit);
+  interval[1] = end - interval[0];
+}
+
+/* atmosphere/attenuate.glsl: incoming RGBA through the track from start to point */
+static void attenuate_f(const glsl_env* e, f3 light, f3 start, f3 point, const float* incoming, float amplification,
+                        float* out) {
+  f3 transmittance = transmittance_track_f(e, start, point);
+  f3 in_scatter = fmulf(ray_scatter_track_f(e, light, start, point), amplification);
+  out[0] = incoming[0] * transmittance.x + in_scatter.x * incoming[3];
+  out[1] = incoming[1] * transmittance.y + in_scatter.y * incoming[3];
+  out[2] = incoming[2] * transmittance.z + in_scatter.z * incoming[3];
+  out[3] = incoming[3];
+}
+
+/* atmosphere/attenuation-outer.glsl: RGB light from origin + a direction,
+ * looking along direction out of the atmosphere */
+static void attenuation_outer_f(const glsl_env* e, f3 light, f3 origin, f3 direction, float a, const float* incoming,
+                                float amplification, float* out) {
+  f3 point = fadd(origin, fmulf(direction, a));
+  f3 transmittance = transmittance_outer_f(e, point, direction);
+  f3 ray_scatter = fmulf(ray_scatter_outer_f(e, light, point, direction), amplification);
+  out[0] = incoming[0] * transmittance.x + ray_scatter.x;
+  out[1] = incoming[1] * transmittance.y + ray_scatter.y;
+  out[2] = incoming[2] * transmittance.z + ray_scatter.z;
+}
+
+/* atmosphere/attenuation-track.glsl: segment = (start, length) along the ray */
+static void attenuation_track_f(const glsl_env* e, f3 light, f3 origin, f3 direction, const float* segment,
+                                const float* incoming, float amplification, float* out) {
+  if (segment[1] > 0) {
+    f3 p = fadd(origin, fmulf(direction, segment[0]));
+    f3 q = fadd(origin, fmulf(direction, segment[0] + segment[1]));
+    attenuate_f(e, light, p, q, incoming, amplification, out);
+  } else {
+    for (int c = 0; c < 4; c++) out[c] = incoming[c];
+  }
+}
+
+/* atmosphere/attenuation-point.glsl with its uniforms origin (the eye) and
+ * light_direction; normalize(v) taken as v times 1 / length(v), as the
+ * track lookups above divide a vector by a distance */
+static void attenuation_point_f(const glsl_env* e, f3 light, f3 origin, f3 point, const float* incoming,
+                                float amplification, float* out) {
+  f3 v = fsub(point, origin);
+  f3 direction = fmulf(v, 1.0f / flen(v));
+  float atmosphere[2];
+  ray_sphere_f(F(0, 0, 0), e->radius + e->max_height, origin, direction, atmosphere);
+  limit_interval_f(atmosphere, flen(fsub(origin, point)));
+  attenuation_track_f(e, light, origin, direction, atmosphere, incoming, amplification, out);
+}
+
+/* atmosphere/transmittance-point.glsl with its uniform light_direction */
+static f3 transmittance_point_f(const glsl_env* e, f3 light, f3 point) {
+  float atmosphere[2];
+  ray_sphere_f(F(0, 0, 0), e->radius + e->max_height, point, light, atmosphere);
+  if (atmosphere[1] > 0) return transmittance_outer_f(e, fadd(point, fmulf(light, atmosphere[0])), light);
+  return F(1, 1, 1);
+}
+
+/* n attenuation queries (out [n][4]):
+ *   kind 0 attenuation_outer(light, p, d, s[0], incoming.rgb), alpha passed through
+ *   kind 1 attenuation_track(light, p, d, (s[0], s[1]), incoming)
+ *   kind 2 attenuation_point(point p, incoming) with the uniform origin d
+ *   kind 3 transmittance_point(p), alpha 1
+ * light, p, d [n][3]; s [n][2]; incoming [n][4]; unused arrays may be NULL. */
+void oracle_glsl_attenuation_batch(const oracle_glsl_tables* t, int kind, long n, const float* light, const float* p,
+                                   const float* d, const float* s, const float* incoming, float amplification,
+                                   float* out) {
+  glsl_env e = {t->radius, t->max_height, t->t_height_size, t->t_elevation_size, t->height_size, t->elevation_size,
+                t->light_elevation_size, t->heading_size, t->transmittance, t->ray_scatter, t->mie_strength,
+                t->weight_bits};
+  for (long i = 0; i < n; i++) {
+    f3 L = F(light[3 * i], light[3 * i + 1], light[3 * i + 2]), P = F(p[3 * i], p[3 * i + 1], p[3 * i + 2]);
+    float* o = out + 4 * i;
+    if (kind == 3) {
+      f3 r = transmittance_point_f(&e, L, P);
+      o[0] = r.x; o[1] = r.y; o[2] = r.z; o[3] = 1;
+      continue;
+    }
+    f3 D = F(d[3 * i], d[3 * i + 1], d[3 * i + 2]);
+    const float* in = incoming + 4 * i;
+    if (kind == 0) {
+      attenuation_outer_f(&e, L, P, D, s[2 * i], in, amplification, o);
+      o[3] = in[3];
+    } else if (kind == 1) {
+      attenuation_track_f(&e, L, P, D, s + 2 * i, in, amplification, o);
+    } else {
+      attenuation_point_f(&e, L, D, P, in, amplification, o);
+    }
+  }
+}
+
 /* kind 0: transmittance_track(p, q); 1: transmittance_outer(p, d);
  * 2: ray_scatter_track(light, p, q); 3: ray_scatter_outer(light, p, d) */
 void oracle_glsl_query(const oracle_glsl_tables* t, int kind, const float* light, const float* p, const float* q,

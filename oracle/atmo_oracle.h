@@ -77,6 +77,11 @@ void oracle_glsl_query(const oracle_glsl_tables* t, int kind, const float* light
                        float* out);
 void oracle_glsl_query_batch(const oracle_glsl_tables* t, int kind, long n, const float* light, const float* p,
                              const float* q, float* out, int* above);
+/* n attenuation queries of atmosphere/attenuation-*.glsl and
+ * transmittance-point.glsl (kinds 0-3; see atmo_oracle.c). */
+void oracle_glsl_attenuation_batch(const oracle_glsl_tables* t, int kind, long n, const float* light, const float* p,
+                                   const float* d, const float* s, const float* incoming, float amplification,
+                                   float* out);
 
 #ifdef __cplusplus
 }

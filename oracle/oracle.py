@@ -455,6 +455,40 @@ def glsl_query_batch(tables: dict, kind: int, light, p, q, weight_bits: int = 0)
     return out, above.astype(bool)
 
 
+def glsl_attenuation_batch(tables: dict, kind: int, light, p, d=None, s=None, incoming=None,
+                           amplification: float = 1.0, weight_bits: int = 0):
+    """n attenuation queries (atmo_oracle.c oracle_glsl_attenuation_batch):
+    kind 0 attenuation_outer(light, p, d, s[0], incoming.rgb), 1
+    attenuation_track(light, p, d, s, incoming), 2 attenuation_point(p,
+    incoming) with the eye d, 3 transmittance_point(p).  Inputs are rounded to
+    float32 first; returns float32 [n][4]."""
+    T = np.ascontiguousarray(tables["transmittance"], dtype=np.float32)
+    S = np.ascontiguousarray(tables["ray_scatter"], dtype=np.float32)
+    M = np.ascontiguousarray(tables["mie_strength"], dtype=np.float32)
+    t = GlslTables()
+    t.radius = tables["radius"]
+    t.max_height = tables["max_height"]
+    t.t_height_size, t.t_elevation_size = tables["transmittance_shape"]
+    (t.height_size, t.elevation_size, t.light_elevation_size, t.heading_size) = tables["ray_scatter_shape"]
+    t.transmittance = T.ctypes.data_as(_fp)
+    t.ray_scatter = S.ctypes.data_as(_fp)
+    t.mie_strength = M.ctypes.data_as(_fp)
+    t.weight_bits = weight_bits
+
+    def f32(a, w):
+        return None if a is None else np.ascontiguousarray(np.asarray(a, dtype=np.float32).reshape(-1, w))
+    lt, pt, dt, st, it = f32(light, 3), f32(p, 3), f32(d, 3), f32(s, 2), f32(incoming, 4)
+    n = pt.shape[0]
+    out = np.empty((n, 4), dtype=np.float32)
+    ptr = lambda a: None if a is None else a.ctypes.data_as(_fp)  # noqa: E731
+    L = lib()
+    L.oracle_glsl_attenuation_batch.argtypes = [ctypes.POINTER(GlslTables), ctypes.c_int, ctypes.c_long, _fp, _fp,
+                                                _fp, _fp, _fp, ctypes.c_float, _fp]
+    L.oracle_glsl_attenuation_batch(ctypes.byref(t), kind, n, ptr(lt), ptr(pt), ptr(dt), ptr(st), ptr(it),
+                                    amplification, out.ctypes.data_as(_fp))
+    return out
+
+
 # --- cloud-noise builders (noise_oracle.c) ----------------------------------------
 
 def worley(divisions: int, size: int, grid):

@@ -31,7 +31,7 @@ EXPORTS = (
     "sfsim_atmo_cond_surrogate_train", "sfsim_atmo_cond_surrogate_parameters", "sfsim_atmo_cond_surrogate_gradients",
     "sfsim_atmo_query_cond_surrogate", "sfsim_atmo_plan_create", "sfsim_atmo_plan_build", "sfsim_atmo_plan_destroy",
     "sfsim_atmo_set_wait_limit", "sfsim_atmo_wait_selftest", "sfsim_atmo_last_transfer_bytes",
-    "sfsim_atmo_iteration_state_bytes", "sfsim_atmo_build_resumable",
+    "sfsim_atmo_iteration_state_bytes", "sfsim_atmo_build_resumable", "sfsim_atmo_query_attenuation",
 )
 
 
@@ -104,6 +104,8 @@ def load(build: bool = False):
     L.sfsim_atmo_context_point_scatter_sum.argtypes = [vp, ctypes.POINTER(vp)]
     L.sfsim_atmo_query_table.argtypes = [vp, ctypes.c_int, ctypes.c_longlong, vp, vp, vp, vp, ctypes.c_int, vp]
     L.sfsim_atmo_query_direct.argtypes = [vp, ctypes.c_longlong, vp, vp, vp, vp, vp]
+    L.sfsim_atmo_query_attenuation.argtypes = [vp, ctypes.c_int, ctypes.c_longlong, vp, vp, vp, vp, vp,
+                                               ctypes.c_float, vp, ctypes.c_int, vp]
     L.sfsim_atmo_gemm_bf16.argtypes = [vp, vp, vp, ctypes.c_int, ctypes.c_int, ctypes.c_longlong, ctypes.c_int, vp]
     L.sfsim_atmo_surrogate_train.argtypes = [vp, ctypes.POINTER(SurrogateConfig), vp]
     L.sfsim_atmo_surrogate_parameters.argtypes = [vp, vp, vp, ctypes.POINTER(ctypes.c_longlong)]

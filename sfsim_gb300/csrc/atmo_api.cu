@@ -1716,6 +1716,35 @@ int sfsim_atmo_query_table(const sfsim_atmo_context* ctx, int kind, long long n,
   return 0;
 }
 
+int sfsim_atmo_query_attenuation(const sfsim_atmo_context* ctx, int kind, long long n, const float* light,
+                                 const float* p, const float* d, const float* s, const float* incoming,
+                                 float amplification, float* out, int weight_bits, void* stream) {
+  if (!ctx) return fail(SFSIM_ATMO_ENULL, "context is NULL");
+  if (kind < 0 || kind > 3) return fail(SFSIM_ATMO_EINVAL, "attenuation kind must be in [0, 3]");
+  if (weight_bits < 0 || weight_bits > 16) return fail(SFSIM_ATMO_EINVAL, "weight_bits must be in [0, 16]");
+  if (n < 0) return fail(SFSIM_ATMO_EINVAL, "n must be non-negative");
+  if (n == 0) return 0;
+  if (!light || !p || !out || (kind <= 2 && (!d || !incoming)) || (kind <= 1 && !s))
+    return fail(SFSIM_ATMO_ENULL, "an input or output array of this kind is NULL");
+  QueryTables q;
+  q.radius = (float)ctx->cfg.radius;
+  q.max_height = (float)ctx->cfg.height;
+  q.mie_g = (float)ctx->cfg.mie.scatter_g;
+  q.t_height = ctx->dims.nT0;
+  q.t_elevation = ctx->dims.nT1;
+  q.height = ctx->dims.n0;
+  q.elevation = ctx->dims.n1;
+  q.light = ctx->dims.n2;
+  q.heading = ctx->dims.n3;
+  q.T = ctx->T;
+  q.S = ctx->S;
+  q.M = ctx->M;
+  launch_query_attenuation(q, kind, n, light, p, d, s, incoming, amplification, out, weight_bits,
+                           (cudaStream_t)stream);
+  CUDA_TRY(cudaGetLastError());
+  return 0;
+}
+
 int sfsim_atmo_query_direct(const sfsim_atmo_context* ctx, long long n, const double* x, const double* v,
                             const double* l, float* out, void* stream) {
   if (!ctx) return fail(SFSIM_ATMO_ENULL, "context is NULL");

@@ -252,6 +252,93 @@ __global__ void k_query_table(GlslEnv e, int kind, long long n, const float* A, 
   out[3 * t + 2] = r.z;
 }
 
+// core/ray-hypersphere.glsl instantiated as ray_sphere (shaders.clj:18-20):
+// (distance to the entry, clipped at 0, and length inside)
+__device__ float2 ray_sphere_g(f3 centre, float radius, f3 origin, f3 direction) {
+  const f3 pos = fsub(origin, centre);
+  const float direction_sqr = fdot(direction, direction);
+  const float direction_pos = fdot(direction, pos);
+  const float discriminant = direction_pos * direction_pos - direction_sqr * (fdot(pos, pos) - radius * radius);
+  if (discriminant > 0) {
+    const float half_length = sqrtf(discriminant) / direction_sqr;
+    const float middle = -fdot(direction, pos) / direction_sqr;
+    float2 r = make_float2(middle - half_length, 2 * half_length);
+    if (r.x < 0) {
+      r.y = fmaxf(0.0f, r.y + r.x);
+      r.x = 0;
+    }
+    return r;
+  }
+  return make_float2(0, 0);
+}
+
+// core/limit-interval.glsl
+__device__ __forceinline__ float2 limit_interval_g(float2 interval, float limit) {
+  const float end = fminf(interval.x + interval.y, limit);
+  return make_float2(interval.x, end - interval.x);
+}
+
+// atmosphere/attenuate.glsl: incoming RGBA through the track from start to point
+__device__ float4 attenuate_g(const GlslEnv& e, f3 l, f3 start, f3 point, float4 in, float amplification) {
+  const f3 t = transmittance_track_g(e, start, point);
+  const f3 s = fmul(ray_scatter_track_g(e, l, start, point), amplification);
+  return make_float4(in.x * t.x + s.x * in.w, in.y * t.y + s.y * in.w, in.z * t.z + s.z * in.w, in.w);
+}
+
+// atmosphere/attenuation-track.glsl: segment = (start, length) along the ray
+__device__ float4 attenuation_track_g(const GlslEnv& e, f3 l, f3 origin, f3 direction, float2 segment, float4 in,
+                                      float amplification) {
+  if (segment.y > 0) {
+    const f3 p = fadd(origin, fmul(direction, segment.x));
+    const f3 q = fadd(origin, fmul(direction, segment.x + segment.y));
+    return attenuate_g(e, l, p, q, in, amplification);
+  }
+  return in;
+}
+
+// Attenuation queries of atmosphere/attenuation-outer.glsl (kind 0, alpha
+// passed through), attenuation-track.glsl (1), attenuation-point.glsl (2,
+// with the uniform origin, the eye, in D) and transmittance-point.glsl (3,
+// alpha 1); normalize(v) is v times 1 / length(v), as the track lookups
+// divide a vector by a distance.
+__global__ void k_query_attenuation(GlslEnv e, int kind, long long n, const float* L, const float* P,
+                                    const float* D, const float* Sg, const float* In, float amplification,
+                                    float* out) {
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  const f3 l = F3(L[3 * t], L[3 * t + 1], L[3 * t + 2]);
+  const f3 p = F3(P[3 * t], P[3 * t + 1], P[3 * t + 2]);
+  float4 r;
+  if (kind == 3) {
+    const float2 atm = ray_sphere_g(F3(0, 0, 0), e.radius + e.max_height, p, l);
+    const f3 tr = atm.y > 0 ? transmittance_outer_g(e, fadd(p, fmul(l, atm.x)), l) : F3(1, 1, 1);
+    r = make_float4(tr.x, tr.y, tr.z, 1.0f);
+  } else {
+    const f3 d = F3(D[3 * t], D[3 * t + 1], D[3 * t + 2]);
+    const float4 in = make_float4(In[4 * t], In[4 * t + 1], In[4 * t + 2], In[4 * t + 3]);
+    if (kind == 0) {
+      const f3 point = fadd(p, fmul(d, Sg[2 * t]));
+      const f3 tr = transmittance_outer_g(e, point, d);
+      const f3 rs = fmul(ray_scatter_outer_g(e, l, point, d), amplification);
+      r = make_float4(in.x * tr.x + rs.x, in.y * tr.y + rs.y, in.z * tr.z + rs.z, in.w);
+    } else if (kind == 1) {
+      r = attenuation_track_g(e, l, p, d, make_float2(Sg[2 * t], Sg[2 * t + 1]), in, amplification);
+    } else {
+      // attenuation_point(point p, incoming) with origin = d
+      const f3 v = fsub(p, d);
+      const f3 direction = fmul(v, 1.0f / sqrtf(fdot(v, v)));
+      float2 atm = ray_sphere_g(F3(0, 0, 0), e.radius + e.max_height, d, direction);
+      const f3 w = fsub(d, p);
+      atm = limit_interval_g(atm, sqrtf(fdot(w, w)));
+      r = attenuation_track_g(e, l, d, direction, atm, in, amplification);
+    }
+  }
+  out[4 * t] = r.x;
+  out[4 * t + 1] = r.y;
+  out[4 * t + 2] = r.z;
+  out[4 * t + 3] = r.w;
+}
+
 static GlslEnv make_env(const QueryTables& q, int weight_bits) {
   GlslEnv e;
   e.radius = q.radius;
@@ -275,6 +362,15 @@ void launch_query_table(const QueryTables& q, int kind, long long n, const float
   const GlslEnv e = make_env(q, weight_bits);
   const int blk = 128;
   k_query_table<<<(unsigned)((n + blk - 1) / blk), blk, 0, st>>>(e, kind, n, a, b, l, out);
+}
+
+void launch_query_attenuation(const QueryTables& q, int kind, long long n, const float* light, const float* p,
+                              const float* d, const float* s, const float* incoming, float amplification, float* out,
+                              int weight_bits, cudaStream_t st) {
+  const GlslEnv e = make_env(q, weight_bits);
+  const int blk = 128;
+  k_query_attenuation<<<(unsigned)((n + blk - 1) / blk), blk, 0, st>>>(e, kind, n, light, p, d, s, incoming,
+                                                                       amplification, out);
 }
 
 // The surrogate's coordinates of (p, d, l): the table coordinates as the

@@ -155,6 +155,9 @@ struct QueryTables {
 // (a, b, l) with the horizon test choosing the table half.  Points [n][3].
 void launch_query_table(const QueryTables& q, int kind, long long n, const float* a, const float* b, const float* l,
                         float* out, int weight_bits, cudaStream_t st);
+void launch_query_attenuation(const QueryTables& q, int kind, long long n, const float* light, const float* p,
+                              const float* d, const float* s, const float* incoming, float amplification, float* out,
+                              int weight_bits, cudaStream_t st);
 
 // Rendered in-scatter S + M phase(mie, v.l) at (x, v, l) by quadrature with
 // the order-summed point-scatter table Jsum (NULL: first order only).

@@ -87,6 +87,25 @@ class Context:
                                                   out.data_ptr(), weight_bits, st), "query_table")
         return out
 
+    def attenuation(self, kind: int, light, p, d=None, s=None, incoming=None, amplification: float = 1.0,
+                    weight_bits: int = 0, out=None):
+        """Attenuation along view rays as the shaders compute it
+        (sfsim_atmo_query_attenuation): kind 0 attenuation_outer(light, p, d,
+        s[:, 0], incoming rgb), 1 attenuation_track(light, p, d, s, incoming),
+        2 attenuation_point(p, incoming) with the eye d, 3
+        transmittance_point(p); CUDA tensors in, an [n, 4] RGBA tensor out."""
+        import torch
+        f = lambda t: t.contiguous().float() if t is not None else None  # noqa: E731
+        light, p, d, s, incoming = f(light), f(p), f(d), f(s), f(incoming)
+        n = p.shape[0]
+        out = out if out is not None else torch.empty((n, 4), dtype=torch.float32, device="cuda")
+        ptr = lambda t: t.data_ptr() if t is not None else None  # noqa: E731
+        st = torch.cuda.current_stream().cuda_stream
+        _lib.check(self._L.sfsim_atmo_query_attenuation(self._ptr, kind, n, ptr(light), ptr(p), ptr(d), ptr(s),
+                                                        ptr(incoming), amplification, out.data_ptr(), weight_bits,
+                                                        st), "query_attenuation")
+        return out
+
     # -- surrogate -------------------------------------------------------------
     def train_surrogate(self, steps=2000, batch=65536, direct_samples=1 << 20, node_fraction=0.0, lr=1e-3,
                         seed=1, huber_delta=0.0):

@@ -1,6 +1,7 @@
 """GPU queries of a built atmosphere against the CPU oracle.
 
-* Table lookups (sfsim_atmo_query_table): the CUDA restatement of the GLSL
+* Table lookups (sfsim_atmo_query_table) and the attenuation shaders built
+  on them (sfsim_atmo_query_attenuation): the CUDA restatement of the GLSL
   consumers against the oracle's C restatement of the same shaders, on the
   tables the GPU built (small and production shapes), on the same FP32 inputs,
   for both exact and GL 8-bit bilinear weights, within 1e-6 per channel.
@@ -141,6 +142,76 @@ def test_table_queries_production_tables(production_ctx):
     cfg, ctx = production_ctx
     report = _check_table_queries(cfg, ctx, 300)
     assert min(report.values()) > 0.99, report
+
+
+def _attenuation_inputs(cfg, kind, n, seed):
+    """Inputs of one attenuation kind: origins and points inside and above
+    the atmosphere (up to twice its height), unit directions and suns,
+    distances along the ray and track segments of up to three heights (some
+    empty, which pass the light through), incoming RGBA in [0, 1]."""
+    rng = np.random.default_rng(seed)
+    R, H = cfg.radius, cfg.height
+
+    def unit(k):
+        v = rng.normal(size=(k, 3))
+        return v / np.linalg.norm(v, axis=1, keepdims=True)
+    def points(k, top):
+        return unit(k) * (R + rng.uniform(0.0, top, k))[:, None]
+    light = unit(n)
+    incoming = rng.uniform(0.0, 1.0, (n, 4))
+    s = None
+    if kind == 0:
+        p, d = points(n, H), unit(n)
+        s = np.stack([rng.uniform(0.0, 0.5 * H, n), np.zeros(n)], axis=1)
+    elif kind == 1:
+        p, d = points(n, 2 * H), unit(n)
+        s = np.stack([rng.uniform(0.0, H, n), rng.uniform(-0.1 * H, 3 * H, n)], axis=1)
+    elif kind == 2:
+        p, d = points(n, H), points(n, 2 * H)  # the point, then the eye
+    else:
+        p, d = points(n, H), None
+    f = lambda z: None if z is None else np.ascontiguousarray(z, dtype=np.float32)  # noqa: E731
+    return f(light), f(p), f(d), f(s), f(incoming)
+
+
+def _check_attenuation(cfg, ctx, seed):
+    """Every attenuation kind (attenuation-outer, -track, -point and
+    transmittance-point), exact and 8-bit weights, 4096 queries each: the
+    CUDA composition against the oracle's C restatement of the same shaders
+    on identical FP32 inputs; both run the same IEEE operations in the same
+    order, so they agree within 1e-6 per channel, in practice bit for bit."""
+    import torch
+    tables = _host_tables(cfg, ctx)
+    same = {}
+    for kind in range(4):
+        light, p, d, s, inc = _attenuation_inputs(cfg, kind, 4096, seed + kind)
+        cuda = lambda z: None if z is None else torch.from_numpy(z).cuda()  # noqa: E731
+        for bits in (0, 8):
+            gpu = ctx.attenuation(kind, cuda(light), cuda(p), cuda(d), cuda(s), cuda(inc), amplification=2.5,
+                                  weight_bits=bits).cpu().numpy()
+            ref = O.glsl_attenuation_batch(tables, kind, light, p, d, s, inc, 2.5, bits)
+            assert np.isfinite(gpu).all(), (kind, bits)
+            err = rel_err(gpu, ref, 1e-6)
+            assert err.max() <= 1e-6, (kind, bits, float(err.max()))
+            same[(kind, bits)] = float(np.mean(np.all(gpu == ref, axis=1)))
+        if kind == 1:  # empty segments pass the light through unchanged
+            empty = s[:, 1] <= 0
+            assert empty.any() and np.array_equal(gpu[empty], inc[empty])
+        if kind == 3:
+            assert np.all(gpu[:, 3] == 1) and np.all(gpu[:, :3] <= 1.0 + 1e-6)
+    return same
+
+
+def test_attenuation_queries_small_tables(small_ctx):
+    cfg, ctx = small_ctx
+    same = _check_attenuation(cfg, ctx, 500)
+    assert min(same.values()) > 0.99, same
+
+
+def test_attenuation_queries_production_tables(production_ctx):
+    cfg, ctx = production_ctx
+    same = _check_attenuation(cfg, ctx, 600)
+    assert min(same.values()) > 0.99, same
 
 
 def test_direct_queries_match_oracle(small_ctx):
