@@ -145,6 +145,8 @@ __device__ __forceinline__ V2<Real> ld2(const Real* p) {
   return *reinterpret_cast<const V2<Real>*>(p);
 }
 
+static_assert(kDirBlock % 2 == 0, "direction pairs start at even indices (8-byte loads of pair fields)");
+
 // Blocks per (height, sun elevation) pair when each evaluates `cpb` of the
 // pair's `nchunks` chunks of 256 nodes; the launch and the kernel share it.
 __host__ __device__ __forceinline__ int point_scatter_blocks_per_pair(int nchunks, int cpb) {
@@ -310,7 +312,11 @@ __global__ void __launch_bounds__(256, point_scatter_min_blocks(sizeof(Real))) k
           split_coord_r<Real>(sun_elevation_index_r<Real>(sg.x, scaleE), d.nE1, &ea, &ta);
           split_coord_r<Real>(sun_elevation_index_r<Real>(sg.y, scaleE), d.nE1, &eb, &tb);
           const int fa = upper_index(ea, d.nE1), fb = upper_index(eb, d.nE1);
-          const int ha = uE0s[wa], hb = uE0s[wa + 1];
+          // both directions' height rows in one 8-byte load (wa is even and
+          // the int array starts 8-byte aligned: kDirFields * used floats, used
+          // a multiple of kDirBlock)
+          const int2 hab = *reinterpret_cast<const int2*>(uE0s + wa);
+          const int ha = hab.x, hb = hab.y;
           const int ka = upper_index(ha, d.nE0), kb = upper_index(hb, d.nE0);
           const R2 sE1 = mk2(ta, tb), sE0 = ld2(dirs + 8 * used + wa);
           const R2 one = mk2(Real(1), Real(1));

@@ -72,7 +72,7 @@ def test_odd_shapes_match_oracle(precision):
         assert_close(gpu[key], ref[key], tol, key)
 
 
-WIDE_SHAPES = [(3, 5, 20, 14), (2, 5, 32, 9)]
+WIDE_SHAPES = [(3, 5, 20, 14), (2, 5, 32, 9), (2, 4, 64, 4)]
 
 
 def wide_config(shape, precision):
@@ -97,7 +97,8 @@ def wide_oracle():
 def test_wide_rows_and_long_rays_match_oracle(wide_oracle, shape, precision):
     """View rows of 20 x 14 = 280 and 32 x 9 = 288 nodes (more than a
     ray-scatter block's 256 threads: the plane build walks its cells; 32 sun
-    elevations store the planes by heading column, 20 by sun-elevation row)
+    elevations store the planes by heading column, 20 by sun-elevation row),
+    64 x 4 = 256 nodes (one cell per thread, heading columns of 68 texels),
     and 150 ray steps (more than the 128 samples whose constants a block
     keeps at once: they are formed chunk by chunk from the staged row
     samples)."""
