@@ -2,11 +2,11 @@
 
 tests/abi_layout.c is compiled against include/sfsim_atmo.h and prints every
 field's offset and size.  Three layouts must equal it:
-  * the coffi `config-struct` / `component-struct` binding written in
-    INTEGRATION.md (the binding a sfsim maintainer would add next to
-    src/clj/sfsim/jolt.clj:35-55), laid out by C's alignment rules with its
-    explicit padding members;
-  * the offset table in INTEGRATION.md;
+  * the coffi `config-struct` / `component-struct` binding of the
+    integration guide at the repository root (the binding a sfsim
+    maintainer would add next to src/clj/sfsim/jolt.clj:35-55), laid out by
+    C's alignment rules with its explicit padding members;
+  * that guide's offset table;
   * the Python ctypes mirror, sfsim_gb300.config.AtmoConfig.
 """
 import ctypes
@@ -50,7 +50,7 @@ _MEMBER = re.compile(r"\[:([\w-]+)\s+(::mem/\w+|\[::mem/array\s+(::mem/\w+)\s+(\
 
 def _struct_members(text, name):
     m = re.search(r"\(def " + re.escape(name) + r"\s+\[::mem/struct\s+\[(.*?)\]\]\)", text, re.S)
-    assert m, f"{name} not found in INTEGRATION.md"
+    assert m, f"{name} not found in the integration guide"
     return _MEMBER.findall(m.group(1))
 
 
