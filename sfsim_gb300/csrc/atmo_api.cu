@@ -348,6 +348,10 @@ cudaEvent_t g_events[kMaxDevices][2 * 512];
 // tables to the host while the scattering iterations still run
 cudaStream_t g_copy_stream[kMaxDevices];
 cudaEvent_t g_early_done[kMaxDevices];
+// surface radiance of each iteration runs on a side stream beside point and
+// ray scatter: forked after the previous iteration, joined before accumulation
+cudaStream_t g_side_stream[kMaxDevices];
+cudaEvent_t g_side_fork[kMaxDevices], g_side_join[kMaxDevices];
 
 struct Carver {
   char* base;
@@ -462,12 +466,14 @@ int ensure_stream(int dev) {
     CUDA_TRY(cudaStreamCreateWithFlags(&g_copy_stream[dev], cudaStreamNonBlocking));
     CUDA_TRY(cudaEventCreateWithFlags(&g_early_done[dev], cudaEventDisableTiming));
     CUDA_TRY(cudaStreamCreateWithFlags(&g_stream[dev], cudaStreamNonBlocking));
+    CUDA_TRY(cudaStreamCreateWithFlags(&g_side_stream[dev], cudaStreamNonBlocking));
+    CUDA_TRY(cudaEventCreateWithFlags(&g_side_fork[dev], cudaEventDisableTiming));
+    CUDA_TRY(cudaEventCreateWithFlags(&g_side_join[dev], cudaEventDisableTiming));
     for (int i = 0; i < 2 * 512; i++) CUDA_TRY(cudaEventCreate(&g_events[dev][i]));
   }
   return 0;
 }
 
-// Stage timing with events on the build stream.
 // Stage boundaries of a build: CUDA events on the build stream when timing
 // is enabled, and always an NVTX range per stage ("sfsim first order",
 // "sfsim iteration 3 ray scatter", ...), so that a profiler can select one
@@ -479,7 +485,7 @@ struct Timer {
   int stage_of[512];
   int iteration = 0;  // iteration of the stages that follow (1-based); 0 outside the loop
   int open = 0;   // NVTX ranges pushed and not yet popped
-  void mark_begin(int stage) {
+  void mark_begin(int stage, cudaStream_t on = nullptr) {
     char name[64];
     if (iteration > 0)
       snprintf(name, sizeof name, "sfsim iteration %d %s", iteration, kStageNames[stage]);
@@ -489,15 +495,16 @@ struct Timer {
     open++;
     if (!g_timing || n >= 511) return;
     stage_of[n / 2] = stage;
-    cudaEventRecord(g_events[dev][n++], st);
+    cudaEventRecord(g_events[dev][n++], on ? on : st);
   }
-  void mark_end() {
+  // `on`: the stream of the matching mark_begin, when not the build stream
+  void mark_end(cudaStream_t on = nullptr) {
     if (open > 0) {
       nvtxRangePop();
       open--;
     }
     if (!g_timing || n % 2 == 0) return;
-    cudaEventRecord(g_events[dev][n++], st);
+    cudaEventRecord(g_events[dev][n++], on ? on : st);
   }
   ~Timer() {
     for (; open > 0; open--) nvtxRangePop();  // a stage left by an error return
@@ -589,6 +596,26 @@ int run_build(const Work<Real>& w, const BuildDims& d, float* oT, float* oE, flo
     Vec4<Real>* dS_new = w.dS[it & 1];
     Vec4<Real>* E_new = w.Eacc[it & 1];
     Vec4<Real>* S_new = w.Sacc[it & 1];
+    // surface radiance reads only the previous iteration's dS (and the
+    // first-order Mie strength): it runs on the side stream beside point and
+    // ray scatter, forked after everything before this iteration (so the dE
+    // buffer it overwrites is no longer read) and joined before accumulation.
+    // Entry points that create no streams (the allocation-free build) keep it
+    // on the build stream, and so do builds with stage timing on, so that
+    // each stage's time is its own and the stages add up to the build.
+    cudaStream_t ss = g_side_stream[tm.dev];
+    const bool fork = ss != nullptr && !g_timing;
+    if (fork) {
+      CUDA_TRY(cudaEventRecord(g_side_fork[tm.dev], st));
+      CUDA_TRY(cudaStreamWaitEvent(ss, g_side_fork[tm.dev], 0));
+    } else {
+      ss = st;
+    }
+    tm.mark_begin(6, ss);
+    launch_surface_radiance<Real>(w.params, d, w.setup.erow, w.setup.hdir, dS_prev, M_first, dE_new, ss);
+    launches++;
+    tm.mark_end(ss);
+    if (fork) CUDA_TRY(cudaEventRecord(g_side_join[tm.dev], ss));
     tm.mark_begin(5);
     if (launch_point_scatter<Real>(w.params, d, w.setup.rowinfo, w.setup.pdirs, w.setup.dimage, w.setup.pcount,
                                    w.setup.prow,
@@ -600,16 +627,14 @@ int run_build(const Work<Real>& w, const BuildDims& d, float* oT, float* oE, flo
       launch_add_to_sum<Real>(d.n4(), d.B, w.J, jsum, it == 0, st);
       launches++;
     }
-    tm.mark_begin(6);
-    launch_surface_radiance<Real>(w.params, d, w.setup.erow, w.setup.hdir, dS_prev, M_first, dE_new, st);
-    launches++;
-    tm.mark_end();
+
     tm.mark_begin(7);
     if (launch_ray_scatter<Real>(w.params, d, w.setup.rowinfo, w.setup.rows, w.setup.geom, w.setup.remapS, w.J,
                                  dS_new, st))
       return fail(SFSIM_ATMO_ECUDA, "ray scatter launch configuration failed");
     launches++;
     tm.mark_end();
+    if (fork) CUDA_TRY(cudaStreamWaitEvent(st, g_side_join[tm.dev], 0));
     tm.mark_begin(8);
     launch_accumulate2<Real>(d.B, d.nE0, d.nE1, w.setup.remapE, E_prev, dE_new, E_new, st);
     launch_accumulate4<Real>(d, w.setup.remapS, S_prev, dS_new, S_new, st);
