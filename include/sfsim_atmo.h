@@ -224,8 +224,8 @@ int sfsim_atmo_build_resumable(const sfsim_atmo_config* cfg, const sfsim_atmo_it
  * accumulate, output.  Returns the number of stages written (at most `n`);
  * for sfsim_atmo_build_device it waits for the build's last event.  With
  * timing on every stage runs on the build stream, so the stages add up to the
- * build; with timing off each iteration's surface radiance runs on a second
- * stream beside point scatter and ray scatter. */
+ * build; with timing off each iteration's surface radiance and accumulation
+ * run on a second stream beside point scatter and ray scatter. */
 int sfsim_atmo_set_timing(int enabled);
 int sfsim_atmo_last_timings(double* ms, int n);
 

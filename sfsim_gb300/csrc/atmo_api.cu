@@ -348,10 +348,10 @@ cudaEvent_t g_events[kMaxDevices][2 * 512];
 // tables to the host while the scattering iterations still run
 cudaStream_t g_copy_stream[kMaxDevices];
 cudaEvent_t g_early_done[kMaxDevices];
-// surface radiance of each iteration runs on a side stream beside point and
-// ray scatter: forked after the previous iteration, joined before accumulation
+// each iteration's surface radiance and accumulation run on a side stream
+// beside point and ray scatter (run_build)
 cudaStream_t g_side_stream[kMaxDevices];
-cudaEvent_t g_side_fork[kMaxDevices], g_side_join[kMaxDevices];
+cudaEvent_t g_side_fork[kMaxDevices], g_side_sr[kMaxDevices], g_side_rs[kMaxDevices], g_side_acc[kMaxDevices];
 
 struct Carver {
   char* base;
@@ -467,8 +467,8 @@ int ensure_stream(int dev) {
     CUDA_TRY(cudaEventCreateWithFlags(&g_early_done[dev], cudaEventDisableTiming));
     CUDA_TRY(cudaStreamCreateWithFlags(&g_stream[dev], cudaStreamNonBlocking));
     CUDA_TRY(cudaStreamCreateWithFlags(&g_side_stream[dev], cudaStreamNonBlocking));
-    CUDA_TRY(cudaEventCreateWithFlags(&g_side_fork[dev], cudaEventDisableTiming));
-    CUDA_TRY(cudaEventCreateWithFlags(&g_side_join[dev], cudaEventDisableTiming));
+    for (cudaEvent_t* e : {&g_side_fork[dev], &g_side_sr[dev], &g_side_rs[dev], &g_side_acc[dev]})
+      CUDA_TRY(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
     for (int i = 0; i < 2 * 512; i++) CUDA_TRY(cudaEventCreate(&g_events[dev][i]));
   }
   return 0;
@@ -590,32 +590,39 @@ int run_build(const Work<Real>& w, const BuildDims& d, float* oT, float* oE, flo
     M_first = nullptr;
     it0 = k;
   }
+  // Each iteration's surface radiance (which reads only the previous
+  // iteration's dS and the first-order Mie strength) and accumulation (which
+  // nothing reads before the next iteration's ray scatter) run on a side
+  // stream beside point and ray scatter:
+  //   side: surface radiance after everything on the build stream so far
+  //         (so the dE buffer it overwrites is no longer read), then the
+  //         accumulation after this iteration's ray scatter;
+  //   build stream: the next point scatter after this surface radiance (its
+  //         dE), the next ray scatter after this accumulation (it overwrites
+  //         the dS buffer accumulation read), the outputs after the last one.
+  // Entry points that create no streams (the allocation-free build) keep
+  // every stage on the build stream, and so do builds with stage timing on
+  // (each stage's time stays its own and the stages add up to the build) and
+  // builds that export per-iteration tables or states.
+  cudaStream_t ss = g_side_stream[tm.dev];
+  const bool fork = ss != nullptr && !g_timing && !inter && !(hooks && hooks->state);
+  if (!fork) ss = st;
   for (int it = it0; it < d.iterations; it++) {
     tm.iteration = it + 1;
     Vec4<Real>* dE_new = w.dE[it & 1];
     Vec4<Real>* dS_new = w.dS[it & 1];
     Vec4<Real>* E_new = w.Eacc[it & 1];
     Vec4<Real>* S_new = w.Sacc[it & 1];
-    // surface radiance reads only the previous iteration's dS (and the
-    // first-order Mie strength): it runs on the side stream beside point and
-    // ray scatter, forked after everything before this iteration (so the dE
-    // buffer it overwrites is no longer read) and joined before accumulation.
-    // Entry points that create no streams (the allocation-free build) keep it
-    // on the build stream, and so do builds with stage timing on, so that
-    // each stage's time is its own and the stages add up to the build.
-    cudaStream_t ss = g_side_stream[tm.dev];
-    const bool fork = ss != nullptr && !g_timing;
     if (fork) {
+      if (it > it0) CUDA_TRY(cudaStreamWaitEvent(st, g_side_sr[tm.dev], 0));  // dE of the last iteration
       CUDA_TRY(cudaEventRecord(g_side_fork[tm.dev], st));
       CUDA_TRY(cudaStreamWaitEvent(ss, g_side_fork[tm.dev], 0));
-    } else {
-      ss = st;
     }
     tm.mark_begin(6, ss);
     launch_surface_radiance<Real>(w.params, d, w.setup.erow, w.setup.hdir, dS_prev, M_first, dE_new, ss);
     launches++;
     tm.mark_end(ss);
-    if (fork) CUDA_TRY(cudaEventRecord(g_side_join[tm.dev], ss));
+    if (fork) CUDA_TRY(cudaEventRecord(g_side_sr[tm.dev], ss));
     tm.mark_begin(5);
     if (launch_point_scatter<Real>(w.params, d, w.setup.rowinfo, w.setup.pdirs, w.setup.dimage, w.setup.pcount,
                                    w.setup.prow,
@@ -628,18 +635,23 @@ int run_build(const Work<Real>& w, const BuildDims& d, float* oT, float* oE, flo
       launches++;
     }
 
+    if (fork && it > it0) CUDA_TRY(cudaStreamWaitEvent(st, g_side_acc[tm.dev], 0));  // its dS buffer read
     tm.mark_begin(7);
     if (launch_ray_scatter<Real>(w.params, d, w.setup.rowinfo, w.setup.rows, w.setup.geom, w.setup.remapS, w.J,
                                  dS_new, st))
       return fail(SFSIM_ATMO_ECUDA, "ray scatter launch configuration failed");
     launches++;
     tm.mark_end();
-    if (fork) CUDA_TRY(cudaStreamWaitEvent(st, g_side_join[tm.dev], 0));
-    tm.mark_begin(8);
-    launch_accumulate2<Real>(d.B, d.nE0, d.nE1, w.setup.remapE, E_prev, dE_new, E_new, st);
-    launch_accumulate4<Real>(d, w.setup.remapS, S_prev, dS_new, S_new, st);
+    if (fork) {
+      CUDA_TRY(cudaEventRecord(g_side_rs[tm.dev], st));
+      CUDA_TRY(cudaStreamWaitEvent(ss, g_side_rs[tm.dev], 0));
+    }
+    tm.mark_begin(8, ss);
+    launch_accumulate2<Real>(d.B, d.nE0, d.nE1, w.setup.remapE, E_prev, dE_new, E_new, ss);
+    launch_accumulate4<Real>(d, w.setup.remapS, S_prev, dS_new, S_new, ss);
     launches += 2;
-    tm.mark_end();
+    tm.mark_end(ss);
+    if (fork) CUDA_TRY(cudaEventRecord(g_side_acc[tm.dev], ss));
     CUDA_TRY(cudaGetLastError());
     if (inter) {
       if (inter->point_scatter)
@@ -668,6 +680,7 @@ int run_build(const Work<Real>& w, const BuildDims& d, float* oT, float* oE, flo
     }
   }
   tm.iteration = 0;
+  if (fork && d.iterations > it0) CUDA_TRY(cudaStreamWaitEvent(st, g_side_acc[tm.dev], 0));  // the final S and E
   tm.mark_begin(9);
   launch_output2<Real>(d.B, d.nE0, d.nE1, w.setup.remapE, E_prev, oE, st);
   launch_output4<Real>(d, w.setup.remapS, S_prev, oS, st);
