@@ -351,7 +351,8 @@ cudaEvent_t g_early_done[kMaxDevices];
 // each iteration's surface radiance and accumulation run on a side stream
 // beside point and ray scatter (run_build)
 cudaStream_t g_side_stream[kMaxDevices];
-cudaEvent_t g_side_fork[kMaxDevices], g_side_sr[kMaxDevices], g_side_rs[kMaxDevices], g_side_acc[kMaxDevices];
+cudaEvent_t g_side_fork[kMaxDevices], g_side_sr[kMaxDevices], g_side_rs[kMaxDevices], g_side_acc[kMaxDevices],
+    g_side_setup[kMaxDevices];
 
 struct Carver {
   char* base;
@@ -467,7 +468,7 @@ int ensure_stream(int dev) {
     CUDA_TRY(cudaEventCreateWithFlags(&g_early_done[dev], cudaEventDisableTiming));
     CUDA_TRY(cudaStreamCreateWithFlags(&g_stream[dev], cudaStreamNonBlocking));
     CUDA_TRY(cudaStreamCreateWithFlags(&g_side_stream[dev], cudaStreamNonBlocking));
-    for (cudaEvent_t* e : {&g_side_fork[dev], &g_side_sr[dev], &g_side_rs[dev], &g_side_acc[dev]})
+    for (cudaEvent_t* e : {&g_side_fork[dev], &g_side_sr[dev], &g_side_rs[dev], &g_side_acc[dev], &g_side_setup[dev]})
       CUDA_TRY(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
     for (int i = 0; i < 2 * 512; i++) CUDA_TRY(cudaEventCreate(&g_events[dev][i]));
   }
@@ -485,6 +486,7 @@ struct Timer {
   int stage_of[512];
   int iteration = 0;  // iteration of the stages that follow (1-based); 0 outside the loop
   int open = 0;   // NVTX ranges pushed and not yet popped
+  bool side = true;  // stages may run on the device's side stream
   void mark_begin(int stage, cudaStream_t on = nullptr) {
     char name[64];
     if (iteration > 0)
@@ -527,20 +529,43 @@ int run_build(const Work<Real>& w, const BuildDims& d, float* oT, float* oE, flo
               Timer& tm, const sfsim_atmo_intermediates* inter, Vec4<float>* jsum = nullptr,
               cudaEvent_t early_done = nullptr, const IterationHooks* hooks = nullptr) {
   int launches = 0;
+  // Only the view-row chain (row info, point rows, remap4, view rows) stands
+  // between the parameters and the first order; the sun table, the other
+  // set-up tables, the transmittance nodes and E0 run beside it on the side
+  // stream, which the first order waits for.  Builds with stage timing on
+  // and entry points without a side stream keep them on the build stream.
+  cudaStream_t ss = tm.side ? g_side_stream[tm.dev] : nullptr;
+  const bool setup_fork = ss != nullptr && !g_timing;
+  cudaStream_t sa = setup_fork ? ss : st;
+  if (setup_fork) {
+    CUDA_TRY(cudaEventRecord(g_side_fork[tm.dev], st));
+    CUDA_TRY(cudaStreamWaitEvent(ss, g_side_fork[tm.dev], 0));
+    if (w.sun) {
+      tm.mark_begin(3, ss);
+      launch_sun_table(w.params, d, w.sun, ss);
+      launches++;
+      tm.mark_end(ss);
+    }
+  }
   tm.mark_begin(0);
-  launch_setup<Real>(w.params, d, w.dirs, w.hdirs, w.setup, st);
+  launch_setup_rows<Real>(w.params, d, w.setup, st);
+  launch_setup_aux<Real>(w.params, d, w.dirs, w.hdirs, w.setup, sa);
   launches += 10;
   tm.mark_end();
-  tm.mark_begin(1);
-  launch_transmittance<Real>(w.params, d, w.T, st);
+  tm.mark_begin(1, sa);
+  launch_transmittance<Real>(w.params, d, w.T, sa);
   launches++;
-  tm.mark_end();
-  tm.mark_begin(2);
-  launch_surface_base<Real>(w.params, d, w.E0, st);
+  tm.mark_end(sa);
+  tm.mark_begin(2, sa);
+  launch_surface_base<Real>(w.params, d, w.E0, sa);
   launches++;
-  tm.mark_end();
+  tm.mark_end(sa);
+  if (setup_fork) {
+    CUDA_TRY(cudaEventRecord(g_side_setup[tm.dev], ss));
+    CUDA_TRY(cudaStreamWaitEvent(st, g_side_setup[tm.dev], 0));
+  }
   tm.mark_begin(3);
-  if (w.sun) {
+  if (w.sun && !setup_fork) {
     launch_sun_table(w.params, d, w.sun, st);
     launches++;
   }
@@ -604,8 +629,7 @@ int run_build(const Work<Real>& w, const BuildDims& d, float* oT, float* oE, flo
   // every stage on the build stream, and so do builds with stage timing on
   // (each stage's time stays its own and the stages add up to the build) and
   // builds that export per-iteration tables or states.
-  cudaStream_t ss = g_side_stream[tm.dev];
-  const bool fork = ss != nullptr && !g_timing && !inter && !(hooks && hooks->state);
+  const bool fork = setup_fork && !inter && !(hooks && hooks->state);
   if (!fork) ss = st;
   for (int it = it0; it < d.iterations; it++) {
     tm.iteration = it + 1;
@@ -1559,6 +1583,7 @@ int build_static_impl(const sfsim_atmo_config& cfg, float* T, float* E, float* S
   tm.dev = dev;
   tm.st = st;
   tm.n = 512;  // a full event list: this entry point records no stage timings
+  tm.side = false;  // and uses no stream but the caller's
   g_have_timings = 0;  // so sfsim_atmo_last_timings reports none for this build
   return run_build<Real>(w, d, T, E, S, M, st, tm, nullptr);
 }

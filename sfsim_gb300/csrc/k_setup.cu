@@ -441,20 +441,32 @@ __global__ void k_half_dirs(const AtmoParams* params, BuildDims d, const DirLoca
 static inline dim3 grid1(long long n, int block, int B) { return dim3((unsigned)((n + block - 1) / block), B); }
 
 template <class Real>
-void launch_setup(const AtmoParams* params, const BuildDims& d, const DirLocal* dirs,
-                  const DirLocal* half_dirs, const SetupBuffers<Real>& o, cudaStream_t st) {
+void launch_setup_rows(const AtmoParams* params, const BuildDims& d, const SetupBuffers<Real>& o, cudaStream_t st) {
   const int blk = 128;
   k_row_info<Real><<<grid1(d.rows(), blk, d.B), blk, 0, st>>>(params, d, o.rowinfo, o.rowmap);
   k_point_rows<Real><<<grid1((long long)d.n0 * d.n2, blk, d.B), blk, 0, st>>>(params, d, o.prow);
   k_remap4<Real><<<grid1(d.n4(), blk, d.B), blk, 0, st>>>(params, d, o.rowinfo, o.rowmap, o.prow, o.remapS,
                                                             o.geom);
+  k_view_rows<Real><<<grid1(d.rows() * d.S, blk, d.B), blk, 0, st>>>(params, d, o.rowinfo, o.rows);
+}
+
+template <class Real>
+void launch_setup_aux(const AtmoParams* params, const BuildDims& d, const DirLocal* dirs,
+                      const DirLocal* half_dirs, const SetupBuffers<Real>& o, cudaStream_t st) {
+  const int blk = 128;
   k_remapT<Real><<<grid1(d.nT(), blk, d.B), blk, 0, st>>>(params, d, o.remapT);
   k_remapE<Real><<<grid1(d.nE(), blk, d.B), blk, 0, st>>>(params, d, o.remapE);
-  k_view_rows<Real><<<grid1(d.rows() * d.S, blk, d.B), blk, 0, st>>>(params, d, o.rowinfo, o.rows);
   k_sphere_setup<Real><<<grid1((long long)d.n0 * d.P, blk, d.B), blk, 0, st>>>(params, d, dirs, o.sdirs);
   k_sphere_partition<Real><<<dim3(d.n0, d.B), 32, 0, st>>>(d, o.sdirs, o.pdirs, o.pcount, o.dimage);
   k_surface_rows<Real><<<grid1(d.nE(), blk, d.B), blk, 0, st>>>(params, d, o.erow);
   k_half_dirs<Real><<<grid1((long long)d.nE0 * d.Ph, blk, d.B), blk, 0, st>>>(params, d, half_dirs, o.hdir);
+}
+
+template <class Real>
+void launch_setup(const AtmoParams* params, const BuildDims& d, const DirLocal* dirs,
+                  const DirLocal* half_dirs, const SetupBuffers<Real>& o, cudaStream_t st) {
+  launch_setup_rows<Real>(params, d, o, st);
+  launch_setup_aux<Real>(params, d, dirs, half_dirs, o, st);
 }
 
 template <class Real>
@@ -469,6 +481,14 @@ void launch_surface_base(const AtmoParams* params, const BuildDims& d, Vec4<Real
   k_surface_base<Real><<<grid1(d.nE(), blk, d.B), blk, 0, st>>>(params, d, E0);
 }
 
+template void launch_setup_rows<float>(const AtmoParams*, const BuildDims&, const SetupBuffers<float>&,
+                                       cudaStream_t);
+template void launch_setup_rows<double>(const AtmoParams*, const BuildDims&, const SetupBuffers<double>&,
+                                        cudaStream_t);
+template void launch_setup_aux<float>(const AtmoParams*, const BuildDims&, const DirLocal*, const DirLocal*,
+                                      const SetupBuffers<float>&, cudaStream_t);
+template void launch_setup_aux<double>(const AtmoParams*, const BuildDims&, const DirLocal*, const DirLocal*,
+                                       const SetupBuffers<double>&, cudaStream_t);
 template void launch_setup<float>(const AtmoParams*, const BuildDims&, const DirLocal*, const DirLocal*,
                                   const SetupBuffers<float>&, cudaStream_t);
 template void launch_setup<double>(const AtmoParams*, const BuildDims&, const DirLocal*, const DirLocal*,

@@ -54,6 +54,15 @@ __host__ __device__ inline long long heading_rows_stride(const BuildDims& d) {
   return 2LL * ((dir_row(d.P) + 7) / 8 * 8) * (d.n3 + 2) * 3;
 }
 
+// The set-up tables in two independent parts: the view-row chain the first
+// order reads (row info, point rows, remap4 with its geometry, view rows)
+// and the rest (remapT, remapE, sphere directions and their partition,
+// surface rows, half directions).  launch_setup runs both on one stream.
+template <class Real>
+void launch_setup_rows(const AtmoParams* params, const BuildDims& d, const SetupBuffers<Real>& o, cudaStream_t st);
+template <class Real>
+void launch_setup_aux(const AtmoParams* params, const BuildDims& d, const DirLocal* dirs,
+                      const DirLocal* half_dirs, const SetupBuffers<Real>& o, cudaStream_t st);
 template <class Real>
 void launch_setup(const AtmoParams* params, const BuildDims& d, const DirLocal* dirs,
                   const DirLocal* half_dirs, const SetupBuffers<Real>& o, cudaStream_t st);
