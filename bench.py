@@ -249,8 +249,10 @@ def run_ours(args):
 
     # --- per-table error of the production tables against the FP64 path of
     # the same kernels (outside the timed regions)
-    err_fp64 = table_errors({k: t.numpy() for k, t in zip(TABLES, host_out)},
-                            A.build(C.production(precision=C.FP64)))
+    fp64_tables = A.build(C.production(precision=C.FP64))
+    err_fp64 = table_errors({k: t.numpy() for k, t in zip(TABLES, host_out)}, fp64_tables)
+    scan_rays = run_scan_rays(A, C, fp64_tables, stages["setup"]) if args.extras else None
+    del fp64_tables
 
     # --- rooflines: point scatter (the largest stage, shared-memory gathers)
     # and the first order (SFU exponentials)
@@ -349,6 +351,7 @@ def run_ours(args):
             "err_vs_fp64": {"tables": err_fp64, "against": ("the FP64 production build of the same kernels "
                                                             "(every cell)")},
             "err_vs_oracle": err_oracle,
+            "scan_rays": scan_rays,
             "cpu_baseline": cpu,
             "sweep": sweep,
             "queries": queries,
@@ -398,6 +401,43 @@ def run_sweep(L, A, C):
     return {"atmospheres": len(cfgs), "shape": list(cfgs[0].ray_scatter_shape), "iterations": cfgs[0].iterations,
             "device_s": dev_ms * 1e-3, "e2e_s": wall, "cells_per_s": len(cfgs) * n4 / (dev_ms * 1e-3),
             "err_vs_fp64": err}
+
+
+def run_scan_rays(A, C, fp64_tables, nested_setup_ms, reps=10):
+    """The production build with the SCAN_RAYS flag (view-ray transmittances
+    by one prefix scan per ray instead of the nested quadrature, a different
+    discretisation): device time per build (CUDA events, L2 flushed between
+    builds), its set-up stage beside the nested build's, and its per-table
+    deviation from the FP64 nested production tables."""
+    import torch
+    cfg = C.production()
+    cfg.flags = C.SCAN_RAYS
+    dev = [torch.empty(s, dtype=torch.float32, device="cuda") for s in A.table_shapes(cfg)]
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
+    for _ in range(3):
+        A.build_device(cfg, dev)
+    torch.cuda.synchronize()
+    ms = []
+    for _ in range(reps):
+        flush.add_(1.0)
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s.record()
+        A.build_device(cfg, dev)
+        e.record()
+        torch.cuda.synchronize()
+        ms.append(s.elapsed_time(e))
+    read = A.stage_timings(True)
+    flush.add_(1.0)
+    A.build_device(cfg, dev)
+    torch.cuda.synchronize()
+    setup_ms = read()["setup"]
+    A.stage_timings(False)
+    err = table_errors(A.build(cfg), fp64_tables)
+    return {"ms_per_build": statistics.median(ms), "setup_ms": setup_ms, "nested_setup_ms": nested_setup_ms,
+            "err_vs_nested_fp64": err,
+            "note": ("not the reference's algorithm: T(x, p_s) from the midpoint rule on the whole cells before "
+                     "p_s plus the half cell up to it, one warp-shuffle scan per view ray; the transmittance "
+                     "table does not depend on it")}
 
 
 def run_reference_production(A, C, reps=10):

@@ -52,6 +52,20 @@ extern "C" {
 #define SFSIM_ATMO_FP32 0
 #define SFSIM_ATMO_FP64 1
 
+/* Bits of sfsim_atmo_config.flags (0: the reference's algorithm).
+ *
+ * SFSIM_ATMO_SCAN_RAYS: the transmittance from a table node x to each
+ *   midpoint sample p_s of its view ray comes from one prefix scan over the
+ *   ray's S cells (O(S) per ray) instead of the reference's nested quadrature
+ *   (S midpoint samples between x and every p_s, O(S^2) per ray;
+ *   atmosphere.clj:192-200 with ray.clj:19-30).  The optical depth to p_s is
+ *   the midpoint rule on the whole cells before p_s plus the half cell up to
+ *   it, sampled at its own midpoint.  A different discretisation: the ray
+ *   scatter, Mie strength and surface radiance tables deviate from the
+ *   reference's by up to about 1e-2 (relative) at 128 ray steps.  The
+ *   transmittance table does not change. */
+#define SFSIM_ATMO_SCAN_RAYS 1
+
 /* One scattering component; mirrors the malli schema `scatter` at
  * src/clj/sfsim/atmosphere.clj:35-39.  A component without
  * ::scatter-quotient uses 1.0, one without ::scatter-g uses 0.0. */
@@ -77,7 +91,7 @@ typedef struct sfsim_atmo_config {
   int sphere_steps;         /* point-scatter sphere steps (theta rings = steps/2) */
   int iterations;           /* multiple-scattering iterations after the first order */
   int precision;            /* SFSIM_ATMO_FP32 or SFSIM_ATMO_FP64 */
-  int flags;                /* reserved, must be 0 */
+  int flags;                /* SFSIM_ATMO_* flag bits; 0 follows the reference */
 } sfsim_atmo_config;
 
 /* Fills `cfg` with the reference's production values

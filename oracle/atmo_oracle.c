@@ -316,6 +316,30 @@ static v3 ray_scatter(const planet_t* p, const comp_t* comps, int ncomp, int ste
   return integral_ray(x, sub(point, x), steps, 1.0, ray_scatter_integrand, &c);
 }
 
+/* The build's SFSIM_ATMO_SCAN_RAYS variant (not the reference's algorithm;
+ * the check of the GPU's scan mode): the same midpoint samples p_n of the
+ * view ray, with T(x, p_n) from the optical depth of the whole cells before
+ * p_n (one extinction sample at each cell midpoint, which is p_m) plus the
+ * half cell up to p_n sampled at its own midpoint, accumulated along the
+ * ray instead of integrated anew for every p_n. */
+static v3 ray_scatter_scan(const planet_t* p, const comp_t* comps, int ncomp, int steps, fn4_t J, const void* Jctx,
+                           v3 x, v3 view, v3 light, int above) {
+  v3 point = above ? atmosphere_intersection(p, x, view) : surface_intersection(p, x, view);
+  v3 D = sub(point, x);
+  ext_ctx e = {p, comps, ncomp};
+  double stepsize = 1.0 / steps;
+  double a = stepsize * mag(D);
+  v3 depth = ZERO, acc = ZERO;
+  for (int n = 0; n < steps; n++) {
+    v3 pn = add(x, mult(D, (0.5 + n) * stepsize));
+    v3 ph = add(x, mult(D, (0.25 + n) * stepsize));
+    v3 tau = add(depth, mult(overall_extinction(&e, ph), 0.5 * a));
+    acc = add(acc, mult(emult(vexp(neg(tau)), J(Jctx, pn, view, light, above)), a));
+    depth = add(depth, mult(overall_extinction(&e, pn), a));
+  }
+  return acc;
+}
+
 /* ------------------------------------------------------------------------ */
 /* sphere.clj:62-105 integrate-circle, spherical-integral; matrix.clj:207,   */
 /* quaternion.clj:166 oriented-matrix / orthogonal                           */
@@ -698,6 +722,7 @@ typedef struct {
   v3 intensity;
   int tshape[2], eshape[2], sshape[4];
   int ray_steps, sphere_steps, iterations;
+  int scan_rays;     /* SFSIM_ATMO_SCAN_RAYS */
 } build_t;
 
 static void build_from_config(const sfsim_atmo_config* cfg, build_t* b) {
@@ -720,6 +745,7 @@ static void build_from_config(const sfsim_atmo_config* cfg, build_t* b) {
   b->ray_steps = cfg->ray_steps;
   b->sphere_steps = cfg->sphere_steps;
   b->iterations = cfg->iterations;
+  b->scan_rays = (cfg->flags & SFSIM_ATMO_SCAN_RAYS) != 0;
 }
 
 /* Node functions for make-lookup-table */
@@ -750,7 +776,8 @@ static void node_ray_scatter(const void* vctx, const int* idx, double* out) {
   v3 point, dir, light;
   int above;
   ray_scatter_backward(&b->planet, b->sshape, di, &point, &dir, &light, &above);
-  vstore(out, ray_scatter(&b->planet, b->comps, 2, b->ray_steps, c->J, c->Jctx, point, dir, light, above));
+  vstore(out, (b->scan_rays ? ray_scatter_scan : ray_scatter)(&b->planet, b->comps, 2, b->ray_steps, c->J, c->Jctx,
+                                                               point, dir, light, above));
 }
 
 typedef struct { const build_t* b; fn4_t dS; const void* dSctx; fn2_t dE; const void* dEctx; } ps_node_ctx;
@@ -1180,6 +1207,16 @@ void oracle_ray_scatter_const(const oracle_planet* p, const oracle_component* co
   for (int i = 0; i < ncomp && i < 2; i++) cc[i] = comp_from(&comps[i]);
   const_ctx c = {vload(J)};
   vstore(out, ray_scatter(&pp, cc, ncomp, steps, const4, &c, vload(x), vload(v), vload(l), above));
+}
+
+void oracle_ray_scatter_scan_const(const oracle_planet* p, const oracle_component* comps, int ncomp, int steps,
+                                   const double* J, const double* x, const double* v, const double* l, int above,
+                                   double* out) {
+  planet_t pp = planet_from(p);
+  comp_t cc[2];
+  for (int i = 0; i < ncomp && i < 2; i++) cc[i] = comp_from(&comps[i]);
+  const_ctx c = {vload(J)};
+  vstore(out, ray_scatter_scan(&pp, cc, ncomp, steps, const4, &c, vload(x), vload(v), vload(l), above));
 }
 
 void oracle_point_scatter_const(const oracle_planet* p, const oracle_component* comps, int ncomp,

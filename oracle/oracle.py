@@ -200,6 +200,14 @@ def ray_scatter_const(p, cs, steps, J, x, v, l, above):
     return np.array(o[:])
 
 
+def ray_scatter_scan_const(p, cs, steps, J, x, v, l, above):
+    """ray_scatter_const with the scan-mode transmittances (SCAN_RAYS)."""
+    o = _out3()
+    lib().oracle_ray_scatter_scan_const(ctypes.byref(p), cs, len(cs), steps, _v(J), _v(x), _v(v), _v(l), int(above),
+                                        o)
+    return np.array(o[:])
+
+
 def point_scatter_const(p, cs, dS, dE, sphere_steps, ray_steps, x, v, l):
     o = _out3()
     lib().oracle_point_scatter_const(ctypes.byref(p), cs, len(cs), _v(dS), _v(dE), sphere_steps, ray_steps, _v(x),

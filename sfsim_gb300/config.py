@@ -31,6 +31,9 @@ import numpy as np
 FP32 = 0
 FP64 = 1
 
+# flag bits of AtmoConfig.flags (sfsim_atmo.h SFSIM_ATMO_*); 0 follows the reference
+SCAN_RAYS = 1  # view-ray transmittances by one prefix scan per ray, not the nested quadrature
+
 
 class Component(ctypes.Structure):
     """sfsim_atmo_component; mirrors the `scatter` schema, atmosphere.clj:35-39."""
@@ -115,7 +118,7 @@ def rayleigh_component() -> Component:
 def make_config(radius=6378000.0, height=35000.0, brightness=(0.3, 0.3, 0.3), intensity=(1.0, 1.0, 1.0),
                 mie=None, rayleigh=None, transmittance_shape=(64, 255), surface_radiance_shape=(16, 63),
                 ray_scatter_shape=(32, 127, 32, 8), ray_steps=100, sphere_steps=15, iterations=5,
-                precision=FP32) -> AtmoConfig:
+                precision=FP32, flags=0) -> AtmoConfig:
     c = AtmoConfig()
     c.radius = float(radius)
     c.height = float(height)
@@ -133,7 +136,7 @@ def make_config(radius=6378000.0, height=35000.0, brightness=(0.3, 0.3, 0.3), in
     c.sphere_steps = int(sphere_steps)
     c.iterations = int(iterations)
     c.precision = int(precision)
-    c.flags = 0
+    c.flags = int(flags)
     return c
 
 

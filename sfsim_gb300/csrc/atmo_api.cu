@@ -89,7 +89,7 @@ int validate(const sfsim_atmo_config* c) {
     return fail(SFSIM_ATMO_EINVAL, "ray_steps must be at least 4 (surface radiance uses ray_steps/4 rings)");
   if (c->precision != SFSIM_ATMO_FP32 && c->precision != SFSIM_ATMO_FP64)
     return fail(SFSIM_ATMO_EINVAL, "precision must be SFSIM_ATMO_FP32 or SFSIM_ATMO_FP64");
-  if (c->flags != 0) return fail(SFSIM_ATMO_EINVAL, "flags must be 0");
+  if (c->flags & ~SFSIM_ATMO_SCAN_RAYS) return fail(SFSIM_ATMO_EINVAL, "flags has an unknown bit");
   long long n4 = 1;
   for (int i = 0; i < 4; i++) n4 *= c->ray_scatter_shape[i];
   if (n4 > (1LL << 31)) return fail(SFSIM_ATMO_ETOOBIG, "ray-scatter table exceeds 2^31 nodes");
@@ -101,7 +101,7 @@ bool same_layout(const sfsim_atmo_config& a, const sfsim_atmo_config& b) {
          memcmp(a.surface_radiance_shape, b.surface_radiance_shape, sizeof(a.surface_radiance_shape)) == 0 &&
          memcmp(a.ray_scatter_shape, b.ray_scatter_shape, sizeof(a.ray_scatter_shape)) == 0 &&
          a.ray_steps == b.ray_steps && a.sphere_steps == b.sphere_steps && a.iterations == b.iterations &&
-         a.precision == b.precision;
+         a.precision == b.precision && a.flags == b.flags;
 }
 
 // Directions of spherical-integral (sphere.clj:62-93): theta rings at
@@ -310,6 +310,7 @@ BuildDims make_dims(const sfsim_atmo_config& c, int B) {
   d.S = c.ray_steps;
   d.sphere_steps = c.sphere_steps;
   d.iterations = c.iterations;
+  d.scan_rays = (c.flags & SFSIM_ATMO_SCAN_RAYS) ? 1 : 0;
   std::vector<DirLocal> v;
   sphere_directions(c.sphere_steps >> 1, c.sphere_steps, M_PI, v);
   d.P = (int)v.size();
@@ -831,7 +832,7 @@ int dispatch(const sfsim_atmo_config* cfgs, int B, float* T, float* E, float* S,
     int rc = validate(&cfgs[b]);
     if (rc) return rc;
     if (!same_layout(cfgs[0], cfgs[b]))
-      return fail(SFSIM_ATMO_EINVAL, "batched configs must share shapes, steps, iterations and precision");
+      return fail(SFSIM_ATMO_EINVAL, "batched configs must share shapes, steps, iterations, precision and flags");
   }
   std::lock_guard<std::mutex> lock(g_mutex);
   if (cfgs[0].precision == SFSIM_ATMO_FP64) return build_impl<double>(cfgs, B, T, E, S, M, host_out, st, inter);

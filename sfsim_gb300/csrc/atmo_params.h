@@ -72,6 +72,7 @@ struct BuildDims {
   int P;                   // directions of integral-sphere(sphere_steps)
   int Ph;                  // directions of integral-half-sphere(ray_steps)
   int iterations;
+  int scan_rays;           // view-ray transmittances by prefix scan (SFSIM_ATMO_SCAN_RAYS)
   // (size - 1) / (1 - exp(-3.6)) of the sun-elevation axes of the ray-scatter
   // space (n2) and of the surface-radiance space (nE1)
   double sun_scale, sun_scale_E;

@@ -196,16 +196,9 @@ __global__ void k_surface_base(const AtmoParams* params, BuildDims d, Vec4<Real>
 // One thread per (row, sample).
 // ---------------------------------------------------------------------------
 
+// Sample s of a row, everything but the optical depth from the row's node.
 template <class Real>
-__global__ void k_view_rows(const AtmoParams* params, BuildDims d, const RowInfo* info, RowSample<Real>* samples) {
-  const long long nrows = d.rows();
-  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  const int b = blockIdx.y;
-  if (t >= nrows * d.S) return;
-  const AtmoParams& P = params[b];
-  const int s = (int)(t % d.S);
-  const long long row = t / d.S;
-  const RowInfo& ri = info[b * nrows + row];
+__device__ inline RowSample<Real> view_sample(const AtmoParams& P, const BuildDims& d, const RowInfo& ri, int s) {
   const int above = ri.above;
   const d3 x = mk3(ri.r, 0, 0), v = mk3(ri.sv, ri.cv, 0);
   const d3 D = mk3(ri.D[0], ri.D[1], ri.D[2]);
@@ -216,9 +209,6 @@ __global__ void k_view_rows(const AtmoParams* params, BuildDims d, const RowInfo
   double pr = mag3(p);
   double h = pr - P.R;
   RowSample<Real> o;
-  // T(x, p_s): the segment x -> p_s is the row's segment D scaled by su
-  const double c0 = dmul(dsub(ri.r, P.R), dadd(ri.r, P.R));
-  segment_depth_q<Real>(P, c0, su * (ri.r * D.x), su * su * dot3(D, D), su * ri.L, d.S, o.tau);
   if (std::is_same<Real, float>::value) {
     // the densities exp(-h/H) as the FP32 integrands form them
     o.er = (Real)Bulk<float>::exp2((float)h * P.f_kr);
@@ -233,7 +223,95 @@ __global__ void k_view_rows(const AtmoParams* params, BuildDims d, const RowInfo
   split_coord<Real>(height_to_index(P, d.n0, pr), d.n0, &o.u0, &o.s0);
   split_coord<Real>(elevation_to_index(P, d.n1, p, v, above), d.n1, &o.u1, &o.s1);
   o.pad = 0;
+  return o;
+}
+
+template <class Real>
+__global__ void k_view_rows(const AtmoParams* params, BuildDims d, const RowInfo* info, RowSample<Real>* samples) {
+  const long long nrows = d.rows();
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  const int b = blockIdx.y;
+  if (t >= nrows * d.S) return;
+  const AtmoParams& P = params[b];
+  const int s = (int)(t % d.S);
+  const long long row = t / d.S;
+  const RowInfo& ri = info[b * nrows + row];
+  RowSample<Real> o = view_sample<Real>(P, d, ri, s);
+  // T(x, p_s): the segment x -> p_s is the row's segment D scaled by su
+  const double su = (0.5 + s) * (1.0 / d.S);
+  const d3 D = mk3(ri.D[0], ri.D[1], ri.D[2]);
+  const double c0 = dmul(dsub(ri.r, P.R), dadd(ri.r, P.R));
+  segment_depth_q<Real>(P, c0, su * (ri.r * D.x), su * su * dot3(D, D), su * ri.L, d.S, o.tau);
   samples[(b * nrows + row) * d.S + s] = o;
+}
+
+// The same samples with the optical depth from the row's node x to each
+// p_s by one prefix scan over the row (SFSIM_ATMO_SCAN_RAYS), instead of S
+// samples between x and every p_s.  With cells [n du, (n + 1) du] of the
+// row parameter u (du = 1/S) and rho_n the density at the midpoint u_n of
+// cell n (the sample points themselves),
+//   tau(x, p_s) = L du (sum_{n<s} rho_n + rho((s + 1/4) du) / 2):
+// the midpoint rule on the whole cells before p_s and on the half cell up
+// to it.  The densities are the integrand of the nested sums: the row's
+// height form q(u) (segment_q_form) in Real.  One warp per row; lane l takes
+// samples l, l + 32, ...; each 32 samples are one shuffle scan, carried on
+// to the next 32.
+template <class Real>
+__global__ void k_view_rows_scan(const AtmoParams* params, BuildDims d, const RowInfo* info,
+                                 RowSample<Real>* samples) {
+  const long long nrows = d.rows();
+  const int lane = threadIdx.x & 31;
+  const long long row = blockIdx.x * (long long)(blockDim.x >> 5) + (threadIdx.x >> 5);
+  const int b = blockIdx.y;
+  if (row >= nrows) return;  // whole warps
+  const AtmoParams& P = params[b];
+  const RowInfo& ri = info[b * nrows + row];
+  const double du = 1.0 / d.S;
+  const double c0 = dmul(dsub(ri.r, P.R), dadd(ri.r, P.R));
+  const d3 D = mk3(ri.D[0], ri.D[1], ri.D[2]);
+  const QForm f = segment_q_form(c0, dmul(ri.r, D.x), dot3(D, D), du);
+  const Real A = (Real)f.A, B = (Real)f.B, C = (Real)f.C, w0 = (Real)f.w0, dur = (Real)du;
+  const Real* hp = Bulk<Real>::hpoly(P);
+  const Real al = Bulk<Real>::alpha(P), be = Bulk<Real>::beta(P), kr = Bulk<Real>::kr(P), km = Bulk<Real>::km(P);
+  const Real Ls = (Real)(ri.L * du);
+  Real carry_r = 0, carry_m = 0;
+  for (int s0 = 0; s0 < d.S; s0 += 32) {
+    const int s = s0 + lane;
+    Real rr = 0, rm = 0, qr = 0, qm = 0;
+    if (s < d.S) {
+      // w of the sample's midpoint (as optical_sums_w forms it) and of the
+      // half cell's midpoint (s + 1/4) du
+      const Real wm = fma(Real(s), dur, w0);
+      const Real wq = fma(Real(s) - Real(0.25), dur, w0);
+      const Real hm = height_from_q<Real, 5>(fma(wm, fma(wm, C, B), A), hp, al, be);
+      const Real hq = height_from_q<Real, 5>(fma(wq, fma(wq, C, B), A), hp, al, be);
+      rr = Bulk<Real>::exp2(hm * kr);
+      rm = Bulk<Real>::exp2(hm * km);
+      qr = Bulk<Real>::exp2(hq * kr);
+      qm = Bulk<Real>::exp2(hq * km);
+    }
+    // inclusive scan over the 32 lanes
+    Real ir = rr, im = rm;
+#pragma unroll
+    for (int k = 1; k < 32; k <<= 1) {
+      const Real ur = __shfl_up_sync(0xffffffffu, ir, k), um = __shfl_up_sync(0xffffffffu, im, k);
+      if (lane >= k) {
+        ir += ur;
+        im += um;
+      }
+    }
+    Real er = __shfl_up_sync(0xffffffffu, ir, 1), em = __shfl_up_sync(0xffffffffu, im, 1);
+    if (lane == 0) er = em = 0;
+    if (s < d.S) {
+      RowSample<Real> o = view_sample<Real>(P, d, ri, s);
+      const Real sr = carry_r + er + Real(0.5) * qr, sm = carry_m + em + Real(0.5) * qm;
+#pragma unroll
+      for (int ch = 0; ch < 3; ch++) o.tau[ch] = Ls * (Bulk<Real>::ray_ext(P, ch) * sr + Bulk<Real>::mie_ext(P, ch) * sm);
+      samples[(b * nrows + row) * d.S + s] = o;
+    }
+    carry_r += __shfl_sync(0xffffffffu, ir, 31);
+    carry_m += __shfl_sync(0xffffffffu, im, 31);
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -447,7 +525,10 @@ void launch_setup_rows(const AtmoParams* params, const BuildDims& d, const Setup
   k_point_rows<Real><<<grid1((long long)d.n0 * d.n2, blk, d.B), blk, 0, st>>>(params, d, o.prow);
   k_remap4<Real><<<grid1(d.n4(), blk, d.B), blk, 0, st>>>(params, d, o.rowinfo, o.rowmap, o.prow, o.remapS,
                                                             o.geom);
-  k_view_rows<Real><<<grid1(d.rows() * d.S, blk, d.B), blk, 0, st>>>(params, d, o.rowinfo, o.rows);
+  if (d.scan_rays)
+    k_view_rows_scan<Real><<<grid1(d.rows(), blk / 32, d.B), blk, 0, st>>>(params, d, o.rowinfo, o.rows);
+  else
+    k_view_rows<Real><<<grid1(d.rows() * d.S, blk, d.B), blk, 0, st>>>(params, d, o.rowinfo, o.rows);
 }
 
 template <class Real>

@@ -52,13 +52,19 @@ def test_table_sizes(lib):
 
 @pytest.mark.parametrize("field,value,code", [
     ("radius", -1.0, -1), ("height", 0.0, -1), ("ray_steps", 0, -1), ("iterations", -1, -1),
-    ("precision", 7, -1), ("flags", 1, -1), ("sphere_steps", 1, -1),
+    ("precision", 7, -1), ("flags", 2, -1), ("flags", -1, -1), ("sphere_steps", 1, -1),
 ])
 def test_validate_rejects(lib, field, value, code):
     c = C.production()
     setattr(c, field, value)
     assert lib.sfsim_atmo_validate(ctypes.byref(c)) == code
     assert lib.sfsim_atmo_last_error()
+
+
+def test_validate_accepts_scan_rays(lib):
+    c = C.production()
+    c.flags = C.SCAN_RAYS
+    assert lib.sfsim_atmo_validate(ctypes.byref(c)) == 0
 
 
 def test_validate_shapes(lib):
