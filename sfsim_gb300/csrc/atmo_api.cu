@@ -311,6 +311,7 @@ BuildDims make_dims(const sfsim_atmo_config& c, int B) {
   d.sphere_steps = c.sphere_steps;
   d.iterations = c.iterations;
   d.scan_rays = (c.flags & SFSIM_ATMO_SCAN_RAYS) ? 1 : 0;
+  d.inv_S = 1.0 / c.ray_steps;
   std::vector<DirLocal> v;
   sphere_directions(c.sphere_steps >> 1, c.sphere_steps, M_PI, v);
   d.P = (int)v.size();
@@ -407,6 +408,7 @@ size_t carve(Work<Real>& w, char* base, const BuildDims& d, bool outputs, bool s
   w.setup.dimage = c.take<unsigned char>(B * d.n0 * dir_image_stride(d, sizeof(Real)));
   w.setup.pcount = c.take<int2>(B * d.n0);
   w.setup.prow = c.take<PointRow<Real>>(B * d.n0 * d.n2);
+  w.setup.hdvs = c.take<double>(d.n3);
   w.setup.erow = c.take<SurfRow<Real>>(B * d.nE());
   w.setup.hdir = c.take<HalfDir<Real>>(B * d.nE0 * (long long)d.Ph);
   w.T = c.take<Vec4<Real>>(B * d.nT());

@@ -72,6 +72,7 @@ struct BuildDims {
   int P;                   // directions of integral-sphere(sphere_steps)
   int Ph;                  // directions of integral-half-sphere(ray_steps)
   int iterations;
+  double inv_S;            // 1 / S, the view rays' step in their parameter
   int scan_rays;           // view-ray transmittances by prefix scan (SFSIM_ATMO_SCAN_RAYS)
   // (size - 1) / (1 - exp(-3.6)) of the sun-elevation axes of the ray-scatter
   // space (n2) and of the surface-radiance space (nE1)
@@ -129,6 +130,10 @@ struct RowInfo {
   double D[3];         // ray segment from x to its extremity
   double L;            // |D|
   double Ls;           // L / ray steps
+  // the height form of the segment x -> x + D about its closest approach
+  // (segment_q_form): qmin = c0 - (x.D)^2 / D.D and t = x.D / D.D (0 when
+  // D.D = 0); a sample segment x -> x + su D has the same qmin and t / su
+  double qmin, t;
   float f_r, f_sv, f_cv, f_D[3], f_Ls;
   int above;           // above-horizon flag of the node
 };
@@ -141,6 +146,7 @@ struct RowInfo {
 template <class Real>
 struct PointRow {
   double ss;  // sin of the sun elevation of index k (index-to-sin-sun-elevation)
+  double cs;  // sqrt(max(0, 1 - ss^2)), the bound of index-to-sun-direction's second component
   int u0, u2;
   Real s0, s2;
   Real bR[3], bM[3];

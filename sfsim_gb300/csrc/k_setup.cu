@@ -39,6 +39,11 @@ __global__ void k_row_info(const AtmoParams* params, BuildDims d, RowInfo* info,
   ri.D[2] = D.z;
   ri.L = mag3(D);
   ri.Ls = ri.L / d.S;
+  {
+    const double c0 = dmul(dsub(r, P.R), dadd(r, P.R)), xD = dmul(r, D.x), DD = dot3(D, D);
+    ri.qmin = DD > 0.0 ? c0 - xD * xD / DD : c0;
+    ri.t = DD > 0.0 ? xD / DD : 0.0;
+  }
   ri.f_r = (float)r;
   ri.f_sv = (float)sv;
   ri.f_cv = (float)cv;
@@ -60,7 +65,8 @@ __global__ void k_row_info(const AtmoParams* params, BuildDims d, RowInfo* info,
 // (i, k) one of k_point_rows, which also holds sin(k).
 template <class Real>
 __global__ void k_remap4(const AtmoParams* params, BuildDims d, const RowInfo* info, const Remap2<Real>* rowmap,
-                         const PointRow<Real>* prow, Remap4<Real>* out, CellGeom<Real>* geom) {
+                         const PointRow<Real>* prow, const double* __restrict__ hdvs, Remap4<Real>* out,
+                         CellGeom<Real>* geom) {
   const long long n4 = d.n4();
   const long long node = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   const int b = blockIdx.y;
@@ -74,7 +80,11 @@ __global__ void k_remap4(const AtmoParams* params, BuildDims d, const RowInfo* i
   const PointRow<Real>& pk = prow[((long long)b * d.n0 + i) * d.n2 + k];
   const double sv = ri.sv, cv = ri.cv;
   const d3 v = mk3(sv, cv, 0);
-  const d3 l = index_to_sun_direction(d.n3, v, pk.ss, (double)a);
+  // index_to_sun_direction(n3, v, ss, a) with its per-heading and
+  // per-sun-elevation terms read from tables (the same operations)
+  const double ss = pk.ss, cs = pk.cs;
+  const double sun_1 = limit_quot(dsub(hdvs[a], dmul(v.x, ss)), v.y, -cs, cs);
+  const d3 l = mk3(ss, sun_1, sqrt(dmax(0.0, dsub(dsub(1.0, sqr(sun_1)), sqr(ss)))));
   Remap4<Real> m;
   m.u[0] = rm.u[0];
   m.s[0] = rm.s[0];
@@ -197,33 +207,77 @@ __global__ void k_surface_base(const AtmoParams* params, BuildDims d, Vec4<Real>
 // ---------------------------------------------------------------------------
 
 // Sample s of a row, everything but the optical depth from the row's node.
+// The sample's coordinates are generic (between nodes), so the FP64 forms
+// are reduced where that moves them by rounding only: the point (r + su D.x,
+// su D.y, su D.z) without adding x's zero components, the atmosphere's
+// horizon distance P.Hh in the height coordinate, and rs = p.v in the
+// elevation coordinate (elevation-to-index forms |p| ((p.v) / |p|)).
 template <class Real>
 __device__ inline RowSample<Real> view_sample(const AtmoParams& P, const BuildDims& d, const RowInfo& ri, int s) {
-  const int above = ri.above;
-  const d3 x = mk3(ri.r, 0, 0), v = mk3(ri.sv, ri.cv, 0);
-  const d3 D = mk3(ri.D[0], ri.D[1], ri.D[2]);
   // sample point as integral-ray forms it (ray.clj:22-24)
-  double stepsize = 1.0 / d.S;
-  double su = (0.5 + s) * stepsize;
-  d3 p = add3(x, mul3(D, su));
-  double pr = mag3(p);
-  double h = pr - P.R;
+  const double su = (0.5 + s) * d.inv_S;
+  const d3 p = mk3(dadd(ri.r, dmul(ri.D[0], su)), dmul(ri.D[1], su), dmul(ri.D[2], su));
+  const double pr = mag3(p);
+  const double h = pr - P.R;
   RowSample<Real> o;
   if (std::is_same<Real, float>::value) {
     // the densities exp(-h/H) as the FP32 integrands form them
     o.er = (Real)Bulk<float>::exp2((float)h * P.f_kr);
     o.em = (Real)Bulk<float>::exp2((float)h * P.f_km);
+    o.inv_r = (Real)__frcp_rn((float)pr);
   } else {
     o.er = (Real)exp(-(h / P.ray_scale));
     o.em = (Real)exp(-(h / P.mie_scale));
+    o.inv_r = (Real)(1.0 / pr);
   }
-  o.q = (Real)((pr - P.R) * (pr + P.R));
+  o.q = (Real)(h * (pr + P.R));
   o.us = (Real)su;
-  o.inv_r = (Real)(1.0 / pr);
-  split_coord<Real>(height_to_index(P, d.n0, pr), d.n0, &o.u0, &o.s0);
-  split_coord<Real>(elevation_to_index(P, d.n1, p, v, above), d.n1, &o.u1, &o.s1);
+  // height-to-index and elevation-to-index (atmosphere.clj:239-253, 273-288)
+  const double rho = horizon_distance(P, pr);
+  split_coord<Real>(dmul((double)(d.n0 - 1), rho / P.Hh), d.n0, &o.u0, &o.s0);
+  const double rs = dadd(dmul(p.x, ri.sv), dmul(p.y, ri.cv));
+  const double Delta = dsub(sqr(rs), sqr(rho));
+  double idx;
+  if (ri.above)
+    idx = dsub(0.5, limit_quot(dsub(rs, sqrt(dmax(0.0, dadd(Delta, P.Hh2)))), dadd(dadd(rho, rho), dmul(2.0, P.Hh)),
+                               -0.5, 0.0));
+  else
+    idx = dadd(0.5, limit_quot(dadd(rs, sqrt(dmax(0.0, Delta))), dadd(rho, rho), -0.5, 0.0));
+  split_coord<Real>(dmul((double)(d.n1 - 1), idx), d.n1, &o.u1, &o.s1);
   o.pad = 0;
   return o;
+}
+
+// T(x, p_s) by the nested midpoint sums over x -> p_s = x + su D (S samples).
+// The segment's height form comes from the row's (qmin and t are the same
+// for every su up to rounding; u* scales as t / su), and its sample step in
+// distance is su L / S.
+template <class Real>
+__device__ inline void view_depth(const AtmoParams& P, const BuildDims& d, const RowInfo& ri, int s, Real tau[3]) {
+  if (!(ri.L > 0.0)) {
+    tau[0] = tau[1] = tau[2] = 0;
+    return;
+  }
+  const double du = d.inv_S, su = (0.5 + s) * du;
+  const double c0 = dmul(dsub(ri.r, P.R), dadd(ri.r, P.R));
+  const double DD = su * su * (ri.D[0] * ri.D[0] + ri.D[1] * ri.D[1] + ri.D[2] * ri.D[2]);
+  QForm f;
+  f.C = DD;
+  if (DD > 0.0 && fabs(ri.qmin) < c0) {
+    f.A = ri.qmin;
+    f.B = 0.0;
+    f.w0 = 0.5 * du + ri.t / su;
+  } else {
+    f.A = c0;
+    f.B = 2.0 * (su * (ri.r * ri.D[0]));
+    f.w0 = 0.5 * du;
+  }
+  Real sr, sm;
+  optical_sums_w<Real, 5>((Real)f.A, (Real)f.B, (Real)f.C, (Real)f.w0, (Real)du, d.S, Bulk<Real>::hpoly(P),
+                          Bulk<Real>::alpha(P), Bulk<Real>::beta(P), Bulk<Real>::kr(P), Bulk<Real>::km(P), sr, sm);
+  const Real a = (Real)(su * ri.Ls);
+#pragma unroll
+  for (int ch = 0; ch < 3; ch++) tau[ch] = a * (Bulk<Real>::ray_ext(P, ch) * sr + Bulk<Real>::mie_ext(P, ch) * sm);
 }
 
 template <class Real>
@@ -237,11 +291,7 @@ __global__ void k_view_rows(const AtmoParams* params, BuildDims d, const RowInfo
   const long long row = t / d.S;
   const RowInfo& ri = info[b * nrows + row];
   RowSample<Real> o = view_sample<Real>(P, d, ri, s);
-  // T(x, p_s): the segment x -> p_s is the row's segment D scaled by su
-  const double su = (0.5 + s) * (1.0 / d.S);
-  const d3 D = mk3(ri.D[0], ri.D[1], ri.D[2]);
-  const double c0 = dmul(dsub(ri.r, P.R), dadd(ri.r, P.R));
-  segment_depth_q<Real>(P, c0, su * (ri.r * D.x), su * su * dot3(D, D), su * ri.L, d.S, o.tau);
+  view_depth<Real>(P, d, ri, s, o.tau);
   samples[(b * nrows + row) * d.S + s] = o;
 }
 
@@ -442,9 +492,14 @@ __global__ void k_sphere_partition(BuildDims d, const SphereDir<Real>* sdirs, Sp
 // sun at elevation k, and beta_c(x) (atmosphere.clj:42-47, 140-151), in FP64
 // once here instead of in every thread of the point-scatter blocks.
 template <class Real>
-__global__ void k_point_rows(const AtmoParams* params, BuildDims d, PointRow<Real>* out) {
+__global__ void k_point_rows(const AtmoParams* params, BuildDims d, PointRow<Real>* out, double* hdvs) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   const int b = blockIdx.y;
+  if (b == 0) {
+    // v.l of heading a as index_to_sun_direction forms it, for every atmosphere
+    const int nt = gridDim.x * blockDim.x;
+    for (int a = t; a < d.n3; a += nt) hdvs[a] = dsub(dmul(2.0, (double)a / (d.n3 - 1)), 1.0);
+  }
   if (t >= d.n0 * d.n2) return;
   const AtmoParams& P = params[b];
   const int i = t / d.n2, k = t % d.n2;
@@ -452,6 +507,7 @@ __global__ void k_point_rows(const AtmoParams* params, BuildDims d, PointRow<Rea
   const double ss = index_to_sin_sun_elevation(d.n2, (double)k);
   PointRow<Real> o;
   o.ss = ss;
+  o.cs = sqrt(dmax(0.0, dsub(1.0, sqr(ss))));
   o.gA = (Real)(r * ss / P.R);
   split_coord<Real>(height_to_index(P, d.n0, r), d.n0, &o.u0, &o.s0);
   split_coord<Real>(sun_elevation_to_index(d.n2, mk3(r, 0, 0), mk3(ss, 0, 0)), d.n2, &o.u2, &o.s2);
@@ -522,9 +578,9 @@ template <class Real>
 void launch_setup_rows(const AtmoParams* params, const BuildDims& d, const SetupBuffers<Real>& o, cudaStream_t st) {
   const int blk = 128;
   k_row_info<Real><<<grid1(d.rows(), blk, d.B), blk, 0, st>>>(params, d, o.rowinfo, o.rowmap);
-  k_point_rows<Real><<<grid1((long long)d.n0 * d.n2, blk, d.B), blk, 0, st>>>(params, d, o.prow);
-  k_remap4<Real><<<grid1(d.n4(), blk, d.B), blk, 0, st>>>(params, d, o.rowinfo, o.rowmap, o.prow, o.remapS,
-                                                            o.geom);
+  k_point_rows<Real><<<grid1((long long)d.n0 * d.n2, blk, d.B), blk, 0, st>>>(params, d, o.prow, o.hdvs);
+  k_remap4<Real><<<grid1(d.n4(), blk, d.B), blk, 0, st>>>(params, d, o.rowinfo, o.rowmap, o.prow, o.hdvs,
+                                                            o.remapS, o.geom);
   if (d.scan_rays)
     k_view_rows_scan<Real><<<grid1(d.rows(), blk / 32, d.B), blk, 0, st>>>(params, d, o.rowinfo, o.rows);
   else

@@ -28,6 +28,7 @@ struct SetupBuffers {
   // directions (dir_image_bytes per height): the fields as arrays, then uE0
   unsigned char* dimage;
   PointRow<Real>* prow;  // [B][n0][n2]
+  double* hdvs;          // [n3]: 2 a / (n3 - 1) - 1, index-to-sun-direction's v.l of heading a
   SurfRow<Real>* erow;   // [B][nE0][nE1]
   HalfDir<Real>* hdir;   // [B][nE0][Ph]
 };
