@@ -330,6 +330,8 @@ int check_smem(const BuildDims& d) {
     return fail(SFSIM_ATMO_ESHAPE, "elevation x heading slab of point scatter exceeds shared memory");
   if (ray_scatter_smem<Real>(d) > kMaxSmem)
     return fail(SFSIM_ATMO_ESHAPE, "sun elevation x heading plane of ray scatter exceeds shared memory");
+  if (first_order_smem<Real>(d) > kMaxSmem)
+    return fail(SFSIM_ATMO_ESHAPE, "the view rows' samples of the first order exceed shared memory");
   return 0;
 }
 
@@ -572,7 +574,8 @@ int run_build(const Work<Real>& w, const BuildDims& d, float* oT, float* oE, flo
     launch_sun_table(w.params, d, w.sun, st);
     launches++;
   }
-  launch_first_order<Real>(w.params, d, w.setup.rowinfo, w.setup.rows, w.setup.geom, w.sun, w.S1R, w.M, st);
+  if (launch_first_order<Real>(w.params, d, w.setup.rowinfo, w.setup.rows, w.setup.geom, w.sun, w.S1R, w.M, st))
+    return fail(SFSIM_ATMO_ECUDA, "first order launch configuration failed");
   launches++;
   tm.mark_end();
   // the transmittance and Mie-strength tables are final here: their outputs

@@ -47,6 +47,13 @@ struct FirstOrderSmem {
   Real er, em, q, us;
 };
 
+template <class Real>
+size_t first_order_smem(const BuildDims& d) {
+  return sizeof(FirstOrderSmem<Real>) * d.S;
+}
+template size_t first_order_smem<float>(const BuildDims&);
+template size_t first_order_smem<double>(const BuildDims&);
+
 // Horizon test of the sun at p_s (atmosphere.clj:95-102, filtered-sun-light
 // :154-160) from b = p_s.l and q = |p_s|^2 - R^2.  Near the boundary FP32
 // inputs cannot decide (b carries ~1 m of rounding), so the test is repeated
@@ -347,20 +354,26 @@ __global__ void __launch_bounds__(WARPS * 32, 4) k_first_order(const AtmoParams*
 }
 
 template <class Real>
-void launch_first_order(const AtmoParams* params, const BuildDims& d, const RowInfo* rowinfo,
-                        const RowSample<Real>* rows, const CellGeom<Real>* geom, const unsigned char* sun_table,
-                        Vec4<Real>* rayleigh, Vec4<Real>* mie, cudaStream_t st) {
+int launch_first_order(const AtmoParams* params, const BuildDims& d, const RowInfo* rowinfo,
+                       const RowSample<Real>* rows, const CellGeom<Real>* geom, const unsigned char* sun_table,
+                       Vec4<Real>* rayleigh, Vec4<Real>* mie, cudaStream_t st) {
   constexpr int WARPS = 8;
-  size_t smem = sizeof(FirstOrderSmem<Real>) * d.S;
+  const size_t smem = first_order_smem<Real>(d);
+  // rows of more than 48 KB of samples (S > 1755 in FP32, > 877 in FP64) need the opt-in
+  if (smem > 48 * 1024 &&
+      cudaFuncSetAttribute(k_first_order<Real, WARPS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+          cudaSuccess)
+    return -1;
   dim3 grid((unsigned)d.rows(), d.B);
   k_first_order<Real, WARPS><<<grid, WARPS * 32, smem, st>>>(params, d, rowinfo, rows, geom, sun_table, rayleigh,
                                                              mie);
+  return 0;
 }
 
-template void launch_first_order<float>(const AtmoParams*, const BuildDims&, const RowInfo*,
+template int launch_first_order<float>(const AtmoParams*, const BuildDims&, const RowInfo*,
                                         const RowSample<float>*, const CellGeom<float>*, const unsigned char*,
                                         Vec4<float>*, Vec4<float>*, cudaStream_t);
-template void launch_first_order<double>(const AtmoParams*, const BuildDims&, const RowInfo*,
+template int launch_first_order<double>(const AtmoParams*, const BuildDims&, const RowInfo*,
                                          const RowSample<double>*, const CellGeom<double>*, const unsigned char*,
                                          Vec4<double>*, Vec4<double>*, cudaStream_t);
 

@@ -74,9 +74,12 @@ void launch_transmittance(const AtmoParams* params, const BuildDims& d, Vec4<Rea
 template <class Real>
 void launch_surface_base(const AtmoParams* params, const BuildDims& d, Vec4<Real>* E0, cudaStream_t st);
 
-// First-order Rayleigh ray scatter and Mie strength (fused).
+// First-order Rayleigh ray scatter and Mie strength (fused); -1 when its
+// shared memory (first_order_smem: the row's samples) cannot be configured.
 template <class Real>
-void launch_first_order(const AtmoParams* params, const BuildDims& d, const RowInfo* rowinfo,
+size_t first_order_smem(const BuildDims& d);
+template <class Real>
+int launch_first_order(const AtmoParams* params, const BuildDims& d, const RowInfo* rowinfo,
                         const RowSample<Real>* rows, const CellGeom<Real>* geom, const unsigned char* sun_table,
                         Vec4<Real>* rayleigh, Vec4<Real>* mie, cudaStream_t st);
 

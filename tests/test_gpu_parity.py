@@ -331,3 +331,35 @@ def test_unsupported_shape_reported():
     assert e.value.code == -5
     ok = A.build(C.small_fp64(precision=C.FP32))
     assert np.isfinite(ok["ray_scatter"]).all()
+
+
+def long_ray_config(ray_steps, precision):
+    return C.make_config(height=100000.0, transmittance_shape=(4, 4), surface_radiance_shape=(2, 4),
+                         ray_scatter_shape=(2, 3, 2, 2), ray_steps=ray_steps, sphere_steps=8, iterations=0,
+                         precision=precision)
+
+
+@pytest.fixture(scope="module")
+def long_ray_oracle():
+    return O.build(long_ray_config(2048, C.FP64))
+
+
+@pytest.mark.parametrize("precision", [C.FP64, C.FP32])
+def test_long_rays_match_oracle(long_ray_oracle, precision):
+    """2048 ray steps: the first order stages 2048 samples per view row, more
+    than the 48 KB of shared memory a launch gets without opting in (FP32
+    57 KB, FP64 115 KB)."""
+    ref = long_ray_oracle
+    gpu = A.build(long_ray_config(2048, precision))
+    for key in ("transmittance", "ray_scatter", "mie_strength"):
+        assert_close(gpu[key], ref[key], TOL[precision], key)
+
+
+def test_longest_rays_build():
+    """The longest rays a configuration may ask for (4096 steps: 229 KB of
+    FP64 samples per view row, within the 227 KiB limit) build in both
+    precisions, and they agree."""
+    d = A.build(long_ray_config(4096, C.FP64))
+    f = A.build(long_ray_config(4096, C.FP32))
+    for key in ("transmittance", "ray_scatter", "mie_strength"):
+        assert_close(f[key], d[key], TOL[C.FP32], key)
