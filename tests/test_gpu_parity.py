@@ -363,3 +363,34 @@ def test_longest_rays_build():
     f = A.build(long_ray_config(4096, C.FP32))
     for key in ("transmittance", "ray_scatter", "mie_strength"):
         assert_close(f[key], d[key], TOL[C.FP32], key)
+
+
+@pytest.mark.parametrize("precision", [C.FP64, C.FP32])
+def test_smallest_tables_match_oracle(precision):
+    """Every dimension at its minimum of 2 nodes, 4 ray steps (the fewest
+    with an iteration: the surface radiance takes ray_steps / 4 rings) and 2
+    sphere steps (2 point-scatter directions, one padded direction block)."""
+    cfg = C.make_config(height=100000.0, transmittance_shape=(2, 2), surface_radiance_shape=(2, 2),
+                        ray_scatter_shape=(2, 2, 2, 2), ray_steps=4, sphere_steps=2, iterations=2,
+                        precision=precision)
+    ref = O.build(C.make_config(height=100000.0, transmittance_shape=(2, 2), surface_radiance_shape=(2, 2),
+                                ray_scatter_shape=(2, 2, 2, 2), ray_steps=4, sphere_steps=2, iterations=2,
+                                precision=C.FP64), intermediates=True)
+    gpu = A.build(cfg, intermediates=True)
+    for it in range(cfg.iterations):
+        for key in ("point_scatter", "surface_delta", "ray_scatter_delta"):
+            assert_close(gpu[key][it], ref[key][it], TOL[precision], f"{key}[{it}]")
+    for key in ("transmittance", "surface_radiance", "ray_scatter", "mie_strength"):
+        assert_close(gpu[key], ref[key], TOL[precision], key)
+
+
+@pytest.mark.parametrize("precision", [C.FP64, C.FP32])
+def test_single_ray_step_first_order(precision):
+    """One ray step and no iterations: each ray is a single midpoint sample."""
+    mk = lambda p: C.make_config(height=100000.0, transmittance_shape=(3, 5), surface_radiance_shape=(2, 3),
+                                 ray_scatter_shape=(3, 4, 3, 2), ray_steps=1, sphere_steps=4, iterations=0,
+                                 precision=p)
+    ref = O.build(mk(C.FP64))
+    gpu = A.build(mk(precision))
+    for key in ("transmittance", "surface_radiance", "ray_scatter", "mie_strength"):
+        assert_close(gpu[key], ref[key], TOL[precision], key)
