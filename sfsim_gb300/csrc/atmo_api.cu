@@ -83,8 +83,10 @@ int validate(const sfsim_atmo_config* c) {
     if (c->ray_scatter_shape[i] < 2) return fail(SFSIM_ATMO_ESHAPE, "every table dimension needs at least 2 nodes");
   if (c->ray_steps < 1 || c->ray_steps > 4096) return fail(SFSIM_ATMO_EINVAL, "ray_steps must be in [1, 4096]");
   if (c->iterations < 0 || c->iterations > 64) return fail(SFSIM_ATMO_EINVAL, "iterations must be in [0, 64]");
-  if (c->iterations > 0 && (c->sphere_steps < 2 || c->sphere_steps > 1024))
-    return fail(SFSIM_ATMO_EINVAL, "sphere_steps must be in [2, 1024]");
+  if (c->sphere_steps < 0 || c->sphere_steps > 1024)
+    return fail(SFSIM_ATMO_EINVAL, "sphere_steps must be in [0, 1024]");
+  if (c->iterations > 0 && c->sphere_steps < 2)
+    return fail(SFSIM_ATMO_EINVAL, "sphere_steps must be in [2, 1024] when there are iterations");
   if (c->iterations > 0 && c->ray_steps < 4)
     return fail(SFSIM_ATMO_EINVAL, "ray_steps must be at least 4 (surface radiance uses ray_steps/4 rings)");
   if (c->precision != SFSIM_ATMO_FP32 && c->precision != SFSIM_ATMO_FP64)

@@ -105,6 +105,10 @@ def test_validate_limits(lib):
     assert code(ray_steps=3, iterations=0) == 0
     assert code(ray_steps=4097) == -1
     assert code(sphere_steps=1025) == -1
+    assert code(sphere_steps=1) == -1                      # iterations need a sphere
+    assert code(sphere_steps=0, iterations=0) == 0         # a first-order build needs none
+    assert code(sphere_steps=1 << 20, iterations=0) == -1  # bounded even when unused
+    assert code(sphere_steps=-2, iterations=0) == -1
     assert code(iterations=65) == -1
 
 
