@@ -161,9 +161,10 @@ int sfsim_atmo_plan_build(sfsim_atmo_plan* plan, float* transmittance, float* su
                           float* ray_scatter, float* mie_strength, void* stream);
 int sfsim_atmo_plan_destroy(sfsim_atmo_plan* plan);
 
-/* Builds `n` independent atmospheres that share shapes, steps, iterations and
- * precision (they may differ in every physical parameter) in one pass of
- * batched kernels.  Outputs are HOST arrays of n consecutive tables each. */
+/* Builds `n` independent atmospheres that share shapes, steps, iterations,
+ * precision and flags (they may differ in every physical parameter) in one
+ * pass of batched kernels, 1 <= n <= 65535 (SFSIM_ATMO_ETOOBIG above).
+ * Outputs are HOST arrays of n consecutive tables each. */
 int sfsim_atmo_build_batch(const sfsim_atmo_config* cfgs, int n, float* transmittance,
                            float* surface_radiance, float* ray_scatter,
                            float* mie_strength);

@@ -834,6 +834,7 @@ int dispatch(const sfsim_atmo_config* cfgs, int B, float* T, float* E, float* S,
              cudaStream_t st, const sfsim_atmo_intermediates* inter) {
   if (!cfgs) return fail(SFSIM_ATMO_ENULL, "config is NULL");
   if (B < 1) return fail(SFSIM_ATMO_EINVAL, "batch size must be at least 1");
+  if (B > 65535) return fail(SFSIM_ATMO_ETOOBIG, "a batch holds at most 65535 atmospheres (one grid row each)");
   if (!T || !E || !S || !M) return fail(SFSIM_ATMO_ENULL, "an output pointer is NULL");
   for (int b = 0; b < B; b++) {
     int rc = validate(&cfgs[b]);

@@ -112,6 +112,15 @@ def test_validate_limits(lib):
     assert code(iterations=65) == -1
 
 
+def test_batch_size_limits(lib):
+    """Batches of 0 or of more than 65535 atmospheres are refused before any
+    device work (each atmosphere is one grid row of the batched kernels)."""
+    cfgs = (C.AtmoConfig * 65536)()
+    out = (ctypes.c_float * 4)()
+    assert lib.sfsim_atmo_build_batch(cfgs, 0, out, out, out, out) == -1
+    assert lib.sfsim_atmo_build_batch(cfgs, 65536, out, out, out, out) == -7
+
+
 def test_null_outputs(lib):
     c = C.small_fp64()
     assert lib.sfsim_atmo_build(ctypes.byref(c), None, None, None, None) == -6
