@@ -332,7 +332,7 @@ int check_smem(const BuildDims& d) {
     return fail(SFSIM_ATMO_ESHAPE, "elevation x heading slab of point scatter exceeds shared memory");
   if (ray_scatter_smem<Real>(d) > kMaxSmem)
     return fail(SFSIM_ATMO_ESHAPE, "sun elevation x heading plane of ray scatter exceeds shared memory");
-  if (first_order_smem<Real>(d) > kMaxSmem)
+  if (first_order_smem<Real>(d, false) > kMaxSmem)
     return fail(SFSIM_ATMO_ESHAPE, "the view rows' samples of the first order exceed shared memory");
   return 0;
 }
@@ -358,7 +358,7 @@ cudaEvent_t g_early_done[kMaxDevices];
 // beside point and ray scatter (run_build)
 cudaStream_t g_side_stream[kMaxDevices];
 cudaEvent_t g_side_fork[kMaxDevices], g_side_sr[kMaxDevices], g_side_rs[kMaxDevices], g_side_acc[kMaxDevices],
-    g_side_setup[kMaxDevices];
+    g_side_setup[kMaxDevices], g_side_sun[kMaxDevices], g_side_rows[kMaxDevices];
 
 struct Carver {
   char* base;
@@ -475,7 +475,8 @@ int ensure_stream(int dev) {
     CUDA_TRY(cudaEventCreateWithFlags(&g_early_done[dev], cudaEventDisableTiming));
     CUDA_TRY(cudaStreamCreateWithFlags(&g_stream[dev], cudaStreamNonBlocking));
     CUDA_TRY(cudaStreamCreateWithFlags(&g_side_stream[dev], cudaStreamNonBlocking));
-    for (cudaEvent_t* e : {&g_side_fork[dev], &g_side_sr[dev], &g_side_rs[dev], &g_side_acc[dev], &g_side_setup[dev]})
+    for (cudaEvent_t* e : {&g_side_fork[dev], &g_side_sr[dev], &g_side_rs[dev], &g_side_acc[dev], &g_side_setup[dev],
+                           &g_side_sun[dev], &g_side_rows[dev]})
       CUDA_TRY(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
     for (int i = 0; i < 2 * 512; i++) CUDA_TRY(cudaEventCreate(&g_events[dev][i]));
   }
@@ -536,13 +537,18 @@ int run_build(const Work<Real>& w, const BuildDims& d, float* oT, float* oE, flo
               Timer& tm, const sfsim_atmo_intermediates* inter, Vec4<float>* jsum = nullptr,
               cudaEvent_t early_done = nullptr, const IterationHooks* hooks = nullptr) {
   int launches = 0;
-  // Only the view-row chain (row info, point rows, remap4, view rows) stands
-  // between the parameters and the first order; the sun table, the other
-  // set-up tables, the transmittance nodes and E0 run beside it on the side
-  // stream, which the first order waits for.  Builds with stage timing on
-  // and entry points without a side stream keep them on the build stream.
+  // The first order needs the sun tables, the rows (row info, point rows)
+  // and the view-row samples; each of its blocks forms its cells' light
+  // directions itself (as k_remap4 does).  So the build stream runs the rows
+  // and the view-row samples, the side stream the sun tables and then the
+  // node maps (remap4), the other set-up tables, the transmittance nodes and
+  // E0 beside the first order; the outputs and the iterations wait for all
+  // of them.  Builds with stage timing on, entry points without a side
+  // stream, and rows whose cells' geometry does not fit beside their samples
+  // in shared memory keep the node maps before the first order.
   cudaStream_t ss = tm.side ? g_side_stream[tm.dev] : nullptr;
   const bool setup_fork = ss != nullptr && !g_timing;
+  const bool cells = setup_fork && first_order_smem<Real>(d, true) <= kMaxSmem;
   cudaStream_t sa = setup_fork ? ss : st;
   if (setup_fork) {
     CUDA_TRY(cudaEventRecord(g_side_fork[tm.dev], st));
@@ -553,11 +559,17 @@ int run_build(const Work<Real>& w, const BuildDims& d, float* oT, float* oE, flo
       launches++;
       tm.mark_end(ss);
     }
+    CUDA_TRY(cudaEventRecord(g_side_sun[tm.dev], ss));
   }
   tm.mark_begin(0);
   launch_setup_rows<Real>(w.params, d, w.setup, st);
-  launch_setup_aux<Real>(w.params, d, w.dirs, w.hdirs, w.setup, sa);
-  launches += 10;
+  if (cells) {
+    CUDA_TRY(cudaEventRecord(g_side_rows[tm.dev], st));
+    CUDA_TRY(cudaStreamWaitEvent(ss, g_side_rows[tm.dev], 0));
+  }
+  launch_node_maps<Real>(w.params, d, w.setup, cells ? ss : st);
+  launch_view_rows<Real>(w.params, d, w.setup, st);
+  launches += 4 + launch_setup_aux<Real>(w.params, d, w.dirs, w.hdirs, w.setup, sa);
   tm.mark_end();
   tm.mark_begin(1, sa);
   launch_transmittance<Real>(w.params, d, w.T, sa);
@@ -569,17 +581,19 @@ int run_build(const Work<Real>& w, const BuildDims& d, float* oT, float* oE, flo
   tm.mark_end(sa);
   if (setup_fork) {
     CUDA_TRY(cudaEventRecord(g_side_setup[tm.dev], ss));
-    CUDA_TRY(cudaStreamWaitEvent(st, g_side_setup[tm.dev], 0));
+    CUDA_TRY(cudaStreamWaitEvent(st, (cells ? g_side_sun : g_side_setup)[tm.dev], 0));
   }
   tm.mark_begin(3);
   if (w.sun && !setup_fork) {
     launch_sun_table(w.params, d, w.sun, st);
     launches++;
   }
-  if (launch_first_order<Real>(w.params, d, w.setup.rowinfo, w.setup.rows, w.setup.geom, w.sun, w.S1R, w.M, st))
+  if (launch_first_order<Real>(w.params, d, w.setup.rowinfo, w.setup.rows, cells ? nullptr : w.setup.geom,
+                               w.setup.prow, w.setup.hdvs, w.sun, w.S1R, w.M, st))
     return fail(SFSIM_ATMO_ECUDA, "first order launch configuration failed");
   launches++;
   tm.mark_end();
+  if (cells) CUDA_TRY(cudaStreamWaitEvent(st, g_side_setup[tm.dev], 0));  // node maps, T, E0 and the rest
   // the transmittance and Mie-strength tables are final here: their outputs
   // (and, for host outputs, their copies) need not wait for the iterations
   tm.mark_begin(9);

@@ -216,6 +216,26 @@ __host__ __device__ inline d3 index_to_sun_direction(int size, d3 direction, dou
   return mk3(sin_sun, sun_1, sun_2);
 }
 
+// index_to_sun_direction(n3, v, ss, a) for v = (sv, cv, 0), with its
+// per-heading term dvs = 2 a / (n3 - 1) - 1 and per-sun-elevation bound
+// cs = sqrt(max(0, 1 - ss^2)) precomputed by the same operations (so the
+// same value); the light direction of every 4-D node.
+__host__ __device__ inline d3 node_light(double sv, double cv, double ss, double cs, double dvs) {
+  const double sun_1 = limit_quot(dsub(dvs, dmul(sv, ss)), cv, -cs, cs);
+  return mk3(ss, sun_1, sqrt(dmax(0.0, dsub(dsub(1.0, sqr(sun_1)), sqr(ss)))));
+}
+
+// A node's light direction and v.l in Real, as the scattering kernels use them.
+template <class Real>
+__host__ __device__ inline CellGeom<Real> cell_geom(double sv, double cv, const d3& l) {
+  CellGeom<Real> g;
+  g.lx = (Real)l.x;
+  g.ly = (Real)l.y;
+  g.lz = (Real)l.z;
+  g.mu = (Real)dot3(mk3(sv, cv, 0), l);
+  return g;
+}
+
 // interpolate.clj:75-98 per dimension: i = clip(c), u = floor(i), s = i - u
 template <class Real>
 __host__ __device__ inline void split_coord(double c, int size, int* u, Real* s) {

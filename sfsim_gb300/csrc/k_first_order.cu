@@ -47,12 +47,15 @@ struct FirstOrderSmem {
   Real er, em, q, us;
 };
 
+// Shared memory of a first-order block: the row's samples, then (when the
+// block forms its cells' light directions itself) one CellGeom per cell.
 template <class Real>
-size_t first_order_smem(const BuildDims& d) {
-  return sizeof(FirstOrderSmem<Real>) * d.S;
+size_t first_order_smem(const BuildDims& d, bool cells) {
+  const size_t samples = (sizeof(FirstOrderSmem<Real>) * d.S + 15) & ~size_t(15);
+  return samples + (cells ? sizeof(CellGeom<Real>) * d.n2 * d.n3 : 0);
 }
-template size_t first_order_smem<float>(const BuildDims&);
-template size_t first_order_smem<double>(const BuildDims&);
+template size_t first_order_smem<float>(const BuildDims&, bool);
+template size_t first_order_smem<double>(const BuildDims&, bool);
 
 // Horizon test of the sun at p_s (atmosphere.clj:95-102, filtered-sun-light
 // :154-160) from b = p_s.l and q = |p_s|^2 - R^2.  Near the boundary FP32
@@ -239,18 +242,33 @@ __device__ __forceinline__ float2 sun_lookup_desc(const unsigned char* __restric
   return make_float2(texit * Bulk<float>::exp2(lr), texit * Bulk<float>::exp2(lm));
 }
 
-template <class Real, int WARPS>
+// CELLS: the block forms its cells' light directions (node_light, as
+// k_remap4 does) in shared memory instead of reading them from `geom`, so
+// that the first order need not wait for k_remap4.
+template <class Real, int WARPS, bool CELLS>
 __global__ void __launch_bounds__(WARPS * 32, 4) k_first_order(const AtmoParams* params, BuildDims d,
                                                             const RowInfo* rowinfo, const RowSample<Real>* rows,
-                                                            const CellGeom<Real>* geom, const unsigned char* sun_table,
+                                                            const CellGeom<Real>* geom, const PointRow<Real>* prow,
+                                                            const double* hdvs, const unsigned char* sun_table,
                                                             Vec4<Real>* rayleigh, Vec4<Real>* mie) {
-  extern __shared__ unsigned char smem_raw[];
+  extern __shared__ __align__(16) unsigned char smem_raw[];
   FirstOrderSmem<Real>* sm = reinterpret_cast<FirstOrderSmem<Real>*>(smem_raw);
   const int b = blockIdx.y;
   const long long row = blockIdx.x;
   const long long nrows = d.rows();
   const AtmoParams& P = params[b];
   const int S = d.S;
+  const int ncell = d.n2 * d.n3;
+  const RowInfo ri = rowinfo[b * nrows + row];
+  CellGeom<Real>* cg = reinterpret_cast<CellGeom<Real>*>(
+      smem_raw + ((sizeof(FirstOrderSmem<Real>) * S + 15) & ~size_t(15)));
+  if (CELLS) {
+    const PointRow<Real>* pr = prow + ((long long)b * d.n0 + row / d.n1) * d.n2;
+    for (int c = threadIdx.x; c < ncell; c += blockDim.x) {
+      const int k = c / d.n3, a = c - k * d.n3;
+      cg[c] = cell_geom<Real>(ri.sv, ri.cv, node_light(ri.sv, ri.cv, pr[k].ss, pr[k].cs, hdvs[a]));
+    }
+  }
   const RowSample<Real>* rs = rows + (b * nrows + row) * S;
   for (int s = threadIdx.x; s < S; s += blockDim.x) {
     RowSample<Real> v = rs[s];
@@ -264,9 +282,7 @@ __global__ void __launch_bounds__(WARPS * 32, 4) k_first_order(const AtmoParams*
   }
   __syncthreads();
 
-  const RowInfo ri = rowinfo[b * nrows + row];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int ncell = d.n2 * d.n3;
   const Real Hh2 = std::is_same<Real, float>::value ? (Real)P.f_Hh2 : (Real)P.Hh2;
   // climbing rays from the top rows of the climbing table, where its
   // interpolation fails for atmospheres dense at the top, are integrated
@@ -293,7 +309,7 @@ __global__ void __launch_bounds__(WARPS * 32, 4) k_first_order(const AtmoParams*
   const unsigned char* tab = sun_table ? sun_table + (size_t)b * kSunTableBytes : nullptr;
 
   for (int cell = warp; cell < ncell; cell += WARPS) {
-    const CellGeom<Real> g = geom[node0 + cell];
+    const CellGeom<Real> g = CELLS ? cg[cell] : geom[node0 + cell];
     const Real b0 = rr * g.lx;  // x.l, x = (r, 0, 0)
     const Real Dl = D0 * g.lx + D1 * g.ly + D2 * g.lz;
     Real accR[3] = {0, 0, 0}, accM[3] = {0, 0, 0};
@@ -355,27 +371,29 @@ __global__ void __launch_bounds__(WARPS * 32, 4) k_first_order(const AtmoParams*
 
 template <class Real>
 int launch_first_order(const AtmoParams* params, const BuildDims& d, const RowInfo* rowinfo,
-                       const RowSample<Real>* rows, const CellGeom<Real>* geom, const unsigned char* sun_table,
-                       Vec4<Real>* rayleigh, Vec4<Real>* mie, cudaStream_t st) {
+                       const RowSample<Real>* rows, const CellGeom<Real>* geom, const PointRow<Real>* prow,
+                       const double* hdvs, const unsigned char* sun_table, Vec4<Real>* rayleigh, Vec4<Real>* mie,
+                       cudaStream_t st) {
   constexpr int WARPS = 8;
-  const size_t smem = first_order_smem<Real>(d);
-  // rows of more than 48 KB of samples (S > 1755 in FP32, > 877 in FP64) need the opt-in
+  const bool cells = geom == nullptr;
+  const size_t smem = first_order_smem<Real>(d, cells);
+  auto kernel = cells ? k_first_order<Real, WARPS, true> : k_first_order<Real, WARPS, false>;
+  // more than 48 KB (long rows, S > 1755 in FP32, > 877 in FP64) needs the opt-in
   if (smem > 48 * 1024 &&
-      cudaFuncSetAttribute(k_first_order<Real, WARPS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
-          cudaSuccess)
+      cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
     return -1;
   dim3 grid((unsigned)d.rows(), d.B);
-  k_first_order<Real, WARPS><<<grid, WARPS * 32, smem, st>>>(params, d, rowinfo, rows, geom, sun_table, rayleigh,
-                                                             mie);
+  kernel<<<grid, WARPS * 32, smem, st>>>(params, d, rowinfo, rows, geom, prow, hdvs, sun_table, rayleigh, mie);
   return 0;
 }
 
-template int launch_first_order<float>(const AtmoParams*, const BuildDims&, const RowInfo*,
-                                        const RowSample<float>*, const CellGeom<float>*, const unsigned char*,
-                                        Vec4<float>*, Vec4<float>*, cudaStream_t);
+template int launch_first_order<float>(const AtmoParams*, const BuildDims&, const RowInfo*, const RowSample<float>*,
+                                       const CellGeom<float>*, const PointRow<float>*, const double*,
+                                       const unsigned char*, Vec4<float>*, Vec4<float>*, cudaStream_t);
 template int launch_first_order<double>(const AtmoParams*, const BuildDims&, const RowInfo*,
-                                         const RowSample<double>*, const CellGeom<double>*, const unsigned char*,
-                                         Vec4<double>*, Vec4<double>*, cudaStream_t);
+                                        const RowSample<double>*, const CellGeom<double>*, const PointRow<double>*,
+                                        const double*, const unsigned char*, Vec4<double>*, Vec4<double>*,
+                                        cudaStream_t);
 
 // Work census of the first order: count[0] = the (node, sample) pairs whose
 // sun is above the horizon (sun-ray optical depths the reference integrates,

@@ -80,11 +80,7 @@ __global__ void k_remap4(const AtmoParams* params, BuildDims d, const RowInfo* i
   const PointRow<Real>& pk = prow[((long long)b * d.n0 + i) * d.n2 + k];
   const double sv = ri.sv, cv = ri.cv;
   const d3 v = mk3(sv, cv, 0);
-  // index_to_sun_direction(n3, v, ss, a) with its per-heading and
-  // per-sun-elevation terms read from tables (the same operations)
-  const double ss = pk.ss, cs = pk.cs;
-  const double sun_1 = limit_quot(dsub(hdvs[a], dmul(v.x, ss)), v.y, -cs, cs);
-  const d3 l = mk3(ss, sun_1, sqrt(dmax(0.0, dsub(dsub(1.0, sqr(sun_1)), sqr(ss)))));
+  const d3 l = node_light(sv, cv, pk.ss, pk.cs, hdvs[a]);
   Remap4<Real> m;
   m.u[0] = rm.u[0];
   m.s[0] = rm.s[0];
@@ -94,12 +90,7 @@ __global__ void k_remap4(const AtmoParams* params, BuildDims d, const RowInfo* i
   m.s[2] = pk.s2;
   split_coord<Real>(sun_angle_to_index(d.n3, v, l), d.n3, &m.u[3], &m.s[3]);
   out[b * n4 + node] = m;
-  CellGeom<Real> g;
-  g.lx = (Real)l.x;
-  g.ly = (Real)l.y;
-  g.lz = (Real)l.z;
-  g.mu = (Real)dot3(v, l);
-  geom[b * n4 + node] = g;
+  geom[b * n4 + node] = cell_geom<Real>(sv, cv, l);
 }
 
 template <class Real>
@@ -579,8 +570,18 @@ void launch_setup_rows(const AtmoParams* params, const BuildDims& d, const Setup
   const int blk = 128;
   k_row_info<Real><<<grid1(d.rows(), blk, d.B), blk, 0, st>>>(params, d, o.rowinfo, o.rowmap);
   k_point_rows<Real><<<grid1((long long)d.n0 * d.n2, blk, d.B), blk, 0, st>>>(params, d, o.prow, o.hdvs);
+}
+
+template <class Real>
+void launch_node_maps(const AtmoParams* params, const BuildDims& d, const SetupBuffers<Real>& o, cudaStream_t st) {
+  const int blk = 128;
   k_remap4<Real><<<grid1(d.n4(), blk, d.B), blk, 0, st>>>(params, d, o.rowinfo, o.rowmap, o.prow, o.hdvs,
                                                             o.remapS, o.geom);
+}
+
+template <class Real>
+void launch_view_rows(const AtmoParams* params, const BuildDims& d, const SetupBuffers<Real>& o, cudaStream_t st) {
+  const int blk = 128;
   if (d.scan_rays)
     k_view_rows_scan<Real><<<grid1(d.rows(), blk / 32, d.B), blk, 0, st>>>(params, d, o.rowinfo, o.rows);
   else
@@ -588,8 +589,8 @@ void launch_setup_rows(const AtmoParams* params, const BuildDims& d, const Setup
 }
 
 template <class Real>
-void launch_setup_aux(const AtmoParams* params, const BuildDims& d, const DirLocal* dirs,
-                      const DirLocal* half_dirs, const SetupBuffers<Real>& o, cudaStream_t st) {
+int launch_setup_aux(const AtmoParams* params, const BuildDims& d, const DirLocal* dirs,
+                     const DirLocal* half_dirs, const SetupBuffers<Real>& o, cudaStream_t st) {
   const int blk = 128;
   k_remapT<Real><<<grid1(d.nT(), blk, d.B), blk, 0, st>>>(params, d, o.remapT);
   k_remapE<Real><<<grid1(d.nE(), blk, d.B), blk, 0, st>>>(params, d, o.remapE);
@@ -601,12 +602,15 @@ void launch_setup_aux(const AtmoParams* params, const BuildDims& d, const DirLoc
   k_surface_rows<Real><<<grid1(d.nE(), blk, d.B), blk, 0, st>>>(params, d, o.erow);
   if (d.Ph > 0)
     k_half_dirs<Real><<<grid1((long long)d.nE0 * d.Ph, blk, d.B), blk, 0, st>>>(params, d, half_dirs, o.hdir);
+  return 4 + (d.P > 0) + (d.Ph > 0);
 }
 
 template <class Real>
 void launch_setup(const AtmoParams* params, const BuildDims& d, const DirLocal* dirs,
                   const DirLocal* half_dirs, const SetupBuffers<Real>& o, cudaStream_t st) {
   launch_setup_rows<Real>(params, d, o, st);
+  launch_node_maps<Real>(params, d, o, st);
+  launch_view_rows<Real>(params, d, o, st);
   launch_setup_aux<Real>(params, d, dirs, half_dirs, o, st);
 }
 
@@ -626,10 +630,18 @@ template void launch_setup_rows<float>(const AtmoParams*, const BuildDims&, cons
                                        cudaStream_t);
 template void launch_setup_rows<double>(const AtmoParams*, const BuildDims&, const SetupBuffers<double>&,
                                         cudaStream_t);
-template void launch_setup_aux<float>(const AtmoParams*, const BuildDims&, const DirLocal*, const DirLocal*,
-                                      const SetupBuffers<float>&, cudaStream_t);
-template void launch_setup_aux<double>(const AtmoParams*, const BuildDims&, const DirLocal*, const DirLocal*,
-                                       const SetupBuffers<double>&, cudaStream_t);
+template void launch_node_maps<float>(const AtmoParams*, const BuildDims&, const SetupBuffers<float>&,
+                                      cudaStream_t);
+template void launch_node_maps<double>(const AtmoParams*, const BuildDims&, const SetupBuffers<double>&,
+                                       cudaStream_t);
+template void launch_view_rows<float>(const AtmoParams*, const BuildDims&, const SetupBuffers<float>&,
+                                      cudaStream_t);
+template void launch_view_rows<double>(const AtmoParams*, const BuildDims&, const SetupBuffers<double>&,
+                                       cudaStream_t);
+template int launch_setup_aux<float>(const AtmoParams*, const BuildDims&, const DirLocal*, const DirLocal*,
+                                     const SetupBuffers<float>&, cudaStream_t);
+template int launch_setup_aux<double>(const AtmoParams*, const BuildDims&, const DirLocal*, const DirLocal*,
+                                      const SetupBuffers<double>&, cudaStream_t);
 template void launch_setup<float>(const AtmoParams*, const BuildDims&, const DirLocal*, const DirLocal*,
                                   const SetupBuffers<float>&, cudaStream_t);
 template void launch_setup<double>(const AtmoParams*, const BuildDims&, const DirLocal*, const DirLocal*,

@@ -55,15 +55,21 @@ __host__ __device__ inline long long heading_rows_stride(const BuildDims& d) {
   return 2LL * ((dir_row(d.P) + 7) / 8 * 8) * (d.n3 + 2) * 3;
 }
 
-// The set-up tables in two independent parts: the view-row chain the first
-// order reads (row info, point rows, remap4 with its geometry, view rows)
-// and the rest (remapT, remapE, sphere directions and their partition,
-// surface rows, half directions).  launch_setup runs both on one stream.
+// The set-up tables in parts: the rows (row info and point rows), then the
+// 4-D node maps with each node's light direction (remap4) and the view-row
+// samples, which both read the rows but not each other, and the rest
+// (remapT, remapE, sphere directions and their partition, surface rows, half
+// directions).  launch_setup runs them all on one stream.
 template <class Real>
 void launch_setup_rows(const AtmoParams* params, const BuildDims& d, const SetupBuffers<Real>& o, cudaStream_t st);
 template <class Real>
-void launch_setup_aux(const AtmoParams* params, const BuildDims& d, const DirLocal* dirs,
-                      const DirLocal* half_dirs, const SetupBuffers<Real>& o, cudaStream_t st);
+void launch_node_maps(const AtmoParams* params, const BuildDims& d, const SetupBuffers<Real>& o, cudaStream_t st);
+template <class Real>
+void launch_view_rows(const AtmoParams* params, const BuildDims& d, const SetupBuffers<Real>& o, cudaStream_t st);
+// Returns the number of kernels it launched.
+template <class Real>
+int launch_setup_aux(const AtmoParams* params, const BuildDims& d, const DirLocal* dirs,
+                     const DirLocal* half_dirs, const SetupBuffers<Real>& o, cudaStream_t st);
 template <class Real>
 void launch_setup(const AtmoParams* params, const BuildDims& d, const DirLocal* dirs,
                   const DirLocal* half_dirs, const SetupBuffers<Real>& o, cudaStream_t st);
@@ -74,14 +80,19 @@ void launch_transmittance(const AtmoParams* params, const BuildDims& d, Vec4<Rea
 template <class Real>
 void launch_surface_base(const AtmoParams* params, const BuildDims& d, Vec4<Real>* E0, cudaStream_t st);
 
-// First-order Rayleigh ray scatter and Mie strength (fused); -1 when its
-// shared memory (first_order_smem: the row's samples) cannot be configured.
+// First-order Rayleigh ray scatter and Mie strength (fused).  With `geom`
+// NULL each block forms its cells' light directions from the point rows and
+// the per-heading table (as k_remap4 does), so the launch needs the rows and
+// the view-row samples but not the node maps.  -1 when its shared memory
+// (first_order_smem: the row's samples, and the cells' geometry when
+// `cells`) cannot be configured.
 template <class Real>
-size_t first_order_smem(const BuildDims& d);
+size_t first_order_smem(const BuildDims& d, bool cells);
 template <class Real>
 int launch_first_order(const AtmoParams* params, const BuildDims& d, const RowInfo* rowinfo,
-                        const RowSample<Real>* rows, const CellGeom<Real>* geom, const unsigned char* sun_table,
-                        Vec4<Real>* rayleigh, Vec4<Real>* mie, cudaStream_t st);
+                       const RowSample<Real>* rows, const CellGeom<Real>* geom, const PointRow<Real>* prow,
+                       const double* hdvs, const unsigned char* sun_table, Vec4<Real>* rayleigh, Vec4<Real>* mie,
+                       cudaStream_t st);
 
 // Sun-ray optical-depth tables of the FP32 first order, per atmosphere: the
 // climbing rays' kSunNR x kSunNM float2, then the descending rays' kDescNX x
