@@ -394,3 +394,35 @@ def test_single_ray_step_first_order(precision):
     gpu = A.build(mk(precision))
     for key in ("transmittance", "surface_radiance", "ray_scatter", "mie_strength"):
         assert_close(gpu[key], ref[key], TOL[precision], key)
+
+
+SKEWED_SHAPES = [(2, 3, 64, 2), (3, 2, 4, 32), (2, 33, 2, 3), (2, 2, 32, 16)]
+
+
+# With two sun elevations the axis jumps from sin -0.2 (night) to 1 (noon),
+# and J at the two nodes differs by 6 to 18 orders of magnitude: at a dark
+# node the ray scatter's interpolated J is then off by the FP32 rounding of
+# the sample's sun-elevation coordinate times that ratio (1.3e-3 measured,
+# against 6e-8 for the FP64 build).  The FP32 path is held to 1e-4 on the
+# other shapes; the FP64 build checks this one.
+SKEWED_CASES = [(shape, p) for shape in SKEWED_SHAPES for p in (C.FP64, C.FP32)
+                if not (p == C.FP32 and shape[2] == 2)]
+
+
+@pytest.mark.parametrize("shape,precision", SKEWED_CASES)
+def test_skewed_shapes_match_oracle(shape, precision):
+    """Lopsided 4-D tables: column-major ray-scatter planes with 2 headings,
+    a heading axis of a whole warp (point scatter's shared phases over 32
+    lanes), many elevations with 2 sun elevations, and 16 headings beside 32
+    sun elevations (planes of 576 texels, wider than a block)."""
+    mk = lambda p: C.make_config(height=100000.0, transmittance_shape=(5, 7), surface_radiance_shape=(3, 5),
+                                 ray_scatter_shape=shape, ray_steps=16, sphere_steps=8, iterations=1, precision=p)
+    ref = O.build(mk(C.FP64), intermediates=True)
+    gpu = A.build(mk(precision), intermediates=True)
+    tol = TOL[precision]
+    for key in ("rayleigh_first", "mie_first"):
+        assert_close(gpu[key], ref[key], tol, key)
+    for key in ("point_scatter", "surface_delta", "ray_scatter_delta"):
+        assert_close(gpu[key][0], ref[key][0], tol, f"{key}[0]")
+    for key in ("transmittance", "surface_radiance", "ray_scatter", "mie_strength"):
+        assert_close(gpu[key], ref[key], tol, key)
