@@ -10,6 +10,7 @@ import numpy as np
 import pytest
 
 from oracle import oracle as O
+from sfsim_gb300 import _lib
 from sfsim_gb300 import atmosphere_lut as A
 from sfsim_gb300 import config as C
 
@@ -83,8 +84,9 @@ def test_scan_batch_and_flag_mix():
         assert np.array_equal(batch[key][1], single[key])
     c = scan_config(C.FP32)
     c.flags = 0
-    with pytest.raises(Exception):
+    with pytest.raises(_lib.AtmoError) as e:
         A.build_batch([a, c])
+    assert e.value.code == -1
 
 
 def test_scan_production_deviation():
