@@ -9,7 +9,8 @@
 //
 // Mapping: one block per view row (height i, elevation j).  The row's S
 // samples (positions, T(x, p_s), the heights' exponentials) come from
-// k_view_rows and sit in shared memory.  Each warp takes one cell (sun
+// k_view_rows and sit in shared memory, and so do the row's cells' light
+// directions when the block forms them itself (CELLS).  Each warp takes one cell (sun
 // elevation k, sun heading a) at a time and its lanes take the samples: a
 // lane integrates the optical depth of the sun ray from its p_s (S midpoint
 // samples, FP32, compensated sums), and the warp reduces the samples with
