@@ -18,6 +18,11 @@
  * t_interpolate.clj that concerns this path, and the LUT end-to-end shader
  * values of t_atmosphere.clj:629-775 through the GLSL restatement at the end
  * of this file.
+ *
+ * One part is not the reference's: ray_scatter_scan, the library's
+ * SFSIM_ATMO_SCAN_RAYS quadrature (used only when a config sets that flag),
+ * restated here so that the GPU's scan mode has a checker of its own; it is
+ * pinned against a numpy restatement in tests/test_oracle_scan.py.
  */
 #include <math.h>
 #include <pthread.h>
