@@ -409,7 +409,8 @@ SKEWED_CASES = [(shape, p) for shape in SKEWED_SHAPES for p in (C.FP64, C.FP32)
                 if not (p == C.FP32 and shape[2] == 2)]
 
 
-@pytest.mark.parametrize("shape,precision", SKEWED_CASES)
+@pytest.mark.parametrize("shape,precision", SKEWED_CASES,
+                         ids=[f"{'x'.join(map(str, sh))}-{'fp64' if p == C.FP64 else 'fp32'}" for sh, p in SKEWED_CASES])
 def test_skewed_shapes_match_oracle(shape, precision):
     """Lopsided 4-D tables: column-major ray-scatter planes with 2 headings,
     a heading axis of a whole warp (point scatter's shared phases over 32
